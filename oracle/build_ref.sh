@@ -1,0 +1,35 @@
+#!/bin/sh
+# Builds oracle/_ref/ref_dump: the reference library's own basis enumeration,
+# Hubbard model and compute_matrix_elements (src/algebra/*, src/utils/*),
+# compiled from a copy of its sources with exactly one change:
+#   src/algebra/fermion/term.h:11  term_size 32 -> 128
+# The stock value caps a monomial at 7 operators, which silently drops
+# every Hubbard term acting on a sector with more than 3 particles
+# (src/algebra/expression_base.h:182-186); 128 gives a 55-operator cap.
+# The copy and the binary live only under oracle/_ref/ (git-ignored).
+# Test infrastructure: the product never calls anything built here.
+set -e
+REF=${MANYBODY_REFERENCE:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+if [ ! -d "$REF/src/algebra" ]; then
+  echo "build_ref.sh: reference sources not found under $REF" >&2
+  exit 2
+fi
+rm -rf "$OUT/src"
+mkdir -p "$OUT/src"
+cp -r "$REF/src/algebra" "$REF/src/utils" "$OUT/src/"
+sed -i 's/^constexpr size_t term_size = 32;$/constexpr size_t term_size = 128;/' \
+  "$OUT/src/algebra/fermion/term.h"
+grep -q '^constexpr size_t term_size = 128;$' "$OUT/src/algebra/fermion/term.h" || {
+  echo "build_ref.sh: term_size patch did not apply" >&2
+  exit 3
+}
+${CXX:-g++} -std=c++20 -O2 -fopenmp -DNDEBUG \
+  -I"$OUT/src" -I"$REF/third-party" \
+  "$HERE/ref_dump.cpp" \
+  "$OUT/src/algebra/basis.cpp" \
+  "$OUT/src/algebra/fermion/expression.cpp" \
+  "$OUT/src/utils/xxhash_impl.cpp" \
+  -o "$OUT/ref_dump"
+echo "built $OUT/ref_dump"

@@ -1,0 +1,113 @@
+// Dumps the reference library's fixed-(N, Sz) fermion basis and the Hubbard
+// Hamiltonian as that library builds it, for golden fixtures.
+//
+//   ref_dump <dims> <t> <U> <particles> <spin_projection> <out.bin>
+//     dims: "8" (1D chain), "4x4" (2D), "2x2x2" (3D), all periodic.
+//
+// Calls, unchanged, the reference's
+//   FermionBasis::with_fixed_particle_number_and_spin   (src/algebra/basis.cpp:91-126)
+//   HubbardModel / HubbardModel2D / HubbardModel3D       (src/algebra/fermion/model/hubbard_model.h)
+//   compute_matrix_elements<MatrixType>                  (src/algebra/matrix_elements.h:74-105)
+// with a coordinate-list MatrixType standing in for arma::sp_cx_mat.
+//
+// Output (little endian): "MBREF001", u64 n_terms, u64 dim, u64 up[dim],
+// u64 down[dim] (occupation bit masks in reference index order), u64 nnz,
+// then nnz records {i64 row, i64 col, f64 re, f64 im} sorted by (row, col).
+#include <complex>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "algebra/fermion/basis.h"
+#include "algebra/fermion/expression.h"
+#include "algebra/fermion/model/hubbard_model.h"
+#include "algebra/matrix_elements.h"
+
+namespace {
+
+struct CooMatrix {
+  using value_type = std::complex<double>;
+  CooMatrix(size_t r, size_t c) : rows(r), cols(c) {}
+  void zeros() { entries.clear(); }
+  value_type& operator()(size_t i, size_t j) { return entries[{i, j}]; }
+  size_t rows, cols;
+  std::map<std::pair<size_t, size_t>, value_type> entries;
+};
+
+std::vector<size_t> parse_dims(const std::string& s) {
+  std::vector<size_t> dims;
+  size_t start = 0;
+  while (start <= s.size()) {
+    size_t x = s.find('x', start);
+    if (x == std::string::npos) x = s.size();
+    dims.push_back(std::stoul(s.substr(start, x - start)));
+    start = x + 1;
+  }
+  return dims;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc != 7) {
+    std::fprintf(stderr, "usage: ref_dump <dims> <t> <U> <particles> <spin_projection> <out>\n");
+    return 2;
+  }
+  const std::vector<size_t> dims = parse_dims(argv[1]);
+  const double t = std::atof(argv[2]);
+  const double u = std::atof(argv[3]);
+  const size_t particles = std::stoul(argv[4]);
+  const int sz = std::atoi(argv[5]);
+
+  size_t orbitals = 1;
+  for (size_t d : dims) orbitals *= d;
+
+  FermionExpression h;
+  if (dims.size() == 1) {
+    h = HubbardModel(t, u, dims[0]).hamiltonian();
+  } else if (dims.size() == 2) {
+    h = HubbardModel2D(t, u, dims[0], dims[1]).hamiltonian();
+  } else if (dims.size() == 3) {
+    h = HubbardModel3D(t, u, dims[0], dims[1], dims[2]).hamiltonian();
+  } else {
+    std::fprintf(stderr, "ref_dump: 1 to 3 dimensions\n");
+    return 2;
+  }
+
+  FermionBasis basis = FermionBasis::with_fixed_particle_number_and_spin(orbitals, particles, sz);
+  CooMatrix m = compute_matrix_elements<CooMatrix>(basis, h);
+
+  FILE* f = std::fopen(argv[6], "wb");
+  if (!f) return 3;
+  std::fwrite("MBREF001", 1, 8, f);
+  const uint64_t n_terms = h.size();
+  const uint64_t dim = basis.set.size();
+  std::fwrite(&n_terms, 8, 1, f);
+  std::fwrite(&dim, 8, 1, f);
+  std::vector<uint64_t> up(dim, 0), down(dim, 0);
+  for (size_t i = 0; i < dim; ++i) {
+    for (const auto& op : basis.set[i]) {
+      if (op.type() != FermionOperator::Type::Creation) return 4;
+      if (op.spin() == FermionOperator::Spin::Up)
+        up[i] |= uint64_t{1} << op.value();
+      else
+        down[i] |= uint64_t{1} << op.value();
+    }
+  }
+  std::fwrite(up.data(), 8, dim, f);
+  std::fwrite(down.data(), 8, dim, f);
+  const uint64_t nnz = m.entries.size();
+  std::fwrite(&nnz, 8, 1, f);
+  for (const auto& [ij, v] : m.entries) {
+    const int64_t rc[2] = {static_cast<int64_t>(ij.first), static_cast<int64_t>(ij.second)};
+    const double re_im[2] = {v.real(), v.imag()};
+    std::fwrite(rc, 8, 2, f);
+    std::fwrite(re_im, 8, 2, f);
+  }
+  std::fclose(f);
+  return 0;
+}

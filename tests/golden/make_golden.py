@@ -1,0 +1,91 @@
+"""Regenerates the golden Hubbard fixtures in tests/golden/ from the reference.
+
+Runs oracle/_ref/ref_dump (built by oracle/build_ref.sh from the reference
+sources: its basis enumeration, HubbardModel{,2D,3D} and
+compute_matrix_elements) for each case below and stores, per case, the
+reference-order basis masks, the sparse H as COO (row, col, value) and the
+Hamiltonian term count, in one compressed .npz per case.  Values are real for
+the real-space Hubbard model; the script checks that every imaginary part is
+exactly zero.
+
+Needs the reference sources, so it runs only where they are present; the
+fixtures it writes are committed and travel with the tests.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF_DUMP = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
+
+# (name, dims, t, U, particles, spin_projection)
+CASES = [
+    ("chain2_n1_sz1", "2", 1.0, 2.0, 1, 1),
+    ("chain2_n2", "2", 1.0, 2.0, 2, 0),
+    ("chain4_n4", "4", 1.0, 4.0, 4, 0),
+    ("chain4_n4_u0", "4", 1.0, 0.0, 4, 0),
+    ("chain5_n5_sz1", "5", 0.7, 3.0, 5, 1),
+    ("chain6_n6", "6", 1.0, 4.0, 6, 0),
+    ("chain6_n4_sz2", "6", 1.3, 2.5, 4, 2),
+    ("chain8_n8", "8", 1.0, 4.0, 8, 0),       # the 1D L=8, 4+4 CPU configuration
+    ("chain3_n0", "3", 1.0, 4.0, 0, 0),       # empty occupation: vacuum only
+    ("chain4_full", "4", 1.0, 4.0, 8, 0),     # completely filled
+    ("chain1_n2", "1", 1.0, 4.0, 2, 0),       # single site: self bond, diagonal cancels to 0
+    ("chain1_n2_u3", "1", 1.0, 3.0, 2, 0),    # single site: self bond + U
+    ("sq2x2_n2", "2x2", 1.0, 2.0, 2, 0),
+    ("sq2x2_n4", "2x2", 1.0, 2.0, 4, 0),
+    ("sq3x3_n4", "3x3", 1.0, 8.0, 4, 0),
+    ("sq3x3_n5_sz1", "3x3", 1.0, 8.0, 5, 1),
+    ("rect2x4_n4", "2x4", 1.0, 3.0, 4, 0),
+    ("rect2x3_n4", "2x3", 0.5, 6.0, 4, 0),
+    ("rect3x4_n4", "3x4", 1.0, 5.0, 4, 0),
+    ("cube2x2x2_n4", "2x2x2", 1.0, 2.0, 4, 0),
+]
+
+TERM_COUNT_CASES = [("1", 2), ("2x2", 2), ("2x2x2", 3)]
+
+
+def dump(dims, t, U, n, sz):
+    with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
+        path = f.name
+    try:
+        subprocess.run([REF_DUMP, dims, repr(t), repr(U), str(n), str(sz), path], check=True)
+        b = open(path, "rb").read()
+    finally:
+        os.unlink(path)
+    assert b[:8] == b"MBREF001"
+    n_terms, dim = (int(v) for v in np.frombuffer(b[8:24], "<u8"))
+    up = np.frombuffer(b[24:24 + 8 * dim], "<u8").copy()
+    dn = np.frombuffer(b[24 + 8 * dim:24 + 16 * dim], "<u8").copy()
+    o = 24 + 16 * dim
+    nnz = int(np.frombuffer(b[o:o + 8], "<u8")[0])
+    rec = np.frombuffer(b[o + 8:], np.dtype([("r", "<i8"), ("c", "<i8"), ("re", "<f8"),
+                                             ("im", "<f8")]))
+    assert len(rec) == nnz
+    assert np.all(rec["im"] == 0.0)
+    return n_terms, up, dn, rec
+
+
+def main():
+    if not os.path.exists(REF_DUMP):
+        sys.exit("build oracle/_ref/ref_dump first: oracle/build_ref.sh")
+    for name, dims, t, U, n, sz in CASES:
+        n_terms, up, dn, rec = dump(dims, t, U, n, sz)
+        dvec = [int(x) for x in dims.split("x")]
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), dims=np.array(dvec, np.int32),
+                            t=t, U=U, particles=n, spin_projection=sz, n_terms=n_terms,
+                            up=up, down=dn, row=rec["r"].astype(np.int32),
+                            col=rec["c"].astype(np.int32), val=rec["re"].copy())
+        print(f"{name}: dim={len(up)} nnz={len(rec)} terms={n_terms}")
+
+
+if __name__ == "__main__":
+    main()
