@@ -1,0 +1,344 @@
+"""Benchmark of the matrix-free Hubbard H|psi> on one GB300 (or N replicas).
+
+Workload (N=1 line): 2D square-lattice Hubbard 4x4 periodic, t=1, U=8,
+N_up = N_down = 6 -- 64,128,064 states, complex128 vectors of 1.026 GB.
+A step is one H|psi> over the whole sector.  `value` is the algorithmic
+bandwidth 2 * 16 B * dim / (device time per apply) with the input resident in
+HBM; `e2e` is the same metric through the reference-facing C-ABI call with
+host buffers in reference order (mb_op_apply_host: host->device copy, basis
+permutation, apply, inverse permutation, device->host copy).
+
+Inputs (1 GB each) are larger than the 129 MB L2, so no flush is needed.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference's CPU path for the same metric: its
+compute_matrix_elements matrix applied by a serial CSC column scatter (the
+reference builds Armadillo with ARMA_OPENMP_THREADS=1), restated in the CPU
+oracle because Armadillo is absent; run on a bounded sample (a smaller sector
+of the same lattice) so the run ends in minutes.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+WORKLOAD = dict(workload="hubbard2d_4x4_n6+6_u8_c128_apply", lattice="4x4", n_up=6, n_down=6,
+                t=1.0, U=8.0, dim=64128064, vector="complex128", order="tensor",
+                l2="inputs (1.03 GB) larger than L2 (129 MB); no flush")
+METRIC = "hubbard_hpsi_GBps"
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return HBM_FALLBACK_GBS, "fallback"
+
+
+def committed_traffic(kernel_key: str):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        v = d.get(kernel_key)
+        if isinstance(v, dict):
+            return v.get("dram_bytes_per_launch")
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+
+    import manybody_gb300 as mb
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+
+    def barrier():
+        if pg:
+            pg.barrier()
+
+    w = WORKLOAD
+    basis = mb.FermionBasis.with_fixed_particle_number_and_spin(16, w["n_up"] + w["n_down"], 0)
+    model = mb.HubbardModel2D(w["t"], w["U"], 4, 4)
+    op = mb.GpuHubbardOperator(basis, model, mb.PREC_F64)
+    dim = op.dimension()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    x = op.seed_vector(0, order=mb.ORDER_TENSOR)
+    y = op.empty()
+    alg_bytes = 2 * 16 * dim
+
+    # --- device-resident apply -------------------------------------------------
+    for _ in range(args.warmup):
+        op.apply(x, out=y, order=mb.ORDER_TENSOR, stream=sp)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            op.apply(x, out=y, order=mb.ORDER_TENSOR, stream=sp)
+            ev[i][1].record(stream)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    total_ms = t_start.elapsed_time(t_end)
+    per = [a.elapsed_time(b) for a, b in ev]
+    if pg:
+        t = torch.tensor([total_ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * alg_bytes * args.steps / (total_ms * 1e-3) / 1e9
+    kernel_ms = statistics.mean(per)
+    achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+
+    # --- end to end through the reference-facing host-buffer call -------------
+    xh = torch.empty(dim, dtype=torch.complex128).pin_memory()
+    yh = torch.empty(dim, dtype=torch.complex128).pin_memory()
+    xh.copy_(op.seed_vector(0).cpu())
+    for _ in range(max(1, args.warmup // 2)):
+        op.apply_host(xh, yh)
+    e2e_steps = max(2, min(args.steps, 10))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        op.apply_host(xh, yh)
+    t1 = time.perf_counter()
+    e2e_s = (t1 - t0) / e2e_steps
+    if pg:
+        t = torch.tensor([e2e_s], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * alg_bytes / e2e_s / 1e9
+
+    if rank != 0:
+        if pg:
+            pg.destroy_process_group()
+        return
+    clocks = clk.summary()
+    out = {
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": "GB/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_per_step, 5),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: Philox4x32-10 seed-0 uniform(-1,1) complex start vector",
+        "config": dict(w, parallelism=f"replicas{world}" if world > 1 else "single_gpu"),
+        "roofline": {
+            "bound": "hbm",
+            "achieved": round(achieved, 2),
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": round(achieved / peak, 4),
+            "traffic": committed_traffic("hubbard2d_4x4_c128_apply"),
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+            "kernel": "k_apply<double>",
+            "algorithmic_bytes_per_launch": alg_bytes,
+            "kernel_ms": round(kernel_ms, 5),
+        },
+        "e2e": {
+            "value": round(e2e_value, 2),
+            "unit": "GB/s",
+            "h2d_bytes_per_step": 16 * dim,
+            "d2h_bytes_per_step": 16 * dim,
+            "call": "mb_op_apply_host(order=reference)",
+            "ms_per_step": round(e2e_s * 1e3, 3),
+        },
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+    print(json.dumps(out), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# CPU reference path (oracle restatement of compute_matrix_elements + serial
+# CSC apply), on a bounded sample.
+# ---------------------------------------------------------------------------
+def cpu_sample_matrix():
+    import oracle
+    # same lattice and interaction, a sector small enough to build in seconds
+    return oracle.hubbard_csc([4, 4], 1.0, 8.0, 3, 3), "4x4 U=8 sector N_up=N_down=3 (313,600 states)"
+
+
+def cpu_baseline(seconds: float = 10.0):
+    import numpy as np
+    H, sample = cpu_sample_matrix()
+    x = np.ascontiguousarray(
+        np.random.default_rng(0).uniform(-1, 1, H.dim) + 1j * np.random.default_rng(1).uniform(-1, 1, H.dim))
+    H.apply(x)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        H.apply(x)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 10000:
+            break
+    per = el / n
+    return {"value": round(2 * 16 * H.dim / per / 1e9, 4), "unit": "GB/s", "cores": 1,
+            "kind": "port",
+            "sample": f"{sample}; serial CSC column-scatter apply, {n} applies in {el:.1f}s, "
+                      f"nnz={H.nnz}"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    H, sample = cpu_sample_matrix()
+    x = np.ascontiguousarray(np.random.default_rng(0).uniform(-1, 1, H.dim) + 0j)
+    for _ in range(args.warmup):
+        H.apply(x)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        H.apply(x)
+        times.append(time.perf_counter() - t0)
+    per = sum(times) / len(times)
+    value = 2 * 16 * H.dim / per / 1e9
+    out = {
+        "metric": METRIC,
+        "value": round(value, 4),
+        "unit": "GB/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(per * 1e3, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic uniform(-1,1) vector",
+        "config": dict(WORKLOAD, sample=sample),
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": 1, "kind": "port",
+                         "sample": f"{sample}; the reference's compute_matrix_elements H "
+                                   f"(restated) applied by a serial CSC column scatter "
+                                   f"(Armadillo sp_cx_mat*cx_vec with ARMA_OPENMP_THREADS=1)"},
+        "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,227 @@
+/*
+ * manybody_gb300.h -- C ABI of the GB300 exact-diagonalisation engine for the
+ * fixed-(N_up, N_down) Hubbard model.
+ *
+ * The calling surface mirrors keyehzy/manybody's Basis / HubbardModel /
+ * compute_matrix_elements / LinearOperator + Lanczos path.  Each entry point
+ * names the reference interface it replaces (file:line within that project).
+ *
+ * Conventions
+ *  - Every function returns an mb_status (MB_OK == 0).  On failure the
+ *    calling thread's last-error string (mb_last_error) says why.  No C++
+ *    exception crosses this boundary.
+ *  - Vectors are interleaved complex numbers: complex128 ({double re, im})
+ *    for MB_PREC_F64 / MB_PREC_Q64, complex64 ({float re, im}) for
+ *    MB_PREC_F32.  "_dev" pointers are device memory on the current CUDA
+ *    device, "_host" pointers host memory.  Buffers are owned by the caller.
+ *  - Vector order: MB_ORDER_REFERENCE indexes a vector by the reference
+ *    basis index (the order of FermionBasis::set); MB_ORDER_TENSOR indexes it
+ *    by r_up * D_down + r_down, the engine's native layout (colex ranks of
+ *    the up and down occupation masks).
+ *  - Streams: a `stream` argument is a cudaStream_t passed as void* (NULL =
+ *    the legacy default stream).  mb_op_apply may be called concurrently on
+ *    one operator from several host threads with distinct streams and
+ *    buffers (the reference calls LinearOperator::apply concurrently from
+ *    OpenMP sample loops, examples/hubbard_momentum_optical_conductivity.cpp:351-400).
+ */
+#ifndef MANYBODY_GB300_H
+#define MANYBODY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  MB_OK = 0,
+  MB_ERR_INVALID_ARG = 1,  /* replaces the reference's assert()s (UB in Release) */
+  MB_ERR_CAPACITY = 2,     /* sector or lattice larger than the engine supports */
+  MB_ERR_ZERO_NORM = 3,    /* lanczos.h:92,138-144 "Input vector has zero norm" */
+  MB_ERR_DIM_MISMATCH = 4, /* lanczos.h:138,186 dimension mismatch */
+  MB_ERR_EIG_FAILED = 5,   /* lanczos.h:270, evolve_state.h:46 eig_sym failure */
+  MB_ERR_OOM = 6,          /* device or host allocation failed */
+  MB_ERR_TIMEOUT = 7,      /* a bounded device wait ran out */
+  MB_ERR_CUDA = 8,         /* a CUDA runtime call failed */
+  MB_ERR_NO_DEVICE = 9     /* no CUDA device / extension unusable */
+} mb_status;
+
+typedef enum { MB_ORDER_REFERENCE = 0, MB_ORDER_TENSOR = 1 } mb_order;
+
+typedef enum {
+  MB_PREC_F64 = 0, /* complex128 vectors, FP64 arithmetic */
+  MB_PREC_F32 = 1, /* complex64 vectors, FP32 arithmetic */
+  MB_PREC_Q64 = 2  /* complex128 at the boundary; block floating point with
+                      64-bit integer mantissas and one exponent per vector
+                      inside (exact integer hopping sums) */
+} mb_precision;
+
+typedef struct mb_basis_s* mb_basis_t;
+typedef struct mb_model_s* mb_model_t;
+typedef struct mb_op_s* mb_op_t;
+
+/* ---- library ------------------------------------------------------------ */
+int mb_version(void);
+/* Thread-local text of the last error raised on this thread ("" if none). */
+const char* mb_last_error(void);
+/* Number of visible CUDA devices (0 without a GPU); never fails. */
+int mb_device_count(int* count);
+/* cudaMalloc / cudaFree / cudaMemcpy helpers for callers without the CUDA
+ * runtime headers.  kind: 0 host->device, 1 device->host, 2 device->device. */
+int mb_alloc(void** dev_ptr, size_t bytes);
+int mb_free(void* dev_ptr);
+int mb_memcpy(void* dst, const void* src, size_t bytes, int kind);
+int mb_synchronize(void);
+
+/* ---- basis: FermionBasis (src/algebra/fermion/basis.h, src/algebra/basis.h:12-76)
+ * mb_basis_create_fixed_spin replaces
+ *   BasisImpl::with_fixed_particle_number_and_spin (src/algebra/basis.cpp:91-126).
+ * Same arguments; invalid combinations (odd N+Sz, |Sz|>N, more particles than
+ * orbitals) return MB_ERR_INVALID_ARG where the reference asserts.  Orbitals
+ * <= 32 and C(L,N_up), C(L,N_down) <= 2^23. */
+int mb_basis_create_fixed_spin(int64_t orbitals, int64_t particles, int spin_projection,
+                               mb_basis_t* out);
+int mb_basis_destroy(mb_basis_t basis);
+/* basis.set.size() (compute_basis_size_spin, src/algebra/basis.cpp:39-50). */
+int mb_basis_size(mb_basis_t basis, int64_t* dim);
+int mb_basis_sector(mb_basis_t basis, int64_t* orbitals, int64_t* n_up, int64_t* n_down,
+                    int64_t* dim_up, int64_t* dim_down);
+/* The keys of basis.set in reference index order, as occupation bit masks
+ * (bit o of up_masks[i] set <=> key i holds creation(Up, o)).  Host arrays of
+ * mb_basis_size entries.  Replaces iterating FermionBasis::set. */
+int mb_basis_export_reference_order(mb_basis_t basis, uint64_t* up_masks, uint64_t* down_masks);
+/* IndexedHashSet::index_of (src/utils/indexed_hash_set.h:158-164) for the key
+ * with these masks; MB_ERR_INVALID_ARG if the key is not in the basis
+ * (IndexedHashSet::contains is false). */
+int mb_basis_index_of(mb_basis_t basis, uint64_t up_mask, uint64_t down_mask, int64_t* index);
+/* ref_of_tensor[r_up * D_down + r_down] = reference index (host array). */
+int mb_basis_permutation(mb_basis_t basis, int64_t* ref_of_tensor);
+
+/* ---- model: HubbardModel / 2D / 3D (src/algebra/fermion/model/hubbard_model.h:10-212)
+ * dims = {L} (HubbardModel(t,u,L)), {Lx,Ly} (HubbardModel2D) or {Lx,Ly,Lz}
+ * (HubbardModel3D); periodic, sites x + Lx*y + Lx*Ly*z (src/utils/index.h:69-88).
+ * A lattice dimension of size 2 lists each bond twice and so hops with -2t,
+ * as the reference's merged expression does (tests/algebra/test_model.cpp:58-74).
+ * Coefficients with |c| < 1000*eps are dropped (src/utils/tolerances.h:7-10). */
+int mb_hubbard_create(const int64_t* dims, int ndim, double t, double u, mb_model_t* out);
+int mb_model_destroy(mb_model_t model);
+/* FermionExpression::size() of hamiltonian(): number of distinct terms. */
+int mb_model_term_count(mb_model_t model, int64_t* n_terms);
+
+/* ---- compute_matrix_elements<sp_cx_mat> (src/algebra/matrix_elements.h:74-105)
+ * Builds H on the GPU as CSR in reference order (row i = basis key i; column
+ * indices ascending), bit-identical to the reference's entries.  Two calls:
+ * first with col_idx == NULL to get *nnz, then with arrays of that size
+ * (row_ptr: dim+1 entries; values: interleaved complex128).  Host arrays. */
+int mb_compute_matrix_elements_csr(mb_basis_t basis, mb_model_t model, int64_t* nnz,
+                                   int64_t* row_ptr, int64_t* col_idx, double* values);
+
+/* ---- operator: SparseComplexMatrixOperator (src/numerics/linear_operator.h:81-91)
+ * replaced by a matrix-free operator on the GPU.  The operator holds the
+ * sector tables on the device; it never stores H. */
+int mb_op_create(mb_basis_t basis, mb_model_t model, int precision, mb_op_t* out);
+int mb_op_destroy(mb_op_t op);
+/* LinearOperator::dimension() (linear_operator.h:42). */
+int mb_op_dimension(mb_op_t op, int64_t* dim);
+int mb_op_precision(mb_op_t op, int* precision);
+/* LinearOperator::apply (linear_operator.h:41): y = H x on device buffers.
+ * Asynchronous on `stream`.  x and y must not overlap. */
+int mb_op_apply(mb_op_t op, const void* x_dev, void* y_dev, int order, void* stream);
+/* y = scale * (H - shift) x + beta * z, fused (z may be NULL when beta == 0).
+ * Covers Negated (scale -1, linear_operator.h:93-105), Scaled, Shifted and
+ * the Chebyshev step 2*Ht*T_n - T_{n-1} (kpm.h:222) in one pass. */
+int mb_op_apply_affine(mb_op_t op, const void* x_dev, void* y_dev, double scale, double shift,
+                       double beta, const void* z_dev, int order, void* stream);
+/* apply() with host buffers: copies x in, applies, copies y out, then waits. */
+int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order);
+
+/* ---- seeded start vectors ----------------------------------------------- *
+ * v[i] = (u1, u2), u ~ U[-1,1) from Philox4x32-10 (Salmon et al., SC'11) with
+ * key = seed and counter (i_lo, i_hi, stream, 0), where i is the TENSOR index
+ * of the element; written in `order`.  Identical bits to the CPU oracle. */
+int mb_fill_uniform(mb_op_t op, uint64_t seed, uint32_t stream_id, void* v_dev, int order,
+                    void* stream);
+/* v[i] = exp(i*2*pi*u), u ~ U[0,1) from the same generator (random phases). */
+int mb_fill_phase(mb_op_t op, uint64_t seed, uint32_t stream_id, void* v_dev, int order,
+                  void* stream);
+
+/* ---- Lanczos (src/numerics/lanczos.h) ------------------------------------ */
+typedef struct {
+  int reorth;           /* 0: plain three-term recurrence (the reference's); 1: full
+                           re-orthogonalisation (classical Gram-Schmidt, twice) */
+  int basis_precision;  /* storage of the Krylov basis for reorth: MB_PREC_F64 or MB_PREC_F32;
+                           -1 = F64 when it fits in free device memory, else F32 */
+  double conv_tol;      /* > 0: stop early once the extremal Ritz value changes by
+                           less than conv_tol * |E| between checks (0 = run k steps) */
+  int check_every;      /* Ritz check period in steps when conv_tol > 0 (default 10) */
+  int refine;           /* MB_PREC_F32 operators: 1 = finish with an FP64 Rayleigh-quotient
+                           refinement of the Ritz vector on an FP64 operator */
+} mb_lanczos_opts;
+
+/* lanczos_pass_one (lanczos.h:130-175) on the operator scaled by `scale`
+ * (1: H, -1: Negated<H> as find_min_eigenpair uses).  alphas[k], betas[k-1]
+ * host arrays; *steps = decomposition steps taken. */
+int mb_lanczos_pass_one(mb_op_t op, const void* b_dev, int order, int64_t k, double scale,
+                        double* alphas, double* betas, int64_t* steps, double* b_norm);
+/* lanczos_pass_two (lanczos.h:177-218): x = sum_j y_j v_j by re-running the
+ * recurrence.  y is complex (interleaved re, im; `steps` entries). */
+int mb_lanczos_pass_two(mb_op_t op, const void* b_dev, int order, double scale,
+                        const double* alphas, const double* betas, int64_t steps, double b_norm,
+                        const double* y, void* x_dev);
+/* find_min_eigenpair (lanczos.h:283-290): Lanczos on Negated<H> from the given
+ * seed vector (the reference draws an unseeded arma::randu seed,
+ * linear_operator.h:26-32), eig of T, pass two.  vec_dev may be NULL.
+ * steps_out (may be NULL) receives the Lanczos steps taken. */
+int mb_find_min_eigenpair(mb_op_t op, int64_t k, const void* seed_dev, int order,
+                          const mb_lanczos_opts* opts, double* e0, void* vec_dev,
+                          int64_t* steps_out);
+/* find_max_eigenpair (lanczos.h:246-281). */
+int mb_find_max_eigenpair(mb_op_t op, int64_t k, const void* seed_dev, int order,
+                          const mb_lanczos_opts* opts, double* e_max, void* vec_dev,
+                          int64_t* steps_out);
+
+/* ---- Krylov time evolution (src/numerics/evolve_state.h) ----------------- *
+ * imaginary = 0: time_evolve_state, psi(t) = exp(-i t H) psi0 (:164-178);
+ * imaginary = 1: imaginary_time_evolve_state, exp(-t H) psi0 (:186-195).
+ * krylov_steps 0 means the reference default (30, EvolutionOptions :110-112). */
+int mb_time_evolve(mb_op_t op, const void* psi0_dev, int order, double t, int64_t krylov_steps,
+                   int imaginary, void* out_dev);
+/* time_evolve_state_steps (evolve_state.h:204-231) from t0 to t1 by dt,
+ * in place on psi_dev. */
+int mb_time_evolve_steps(mb_op_t op, void* psi_dev, int order, double t0, double t1, double dt,
+                         int64_t krylov_steps);
+
+/* ---- KPM (src/numerics/kpm.h, src/numerics/rescaling.h) ------------------ *
+ * Density-of-states Chebyshev moments mu[n] = (1/R) sum_r <r|T_n(Ht)|r> / D,
+ * Ht = (H - b)/a with (a, b) = rescaling::from_bounds(e_min, e_max, padding)
+ * (rescaling.h:33-38), R = n_probes random-phase vectors from
+ * mb_fill_phase(seed, stream_id = 1 + probe).  Uses the doubling identities
+ * mu_2n = 2<T_n|T_n> - mu_0, mu_2n+1 = 2<T_n+1|T_n> - mu_1 (n_moments/2
+ * matvecs per probe).  The reference implements only the Fermi projector;
+ * the DOS moments restate its Chebyshev recurrence (kpm.h:212-229). */
+int mb_kpm_dos_moments(mb_op_t op, int64_t n_moments, int64_t n_probes, uint64_t seed,
+                       double e_min, double e_max, double padding, double* mu);
+/* jackson_kernel (kpm.h:19-30), lorentz_kernel (kpm.h:34-44). */
+int mb_kpm_jackson_kernel(int64_t n, double* g);
+int mb_kpm_lorentz_kernel(int64_t n, double lambda, double* g);
+/* SparseKPMProjector(H, M, e_min, e_max, e_fermi, padding).apply(v)
+ * (kpm.h:184-241) on a complex vector. */
+int mb_kpm_projector_apply(mb_op_t op, int64_t expansion_order, double e_min, double e_max,
+                           double e_fermi, double padding, const void* v_dev, int order,
+                           void* out_dev);
+/* estimate_bounds (src/numerics/linear_operator_utils.h:53-77) by power
+ * iterations from the seeded vector (seed, stream_id 0). */
+int mb_estimate_bounds(mb_op_t op, int64_t power_iterations, double spectral_padding,
+                       uint64_t seed, double* lower, double* upper);
+
+/* ---- block reductions on device vectors (for drivers above this ABI) ---- */
+/* *out = Re <x, y> (arma::cdot real part), FP64 accumulation, deterministic. */
+int mb_dot_re(mb_op_t op, const void* x_dev, const void* y_dev, double* out);
+int mb_norm(mb_op_t op, const void* x_dev, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MANYBODY_GB300_H */

@@ -1,0 +1,548 @@
+"""manybody_gb300 -- GB300 matrix-free Hubbard engine, Python front end.
+
+Mirrors the calling surface of keyehzy/manybody's hot path
+(FermionBasis / HubbardModel{,2D,3D} / compute_matrix_elements /
+LinearOperator + Lanczos, KPM and Krylov evolution) over the C ABI in
+include/manybody_gb300.h, implemented by the in-tree CUDA library
+manybody_gb300/libmanybody_gb300.so (built by manybody_gb300/build.py).
+
+Device vectors are torch CUDA tensors of dtype complex128 (MB_PREC_F64) or
+complex64 (MB_PREC_F32); torch supplies allocation and streams only.  There
+is no CPU fallback: without the native library every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libmanybody_gb300.so")
+
+MB_OK = 0
+MB_ERR_INVALID_ARG = 1
+MB_ERR_CAPACITY = 2
+MB_ERR_ZERO_NORM = 3
+MB_ERR_DIM_MISMATCH = 4
+MB_ERR_EIG_FAILED = 5
+MB_ERR_OOM = 6
+MB_ERR_TIMEOUT = 7
+MB_ERR_CUDA = 8
+MB_ERR_NO_DEVICE = 9
+
+ORDER_REFERENCE = 0
+ORDER_TENSOR = 1
+
+PREC_F64 = 0
+PREC_F32 = 1
+
+_STATUS_NAMES = {
+    1: "MB_ERR_INVALID_ARG", 2: "MB_ERR_CAPACITY", 3: "MB_ERR_ZERO_NORM",
+    4: "MB_ERR_DIM_MISMATCH", 5: "MB_ERR_EIG_FAILED", 6: "MB_ERR_OOM", 7: "MB_ERR_TIMEOUT",
+    8: "MB_ERR_CUDA", 9: "MB_ERR_NO_DEVICE",
+}
+
+
+class MbError(RuntimeError):
+    """A non-zero mb_status from the native library."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+_i64 = C.c_int64
+_i64p = C.POINTER(C.c_int64)
+_u64p = C.POINTER(C.c_uint64)
+_dp = C.POINTER(C.c_double)
+_vp = C.c_void_p
+
+
+class LanczosOpts(C.Structure):
+    _fields_ = [("reorth", C.c_int), ("basis_precision", C.c_int), ("conv_tol", C.c_double),
+                ("check_every", C.c_int), ("refine", C.c_int)]
+
+
+# name -> (restype, argtypes); every exported symbol of include/manybody_gb300.h.
+SIGNATURES = {
+    "mb_version": (C.c_int, []),
+    "mb_last_error": (C.c_char_p, []),
+    "mb_device_count": (C.c_int, [C.POINTER(C.c_int)]),
+    "mb_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
+    "mb_free": (C.c_int, [_vp]),
+    "mb_memcpy": (C.c_int, [_vp, _vp, C.c_size_t, C.c_int]),
+    "mb_synchronize": (C.c_int, []),
+    "mb_basis_create_fixed_spin": (C.c_int, [_i64, _i64, C.c_int, C.POINTER(_vp)]),
+    "mb_basis_destroy": (C.c_int, [_vp]),
+    "mb_basis_size": (C.c_int, [_vp, _i64p]),
+    "mb_basis_sector": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p, _i64p]),
+    "mb_basis_export_reference_order": (C.c_int, [_vp, _u64p, _u64p]),
+    "mb_basis_index_of": (C.c_int, [_vp, C.c_uint64, C.c_uint64, _i64p]),
+    "mb_basis_permutation": (C.c_int, [_vp, _i64p]),
+    "mb_hubbard_create": (C.c_int, [_i64p, C.c_int, C.c_double, C.c_double, C.POINTER(_vp)]),
+    "mb_model_destroy": (C.c_int, [_vp]),
+    "mb_model_term_count": (C.c_int, [_vp, _i64p]),
+    "mb_compute_matrix_elements_csr": (C.c_int, [_vp, _vp, _i64p, _i64p, _i64p, _dp]),
+    "mb_op_create": (C.c_int, [_vp, _vp, C.c_int, C.POINTER(_vp)]),
+    "mb_op_destroy": (C.c_int, [_vp]),
+    "mb_op_dimension": (C.c_int, [_vp, _i64p]),
+    "mb_op_precision": (C.c_int, [_vp, C.POINTER(C.c_int)]),
+    "mb_op_apply": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
+    "mb_op_apply_affine": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_double, _vp,
+                                     C.c_int, _vp]),
+    "mb_op_apply_host": (C.c_int, [_vp, _vp, _vp, C.c_int]),
+    "mb_fill_uniform": (C.c_int, [_vp, C.c_uint64, C.c_uint32, _vp, C.c_int, _vp]),
+    "mb_fill_phase": (C.c_int, [_vp, C.c_uint64, C.c_uint32, _vp, C.c_int, _vp]),
+    "mb_lanczos_pass_one": (C.c_int, [_vp, _vp, C.c_int, _i64, C.c_double, _dp, _dp, _i64p, _dp]),
+    "mb_lanczos_pass_two": (C.c_int, [_vp, _vp, C.c_int, C.c_double, _dp, _dp, _i64, C.c_double,
+                                      _dp, _vp]),
+    "mb_find_min_eigenpair": (C.c_int, [_vp, _i64, _vp, C.c_int, C.POINTER(LanczosOpts), _dp, _vp,
+                                        _i64p]),
+    "mb_find_max_eigenpair": (C.c_int, [_vp, _i64, _vp, C.c_int, C.POINTER(LanczosOpts), _dp, _vp,
+                                        _i64p]),
+    "mb_time_evolve": (C.c_int, [_vp, _vp, C.c_int, C.c_double, _i64, C.c_int, _vp]),
+    "mb_time_evolve_steps": (C.c_int, [_vp, _vp, C.c_int, C.c_double, C.c_double, C.c_double,
+                                       _i64]),
+    "mb_kpm_dos_moments": (C.c_int, [_vp, _i64, _i64, C.c_uint64, C.c_double, C.c_double,
+                                     C.c_double, _dp]),
+    "mb_kpm_jackson_kernel": (C.c_int, [_i64, _dp]),
+    "mb_kpm_lorentz_kernel": (C.c_int, [_i64, C.c_double, _dp]),
+    "mb_kpm_projector_apply": (C.c_int, [_vp, _i64, C.c_double, C.c_double, C.c_double,
+                                         C.c_double, _vp, C.c_int, _vp]),
+    "mb_estimate_bounds": (C.c_int, [_vp, _i64, C.c_double, C.c_uint64, _dp, _dp]),
+    "mb_dot_re": (C.c_int, [_vp, _vp, _vp, _dp]),
+    "mb_norm": (C.c_int, [_vp, _vp, _dp]),
+}
+
+
+def lib():
+    """The loaded native library; raises if it was never built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"native library missing: {LIB_PATH} (run `python -m manybody_gb300.build`)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int):
+    if status != MB_OK:
+        raise MbError(status, lib().mb_last_error().decode(errors="replace"))
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    lib().mb_device_count(C.byref(n))
+    return n.value
+
+
+def _ptr(t) -> int:
+    """Device pointer of a torch tensor (or an int)."""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    if not t.is_contiguous():
+        raise ValueError("vectors must be contiguous")
+    return t.data_ptr()
+
+
+# ---------------------------------------------------------------------------
+# FermionBasis (src/algebra/fermion/basis.h)
+# ---------------------------------------------------------------------------
+class FermionBasis:
+    """Fixed-(N, Sz) fermion basis; mirrors BasisImpl (src/algebra/basis.h:12-76)."""
+
+    def __init__(self, handle, orbitals, particles):
+        self._h = handle
+        self.orbitals = orbitals
+        self.particles = particles
+
+    @classmethod
+    def with_fixed_particle_number_and_spin(cls, orbitals: int, particles: int,
+                                            spin_projection: int) -> "FermionBasis":
+        h = C.c_void_p()
+        _check(lib().mb_basis_create_fixed_spin(orbitals, particles, spin_projection, C.byref(h)))
+        return cls(h, orbitals, particles)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.mb_basis_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def size(self) -> int:
+        n = C.c_int64()
+        _check(lib().mb_basis_size(self._h, C.byref(n)))
+        return n.value
+
+    def __len__(self):
+        return self.size()
+
+    def sector(self):
+        v = [C.c_int64() for _ in range(5)]
+        _check(lib().mb_basis_sector(self._h, *[C.byref(x) for x in v]))
+        L, nu, nd, du, dd = (x.value for x in v)
+        return dict(orbitals=L, n_up=nu, n_down=nd, dim_up=du, dim_down=dd)
+
+    def keys(self):
+        """(up_masks, down_masks) uint64 arrays in reference index order."""
+        n = self.size()
+        up = np.zeros(n, np.uint64)
+        dn = np.zeros(n, np.uint64)
+        _check(lib().mb_basis_export_reference_order(self._h, up.ctypes.data_as(_u64p),
+                                                     dn.ctypes.data_as(_u64p)))
+        return up, dn
+
+    def index_of(self, up_mask: int, down_mask: int) -> int:
+        r = C.c_int64()
+        _check(lib().mb_basis_index_of(self._h, up_mask, down_mask, C.byref(r)))
+        return r.value
+
+    def contains(self, up_mask: int, down_mask: int) -> bool:
+        try:
+            self.index_of(up_mask, down_mask)
+            return True
+        except MbError:
+            return False
+
+    def permutation(self) -> np.ndarray:
+        """ref_of_tensor[r_up * D_down + r_down] = reference index."""
+        p = np.zeros(self.size(), np.int64)
+        _check(lib().mb_basis_permutation(self._h, p.ctypes.data_as(_i64p)))
+        return p
+
+
+# ---------------------------------------------------------------------------
+# HubbardModel / 2D / 3D (src/algebra/fermion/model/hubbard_model.h)
+# ---------------------------------------------------------------------------
+class _Hubbard:
+    def __init__(self, t: float, u: float, dims):
+        self.t, self.u, self.dims = float(t), float(u), tuple(int(d) for d in dims)
+        d = (C.c_int64 * len(self.dims))(*self.dims)
+        h = C.c_void_p()
+        _check(lib().mb_hubbard_create(d, len(self.dims), self.t, self.u, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.mb_model_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def orbitals(self) -> int:
+        return int(np.prod(self.dims))
+
+    def term_count(self) -> int:
+        """hamiltonian().size(): number of distinct operator terms."""
+        n = C.c_int64()
+        _check(lib().mb_model_term_count(self._h, C.byref(n)))
+        return n.value
+
+
+class HubbardModel(_Hubbard):
+    def __init__(self, t, u, size):
+        super().__init__(t, u, (size,))
+
+
+class HubbardModel2D(_Hubbard):
+    def __init__(self, t, u, size_x, size_y):
+        super().__init__(t, u, (size_x, size_y))
+
+
+class HubbardModel3D(_Hubbard):
+    def __init__(self, t, u, size_x, size_y, size_z):
+        super().__init__(t, u, (size_x, size_y, size_z))
+
+
+@dataclass
+class CsrMatrix:
+    """Reference-order sparse H: row_ptr (dim+1), col_idx, values (complex128)."""
+    dim: int
+    row_ptr: np.ndarray
+    col_idx: np.ndarray
+    values: np.ndarray
+
+    @property
+    def nnz(self) -> int:
+        return int(self.row_ptr[-1])
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.values, self.col_idx, self.row_ptr), shape=(self.dim, self.dim))
+
+
+def compute_matrix_elements(basis: FermionBasis, model: _Hubbard) -> CsrMatrix:
+    """compute_matrix_elements<sp_cx_mat> (src/algebra/matrix_elements.h:74-105), built on GPU."""
+    nnz = C.c_int64()
+    dim = basis.size()
+    rp = np.zeros(dim + 1, np.int64)
+    _check(lib().mb_compute_matrix_elements_csr(basis.handle, model.handle, C.byref(nnz),
+                                                rp.ctypes.data_as(_i64p), None, None))
+    n = nnz.value
+    ci = np.zeros(max(n, 1), np.int64)
+    vals = np.zeros(max(n, 1), np.complex128)
+    _check(lib().mb_compute_matrix_elements_csr(basis.handle, model.handle, C.byref(nnz),
+                                                rp.ctypes.data_as(_i64p), ci.ctypes.data_as(_i64p),
+                                                vals.view(np.float64).ctypes.data_as(_dp)))
+    return CsrMatrix(dim, rp, ci[:n], vals[:n])
+
+
+# ---------------------------------------------------------------------------
+# Matrix-free operator (replaces SparseComplexMatrixOperator,
+# src/numerics/linear_operator.h:81-91) and the Krylov drivers.
+# ---------------------------------------------------------------------------
+class GpuHubbardOperator:
+    """LinearOperator with apply(v) -> H v and dimension(), on the current GPU."""
+
+    def __init__(self, basis: FermionBasis, model: _Hubbard, precision: int = PREC_F64):
+        h = C.c_void_p()
+        _check(lib().mb_op_create(basis.handle, model.handle, precision, C.byref(h)))
+        self._h = h
+        self.precision = precision
+        self.basis = basis
+        self.model = model
+        self._dim = basis.size()
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.mb_op_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def dimension(self) -> int:
+        return self._dim
+
+    @property
+    def dtype(self):
+        import torch
+        return torch.complex64 if self.precision == PREC_F32 else torch.complex128
+
+    def empty(self):
+        import torch
+        return torch.empty(self._dim, dtype=self.dtype, device="cuda")
+
+    def _stream(self, stream):
+        if stream is None:
+            import torch
+            return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        return C.c_void_p(int(stream))
+
+    def apply(self, x, out=None, order: int = ORDER_REFERENCE, stream=None):
+        """y = H x (LinearOperator::apply, linear_operator.h:41)."""
+        y = self.empty() if out is None else out
+        _check(lib().mb_op_apply(self._h, _ptr(x), _ptr(y), order, self._stream(stream)))
+        return y
+
+    def apply_affine(self, x, scale=1.0, shift=0.0, beta=0.0, z=None, out=None,
+                     order: int = ORDER_REFERENCE, stream=None):
+        y = self.empty() if out is None else out
+        _check(lib().mb_op_apply_affine(self._h, _ptr(x), _ptr(y), scale, shift, beta, _ptr(z),
+                                        order, self._stream(stream)))
+        return y
+
+    def apply_host(self, x: np.ndarray, y: np.ndarray, order: int = ORDER_REFERENCE):
+        """apply() on host buffers (numpy or pinned torch CPU tensors)."""
+        xp = x.ctypes.data if isinstance(x, np.ndarray) else x.data_ptr()
+        yp = y.ctypes.data if isinstance(y, np.ndarray) else y.data_ptr()
+        _check(lib().mb_op_apply_host(self._h, xp, yp, order))
+        return y
+
+    def seed_vector(self, seed: int = 0, stream_id: int = 0, order: int = ORDER_REFERENCE,
+                    out=None):
+        v = self.empty() if out is None else out
+        _check(lib().mb_fill_uniform(self._h, seed, stream_id, _ptr(v), order,
+                                     self._stream(None)))
+        return v
+
+    def phase_vector(self, seed: int, stream_id: int = 0, order: int = ORDER_REFERENCE, out=None):
+        v = self.empty() if out is None else out
+        _check(lib().mb_fill_phase(self._h, seed, stream_id, _ptr(v), order, self._stream(None)))
+        return v
+
+    def dot_re(self, x, y) -> float:
+        r = C.c_double()
+        _check(lib().mb_dot_re(self._h, _ptr(x), _ptr(y), C.byref(r)))
+        return r.value
+
+    def norm(self, x) -> float:
+        r = C.c_double()
+        _check(lib().mb_norm(self._h, _ptr(x), C.byref(r)))
+        return r.value
+
+
+def _sync_torch():
+    import torch
+    torch.cuda.synchronize()
+
+
+@dataclass
+class LanczosDecomposition:
+    alphas: np.ndarray
+    betas: np.ndarray
+    steps_taken: int
+    b_norm: float
+
+
+def lanczos_pass_one(op: GpuHubbardOperator, b, k: int, scale: float = 1.0,
+                     order: int = ORDER_REFERENCE) -> LanczosDecomposition:
+    """lanczos_pass_one (src/numerics/lanczos.h:130-175)."""
+    _sync_torch()
+    a = np.zeros(max(k, 1))
+    bb = np.zeros(max(k, 1))
+    steps = C.c_int64()
+    bn = C.c_double()
+    _check(lib().mb_lanczos_pass_one(op.handle, _ptr(b), order, k, scale, a.ctypes.data_as(_dp),
+                                     bb.ctypes.data_as(_dp), C.byref(steps), C.byref(bn)))
+    m = steps.value
+    return LanczosDecomposition(a[:m].copy(), bb[:max(m - 1, 0)].copy(), m, bn.value)
+
+
+def lanczos_pass_two(op: GpuHubbardOperator, b, decomp: LanczosDecomposition, y_k,
+                     scale: float = 1.0, order: int = ORDER_REFERENCE, out=None):
+    """lanczos_pass_two (src/numerics/lanczos.h:177-218); y_k complex."""
+    _sync_torch()
+    x = op.empty() if out is None else out
+    y = np.ascontiguousarray(np.asarray(y_k, np.complex128))
+    al = np.ascontiguousarray(decomp.alphas, np.float64)
+    be = np.ascontiguousarray(decomp.betas if len(decomp.betas) else np.zeros(1), np.float64)
+    _check(lib().mb_lanczos_pass_two(op.handle, _ptr(b), order, scale, al.ctypes.data_as(_dp),
+                                     be.ctypes.data_as(_dp), decomp.steps_taken, decomp.b_norm,
+                                     y.view(np.float64).ctypes.data_as(_dp), _ptr(x)))
+    return x
+
+
+@dataclass
+class EigenPair:
+    value: float
+    vector: object
+    steps: int
+
+
+def _eigenpair(fn, op, k, seed, order, reorth, basis_precision, conv_tol, check_every,
+               want_vector):
+    _sync_torch()
+    opts = LanczosOpts(int(reorth), basis_precision, conv_tol, check_every, 0)
+    e = C.c_double()
+    steps = C.c_int64()
+    vec = op.empty() if want_vector else None
+    _check(fn(op.handle, k, _ptr(seed), order, C.byref(opts), C.byref(e), _ptr(vec),
+              C.byref(steps)))
+    return EigenPair(e.value, vec, steps.value)
+
+
+def find_min_eigenpair(op: GpuHubbardOperator, k: int, seed=None, order: int = ORDER_REFERENCE,
+                       reorth: bool = False, basis_precision: int = -1, conv_tol: float = 0.0,
+                       check_every: int = 10, want_vector: bool = True) -> EigenPair:
+    """find_min_eigenpair (src/numerics/lanczos.h:283-290) from a seeded start vector."""
+    if seed is None:
+        seed = op.seed_vector(0, order=order)
+    return _eigenpair(lib().mb_find_min_eigenpair, op, k, seed, order, reorth, basis_precision,
+                      conv_tol, check_every, want_vector)
+
+
+def find_max_eigenpair(op: GpuHubbardOperator, k: int, seed=None, order: int = ORDER_REFERENCE,
+                       reorth: bool = False, basis_precision: int = -1, conv_tol: float = 0.0,
+                       check_every: int = 10, want_vector: bool = True) -> EigenPair:
+    """find_max_eigenpair (src/numerics/lanczos.h:246-281)."""
+    if seed is None:
+        seed = op.seed_vector(0, order=order)
+    return _eigenpair(lib().mb_find_max_eigenpair, op, k, seed, order, reorth, basis_precision,
+                      conv_tol, check_every, want_vector)
+
+
+def time_evolve_state(op: GpuHubbardOperator, psi0, t: float, krylov_steps: int = 30,
+                      order: int = ORDER_REFERENCE, out=None):
+    """time_evolve_state (src/numerics/evolve_state.h:164-178): exp(-i t H) psi0."""
+    _sync_torch()
+    y = op.empty() if out is None else out
+    _check(lib().mb_time_evolve(op.handle, _ptr(psi0), order, t, krylov_steps, 0, _ptr(y)))
+    return y
+
+
+def imaginary_time_evolve_state(op: GpuHubbardOperator, psi0, t: float, krylov_steps: int = 30,
+                                order: int = ORDER_REFERENCE, out=None):
+    """imaginary_time_evolve_state (src/numerics/evolve_state.h): exp(-t H) psi0."""
+    _sync_torch()
+    y = op.empty() if out is None else out
+    _check(lib().mb_time_evolve(op.handle, _ptr(psi0), order, t, krylov_steps, 1, _ptr(y)))
+    return y
+
+
+def time_evolve_state_steps(op: GpuHubbardOperator, psi, t0: float, t1: float, dt: float,
+                            krylov_steps: int = 30, order: int = ORDER_REFERENCE):
+    """time_evolve_state_steps (src/numerics/evolve_state.h:204-231), in place."""
+    _sync_torch()
+    _check(lib().mb_time_evolve_steps(op.handle, _ptr(psi), order, t0, t1, dt, krylov_steps))
+    return psi
+
+
+def kpm_dos_moments(op: GpuHubbardOperator, n_moments: int, n_probes: int, seed: int,
+                    e_min: float, e_max: float, padding: float = 0.01) -> np.ndarray:
+    """DOS Chebyshev moments (1/R) sum_r <r|T_n(Ht)|r> / D with random-phase probes."""
+    _sync_torch()
+    mu = np.zeros(n_moments)
+    _check(lib().mb_kpm_dos_moments(op.handle, n_moments, n_probes, seed, e_min, e_max, padding,
+                                    mu.ctypes.data_as(_dp)))
+    return mu
+
+
+def jackson_kernel(n: int) -> np.ndarray:
+    g = np.zeros(n + 1)
+    _check(lib().mb_kpm_jackson_kernel(n, g.ctypes.data_as(_dp)))
+    return g
+
+
+def lorentz_kernel(n: int, lam: float = 4.0) -> np.ndarray:
+    g = np.zeros(n + 1)
+    _check(lib().mb_kpm_lorentz_kernel(n, lam, g.ctypes.data_as(_dp)))
+    return g
+
+
+class SparseKPMProjector:
+    """kpm::SparseKPMProjector (src/numerics/kpm.h:184-241) over the GPU operator."""
+
+    def __init__(self, op: GpuHubbardOperator, expansion_order: int, e_min: float, e_max: float,
+                 e_fermi: float = 0.0, padding: float = 0.01):
+        self.op, self.M = op, expansion_order
+        self.e_min, self.e_max, self.e_fermi, self.padding = e_min, e_max, e_fermi, padding
+
+    def dimension(self) -> int:
+        return self.op.dimension()
+
+    def apply(self, v, order: int = ORDER_REFERENCE, out=None):
+        _sync_torch()
+        y = self.op.empty() if out is None else out
+        _check(lib().mb_kpm_projector_apply(self.op.handle, self.M, self.e_min, self.e_max,
+                                            self.e_fermi, self.padding, _ptr(v), order, _ptr(y)))
+        return y
+
+
+def estimate_bounds(op: GpuHubbardOperator, power_iterations: int, spectral_padding: float,
+                    seed: int = 0):
+    """estimate_bounds (src/numerics/linear_operator_utils.h:53-77)."""
+    _sync_torch()
+    lo, hi = C.c_double(), C.c_double()
+    _check(lib().mb_estimate_bounds(op.handle, power_iterations, spectral_padding, seed,
+                                    C.byref(lo), C.byref(hi)))
+    return lo.value, hi.value

@@ -1,0 +1,376 @@
+// Host side of the engine: sector bases, the Hubbard model's bond list, the
+// per-spin hop tables, the tridiagonal eigensolver, and the basis / model
+// entry points of the C ABI.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "mb_internal.h"
+
+namespace mb {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+const Binom& binom_table() {
+  static const Binom table = [] {
+    Binom b{};
+    for (int n = 0; n < kMaxOrbitals + 2; ++n) {
+      b.c[n][0] = 1;
+      for (int k = 1; k <= n; ++k) b.c[n][k] = b.c[n - 1][k - 1] + (k <= n - 1 ? b.c[n - 1][k] : 0);
+    }
+    return b;
+  }();
+  return table;
+}
+
+// Masks with n of L bits set, in increasing numeric order (= colex order).
+static SpinSector make_sector(int L, int n) {
+  SpinSector s;
+  s.L = L;
+  s.n = n;
+  s.D = binom_at(binom_table(), L, n);
+  MB_REQUIRE(s.D <= kMaxSectorDim, MB_ERR_CAPACITY,
+             "spin sector C(" + std::to_string(L) + "," + std::to_string(n) +
+                 ") exceeds 2^23 states");
+  s.masks.resize((size_t)s.D);
+  if (n == 0) {
+    s.masks[0] = 0;
+    return s;
+  }
+  uint64_t m = (uint64_t(1) << n) - 1;
+  for (int64_t r = 0; r < s.D; ++r) {
+    s.masks[(size_t)r] = (uint32_t)m;
+    // Gosper's hack: next integer with the same popcount.
+    const uint64_t c = m & (~m + 1);
+    const uint64_t rr = m + c;
+    m = (((rr ^ m) >> 2) / c) | rr;
+  }
+  return s;
+}
+
+HopTable build_hop_table(const SpinSector& s, const mb_model_s& m) {
+  HopTable t;
+  const Binom& B = binom_table();
+  t.off.resize((size_t)s.D + 1);
+  t.off[0] = 0;
+  std::vector<uint32_t> ent;
+  ent.reserve((size_t)s.D * 8);
+  for (int64_t r = 0; r < s.D; ++r) {
+    const uint32_t mask = s.masks[(size_t)r];
+    if (m.has_hop) {
+      for (const auto& bd : m.bonds) {
+        const uint32_t ba = (mask >> bd.a) & 1u, bb = (mask >> bd.b) & 1u;
+        if (ba == bb) continue;
+        const uint32_t target = mask ^ (1u << bd.a) ^ (1u << bd.b);
+        const uint32_t between = ((1u << bd.b) - 1u) & ~((2u << bd.a) - 1u);
+        const uint32_t sign = (uint32_t)__builtin_popcount(mask & between) & 1u;
+        const int64_t tr = colex_rank(B, target);
+        ent.push_back(((uint32_t)tr << 8) | sign | (bd.mult == 2 ? 2u : 0u));
+      }
+    }
+    const int64_t deg = (int64_t)ent.size() - t.off[(size_t)r];
+    t.max_degree = std::max<int>(t.max_degree, (int)deg);
+    t.off[(size_t)r + 1] = (int32_t)ent.size();
+    MB_REQUIRE(ent.size() < (size_t)INT32_MAX, MB_ERR_CAPACITY, "hop table too large");
+  }
+  t.ent = std::move(ent);
+  bool any_self = false;
+  for (int v : m.self_mult) any_self = any_self || v;
+  if (any_self && m.has_hop) {
+    t.has_self = true;
+    t.self_energy.assign((size_t)s.D, 0.0);
+    for (int64_t r = 0; r < s.D; ++r) {
+      const uint32_t mask = s.masks[(size_t)r];
+      double e = 0.0;
+      for (int i = 0; i < m.L; ++i)
+        if (m.self_mult[(size_t)i] && ((mask >> i) & 1u)) e += -2.0 * m.t * m.self_mult[(size_t)i];
+      t.self_energy[(size_t)r] = e;
+    }
+  }
+  return t;
+}
+
+std::vector<double> u_fold_table(double u, bool has_u, int L) {
+  std::vector<double> f((size_t)L + 1, 0.0);
+  double acc = 0.0;
+  for (int k = 1; k <= L; ++k) {
+    acc = (k == 1) ? u : acc + u;
+    f[(size_t)k] = has_u ? acc : 0.0;
+  }
+  return f;
+}
+
+// Symmetric tridiagonal eigenproblem by the implicit QL algorithm with
+// Wilkinson shifts (Bowdler, Martin, Reinsch & Wilkinson, Numer. Math. 11,
+// 1968; EISPACK tql2).  d: diagonal (n), e: off-diagonal (n-1).  On return d
+// holds the eigenvalues ascending and z (if given, n*n column-major) the
+// orthonormal eigenvectors.  Replaces arma::eig_sym on T_k
+// (src/numerics/lanczos.h:258-270, evolve_state.h:33-47).
+bool tridiag_eig(int n, std::vector<double>& d, const std::vector<double>& e_in,
+                 std::vector<double>* z) {
+  if (n <= 0) return true;
+  std::vector<double> e((size_t)n, 0.0);
+  for (int i = 0; i + 1 < n; ++i) e[(size_t)i] = e_in[(size_t)i];
+  if (z) {
+    z->assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) (*z)[(size_t)i * n + i] = 1.0;
+  }
+  auto Z = [&](int row, int col) -> double& { return (*z)[(size_t)col * n + row]; };
+  const double eps = 2.220446049250313e-16;
+  for (int l = 0; l < n; ++l) {
+    int iter = 0;
+    while (true) {
+      int m = l;
+      for (; m < n - 1; ++m) {
+        const double dd = std::fabs(d[(size_t)m]) + std::fabs(d[(size_t)m + 1]);
+        if (std::fabs(e[(size_t)m]) <= eps * dd) break;
+      }
+      if (m == l) break;
+      if (++iter > 64) return false;
+      double g = (d[(size_t)l + 1] - d[(size_t)l]) / (2.0 * e[(size_t)l]);
+      double r = std::hypot(g, 1.0);
+      g = d[(size_t)m] - d[(size_t)l] + e[(size_t)l] / (g + std::copysign(r, g));
+      double s = 1.0, c = 1.0, p = 0.0;
+      bool deflated = false;
+      for (int i = m - 1; i >= l; --i) {
+        const double f = s * e[(size_t)i], b = c * e[(size_t)i];
+        r = std::hypot(f, g);
+        e[(size_t)i + 1] = r;
+        if (r == 0.0) {
+          d[(size_t)i + 1] -= p;
+          e[(size_t)m] = 0.0;
+          deflated = true;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = d[(size_t)i + 1] - p;
+        r = (d[(size_t)i] - g) * s + 2.0 * c * b;
+        p = s * r;
+        d[(size_t)i + 1] = g + p;
+        g = c * r - b;
+        if (z) {
+          for (int k = 0; k < n; ++k) {
+            const double zf = Z(k, i + 1);
+            Z(k, i + 1) = s * Z(k, i) + c * zf;
+            Z(k, i) = c * Z(k, i) - s * zf;
+          }
+        }
+      }
+      if (deflated) continue;
+      d[(size_t)l] -= p;
+      e[(size_t)l] = g;
+      e[(size_t)m] = 0.0;
+    }
+  }
+  // Selection sort, ascending, carrying vectors.
+  for (int i = 0; i + 1 < n; ++i) {
+    int k = i;
+    for (int j = i + 1; j < n; ++j)
+      if (d[(size_t)j] < d[(size_t)k]) k = j;
+    if (k != i) {
+      std::swap(d[(size_t)i], d[(size_t)k]);
+      if (z)
+        for (int r = 0; r < n; ++r) std::swap(Z(r, i), Z(r, k));
+    }
+  }
+  return true;
+}
+
+}  // namespace mb
+
+using namespace mb;
+
+extern "C" {
+
+int mb_version(void) { return 10000; }
+
+const char* mb_last_error(void) { return g_last_error.c_str(); }
+
+int mb_basis_create_fixed_spin(int64_t orbitals, int64_t particles, int spin_projection,
+                               mb_basis_t* out) {
+  return guard([&] {
+    MB_REQUIRE(out, MB_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    MB_REQUIRE(orbitals >= 1 && orbitals <= kMaxOrbitals, MB_ERR_CAPACITY,
+               "orbitals must be in [1, 32]");
+    MB_REQUIRE(particles >= 0 && particles <= 2 * orbitals, MB_ERR_INVALID_ARG,
+               "particles must be in [0, 2*orbitals]");
+    const int64_t sz = spin_projection;
+    MB_REQUIRE(std::llabs(sz) <= particles, MB_ERR_INVALID_ARG, "|spin_projection| > particles");
+    MB_REQUIRE((particles + sz) % 2 == 0, MB_ERR_INVALID_ARG,
+               "particles + spin_projection must be even");
+    const int64_t up = (particles + sz) / 2, down = particles - up;
+    MB_REQUIRE(up <= orbitals && down <= orbitals, MB_ERR_INVALID_ARG,
+               "more particles of one spin than orbitals");
+    auto b = std::make_unique<mb_basis_s>();
+    b->L = (int)orbitals;
+    b->n_up = (int)up;
+    b->n_down = (int)down;
+    b->up = make_sector(b->L, b->n_up);
+    b->down = make_sector(b->L, b->n_down);
+    b->dim = b->up.D * b->down.D;
+    MB_REQUIRE(b->dim < (int64_t)INT32_MAX, MB_ERR_CAPACITY, "sector dimension exceeds 2^31");
+    *out = b.release();
+  });
+}
+
+int mb_basis_destroy(mb_basis_t basis) {
+  delete basis;
+  return MB_OK;
+}
+
+int mb_basis_size(mb_basis_t basis, int64_t* dim) {
+  return guard([&] {
+    MB_REQUIRE(basis && dim, MB_ERR_INVALID_ARG, "NULL argument");
+    *dim = basis->dim;
+  });
+}
+
+int mb_basis_sector(mb_basis_t basis, int64_t* orbitals, int64_t* n_up, int64_t* n_down,
+                    int64_t* dim_up, int64_t* dim_down) {
+  return guard([&] {
+    MB_REQUIRE(basis, MB_ERR_INVALID_ARG, "NULL basis");
+    if (orbitals) *orbitals = basis->L;
+    if (n_up) *n_up = basis->n_up;
+    if (n_down) *n_down = basis->n_down;
+    if (dim_up) *dim_up = basis->up.D;
+    if (dim_down) *dim_down = basis->down.D;
+  });
+}
+
+int mb_basis_export_reference_order(mb_basis_t basis, uint64_t* up_masks, uint64_t* down_masks) {
+  return guard([&] {
+    MB_REQUIRE(basis && up_masks && down_masks, MB_ERR_INVALID_ARG, "NULL argument");
+    const Binom& B = binom_table();
+    const int64_t Dd = basis->down.D;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < basis->dim; ++i) {
+      const uint32_t u = basis->up.masks[(size_t)(i / Dd)], d = basis->down.masks[(size_t)(i % Dd)];
+      const int64_t r = reference_rank(B, u, d, basis->L);
+      up_masks[r] = u;
+      down_masks[r] = d;
+    }
+  });
+}
+
+int mb_basis_index_of(mb_basis_t basis, uint64_t up_mask, uint64_t down_mask, int64_t* index) {
+  return guard([&] {
+    MB_REQUIRE(basis && index, MB_ERR_INVALID_ARG, "NULL argument");
+    const uint64_t lim = basis->L >= 64 ? ~uint64_t(0) : ((uint64_t(1) << basis->L) - 1);
+    MB_REQUIRE((up_mask & ~lim) == 0 && (down_mask & ~lim) == 0 &&
+                   __builtin_popcountll(up_mask) == basis->n_up &&
+                   __builtin_popcountll(down_mask) == basis->n_down,
+               MB_ERR_INVALID_ARG, "key is not in the basis");
+    *index = reference_rank(binom_table(), (uint32_t)up_mask, (uint32_t)down_mask, basis->L);
+  });
+}
+
+int mb_basis_permutation(mb_basis_t basis, int64_t* ref_of_tensor) {
+  return guard([&] {
+    MB_REQUIRE(basis && ref_of_tensor, MB_ERR_INVALID_ARG, "NULL argument");
+    const Binom& B = binom_table();
+    const int64_t Dd = basis->down.D;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < basis->dim; ++i)
+      ref_of_tensor[i] = reference_rank(B, basis->up.masks[(size_t)(i / Dd)],
+                                        basis->down.masks[(size_t)(i % Dd)], basis->L);
+  });
+}
+
+int mb_hubbard_create(const int64_t* dims, int ndim, double t, double u, mb_model_t* out) {
+  return guard([&] {
+    MB_REQUIRE(out && dims, MB_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    MB_REQUIRE(ndim >= 1 && ndim <= 3, MB_ERR_INVALID_ARG, "ndim must be 1, 2 or 3");
+    int64_t L = 1;
+    for (int d = 0; d < ndim; ++d) {
+      MB_REQUIRE(dims[d] >= 1, MB_ERR_INVALID_ARG, "lattice dimension of size zero");
+      L *= dims[d];
+      MB_REQUIRE(L <= kMaxOrbitals, MB_ERR_CAPACITY, "more than 32 sites");
+    }
+    MB_REQUIRE(std::isfinite(t) && std::isfinite(u), MB_ERR_INVALID_ARG, "t and U must be finite");
+    auto m = std::make_unique<mb_model_s>();
+    m->dims.assign(dims, dims + ndim);
+    m->L = (int)L;
+    m->t = t;
+    m->u = u;
+    m->has_hop = !(t * t < kTol * kTol);
+    m->has_u = !(u * u < kTol * kTol);
+    m->self_mult.assign((size_t)L, 0);
+    const int64_t Lx = dims[0], Ly = ndim > 1 ? dims[1] : 1, Lz = ndim > 2 ? dims[2] : 1;
+    std::map<std::pair<int, int>, int> pairs;  // ordered like the reference's site loops
+    std::vector<std::pair<int, int>> order;
+    for (int64_t x = 0; x < Lx; ++x)
+      for (int64_t y = 0; y < Ly; ++y)
+        for (int64_t z = 0; z < Lz; ++z) {
+          const int site = (int)(x + Lx * (y + Ly * z));
+          const int nb[3] = {(int)(((x + 1) % Lx) + Lx * (y + Ly * z)),
+                             (int)(x + Lx * (((y + 1) % Ly) + Ly * z)),
+                             (int)(x + Lx * (y + Ly * ((z + 1) % Lz)))};
+          for (int d = 0; d < ndim; ++d) {
+            if (nb[d] == site) {
+              m->self_mult[(size_t)site] += 1;
+              continue;
+            }
+            const auto key = std::make_pair(std::min(site, nb[d]), std::max(site, nb[d]));
+            if (pairs[key]++ == 0) order.push_back(key);
+          }
+        }
+    for (const auto& k : order) {
+      const int mult = pairs[k];
+      MB_REQUIRE(mult <= 2, MB_ERR_INVALID_ARG, "bond listed more than twice");
+      m->bonds.push_back({k.first, k.second, mult});
+    }
+    int64_t terms = 0;
+    if (m->has_hop) {
+      terms += 4 * (int64_t)m->bonds.size();
+      for (int v : m->self_mult) terms += v ? 2 : 0;
+    }
+    if (m->has_u) terms += L;
+    m->n_terms = terms;
+    *out = m.release();
+  });
+}
+
+int mb_model_destroy(mb_model_t model) {
+  delete model;
+  return MB_OK;
+}
+
+int mb_model_term_count(mb_model_t model, int64_t* n_terms) {
+  return guard([&] {
+    MB_REQUIRE(model && n_terms, MB_ERR_INVALID_ARG, "NULL argument");
+    *n_terms = model->n_terms;
+  });
+}
+
+int mb_kpm_jackson_kernel(int64_t n, double* g) {
+  return guard([&] {
+    MB_REQUIRE(g && n >= 0, MB_ERR_INVALID_ARG, "bad argument");
+    const double pi = 3.14159265358979323846;
+    const double denom = (double)(n + 1);
+    const double cot_val = 1.0 / std::tan(pi / denom);
+    for (int64_t k = 0; k <= n; ++k) {
+      const double nd = (double)k;
+      const double arg = pi * nd / denom;
+      g[k] = ((denom - nd) * std::cos(arg) + std::sin(arg) * cot_val) / denom;
+    }
+  });
+}
+
+int mb_kpm_lorentz_kernel(int64_t n, double lambda, double* g) {
+  return guard([&] {
+    MB_REQUIRE(g && n >= 1, MB_ERR_INVALID_ARG, "bad argument");
+    const double sl = std::sinh(lambda);
+    for (int64_t k = 0; k <= n; ++k)
+      g[k] = std::sinh(lambda * (1.0 - (double)k / (double)n)) / sl;
+  });
+}
+
+}  // extern "C"

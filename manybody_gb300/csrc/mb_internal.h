@@ -1,0 +1,274 @@
+// Internal declarations shared by the engine's host and CUDA sources.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/manybody_gb300.h"
+
+namespace mb {
+
+// ---------------------------------------------------------------------------
+// Errors: internal code throws mb::Error; the C ABI converts it to a status
+// and stores the message in the thread-local last-error string.
+// ---------------------------------------------------------------------------
+struct Error : std::runtime_error {
+  int status;
+  Error(int s, const std::string& msg) : std::runtime_error(msg), status(s) {}
+};
+
+void set_last_error(const std::string& msg);
+
+#define MB_CUDA(call)                                                                  \
+  do {                                                                                 \
+    cudaError_t mb_err_ = (call);                                                      \
+    if (mb_err_ != cudaSuccess) {                                                      \
+      int mb_code_ = mb_err_ == cudaErrorMemoryAllocation ? MB_ERR_OOM : MB_ERR_CUDA;  \
+      throw ::mb::Error(mb_code_, std::string(#call) + ": " + cudaGetErrorString(mb_err_)); \
+    }                                                                                  \
+  } while (0)
+
+#define MB_REQUIRE(cond, status, msg)                 \
+  do {                                                \
+    if (!(cond)) throw ::mb::Error((status), (msg));  \
+  } while (0)
+
+// Tolerance 1000 * eps (src/utils/tolerances.h:7-10).
+constexpr double kTol = 1000.0 * 2.220446049250313e-16;
+constexpr int kMaxOrbitals = 32;
+constexpr int64_t kMaxSectorDim = int64_t(1) << 23;  // per spin; hop entries keep 24 bits
+
+// ---------------------------------------------------------------------------
+// Binomials and ranks (host + device).
+// ---------------------------------------------------------------------------
+struct Binom {
+  int64_t c[kMaxOrbitals + 2][kMaxOrbitals + 2];
+};
+const Binom& binom_table();
+
+__host__ __device__ inline int64_t binom_at(const Binom& B, int n, int k) {
+  return (k < 0 || n < 0 || k > n) ? 0 : B.c[n][k];
+}
+
+// Colex rank of an n-bit combination: sum_i C(p_i, i), p_1 < ... < p_n the
+// set bit positions.  Increasing integers with n bits set enumerate ranks
+// 0, 1, 2, ... in order (Gosper's hack order).
+__host__ __device__ inline int64_t colex_rank(const Binom& B, uint32_t m) {
+  int64_t r = 0;
+  int i = 1;
+  while (m) {
+#ifdef __CUDA_ARCH__
+    int p = __ffs(m) - 1;
+#else
+    int p = __builtin_ctz(m);
+#endif
+    r += B.c[p][i];
+    ++i;
+    m &= m - 1;
+  }
+  return r;
+}
+
+// Reference index of the state (up, down) on L orbitals.  The reference
+// enumerates states depth-first (src/algebra/basis.cpp:267-302): each level
+// appends one occupied slot, slots taken orbital-major with Up before Down on
+// the same orbital, children visited in (spin, orbital) order.  The index of a
+// state is therefore the number of complete sequences that are
+// lexicographically smaller under the element order (spin, orbital): at each
+// position, every valid smaller alternative e' contributes
+// C(#Up slots after e', Up left) * C(#Down slots after e', Down left).
+__host__ __device__ inline int64_t reference_rank(const Binom& B, uint32_t up, uint32_t down,
+                                                  int L) {
+#ifdef __CUDA_ARCH__
+  int ul = __popc(up), dl = __popc(down);
+#else
+  int ul = __builtin_popcount(up), dl = __builtin_popcount(down);
+#endif
+  int back_orb = -1, back_spin = 1;
+  int64_t r = 0;
+  for (int o = 0; o < L; ++o) {
+    for (int s = 0; s < 2; ++s) {
+      if (!(((s ? down : up) >> o) & 1u)) continue;
+      if (ul > 0) {
+        const int hi = (s == 0) ? o : L;
+        for (int op = back_orb + 1; op < hi; ++op)
+          r += binom_at(B, L - 1 - op, ul - 1) * binom_at(B, L - op, dl);
+      }
+      if (s == 1) {
+        for (int op = back_orb + (back_spin == 1 ? 1 : 0); op < o; ++op)
+          r += binom_at(B, L - 1 - op, ul) * binom_at(B, L - 1 - op, dl - 1);
+      }
+      if (s == 0) --ul; else --dl;
+      back_orb = o;
+      back_spin = s;
+    }
+  }
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// Host objects behind the opaque handles.
+// ---------------------------------------------------------------------------
+struct SpinSector {
+  int L = 0, n = 0;
+  int64_t D = 0;
+  std::vector<uint32_t> masks;  // colex rank -> occupation mask
+};
+
+}  // namespace mb
+
+struct mb_basis_s {
+  int L = 0, n_up = 0, n_down = 0;
+  int64_t dim = 0;
+  mb::SpinSector up, down;
+};
+
+struct mb_model_s {
+  std::vector<int64_t> dims;
+  int L = 0;
+  double t = 0.0, u = 0.0;
+  bool has_hop = false, has_u = false;
+  // Undirected bonds a < b with their multiplicity (1, or 2 when a lattice
+  // dimension of size 2 lists the pair twice).
+  struct Bond { int a, b, mult; };
+  std::vector<Bond> bonds;
+  // self_mult[i] = number of hopping(i, i) calls (a dimension of size 1).
+  std::vector<int> self_mult;
+  int64_t n_terms = 0;
+};
+
+namespace mb {
+
+// Hop table of one spin sector: CSR over colex ranks.  Entry =
+// (target_rank << 8) | code; code bit0 = negative sign, bit1 = doubled bond.
+// The element <target|c+_x c_y|source> of one bond is
+// (-1)^popcount(source & bits strictly between x and y).
+struct HopTable {
+  std::vector<int32_t> off;
+  std::vector<uint32_t> ent;
+  int max_degree = 0;
+  std::vector<double> self_energy;  // per state: sum over self bonds of -2t*mult*occupation
+  bool has_self = false;
+};
+HopTable build_hop_table(const SpinSector& s, const mb_model_s& m);
+
+// Left fold U + U + ... (k terms), the order-independent value the reference
+// accumulates for k doubly occupied sites (matrix_elements.h:85-96).
+std::vector<double> u_fold_table(double u, bool has_u, int L);
+
+// Device-side view of an operator (POD; passed to kernels by value).
+struct OpView {
+  int64_t Du, Dd, dim;
+  int L;
+  const uint32_t* up_mask;
+  const uint32_t* dn_mask;
+  const int32_t* up_off;
+  const uint32_t* up_ent;
+  const int32_t* dn_off;
+  const uint32_t* dn_ent;
+  const double* u_fold;     // [L+1]
+  const double* self_up;    // [Du] or nullptr
+  const double* self_dn;    // [Dd] or nullptr
+  const float* u_fold_f;    // float copies for complex64 operators
+  const float* self_up_f;
+  const float* self_dn_f;
+  double t;
+  int max_up_degree;
+  int max_dn_degree;
+};
+
+}  // namespace mb
+
+struct mb_op_s {
+  int device = 0;
+  int precision = MB_PREC_F64;
+  int L = 0, n_up = 0, n_down = 0;
+  int64_t Du = 0, Dd = 0, dim = 0;
+  double t = 0.0, u = 0.0;
+  mb::OpView view{};
+  std::vector<void*> allocations;  // device buffers owned by the op
+  int32_t* perm = nullptr;         // tensor -> reference index (lazy)
+  std::mutex mu;
+  struct Scratch {
+    void* a = nullptr;  // tensor-order copies for reference-order calls
+    void* b = nullptr;
+    void* hx = nullptr;  // device staging for host-buffer calls
+    void* hy = nullptr;
+  };
+  std::map<cudaStream_t, Scratch> scratch;
+  bool q_ready = false;            // Q64 extra tables built
+  void* q_tables = nullptr;
+};
+
+namespace mb {
+
+// Kernel launchers (mb_kernels.cu).  All asynchronous on `st`.
+size_t elem_bytes(int precision);
+void launch_apply(const OpView& v, int precision, const void* x, void* y, double scale,
+                  double shift, double beta, const void* z, double* partials, int dot_mode,
+                  cudaStream_t st);
+int apply_grid(const OpView& v, int precision);
+void launch_reduce(const double* partials, int nblocks, int ncomp, double* out, cudaStream_t st);
+int blas_grid(int64_t n);
+// y = a*x + b*y (complex coefficients); dots of the result if dot_mode.
+void launch_axpby(int precision, int64_t n, double ar, double ai, const void* x, double br,
+                  double bi, void* y, double* partials, int dot_mode, cudaStream_t st);
+// partials for Re<x,y> (comp 0), Im<x,y> (comp 1), <y,y> (comp 2).
+void launch_dot(int precision, int64_t n, const void* x, const void* y, double* partials,
+                cudaStream_t st);
+int multi_dot_grid(int64_t n);
+// c[j] = <V_j, w> for j < m (complex, 2 comps each) -> partials [blocks][2m]
+void launch_multi_dot(int vprec, int wprec, int64_t n, const void* V, int64_t ld, int m,
+                      const void* w, double* partials, cudaStream_t st);
+// w -= sum_j c[j] V_j ; c on device (interleaved complex), then <w,w> partials
+void launch_multi_axpy(int vprec, int wprec, int64_t n, const void* V, int64_t ld, int m,
+                       const double* c, void* w, double* partials, cudaStream_t st);
+void launch_convert(int from_prec, int to_prec, int64_t n, const void* x, void* y,
+                    cudaStream_t st);
+void launch_gather(int precision, int64_t n, const int32_t* perm, const void* src, void* dst,
+                   cudaStream_t st);   // dst[i] = src[perm[i]]
+void launch_scatter(int precision, int64_t n, const int32_t* perm, const void* src, void* dst,
+                    cudaStream_t st);  // dst[perm[i]] = src[i]
+void launch_fill_rng(int precision, int64_t Du, int64_t Dd, uint64_t seed, uint32_t stream_id,
+                     int phase, void* dst, cudaStream_t st);
+void launch_perm(const OpView& v, int32_t* perm, cudaStream_t st);
+void launch_csr_count(const OpView& v, const int32_t* perm, int32_t* row_count, cudaStream_t st);
+void launch_csr_fill(const OpView& v, const int32_t* perm, const int64_t* row_ptr,
+                     int64_t* col_idx, double* values, cudaStream_t st);
+void upload_binomials(cudaStream_t st);
+
+// Host tridiagonal eigensolver (implicit QL, mb_tridiag.cpp).
+bool tridiag_eig(int n, std::vector<double>& d, const std::vector<double>& e,
+                 std::vector<double>* z);
+
+}  // namespace mb
+
+namespace mb {
+
+// Runs f and converts exceptions to an mb_status + thread-local message.
+template <typename F>
+int guard(F&& f) {
+  try {
+    f();
+    return MB_OK;
+  } catch (const Error& e) {
+    set_last_error(e.what());
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    set_last_error("host allocation failed");
+    return MB_ERR_OOM;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return MB_ERR_INVALID_ARG;
+  }
+}
+
+}  // namespace mb

@@ -1,0 +1,687 @@
+// CUDA kernels of the matrix-free Hubbard operator and the Krylov drivers.
+//
+// Layout in HBM: a state vector is X[r_up * D_down + r_down] (tensor order),
+// interleaved complex (double2 / float2), r_up / r_down the colex ranks of the
+// up / down occupation masks.  H = H_up (x) 1 + 1 (x) H_down + diag, where the
+// per-spin hopping matrices come from hop tables (CSR over ranks, see
+// mb_internal.h) and diag = U * popcount(up & down) (+ self-bond energies).
+#include <cuda_runtime.h>
+
+#include "mb_internal.h"
+
+namespace mb {
+
+template <typename T> struct C2;
+template <> struct C2<double> { using type = double2; };
+template <> struct C2<float> { using type = float2; };
+
+size_t elem_bytes(int precision) { return precision == MB_PREC_F32 ? 8 : 16; }
+
+// ---------------------------------------------------------------------------
+// Dot-product accumulators.  FP64 dots on this GPU's FP64 pipe for double
+// vectors; for float vectors a compensated float pair (TwoSum on exact
+// TwoProd terms, Knuth / Ogita-Rump-Oishi) so no FP64 instruction runs per
+// element.
+// ---------------------------------------------------------------------------
+template <typename T> struct DotAcc;
+template <> struct DotAcc<double> {
+  double s = 0.0;
+  __device__ void add_prod(double a, double b) { s = fma(a, b, s); }
+  __device__ double value() const { return s; }
+};
+template <> struct DotAcc<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ void add_prod(float a, float b) {
+    const float p = a * b;
+    const float pe = fmaf(a, b, -p);
+    const float s = hi + p;
+    const float bp = s - hi;
+    const float e = (hi - (s - bp)) + (p - bp);
+    hi = s;
+    lo += e + pe;
+  }
+  __device__ double value() const { return (double)hi + (double)lo; }
+};
+
+// Block reduction of NC doubles; thread 0 writes partials[blockIdx.x*NC + k].
+template <int NC>
+__device__ void block_reduce_store(double (&v)[NC], double* partials) {
+  __shared__ double red[32][NC > 0 ? NC : 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    double a = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    v[k] = a;
+  }
+  __syncthreads();
+  if (lane == 0)
+    for (int k = 0; k < NC; ++k) red[warp][k] = v[k];
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int k = 0; k < NC; ++k) {
+      double a = lane < nw ? red[lane][k] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+      if (lane == 0) partials[(size_t)blockIdx.x * NC + k] = a;
+    }
+  }
+}
+
+// Fixed-order final reduction: out[k] = sum_b partials[b*ncomp + k].
+__global__ void k_reduce(const double* __restrict__ partials, int nblocks, int ncomp,
+                         double* __restrict__ out) {
+  __shared__ double s[256];
+  for (int k = 0; k < ncomp; ++k) {
+    double a = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) a += partials[(size_t)b * ncomp + k];
+    s[threadIdx.x] = a;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[k] = s[0];
+    __syncthreads();
+  }
+}
+
+void launch_reduce(const double* partials, int nblocks, int ncomp, double* out, cudaStream_t st) {
+  k_reduce<<<1, 256, 0, st>>>(partials, nblocks, ncomp, out);
+  MB_CUDA(cudaGetLastError());
+}
+
+static int num_sms() {
+  static int sms = -1;
+  if (sms < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+static int max_smem_optin() {
+  static int v = -1;
+  if (v < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  }
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// The matrix-free apply:  y = scale * (H - shift) x + beta * z
+// with optional fused dot products (dot_mode bit0: Re<x,y>, bit1: <y,y>,
+// bit2: <x,x>).  One CTA processes whole rows r_up (grid-stride): it stages
+// the row X[r_up, :] in shared memory (when it fits), so the down hops, which
+// stay inside the row, gather from shared memory, while the up hops read the
+// neighbour rows X[r_up', c] straight from HBM/L2 with coalesced 8/16-byte
+// loads (consecutive threads take consecutive columns).  The up-neighbour
+// list of the row (same for every column) sits in shared memory.
+// ---------------------------------------------------------------------------
+constexpr int kApplyThreads = 1024;
+
+template <typename T>
+__device__ __forceinline__ T hop_weight(uint32_t e) {
+  T w = (e & 2u) ? T(2) : T(1);
+  return (e & 1u) ? -w : w;
+}
+
+template <typename T, bool STAGED, int DOTS>
+__global__ void __launch_bounds__(kApplyThreads)
+k_apply(OpView v, const typename C2<T>::type* __restrict__ x, typename C2<T>::type* y,
+        T hop_coef, T dscale, T shift, T beta, const typename C2<T>::type* z,
+        const T* __restrict__ ufold, const T* __restrict__ self_up, const T* __restrict__ self_dn,
+        double* __restrict__ partials) {
+  using V2 = typename C2<T>::type;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int up_words = (v.max_up_degree + 3) & ~3;
+  uint32_t* s_upn = reinterpret_cast<uint32_t*>(smem);
+  V2* s_row = reinterpret_cast<V2*>(smem + sizeof(uint32_t) * up_words);
+  const int64_t Dd = v.Dd;
+  DotAcc<T> a_xy, a_yy, a_xx;
+
+  for (int64_t r = blockIdx.x; r < v.Du; r += gridDim.x) {
+    const V2* xrow = x + r * Dd;
+    __syncthreads();
+    const int u0 = v.up_off[r], nup = v.up_off[r + 1] - u0;
+    for (int j = threadIdx.x; j < nup; j += blockDim.x) s_upn[j] = v.up_ent[u0 + j];
+    if (STAGED)
+      for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) s_row[c] = xrow[c];
+    __syncthreads();
+    const uint32_t um = v.up_mask[r];
+    const T su = self_up ? self_up[r] : T(0);
+    for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) {
+      T ar = T(0), ai = T(0);
+      const int d0 = v.dn_off[c], d1 = v.dn_off[c + 1];
+      for (int j = d0; j < d1; ++j) {
+        const uint32_t e = __ldg(&v.dn_ent[j]);
+        const V2 val = STAGED ? s_row[e >> 8] : __ldg(&xrow[e >> 8]);
+        const T w = hop_weight<T>(e);
+        ar = fma(w, val.x, ar);
+        ai = fma(w, val.y, ai);
+      }
+#pragma unroll 4
+      for (int j = 0; j < nup; ++j) {
+        const uint32_t e = s_upn[j];
+        const V2 val = __ldg(&x[(int64_t)(e >> 8) * Dd + c]);
+        const T w = hop_weight<T>(e);
+        ar = fma(w, val.x, ar);
+        ai = fma(w, val.y, ai);
+      }
+      const V2 xv = STAGED ? s_row[c] : xrow[c];
+      T dv = ufold[__popc(um & v.dn_mask[c])] + su;
+      if (self_dn) dv += self_dn[c];
+      const T ds = dscale * (dv - shift);
+      V2 out;
+      out.x = fma(hop_coef, ar, ds * xv.x);
+      out.y = fma(hop_coef, ai, ds * xv.y);
+      const int64_t idx = r * Dd + c;
+      if (z) {
+        const V2 zv = z[idx];
+        out.x = fma(beta, zv.x, out.x);
+        out.y = fma(beta, zv.y, out.y);
+      }
+      y[idx] = out;
+      if (DOTS & 1) { a_xy.add_prod(xv.x, out.x); a_xy.add_prod(xv.y, out.y); }
+      if (DOTS & 2) { a_yy.add_prod(out.x, out.x); a_yy.add_prod(out.y, out.y); }
+      if (DOTS & 4) { a_xx.add_prod(xv.x, xv.x); a_xx.add_prod(xv.y, xv.y); }
+    }
+  }
+  if (DOTS) {
+    double vals[3] = {a_xy.value(), a_yy.value(), a_xx.value()};
+    block_reduce_store<3>(vals, partials);
+  }
+}
+
+static size_t apply_smem(const OpView& v, int precision, bool staged) {
+  const int up_words = (v.max_up_degree + 3) & ~3;
+  size_t s = sizeof(uint32_t) * (size_t)up_words;
+  if (staged) s += elem_bytes(precision) * (size_t)v.Dd;
+  return s;
+}
+
+static bool apply_staged(const OpView& v, int precision) {
+  return apply_smem(v, precision, true) + 1024 <= (size_t)max_smem_optin();
+}
+
+int apply_grid(const OpView& v, int /*precision*/) {
+  int64_t g = (int64_t)num_sms();
+  if (g > v.Du) g = v.Du;
+  return (int)(g > 0 ? g : 1);
+}
+
+template <typename T, bool STAGED, int DOTS>
+static void apply_t(const OpView& v, const void* x, void* y, double scale, double shift,
+                    double beta, const void* z, double* partials, cudaStream_t st) {
+  using V2 = typename C2<T>::type;
+  const size_t smem = apply_smem(v, sizeof(T) == 8 ? MB_PREC_F64 : MB_PREC_F32, STAGED);
+  auto kern = k_apply<T, STAGED, DOTS>;
+  MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const T* uf = sizeof(T) == 8 ? (const T*)v.u_fold : (const T*)v.u_fold_f;
+  const T* su = sizeof(T) == 8 ? (const T*)v.self_up : (const T*)v.self_up_f;
+  const T* sd = sizeof(T) == 8 ? (const T*)v.self_dn : (const T*)v.self_dn_f;
+  const int grid = apply_grid(v, 0);
+  kern<<<grid, kApplyThreads, smem, st>>>(v, (const V2*)x, (V2*)y, (T)(-v.t * scale), (T)scale,
+                                          (T)shift, (T)beta, (const V2*)z, uf, su, sd, partials);
+  MB_CUDA(cudaGetLastError());
+}
+
+template <typename T, bool STAGED>
+static void apply_dots(const OpView& v, const void* x, void* y, double scale, double shift,
+                       double beta, const void* z, double* partials, int dot_mode,
+                       cudaStream_t st) {
+  switch (dot_mode) {
+    case 0: apply_t<T, STAGED, 0>(v, x, y, scale, shift, beta, z, partials, st); break;
+    case 1: apply_t<T, STAGED, 1>(v, x, y, scale, shift, beta, z, partials, st); break;
+    case 2: apply_t<T, STAGED, 2>(v, x, y, scale, shift, beta, z, partials, st); break;
+    case 3: apply_t<T, STAGED, 3>(v, x, y, scale, shift, beta, z, partials, st); break;
+    case 5: apply_t<T, STAGED, 5>(v, x, y, scale, shift, beta, z, partials, st); break;
+    default: apply_t<T, STAGED, 7>(v, x, y, scale, shift, beta, z, partials, st); break;
+  }
+}
+
+void launch_apply(const OpView& v, int precision, const void* x, void* y, double scale,
+                  double shift, double beta, const void* z, double* partials, int dot_mode,
+                  cudaStream_t st) {
+  const bool staged = apply_staged(v, precision);
+  if (precision == MB_PREC_F32) {
+    if (staged) apply_dots<float, true>(v, x, y, scale, shift, beta, z, partials, dot_mode, st);
+    else apply_dots<float, false>(v, x, y, scale, shift, beta, z, partials, dot_mode, st);
+  } else {
+    if (staged) apply_dots<double, true>(v, x, y, scale, shift, beta, z, partials, dot_mode, st);
+    else apply_dots<double, false>(v, x, y, scale, shift, beta, z, partials, dot_mode, st);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Vector kernels (grid-stride, one complex element per step).
+// ---------------------------------------------------------------------------
+constexpr int kBlasThreads = 256;
+
+int blas_grid(int64_t n) {
+  int64_t g = (n + kBlasThreads - 1) / kBlasThreads;
+  const int64_t cap = (int64_t)num_sms() * 8;
+  if (g > cap) g = cap;
+  return (int)(g > 0 ? g : 1);
+}
+
+// y = a*x + b*y, complex a, b; dot_mode bit1: <y,y> of the result.
+template <typename T, int DOTS>
+__global__ void k_axpby(int64_t n, T ar, T ai, const typename C2<T>::type* __restrict__ x, T br,
+                        T bi, typename C2<T>::type* __restrict__ y, double* __restrict__ partials) {
+  using V2 = typename C2<T>::type;
+  DotAcc<T> acc;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const V2 xv = x ? x[i] : V2{T(0), T(0)};
+    const V2 yv = (br != T(0) || bi != T(0)) ? y[i] : V2{T(0), T(0)};
+    V2 o;
+    o.x = ar * xv.x - ai * xv.y + br * yv.x - bi * yv.y;
+    o.y = ar * xv.y + ai * xv.x + br * yv.y + bi * yv.x;
+    y[i] = o;
+    if (DOTS & 2) { acc.add_prod(o.x, o.x); acc.add_prod(o.y, o.y); }
+  }
+  if (DOTS) {
+    double vals[3] = {0.0, acc.value(), 0.0};
+    block_reduce_store<3>(vals, partials);
+  }
+}
+
+void launch_axpby(int precision, int64_t n, double ar, double ai, const void* x, double br,
+                  double bi, void* y, double* partials, int dot_mode, cudaStream_t st) {
+  const int g = blas_grid(n);
+  if (precision == MB_PREC_F32) {
+    if (dot_mode) k_axpby<float, 2><<<g, kBlasThreads, 0, st>>>(n, (float)ar, (float)ai, (const float2*)x, (float)br, (float)bi, (float2*)y, partials);
+    else k_axpby<float, 0><<<g, kBlasThreads, 0, st>>>(n, (float)ar, (float)ai, (const float2*)x, (float)br, (float)bi, (float2*)y, partials);
+  } else {
+    if (dot_mode) k_axpby<double, 2><<<g, kBlasThreads, 0, st>>>(n, ar, ai, (const double2*)x, br, bi, (double2*)y, partials);
+    else k_axpby<double, 0><<<g, kBlasThreads, 0, st>>>(n, ar, ai, (const double2*)x, br, bi, (double2*)y, partials);
+  }
+  MB_CUDA(cudaGetLastError());
+}
+
+// Re<x,y>, Im<x,y>, <y,y> with <x,y> = sum conj(x_i) y_i (arma::cdot).
+template <typename T>
+__global__ void k_dot(int64_t n, const typename C2<T>::type* __restrict__ x,
+                      const typename C2<T>::type* __restrict__ y, double* __restrict__ partials) {
+  using V2 = typename C2<T>::type;
+  DotAcc<T> re, im, yy;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const V2 a = x[i], b = y[i];
+    re.add_prod(a.x, b.x);
+    re.add_prod(a.y, b.y);
+    im.add_prod(a.x, b.y);
+    im.add_prod(-a.y, b.x);
+    yy.add_prod(b.x, b.x);
+    yy.add_prod(b.y, b.y);
+  }
+  double vals[3] = {re.value(), im.value(), yy.value()};
+  block_reduce_store<3>(vals, partials);
+}
+
+void launch_dot(int precision, int64_t n, const void* x, const void* y, double* partials,
+                cudaStream_t st) {
+  const int g = blas_grid(n);
+  if (precision == MB_PREC_F32)
+    k_dot<float><<<g, kBlasThreads, 0, st>>>(n, (const float2*)x, (const float2*)y, partials);
+  else
+    k_dot<double><<<g, kBlasThreads, 0, st>>>(n, (const double2*)x, (const double2*)y, partials);
+  MB_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// Re-orthogonalisation against a stored basis V (columns V_j, leading
+// dimension ld elements), V in FP64 or FP32, w in FP64 or FP32.
+// multi_dot: c_j = <V_j, w>; each block keeps per-j sums in shared memory
+// over the chunks it owns and writes one partial per j.
+// ---------------------------------------------------------------------------
+constexpr int kMdChunk = 1024;
+constexpr int kMdThreads = 256;
+constexpr int kMaxBasis = 1024;
+
+template <typename TV, typename TW>
+__global__ void __launch_bounds__(kMdThreads)
+k_multi_dot(int64_t n, const typename C2<TV>::type* __restrict__ V, int64_t ld, int m,
+            const typename C2<TW>::type* __restrict__ w, double* __restrict__ partials) {
+  using VV = typename C2<TV>::type;
+  using VW = typename C2<TW>::type;
+  __shared__ double acc[2 * kMaxBasis];
+  __shared__ double2 sw[kMdChunk];
+  for (int j = threadIdx.x; j < 2 * m; j += blockDim.x) acc[j] = 0.0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int64_t base = (int64_t)blockIdx.x * kMdChunk; base < n; base += (int64_t)gridDim.x * kMdChunk) {
+    const int len = (int)((n - base) < kMdChunk ? (n - base) : kMdChunk);
+    __syncthreads();
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+      const VW a = w[base + i];
+      sw[i] = make_double2((double)a.x, (double)a.y);
+    }
+    __syncthreads();
+    for (int j = warp; j < m; j += nwarps) {
+      const VV* vj = V + (int64_t)j * ld + base;
+      double cr = 0.0, ci = 0.0;
+      for (int i = lane; i < len; i += 32) {
+        const VV a = vj[i];
+        const double ar = (double)a.x, ai = (double)a.y;
+        const double2 b = sw[i];
+        cr = fma(ar, b.x, cr);
+        cr = fma(ai, b.y, cr);
+        ci = fma(ar, b.y, ci);
+        ci = fma(-ai, b.x, ci);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        cr += __shfl_down_sync(0xffffffffu, cr, o);
+        ci += __shfl_down_sync(0xffffffffu, ci, o);
+      }
+      if (lane == 0) { acc[2 * j] += cr; acc[2 * j + 1] += ci; }
+    }
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < 2 * m; j += blockDim.x)
+    partials[(size_t)blockIdx.x * 2 * m + j] = acc[j];
+}
+
+static int md_grid(int64_t n) {
+  int64_t g = (n + kMdChunk - 1) / kMdChunk;
+  const int64_t cap = (int64_t)num_sms() * 2;
+  if (g > cap) g = cap;
+  return (int)(g > 0 ? g : 1);
+}
+
+int multi_dot_grid(int64_t n) { return md_grid(n); }
+
+void launch_multi_dot(int vprec, int wprec, int64_t n, const void* V, int64_t ld, int m,
+                      const void* w, double* partials, cudaStream_t st) {
+  MB_REQUIRE(m <= kMaxBasis, MB_ERR_CAPACITY, "re-orthogonalisation basis larger than 1024");
+  const int g = md_grid(n);
+  if (vprec == MB_PREC_F32 && wprec == MB_PREC_F32)
+    k_multi_dot<float, float><<<g, kMdThreads, 0, st>>>(n, (const float2*)V, ld, m, (const float2*)w, partials);
+  else if (vprec == MB_PREC_F32)
+    k_multi_dot<float, double><<<g, kMdThreads, 0, st>>>(n, (const float2*)V, ld, m, (const double2*)w, partials);
+  else if (wprec == MB_PREC_F32)
+    k_multi_dot<double, float><<<g, kMdThreads, 0, st>>>(n, (const double2*)V, ld, m, (const float2*)w, partials);
+  else
+    k_multi_dot<double, double><<<g, kMdThreads, 0, st>>>(n, (const double2*)V, ld, m, (const double2*)w, partials);
+  MB_CUDA(cudaGetLastError());
+}
+
+// w -= sum_j c_j V_j (c complex, on device), then <w,w> partials.
+template <typename TV, typename TW>
+__global__ void __launch_bounds__(kBlasThreads)
+k_multi_axpy(int64_t n, const typename C2<TV>::type* __restrict__ V, int64_t ld, int m,
+             const double* __restrict__ c, typename C2<TW>::type* __restrict__ w,
+             double* __restrict__ partials) {
+  using VV = typename C2<TV>::type;
+  using VW = typename C2<TW>::type;
+  __shared__ double sc[2 * kMaxBasis];
+  for (int j = threadIdx.x; j < 2 * m; j += blockDim.x) sc[j] = c[j];
+  __syncthreads();
+  DotAcc<double> ww;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const VW wv = w[i];
+    double sr = (double)wv.x, si = (double)wv.y;
+    for (int j = 0; j < m; ++j) {
+      const VV a = V[(int64_t)j * ld + i];
+      const double cr = sc[2 * j], ci = sc[2 * j + 1];
+      sr -= cr * (double)a.x - ci * (double)a.y;
+      si -= cr * (double)a.y + ci * (double)a.x;
+    }
+    VW o;
+    o.x = (decltype(o.x))sr;
+    o.y = (decltype(o.y))si;
+    w[i] = o;
+    ww.add_prod((double)o.x, (double)o.x);
+    ww.add_prod((double)o.y, (double)o.y);
+  }
+  double vals[3] = {0.0, ww.value(), 0.0};
+  block_reduce_store<3>(vals, partials);
+}
+
+void launch_multi_axpy(int vprec, int wprec, int64_t n, const void* V, int64_t ld, int m,
+                       const double* c, void* w, double* partials, cudaStream_t st) {
+  MB_REQUIRE(m <= kMaxBasis, MB_ERR_CAPACITY, "re-orthogonalisation basis larger than 1024");
+  const int g = blas_grid(n);
+  if (vprec == MB_PREC_F32 && wprec == MB_PREC_F32)
+    k_multi_axpy<float, float><<<g, kBlasThreads, 0, st>>>(n, (const float2*)V, ld, m, c, (float2*)w, partials);
+  else if (vprec == MB_PREC_F32)
+    k_multi_axpy<float, double><<<g, kBlasThreads, 0, st>>>(n, (const float2*)V, ld, m, c, (double2*)w, partials);
+  else if (wprec == MB_PREC_F32)
+    k_multi_axpy<double, float><<<g, kBlasThreads, 0, st>>>(n, (const double2*)V, ld, m, c, (float2*)w, partials);
+  else
+    k_multi_axpy<double, double><<<g, kBlasThreads, 0, st>>>(n, (const double2*)V, ld, m, c, (double2*)w, partials);
+  MB_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// Precision conversion and permutations.
+// ---------------------------------------------------------------------------
+template <typename TA, typename TB>
+__global__ void k_convert(int64_t n, const typename C2<TA>::type* __restrict__ a,
+                          typename C2<TB>::type* __restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const auto v = a[i];
+    typename C2<TB>::type o;
+    o.x = (TB)v.x;
+    o.y = (TB)v.y;
+    b[i] = o;
+  }
+}
+
+void launch_convert(int from_prec, int to_prec, int64_t n, const void* x, void* y,
+                    cudaStream_t st) {
+  const int g = blas_grid(n);
+  const bool f32a = from_prec == MB_PREC_F32, f32b = to_prec == MB_PREC_F32;
+  if (f32a == f32b) {
+    MB_CUDA(cudaMemcpyAsync(y, x, elem_bytes(from_prec) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    return;
+  }
+  if (f32a) k_convert<float, double><<<g, kBlasThreads, 0, st>>>(n, (const float2*)x, (double2*)y);
+  else k_convert<double, float><<<g, kBlasThreads, 0, st>>>(n, (const double2*)x, (float2*)y);
+  MB_CUDA(cudaGetLastError());
+}
+
+template <typename V2, bool SCATTER>
+__global__ void k_permute(int64_t n, const int32_t* __restrict__ perm, const V2* __restrict__ src,
+                          V2* __restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = perm[i];
+    if (SCATTER) dst[p] = src[i];
+    else dst[i] = src[p];
+  }
+}
+
+void launch_gather(int precision, int64_t n, const int32_t* perm, const void* src, void* dst,
+                   cudaStream_t st) {
+  const int g = blas_grid(n);
+  if (precision == MB_PREC_F32) k_permute<float2, false><<<g, kBlasThreads, 0, st>>>(n, perm, (const float2*)src, (float2*)dst);
+  else k_permute<double2, false><<<g, kBlasThreads, 0, st>>>(n, perm, (const double2*)src, (double2*)dst);
+  MB_CUDA(cudaGetLastError());
+}
+
+void launch_scatter(int precision, int64_t n, const int32_t* perm, const void* src, void* dst,
+                    cudaStream_t st) {
+  const int g = blas_grid(n);
+  if (precision == MB_PREC_F32) k_permute<float2, true><<<g, kBlasThreads, 0, st>>>(n, perm, (const float2*)src, (float2*)dst);
+  else k_permute<double2, true><<<g, kBlasThreads, 0, st>>>(n, perm, (const double2*)src, (double2*)dst);
+  MB_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror & Shaw, SC'11).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void philox10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t lo0 = 0xD2511F53u * c[0], hi0 = __umulhi(0xD2511F53u, c[0]);
+    const uint32_t lo1 = 0xCD9E8D57u * c[2], hi1 = __umulhi(0xCD9E8D57u, c[2]);
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = lo1;
+    c[2] = n2;
+    c[3] = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+// 52 random bits placed in [2,4), minus 3: uniform on [-1, 1), exact.
+__device__ __forceinline__ double u52_pm1(uint32_t hi, uint32_t lo) {
+  const uint64_t m = ((((uint64_t)hi) << 32) | lo) >> 12;
+  return __longlong_as_double((long long)(0x4000000000000000ull | m)) - 3.0;
+}
+
+template <typename V2>
+__global__ void k_fill_rng(int64_t n, uint64_t seed, uint32_t stream_id, int phase,
+                           V2* __restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t c[4] = {(uint32_t)i, (uint32_t)((uint64_t)i >> 32), stream_id, 0u};
+    philox10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    double re, im;
+    if (phase) {
+      const double u = (u52_pm1(c[0], c[1]) + 1.0) * 0.5;
+      sincospi(2.0 * u, &im, &re);
+    } else {
+      re = u52_pm1(c[0], c[1]);
+      im = u52_pm1(c[2], c[3]);
+    }
+    V2 o;
+    o.x = (decltype(o.x))re;
+    o.y = (decltype(o.y))im;
+    dst[i] = o;
+  }
+}
+
+void launch_fill_rng(int precision, int64_t Du, int64_t Dd, uint64_t seed, uint32_t stream_id,
+                     int phase, void* dst, cudaStream_t st) {
+  const int64_t n = Du * Dd;
+  const int g = blas_grid(n);
+  if (precision == MB_PREC_F32) k_fill_rng<float2><<<g, kBlasThreads, 0, st>>>(n, seed, stream_id, phase, (float2*)dst);
+  else k_fill_rng<double2><<<g, kBlasThreads, 0, st>>>(n, seed, stream_id, phase, (double2*)dst);
+  MB_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// Tensor index -> reference index, and the reference-order CSR export.
+// ---------------------------------------------------------------------------
+__constant__ Binom c_binom;
+
+void upload_binomials(cudaStream_t st) {
+  MB_CUDA(cudaMemcpyToSymbolAsync(c_binom, &binom_table(), sizeof(Binom), 0,
+                                  cudaMemcpyHostToDevice, st));
+}
+
+__global__ void k_perm(OpView v, int32_t* __restrict__ perm) {
+  __shared__ Binom sb;
+  for (int i = threadIdx.x; i < (int)(sizeof(Binom) / sizeof(int64_t)); i += blockDim.x)
+    (&sb.c[0][0])[i] = (&c_binom.c[0][0])[i];
+  __syncthreads();
+  const int64_t n = v.dim;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ru = i / v.Dd, rd = i - ru * v.Dd;
+    perm[i] = (int32_t)reference_rank(sb, v.up_mask[ru], v.dn_mask[rd], v.L);
+  }
+}
+
+void launch_perm(const OpView& v, int32_t* perm, cudaStream_t st) {
+  k_perm<<<blas_grid(v.dim), kBlasThreads, 0, st>>>(v, perm);
+  MB_CUDA(cudaGetLastError());
+}
+
+constexpr int kMaxRowNnz = 256;
+
+__device__ __forceinline__ double diag_value(const OpView& v, int64_t ru, int64_t rd) {
+  double d = v.u_fold[__popc(v.up_mask[ru] & v.dn_mask[rd])];
+  if (v.self_up) d += v.self_up[ru];
+  if (v.self_dn) d += v.self_dn[rd];
+  return d;
+}
+
+// Row of the reference-order CSR for tensor state i: hops from both spin
+// tables (value -t * weight), plus the diagonal unless |d| < 1000*eps (the
+// reference drops such coefficients, expression_base.h:79-97).
+__global__ void k_csr_count(OpView v, const int32_t* __restrict__ perm, int32_t* __restrict__ cnt) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < v.dim;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ru = i / v.Dd, rd = i - ru * v.Dd;
+    int c = (v.up_off[ru + 1] - v.up_off[ru]) + (v.dn_off[rd + 1] - v.dn_off[rd]);
+    const double d = diag_value(v, ru, rd);
+    if (!(d * d < kTol * kTol)) c += 1;
+    cnt[perm[i]] = c;
+  }
+}
+
+void launch_csr_count(const OpView& v, const int32_t* perm, int32_t* row_count, cudaStream_t st) {
+  k_csr_count<<<blas_grid(v.dim), kBlasThreads, 0, st>>>(v, perm, row_count);
+  MB_CUDA(cudaGetLastError());
+}
+
+__global__ void k_csr_fill(OpView v, const int32_t* __restrict__ perm, const int64_t* __restrict__ row_ptr,
+                           int64_t* __restrict__ col_idx, double* __restrict__ values,
+                           int* __restrict__ overflow) {
+  int64_t cols[kMaxRowNnz];
+  double vals[kMaxRowNnz];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < v.dim;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ru = i / v.Dd, rd = i - ru * v.Dd;
+    int m = 0;
+    const double d = diag_value(v, ru, rd);
+    if (!(d * d < kTol * kTol)) { cols[m] = perm[i]; vals[m] = d; ++m; }
+    for (int j = v.up_off[ru]; j < v.up_off[ru + 1]; ++j) {
+      const uint32_t e = v.up_ent[j];
+      if (m >= kMaxRowNnz) { atomicExch(overflow, 1); break; }
+      cols[m] = perm[(int64_t)(e >> 8) * v.Dd + rd];
+      vals[m] = -v.t * ((e & 2u) ? 2.0 : 1.0) * ((e & 1u) ? -1.0 : 1.0);
+      ++m;
+    }
+    for (int j = v.dn_off[rd]; j < v.dn_off[rd + 1]; ++j) {
+      const uint32_t e = v.dn_ent[j];
+      if (m >= kMaxRowNnz) { atomicExch(overflow, 1); break; }
+      cols[m] = perm[ru * v.Dd + (e >> 8)];
+      vals[m] = -v.t * ((e & 2u) ? 2.0 : 1.0) * ((e & 1u) ? -1.0 : 1.0);
+      ++m;
+    }
+    for (int a = 1; a < m; ++a) {
+      const int64_t kc = cols[a];
+      const double kv = vals[a];
+      int b = a - 1;
+      while (b >= 0 && cols[b] > kc) { cols[b + 1] = cols[b]; vals[b + 1] = vals[b]; --b; }
+      cols[b + 1] = kc;
+      vals[b + 1] = kv;
+    }
+    const int64_t base = row_ptr[perm[i]];
+    for (int a = 0; a < m; ++a) {
+      col_idx[base + a] = cols[a];
+      values[2 * (base + a)] = vals[a];
+      values[2 * (base + a) + 1] = 0.0;
+    }
+  }
+}
+
+void launch_csr_fill(const OpView& v, const int32_t* perm, const int64_t* row_ptr,
+                     int64_t* col_idx, double* values, cudaStream_t st) {
+  int* overflow = nullptr;
+  MB_CUDA(cudaMallocAsync(&overflow, sizeof(int), st));
+  MB_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), st));
+  k_csr_fill<<<blas_grid(v.dim), 128, 0, st>>>(v, perm, row_ptr, col_idx, values, overflow);
+  MB_CUDA(cudaGetLastError());
+  int h = 0;
+  MB_CUDA(cudaMemcpyAsync(&h, overflow, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MB_CUDA(cudaStreamSynchronize(st));
+  MB_CUDA(cudaFreeAsync(overflow, st));
+  MB_REQUIRE(!h, MB_ERR_CAPACITY, "a Hamiltonian row has more than 256 entries");
+}
+
+}  // namespace mb

@@ -1,0 +1,921 @@
+// Operator handle and the device-resident Krylov drivers behind the C ABI.
+//
+// Every solver keeps its vectors on the device in tensor order and in the
+// operator's precision; only alpha/beta scalars (and the small tridiagonal
+// problems) touch the host.  Reference-order arguments are permuted on the
+// device at entry and exit.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "mb_internal.h"
+
+namespace mb {
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t b) : bytes(b) {
+    if (b) MB_CUDA(cudaMalloc(&p, b));
+  }
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    std::swap(p, o.p);
+    std::swap(bytes, o.bytes);
+    return *this;
+  }
+};
+
+template <typename T>
+T* upload(mb_op_s* op, const std::vector<T>& h) {
+  if (h.empty()) return nullptr;
+  void* p = nullptr;
+  MB_CUDA(cudaMalloc(&p, sizeof(T) * h.size()));
+  op->allocations.push_back(p);
+  MB_CUDA(cudaMemcpy(p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+  return (T*)p;
+}
+
+int g_binom_uploaded_dev = -1;
+std::mutex g_binom_mu;
+
+void ensure_binomials() {
+  int dev = 0;
+  MB_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_binom_mu);
+  if (g_binom_uploaded_dev != dev) {
+    upload_binomials(0);
+    MB_CUDA(cudaStreamSynchronize(0));
+    g_binom_uploaded_dev = dev;
+  }
+}
+
+void require_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  MB_REQUIRE(e == cudaSuccess && n > 0, MB_ERR_NO_DEVICE, "no CUDA device available");
+}
+
+// Reduction helper: partials -> device result -> host (pinned) values.
+struct Reducer {
+  DevBuf partials, out;
+  double* host = nullptr;
+  int cap_blocks, cap_comp;
+  Reducer(int blocks, int comps) : partials(sizeof(double) * (size_t)blocks * comps),
+                                   out(sizeof(double) * (size_t)comps), cap_blocks(blocks),
+                                   cap_comp(comps) {
+    MB_CUDA(cudaMallocHost(&host, sizeof(double) * (size_t)comps));
+  }
+  ~Reducer() {
+    if (host) cudaFreeHost(host);
+  }
+  double* p() { return (double*)partials.p; }
+  // Reduce `nblocks` x `ncomp` partials and copy to host; waits on st.
+  const double* fetch(int nblocks, int ncomp, cudaStream_t st) {
+    launch_reduce(p(), nblocks, ncomp, (double*)out.p, st);
+    MB_CUDA(cudaMemcpyAsync(host, out.p, sizeof(double) * ncomp, cudaMemcpyDeviceToHost, st));
+    MB_CUDA(cudaStreamSynchronize(st));
+    return host;
+  }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Operator construction.
+// ---------------------------------------------------------------------------
+static void build_op(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m) {
+  MB_CUDA(cudaGetDevice(&op->device));
+  op->L = b->L;
+  op->n_up = b->n_up;
+  op->n_down = b->n_down;
+  op->Du = b->up.D;
+  op->Dd = b->down.D;
+  op->dim = b->dim;
+  op->t = m->t;
+  op->u = m->u;
+  const HopTable tu = build_hop_table(b->up, *m);
+  const bool same = b->n_up == b->n_down;
+  HopTable td_store;
+  if (!same) td_store = build_hop_table(b->down, *m);
+  const HopTable& td = same ? tu : td_store;
+  OpView& v = op->view;
+  v.Du = op->Du;
+  v.Dd = op->Dd;
+  v.dim = op->dim;
+  v.L = op->L;
+  v.t = m->t;
+  v.up_mask = upload(op, b->up.masks);
+  v.up_off = upload(op, tu.off);
+  v.up_ent = upload(op, tu.ent.empty() ? std::vector<uint32_t>{0u} : tu.ent);
+  if (same) {
+    v.dn_mask = v.up_mask;
+    v.dn_off = v.up_off;
+    v.dn_ent = v.up_ent;
+  } else {
+    v.dn_mask = upload(op, b->down.masks);
+    v.dn_off = upload(op, td.off);
+    v.dn_ent = upload(op, td.ent.empty() ? std::vector<uint32_t>{0u} : td.ent);
+  }
+  v.max_up_degree = tu.max_degree;
+  v.max_dn_degree = td.max_degree;
+  const std::vector<double> uf = u_fold_table(m->u, m->has_u, op->L);
+  v.u_fold = upload(op, uf);
+  v.u_fold_f = upload(op, std::vector<float>(uf.begin(), uf.end()));
+  if (tu.has_self) {
+    v.self_up = upload(op, tu.self_energy);
+    v.self_up_f = upload(op, std::vector<float>(tu.self_energy.begin(), tu.self_energy.end()));
+  }
+  if (td.has_self) {
+    if (same) {
+      v.self_dn = v.self_up;
+      v.self_dn_f = v.self_up_f;
+    } else {
+      v.self_dn = upload(op, td.self_energy);
+      v.self_dn_f = upload(op, std::vector<float>(td.self_energy.begin(), td.self_energy.end()));
+    }
+  }
+  ensure_binomials();
+}
+
+static mb_op_s::Scratch& scratch_for(mb_op_s* op, cudaStream_t st, int nvec) {
+  std::lock_guard<std::mutex> lk(op->mu);
+  auto& s = op->scratch[st];
+  const size_t vb = elem_bytes(op->precision) * (size_t)op->dim;
+  if (nvec >= 1 && !s.a) {
+    MB_CUDA(cudaMalloc(&s.a, vb));
+  }
+  if (nvec >= 2 && !s.b) {
+    MB_CUDA(cudaMalloc(&s.b, vb));
+  }
+  if (nvec >= 4 && !s.hx) {
+    MB_CUDA(cudaMalloc(&s.hx, vb));
+    MB_CUDA(cudaMalloc(&s.hy, vb));
+  }
+  return s;
+}
+
+static void ensure_perm(mb_op_s* op) {
+  std::lock_guard<std::mutex> lk(op->mu);
+  if (op->perm) return;
+  void* p = nullptr;
+  MB_CUDA(cudaMalloc(&p, sizeof(int32_t) * (size_t)op->dim));
+  op->allocations.push_back(p);
+  launch_perm(op->view, (int32_t*)p, 0);
+  MB_CUDA(cudaStreamSynchronize(0));
+  op->perm = (int32_t*)p;
+}
+
+static void to_tensor(mb_op_s* op, const void* src, void* dst, int order, cudaStream_t st) {
+  if (order == MB_ORDER_TENSOR) {
+    if (src != dst)
+      MB_CUDA(cudaMemcpyAsync(dst, src, elem_bytes(op->precision) * (size_t)op->dim,
+                              cudaMemcpyDeviceToDevice, st));
+    return;
+  }
+  ensure_perm(op);
+  launch_gather(op->precision, op->dim, op->perm, src, dst, st);
+}
+
+static void from_tensor(mb_op_s* op, const void* src, void* dst, int order, cudaStream_t st) {
+  if (order == MB_ORDER_TENSOR) {
+    if (src != dst)
+      MB_CUDA(cudaMemcpyAsync(dst, src, elem_bytes(op->precision) * (size_t)op->dim,
+                              cudaMemcpyDeviceToDevice, st));
+    return;
+  }
+  ensure_perm(op);
+  launch_scatter(op->precision, op->dim, op->perm, src, dst, st);
+}
+
+static void check_order(int order) {
+  MB_REQUIRE(order == MB_ORDER_REFERENCE || order == MB_ORDER_TENSOR, MB_ERR_INVALID_ARG,
+             "order must be MB_ORDER_REFERENCE or MB_ORDER_TENSOR");
+}
+
+// y = scale*(H - shift) x + beta z in `order`.
+static void apply_affine(mb_op_s* op, const void* x, void* y, double scale, double shift,
+                         double beta, const void* z, int order, cudaStream_t st) {
+  check_order(order);
+  MB_REQUIRE(x && y, MB_ERR_INVALID_ARG, "NULL vector");
+  MB_REQUIRE(x != y, MB_ERR_INVALID_ARG, "x and y must not overlap");
+  if (beta != 0.0) MB_REQUIRE(z, MB_ERR_INVALID_ARG, "z is NULL with beta != 0");
+  if (order == MB_ORDER_TENSOR) {
+    launch_apply(op->view, op->precision, x, y, scale, shift, beta, beta != 0.0 ? z : nullptr,
+                 nullptr, 0, st);
+    return;
+  }
+  auto& s = scratch_for(op, st, 2);
+  to_tensor(op, x, s.a, order, st);
+  const void* zt = nullptr;
+  if (beta != 0.0) {
+    // z gathered into y's slot would clobber z when z == y; use b then swap roles.
+    to_tensor(op, z, s.b, order, st);
+    zt = s.b;
+  }
+  // In-place on s.b when z is used: each element reads z[i] before writing y[i].
+  launch_apply(op->view, op->precision, s.a, s.b, scale, shift, beta, zt, nullptr, 0, st);
+  from_tensor(op, s.b, y, order, st);
+}
+
+// ---------------------------------------------------------------------------
+// Lanczos (src/numerics/lanczos.h) on scale*H, device-resident.
+// ---------------------------------------------------------------------------
+struct Krylov {
+  mb_op_s* op;
+  cudaStream_t st;
+  int64_t n;
+  int prec;
+  size_t vb;
+  DevBuf v_prev, v_curr, w, basis, coef;
+  int basis_prec = MB_PREC_F64;
+  int64_t basis_cap = 0;
+  Reducer red;
+  int grid_apply, grid_blas;
+
+  Krylov(mb_op_s* o, cudaStream_t s)
+      : op(o), st(s), n(o->dim), prec(o->precision), vb(elem_bytes(o->precision) * (size_t)o->dim),
+        v_prev(vb), v_curr(vb), w(vb),
+        red(std::max(std::max(apply_grid(o->view, o->precision), blas_grid(o->dim)), 1024) , 2 * 1024 + 8),
+        grid_apply(apply_grid(o->view, o->precision)), grid_blas(blas_grid(o->dim)) {}
+
+  double norm_of(const void* x) {
+    launch_dot(prec, n, x, x, red.p(), st);
+    const double* h = red.fetch(grid_blas, 3, st);
+    return std::sqrt(h[2]);
+  }
+
+  void reserve_basis(int64_t k, int want_prec) {
+    size_t free_b = 0, total_b = 0;
+    MB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    int p = want_prec;
+    const size_t need64 = (size_t)k * 16 * (size_t)n, need32 = (size_t)k * 8 * (size_t)n;
+    if (p < 0) p = (need64 + (size_t)(1u << 30) < free_b) ? MB_PREC_F64 : MB_PREC_F32;
+    if (prec == MB_PREC_F32) p = MB_PREC_F32;
+    const size_t need = p == MB_PREC_F64 ? need64 : need32;
+    MB_REQUIRE(need + (size_t)(256u << 20) < free_b, MB_ERR_OOM,
+               "Krylov basis for full re-orthogonalisation does not fit in device memory");
+    basis = DevBuf(need);
+    basis_prec = p;
+    basis_cap = k;
+    coef = DevBuf(sizeof(double) * 2 * (size_t)std::max<int64_t>(k, 1));
+  }
+
+  void* basis_col(int64_t j) {
+    return (char*)basis.p + elem_bytes(basis_prec) * (size_t)n * (size_t)j;
+  }
+
+  // CGS2: two passes of w -= V (V^H w); returns ||w||^2 after the last pass.
+  double reorth(int m) {
+    double nrm2 = 0.0;
+    for (int pass = 0; pass < 2; ++pass) {
+      launch_multi_dot(basis_prec, prec, n, basis.p, n, m, w.p, red.p(), st);
+      launch_reduce(red.p(), multi_dot_grid(n), 2 * m, (double*)coef.p, st);
+      launch_multi_axpy(basis_prec, prec, n, basis.p, n, m, (const double*)coef.p, w.p, red.p(),
+                        st);
+      nrm2 = red.fetch(grid_blas, 3, st)[1];
+    }
+    return nrm2;
+  }
+
+  // Pass one from b (tensor order, op precision).  Returns steps taken.
+  int64_t pass_one(const void* b, int64_t k, double scale, std::vector<double>& alphas,
+                   std::vector<double>& betas, double& b_norm, bool reorth, double conv_tol,
+                   int check_every, std::vector<double>* ritz_trace = nullptr) {
+    b_norm = norm_of(b);
+    MB_REQUIRE(b_norm > kTol, MB_ERR_ZERO_NORM, "Input vector has zero norm");
+    alphas.clear();
+    betas.clear();
+    if (k == 0) return 0;
+    // v_curr = b / ||b||, v_prev = 0
+    launch_axpby(prec, n, 1.0 / b_norm, 0.0, b, 0.0, 0.0, v_curr.p, nullptr, 0, st);
+    MB_CUDA(cudaMemsetAsync(v_prev.p, 0, vb, st));
+    double beta_prev = 0.0;
+    int64_t steps = 0;
+    double last_ritz = 0.0;
+    bool have_ritz = false;
+    for (int64_t it = 0; it < k; ++it) {
+      if (reorth) launch_convert(prec, basis_prec, n, v_curr.p, basis_col(it), st);
+      // w = scale*H v - beta_prev v_prev ; alpha = Re<v, w>   (lanczos.h:25-33)
+      launch_apply(op->view, prec, v_curr.p, w.p, scale, 0.0, -beta_prev,
+                   beta_prev != 0.0 ? v_prev.p : nullptr, red.p(), 1, st);
+      const double alpha = red.fetch(grid_apply, 3, st)[0];
+      // w -= alpha v ; beta = ||w||                             (lanczos.h:34-36)
+      launch_axpby(prec, n, -alpha, 0.0, v_curr.p, 1.0, 0.0, w.p, red.p(), 1, st);
+      double nrm2 = red.fetch(grid_blas, 3, st)[1];
+      if (reorth) nrm2 = this->reorth((int)(it + 1));
+      const double beta = std::sqrt(nrm2);
+      alphas.push_back(alpha);
+      steps += 1;
+      if (beta <= kTol) break;
+      if (it + 1 < k) betas.push_back(beta);
+      // v_prev <- v, v <- w / beta                               (lanczos.h:113-121)
+      std::swap(v_prev.p, v_curr.p);
+      std::swap(v_curr.p, w.p);
+      launch_axpby(prec, n, 0.0, 0.0, nullptr, 1.0 / beta, 0.0, v_curr.p, nullptr, 0, st);
+      beta_prev = beta;
+      if (conv_tol > 0.0 && check_every > 0 && (steps % check_every) == 0 && it + 1 < k) {
+        std::vector<double> d(alphas), e(betas);
+        e.resize(d.size() > 0 ? d.size() - 1 : 0);
+        if (tridiag_eig((int)d.size(), d, e, nullptr)) {
+          const double ritz = d.back();
+          if (ritz_trace) ritz_trace->push_back(ritz);
+          if (have_ritz && std::fabs(ritz - last_ritz) <= conv_tol * std::fabs(ritz)) {
+            betas.resize(steps > 0 ? steps - 1 : 0);
+            break;
+          }
+          last_ritz = ritz;
+          have_ritz = true;
+        }
+      }
+    }
+    if ((int64_t)betas.size() > std::max<int64_t>(steps - 1, 0)) betas.resize(steps - 1);
+    return steps;
+  }
+
+  // Pass two (lanczos.h:177-218): x = sum_j y_j v_j by re-running the
+  // recurrence; y complex.  x in tensor order, op precision.
+  void pass_two(const void* b, int64_t steps, double scale, const std::vector<double>& alphas,
+                const std::vector<double>& betas, double b_norm,
+                const std::vector<std::complex<double>>& y, void* x) {
+    MB_REQUIRE(b_norm > kTol, MB_ERR_ZERO_NORM, "Input vector has zero norm");
+    MB_REQUIRE((int64_t)y.size() == steps, MB_ERR_DIM_MISMATCH,
+               "Dimension mismatch: y_k size must match decomposition steps");
+    if (steps == 0) {
+      MB_CUDA(cudaMemsetAsync(x, 0, vb, st));
+      return;
+    }
+    launch_axpby(prec, n, 1.0 / b_norm, 0.0, b, 0.0, 0.0, v_curr.p, nullptr, 0, st);
+    MB_CUDA(cudaMemsetAsync(v_prev.p, 0, vb, st));
+    launch_axpby(prec, n, y[0].real(), y[0].imag(), v_curr.p, 0.0, 0.0, x, nullptr, 0, st);
+    for (int64_t j = 0; j + 1 < steps; ++j) {
+      const double alpha_j = alphas[(size_t)j], beta_j = betas[(size_t)j];
+      const double beta_prev = j == 0 ? 0.0 : betas[(size_t)j - 1];
+      launch_apply(op->view, prec, v_curr.p, w.p, scale, 0.0, -beta_prev,
+                   beta_prev != 0.0 ? v_prev.p : nullptr, nullptr, 0, st);
+      // w = (w - alpha v) / beta
+      launch_axpby(prec, n, -alpha_j / beta_j, 0.0, v_curr.p, 1.0 / beta_j, 0.0, w.p, nullptr, 0,
+                   st);
+      launch_axpby(prec, n, y[(size_t)j + 1].real(), y[(size_t)j + 1].imag(), w.p, 1.0, 0.0, x,
+                   nullptr, 0, st);
+      std::swap(v_prev.p, v_curr.p);
+      std::swap(v_curr.p, w.p);
+    }
+  }
+
+  // x = sum_j y_j V_j from the stored basis (full re-orthogonalisation runs).
+  void combine_basis(int64_t steps, const std::vector<std::complex<double>>& y, void* x) {
+    std::vector<double> c(2 * (size_t)steps);
+    for (int64_t j = 0; j < steps; ++j) {
+      c[2 * (size_t)j] = -y[(size_t)j].real();
+      c[2 * (size_t)j + 1] = -y[(size_t)j].imag();
+    }
+    MB_CUDA(cudaMemcpyAsync(coef.p, c.data(), sizeof(double) * c.size(), cudaMemcpyHostToDevice, st));
+    MB_CUDA(cudaMemsetAsync(x, 0, vb, st));
+    launch_multi_axpy(basis_prec, prec, n, basis.p, n, (int)steps, (const double*)coef.p, x,
+                      red.p(), st);
+    MB_CUDA(cudaStreamSynchronize(st));
+  }
+};
+
+static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
+                      const mb_lanczos_opts* opts, double sign, double* e_out, void* vec,
+                      int64_t* steps_out) {
+  check_order(order);
+  MB_REQUIRE(seed && e_out, MB_ERR_INVALID_ARG, "NULL argument");
+  MB_REQUIRE(k >= 0, MB_ERR_INVALID_ARG, "k must be >= 0");
+  mb_lanczos_opts o{};
+  o.basis_precision = -1;
+  o.check_every = 10;
+  if (opts) o = *opts;
+  if (o.check_every <= 0) o.check_every = 10;
+  cudaStream_t st = 0;
+  Krylov kr(op, st);
+  DevBuf bt(kr.vb);
+  to_tensor(op, seed, bt.p, order, st);
+  const bool reorth = o.reorth != 0 && k > 0;
+  if (reorth) kr.reserve_basis(k, o.basis_precision);
+  std::vector<double> alphas, betas;
+  double b_norm = 0.0;
+  // find_min_eigenpair runs find_max_eigenpair on Negated<Op> (lanczos.h:283-290).
+  const int64_t m = kr.pass_one(bt.p, k, sign, alphas, betas, b_norm, reorth, o.conv_tol,
+                                o.check_every);
+  if (steps_out) *steps_out = m;
+  if (m == 0) {
+    *e_out = 0.0;
+    if (vec) MB_CUDA(cudaMemsetAsync(vec, 0, kr.vb, st));
+    MB_CUDA(cudaStreamSynchronize(st));
+    return;
+  }
+  std::vector<double> d(alphas), z;
+  std::vector<double> e(betas);
+  e.resize((size_t)m - 1);
+  MB_REQUIRE(tridiag_eig((int)m, d, e, &z), MB_ERR_EIG_FAILED,
+             "Eigenvalue decomposition of T_k failed");
+  *e_out = sign * d[(size_t)m - 1];
+  if (vec) {
+    std::vector<std::complex<double>> y((size_t)m);
+    for (int64_t i = 0; i < m; ++i) y[(size_t)i] = z[(size_t)(m - 1) * m + i] * b_norm;
+    DevBuf xt(kr.vb);
+    if (reorth) {
+      kr.combine_basis(m, y, xt.p);
+    } else {
+      kr.pass_two(bt.p, m, sign, alphas, betas, b_norm, y, xt.p);
+    }
+    from_tensor(op, xt.p, vec, order, st);
+  }
+  MB_CUDA(cudaStreamSynchronize(st));
+}
+
+// Krylov expmv (evolve_state.h:120-151).
+static void evolve(mb_op_s* op, const void* psi0, int order, double t, int64_t krylov_steps,
+                   int imaginary, void* out) {
+  check_order(order);
+  MB_REQUIRE(psi0 && out, MB_ERR_INVALID_ARG, "NULL vector");
+  cudaStream_t st = 0;
+  Krylov kr(op, st);
+  DevBuf bt(kr.vb);
+  to_tensor(op, psi0, bt.p, order, st);
+  const double psi_norm = kr.norm_of(bt.p);
+  if (psi_norm <= kTol) {  // evolve_state returns psi0 unchanged (:130-133)
+    if (out != psi0) MB_CUDA(cudaMemcpyAsync(out, psi0, kr.vb, cudaMemcpyDeviceToDevice, st));
+    MB_CUDA(cudaStreamSynchronize(st));
+    return;
+  }
+  int64_t k = krylov_steps <= 0 ? 30 : krylov_steps;
+  if (k > op->dim) k = op->dim;
+  std::vector<double> alphas, betas;
+  double b_norm = 0.0;
+  const int64_t m = kr.pass_one(bt.p, k, 1.0, alphas, betas, b_norm, false, 0.0, 0);
+  // expm_tridiagonal_first_column_{unitary,imaginary} (evolve_state.h:22-106)
+  std::vector<double> d(alphas), z, e(betas);
+  e.resize((size_t)std::max<int64_t>(m - 1, 0));
+  MB_REQUIRE(tridiag_eig((int)m, d, e, &z), MB_ERR_EIG_FAILED,
+             "Eigenvalue decomposition of T_k failed");
+  std::vector<std::complex<double>> y((size_t)m);
+  for (int64_t i = 0; i < m; ++i) {
+    std::complex<double> s = 0.0;
+    for (int64_t j = 0; j < m; ++j) {
+      const double wj = z[(size_t)j * m + 0];
+      const std::complex<double> ex =
+          imaginary ? std::complex<double>(std::exp(-t * d[(size_t)j]), 0.0)
+                    : std::exp(std::complex<double>(0.0, -t * d[(size_t)j]));
+      s += z[(size_t)j * m + i] * ex * wj;
+    }
+    y[(size_t)i] = s * b_norm;  // solve() scales y by ||b|| (lanczos.h:231-233)
+  }
+  DevBuf xt(kr.vb);
+  kr.pass_two(bt.p, m, 1.0, alphas, betas, b_norm, y, xt.p);
+  from_tensor(op, xt.p, out, order, st);
+  MB_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace mb
+
+using namespace mb;
+
+extern "C" {
+
+int mb_device_count(int* count) {
+  if (!count) return MB_ERR_INVALID_ARG;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) n = 0;
+  *count = n;
+  return MB_OK;
+}
+
+int mb_alloc(void** dev_ptr, size_t bytes) {
+  return guard([&] {
+    MB_REQUIRE(dev_ptr, MB_ERR_INVALID_ARG, "NULL argument");
+    require_device();
+    MB_CUDA(cudaMalloc(dev_ptr, bytes));
+  });
+}
+
+int mb_free(void* dev_ptr) {
+  return guard([&] { MB_CUDA(cudaFree(dev_ptr)); });
+}
+
+int mb_memcpy(void* dst, const void* src, size_t bytes, int kind) {
+  return guard([&] {
+    MB_REQUIRE(kind >= 0 && kind <= 2, MB_ERR_INVALID_ARG, "kind must be 0, 1 or 2");
+    const cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice
+                             : kind == 1 ? cudaMemcpyDeviceToHost
+                                         : cudaMemcpyDeviceToDevice;
+    MB_CUDA(cudaMemcpy(dst, src, bytes, k));
+  });
+}
+
+int mb_synchronize(void) {
+  return guard([&] { MB_CUDA(cudaDeviceSynchronize()); });
+}
+
+int mb_op_create(mb_basis_t basis, mb_model_t model, int precision, mb_op_t* out) {
+  return guard([&] {
+    MB_REQUIRE(basis && model && out, MB_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    MB_REQUIRE(precision == MB_PREC_F64 || precision == MB_PREC_F32, MB_ERR_INVALID_ARG,
+               "precision must be MB_PREC_F64 or MB_PREC_F32");
+    MB_REQUIRE(model->L == basis->L, MB_ERR_DIM_MISMATCH,
+               "model sites and basis orbitals differ");
+    require_device();
+    auto op = std::make_unique<mb_op_s>();
+    op->precision = precision;
+    try {
+      build_op(op.get(), basis, model);
+    } catch (...) {
+      for (void* p : op->allocations) cudaFree(p);
+      throw;
+    }
+    *out = op.release();
+  });
+}
+
+int mb_op_destroy(mb_op_t op) {
+  if (!op) return MB_OK;
+  cudaSetDevice(op->device);
+  cudaDeviceSynchronize();
+  for (auto& kv : op->scratch) {
+    for (void* p : {kv.second.a, kv.second.b, kv.second.hx, kv.second.hy})
+      if (p) cudaFree(p);
+  }
+  for (void* p : op->allocations) cudaFree(p);
+  delete op;
+  return MB_OK;
+}
+
+int mb_op_dimension(mb_op_t op, int64_t* dim) {
+  return guard([&] {
+    MB_REQUIRE(op && dim, MB_ERR_INVALID_ARG, "NULL argument");
+    *dim = op->dim;
+  });
+}
+
+int mb_op_precision(mb_op_t op, int* precision) {
+  return guard([&] {
+    MB_REQUIRE(op && precision, MB_ERR_INVALID_ARG, "NULL argument");
+    *precision = op->precision;
+  });
+}
+
+int mb_op_apply(mb_op_t op, const void* x_dev, void* y_dev, int order, void* stream) {
+  return guard([&] {
+    MB_REQUIRE(op, MB_ERR_INVALID_ARG, "NULL operator");
+    apply_affine(op, x_dev, y_dev, 1.0, 0.0, 0.0, nullptr, order, (cudaStream_t)stream);
+  });
+}
+
+int mb_op_apply_affine(mb_op_t op, const void* x_dev, void* y_dev, double scale, double shift,
+                       double beta, const void* z_dev, int order, void* stream) {
+  return guard([&] {
+    MB_REQUIRE(op, MB_ERR_INVALID_ARG, "NULL operator");
+    apply_affine(op, x_dev, y_dev, scale, shift, beta, z_dev, order, (cudaStream_t)stream);
+  });
+}
+
+int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
+  return guard([&] {
+    MB_REQUIRE(op && x_host && y_host, MB_ERR_INVALID_ARG, "NULL argument");
+    check_order(order);
+    const size_t vb = elem_bytes(op->precision) * (size_t)op->dim;
+    cudaStream_t st = 0;
+    auto& s = scratch_for(op, st, 4);
+    MB_CUDA(cudaMemcpyAsync(s.hx, x_host, vb, cudaMemcpyHostToDevice, st));
+    if (order == MB_ORDER_TENSOR) {
+      launch_apply(op->view, op->precision, s.hx, s.hy, 1.0, 0.0, 0.0, nullptr, nullptr, 0, st);
+    } else {
+      to_tensor(op, s.hx, s.a, order, st);
+      launch_apply(op->view, op->precision, s.a, s.b, 1.0, 0.0, 0.0, nullptr, nullptr, 0, st);
+      from_tensor(op, s.b, s.hy, order, st);
+    }
+    MB_CUDA(cudaMemcpyAsync(y_host, s.hy, vb, cudaMemcpyDeviceToHost, st));
+    MB_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+int mb_fill_uniform(mb_op_t op, uint64_t seed, uint32_t stream_id, void* v_dev, int order,
+                    void* stream) {
+  return guard([&] {
+    MB_REQUIRE(op && v_dev, MB_ERR_INVALID_ARG, "NULL argument");
+    check_order(order);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (order == MB_ORDER_TENSOR) {
+      launch_fill_rng(op->precision, op->Du, op->Dd, seed, stream_id, 0, v_dev, st);
+    } else {
+      auto& s = scratch_for(op, st, 1);
+      launch_fill_rng(op->precision, op->Du, op->Dd, seed, stream_id, 0, s.a, st);
+      from_tensor(op, s.a, v_dev, order, st);
+    }
+  });
+}
+
+int mb_fill_phase(mb_op_t op, uint64_t seed, uint32_t stream_id, void* v_dev, int order,
+                  void* stream) {
+  return guard([&] {
+    MB_REQUIRE(op && v_dev, MB_ERR_INVALID_ARG, "NULL argument");
+    check_order(order);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (order == MB_ORDER_TENSOR) {
+      launch_fill_rng(op->precision, op->Du, op->Dd, seed, stream_id, 1, v_dev, st);
+    } else {
+      auto& s = scratch_for(op, st, 1);
+      launch_fill_rng(op->precision, op->Du, op->Dd, seed, stream_id, 1, s.a, st);
+      from_tensor(op, s.a, v_dev, order, st);
+    }
+  });
+}
+
+int mb_compute_matrix_elements_csr(mb_basis_t basis, mb_model_t model, int64_t* nnz,
+                                   int64_t* row_ptr, int64_t* col_idx, double* values) {
+  return guard([&] {
+    MB_REQUIRE(basis && model && nnz, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(model->L == basis->L, MB_ERR_DIM_MISMATCH, "model sites and basis orbitals differ");
+    require_device();
+    mb_op_s tmp;
+    tmp.precision = MB_PREC_F64;
+    struct Cleanup {
+      mb_op_s& o;
+      ~Cleanup() {
+        for (void* p : o.allocations) cudaFree(p);
+      }
+    } cleanup{tmp};
+    build_op(&tmp, basis, model);
+    ensure_perm(&tmp);
+    const int64_t dim = tmp.dim;
+    cudaStream_t st = 0;
+    DevBuf cnt(sizeof(int32_t) * (size_t)dim);
+    launch_csr_count(tmp.view, tmp.perm, (int32_t*)cnt.p, st);
+    std::vector<int32_t> hc((size_t)dim);
+    MB_CUDA(cudaMemcpy(hc.data(), cnt.p, sizeof(int32_t) * (size_t)dim, cudaMemcpyDeviceToHost));
+    std::vector<int64_t> rp((size_t)dim + 1, 0);
+    for (int64_t i = 0; i < dim; ++i) rp[(size_t)i + 1] = rp[(size_t)i] + hc[(size_t)i];
+    const int64_t total = rp[(size_t)dim];
+    if (!col_idx) {
+      *nnz = total;
+      if (row_ptr) std::memcpy(row_ptr, rp.data(), sizeof(int64_t) * rp.size());
+      return;
+    }
+    MB_REQUIRE(*nnz >= total, MB_ERR_CAPACITY, "nnz capacity smaller than the matrix");
+    MB_REQUIRE(row_ptr && values, MB_ERR_INVALID_ARG, "NULL row_ptr or values");
+    DevBuf drp(sizeof(int64_t) * rp.size()), dci(sizeof(int64_t) * (size_t)std::max<int64_t>(total, 1)),
+        dv(sizeof(double) * 2 * (size_t)std::max<int64_t>(total, 1));
+    MB_CUDA(cudaMemcpy(drp.p, rp.data(), sizeof(int64_t) * rp.size(), cudaMemcpyHostToDevice));
+    launch_csr_fill(tmp.view, tmp.perm, (const int64_t*)drp.p, (int64_t*)dci.p, (double*)dv.p, st);
+    std::memcpy(row_ptr, rp.data(), sizeof(int64_t) * rp.size());
+    MB_CUDA(cudaMemcpy(col_idx, dci.p, sizeof(int64_t) * (size_t)total, cudaMemcpyDeviceToHost));
+    MB_CUDA(cudaMemcpy(values, dv.p, sizeof(double) * 2 * (size_t)total, cudaMemcpyDeviceToHost));
+    *nnz = total;
+  });
+}
+
+int mb_lanczos_pass_one(mb_op_t op, const void* b_dev, int order, int64_t k, double scale,
+                        double* alphas, double* betas, int64_t* steps, double* b_norm) {
+  return guard([&] {
+    MB_REQUIRE(op && b_dev && alphas && steps && b_norm, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(k >= 0, MB_ERR_INVALID_ARG, "k must be >= 0");
+    check_order(order);
+    cudaStream_t st = 0;
+    Krylov kr(op, st);
+    DevBuf bt(kr.vb);
+    to_tensor(op, b_dev, bt.p, order, st);
+    std::vector<double> a, b;
+    const int64_t m = kr.pass_one(bt.p, k, scale, a, b, *b_norm, false, 0.0, 0);
+    std::copy(a.begin(), a.end(), alphas);
+    if (betas) std::copy(b.begin(), b.end(), betas);
+    *steps = m;
+  });
+}
+
+int mb_lanczos_pass_two(mb_op_t op, const void* b_dev, int order, double scale,
+                        const double* alphas, const double* betas, int64_t steps, double b_norm,
+                        const double* y, void* x_dev) {
+  return guard([&] {
+    MB_REQUIRE(op && b_dev && x_dev, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(steps == 0 || (alphas && y), MB_ERR_INVALID_ARG, "NULL coefficients");
+    MB_REQUIRE(steps <= 1 || betas, MB_ERR_INVALID_ARG, "NULL betas");
+    check_order(order);
+    cudaStream_t st = 0;
+    Krylov kr(op, st);
+    DevBuf bt(kr.vb), xt(kr.vb);
+    to_tensor(op, b_dev, bt.p, order, st);
+    std::vector<double> a(alphas, alphas + steps), b;
+    if (steps > 1) b.assign(betas, betas + steps - 1);
+    std::vector<std::complex<double>> yy((size_t)steps);
+    for (int64_t i = 0; i < steps; ++i) yy[(size_t)i] = {y[2 * i], y[2 * i + 1]};
+    kr.pass_two(bt.p, steps, scale, a, b, b_norm, yy, xt.p);
+    from_tensor(op, xt.p, x_dev, order, st);
+    MB_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+int mb_find_min_eigenpair(mb_op_t op, int64_t k, const void* seed_dev, int order,
+                          const mb_lanczos_opts* opts, double* e0, void* vec_dev,
+                          int64_t* steps_out) {
+  return guard([&] {
+    MB_REQUIRE(op, MB_ERR_INVALID_ARG, "NULL operator");
+    eigenpair(op, k, seed_dev, order, opts, -1.0, e0, vec_dev, steps_out);
+  });
+}
+
+int mb_find_max_eigenpair(mb_op_t op, int64_t k, const void* seed_dev, int order,
+                          const mb_lanczos_opts* opts, double* e_max, void* vec_dev,
+                          int64_t* steps_out) {
+  return guard([&] {
+    MB_REQUIRE(op, MB_ERR_INVALID_ARG, "NULL operator");
+    eigenpair(op, k, seed_dev, order, opts, 1.0, e_max, vec_dev, steps_out);
+  });
+}
+
+int mb_time_evolve(mb_op_t op, const void* psi0_dev, int order, double t, int64_t krylov_steps,
+                   int imaginary, void* out_dev) {
+  return guard([&] {
+    MB_REQUIRE(op, MB_ERR_INVALID_ARG, "NULL operator");
+    evolve(op, psi0_dev, order, t, krylov_steps, imaginary, out_dev);
+  });
+}
+
+int mb_time_evolve_steps(mb_op_t op, void* psi_dev, int order, double t0, double t1, double dt,
+                         int64_t krylov_steps) {
+  return guard([&] {
+    MB_REQUIRE(op && psi_dev, MB_ERR_INVALID_ARG, "NULL argument");
+    if (dt == 0.0 || (t1 - t0) == 0.0) return;
+    const double direction = (t1 >= t0) ? 1.0 : -1.0;
+    dt = std::fabs(dt) * direction;
+    double t = t0;
+    DevBuf tmp(elem_bytes(op->precision) * (size_t)op->dim);
+    while ((direction > 0 && t < t1) || (direction < 0 && t > t1)) {
+      const double step = direction > 0 ? std::min(dt, t1 - t) : std::max(dt, t1 - t);
+      evolve(op, psi_dev, order, step, krylov_steps, 0, tmp.p);
+      MB_CUDA(cudaMemcpy(psi_dev, tmp.p, tmp.bytes, cudaMemcpyDeviceToDevice));
+      t += step;
+    }
+  });
+}
+
+int mb_kpm_dos_moments(mb_op_t op, int64_t n_moments, int64_t n_probes, uint64_t seed,
+                       double e_min, double e_max, double padding, double* mu) {
+  return guard([&] {
+    MB_REQUIRE(op && mu, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(n_moments >= 1 && n_probes >= 1, MB_ERR_INVALID_ARG,
+               "need at least one moment and one probe");
+    MB_REQUIRE(e_max > e_min, MB_ERR_INVALID_ARG, "e_max must exceed e_min");
+    const double a = (e_max - e_min) / 2.0 * (1.0 + padding);  // rescaling.h:33-38
+    const double b = (e_max + e_min) / 2.0;
+    cudaStream_t st = 0;
+    const size_t vb = elem_bytes(op->precision) * (size_t)op->dim;
+    DevBuf t0(vb), t1(vb);
+    const int ga = apply_grid(op->view, op->precision), gb = blas_grid(op->dim);
+    Reducer red(std::max(ga, gb), 3);
+    // Device-side moment sums per step, read once per probe.  Step s produces
+    // T_{s+1}; moments up to n_moments-1 need T_j for j <= n_moments/2.
+    const int64_t nsteps = std::max<int64_t>(n_moments / 2, 1);
+    DevBuf dots(sizeof(double) * 3 * (size_t)nsteps);
+    std::vector<double> acc((size_t)n_moments, 0.0), hd(3 * (size_t)nsteps);
+    for (int64_t p = 0; p < n_probes; ++p) {
+      void* cur = t0.p;   // T_n
+      void* oth = t1.p;   // T_{n-1}, then T_{n+1}
+      launch_fill_rng(op->precision, op->Du, op->Dd, seed, (uint32_t)(1 + p), 1, cur, st);
+      // step 0: T1 = Ht T0 into oth; dots <T0,T1>, <T1,T1>, <T0,T0>
+      launch_apply(op->view, op->precision, cur, oth, 1.0 / a, b, 0.0, nullptr, red.p(), 7, st);
+      launch_reduce(red.p(), ga, 3, (double*)dots.p, st);
+      std::swap(cur, oth);  // cur = T1, oth = T0
+      for (int64_t s = 1; s < nsteps; ++s) {
+        // T_{s+1} = 2 Ht T_s - T_{s-1}, written over T_{s-1}
+        launch_apply(op->view, op->precision, cur, oth, 2.0 / a, b, -1.0, oth, red.p(), 3, st);
+        launch_reduce(red.p(), ga, 3, (double*)dots.p + 3 * s, st);
+        std::swap(cur, oth);
+      }
+      MB_CUDA(cudaMemcpyAsync(hd.data(), dots.p, sizeof(double) * hd.size(), cudaMemcpyDeviceToHost, st));
+      MB_CUDA(cudaStreamSynchronize(st));
+      // s=0: hd[0]=<T0,T1>=mu1, hd[1]=<T1,T1>, hd[2]=<T0,T0>=mu0
+      // s>=1: hd[3s]=<T_s,T_{s+1}>, hd[3s+1]=<T_{s+1},T_{s+1}>
+      const double mu0 = hd[2], mu1 = hd[0];
+      std::vector<double> m((size_t)n_moments, 0.0);
+      m[0] = mu0;
+      if (n_moments > 1) m[1] = mu1;
+      for (int64_t s = 1; 2 * s < n_moments; ++s) {
+        m[(size_t)(2 * s)] = 2.0 * hd[3 * (size_t)(s - 1) + 1] - mu0;  // <T_s, T_s>
+        if (2 * s + 1 < n_moments) m[(size_t)(2 * s + 1)] = 2.0 * hd[3 * (size_t)s] - mu1;
+      }
+      for (int64_t i = 0; i < n_moments; ++i) acc[(size_t)i] += m[(size_t)i];
+    }
+    const double norm = 1.0 / ((double)n_probes * (double)op->dim);
+    for (int64_t i = 0; i < n_moments; ++i) mu[i] = acc[(size_t)i] * norm;
+  });
+}
+
+int mb_kpm_projector_apply(mb_op_t op, int64_t expansion_order, double e_min, double e_max,
+                           double e_fermi, double padding, const void* v_dev, int order,
+                           void* out_dev) {
+  return guard([&] {
+    MB_REQUIRE(op && v_dev && out_dev, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(expansion_order >= 0, MB_ERR_INVALID_ARG, "negative expansion order");
+    check_order(order);
+    const int64_t M = expansion_order;
+    const double a = (e_max - e_min) / 2.0 * (1.0 + padding);
+    const double b = (e_max + e_min) / 2.0;
+    const double eps = (e_fermi - b) / a;
+    const double pi = 3.14159265358979323846;
+    std::vector<double> g((size_t)M + 1), mu((size_t)M + 1);
+    mb_kpm_jackson_kernel(M, g.data());
+    const double ac = std::acos(eps);  // projector_moments (kpm.h:51-61)
+    mu[0] = 1.0 - ac / pi;
+    for (int64_t m = 1; m <= M; ++m) mu[(size_t)m] = -2.0 * std::sin((double)m * ac) / ((double)m * pi);
+    cudaStream_t st = 0;
+    const size_t vb = elem_bytes(op->precision) * (size_t)op->dim;
+    DevBuf tp(vb), tc(vb), res(vb);
+    to_tensor(op, v_dev, tp.p, order, st);
+    launch_axpby(op->precision, op->dim, g[0] * mu[0], 0.0, tp.p, 0.0, 0.0, res.p, nullptr, 0, st);
+    if (M > 0) {
+      launch_apply(op->view, op->precision, tp.p, tc.p, 1.0 / a, b, 0.0, nullptr, nullptr, 0, st);
+      launch_axpby(op->precision, op->dim, g[1] * mu[1], 0.0, tc.p, 1.0, 0.0, res.p, nullptr, 0, st);
+      void* prev = tp.p;
+      void* cur = tc.p;
+      for (int64_t m = 2; m <= M; ++m) {
+        launch_apply(op->view, op->precision, cur, prev, 2.0 / a, b, -1.0, prev, nullptr, 0, st);
+        std::swap(prev, cur);
+        launch_axpby(op->precision, op->dim, g[(size_t)m] * mu[(size_t)m], 0.0, cur, 1.0, 0.0,
+                     res.p, nullptr, 0, st);
+      }
+    }
+    from_tensor(op, res.p, out_dev, order, st);
+    MB_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+int mb_estimate_bounds(mb_op_t op, int64_t power_iterations, double spectral_padding,
+                       uint64_t seed, double* lower, double* upper) {
+  return guard([&] {
+    MB_REQUIRE(op && lower && upper, MB_ERR_INVALID_ARG, "NULL argument");
+    cudaStream_t st = 0;
+    const size_t vb = elem_bytes(op->precision) * (size_t)op->dim;
+    DevBuf s0(vb), v(vb), w(vb);
+    launch_fill_rng(op->precision, op->Du, op->Dd, seed, 0, 0, s0.p, st);
+    const int ga = apply_grid(op->view, op->precision), gb = blas_grid(op->dim);
+    Reducer red(std::max(ga, gb), 3);
+    // power_method (linear_operator_utils.h:18-51) on scale*(H - shift)
+    auto power = [&](double scale, double shift) -> double {
+      if (power_iterations == 0) return 0.0;
+      launch_dot(op->precision, op->dim, s0.p, s0.p, red.p(), st);
+      double nrm = std::sqrt(red.fetch(gb, 3, st)[2]);
+      if (nrm == 0.0) return 0.0;
+      launch_axpby(op->precision, op->dim, 1.0 / nrm, 0.0, s0.p, 0.0, 0.0, v.p, nullptr, 0, st);
+      double eig = 0.0;
+      for (int64_t i = 0; i < power_iterations; ++i) {
+        launch_apply(op->view, op->precision, v.p, w.p, scale, shift, 0.0, nullptr, red.p(), 7, st);
+        const double* h = red.fetch(ga, 3, st);
+        const double num = h[0], den = h[2], wn = std::sqrt(h[1]);
+        if (den == 0.0) return 0.0;
+        eig = num / den;
+        if (wn == 0.0) return 0.0;
+        launch_axpby(op->precision, op->dim, 1.0 / wn, 0.0, w.p, 0.0, 0.0, v.p, nullptr, 0, st);
+      }
+      return eig;
+    };
+    const double dominant = std::fabs(power(1.0, 0.0));
+    if (dominant == 0.0) {
+      *lower = *upper = 0.0;
+      return;
+    }
+    const double shift = dominant * (1.0 + spectral_padding) + 2.220446049250313e-16;
+    // Shifted: H + shift ; NegShift: -H + shift  (linear_operator.h:124-151)
+    const double beta = power(1.0, -shift) - shift;
+    const double alpha = shift - power(-1.0, shift);
+    *lower = std::min(alpha, beta);
+    *upper = std::max(alpha, beta);
+  });
+}
+
+int mb_dot_re(mb_op_t op, const void* x_dev, const void* y_dev, double* out) {
+  return guard([&] {
+    MB_REQUIRE(op && x_dev && y_dev && out, MB_ERR_INVALID_ARG, "NULL argument");
+    const int gb = blas_grid(op->dim);
+    Reducer red(gb, 3);
+    launch_dot(op->precision, op->dim, x_dev, y_dev, red.p(), 0);
+    *out = red.fetch(gb, 3, 0)[0];
+  });
+}
+
+int mb_norm(mb_op_t op, const void* x_dev, double* out) {
+  return guard([&] {
+    MB_REQUIRE(op && x_dev && out, MB_ERR_INVALID_ARG, "NULL argument");
+    const int gb = blas_grid(op->dim);
+    Reducer red(gb, 3);
+    launch_dot(op->precision, op->dim, x_dev, x_dev, red.p(), 0);
+    *out = std::sqrt(red.fetch(gb, 3, 0)[2]);
+  });
+}
+
+}  // extern "C"

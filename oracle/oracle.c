@@ -300,19 +300,72 @@ static int col_entry_cmp(const void* a, const void* b) {
   return x->row < y->row ? -1 : (x->row > y->row ? 1 : 0);
 }
 
+/* Entries of column j of H (compute_matrix_elements, matrix_elements.h:80-104):
+ * canonicalize(H * key_j) (ExpressionBase::operator*=, expression_base.h:175-193,
+ * then canonicalize again at matrix_elements.h:85 -- the identity on
+ * normal-ordered terms), keep the pure creator strings of the sector
+ * (set.contains), look up their index, sort by row.  Returns the count. */
+static int column_entries(const or_expr* h, int L, int nup, int ndn, uint64_t um_j, uint64_t dm_j,
+                          const key_idx* lookup, int64_t dim, col_entry* col, int col_cap) {
+  or_op key[OR_MAX_OPS];
+  int kn = state_key(L, um_j, dm_j, key);
+  or_expr prod;
+  expr_init(&prod);
+  for (int a = 0; a < h->n; ++a) {
+    if (h->t[a].n + kn > OR_MAX_OPS) continue;
+    if (is_zero(h->t[a].re, h->t[a].im)) continue;
+    or_op cat[OR_MAX_OPS];
+    memcpy(cat, h->t[a].ops, sizeof(or_op) * (size_t)h->t[a].n);
+    memcpy(cat + h->t[a].n, key, sizeof(or_op) * (size_t)kn);
+    canonicalize_recursive(h->t[a].n + kn, cat, h->t[a].re, h->t[a].im, &prod);
+  }
+  int m = 0;
+  for (int p = 0; p < prod.n; ++p) {
+    const or_term* tm = &prod.t[p];
+    if (tm->n != nup + ndn) continue;
+    uint64_t um = 0, dm = 0;
+    int ok = 1;
+    for (int q = 0; q < tm->n; ++q) {
+      if (op_type(tm->ops[q]) != 0) { ok = 0; break; }
+      if (op_spin(tm->ops[q]) == 0) um |= 1ull << op_value(tm->ops[q]);
+      else dm |= 1ull << op_value(tm->ops[q]);
+    }
+    if (!ok) continue;
+    or_op chk[OR_MAX_OPS];
+    int cn = state_key(L, um, dm, chk);
+    if (!key_equal(tm, cn, chk)) continue;
+    key_idx probe = {um, dm, 0};
+    key_idx* hit = (key_idx*)bsearch(&probe, lookup, (size_t)dim, sizeof(key_idx), key_cmp);
+    if (!hit) continue;
+    if (m < col_cap) {
+      col[m].row = hit->idx;
+      col[m].re = tm->re;
+      col[m].im = tm->im;
+    }
+    ++m;
+  }
+  expr_free(&prod);
+  if (m <= col_cap) qsort(col, (size_t)m, sizeof(col_entry), col_entry_cmp);
+  return m;
+}
+
+#define OR_COL_CAP 1024
+
 /*
  * H(i,j) = coefficient of basis key i in canonicalize(H * key_j), written as
  * CSC (column j's rows ascending); for the Hermitian real-space Hubbard H the
- * same arrays read as CSR of H^T = H.  col_ptr has dim+1 entries.  Pass
- * row_idx == NULL to count only.  Returns nnz, or -1 on bad arguments /
- * capacity.
+ * same arrays read as CSR of H^T = H.  Two calls: with row_idx == NULL it
+ * fills col_ptr (dim+1 entries) and returns nnz; then with row_idx/re/im of
+ * that capacity and the same col_ptr it fills the entries.  Columns are
+ * processed in parallel (OpenMP, as the reference's #pragma omp parallel for
+ * schedule(dynamic), matrix_elements.h:80-82).  Returns nnz or -1.
  */
 int64_t or_matrix_elements_csc(const int* dims, int ndim, double t, double U, int nup, int ndn,
                                int64_t* col_ptr, int64_t* row_idx, double* re, double* im,
                                int64_t cap) {
   int L = 1;
   for (int d = 0; d < ndim; ++d) L *= dims[d];
-  if (ndim < 1 || ndim > 3 || L > 60) return -1;
+  if (ndim < 1 || ndim > 3 || L > 60 || !col_ptr) return -1;
   int64_t dim = or_basis_size(L, nup, ndn);
   if (dim <= 0) return -1;
   uint64_t* up = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)dim);
@@ -325,78 +378,46 @@ int64_t or_matrix_elements_csc(const int* dims, int ndim, double t, double U, in
     lookup[i].idx = i;
   }
   qsort(lookup, (size_t)dim, sizeof(key_idx), key_cmp);
-
   or_expr h;
   expr_init(&h);
   hubbard_terms(dims, ndim, t, U, &h);
-  const int cap_ops = OR_MAX_OPS;
-
   int64_t nnz = 0;
-  col_entry* col = NULL;
-  int col_cap = 0;
-  if (col_ptr) col_ptr[0] = 0;
-  for (int64_t j = 0; j < dim; ++j) {
-    or_op key[OR_MAX_OPS];
-    int kn = state_key(L, up[j], dn[j], key);
-    /* ExpressionBase::operator*= (expression_base.h:175-193) then
-     * canonicalize again (matrix_elements.h:85); the second canonicalization
-     * of normal-ordered terms is the identity. */
-    or_expr prod;
-    expr_init(&prod);
-    for (int a = 0; a < h.n; ++a) {
-      if (h.t[a].n + kn > cap_ops) continue;
-      or_op cat[OR_MAX_OPS];
-      memcpy(cat, h.t[a].ops, sizeof(or_op) * (size_t)h.t[a].n);
-      memcpy(cat + h.t[a].n, key, sizeof(or_op) * (size_t)kn);
-      if (is_zero(h.t[a].re, h.t[a].im)) continue;
-      canonicalize_recursive(h.t[a].n + kn, cat, h.t[a].re, h.t[a].im, &prod);
+  int failed = 0;
+  if (!row_idx) {
+#pragma omp parallel
+    {
+      col_entry* col = (col_entry*)malloc(sizeof(col_entry) * OR_COL_CAP);
+#pragma omp for schedule(dynamic, 64)
+      for (int64_t j = 0; j < dim; ++j)
+        col_ptr[j + 1] = column_entries(&h, L, nup, ndn, up[j], dn[j], lookup, dim, col, OR_COL_CAP);
+      free(col);
     }
-    int m = 0;
-    if (prod.n > col_cap) {
-      col_cap = prod.n * 2;
-      col = (col_entry*)realloc(col, sizeof(col_entry) * (size_t)col_cap);
-    }
-    for (int p = 0; p < prod.n; ++p) {
-      /* set.contains(term) -- only pure creator strings of the sector match. */
-      const or_term* tm = &prod.t[p];
-      if (tm->n != nup + ndn) continue;
-      uint64_t um = 0, dm = 0;
-      int ok = 1;
-      for (int q = 0; q < tm->n; ++q) {
-        if (op_type(tm->ops[q]) != 0) { ok = 0; break; }
-        if (op_spin(tm->ops[q]) == 0) um |= 1ull << op_value(tm->ops[q]);
-        else dm |= 1ull << op_value(tm->ops[q]);
+    col_ptr[0] = 0;
+    for (int64_t j = 0; j < dim; ++j) col_ptr[j + 1] += col_ptr[j];
+    nnz = col_ptr[dim];
+  } else {
+    if (col_ptr[dim] > cap) failed = 1;
+#pragma omp parallel
+    {
+      col_entry* col = (col_entry*)malloc(sizeof(col_entry) * OR_COL_CAP);
+#pragma omp for schedule(dynamic, 64)
+      for (int64_t j = 0; j < dim; ++j) {
+        if (failed) continue;
+        int m = column_entries(&h, L, nup, ndn, up[j], dn[j], lookup, dim, col, OR_COL_CAP);
+        if (m > OR_COL_CAP || col_ptr[j] + m != col_ptr[j + 1]) {
+          failed = 1;
+          continue;
+        }
+        for (int p = 0; p < m; ++p) {
+          row_idx[col_ptr[j] + p] = col[p].row;
+          re[col_ptr[j] + p] = col[p].re;
+          im[col_ptr[j] + p] = col[p].im;
+        }
       }
-      if (!ok) continue;
-      or_op chk[OR_MAX_OPS];
-      int cn = state_key(L, um, dm, chk);
-      if (!key_equal(tm, cn, chk)) continue;
-      key_idx probe = {um, dm, 0};
-      key_idx* hit = (key_idx*)bsearch(&probe, lookup, (size_t)dim, sizeof(key_idx), key_cmp);
-      if (!hit) continue;
-      col[m].row = hit->idx;
-      col[m].re = tm->re;
-      col[m].im = tm->im;
-      ++m;
+      free(col);
     }
-    qsort(col, (size_t)m, sizeof(col_entry), col_entry_cmp);
-    if (row_idx) {
-      if (nnz + m > cap) {
-        nnz = -1;
-        expr_free(&prod);
-        break;
-      }
-      for (int p = 0; p < m; ++p) {
-        row_idx[nnz + p] = col[p].row;
-        re[nnz + p] = col[p].re;
-        im[nnz + p] = col[p].im;
-      }
-    }
-    nnz += m;
-    if (col_ptr) col_ptr[j + 1] = nnz;
-    expr_free(&prod);
+    nnz = failed ? -1 : col_ptr[dim];
   }
-  free(col);
   expr_free(&h);
   free(lookup);
   free(up);
@@ -697,8 +718,8 @@ int or_find_min_eigenpair(int64_t dim, const int64_t* col_ptr, const int64_t* ro
   double* basis = reorth ? (double*)malloc(sizeof(double) * 2 * (size_t)dim * (size_t)k) : NULL;
   double b_norm = 0.0;
   int m = or_lanczos_pass_one(&op, seed, k, alphas, betas, &b_norm, reorth, basis);
-  free(basis);
   if (m < 0) {
+    free(basis);
     free(alphas);
     free(betas);
     return -1;
@@ -706,6 +727,7 @@ int or_find_min_eigenpair(int64_t dim, const int64_t* col_ptr, const int64_t* ro
   if (m == 0) {
     *e0 = 0.0;
     if (vec) memset(vec, 0, sizeof(double) * 2 * (size_t)dim);
+    free(basis);
     free(alphas);
     free(betas);
     return 0;
@@ -714,7 +736,7 @@ int or_find_min_eigenpair(int64_t dim, const int64_t* col_ptr, const int64_t* ro
   double* z = (double*)malloc(sizeof(double) * (size_t)m * (size_t)m);
   memcpy(d, alphas, sizeof(double) * (size_t)m);
   if (or_tridiag_eig(m, d, betas, z) != 0) {
-    free(d); free(z); free(alphas); free(betas);
+    free(d); free(z); free(alphas); free(betas); free(basis);
     return -2;
   }
   *e0 = -d[m - 1];
@@ -724,7 +746,15 @@ int or_find_min_eigenpair(int64_t dim, const int64_t* col_ptr, const int64_t* ro
     double* yr = (double*)malloc(sizeof(double) * (size_t)m);
     double* yi = (double*)calloc((size_t)m, sizeof(double));
     for (int i = 0; i < m; ++i) yr[i] = z[i + (size_t)m * (m - 1)] * b_norm;
-    or_lanczos_pass_two(&op, seed, m, alphas, betas, b_norm, yr, yi, vec);
+    if (basis) { /* re-orthogonalised run: x = sum_j y_j v_j from the stored basis */
+      memset(vec, 0, sizeof(double) * 2 * (size_t)dim);
+      for (int j = 0; j < m; ++j) {
+        const double* vj = basis + (size_t)2 * dim * j;
+        for (int64_t i = 0; i < 2 * dim; ++i) vec[i] += yr[j] * vj[i];
+      }
+    } else {
+      or_lanczos_pass_two(&op, seed, m, alphas, betas, b_norm, yr, yi, vec);
+    }
     free(yr);
     free(yi);
   }
@@ -732,6 +762,7 @@ int or_find_min_eigenpair(int64_t dim, const int64_t* col_ptr, const int64_t* ro
   free(z);
   free(alphas);
   free(betas);
+  free(basis);
   return m;
 }
 
