@@ -136,6 +136,20 @@ int mb_op_apply_affine(mb_op_t op, const void* x_dev, void* y_dev, double scale,
 /* apply() with host buffers: copies x in, applies, copies y out, then waits. */
 int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order);
 
+/* y = H x on device buffers in REFERENCE order, without allocating: no
+ * cudaMalloc/cudaFree, no allocating library call.  No counterpart in the
+ * reference.  For callers that cannot let the library allocate device memory
+ * (a host framework that owns all device memory through its own pool, a
+ * latency-critical loop that cannot afford cudaMalloc's implicit device
+ * synchronisation).  mb_op_apply's permutation scratch comes instead from one
+ * fixed 32 MiB array inside the library (two vectors of up to 1,048,576
+ * complex128 elements), held on every GPU that loads the library until exit;
+ * larger sectors return MB_ERR_CAPACITY.  The first call on a device sets up
+ * (looks up the array's address, uploads a small table) with the operator's
+ * device current; make it before any stream capture.  All calls on a device
+ * share the array: calls that overlap on the GPU race; serialise them. */
+int mb_op_apply_noalloc(mb_op_t op, const void* x_dev, void* y_dev, void* stream);
+
 /* ---- seeded start vectors ----------------------------------------------- *
  * v[i] = (u1, u2), u ~ U[-1,1) from Philox4x32-10 (Salmon et al., SC'11) with
  * key = seed and counter (i_lo, i_hi, stream, 0), where i is the TENSOR index

@@ -95,6 +95,7 @@ SIGNATURES = {
     "mb_op_apply_affine": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_double, _vp,
                                      C.c_int, _vp]),
     "mb_op_apply_host": (C.c_int, [_vp, _vp, _vp, C.c_int]),
+    "mb_op_apply_noalloc": (C.c_int, [_vp, _vp, _vp, _vp]),
     "mb_fill_uniform": (C.c_int, [_vp, C.c_uint64, C.c_uint32, _vp, C.c_int, _vp]),
     "mb_fill_phase": (C.c_int, [_vp, C.c_uint64, C.c_uint32, _vp, C.c_int, _vp]),
     "mb_lanczos_pass_one": (C.c_int, [_vp, _vp, C.c_int, _i64, C.c_double, _dp, _dp, _i64p, _dp]),
@@ -359,6 +360,13 @@ class GpuHubbardOperator:
         y = self.empty() if out is None else out
         _check(lib().mb_op_apply_affine(self._h, _ptr(x), _ptr(y), scale, shift, beta, _ptr(z),
                                         order, self._stream(stream)))
+        return y
+
+    def apply_noalloc(self, x, out=None, stream=None):
+        """Reference-order y = H x that allocates nothing inside the library:
+        for callers that own all device memory (see mb_op_apply_noalloc)."""
+        y = self.empty() if out is None else out
+        _check(lib().mb_op_apply_noalloc(self._h, _ptr(x), _ptr(y), self._stream(stream)))
         return y
 
     def apply_host(self, x: np.ndarray, y: np.ndarray, order: int = ORDER_REFERENCE):
