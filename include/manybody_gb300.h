@@ -229,6 +229,25 @@ int mb_kpm_projector_apply(mb_op_t op, int64_t expansion_order, double e_min, do
 int mb_estimate_bounds(mb_op_t op, int64_t power_iterations, double spectral_padding,
                        uint64_t seed, double* lower, double* upper);
 
+/* ---- block-floating-point vectors (MB_PREC_Q64 operators) ---------------- *
+ * A Q64 vector is n pairs of int64 mantissas {re, im} (16 bytes per element,
+ * like complex128) plus one int exponent E: element = (re + i im) * 2^E.
+ * Mantissas stay below 2^bits (mb_q64_mantissa_bits), which leaves room for
+ * the exact integer hop sums.  These entry points expose the engine's
+ * internal vector format to drivers that keep many applies on the device;
+ * they have no counterpart in the reference. */
+int mb_q64_mantissa_bits(mb_op_t op, int* bits);
+/* complex128 (order) -> Q64 in tensor order; *exponent receives E.  Waits. */
+int mb_q64_from_f64(mb_op_t op, const void* x_dev, int order, void* xq_dev, int* exponent,
+                    void* stream);
+/* Q64 (tensor order) -> complex128 in `order` (correctly rounded).  Waits. */
+int mb_q64_to_f64(mb_op_t op, const void* xq_dev, int exponent, int order, void* x_dev,
+                  void* stream);
+/* yq = H xq on Q64 vectors in tensor order; *y_exponent receives the output
+ * exponent (known before the kernel runs).  Asynchronous on `stream`. */
+int mb_op_apply_q64(mb_op_t op, const void* xq_dev, int x_exponent, void* yq_dev,
+                    int* y_exponent, void* stream);
+
 /* ---- block reductions on device vectors (for drivers above this ABI) ---- */
 /* *out = Re <x, y> (arma::cdot real part), FP64 accumulation, deterministic. */
 int mb_dot_re(mb_op_t op, const void* x_dev, const void* y_dev, double* out);

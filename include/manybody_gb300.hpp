@@ -1,0 +1,199 @@
+// manybody_gb300.hpp -- header-only C++ layer over the C ABI that keeps the
+// reference library's calling surface (keyehzy/manybody):
+//
+//   reference                                        here
+//   FermionBasis::with_fixed_particle_number_and_spin mbgpu::FermionBasis::with_fixed_particle_number_and_spin
+//     (src/algebra/basis.cpp:91-126)
+//   basis.set.size() / index_of / contains            size() / index_of() / contains()
+//   HubbardModel / 2D / 3D (t, u, sizes...)           mbgpu::HubbardModel / 2D / 3D
+//     (src/algebra/fermion/model/hubbard_model.h)
+//   compute_matrix_elements<sp_cx_mat>(basis, H)      mbgpu::compute_matrix_elements(basis, model)
+//     (src/algebra/matrix_elements.h:74-105)
+//   SparseComplexMatrixOperator (linear_operator.h:81-91)
+//                                                     mbgpu::GpuHubbardOperator<VectorType>
+//   find_min_eigenpair(op, k) (lanczos.h:283-290)     mbgpu::find_min_eigenpair(op, k, seed)
+//
+// GpuHubbardOperator<V> models the reference's LinearOperator concept
+// (VectorType, ScalarType, apply(const V&) const -> V, dimension()), so the
+// reference's own header-only drivers (lanczos.h, kpm.h, evolve_state.h)
+// accept it unchanged with V = arma::cx_vec: apply() copies the host vector
+// to the GPU, applies H there (reference order) and copies the result back.
+// V needs only V(n), .memptr() and .n_elem (arma::cx_vec has them).  The
+// device-resident drivers (find_min_eigenpair etc. below) keep the whole
+// Krylov iteration on the GPU and are the fast path.
+//
+// Errors: every failing mb_* call throws mbgpu::Error (a std::runtime_error
+// carrying the mb_status), matching the reference's use of exceptions.
+#pragma once
+
+#include <complex>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "manybody_gb300.h"
+
+namespace mbgpu {
+
+struct Error : std::runtime_error {
+  int status;
+  Error(int s, const std::string& what) : std::runtime_error(what), status(s) {}
+};
+
+inline void check(int status) {
+  if (status != MB_OK) throw Error(status, mb_last_error());
+}
+
+class FermionBasis {
+ public:
+  static FermionBasis with_fixed_particle_number_and_spin(size_t orbitals, size_t particles,
+                                                          int spin_projection) {
+    mb_basis_t h = nullptr;
+    check(mb_basis_create_fixed_spin((int64_t)orbitals, (int64_t)particles, spin_projection, &h));
+    return FermionBasis(h, orbitals, particles);
+  }
+  FermionBasis(FermionBasis&& o) noexcept : h_(std::exchange(o.h_, nullptr)),
+                                            orbitals(o.orbitals), particles(o.particles) {}
+  FermionBasis& operator=(FermionBasis&& o) noexcept {
+    std::swap(h_, o.h_);
+    orbitals = o.orbitals;
+    particles = o.particles;
+    return *this;
+  }
+  FermionBasis(const FermionBasis&) = delete;
+  FermionBasis& operator=(const FermionBasis&) = delete;
+  ~FermionBasis() { mb_basis_destroy(h_); }
+
+  size_t size() const {
+    int64_t n = 0;
+    check(mb_basis_size(h_, &n));
+    return (size_t)n;
+  }
+  size_t index_of(uint64_t up_mask, uint64_t down_mask) const {
+    int64_t i = 0;
+    check(mb_basis_index_of(h_, up_mask, down_mask, &i));
+    return (size_t)i;
+  }
+  bool contains(uint64_t up_mask, uint64_t down_mask) const {
+    int64_t i = 0;
+    return mb_basis_index_of(h_, up_mask, down_mask, &i) == MB_OK;
+  }
+  // Keys in reference index order as (up mask, down mask).
+  std::pair<std::vector<uint64_t>, std::vector<uint64_t>> keys() const {
+    std::vector<uint64_t> up(size()), down(size());
+    check(mb_basis_export_reference_order(h_, up.data(), down.data()));
+    return {std::move(up), std::move(down)};
+  }
+  mb_basis_t handle() const { return h_; }
+
+ private:
+  FermionBasis(mb_basis_t h, size_t o, size_t p) : h_(h), orbitals(o), particles(p) {}
+  mb_basis_t h_ = nullptr;
+
+ public:
+  size_t orbitals = 0;
+  size_t particles = 0;
+};
+
+class HubbardModelBase {
+ public:
+  HubbardModelBase(double t, double u, std::vector<int64_t> dims) : t(t), u(u) {
+    check(mb_hubbard_create(dims.data(), (int)dims.size(), t, u, &h_));
+  }
+  HubbardModelBase(HubbardModelBase&& o) noexcept : t(o.t), u(o.u), h_(std::exchange(o.h_, nullptr)) {}
+  HubbardModelBase(const HubbardModelBase&) = delete;
+  HubbardModelBase& operator=(const HubbardModelBase&) = delete;
+  ~HubbardModelBase() { mb_model_destroy(h_); }
+  // FermionExpression::size() of hamiltonian()
+  size_t term_count() const {
+    int64_t n = 0;
+    check(mb_model_term_count(h_, &n));
+    return (size_t)n;
+  }
+  mb_model_t handle() const { return h_; }
+  double t, u;
+
+ private:
+  mb_model_t h_ = nullptr;
+};
+
+struct HubbardModel : HubbardModelBase {
+  HubbardModel(double t, double u, size_t size) : HubbardModelBase(t, u, {(int64_t)size}) {}
+};
+struct HubbardModel2D : HubbardModelBase {
+  HubbardModel2D(double t, double u, size_t sx, size_t sy)
+      : HubbardModelBase(t, u, {(int64_t)sx, (int64_t)sy}) {}
+};
+struct HubbardModel3D : HubbardModelBase {
+  HubbardModel3D(double t, double u, size_t sx, size_t sy, size_t sz)
+      : HubbardModelBase(t, u, {(int64_t)sx, (int64_t)sy, (int64_t)sz}) {}
+};
+
+// Reference-order CSR of H, values complex<double>.
+struct CsrMatrix {
+  size_t n = 0;
+  std::vector<int64_t> row_ptr, col_idx;
+  std::vector<std::complex<double>> values;
+};
+
+inline CsrMatrix compute_matrix_elements(const FermionBasis& basis, const HubbardModelBase& model) {
+  CsrMatrix m;
+  m.n = basis.size();
+  int64_t nnz = 0;
+  m.row_ptr.resize(m.n + 1);
+  check(mb_compute_matrix_elements_csr(basis.handle(), model.handle(), &nnz, m.row_ptr.data(),
+                                       nullptr, nullptr));
+  m.col_idx.resize((size_t)nnz);
+  m.values.resize((size_t)nnz);
+  check(mb_compute_matrix_elements_csr(basis.handle(), model.handle(), &nnz, m.row_ptr.data(),
+                                       m.col_idx.data(),
+                                       reinterpret_cast<double*>(m.values.data())));
+  return m;
+}
+
+// The matrix-free GPU operator, shaped like the reference's LinearOperator.
+template <typename Vector>
+class GpuHubbardOperator {
+ public:
+  using VectorType = Vector;
+  using ScalarType = std::complex<double>;
+
+  GpuHubbardOperator(const FermionBasis& basis, const HubbardModelBase& model,
+                     int precision = MB_PREC_F64) {
+    check(mb_op_create(basis.handle(), model.handle(), precision, &h_));
+    check(mb_op_dimension(h_, &dim_));
+  }
+  GpuHubbardOperator(GpuHubbardOperator&& o) noexcept : h_(std::exchange(o.h_, nullptr)), dim_(o.dim_) {}
+  GpuHubbardOperator(const GpuHubbardOperator&) = delete;
+  ~GpuHubbardOperator() { mb_op_destroy(h_); }
+
+  // LinearOperator::apply (linear_operator.h:41): a fresh vector H v.
+  VectorType apply(const VectorType& v) const {
+    if ((int64_t)v.n_elem != dim_) throw Error(MB_ERR_DIM_MISMATCH, "vector dimension mismatch");
+    VectorType out((size_t)dim_);
+    check(mb_op_apply_host(h_, v.memptr(), out.memptr(), MB_ORDER_REFERENCE));
+    return out;
+  }
+  size_t dimension() const { return (size_t)dim_; }
+  mb_op_t handle() const { return h_; }
+
+ private:
+  mb_op_t h_ = nullptr;
+  int64_t dim_ = 0;
+};
+
+// Device-resident find_min_eigenpair (lanczos.h:283-290) from a device seed
+// vector in reference order.  Returns E0; writes the Ritz vector if vec_dev.
+template <typename Op>
+double find_min_eigenpair(const Op& op, size_t k, const void* seed_dev, void* vec_dev = nullptr,
+                          const mb_lanczos_opts* opts = nullptr) {
+  double e0 = 0.0;
+  int64_t steps = 0;
+  check(mb_find_min_eigenpair(op.handle(), (int64_t)k, seed_dev, MB_ORDER_REFERENCE, opts, &e0,
+                              vec_dev, &steps));
+  return e0;
+}
+
+}  // namespace mbgpu

@@ -37,6 +37,7 @@ ORDER_TENSOR = 1
 
 PREC_F64 = 0
 PREC_F32 = 1
+PREC_Q64 = 2
 
 _STATUS_NAMES = {
     1: "MB_ERR_INVALID_ARG", 2: "MB_ERR_CAPACITY", 3: "MB_ERR_ZERO_NORM",
@@ -115,6 +116,10 @@ SIGNATURES = {
     "mb_kpm_projector_apply": (C.c_int, [_vp, _i64, C.c_double, C.c_double, C.c_double,
                                          C.c_double, _vp, C.c_int, _vp]),
     "mb_estimate_bounds": (C.c_int, [_vp, _i64, C.c_double, C.c_uint64, _dp, _dp]),
+    "mb_q64_mantissa_bits": (C.c_int, [_vp, C.POINTER(C.c_int)]),
+    "mb_q64_from_f64": (C.c_int, [_vp, _vp, C.c_int, _vp, C.POINTER(C.c_int), _vp]),
+    "mb_q64_to_f64": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _vp, _vp]),
+    "mb_op_apply_q64": (C.c_int, [_vp, _vp, C.c_int, _vp, C.POINTER(C.c_int), _vp]),
     "mb_dot_re": (C.c_int, [_vp, _vp, _vp, _dp]),
     "mb_norm": (C.c_int, [_vp, _vp, _dp]),
 }
@@ -387,6 +392,37 @@ class GpuHubbardOperator:
         v = self.empty() if out is None else out
         _check(lib().mb_fill_phase(self._h, seed, stream_id, _ptr(v), order, self._stream(None)))
         return v
+
+    # --- block-floating-point (PREC_Q64) vectors: int64 mantissas + exponent ---
+    def q64_empty(self):
+        import torch
+        return torch.empty((self._dim, 2), dtype=torch.int64, device="cuda")
+
+    def q64_from_f64(self, x, order: int = ORDER_REFERENCE, out=None, stream=None):
+        q = self.q64_empty() if out is None else out
+        e = C.c_int()
+        _check(lib().mb_q64_from_f64(self._h, _ptr(x), order, _ptr(q), C.byref(e),
+                                     self._stream(stream)))
+        return q, e.value
+
+    def q64_to_f64(self, q, exponent: int, order: int = ORDER_REFERENCE, out=None, stream=None):
+        y = self.empty() if out is None else out
+        _check(lib().mb_q64_to_f64(self._h, _ptr(q), exponent, order, _ptr(y),
+                                   self._stream(stream)))
+        return y
+
+    def apply_q64(self, q, exponent: int, out=None, stream=None):
+        """H applied to a Q64 vector (tensor order); returns (mantissas, exponent)."""
+        y = self.q64_empty() if out is None else out
+        e = C.c_int()
+        _check(lib().mb_op_apply_q64(self._h, _ptr(q), exponent, _ptr(y), C.byref(e),
+                                     self._stream(stream)))
+        return y, e.value
+
+    def q64_mantissa_bits(self) -> int:
+        b = C.c_int()
+        _check(lib().mb_q64_mantissa_bits(self._h, C.byref(b)))
+        return b.value
 
     def dot_re(self, x, y) -> float:
         r = C.c_double()

@@ -180,6 +180,24 @@ struct OpView {
   const float* u_fold_f;    // float copies for complex64 operators
   const float* self_up_f;
   const float* self_dn_f;
+  // Down hops again in slot-major ("ELL") layout for coalesced reads:
+  // dn_ell[j * Dd + c] is column c's j-th entry, j < dn_cnt[c] <= dn_ell_k.
+  const uint32_t* dn_ell;
+  const uint8_t* dn_cnt;
+  int dn_ell_k;
+  // On-the-fly down hops (lattices with <= 64 bonds): per down state the
+  // bitmask of bonds with exactly one occupied end; per bond its two-site
+  // mask, the mask of sites strictly between its ends, its multiplicity;
+  // colex-rank tables in 8-bit chunks: rank(m) = sum_k
+  // dn_rank[(k*(n+1) + cb_k)*256 + byte_k(m)], cb_k = set bits below chunk k.
+  const unsigned long long* dn_vmask;
+  const uint32_t* bond_pair;
+  const uint32_t* bond_between;
+  const uint32_t* bond_mult;
+  const int32_t* dn_rank;
+  int n_bonds;
+  int dn_nchunks;
+  int dn_n;
   double t;
   int max_up_degree;
   int max_dn_degree;
@@ -204,8 +222,19 @@ struct mb_op_s {
     void* hy = nullptr;
   };
   std::map<cudaStream_t, Scratch> scratch;
-  bool q_ready = false;            // Q64 extra tables built
-  void* q_tables = nullptr;
+  // Block-floating-point (MB_PREC_Q64) operators.
+  double q_wmax = 0.0;              // largest sum of |hop weights| of one state
+  int q_qbits = 62;                 // mantissas kept below 2^q_qbits
+  bool q_has_double = false;        // any bond of multiplicity 2
+  std::vector<double> ufold_host;   // U fold table (host copy)
+  struct QScratch {
+    void* xq = nullptr;
+    void* yq = nullptr;
+    void* sq = nullptr;    // down-hop partial sums of the two-pass apply
+    void* prm = nullptr;   // QParams
+    int* ints = nullptr;   // [max exp, Ex, unused, unused]
+  };
+  std::map<cudaStream_t, QScratch> qscratch;
 };
 
 namespace mb {
@@ -244,6 +273,8 @@ void launch_csr_count(const OpView& v, const int32_t* perm, int32_t* row_count, 
 void launch_csr_fill(const OpView& v, const int32_t* perm, const int64_t* row_ptr,
                      int64_t* col_idx, double* values, cudaStream_t st);
 void upload_binomials(cudaStream_t st);
+// tensor -> reference index table of an operator, built on first use
+int32_t* op_perm(mb_op_s* op);
 
 // Host tridiagonal eigensolver (implicit QL, mb_tridiag.cpp).
 bool tridiag_eig(int n, std::vector<double>& d, const std::vector<double>& e,

@@ -16,6 +16,17 @@
 
 namespace mb {
 
+// Q64 hooks (mb_q64_ops.cu)
+void q_op_prepare(mb_op_s* op, const mb_model_s* m, const HopTable& tu, const HopTable& td);
+void q_op_release(mb_op_s* op);
+void q_apply_affine(mb_op_s* op, const void* x, void* y, double scale, double shift, double beta,
+                    const void* z, int order, cudaStream_t st);
+void q_eigenpair(mb_op_s* op, int64_t k, const void* seed, int order, const mb_lanczos_opts* opts,
+                 double sign, double* e_out, void* vec, int64_t* steps_out);
+void q_evolve(mb_op_s* op, const void* psi0, int order, double t, int64_t krylov_steps,
+              int imaginary, void* out);
+int32_t* op_perm(mb_op_s* op);
+
 namespace {
 
 struct DevBuf {
@@ -131,6 +142,66 @@ static void build_op(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m) {
   }
   v.max_up_degree = tu.max_degree;
   v.max_dn_degree = td.max_degree;
+  {
+    // slot-major copy of the down-hop table (coalesced across columns)
+    MB_REQUIRE(td.max_degree <= 255, MB_ERR_CAPACITY, "more than 255 hops from one state");
+    const int K = std::max(td.max_degree, 1);
+    std::vector<uint32_t> ell((size_t)K * (size_t)op->Dd, 0u);
+    std::vector<uint8_t> cnt((size_t)op->Dd, 0);
+    for (int64_t c = 0; c < op->Dd; ++c) {
+      const int32_t o0 = td.off[(size_t)c], o1 = td.off[(size_t)c + 1];
+      cnt[(size_t)c] = (uint8_t)(o1 - o0);
+      for (int32_t j = o0; j < o1; ++j) ell[(size_t)(j - o0) * (size_t)op->Dd + (size_t)c] = td.ent[(size_t)j];
+    }
+    v.dn_ell = upload(op, ell);
+    v.dn_cnt = upload(op, cnt);
+    v.dn_ell_k = K;
+  }
+  if (m->has_hop && !m->bonds.empty() && m->bonds.size() <= 64) {
+    // on-the-fly down hops: bonds, per-state valid-bond masks, rank tables
+    const int nb = (int)m->bonds.size();
+    std::vector<uint32_t> pair((size_t)nb), betw((size_t)nb), mult((size_t)nb);
+    for (int b = 0; b < nb; ++b) {
+      const auto& bd = m->bonds[(size_t)b];
+      pair[(size_t)b] = (1u << bd.a) | (1u << bd.b);
+      betw[(size_t)b] = ((1u << bd.b) - 1u) & ~((2u << bd.a) - 1u);
+      mult[(size_t)b] = (uint32_t)bd.mult;
+    }
+    const SpinSector& dsec = b->down;
+    std::vector<unsigned long long> vm((size_t)dsec.D, 0ull);
+    for (int64_t r = 0; r < dsec.D; ++r) {
+      const uint32_t d = dsec.masks[(size_t)r];
+      unsigned long long bits = 0ull;
+      for (int bb = 0; bb < nb; ++bb) {
+        const uint32_t t = d & pair[(size_t)bb];
+        if (t != 0u && t != pair[(size_t)bb]) bits |= 1ull << bb;
+      }
+      vm[(size_t)r] = bits;
+    }
+    const int n = dsec.n, nchunks = (op->L + 7) / 8;
+    const Binom& B = binom_table();
+    std::vector<int32_t> rt((size_t)nchunks * (size_t)(n + 1) * 256, 0);
+    for (int k = 0; k < nchunks; ++k)
+      for (int cb = 0; cb <= n; ++cb)
+        for (int byte = 0; byte < 256; ++byte) {
+          int64_t sum = 0;
+          int idx = 0;
+          for (int i = 0; i < 8; ++i)
+            if ((byte >> i) & 1) {
+              ++idx;
+              sum += binom_at(B, 8 * k + i, cb + idx);
+            }
+          rt[((size_t)k * (size_t)(n + 1) + (size_t)cb) * 256 + (size_t)byte] = (int32_t)sum;
+        }
+    v.dn_vmask = upload(op, vm);
+    v.bond_pair = upload(op, pair);
+    v.bond_between = upload(op, betw);
+    v.bond_mult = upload(op, mult);
+    v.dn_rank = upload(op, rt);
+    v.n_bonds = nb;
+    v.dn_nchunks = nchunks;
+    v.dn_n = n;
+  }
   const std::vector<double> uf = u_fold_table(m->u, m->has_u, op->L);
   v.u_fold = upload(op, uf);
   v.u_fold_f = upload(op, std::vector<float>(uf.begin(), uf.end()));
@@ -148,6 +219,7 @@ static void build_op(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m) {
     }
   }
   ensure_binomials();
+  if (op->precision == MB_PREC_Q64) q_op_prepare(op, m, tu, td);
 }
 
 static mb_op_s::Scratch& scratch_for(mb_op_s* op, cudaStream_t st, int nvec) {
@@ -176,6 +248,11 @@ static void ensure_perm(mb_op_s* op) {
   launch_perm(op->view, (int32_t*)p, 0);
   MB_CUDA(cudaStreamSynchronize(0));
   op->perm = (int32_t*)p;
+}
+
+int32_t* op_perm(mb_op_s* op) {
+  ensure_perm(op);
+  return op->perm;
 }
 
 static void to_tensor(mb_op_s* op, const void* src, void* dst, int order, cudaStream_t st) {
@@ -212,6 +289,10 @@ static void apply_affine(mb_op_s* op, const void* x, void* y, double scale, doub
   MB_REQUIRE(x && y, MB_ERR_INVALID_ARG, "NULL vector");
   MB_REQUIRE(x != y, MB_ERR_INVALID_ARG, "x and y must not overlap");
   if (beta != 0.0) MB_REQUIRE(z, MB_ERR_INVALID_ARG, "z is NULL with beta != 0");
+  if (op->precision == MB_PREC_Q64) {
+    q_apply_affine(op, x, y, scale, shift, beta, beta != 0.0 ? z : nullptr, order, st);
+    return;
+  }
   if (order == MB_ORDER_TENSOR) {
     launch_apply(op->view, op->precision, x, y, scale, shift, beta, beta != 0.0 ? z : nullptr,
                  nullptr, 0, st);
@@ -394,6 +475,11 @@ static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
                       const mb_lanczos_opts* opts, double sign, double* e_out, void* vec,
                       int64_t* steps_out) {
   check_order(order);
+  if (op->precision == MB_PREC_Q64) {
+    MB_REQUIRE(seed && e_out, MB_ERR_INVALID_ARG, "NULL argument");
+    q_eigenpair(op, k, seed, order, opts, sign, e_out, vec, steps_out);
+    return;
+  }
   MB_REQUIRE(seed && e_out, MB_ERR_INVALID_ARG, "NULL argument");
   MB_REQUIRE(k >= 0, MB_ERR_INVALID_ARG, "k must be >= 0");
   mb_lanczos_opts o{};
@@ -444,6 +530,10 @@ static void evolve(mb_op_s* op, const void* psi0, int order, double t, int64_t k
                    int imaginary, void* out) {
   check_order(order);
   MB_REQUIRE(psi0 && out, MB_ERR_INVALID_ARG, "NULL vector");
+  if (op->precision == MB_PREC_Q64) {
+    q_evolve(op, psi0, order, t, krylov_steps, imaginary, out);
+    return;
+  }
   cudaStream_t st = 0;
   Krylov kr(op, st);
   DevBuf bt(kr.vb);
@@ -526,8 +616,8 @@ int mb_op_create(mb_basis_t basis, mb_model_t model, int precision, mb_op_t* out
   return guard([&] {
     MB_REQUIRE(basis && model && out, MB_ERR_INVALID_ARG, "NULL argument");
     *out = nullptr;
-    MB_REQUIRE(precision == MB_PREC_F64 || precision == MB_PREC_F32, MB_ERR_INVALID_ARG,
-               "precision must be MB_PREC_F64 or MB_PREC_F32");
+    MB_REQUIRE(precision == MB_PREC_F64 || precision == MB_PREC_F32 || precision == MB_PREC_Q64,
+               MB_ERR_INVALID_ARG, "precision must be MB_PREC_F64, MB_PREC_F32 or MB_PREC_Q64");
     MB_REQUIRE(model->L == basis->L, MB_ERR_DIM_MISMATCH,
                "model sites and basis orbitals differ");
     require_device();
@@ -551,6 +641,7 @@ int mb_op_destroy(mb_op_t op) {
     for (void* p : {kv.second.a, kv.second.b, kv.second.hx, kv.second.hy})
       if (p) cudaFree(p);
   }
+  q_op_release(op);
   for (void* p : op->allocations) cudaFree(p);
   delete op;
   return MB_OK;
@@ -593,13 +684,7 @@ int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
     cudaStream_t st = 0;
     auto& s = scratch_for(op, st, 4);
     MB_CUDA(cudaMemcpyAsync(s.hx, x_host, vb, cudaMemcpyHostToDevice, st));
-    if (order == MB_ORDER_TENSOR) {
-      launch_apply(op->view, op->precision, s.hx, s.hy, 1.0, 0.0, 0.0, nullptr, nullptr, 0, st);
-    } else {
-      to_tensor(op, s.hx, s.a, order, st);
-      launch_apply(op->view, op->precision, s.a, s.b, 1.0, 0.0, 0.0, nullptr, nullptr, 0, st);
-      from_tensor(op, s.b, s.hy, order, st);
-    }
+    apply_affine(op, s.hx, s.hy, 1.0, 0.0, 0.0, nullptr, order, st);
     MB_CUDA(cudaMemcpyAsync(y_host, s.hy, vb, cudaMemcpyDeviceToHost, st));
     MB_CUDA(cudaStreamSynchronize(st));
   });

@@ -1,0 +1,851 @@
+// Block floating point ("Q64") path: FP64-class accuracy without the FP64 pipe.
+//
+// On GB300 the FP64 units run at 1/64 of the FP32 rate (a rate probe on the
+// part measured 1.9 FP64 FMA per clock per SM against 109 FP32 FMA), so a
+// matrix-free H|psi> that adds 33 complex128 terms per output element in
+// FP64 is ALU-bound at ~2 % of HBM bandwidth.  Here a vector is stored as
+// 64-bit integer mantissas (re, im) with ONE binary exponent per vector:
+// value_i = q_i * 2^E.  The hopping part of H has integer weights (+-1, +-2
+// times -t), so sum_j w_j q_j is an exact int64 sum (integer adders run at
+// full rate); only the per-element products by -t*scale and by the diagonal
+// U*n_double - shift are 64x64->128-bit integer multiplies, and one rounding
+// shift produces the output mantissa.  Every vector keeps |q| < 2^qbits,
+// qbits = 62 - ceil(log2(W)), W the largest sum of |hop weights| of a state,
+// so the hop sums cannot overflow.  Accuracy: the quantum is 2^(E) with
+// 2^(E+qbits) >~ max|x|, i.e. ~57 bits relative to the largest element;
+// dot products are accumulated exactly in 128-bit integers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "mb_internal.h"
+#include "mb_q64.h"
+
+namespace mb {
+
+// ---------------------------------------------------------------------------
+// Exact conversions between FP64 and fixed point, integer operations only.
+// ---------------------------------------------------------------------------
+// round(x * 2^-E) for |x| < 2^(E+62); ties rounded away from zero.
+__device__ __forceinline__ long long f64_to_fixed(double x, int E) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  if (ex == 0) return 0;  // zero / subnormal: below any representable quantum here
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const int s = ex - 1075 - E;  // x = m * 2^(ex-1075) = (m * 2^s) * 2^E
+  unsigned long long q;
+  if (s >= 0) q = m << s;
+  else if (s > -60) q = (m + (1ull << (-s - 1))) >> (-s);
+  else q = 0;
+  return (b >> 63) ? -(long long)q : (long long)q;
+}
+
+// q * 2^E rounded to nearest even (the exact value of the integer times the
+// power of two), integer operations only.
+__device__ __forceinline__ double fixed_to_f64(long long q, int E) {
+  if (q == 0) return 0.0;
+  const unsigned long long sign = q < 0 ? 0x8000000000000000ull : 0ull;
+  unsigned long long a = q < 0 ? (unsigned long long)(-q) : (unsigned long long)q;
+  const int lz = __clzll(a);
+  a <<= lz;                                  // bit 63 set
+  unsigned long long m = a >> 11;            // 53 bits
+  const unsigned long long rem = a & 0x7FFull;
+  int e2 = 63 - lz + E;                      // value = (a / 2^63) * 2^e2
+  if (rem > 0x400ull || (rem == 0x400ull && (m & 1ull))) {
+    m += 1;
+    if (m == (1ull << 53)) {
+      m >>= 1;
+      e2 += 1;
+    }
+  }
+  const int biased = e2 + 1023;
+  if (biased <= 0) return 0.0;
+  if (biased >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
+  const unsigned long long bits = sign | ((unsigned long long)biased << 52) | (m & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ unsigned long long mag(long long q) {
+  return q < 0 ? (unsigned long long)(-q) : (unsigned long long)q;
+}
+
+// 128-bit product accumulated with 32 low bits dropped (exact enough: each
+// product loses < 2^32 units against sums of order 2^100+).
+__device__ __forceinline__ __int128 prod_hi(long long a, long long b) {
+  return ((__int128)a * (__int128)b) >> 32;
+}
+
+__device__ __forceinline__ double i128_to_f64(__int128 v) {
+  const long long hi = (long long)(v >> 64);
+  const unsigned long long lo = (unsigned long long)v;
+  return (double)hi * 18446744073709551616.0 + (double)lo;
+}
+
+__device__ __forceinline__ long long round_shift(__int128 p, int sh) {
+  if (sh <= 0) return (long long)(p << (-sh));
+  if (sh >= 127) return 0;
+  return (long long)((p + ((__int128)1 << (sh - 1))) >> sh);
+}
+
+template <int NC>
+__device__ void q_block_reduce(double (&v)[NC], unsigned long long magor, double* partials,
+                               unsigned long long* max_or) {
+  __shared__ double red[32][NC];
+  __shared__ unsigned long long mor[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    double a = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    v[k] = a;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) magor |= __shfl_down_sync(0xffffffffu, magor, o);
+  __syncthreads();
+  if (lane == 0) {
+    for (int k = 0; k < NC; ++k) red[warp][k] = v[k];
+    mor[warp] = magor;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    unsigned long long m = lane < nw ? mor[lane] : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m |= __shfl_down_sync(0xffffffffu, m, o);
+    for (int k = 0; k < NC; ++k) {
+      double a = lane < nw ? red[lane][k] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+      if (lane == 0 && partials) partials[(size_t)blockIdx.x * NC + k] = a;
+    }
+    if (lane == 0 && max_or && m) atomicOr(max_or, m);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The Q64 apply: y = scale (H - shift) x + beta z on mantissas.
+//   P = c1 * S + cq[popc(up & down)] * x_q + c3 * z_q      (128-bit)
+//   y_q = round(P / 2^sh)
+// S = sum over hops of +-x_q (or 2x for doubled bonds), exact in int64.
+// Same row-staged structure as the floating-point kernel: one CTA per row
+// r_up at a time, the row in shared memory for the down hops, coalesced
+// 16-byte loads of the neighbour rows for the up hops.
+// dots (DOTS bit0): Re<x,y> and <y,y> as exact integer sums >> 32.
+// ---------------------------------------------------------------------------
+constexpr int kQThreads = 1024;
+
+template <bool STAGED, int DOTS, bool HAS_Z, bool DBL>
+__global__ void __launch_bounds__(kQThreads)
+k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlong2* z,
+          const QParams* __restrict__ prm, double* __restrict__ partials,
+          unsigned long long* __restrict__ max_or) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int up_words = (v.max_up_degree + 3) & ~3;
+  uint32_t* s_upn = reinterpret_cast<uint32_t*>(smem);
+  longlong2* s_row = reinterpret_cast<longlong2*>(smem + sizeof(uint32_t) * up_words);
+  __shared__ long long s_cq[kMaxOrbitals + 1];
+  __shared__ long long s_c1, s_c3;
+  __shared__ int s_sh;
+  if (threadIdx.x <= (unsigned)v.L) s_cq[threadIdx.x] = prm->cq[threadIdx.x];
+  if (threadIdx.x == 0) {
+    s_c1 = prm->c1;
+    s_c3 = prm->c3;
+    s_sh = prm->sh;
+  }
+  const int64_t Dd = v.Dd;
+  __int128 a_xy = 0, a_yy = 0;
+  unsigned long long mor = 0;
+
+  for (int64_t r = blockIdx.x; r < v.Du; r += gridDim.x) {
+    const longlong2* xrow = x + r * Dd;
+    __syncthreads();
+    const int u0 = v.up_off[r], nup = v.up_off[r + 1] - u0;
+    for (int j = threadIdx.x; j < nup; j += blockDim.x) s_upn[j] = v.up_ent[u0 + j];
+    if (STAGED)
+      for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) s_row[c] = xrow[c];
+    __syncthreads();
+    const uint32_t um = v.up_mask[r];
+    const long long c1 = s_c1, c3 = s_c3;
+    const int sh = s_sh;
+    for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) {
+      long long sr = 0, si = 0;
+      int negs = 0;
+      const int d0 = v.dn_off[c], d1 = v.dn_off[c + 1];
+      for (int j = d0; j < d1; ++j) {
+        const uint32_t e = __ldg(&v.dn_ent[j]);
+        const longlong2 val = STAGED ? s_row[e >> 8] : __ldg(&xrow[e >> 8]);
+        const long long m = -(long long)(e & 1u);   // 0 or -1
+        long long tr = val.x ^ m, ti = val.y ^ m;   // -v = (v ^ -1) + 1: the +1s are counted
+        if (DBL && (e & 2u)) { tr = tr + tr + (m & 1); ti = ti + ti + (m & 1); }
+        sr += tr;
+        si += ti;
+        negs += (int)(e & 1u);
+      }
+#pragma unroll 4
+      for (int j = 0; j < nup; ++j) {
+        const uint32_t e = s_upn[j];
+        const longlong2 val = __ldg(&x[(int64_t)(e >> 8) * Dd + c]);
+        const long long m = -(long long)(e & 1u);
+        long long tr = val.x ^ m, ti = val.y ^ m;
+        if (DBL && (e & 2u)) { tr = tr + tr + (m & 1); ti = ti + ti + (m & 1); }
+        sr += tr;
+        si += ti;
+        negs += (int)(e & 1u);
+      }
+      sr += negs;
+      si += negs;
+      const longlong2 xv = STAGED ? s_row[c] : xrow[c];
+      const long long dq = s_cq[__popc(um & v.dn_mask[c])];
+      __int128 pr = (__int128)c1 * sr + (__int128)dq * xv.x;
+      __int128 pi = (__int128)c1 * si + (__int128)dq * xv.y;
+      const int64_t idx = r * Dd + c;
+      if (HAS_Z) {
+        const longlong2 zv = z[idx];
+        pr += (__int128)c3 * zv.x;
+        pi += (__int128)c3 * zv.y;
+      }
+      longlong2 out;
+      out.x = round_shift(pr, sh);
+      out.y = round_shift(pi, sh);
+      y[idx] = out;
+      if (DOTS & 1) a_xy += prod_hi(xv.x, out.x) + prod_hi(xv.y, out.y);
+      if (DOTS & 2) a_yy += prod_hi(out.x, out.x) + prod_hi(out.y, out.y);
+      if (DOTS & 4) mor |= mag(out.x) | mag(out.y);
+    }
+  }
+  if (DOTS) {
+    double vals[2] = {i128_to_f64(a_xy), i128_to_f64(a_yy)};
+    q_block_reduce<2>(vals, mor, partials, max_or);
+  }
+}
+
+static int sm_count() {
+  static int sms = -1;
+  if (sms < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  return sms > 0 ? sms : 1;
+}
+
+static int smem_optin() {
+  static int v = -1;
+  if (v < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  }
+  return v;
+}
+
+int q_apply_grid(const OpView& v) {
+  int64_t g = sm_count();
+  if (g > v.Du) g = v.Du;
+  return (int)std::max<int64_t>(g, 1);
+}
+
+template <bool STAGED, int DOTS, bool HAS_Z, bool DBL>
+static void q_apply_t(const OpView& v, const void* x, void* y, const void* z, const QParams* prm,
+                      double* partials, unsigned long long* max_or, cudaStream_t st) {
+  const int up_words = (v.max_up_degree + 3) & ~3;
+  size_t smem = sizeof(uint32_t) * (size_t)up_words;
+  if (STAGED) smem += sizeof(longlong2) * (size_t)v.Dd;
+  auto kern = k_apply_q<STAGED, DOTS, HAS_Z, DBL>;
+  MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<q_apply_grid(v), kQThreads, smem, st>>>(v, (const longlong2*)x, (longlong2*)y,
+                                                   (const longlong2*)z, prm, partials, max_or);
+  MB_CUDA(cudaGetLastError());
+}
+
+template <bool STAGED, bool DBL>
+static void q_apply_sel(const OpView& v, const void* x, void* y, const void* z,
+                        const QParams* prm, double* partials, unsigned long long* max_or,
+                        int dots, cudaStream_t st) {
+  if (z) {
+    if (dots) q_apply_t<STAGED, 7, true, DBL>(v, x, y, z, prm, partials, max_or, st);
+    else q_apply_t<STAGED, 0, true, DBL>(v, x, y, z, prm, partials, max_or, st);
+  } else {
+    if (dots) q_apply_t<STAGED, 7, false, DBL>(v, x, y, z, prm, partials, max_or, st);
+    else q_apply_t<STAGED, 0, false, DBL>(v, x, y, z, prm, partials, max_or, st);
+  }
+}
+
+void launch_apply_q(const OpView& v, bool has_double_bonds, const void* x, void* y, const void* z,
+                    const QParams* prm, double* partials, unsigned long long* max_or, int dots,
+                    cudaStream_t st) {
+  const size_t need = sizeof(uint32_t) * (size_t)((v.max_up_degree + 3) & ~3) +
+                      sizeof(longlong2) * (size_t)v.Dd + 2048;
+  const bool staged = need <= (size_t)smem_optin();
+  if (staged) {
+    if (has_double_bonds) q_apply_sel<true, true>(v, x, y, z, prm, partials, max_or, dots, st);
+    else q_apply_sel<true, false>(v, x, y, z, prm, partials, max_or, dots, st);
+  } else {
+    if (has_double_bonds) q_apply_sel<false, true>(v, x, y, z, prm, partials, max_or, dots, st);
+    else q_apply_sel<false, false>(v, x, y, z, prm, partials, max_or, dots, st);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Split apply for large sectors: the up hops read whole neighbour rows, and
+// with ~16 neighbours per row spread over the sector (the hop graph is an
+// expander) no row order keeps them in L2 -- the fused kernel re-reads each
+// row ~6x from DRAM.  So the apply runs as two streaming passes:
+//   K1 (rows):    S[r,:] = sum over down hops of +-x[r,c'] (exact int64),
+//                 the row staged in shared memory;
+//   K2 (columns): work items (column block b, row r) in b-major order, so
+//                 all CTAs sweep one 256-column slab of every row at a time
+//                 (D_up * 4 KB, L2-resident) and each neighbour segment
+//                 x[r',b] comes from L2; it adds the up hops to S and does
+//                 the 128-bit epilogue of the fused kernel.
+// DRAM: K1 reads x, writes S; K2 reads S, x (once, via L2), writes y.
+// ---------------------------------------------------------------------------
+constexpr int kK1Threads = 1024;
+constexpr int kK2Threads = 256;
+
+template <bool STAGED, bool DBL>
+__global__ void __launch_bounds__(kK1Threads, 1)
+k_q_down_rows(OpView v, const longlong2* __restrict__ x, longlong2* __restrict__ s_out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  longlong2* s_row = reinterpret_cast<longlong2*>(smem);
+  const int64_t Dd = v.Dd;
+  for (int64_t r = blockIdx.x; r < v.Du; r += gridDim.x) {
+    const longlong2* xrow = x + r * Dd;
+    if (STAGED) {
+      __syncthreads();
+      for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) s_row[c] = xrow[c];
+      __syncthreads();
+    }
+    for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) {
+      long long sr = 0, si = 0;
+      int negs = 0;
+      const int cnt = __ldg(&v.dn_cnt[c]);
+#pragma unroll 4
+      for (int j = 0; j < cnt; ++j) {
+        const uint32_t e = __ldg(&v.dn_ell[(int64_t)j * Dd + c]);
+        const longlong2 val = STAGED ? s_row[e >> 8] : __ldg(&xrow[e >> 8]);
+        const long long m = -(long long)(e & 1u);
+        long long tr = val.x ^ m, ti = val.y ^ m;
+        if (DBL && (e & 2u)) { tr = tr + tr + (m & 1); ti = ti + ti + (m & 1); }
+        sr += tr;
+        si += ti;
+        negs += (int)(e & 1u);
+      }
+      __stcs(&s_out[r * Dd + c], make_longlong2(sr + negs, si + negs));
+    }
+  }
+}
+
+// K1 with the down hops computed on the fly: no per-row table stream.
+// Shared memory: rank tables, bond masks, then the staged row.
+__device__ __forceinline__ int otf_rank(const int32_t* s_rank, uint32_t m, int nchunks,
+                                         int stride) {
+  int r = 0, cb = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (k < nchunks) {
+      const uint32_t byte = (m >> (8 * k)) & 0xFFu;
+      r += s_rank[(k * stride + cb) * 256 + (int)byte];
+      cb += __popc(byte);
+    }
+  }
+  return r;
+}
+
+static size_t otf_prefix_bytes(const OpView& v) {
+  return sizeof(int32_t) * (size_t)v.dn_nchunks * (size_t)(v.dn_n + 1) * 256 + 3 * 64 * sizeof(uint32_t);
+}
+
+template <bool DBL>
+__global__ void __launch_bounds__(kK1Threads, 1)
+k_q_down_rows_otf(OpView v, const longlong2* __restrict__ x, longlong2* __restrict__ s_out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int stride = v.dn_n + 1;
+  const int rank_words = v.dn_nchunks * stride * 256;
+  int32_t* s_rank = reinterpret_cast<int32_t*>(smem);
+  uint32_t* s_pair = reinterpret_cast<uint32_t*>(s_rank + rank_words);
+  uint32_t* s_betw = s_pair + 64;
+  uint32_t* s_mult = s_betw + 64;
+  longlong2* s_row = reinterpret_cast<longlong2*>(s_mult + 64);
+  for (int i = threadIdx.x; i < rank_words; i += blockDim.x) s_rank[i] = v.dn_rank[i];
+  for (int i = threadIdx.x; i < v.n_bonds; i += blockDim.x) {
+    s_pair[i] = v.bond_pair[i];
+    s_betw[i] = v.bond_between[i];
+    s_mult[i] = v.bond_mult[i];
+  }
+  const int64_t Dd = v.Dd;
+  const int nch = v.dn_nchunks;
+  for (int64_t r = blockIdx.x; r < v.Du; r += gridDim.x) {
+    const longlong2* xrow = x + r * Dd;
+    __syncthreads();
+    for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) s_row[c] = xrow[c];
+    __syncthreads();
+    for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) {
+      const uint32_t d = __ldg(&v.dn_mask[c]);
+      unsigned long long vm = __ldg(&v.dn_vmask[c]);
+      long long sr = 0, si = 0;
+      int negs = 0;
+      while (vm) {
+        const int bnd = __ffsll((long long)vm) - 1;
+        vm &= vm - 1ull;
+        const uint32_t d2 = d ^ s_pair[bnd];
+        const int neg = __popc(d & s_betw[bnd]) & 1;
+        const longlong2 val = s_row[otf_rank(s_rank, d2, nch, stride)];
+        const long long m = -(long long)neg;
+        long long tr = val.x ^ m, ti = val.y ^ m;
+        if (DBL && s_mult[bnd] == 2u) { tr = tr + tr + (m & 1); ti = ti + ti + (m & 1); }
+        sr += tr;
+        si += ti;
+        negs += neg;
+      }
+      __stcs(&s_out[r * Dd + c], make_longlong2(sr + negs, si + negs));
+    }
+  }
+}
+
+constexpr int kK2Cols = 2;  // columns per thread (two independent hop chains)
+
+template <int DOTS, bool HAS_Z, bool DBL>
+__global__ void __launch_bounds__(kK2Threads)
+k_q_up_cols(OpView v, const longlong2* __restrict__ x, const longlong2* __restrict__ s_in,
+            longlong2* y, const longlong2* z, const QParams* __restrict__ prm,
+            double* __restrict__ partials, unsigned long long* __restrict__ max_or) {
+  __shared__ long long s_cq[kMaxOrbitals + 1];
+  if (threadIdx.x <= (unsigned)v.L) s_cq[threadIdx.x] = prm->cq[threadIdx.x];
+  __syncthreads();
+  const long long c1 = prm->c1, c3 = prm->c3;
+  const int sh = prm->sh;
+  const int64_t Dd = v.Dd, Du = v.Du;
+  constexpr int W = kK2Threads * kK2Cols;
+  const int64_t nblk = (Dd + W - 1) / W;
+  const int64_t items = nblk * Du;
+  __int128 a_xy = 0, a_yy = 0;
+  unsigned long long mor = 0;
+  for (int64_t it = blockIdx.x; it < items; it += gridDim.x) {
+    const int64_t b = it / Du, r = it - b * Du;
+    const int64_t c0 = b * W + threadIdx.x;
+    const int u0 = __ldg(&v.up_off[r]), u1 = __ldg(&v.up_off[r + 1]);
+    const uint32_t um = __ldg(&v.up_mask[r]);
+    long long sr[kK2Cols], si[kK2Cols];
+    bool ok[kK2Cols];
+#pragma unroll
+    for (int q = 0; q < kK2Cols; ++q) {
+      const int64_t c = c0 + q * kK2Threads;
+      ok[q] = c < Dd;
+      const longlong2 s0 = ok[q] ? __ldcs(&s_in[r * Dd + c]) : make_longlong2(0, 0);
+      sr[q] = s0.x;
+      si[q] = s0.y;
+    }
+    int negs = 0;
+#pragma unroll 4
+    for (int j = u0; j < u1; ++j) {
+      const uint32_t e = __ldg(&v.up_ent[j]);
+      const longlong2* xr = x + (int64_t)(e >> 8) * Dd;
+      const long long m = -(long long)(e & 1u);
+#pragma unroll
+      for (int q = 0; q < kK2Cols; ++q) {
+        const longlong2 val = ok[q] ? __ldg(&xr[c0 + q * kK2Threads]) : make_longlong2(0, 0);
+        long long tr = val.x ^ m, ti = val.y ^ m;
+        if (DBL && (e & 2u)) { tr = tr + tr + (m & 1); ti = ti + ti + (m & 1); }
+        sr[q] += tr;
+        si[q] += ti;
+      }
+      negs += (int)(e & 1u);
+    }
+#pragma unroll
+    for (int q = 0; q < kK2Cols; ++q) {
+      if (!ok[q]) continue;
+      const int64_t c = c0 + q * kK2Threads;
+      const int64_t idx = r * Dd + c;
+      const long long srq = sr[q] + negs, siq = si[q] + negs;
+      const longlong2 xv = x[idx];
+      const long long dq = s_cq[__popc(um & __ldg(&v.dn_mask[c]))];
+      __int128 pr = (__int128)c1 * srq + (__int128)dq * xv.x;
+      __int128 pi = (__int128)c1 * siq + (__int128)dq * xv.y;
+      if (HAS_Z) {
+        const longlong2 zv = z[idx];
+        pr += (__int128)c3 * zv.x;
+        pi += (__int128)c3 * zv.y;
+      }
+      longlong2 out;
+      out.x = round_shift(pr, sh);
+      out.y = round_shift(pi, sh);
+      __stcs(&y[idx], out);  // streamed: keep the x slab resident in L2
+      if (DOTS & 1) a_xy += prod_hi(xv.x, out.x) + prod_hi(xv.y, out.y);
+      if (DOTS & 2) a_yy += prod_hi(out.x, out.x) + prod_hi(out.y, out.y);
+      if (DOTS & 4) mor |= mag(out.x) | mag(out.y);
+    }
+  }
+  if (DOTS) {
+    double vals[2] = {i128_to_f64(a_xy), i128_to_f64(a_yy)};
+    q_block_reduce<2>(vals, mor, partials, max_or);
+  }
+}
+
+static int q_split_grid() { return sm_count() * 8; }
+
+// Up-hop grid size used by the split apply (partials are per block).
+int q_apply_split_grid() { return q_split_grid(); }
+
+template <int DOTS, bool HAS_Z, bool DBL>
+static void q_split_t(const OpView& v, const void* x, void* y, const void* z, void* s_scratch,
+                      const QParams* prm, double* partials, unsigned long long* max_or,
+                      cudaStream_t st) {
+  const size_t row_bytes = sizeof(longlong2) * (size_t)v.Dd;
+  const bool staged = row_bytes + 2048 <= (size_t)smem_optin();
+  int g1 = sm_count();
+  if (g1 > v.Du) g1 = (int)v.Du;
+  const size_t otf_bytes = v.dn_vmask ? otf_prefix_bytes(v) + row_bytes : 0;
+  if (v.dn_vmask && otf_bytes + 1024 <= (size_t)smem_optin()) {
+    auto k1 = k_q_down_rows_otf<DBL>;
+    MB_CUDA(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)otf_bytes));
+    k1<<<g1, kK1Threads, otf_bytes, st>>>(v, (const longlong2*)x, (longlong2*)s_scratch);
+  } else if (staged) {
+    auto k1 = k_q_down_rows<true, DBL>;
+    MB_CUDA(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_bytes));
+    k1<<<g1, kK1Threads, row_bytes, st>>>(v, (const longlong2*)x, (longlong2*)s_scratch);
+  } else {
+    k_q_down_rows<false, DBL><<<g1, kK1Threads, 0, st>>>(v, (const longlong2*)x,
+                                                         (longlong2*)s_scratch);
+  }
+  MB_CUDA(cudaGetLastError());
+  k_q_up_cols<DOTS, HAS_Z, DBL><<<q_split_grid(), kK2Threads, 0, st>>>(
+      v, (const longlong2*)x, (const longlong2*)s_scratch, (longlong2*)y, (const longlong2*)z,
+      prm, partials, max_or);
+  MB_CUDA(cudaGetLastError());
+}
+
+template <bool DBL>
+static void q_split_sel(const OpView& v, const void* x, void* y, const void* z, void* s,
+                        const QParams* prm, double* partials, unsigned long long* max_or,
+                        int dots, cudaStream_t st) {
+  if (z) {
+    if (dots) q_split_t<7, true, DBL>(v, x, y, z, s, prm, partials, max_or, st);
+    else q_split_t<0, true, DBL>(v, x, y, z, s, prm, partials, max_or, st);
+  } else {
+    if (dots) q_split_t<7, false, DBL>(v, x, y, z, s, prm, partials, max_or, st);
+    else q_split_t<0, false, DBL>(v, x, y, z, s, prm, partials, max_or, st);
+  }
+}
+
+// Sectors at least this large use the split apply when scratch is given.
+constexpr int64_t kSplitMinDim = int64_t(1) << 22;
+
+// MB_APPLY_VARIANT=fused|split overrides the size rule (tuning knob).
+bool q_use_split(const OpView& v) {
+  static const int forced = [] {
+    const char* e = getenv("MB_APPLY_VARIANT");
+    if (!e) return -1;
+    if (!strcmp(e, "fused")) return 0;
+    if (!strcmp(e, "split")) return 1;
+    return -1;
+  }();
+  if (forced >= 0) return forced == 1;
+  // Measured on GB300 (4x4 and 1D L=16 sectors): the fused kernel is faster
+  // than the two-pass split at every size tried, so it is the default.
+  (void)v;
+  return false;
+}
+
+void launch_apply_q2(const OpView& v, bool has_double_bonds, const void* x, void* y,
+                     const void* z, void* s_scratch, const QParams* prm, double* partials,
+                     unsigned long long* max_or, int dots, cudaStream_t st) {
+  if (!s_scratch || !q_use_split(v)) {
+    launch_apply_q(v, has_double_bonds, x, y, z, prm, partials, max_or, dots, st);
+    return;
+  }
+  if (has_double_bonds) q_split_sel<true>(v, x, y, z, s_scratch, prm, partials, max_or, dots, st);
+  else q_split_sel<false>(v, x, y, z, s_scratch, prm, partials, max_or, dots, st);
+}
+
+int q_apply_grid_for(const OpView& v, bool split) {
+  return split ? q_split_grid() : q_apply_grid(v);
+}
+
+// ---------------------------------------------------------------------------
+// Parameter planning (host and device): fixed-point coefficients for
+// y = scale (H - shift) x + beta z given the exponents of x and z.
+// ---------------------------------------------------------------------------
+__host__ __device__ static int ceil_log2_pos(double v) {
+  // smallest k with v <= 2^k (v > 0)
+  int e;
+  const double m = frexp(v, &e);  // v = m * 2^e, m in [0.5, 1)
+  return (m == 0.5) ? e - 1 : e;
+}
+
+__host__ __device__ void q_plan(QParams* p, const QPlanInput& in) {
+  const double c1r = -in.t * in.scale;
+  double maxcq = 0.0;
+  for (int k = 0; k <= in.L; ++k) {
+    const double cq = in.scale * (in.ufold[k] - in.shift);
+    maxcq = fmax(maxcq, fabs(cq));
+  }
+  const double c3r = in.has_z ? in.beta * ldexp(1.0, in.ez - in.ex) : 0.0;
+  const double maxc = fmax(fmax(fabs(c1r), maxcq), fabs(c3r));
+  const double bound = fabs(c1r) * in.w_max + maxcq + fabs(c3r);
+  int G = 60;
+  if (maxc > 0.0) G = 61 - ceil_log2_pos(maxc);
+  int ey = in.ex;
+  if (bound > 0.0) ey = in.ex + ceil_log2_pos(bound);
+  p->c1 = llrint(ldexp(c1r, G));
+  for (int k = 0; k <= in.L; ++k) p->cq[k] = llrint(ldexp(in.scale * (in.ufold[k] - in.shift), G));
+  for (int k = in.L + 1; k <= kMaxOrbitals; ++k) p->cq[k] = 0;
+  p->c3 = in.has_z ? llrint(ldexp(c3r, G)) : 0;
+  p->G = G;
+  p->ex = in.ex;
+  p->ey = ey;
+  p->ez = in.ez;
+  p->sh = G + ey - in.ex;
+}
+
+// ---------------------------------------------------------------------------
+// Conversions, with optional permutation (reference <-> tensor order).
+// ---------------------------------------------------------------------------
+constexpr int kQBlas = 256;
+
+int q_blas_grid(int64_t n) {
+  int64_t g = (n + kQBlas - 1) / kQBlas;
+  const int64_t cap = (int64_t)sm_count() * 8;
+  if (g > cap) g = cap;
+  return (int)std::max<int64_t>(g, 1);
+}
+
+// max biased exponent over all components of a complex128 vector
+__global__ void k_f64_maxexp(int64_t n, const double2* __restrict__ x, int* __restrict__ out) {
+  int m = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = x[i];
+    const int ea = (int)(((unsigned long long)__double_as_longlong(v.x) >> 52) & 0x7FF);
+    const int eb = (int)(((unsigned long long)__double_as_longlong(v.y) >> 52) & 0x7FF);
+    m = max(m, max(ea, eb));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// Ex from the max biased exponent: |x| < 2^(emax - 1022) -> Ex = that - qbits.
+__global__ void k_exp_from_max(const int* __restrict__ emax, int qbits, int* __restrict__ ex) {
+  const int e = *emax;
+  *ex = (e == 0) ? -1074 : (e - 1022 - qbits);
+}
+
+__global__ void k_to_fixed(int64_t n, const double2* __restrict__ src, const int32_t* __restrict__ perm,
+                           const int* __restrict__ ex, longlong2* __restrict__ dst) {
+  const int E = *ex;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = src[perm ? (int64_t)perm[i] : i];
+    dst[i] = make_longlong2(f64_to_fixed(v.x, E), f64_to_fixed(v.y, E));
+  }
+}
+
+__global__ void k_from_fixed(int64_t n, const longlong2* __restrict__ src,
+                             const int32_t* __restrict__ perm, const int* __restrict__ ey,
+                             double2* __restrict__ dst) {
+  const int E = *ey;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const longlong2 q = src[i];
+    dst[perm ? (int64_t)perm[i] : i] = make_double2(fixed_to_f64(q.x, E), fixed_to_f64(q.y, E));
+  }
+}
+
+// One-thread planner on the device (keeps mb_op_apply asynchronous).
+__global__ void k_plan(QPlanInput in, const int* __restrict__ ex, QParams* __restrict__ p) {
+  in.ex = *ex;
+  in.ez = in.ex;
+  q_plan(p, in);
+}
+
+void launch_f64_to_q(int64_t n, const void* src, const int32_t* perm, int qbits, int* scratch_int2,
+                     void* dst, cudaStream_t st) {
+  MB_CUDA(cudaMemsetAsync(scratch_int2, 0, sizeof(int), st));
+  k_f64_maxexp<<<q_blas_grid(n), kQBlas, 0, st>>>(n, (const double2*)src, scratch_int2);
+  k_exp_from_max<<<1, 1, 0, st>>>(scratch_int2, qbits, scratch_int2 + 1);
+  k_to_fixed<<<q_blas_grid(n), kQBlas, 0, st>>>(n, (const double2*)src, perm, scratch_int2 + 1,
+                                                 (longlong2*)dst);
+  MB_CUDA(cudaGetLastError());
+}
+
+void launch_q_to_f64(int64_t n, const void* src, const int32_t* perm, const int* e_dev, void* dst,
+                     cudaStream_t st) {
+  k_from_fixed<<<q_blas_grid(n), kQBlas, 0, st>>>(n, (const longlong2*)src, perm, e_dev,
+                                                   (double2*)dst);
+  MB_CUDA(cudaGetLastError());
+}
+
+void launch_q_plan(const QPlanInput& in, const int* ex_dev, QParams* p_dev, cudaStream_t st) {
+  k_plan<<<1, 1, 0, st>>>(in, ex_dev, p_dev);
+  MB_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// Vector kernels on mantissas.
+//   out = round((A a + B b) / 2^sh), A, B complex fixed-point (re, im), b optional;
+//   partials: <out,out>>>32 ; max_or: OR of |out| components.
+// ---------------------------------------------------------------------------
+__global__ void k_q_lincomb(int64_t n, const longlong2* a, long long ar, long long ai,
+                            const longlong2* b, long long br, long long bi, int sh,
+                            longlong2* out, double* __restrict__ partials,
+                            unsigned long long* __restrict__ max_or) {
+  __int128 nn = 0;
+  unsigned long long mor = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const longlong2 va = a ? a[i] : make_longlong2(0, 0);
+    __int128 pr = (__int128)ar * va.x - (__int128)ai * va.y;
+    __int128 pi = (__int128)ar * va.y + (__int128)ai * va.x;
+    if (b) {
+      const longlong2 vb = b[i];
+      pr += (__int128)br * vb.x - (__int128)bi * vb.y;
+      pi += (__int128)br * vb.y + (__int128)bi * vb.x;
+    }
+    longlong2 o;
+    o.x = round_shift(pr, sh);
+    o.y = round_shift(pi, sh);
+    out[i] = o;
+    nn += prod_hi(o.x, o.x) + prod_hi(o.y, o.y);
+    mor |= mag(o.x) | mag(o.y);
+  }
+  if (partials || max_or) {
+    double vals[2] = {i128_to_f64(nn), 0.0};
+    q_block_reduce<2>(vals, mor, partials, max_or);
+  }
+}
+
+void launch_q_lincomb(int64_t n, const void* a, long long ar, long long ai, const void* b,
+                      long long br, long long bi, int sh, void* out, double* partials,
+                      unsigned long long* max_or, cudaStream_t st) {
+  k_q_lincomb<<<q_blas_grid(n), kQBlas, 0, st>>>(n, (const longlong2*)a, ar, ai,
+                                                 (const longlong2*)b, br, bi, sh,
+                                                 (longlong2*)out, partials, max_or);
+  MB_CUDA(cudaGetLastError());
+}
+
+// Re/Im <a, b> = sum conj(a) b as exact integer sums >> 32 -> partials[2].
+__global__ void k_q_dot(int64_t n, const longlong2* __restrict__ a, const longlong2* __restrict__ b,
+                        double* __restrict__ partials) {
+  __int128 re = 0, im = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const longlong2 u = a[i], w = b[i];
+    re += prod_hi(u.x, w.x) + prod_hi(u.y, w.y);
+    im += prod_hi(u.x, w.y) - prod_hi(u.y, w.x);
+  }
+  double vals[2] = {i128_to_f64(re), i128_to_f64(im)};
+  q_block_reduce<2>(vals, 0ull, partials, nullptr);
+}
+
+void launch_q_dot(int64_t n, const void* a, const void* b, double* partials, cudaStream_t st) {
+  k_q_dot<<<q_blas_grid(n), kQBlas, 0, st>>>(n, (const longlong2*)a, (const longlong2*)b, partials);
+  MB_CUDA(cudaGetLastError());
+}
+
+// Re-orthogonalisation against a stored basis of Q64 vectors V_j (exponents
+// per column).  c_j = <V_j, w> per block partials [blocks][2m].
+constexpr int kQmdChunk = 512;
+constexpr int kQmdThreads = 256;
+
+__global__ void __launch_bounds__(kQmdThreads)
+k_q_multi_dot(int64_t n, const longlong2* __restrict__ V, int64_t ld, int m,
+              const longlong2* __restrict__ w, double* __restrict__ partials) {
+  __shared__ double acc[2 * kQMaxBasis];
+  __shared__ longlong2 sw[kQmdChunk];
+  for (int j = threadIdx.x; j < 2 * m; j += blockDim.x) acc[j] = 0.0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int64_t base = (int64_t)blockIdx.x * kQmdChunk; base < n;
+       base += (int64_t)gridDim.x * kQmdChunk) {
+    const int len = (int)((n - base) < kQmdChunk ? (n - base) : kQmdChunk);
+    __syncthreads();
+    for (int i = threadIdx.x; i < len; i += blockDim.x) sw[i] = w[base + i];
+    __syncthreads();
+    for (int j = warp; j < m; j += nwarps) {
+      const longlong2* vj = V + (int64_t)j * ld + base;
+      __int128 cr = 0, ci = 0;
+      for (int i = lane; i < len; i += 32) {
+        const longlong2 a = vj[i], b = sw[i];
+        cr += prod_hi(a.x, b.x) + prod_hi(a.y, b.y);
+        ci += prod_hi(a.x, b.y) - prod_hi(a.y, b.x);
+      }
+      double dr = i128_to_f64(cr), di = i128_to_f64(ci);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        dr += __shfl_down_sync(0xffffffffu, dr, o);
+        di += __shfl_down_sync(0xffffffffu, di, o);
+      }
+      if (lane == 0) {
+        acc[2 * j] += dr;
+        acc[2 * j + 1] += di;
+      }
+    }
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < 2 * m; j += blockDim.x)
+    partials[(size_t)blockIdx.x * 2 * m + j] = acc[j];
+}
+
+int q_multi_dot_grid(int64_t n) {
+  int64_t g = (n + kQmdChunk - 1) / kQmdChunk;
+  const int64_t cap = (int64_t)sm_count() * 2;
+  if (g > cap) g = cap;
+  return (int)std::max<int64_t>(g, 1);
+}
+
+void launch_q_multi_dot(int64_t n, const void* V, int64_t ld, int m, const void* w,
+                        double* partials, cudaStream_t st) {
+  MB_REQUIRE(m <= kQMaxBasis, MB_ERR_CAPACITY, "re-orthogonalisation basis larger than 1024");
+  k_q_multi_dot<<<q_multi_dot_grid(n), kQmdThreads, 0, st>>>(n, (const longlong2*)V, ld, m,
+                                                             (const longlong2*)w, partials);
+  MB_CUDA(cudaGetLastError());
+}
+
+// w = round((w - sum_j c_j V_j) / 2^shw), c_j fixed point (re, im) at scale
+// 2^-G in w-mantissa units; the caller adds shw to w's exponent.
+__global__ void __launch_bounds__(kQBlas)
+k_q_multi_axpy(int64_t n, const longlong2* __restrict__ V, int64_t ld, int m,
+               const long long* __restrict__ c, int G, int shw, longlong2* __restrict__ w,
+               double* __restrict__ partials, unsigned long long* __restrict__ max_or) {
+  __shared__ long long sc[2 * kQMaxBasis];
+  for (int j = threadIdx.x; j < 2 * m; j += blockDim.x) sc[j] = c[j];
+  __syncthreads();
+  __int128 nn = 0;
+  unsigned long long mor = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const longlong2 wv = w[i];
+    __int128 sr = (__int128)wv.x << G, si = (__int128)wv.y << G;
+    for (int j = 0; j < m; ++j) {
+      const longlong2 a = V[(int64_t)j * ld + i];
+      const long long cr = sc[2 * j], ci = sc[2 * j + 1];
+      sr -= (__int128)cr * a.x - (__int128)ci * a.y;
+      si -= (__int128)cr * a.y + (__int128)ci * a.x;
+    }
+    longlong2 o;
+    o.x = round_shift(sr, G + shw);
+    o.y = round_shift(si, G + shw);
+    w[i] = o;
+    nn += prod_hi(o.x, o.x) + prod_hi(o.y, o.y);
+    mor |= mag(o.x) | mag(o.y);
+  }
+  double vals[2] = {i128_to_f64(nn), 0.0};
+  q_block_reduce<2>(vals, mor, partials, max_or);
+}
+
+void launch_q_multi_axpy(int64_t n, const void* V, int64_t ld, int m, const long long* c, int G,
+                         int shw, void* w, double* partials, unsigned long long* max_or,
+                         cudaStream_t st) {
+  MB_REQUIRE(m <= kQMaxBasis, MB_ERR_CAPACITY, "re-orthogonalisation basis larger than 1024");
+  k_q_multi_axpy<<<q_blas_grid(n), kQBlas, 0, st>>>(n, (const longlong2*)V, ld, m, c, G, shw,
+                                                    (longlong2*)w, partials, max_or);
+  MB_CUDA(cudaGetLastError());
+}
+
+}  // namespace mb

@@ -1,0 +1,554 @@
+// Drivers of block-floating-point (MB_PREC_Q64) operators: the FP64-in /
+// FP64-out apply, native Q64 entry points, and Lanczos / Krylov evolution
+// on Q64 vectors.  Exponent bookkeeping happens on the host between kernel
+// launches (the Lanczos loop reads alpha and beta every step anyway); the
+// stand-alone apply plans on the device so it stays asynchronous.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "mb_internal.h"
+#include "mb_q64.h"
+
+namespace mb {
+
+namespace {
+
+struct QBuf {
+  void* p = nullptr;
+  QBuf() = default;
+  explicit QBuf(size_t b) {
+    if (b) MB_CUDA(cudaMalloc(&p, b));
+  }
+  ~QBuf() {
+    if (p) cudaFree(p);
+  }
+  QBuf(const QBuf&) = delete;
+  QBuf& operator=(const QBuf&) = delete;
+  QBuf& operator=(QBuf&& o) noexcept {
+    std::swap(p, o.p);
+    return *this;
+  }
+};
+
+int ceil_log2(double v) {  // smallest k with v <= 2^k, v > 0
+  int e;
+  const double m = std::frexp(v, &e);
+  return m == 0.5 ? e - 1 : e;
+}
+
+}  // namespace
+
+void q_op_prepare(mb_op_s* op, const mb_model_s* m, const HopTable& tu, const HopTable& td) {
+  MB_REQUIRE(!tu.has_self && !td.has_self, MB_ERR_INVALID_ARG,
+             "MB_PREC_Q64 operators need a lattice without size-1 dimensions (self bonds); "
+             "use MB_PREC_F64");
+  auto wsum = [](const HopTable& t, int64_t D) {
+    double best = 0.0;
+    for (int64_t r = 0; r < D; ++r) {
+      double s = 0.0;
+      for (int32_t j = t.off[(size_t)r]; j < t.off[(size_t)r + 1]; ++j) s += (t.ent[(size_t)j] & 2u) ? 2.0 : 1.0;
+      best = std::max(best, s);
+    }
+    return best;
+  };
+  op->q_wmax = wsum(tu, op->Du) + wsum(td, op->Dd);
+  op->q_qbits = 62 - (op->q_wmax > 1.0 ? ceil_log2(op->q_wmax) : 0);
+  op->q_has_double = false;
+  for (const auto& b : m->bonds) op->q_has_double = op->q_has_double || b.mult == 2;
+  op->ufold_host = u_fold_table(m->u, m->has_u, op->L);
+}
+
+void q_op_release(mb_op_s* op) {
+  for (auto& kv : op->qscratch) {
+    for (void* p : {kv.second.xq, kv.second.yq, kv.second.sq, kv.second.prm, (void*)kv.second.ints})
+      if (p) cudaFree(p);
+  }
+  op->qscratch.clear();
+}
+
+static QPlanInput plan_input(const mb_op_s* op, double scale, double shift, double beta, int ex,
+                             int ez, bool has_z) {
+  QPlanInput in{};
+  in.t = op->t;
+  in.scale = scale;
+  in.shift = shift;
+  in.beta = beta;
+  for (int k = 0; k <= op->L; ++k) in.ufold[k] = op->ufold_host[(size_t)k];
+  in.w_max = op->q_wmax;
+  in.L = op->L;
+  in.ex = ex;
+  in.ez = ez;
+  in.has_z = has_z ? 1 : 0;
+  return in;
+}
+
+static mb_op_s::QScratch& qscratch_for(mb_op_s* op, cudaStream_t st) {
+  std::lock_guard<std::mutex> lk(op->mu);
+  auto& s = op->qscratch[st];
+  if (!s.xq) {
+    const size_t vb = sizeof(longlong2) * (size_t)op->dim;
+    MB_CUDA(cudaMalloc(&s.xq, vb));
+    MB_CUDA(cudaMalloc(&s.yq, vb));
+    if (q_use_split(op->view)) MB_CUDA(cudaMalloc(&s.sq, vb));
+    MB_CUDA(cudaMalloc(&s.prm, sizeof(QParams)));
+    MB_CUDA(cudaMalloc((void**)&s.ints, 4 * sizeof(int)));
+  }
+  return s;
+}
+
+// y = scale (H - shift) x + beta z on complex128 vectors through Q64.
+// z, when used, is folded in FP64 after the Q64 apply (z keeps its own
+// magnitude): y = Q64[scale (H - shift) x] + beta z.
+void q_apply_affine(mb_op_s* op, const void* x, void* y, double scale, double shift, double beta,
+                    const void* z, int order, cudaStream_t st) {
+  auto& s = qscratch_for(op, st);
+  int32_t* perm = order == MB_ORDER_REFERENCE ? op_perm(op) : nullptr;
+  launch_f64_to_q(op->dim, x, perm, op->q_qbits, s.ints, s.xq, st);
+  launch_q_plan(plan_input(op, scale, shift, 0.0, 0, 0, false), s.ints + 1, (QParams*)s.prm, st);
+  launch_apply_q2(op->view, op->q_has_double, s.xq, s.yq, nullptr, s.sq, (const QParams*)s.prm,
+                  nullptr, nullptr, 0, st);
+  // the output exponent sits in the planned QParams (field ey)
+  const int* ey = (const int*)((const char*)s.prm + offsetof(QParams, ey));
+  if (!z) {
+    launch_q_to_f64(op->dim, s.yq, perm, ey, y, st);
+    return;
+  }
+  // y = beta z + (Q64 result): z may alias y; convert into a tensor-order
+  // temporary, then combine with the FP64 vector kernel.
+  QBuf tmp(sizeof(double2) * (size_t)op->dim);
+  launch_q_to_f64(op->dim, s.yq, perm, ey, tmp.p, st);
+  launch_axpby(MB_PREC_F64, op->dim, beta, 0.0, z, 1.0, 0.0, tmp.p, nullptr, 0, st);
+  MB_CUDA(cudaMemcpyAsync(y, tmp.p, sizeof(double2) * (size_t)op->dim, cudaMemcpyDeviceToDevice, st));
+  MB_CUDA(cudaStreamSynchronize(st));
+}
+
+// ---------------------------------------------------------------------------
+// Q64 Krylov machinery.
+// ---------------------------------------------------------------------------
+namespace {
+
+// Non-owning view of a Q64 vector: mantissas, exponent, bound on max |q|.
+struct QRef {
+  void* p = nullptr;
+  int E = 0;
+  double maxq = 0.0;
+};
+
+struct QVec {
+  QBuf buf;
+  QRef r;
+  explicit QVec(int64_t n) : buf(sizeof(longlong2) * (size_t)n) { r.p = buf.p; }
+};
+
+struct QKrylov {
+  mb_op_s* op;
+  cudaStream_t st;
+  int64_t n;
+  int qbits;
+  QBuf partials, red_out, maxor, prm, sbuf;
+  double* host = nullptr;      // pinned: reduce outputs, then the max word
+  QParams* hprm = nullptr;     // pinned
+  int grid_apply, grid_blas, grid_md;
+  QBuf basis;                  // reorth basis: columns of n mantissas
+  int64_t basis_cap = 0;
+  std::vector<int> basis_E;
+  std::vector<double> basis_max;
+  QBuf coef;
+  long long* hcoef = nullptr;  // pinned
+
+  QKrylov(mb_op_s* o, cudaStream_t s)
+      : op(o), st(s), n(o->dim), qbits(o->q_qbits),
+        partials(sizeof(double) *
+                 (size_t)std::max(std::max(q_apply_grid_for(o->view, true), q_apply_grid(o->view)) * 2,
+                                  std::max(q_blas_grid(o->dim) * 2,
+                                           q_multi_dot_grid(o->dim) * 2 * kQMaxBasis))),
+        red_out(sizeof(double) * 2 * kQMaxBasis), maxor(sizeof(unsigned long long)),
+        prm(sizeof(QParams)),
+        sbuf(q_use_split(o->view) ? sizeof(longlong2) * (size_t)o->dim : 0),
+        grid_apply(q_apply_grid_for(o->view, q_use_split(o->view))), grid_blas(q_blas_grid(o->dim)),
+        grid_md(q_multi_dot_grid(o->dim)), coef(sizeof(long long) * 2 * kQMaxBasis) {
+    MB_CUDA(cudaMallocHost((void**)&host, sizeof(double) * (2 * kQMaxBasis + 8)));
+    MB_CUDA(cudaMallocHost((void**)&hprm, sizeof(QParams)));
+    MB_CUDA(cudaMallocHost((void**)&hcoef, sizeof(long long) * 2 * kQMaxBasis));
+  }
+  ~QKrylov() {
+    if (host) cudaFreeHost(host);
+    if (hprm) cudaFreeHost(hprm);
+    if (hcoef) cudaFreeHost(hcoef);
+  }
+
+  double* part() { return (double*)partials.p; }
+  unsigned long long* mor() { return (unsigned long long*)maxor.p; }
+  void zero_max() { MB_CUDA(cudaMemsetAsync(maxor.p, 0, sizeof(unsigned long long), st)); }
+
+  // Reduce partials (nblocks x ncomp) plus the max word; waits on the stream.
+  const double* fetch(int nblocks, int ncomp, double* maxq_out) {
+    launch_reduce(part(), nblocks, ncomp, (double*)red_out.p, st);
+    MB_CUDA(cudaMemcpyAsync(host, red_out.p, sizeof(double) * ncomp, cudaMemcpyDeviceToHost, st));
+    MB_CUDA(cudaMemcpyAsync(host + ncomp, maxor.p, sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, st));
+    MB_CUDA(cudaStreamSynchronize(st));
+    if (maxq_out) {
+      unsigned long long m;
+      std::memcpy(&m, host + ncomp, sizeof(m));
+      *maxq_out = m ? std::ldexp(1.0, 64 - __builtin_clzll(m)) : 0.0;  // max < 2^bitlen(OR)
+    }
+    return host;
+  }
+
+  // out = ca a + cb b (complex coefficients; out may alias a or b).  The
+  // output exponent comes from the bound |ca| max|a| + |cb| max|b|.
+  // Returns ||out||^2.
+  double lincomb(QRef& out, const QRef* a, std::complex<double> ca, const QRef* b,
+                 std::complex<double> cb) {
+    const double ba = a ? std::abs(ca) * std::ldexp(a->maxq, a->E) : 0.0;
+    const double bb = b ? std::abs(cb) * std::ldexp(b->maxq, b->E) : 0.0;
+    const double bound = (ba + bb) * (1.0 + 1e-12);
+    const int Eo = bound > 0.0 ? ceil_log2(bound) - qbits : (a ? a->E : (b ? b->E : 0));
+    double cmax = 0.0;
+    if (a) cmax = std::max(cmax, std::abs(ca) * std::ldexp(1.0, a->E - Eo));
+    if (b) cmax = std::max(cmax, std::abs(cb) * std::ldexp(1.0, b->E - Eo));
+    const int Gs = cmax > 0.0 ? std::min(61 - ceil_log2(cmax), 120) : 0;
+    auto fx = [&](double c, int E) -> long long { return std::llrint(std::ldexp(c, E - Eo + Gs)); };
+    long long ar = 0, ai = 0, br = 0, bi = 0;
+    if (a) { ar = fx(ca.real(), a->E); ai = fx(ca.imag(), a->E); }
+    if (b) { br = fx(cb.real(), b->E); bi = fx(cb.imag(), b->E); }
+    zero_max();
+    launch_q_lincomb(n, a ? a->p : nullptr, ar, ai, b ? b->p : nullptr, br, bi, Gs, out.p, part(),
+                     mor(), st);
+    double mq = 0.0;
+    const double* h = fetch(grid_blas, 2, &mq);
+    out.E = Eo;
+    out.maxq = std::max(mq, 1.0);
+    return h[0] * std::ldexp(1.0, 2 * Eo + 32);
+  }
+
+  // w = scale H v - beta_prev v_prev; returns (Re<v,w>, ||w||^2).
+  std::pair<double, double> apply(QRef& w, const QRef& v, double scale, double beta_prev,
+                                  const QRef* v_prev) {
+    const bool hz = v_prev && beta_prev != 0.0;
+    q_plan(hprm, plan_input(op, scale, 0.0, -beta_prev, v.E, hz ? v_prev->E : v.E, hz));
+    MB_CUDA(cudaMemcpyAsync(prm.p, hprm, sizeof(QParams), cudaMemcpyHostToDevice, st));
+    zero_max();
+    launch_apply_q2(op->view, op->q_has_double, v.p, w.p, hz ? v_prev->p : nullptr, sbuf.p,
+                    (const QParams*)prm.p, part(), mor(), 1, st);
+    double mq = 0.0;
+    const double* h = fetch(grid_apply, 2, &mq);
+    w.E = hprm->ey;
+    w.maxq = std::max(mq, 1.0);
+    return {h[0] * std::ldexp(1.0, v.E + w.E + 32), h[1] * std::ldexp(1.0, 2 * w.E + 32)};
+  }
+
+  void reserve_basis(int64_t k) {
+    size_t free_b = 0, total_b = 0;
+    MB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t need = (size_t)k * sizeof(longlong2) * (size_t)n;
+    MB_REQUIRE(need + (size_t)(512u << 20) < free_b, MB_ERR_OOM,
+               "Krylov basis for full re-orthogonalisation does not fit in device memory");
+    MB_REQUIRE(k <= kQMaxBasis, MB_ERR_CAPACITY, "re-orthogonalisation basis larger than 1024");
+    basis = QBuf(need);
+    basis_cap = k;
+  }
+
+  QRef column(int64_t j) const {
+    QRef r;
+    r.p = (char*)basis.p + sizeof(longlong2) * (size_t)n * (size_t)j;
+    r.E = basis_E[(size_t)j];
+    r.maxq = basis_max[(size_t)j];
+    return r;
+  }
+
+  void store_basis(const QRef& v) {
+    const int64_t j = (int64_t)basis_E.size();
+    MB_REQUIRE(j < basis_cap, MB_ERR_CAPACITY, "basis full");
+    MB_CUDA(cudaMemcpyAsync((char*)basis.p + sizeof(longlong2) * (size_t)n * (size_t)j, v.p,
+                            sizeof(longlong2) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    basis_E.push_back(v.E);
+    basis_max.push_back(v.maxq);
+  }
+
+  // Classical Gram-Schmidt, twice: w -= V (V^H w).  Returns ||w||^2.
+  double reorth(QRef& w) {
+    const int m = (int)basis_E.size();
+    double nrm2 = 0.0;
+    for (int pass = 0; pass < 2; ++pass) {
+      launch_q_multi_dot(n, basis.p, n, m, w.p, part(), st);
+      const double* h = fetch(grid_md, 2 * m, nullptr);
+      std::vector<std::complex<double>> c((size_t)m);
+      double bmant = w.maxq;  // bound of the result in w-mantissa units
+      for (int j = 0; j < m; ++j) {
+        const double s = std::ldexp(1.0, basis_E[(size_t)j] + w.E + 32);
+        c[(size_t)j] = {h[2 * j] * s, h[2 * j + 1] * s};
+        bmant += std::abs(c[(size_t)j]) * std::ldexp(basis_max[(size_t)j], basis_E[(size_t)j] - w.E);
+      }
+      const int shw = std::max(0, ceil_log2(bmant * (1.0 + 1e-12)) - qbits);
+      const int G = std::max(0, std::min(62, 124 - ceil_log2(std::max(bmant, 1.0))));
+      for (int j = 0; j < m; ++j) {
+        hcoef[2 * j] = std::llrint(std::ldexp(c[(size_t)j].real(), basis_E[(size_t)j] - w.E + G));
+        hcoef[2 * j + 1] = std::llrint(std::ldexp(c[(size_t)j].imag(), basis_E[(size_t)j] - w.E + G));
+      }
+      MB_CUDA(cudaMemcpyAsync(coef.p, hcoef, sizeof(long long) * 2 * (size_t)m,
+                              cudaMemcpyHostToDevice, st));
+      zero_max();
+      launch_q_multi_axpy(n, basis.p, n, m, (const long long*)coef.p, G, shw, w.p, part(), mor(), st);
+      double mq = 0.0;
+      const double* h2 = fetch(grid_blas, 2, &mq);
+      w.E += shw;
+      w.maxq = std::max(mq, 1.0);
+      nrm2 = h2[0] * std::ldexp(1.0, 2 * w.E + 32);
+    }
+    return nrm2;
+  }
+
+  // Pass one from b (Q64, tensor order) (lanczos.h:130-175).
+  int64_t pass_one(const QRef& b, double b_norm, int64_t k, double scale,
+                   std::vector<double>& alphas, std::vector<double>& betas, bool reorth_on,
+                   double conv_tol, int check_every, QRef* vp, QRef* vc, QRef* ww) {
+    alphas.clear();
+    betas.clear();
+    if (k == 0) return 0;
+    lincomb(*vc, &b, 1.0 / b_norm, nullptr, 0.0);
+    double beta_prev = 0.0;
+    int64_t steps = 0;
+    double last_ritz = 0.0;
+    bool have_ritz = false;
+    for (int64_t it = 0; it < k; ++it) {
+      if (reorth_on) store_basis(*vc);
+      const double alpha = apply(*ww, *vc, scale, beta_prev, beta_prev != 0.0 ? vp : nullptr).first;
+      QRef wv = *ww;
+      double nrm2 = lincomb(*ww, vc, -alpha, &wv, 1.0);  // w -= alpha v
+      if (reorth_on) nrm2 = reorth(*ww);
+      const double beta = std::sqrt(nrm2);
+      alphas.push_back(alpha);
+      steps += 1;
+      if (beta <= kTol) break;
+      if (it + 1 < k) betas.push_back(beta);
+      std::swap(vp, vc);  // v_prev <- v
+      std::swap(vc, ww);  // v <- w / beta
+      QRef cur = *vc;
+      lincomb(*vc, &cur, 1.0 / beta, nullptr, 0.0);
+      beta_prev = beta;
+      if (conv_tol > 0.0 && check_every > 0 && (steps % check_every) == 0 && it + 1 < k) {
+        std::vector<double> d(alphas), e(betas);
+        e.resize(d.size() - 1);
+        if (tridiag_eig((int)d.size(), d, e, nullptr)) {
+          const double ritz = d.back();
+          if (have_ritz && std::fabs(ritz - last_ritz) <= conv_tol * std::fabs(ritz)) {
+            betas.resize((size_t)steps - 1);
+            break;
+          }
+          last_ritz = ritz;
+          have_ritz = true;
+        }
+      }
+    }
+    if ((int64_t)betas.size() > std::max<int64_t>(steps - 1, 0)) betas.resize((size_t)steps - 1);
+    return steps;
+  }
+
+  // x = sum_j y_j v_j by re-running the recurrence (lanczos.h:177-218).
+  void pass_two(const QRef& b, double b_norm, int64_t steps, double scale,
+                const std::vector<double>& alphas, const std::vector<double>& betas,
+                const std::vector<std::complex<double>>& y, QRef& x, QRef* vp, QRef* vc,
+                QRef* ww) {
+    lincomb(*vc, &b, 1.0 / b_norm, nullptr, 0.0);
+    lincomb(x, vc, y[0], nullptr, 0.0);
+    for (int64_t j = 0; j + 1 < steps; ++j) {
+      const double beta_prev = j == 0 ? 0.0 : betas[(size_t)j - 1];
+      apply(*ww, *vc, scale, beta_prev, beta_prev != 0.0 ? vp : nullptr);
+      QRef wv = *ww;
+      lincomb(*ww, vc, -alphas[(size_t)j] / betas[(size_t)j], &wv, 1.0 / betas[(size_t)j]);
+      QRef xv = x;
+      lincomb(x, &xv, 1.0, ww, y[(size_t)j + 1]);
+      std::swap(vp, vc);
+      std::swap(vc, ww);
+    }
+  }
+
+  // x = sum_j y_j V_j from the stored basis.
+  void combine_basis(int64_t steps, const std::vector<std::complex<double>>& y, QRef& x) {
+    for (int64_t j = 0; j < steps; ++j) {
+      const QRef vj = column(j);
+      if (j == 0) {
+        lincomb(x, &vj, y[0], nullptr, 0.0);
+      } else {
+        QRef xv = x;
+        lincomb(x, &xv, 1.0, &vj, y[(size_t)j]);
+      }
+    }
+  }
+
+  // complex128 (order) -> Q64 tensor order; returns ||b||.
+  double load(const void* src, int order, QRef& out) {
+    int32_t* perm = order == MB_ORDER_REFERENCE ? op_perm(op) : nullptr;
+    QBuf ints(4 * sizeof(int));
+    launch_f64_to_q(n, src, perm, qbits, (int*)ints.p, out.p, st);
+    int hE[2];
+    MB_CUDA(cudaMemcpyAsync(hE, ints.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    MB_CUDA(cudaStreamSynchronize(st));
+    out.E = hE[1];
+    out.maxq = std::ldexp(1.0, qbits);
+    launch_q_dot(n, out.p, out.p, part(), st);
+    const double* h = fetch(grid_blas, 2, nullptr);
+    return std::sqrt(h[0] * std::ldexp(1.0, 2 * out.E + 32));
+  }
+
+  void store(const QRef& x, int order, void* dst) {
+    int32_t* perm = order == MB_ORDER_REFERENCE ? op_perm(op) : nullptr;
+    QBuf e(sizeof(int));
+    MB_CUDA(cudaMemcpyAsync(e.p, &x.E, sizeof(int), cudaMemcpyHostToDevice, st));
+    launch_q_to_f64(n, x.p, perm, (const int*)e.p, dst, st);
+    MB_CUDA(cudaStreamSynchronize(st));
+  }
+};
+
+}  // namespace
+
+void q_eigenpair(mb_op_s* op, int64_t k, const void* seed, int order, const mb_lanczos_opts* opts,
+                 double sign, double* e_out, void* vec, int64_t* steps_out) {
+  MB_REQUIRE(k >= 0, MB_ERR_INVALID_ARG, "k must be >= 0");
+  mb_lanczos_opts o{};
+  o.basis_precision = -1;
+  o.check_every = 10;
+  if (opts) o = *opts;
+  if (o.check_every <= 0) o.check_every = 10;
+  cudaStream_t st = 0;
+  QKrylov kr(op, st);
+  const int64_t n = op->dim;
+  QVec b(n), vp(n), vc(n), w(n);
+  const double b_norm = kr.load(seed, order, b.r);
+  MB_REQUIRE(b_norm > kTol, MB_ERR_ZERO_NORM, "Input vector has zero norm");
+  const bool reorth = o.reorth != 0 && k > 0;
+  if (reorth) kr.reserve_basis(k);
+  std::vector<double> alphas, betas;
+  const int64_t m = kr.pass_one(b.r, b_norm, k, sign, alphas, betas, reorth, o.conv_tol,
+                                o.check_every, &vp.r, &vc.r, &w.r);
+  if (steps_out) *steps_out = m;
+  if (m == 0) {
+    *e_out = 0.0;
+    if (vec) MB_CUDA(cudaMemset(vec, 0, sizeof(double2) * (size_t)n));
+    return;
+  }
+  std::vector<double> d(alphas), z, e(betas);
+  e.resize((size_t)m - 1);
+  MB_REQUIRE(tridiag_eig((int)m, d, e, &z), MB_ERR_EIG_FAILED,
+             "Eigenvalue decomposition of T_k failed");
+  *e_out = sign * d[(size_t)m - 1];
+  if (vec) {
+    std::vector<std::complex<double>> y((size_t)m);
+    for (int64_t i = 0; i < m; ++i) y[(size_t)i] = z[(size_t)(m - 1) * m + i] * b_norm;
+    QVec x(n);
+    if (reorth) kr.combine_basis(m, y, x.r);
+    else kr.pass_two(b.r, b_norm, m, sign, alphas, betas, y, x.r, &vp.r, &vc.r, &w.r);
+    kr.store(x.r, order, vec);
+  }
+}
+
+void q_evolve(mb_op_s* op, const void* psi0, int order, double t, int64_t krylov_steps,
+              int imaginary, void* out) {
+  cudaStream_t st = 0;
+  QKrylov kr(op, st);
+  const int64_t n = op->dim;
+  QVec b(n), vp(n), vc(n), w(n);
+  const double psi_norm = kr.load(psi0, order, b.r);
+  if (psi_norm <= kTol) {
+    if (out != psi0) MB_CUDA(cudaMemcpy(out, psi0, sizeof(double2) * (size_t)n, cudaMemcpyDeviceToDevice));
+    return;
+  }
+  int64_t k = krylov_steps <= 0 ? 30 : krylov_steps;
+  if (k > n) k = n;
+  std::vector<double> alphas, betas;
+  const int64_t m = kr.pass_one(b.r, psi_norm, k, 1.0, alphas, betas, false, 0.0, 0, &vp.r,
+                                &vc.r, &w.r);
+  std::vector<double> d(alphas), z, e(betas);
+  e.resize((size_t)std::max<int64_t>(m - 1, 0));
+  MB_REQUIRE(tridiag_eig((int)m, d, e, &z), MB_ERR_EIG_FAILED,
+             "Eigenvalue decomposition of T_k failed");
+  std::vector<std::complex<double>> y((size_t)m);
+  for (int64_t i = 0; i < m; ++i) {
+    std::complex<double> s = 0.0;
+    for (int64_t j = 0; j < m; ++j) {
+      const std::complex<double> ex =
+          imaginary ? std::complex<double>(std::exp(-t * d[(size_t)j]), 0.0)
+                    : std::exp(std::complex<double>(0.0, -t * d[(size_t)j]));
+      s += z[(size_t)j * m + i] * ex * z[(size_t)j * m + 0];
+    }
+    y[(size_t)i] = s * psi_norm;
+  }
+  QVec x(n);
+  kr.pass_two(b.r, psi_norm, m, 1.0, alphas, betas, y, x.r, &vp.r, &vc.r, &w.r);
+  kr.store(x.r, order, out);
+}
+
+}  // namespace mb
+
+using namespace mb;
+
+extern "C" {
+
+int mb_q64_from_f64(mb_op_t op, const void* x_dev, int order, void* xq_dev, int* exponent,
+                    void* stream) {
+  return guard([&] {
+    MB_REQUIRE(op && x_dev && xq_dev && exponent, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(op->precision == MB_PREC_Q64, MB_ERR_INVALID_ARG, "operator is not MB_PREC_Q64");
+    MB_REQUIRE(order == MB_ORDER_REFERENCE || order == MB_ORDER_TENSOR, MB_ERR_INVALID_ARG,
+               "bad order");
+    cudaStream_t st = (cudaStream_t)stream;
+    int32_t* perm = order == MB_ORDER_REFERENCE ? op_perm(op) : nullptr;
+    QBuf ints(4 * sizeof(int));
+    launch_f64_to_q(op->dim, x_dev, perm, op->q_qbits, (int*)ints.p, xq_dev, st);
+    int h[2];
+    MB_CUDA(cudaMemcpyAsync(h, ints.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    MB_CUDA(cudaStreamSynchronize(st));
+    *exponent = h[1];
+  });
+}
+
+int mb_q64_to_f64(mb_op_t op, const void* xq_dev, int exponent, int order, void* x_dev,
+                  void* stream) {
+  return guard([&] {
+    MB_REQUIRE(op && x_dev && xq_dev, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(order == MB_ORDER_REFERENCE || order == MB_ORDER_TENSOR, MB_ERR_INVALID_ARG,
+               "bad order");
+    cudaStream_t st = (cudaStream_t)stream;
+    int32_t* perm = order == MB_ORDER_REFERENCE ? op_perm(op) : nullptr;
+    QBuf e(sizeof(int));
+    MB_CUDA(cudaMemcpyAsync(e.p, &exponent, sizeof(int), cudaMemcpyHostToDevice, st));
+    launch_q_to_f64(op->dim, xq_dev, perm, (const int*)e.p, x_dev, st);
+    MB_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+int mb_op_apply_q64(mb_op_t op, const void* xq_dev, int x_exponent, void* yq_dev,
+                    int* y_exponent, void* stream) {
+  return guard([&] {
+    MB_REQUIRE(op && xq_dev && yq_dev && y_exponent, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(op->precision == MB_PREC_Q64, MB_ERR_INVALID_ARG, "operator is not MB_PREC_Q64");
+    MB_REQUIRE(xq_dev != yq_dev, MB_ERR_INVALID_ARG, "x and y must not overlap");
+    cudaStream_t st = (cudaStream_t)stream;
+    auto& s = qscratch_for(op, st);
+    QParams p{};
+    q_plan(&p, plan_input(op, 1.0, 0.0, 0.0, x_exponent, x_exponent, false));
+    // a plan per call: the parameter block lives in per-stream scratch, and
+    // the copy is ordered before the kernel on the same stream.
+    MB_CUDA(cudaMemcpyAsync(s.prm, &p, sizeof(QParams), cudaMemcpyHostToDevice, st));
+    launch_apply_q2(op->view, op->q_has_double, xq_dev, yq_dev, nullptr, s.sq,
+                    (const QParams*)s.prm, nullptr, nullptr, 0, st);
+    *y_exponent = p.ey;
+  });
+}
+
+int mb_q64_mantissa_bits(mb_op_t op, int* bits) {
+  return guard([&] {
+    MB_REQUIRE(op && bits, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(op->precision == MB_PREC_Q64, MB_ERR_INVALID_ARG, "operator is not MB_PREC_Q64");
+    *bits = op->q_qbits;
+  });
+}
+
+}  // extern "C"

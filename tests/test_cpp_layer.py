@@ -1,0 +1,31 @@
+"""The header-only C++ layer compiles against the C ABI and behaves like the
+reference's FermionBasis / HubbardModel / LinearOperator surface."""
+import os
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+SRC = os.path.join(ROOT, "tests", "cpp", "hpp_check.cpp")
+
+
+@pytest.fixture(scope="module")
+def hpp_binary(tmp_path_factory, mb):
+    out = str(tmp_path_factory.mktemp("cpp") / "hpp_check")
+    libdir = os.path.dirname(mb.LIB_PATH)
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"),
+                    SRC, "-L", libdir, "-lmanybody_gb300", f"-Wl,-rpath,{libdir}", "-o", out],
+                   check=True)
+    return out
+
+
+def test_cpp_layer_host(hpp_binary):
+    r = subprocess.run([hpp_binary, "host"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+@pytest.mark.gpu
+def test_cpp_layer_gpu(hpp_binary, cuda):
+    r = subprocess.run([hpp_binary, "gpu"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
