@@ -248,6 +248,50 @@ int mb_q64_to_f64(mb_op_t op, const void* xq_dev, int exponent, int order, void*
 int mb_op_apply_q64(mb_op_t op, const void* xq_dev, int x_exponent, void* yq_dev,
                     int* y_exponent, void* stream);
 
+/* ---- batched / served solves ------------------------------------------------ *
+ * An engine advances many independent sectors of uneven size together: one
+ * Lanczos step of every active request per engine step, complex64 vectors with
+ * FP64 alpha/beta, an optional replay pass that rebuilds the Ritz vector and
+ * an FP64 Rayleigh-quotient refinement of the energy.  Requests are admitted
+ * while the device-memory budget allows and retire when converged, so new
+ * requests join while others run.  No counterpart in the reference (its
+ * closest analogue are the OpenMP sample loops over independent vectors,
+ * examples/hubbard_momentum_optical_conductivity.cpp:351-400). */
+typedef struct mb_engine_s* mb_engine_t;
+typedef struct {
+  int64_t dims[3]; /* lattice sizes (periodic), as mb_hubbard_create */
+  int ndim;
+  int n_up, n_down;
+  double t, u;
+} mb_sector_desc;
+/* device_bytes_budget <= 0: 80 % of the free device memory. */
+int mb_engine_create(int64_t device_bytes_budget, mb_engine_t* out);
+int mb_engine_destroy(mb_engine_t engine);
+/* Device bytes a request of this sector holds while active. */
+int mb_engine_footprint(const mb_sector_desc* desc, int64_t* bytes);
+/* Ground state of one sector: Lanczos on -H from the Philox start vector of
+ * `seed` (tensor order), until the lowest Ritz value changes by less than
+ * rel_tol * |E| between checks (every 10 steps; rel_tol 0: run kmax steps),
+ * at most kmax <= 512 steps; refine = 1 adds the replay pass and the FP64
+ * Rayleigh quotient.  MB_ERR_CAPACITY when the budget is full (retry after
+ * mb_engine_step retires requests). */
+int mb_engine_submit_ground_state(mb_engine_t engine, const mb_sector_desc* desc, uint64_t seed,
+                                  int64_t kmax, double rel_tol, int refine, int64_t* request_id);
+/* Run up to n_steps engine steps; *n_active = requests still running. */
+int mb_engine_step(mb_engine_t engine, int n_steps, int* n_active);
+/* *done = 1 once the request finished: energy (refined if asked), the
+ * unrefined Ritz value, Lanczos steps and submit-to-finish seconds. */
+int mb_engine_poll(mb_engine_t engine, int64_t request_id, int* done, double* e0, double* e0_raw,
+                   int64_t* steps, double* latency_s);
+/* Warps per block of the grouped kernels (2, 4, 8, 16): the autotuner's knob. */
+int mb_engine_set_warps(mb_engine_t engine, int warps_per_block);
+/* Times the grouped apply at each block shape on the current requests and
+ * keeps the fastest; *chosen = warps per block, *ms = its time per apply. */
+int mb_engine_autotune(mb_engine_t engine, int* chosen, double* ms);
+/* n_steps steps with no host round trip between them (fixed-length batches),
+ * optionally as one captured CUDA graph replayed n_steps times. */
+int mb_engine_step_fixed(mb_engine_t engine, int n_steps, int use_graph, int* n_active);
+
 /* ---- block reductions on device vectors (for drivers above this ABI) ---- */
 /* *out = Re <x, y> (arma::cdot real part), FP64 accumulation, deterministic. */
 int mb_dot_re(mb_op_t op, const void* x_dev, const void* y_dev, double* out);

@@ -63,6 +63,11 @@ _dp = C.POINTER(C.c_double)
 _vp = C.c_void_p
 
 
+class SectorDesc(C.Structure):
+    _fields_ = [("dims", C.c_int64 * 3), ("ndim", C.c_int), ("n_up", C.c_int), ("n_down", C.c_int),
+                ("t", C.c_double), ("u", C.c_double)]
+
+
 class LanczosOpts(C.Structure):
     _fields_ = [("reorth", C.c_int), ("basis_precision", C.c_int), ("conv_tol", C.c_double),
                 ("check_every", C.c_int), ("refine", C.c_int)]
@@ -120,6 +125,16 @@ SIGNATURES = {
     "mb_q64_from_f64": (C.c_int, [_vp, _vp, C.c_int, _vp, C.POINTER(C.c_int), _vp]),
     "mb_q64_to_f64": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _vp, _vp]),
     "mb_op_apply_q64": (C.c_int, [_vp, _vp, C.c_int, _vp, C.POINTER(C.c_int), _vp]),
+    "mb_engine_create": (C.c_int, [_i64, C.POINTER(_vp)]),
+    "mb_engine_destroy": (C.c_int, [_vp]),
+    "mb_engine_footprint": (C.c_int, [C.POINTER(SectorDesc), _i64p]),
+    "mb_engine_submit_ground_state": (C.c_int, [_vp, C.POINTER(SectorDesc), C.c_uint64, _i64,
+                                                C.c_double, C.c_int, _i64p]),
+    "mb_engine_step": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
+    "mb_engine_step_fixed": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "mb_engine_poll": (C.c_int, [_vp, _i64, C.POINTER(C.c_int), _dp, _dp, _i64p, _dp]),
+    "mb_engine_set_warps": (C.c_int, [_vp, C.c_int]),
+    "mb_engine_autotune": (C.c_int, [_vp, C.POINTER(C.c_int), _dp]),
     "mb_dot_re": (C.c_int, [_vp, _vp, _vp, _dp]),
     "mb_norm": (C.c_int, [_vp, _vp, _dp]),
 }
@@ -590,3 +605,100 @@ def estimate_bounds(op: GpuHubbardOperator, power_iterations: int, spectral_padd
     _check(lib().mb_estimate_bounds(op.handle, power_iterations, spectral_padding, seed,
                                     C.byref(lo), C.byref(hi)))
     return lo.value, hi.value
+
+
+# ---------------------------------------------------------------------------
+# Batched / served ground states (mb_engine_*).
+# ---------------------------------------------------------------------------
+def sector(dims, n_up, n_down, t=1.0, u=0.0) -> SectorDesc:
+    d = SectorDesc()
+    dims = list(dims)
+    for i, v in enumerate(dims):
+        d.dims[i] = int(v)
+    d.ndim = len(dims)
+    d.n_up, d.n_down, d.t, d.u = int(n_up), int(n_down), float(t), float(u)
+    return d
+
+
+@dataclass
+class EngineResult:
+    e0: float
+    e0_raw: float
+    steps: int
+    latency_s: float
+
+
+class Engine:
+    """Many independent sectors advanced together (continuous batching)."""
+
+    def __init__(self, device_bytes_budget: int = 0):
+        h = C.c_void_p()
+        _check(lib().mb_engine_create(device_bytes_budget, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.mb_engine_destroy(self._h)
+            self._h = None
+
+    @staticmethod
+    def footprint(desc: SectorDesc) -> int:
+        b = C.c_int64()
+        _check(lib().mb_engine_footprint(C.byref(desc), C.byref(b)))
+        return b.value
+
+    def try_submit(self, desc: SectorDesc, seed: int = 0, kmax: int = 200, rel_tol: float = 0.0,
+                   refine: bool = True):
+        """Request id, or None when the device-memory budget is full."""
+        rid = C.c_int64()
+        rc = lib().mb_engine_submit_ground_state(self._h, C.byref(desc), seed, kmax, rel_tol,
+                                                 int(refine), C.byref(rid))
+        if rc == MB_ERR_CAPACITY:
+            return None
+        _check(rc)
+        return rid.value
+
+    def step(self, n: int = 1) -> int:
+        a = C.c_int()
+        _check(lib().mb_engine_step(self._h, n, C.byref(a)))
+        return a.value
+
+    def step_fixed(self, n: int, use_graph: bool = True) -> int:
+        a = C.c_int()
+        _check(lib().mb_engine_step_fixed(self._h, n, int(use_graph), C.byref(a)))
+        return a.value
+
+    def poll(self, rid: int):
+        done = C.c_int()
+        e0, er, lat = C.c_double(), C.c_double(), C.c_double()
+        st = C.c_int64()
+        _check(lib().mb_engine_poll(self._h, rid, C.byref(done), C.byref(e0), C.byref(er),
+                                    C.byref(st), C.byref(lat)))
+        return EngineResult(e0.value, er.value, st.value, lat.value) if done.value else None
+
+    def set_warps(self, w: int):
+        _check(lib().mb_engine_set_warps(self._h, w))
+
+    def autotune(self):
+        w, ms = C.c_int(), C.c_double()
+        _check(lib().mb_engine_autotune(self._h, C.byref(w), C.byref(ms)))
+        return w.value, ms.value
+
+
+def batch_ground_states(descs, seeds=None, kmax: int = 150, refine: bool = True,
+                        use_graph: bool = True, autotune: bool = True):
+    """Fixed-length batched Lanczos for many sectors: returns [EngineResult]."""
+    eng = Engine()
+    seeds = seeds if seeds is not None else [0] * len(descs)
+    ids = []
+    for d, s in zip(descs, seeds):
+        rid = eng.try_submit(d, s, kmax, 0.0, refine)
+        if rid is None:
+            raise MbError(MB_ERR_CAPACITY, "batch does not fit the device-memory budget")
+        ids.append(rid)
+    if autotune:
+        eng.autotune()
+    eng.step_fixed(kmax, use_graph)           # pass one (all requests, kmax steps)
+    while eng.step_fixed(kmax, use_graph):    # replay + refinement
+        pass
+    return [eng.poll(i) for i in ids]

@@ -1,0 +1,974 @@
+// Batched / served solver engine: many independent Hubbard sectors of uneven
+// size advanced together, one Lanczos (or Chebyshev) step of every active
+// slot per engine step.
+//
+// Layout.  A slot owns FP32 complex vectors (three rotating Lanczos buffers
+// and a Ritz accumulator) and per-step FP64 alpha/beta arrays, all on the
+// device; sector tables (masks, hop tables) are shared by every slot with the
+// same lattice and filling.  A step is a fixed sequence of grouped kernels
+// over a flat work list of (slot, row r_up) items -- one warp per item, so
+// sectors from 3k to 12M states mix in one launch -- and per-slot fixed-order
+// reductions (deterministic: a slot's result does not depend on what else
+// runs).  alpha and beta never leave the device inside a step, so a fixed
+// batch is captured once as a CUDA graph and replayed; the serving loop
+// instead reads alpha/beta after each step to test convergence and to admit
+// and retire requests.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "mb_internal.h"
+
+namespace mb {
+
+constexpr int kEngMaxK = 512;  // Lanczos steps a slot can record
+
+// Device descriptor of one slot (POD).
+struct SlotDesc {
+  const uint32_t* up_mask;
+  const uint32_t* dn_mask;
+  const int32_t* up_off;
+  const uint32_t* up_ent;
+  const int32_t* dn_off;
+  const uint32_t* dn_ent;
+  int64_t Du, Dd;
+  float2* buf[3];   // Lanczos vectors: v_prev = buf[k%3], v = buf[(k+1)%3], w = buf[(k+2)%3]
+  float2* xacc;     // Ritz vector accumulator (replay pass)
+  double* alpha;    // [kEngMaxK]
+  double* beta;     // [kEngMaxK]
+  double* yk;       // Ritz coefficients for the replay pass [kEngMaxK]
+  float ufold[kMaxOrbitals + 1];
+  float t;
+  float scale;      // -1: Negated H (ground state), +1: H
+  int kmax;         // pass one: steps to run at most
+  int k;            // this slot's step counter
+  int mode;         // kModeIdle, kModeLanczos, kModeReplay
+  int steps;        // pass-one steps taken (m)
+  int item0, item1; // this slot's range of work items
+};
+
+constexpr int kModeIdle = 0;
+constexpr int kModeLanczos = 1;
+constexpr int kModeReplay = 2;
+
+// ---------------------------------------------------------------------------
+// Kernels.  One warp per (slot, row) item; lanes stride over the row.
+// ---------------------------------------------------------------------------
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+k_eng_apply(const SlotDesc* __restrict__ slots, const int2* __restrict__ items, int n_items,
+            double* __restrict__ part) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int it = blockIdx.x * WARPS + warp; it < n_items; it += gridDim.x * WARPS) {
+    const int2 item = items[it];
+    const SlotDesc& s = slots[item.x];
+    const int k = s.k;
+    const bool replay = s.mode == kModeReplay;
+    double dxy = 0.0;
+    if ((s.mode == kModeLanczos && k < s.kmax) || (replay && k + 1 < s.steps)) {
+      const int64_t r = item.y, Dd = s.Dd;
+      const float2* v = s.buf[(k + 1) % 3] + r * Dd;
+      const float2* x = s.buf[(k + 1) % 3];
+      const float2* z = s.buf[k % 3] + r * Dd;
+      float2* w = s.buf[(k + 2) % 3] + r * Dd;
+      // w = scale (H v) - beta_{k-1} v_prev   (lanczos.h:25-31)
+      const double bprev = k > 0 ? s.beta[k - 1] : 0.0;
+      const float beta = (float)(-bprev);
+      const float hop = -s.t * s.scale;
+      const uint32_t um = s.up_mask[r];
+      const int u0 = s.up_off[r], u1 = s.up_off[r + 1];
+      float hi = 0.f, lo = 0.f;
+      for (int64_t c = lane; c < Dd; c += 32) {
+        float ar = 0.f, ai = 0.f;
+        for (int j = s.dn_off[c]; j < s.dn_off[c + 1]; ++j) {
+          const uint32_t e = __ldg(&s.dn_ent[j]);
+          const float2 val = v[e >> 8];
+          float wgt = (e & 2u) ? 2.f : 1.f;
+          if (e & 1u) wgt = -wgt;
+          ar = fmaf(wgt, val.x, ar);
+          ai = fmaf(wgt, val.y, ai);
+        }
+        for (int j = u0; j < u1; ++j) {
+          const uint32_t e = __ldg(&s.up_ent[j]);
+          const float2 val = x[(int64_t)(e >> 8) * Dd + c];
+          float wgt = (e & 2u) ? 2.f : 1.f;
+          if (e & 1u) wgt = -wgt;
+          ar = fmaf(wgt, val.x, ar);
+          ai = fmaf(wgt, val.y, ai);
+        }
+        const float2 xv = v[c];
+        const float d = s.scale * s.ufold[__popc(um & s.dn_mask[c])];
+        float2 o;
+        o.x = fmaf(hop, ar, d * xv.x);
+        o.y = fmaf(hop, ai, d * xv.y);
+        if (k > 0) {
+          const float2 zv = z[c];
+          o.x = fmaf(beta, zv.x, o.x);
+          o.y = fmaf(beta, zv.y, o.y);
+        }
+        w[c] = o;
+        if (!replay) {
+          // compensated Re<v, w> (exact float products, TwoSum)
+          float p = xv.x * o.x, pe = fmaf(xv.x, o.x, -p);
+          float s1 = hi + p, bp = s1 - hi;
+          lo += ((hi - (s1 - bp)) + (p - bp)) + pe;
+          hi = s1;
+          p = xv.y * o.y;
+          pe = fmaf(xv.y, o.y, -p);
+          s1 = hi + p;
+          bp = s1 - hi;
+          lo += ((hi - (s1 - bp)) + (p - bp)) + pe;
+          hi = s1;
+        }
+      }
+      dxy = (double)hi + (double)lo;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) dxy += __shfl_down_sync(0xffffffffu, dxy, o);
+    }
+    if (lane == 0 && part) part[it] = dxy;
+  }
+}
+
+// Per-slot fixed-order sum of item partials into alpha[k] (what = 0) or
+// beta[k] = sqrt(sum) (what = 1).
+__global__ void k_eng_seg_reduce(SlotDesc* __restrict__ slots, int n_slots,
+                                 const double* __restrict__ part, int what) {
+  for (int si = blockIdx.x; si < n_slots; si += gridDim.x) {
+    SlotDesc& s = slots[si];
+    const int k = s.k;
+    __shared__ double red[256];
+    double a = 0.0;
+    for (int it = s.item0 + threadIdx.x; it < s.item1; it += blockDim.x) a += part[it];
+    red[threadIdx.x] = a;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0 && s.mode == kModeLanczos && k < s.kmax) {
+      if (what == 0) s.alpha[k] = red[0];
+      else s.beta[k] = sqrt(fmax(red[0], 0.0));
+    }
+    __syncthreads();
+  }
+}
+
+// w -= alpha_k v ; partial ||w||^2 per item.
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+k_eng_update(const SlotDesc* __restrict__ slots, const int2* __restrict__ items, int n_items,
+             double* __restrict__ part) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int it = blockIdx.x * WARPS + warp; it < n_items; it += gridDim.x * WARPS) {
+    const int2 item = items[it];
+    const SlotDesc& s = slots[item.x];
+    const int k = s.k;
+    double nn = 0.0;
+    if (s.mode == kModeLanczos && k < s.kmax) {
+      const int64_t r = item.y, Dd = s.Dd;
+      const float2* v = s.buf[(k + 1) % 3] + r * Dd;
+      float2* w = s.buf[(k + 2) % 3] + r * Dd;
+      const float a = (float)s.alpha[k];
+      float hi = 0.f, lo = 0.f;
+      for (int64_t c = lane; c < Dd; c += 32) {
+        float2 o = w[c];
+        const float2 xv = v[c];
+        o.x = fmaf(-a, xv.x, o.x);
+        o.y = fmaf(-a, xv.y, o.y);
+        w[c] = o;
+        float p = o.x * o.x, pe = fmaf(o.x, o.x, -p);
+        float s1 = hi + p, bp = s1 - hi;
+        lo += ((hi - (s1 - bp)) + (p - bp)) + pe;
+        hi = s1;
+        p = o.y * o.y;
+        pe = fmaf(o.y, o.y, -p);
+        s1 = hi + p;
+        bp = s1 - hi;
+        lo += ((hi - (s1 - bp)) + (p - bp)) + pe;
+        hi = s1;
+      }
+      nn = (double)hi + (double)lo;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) nn += __shfl_down_sync(0xffffffffu, nn, o);
+    }
+    if (lane == 0) part[it] = nn;
+  }
+}
+
+// Replay pass: w = (w - alpha_k v) / beta_k ; x += y_{k+1} w.
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+k_eng_replay_update(const SlotDesc* __restrict__ slots, const int2* __restrict__ items,
+                    int n_items) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int it = blockIdx.x * WARPS + warp; it < n_items; it += gridDim.x * WARPS) {
+    const int2 item = items[it];
+    const SlotDesc& s = slots[item.x];
+    const int k = s.k;
+    if (!(s.mode == kModeReplay && k + 1 < s.steps)) continue;
+    const int64_t r = item.y, Dd = s.Dd;
+    const float2* v = s.buf[(k + 1) % 3] + r * Dd;
+    float2* w = s.buf[(k + 2) % 3] + r * Dd;
+    float2* x = s.xacc + r * Dd;
+    const float a = (float)s.alpha[k], ib = (float)(1.0 / s.beta[k]);
+    const float y = (float)s.yk[k + 1];
+    for (int64_t c = lane; c < Dd; c += 32) {
+      float2 o = w[c];
+      const float2 xv = v[c];
+      o.x = (o.x - a * xv.x) * ib;
+      o.y = (o.y - a * xv.y) * ib;
+      w[c] = o;
+      float2 acc = x[c];
+      acc.x = fmaf(y, o.x, acc.x);
+      acc.y = fmaf(y, o.y, acc.y);
+      x[c] = acc;
+    }
+  }
+}
+
+// v_{k+1} = w / beta_k (in place on w); marks breakdown / completion.
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+k_eng_normalize(const SlotDesc* __restrict__ slots, const int2* __restrict__ items, int n_items) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int it = blockIdx.x * WARPS + warp; it < n_items; it += gridDim.x * WARPS) {
+    const int2 item = items[it];
+    const SlotDesc& s = slots[item.x];
+    const int k = s.k;
+    if (!(s.mode == kModeLanczos && k < s.kmax)) continue;
+    const double b = s.beta[k];
+    if (!(b > kTol)) continue;
+    const int64_t r = item.y, Dd = s.Dd;
+    float2* w = s.buf[(k + 2) % 3] + r * Dd;
+    const float ib = (float)(1.0 / b);
+    for (int64_t c = lane; c < Dd; c += 32) {
+      float2 o = w[c];
+      o.x *= ib;
+      o.y *= ib;
+      w[c] = o;
+    }
+  }
+}
+
+// End of step: advance each slot's counter; a Lanczos slot that broke down
+// (beta <= 1000 eps, lanczos.h:35) or reached kmax goes idle.
+__global__ void k_eng_advance(SlotDesc* __restrict__ slots, int n_slots) {
+  for (int si = threadIdx.x + blockIdx.x * blockDim.x; si < n_slots; si += blockDim.x * gridDim.x) {
+    SlotDesc& s = slots[si];
+    const int k = s.k;
+    if (s.mode == kModeLanczos && k < s.kmax) {
+      s.steps = k + 1;
+      s.k = k + 1;
+      if (!(s.beta[k] > kTol) || k + 1 >= s.kmax) s.mode = kModeIdle;
+    } else if (s.mode == kModeReplay && k + 1 < s.steps) {
+      s.k = k + 1;
+      if (k + 2 >= s.steps) s.mode = kModeIdle;
+    } else if (s.mode == kModeReplay) {
+      s.mode = kModeIdle;
+    }
+  }
+}
+
+// Replay start: v = b / ||b|| was kept in buf[1]; x = y_0 v.
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+k_eng_replay_init(const SlotDesc* __restrict__ slots, const int2* __restrict__ items, int n_items) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int it = blockIdx.x * WARPS + warp; it < n_items; it += gridDim.x * WARPS) {
+    const int2 item = items[it];
+    const SlotDesc& s = slots[item.x];
+    if (s.steps == 0) continue;
+    const int64_t r = item.y, Dd = s.Dd;
+    const float2* v = s.buf[1] + r * Dd;
+    float2* x = s.xacc + r * Dd;
+    float2* vp = s.buf[0] + r * Dd;
+    const float y0 = (float)s.yk[0];
+    for (int64_t c = lane; c < Dd; c += 32) {
+      const float2 a = v[c];
+      x[c] = make_float2(y0 * a.x, y0 * a.y);
+      vp[c] = make_float2(0.f, 0.f);
+    }
+  }
+}
+
+// Start vectors: Philox4x32-10 uniform(-1,1) at counter = tensor index,
+// normalised later (pass one scales by 1/||b||).
+__device__ __forceinline__ void eng_philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t lo0 = 0xD2511F53u * c[0], hi0 = __umulhi(0xD2511F53u, c[0]);
+    const uint32_t lo1 = 0xCD9E8D57u * c[2], hi1 = __umulhi(0xCD9E8D57u, c[2]);
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = lo1;
+    c[2] = n2;
+    c[3] = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+__global__ void k_eng_seed(float2* __restrict__ v, int64_t n, uint64_t seed, double inv_norm_hint) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t c[4] = {(uint32_t)i, (uint32_t)((uint64_t)i >> 32), 0u, 0u};
+    eng_philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const uint64_t m0 = ((((uint64_t)c[0]) << 32) | c[1]) >> 12;
+    const uint64_t m1 = ((((uint64_t)c[2]) << 32) | c[3]) >> 12;
+    const double re = __longlong_as_double((long long)(0x4000000000000000ull | m0)) - 3.0;
+    const double im = __longlong_as_double((long long)(0x4000000000000000ull | m1)) - 3.0;
+    v[i] = make_float2((float)re, (float)im);
+  }
+}
+
+// ||b||^2 of one slot's start vector (compensated), single block.
+__global__ void k_eng_norm2(const float2* __restrict__ v, int64_t n, double* __restrict__ out) {
+  __shared__ double red[256];
+  float hi = 0.f, lo = 0.f;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const float2 a = v[i];
+    float p = a.x * a.x, pe = fmaf(a.x, a.x, -p);
+    float s1 = hi + p, bp = s1 - hi;
+    lo += ((hi - (s1 - bp)) + (p - bp)) + pe;
+    hi = s1;
+    p = a.y * a.y;
+    pe = fmaf(a.y, a.y, -p);
+    s1 = hi + p;
+    bp = s1 - hi;
+    lo += ((hi - (s1 - bp)) + (p - bp)) + pe;
+    hi = s1;
+  }
+  red[threadIdx.x] = (double)hi + (double)lo;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+__global__ void k_eng_scale(float2* __restrict__ v, int64_t n, float s) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 a = v[i];
+    v[i] = make_float2(a.x * s, a.y * s);
+  }
+}
+
+__global__ void k_f32_to_f64(const float2* __restrict__ a, double2* __restrict__ b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 v = a[i];
+    b[i] = make_double2((double)v.x, (double)v.y);
+  }
+}
+
+}  // namespace mb
+
+// ===========================================================================
+// Host side.
+// ===========================================================================
+namespace mb {
+
+struct EngBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  EngBuf() = default;
+  explicit EngBuf(size_t b) : bytes(b) {
+    if (b) MB_CUDA(cudaMalloc(&p, b));
+  }
+  ~EngBuf() {
+    if (p) cudaFree(p);
+  }
+  EngBuf(const EngBuf&) = delete;
+  EngBuf& operator=(const EngBuf&) = delete;
+};
+
+// Sector tables shared by all slots with the same lattice and filling.
+struct TableSet {
+  mb_basis_s basis;
+  mb_model_s model;  // bonds only; t and U come per slot
+  std::vector<std::unique_ptr<EngBuf>> bufs;
+  const uint32_t *up_mask = nullptr, *dn_mask = nullptr, *up_ent = nullptr, *dn_ent = nullptr;
+  const int32_t *up_off = nullptr, *dn_off = nullptr;
+  int max_up_deg = 0, max_dn_deg = 0;
+  int64_t bytes = 0;
+  int refs = 0;
+};
+
+template <typename T>
+const T* tupload(TableSet& ts, const std::vector<T>& h) {
+  auto b = std::make_unique<EngBuf>(sizeof(T) * std::max<size_t>(h.size(), 1));
+  if (!h.empty()) MB_CUDA(cudaMemcpy(b->p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+  ts.bytes += (int64_t)b->bytes;
+  const T* p = (const T*)b->p;
+  ts.bufs.push_back(std::move(b));
+  return p;
+}
+
+using SectorKey = std::tuple<std::vector<int64_t>, int, int>;
+
+struct EngineSlot {
+  int64_t id = -1;
+  std::shared_ptr<TableSet> tables;
+  double t = 1.0, u = 0.0;
+  uint64_t seed = 0;
+  int64_t kmax = 0;
+  double rel_tol = 0.0;
+  int check_every = 10;
+  int refine = 1;
+  std::unique_ptr<EngBuf> vecs;   // 4 vectors: buf0..2, xacc (complex64)
+  std::unique_ptr<EngBuf> scal;   // alpha, beta, yk (double x kEngMaxK each)
+  int64_t dim = 0, Du = 0, Dd = 0;
+  int64_t bytes = 0;
+  int phase = 0;                  // 0 pass one, 1 replay, 2 done
+  double b_norm = 0.0;
+  double last_ritz = 0.0;
+  bool have_ritz = false;
+  int m = 0;                      // pass-one steps
+  double e_raw = 0.0, e0 = 0.0;
+  std::chrono::steady_clock::time_point t_submit, t_done;
+};
+
+}  // namespace mb
+
+struct mb_engine_s {
+  int64_t budget = 0, in_use = 0;
+  int warps = 8;                  // chosen by the autotuner
+  bool tuned = false;
+  std::map<mb::SectorKey, std::shared_ptr<mb::TableSet>> tables;
+  std::vector<std::unique_ptr<mb::EngineSlot>> slots;   // active (phases 0, 1)
+  std::map<int64_t, std::unique_ptr<mb::EngineSlot>> done;
+  int64_t next_id = 1;
+  // device work lists
+  std::unique_ptr<mb::EngBuf> d_slots, d_items, d_part;
+  std::vector<mb::SlotDesc> h_slots;
+  int n_items = 0;
+  bool dirty = true;
+  cudaStream_t st = nullptr;
+  ~mb_engine_s() {
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
+namespace mb {
+namespace {
+
+std::shared_ptr<TableSet> get_tables(mb_engine_s* e, const mb_sector_desc& d) {
+  std::vector<int64_t> dims(d.dims, d.dims + d.ndim);
+  SectorKey key(dims, d.n_up, d.n_down);
+  auto it = e->tables.find(key);
+  if (it != e->tables.end()) return it->second;
+  auto ts = std::make_shared<TableSet>();
+  mb_basis_t b = nullptr;
+  mb_model_t m = nullptr;
+  int64_t L = 1;
+  for (int i = 0; i < d.ndim; ++i) L *= d.dims[i];
+  int rc = mb_basis_create_fixed_spin(L, d.n_up + d.n_down, d.n_up - d.n_down, &b);
+  if (rc) throw Error(rc, mb_last_error());
+  rc = mb_hubbard_create(d.dims, d.ndim, 1.0, 1.0, &m);
+  if (rc) {
+    mb_basis_destroy(b);
+    throw Error(rc, mb_last_error());
+  }
+  ts->basis = *b;
+  ts->model = *m;
+  mb_basis_destroy(b);
+  mb_model_destroy(m);
+  for (int v : ts->model.self_mult)
+    MB_REQUIRE(!v, MB_ERR_INVALID_ARG, "the engine needs lattices without size-1 dimensions");
+  const HopTable tu = build_hop_table(ts->basis.up, ts->model);
+  const HopTable td = build_hop_table(ts->basis.down, ts->model);
+  ts->up_mask = tupload(*ts, ts->basis.up.masks);
+  ts->dn_mask = tupload(*ts, ts->basis.down.masks);
+  ts->up_off = tupload(*ts, tu.off);
+  ts->up_ent = tupload(*ts, tu.ent);
+  ts->dn_off = tupload(*ts, td.off);
+  ts->dn_ent = tupload(*ts, td.ent);
+  ts->max_up_deg = tu.max_degree;
+  ts->max_dn_deg = td.max_degree;
+  e->tables[key] = ts;
+  return ts;
+}
+
+// Device bytes of one slot: 4 complex64 vectors plus 3 x kEngMaxK doubles.
+int64_t slot_bytes(int64_t dim) { return 4 * 8 * dim + 3 * 8 * kEngMaxK; }
+
+void rebuild(mb_engine_s* e) {
+  if (!e->dirty) return;
+  e->h_slots.clear();
+  std::vector<int2> items;
+  for (auto& sp : e->slots) {
+    EngineSlot& s = *sp;
+    SlotDesc d{};
+    const TableSet& ts = *s.tables;
+    d.up_mask = ts.up_mask;
+    d.dn_mask = ts.dn_mask;
+    d.up_off = ts.up_off;
+    d.up_ent = ts.up_ent;
+    d.dn_off = ts.dn_off;
+    d.dn_ent = ts.dn_ent;
+    d.Du = s.Du;
+    d.Dd = s.Dd;
+    float2* base = (float2*)s.vecs->p;
+    for (int q = 0; q < 3; ++q) d.buf[q] = base + (size_t)q * (size_t)s.dim;
+    d.xacc = base + 3 * (size_t)s.dim;
+    double* sc = (double*)s.scal->p;
+    d.alpha = sc;
+    d.beta = sc + kEngMaxK;
+    d.yk = sc + 2 * kEngMaxK;
+    const std::vector<double> uf = u_fold_table(s.u, !(s.u * s.u < kTol * kTol), ts.basis.L);
+    for (int kk = 0; kk <= kMaxOrbitals; ++kk) d.ufold[kk] = kk < (int)uf.size() ? (float)uf[(size_t)kk] : 0.f;
+    d.t = (float)s.t;
+    d.scale = -1.f;
+    d.kmax = (int)s.kmax;
+    d.item0 = (int)items.size();
+    for (int64_t r = 0; r < s.Du; ++r) items.push_back(make_int2((int)e->h_slots.size(), (int)r));
+    d.item1 = (int)items.size();
+    e->h_slots.push_back(d);
+  }
+  e->n_items = (int)items.size();
+  e->d_slots = std::make_unique<EngBuf>(sizeof(SlotDesc) * std::max<size_t>(e->h_slots.size(), 1));
+  e->d_items = std::make_unique<EngBuf>(sizeof(int2) * std::max<size_t>(items.size(), 1));
+  e->d_part = std::make_unique<EngBuf>(sizeof(double) * std::max<size_t>(items.size(), 1));
+  if (!items.empty())
+    MB_CUDA(cudaMemcpyAsync(e->d_items->p, items.data(), sizeof(int2) * items.size(),
+                            cudaMemcpyHostToDevice, e->st));
+  MB_CUDA(cudaStreamSynchronize(e->st));
+  e->dirty = false;
+}
+
+// Pull the per-slot mode/k/steps fields back after a step.
+void fetch_slots(mb_engine_s* e) {
+  if (e->h_slots.empty()) return;
+  MB_CUDA(cudaMemcpyAsync(e->h_slots.data(), e->d_slots->p, sizeof(SlotDesc) * e->h_slots.size(),
+                          cudaMemcpyDeviceToHost, e->st));
+  MB_CUDA(cudaStreamSynchronize(e->st));
+}
+
+void push_slots(mb_engine_s* e) {
+  if (e->h_slots.empty()) return;
+  MB_CUDA(cudaMemcpyAsync(e->d_slots->p, e->h_slots.data(), sizeof(SlotDesc) * e->h_slots.size(),
+                          cudaMemcpyHostToDevice, e->st));
+  MB_CUDA(cudaStreamSynchronize(e->st));
+}
+
+int eng_grid(int n_items, int warps) {
+  static int sms = -1;
+  if (sms < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  int g = (n_items + warps - 1) / warps;
+  const int cap = sms * (2048 / (32 * warps));
+  return std::max(1, std::min(g, cap));
+}
+
+template <int W>
+void step_kernels(mb_engine_s* e) {
+  const SlotDesc* ds = (const SlotDesc*)e->d_slots->p;
+  SlotDesc* dsm = (SlotDesc*)e->d_slots->p;
+  const int2* it = (const int2*)e->d_items->p;
+  double* part = (double*)e->d_part->p;
+  const int n = e->n_items, ns = (int)e->h_slots.size();
+  const int g = eng_grid(n, W);
+  k_eng_apply<W><<<g, W * 32, 0, e->st>>>(ds, it, n, part);
+  k_eng_seg_reduce<<<std::min(ns, 1024), 256, 0, e->st>>>(dsm, ns, part, 0);
+  k_eng_update<W><<<g, W * 32, 0, e->st>>>(ds, it, n, part);
+  k_eng_replay_update<W><<<g, W * 32, 0, e->st>>>(ds, it, n);
+  k_eng_seg_reduce<<<std::min(ns, 1024), 256, 0, e->st>>>(dsm, ns, part, 1);
+  k_eng_normalize<W><<<g, W * 32, 0, e->st>>>(ds, it, n);
+  k_eng_advance<<<(ns + 255) / 256, 256, 0, e->st>>>(dsm, ns);
+}
+
+void launch_step(mb_engine_s* e) {
+  switch (e->warps) {
+    case 2: step_kernels<2>(e); break;
+    case 4: step_kernels<4>(e); break;
+    case 16: step_kernels<16>(e); break;
+    default: step_kernels<8>(e); break;
+  }
+  MB_CUDA(cudaGetLastError());
+}
+
+// Seed, normalise and arm a slot for pass one (or replay).
+void arm_slot(mb_engine_s* e, EngineSlot& s, SlotDesc& d, bool replay) {
+  float2* b1 = d.buf[1];
+  k_eng_seed<<<256, 256, 0, e->st>>>(b1, s.dim, s.seed, 1.0);
+  EngBuf nb(sizeof(double));
+  k_eng_norm2<<<1, 256, 0, e->st>>>(b1, s.dim, (double*)nb.p);
+  double n2 = 0.0;
+  MB_CUDA(cudaMemcpyAsync(&n2, nb.p, sizeof(double), cudaMemcpyDeviceToHost, e->st));
+  MB_CUDA(cudaStreamSynchronize(e->st));
+  s.b_norm = std::sqrt(n2);
+  MB_REQUIRE(s.b_norm > kTol, MB_ERR_ZERO_NORM, "Input vector has zero norm");
+  k_eng_scale<<<256, 256, 0, e->st>>>(b1, s.dim, (float)(1.0 / s.b_norm));
+  MB_CUDA(cudaMemsetAsync(d.buf[0], 0, 8 * (size_t)s.dim, e->st));
+  d.k = 0;
+  if (replay) {
+    d.mode = kModeReplay;
+    d.steps = s.m;
+  } else {
+    d.mode = kModeLanczos;
+    d.steps = 0;
+  }
+}
+
+double ritz_min(const std::vector<double>& a, const std::vector<double>& b, int m,
+                std::vector<double>* vec) {
+  std::vector<double> d(a.begin(), a.begin() + m), z, ee(b.begin(), b.begin() + std::max(m - 1, 0));
+  MB_REQUIRE(tridiag_eig(m, d, ee, vec ? &z : nullptr), MB_ERR_EIG_FAILED,
+             "Eigenvalue decomposition of T_k failed");
+  if (vec) {
+    vec->assign((size_t)m, 0.0);
+    for (int i = 0; i < m; ++i) (*vec)[(size_t)i] = z[(size_t)(m - 1) * m + i];
+  }
+  return d[(size_t)m - 1];  // largest of -T: -E0
+}
+
+// FP64 Rayleigh quotient of the slot's Ritz vector on an FP64 operator view.
+double rayleigh_fp64(mb_engine_s* e, EngineSlot& s, const SlotDesc& d) {
+  const TableSet& ts = *s.tables;
+  OpView v{};
+  v.Du = s.Du;
+  v.Dd = s.Dd;
+  v.dim = s.dim;
+  v.L = ts.basis.L;
+  v.up_mask = ts.up_mask;
+  v.dn_mask = ts.dn_mask;
+  v.up_off = ts.up_off;
+  v.up_ent = ts.up_ent;
+  v.dn_off = ts.dn_off;
+  v.dn_ent = ts.dn_ent;
+  v.max_up_degree = ts.max_up_deg;
+  v.max_dn_degree = ts.max_dn_deg;
+  v.t = s.t;
+  const std::vector<double> uf = u_fold_table(s.u, !(s.u * s.u < kTol * kTol), ts.basis.L);
+  EngBuf duf(sizeof(double) * uf.size());
+  MB_CUDA(cudaMemcpy(duf.p, uf.data(), sizeof(double) * uf.size(), cudaMemcpyHostToDevice));
+  v.u_fold = (const double*)duf.p;
+  EngBuf xd(16 * (size_t)s.dim), yd(16 * (size_t)s.dim);
+  k_f32_to_f64<<<256, 256, 0, e->st>>>(d.xacc, (double2*)xd.p, s.dim);
+  const int g = apply_grid(v, MB_PREC_F64);
+  EngBuf part(sizeof(double) * 3 * (size_t)std::max(g, 1)), out(sizeof(double) * 3);
+  launch_apply(v, MB_PREC_F64, xd.p, yd.p, 1.0, 0.0, 0.0, nullptr, (double*)part.p, 7, e->st);
+  launch_reduce((const double*)part.p, g, 3, (double*)out.p, e->st);
+  double h[3];
+  MB_CUDA(cudaMemcpyAsync(h, out.p, sizeof(h), cudaMemcpyDeviceToHost, e->st));
+  MB_CUDA(cudaStreamSynchronize(e->st));
+  return h[0] / h[2];  // <x, H x> / <x, x>
+}
+
+// Host bookkeeping after a step: convergence, replay, refinement, retirement.
+void after_step(mb_engine_s* e) {
+  fetch_slots(e);
+  bool changed = false;
+  for (size_t i = 0; i < e->slots.size(); ++i) {
+    EngineSlot& s = *e->slots[i];
+    SlotDesc& d = e->h_slots[i];
+    if (s.phase == 0) {
+      const int m = d.steps;
+      bool finished = d.mode == kModeIdle;
+      if (!finished && s.rel_tol > 0.0 && m >= 2 && (m % s.check_every) == 0) {
+        std::vector<double> a((size_t)m), b((size_t)m);
+        MB_CUDA(cudaMemcpy(a.data(), d.alpha, sizeof(double) * m, cudaMemcpyDeviceToHost));
+        MB_CUDA(cudaMemcpy(b.data(), d.beta, sizeof(double) * m, cudaMemcpyDeviceToHost));
+        const double r = ritz_min(a, b, m, nullptr);
+        if (s.have_ritz && std::fabs(r - s.last_ritz) <= s.rel_tol * std::fabs(r)) finished = true;
+        s.last_ritz = r;
+        s.have_ritz = true;
+      }
+      if (finished) {
+        s.m = m;
+        std::vector<double> a((size_t)m), b((size_t)m), y;
+        MB_CUDA(cudaMemcpy(a.data(), d.alpha, sizeof(double) * m, cudaMemcpyDeviceToHost));
+        MB_CUDA(cudaMemcpy(b.data(), d.beta, sizeof(double) * m, cudaMemcpyDeviceToHost));
+        s.e_raw = -ritz_min(a, b, m, s.refine ? &y : nullptr);
+        s.e0 = s.e_raw;
+        if (s.refine && m > 0) {
+          for (auto& yv : y) yv *= s.b_norm;
+          MB_CUDA(cudaMemcpy(d.yk, y.data(), sizeof(double) * m, cudaMemcpyHostToDevice));
+          arm_slot(e, s, d, true);
+          // x = y_0 v_0, v_prev = 0
+          const int2* it = (const int2*)e->d_items->p;
+          push_slots(e);
+          k_eng_replay_init<8><<<eng_grid(d.item1 - d.item0, 8), 256, 0, e->st>>>(
+              (const SlotDesc*)e->d_slots->p, it + d.item0, d.item1 - d.item0);
+          s.phase = 1;
+        } else {
+          s.phase = 2;
+        }
+        changed = true;
+      }
+    } else if (s.phase == 1 && d.mode == kModeIdle) {
+      s.e0 = rayleigh_fp64(e, s, d);
+      s.phase = 2;
+      changed = true;
+    }
+  }
+  // retire finished slots
+  for (size_t i = 0; i < e->slots.size();) {
+    if (e->slots[i]->phase == 2) {
+      auto sp = std::move(e->slots[i]);
+      sp->t_done = std::chrono::steady_clock::now();
+      e->in_use -= sp->bytes;
+      sp->vecs.reset();
+      sp->scal.reset();
+      sp->tables.reset();
+      e->done[sp->id] = std::move(sp);
+      e->slots.erase(e->slots.begin() + (long)i);
+      changed = true;
+    } else {
+      ++i;
+    }
+  }
+  if (changed) {
+    // keep device-side progress (k, mode) of the surviving slots
+    std::vector<SlotDesc> keep;
+    e->dirty = true;
+    std::vector<SlotDesc> old = e->h_slots;
+    rebuild(e);
+    // rebuild() reset per-slot fields: copy progress over by buffer identity
+    for (auto& nd : e->h_slots)
+      for (auto& od : old)
+        if (od.buf[0] == nd.buf[0]) {
+          nd.k = od.k;
+          nd.mode = od.mode;
+          nd.steps = od.steps;
+        }
+    push_slots(e);
+  }
+}
+
+}  // namespace
+}  // namespace mb
+
+using namespace mb;
+
+extern "C" {
+
+int mb_engine_create(int64_t device_bytes_budget, mb_engine_t* out) {
+  return guard([&] {
+    MB_REQUIRE(out, MB_ERR_INVALID_ARG, "NULL argument");
+    int n = 0;
+    MB_REQUIRE(cudaGetDeviceCount(&n) == cudaSuccess && n > 0, MB_ERR_NO_DEVICE,
+               "no CUDA device available");
+    auto e = std::make_unique<mb_engine_s>();
+    size_t free_b = 0, total_b = 0;
+    MB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    e->budget = device_bytes_budget > 0 ? device_bytes_budget : (int64_t)(free_b * 0.8);
+    MB_CUDA(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
+    *out = (mb_engine_t)e.release();
+  });
+}
+
+int mb_engine_destroy(mb_engine_t eng) {
+  auto* e = (mb_engine_s*)eng;
+  if (e) {
+    cudaStreamSynchronize(e->st);
+    delete e;
+  }
+  return MB_OK;
+}
+
+int mb_engine_footprint(const mb_sector_desc* d, int64_t* bytes) {
+  return guard([&] {
+    MB_REQUIRE(d && bytes, MB_ERR_INVALID_ARG, "NULL argument");
+    int64_t L = 1;
+    for (int i = 0; i < d->ndim; ++i) L *= d->dims[i];
+    MB_REQUIRE(L >= 1 && L <= kMaxOrbitals, MB_ERR_CAPACITY, "orbitals must be in [1, 32]");
+    const int64_t dim = binom_at(binom_table(), (int)L, d->n_up) * binom_at(binom_table(), (int)L, d->n_down);
+    *bytes = slot_bytes(dim);
+  });
+}
+
+int mb_engine_submit_ground_state(mb_engine_t eng, const mb_sector_desc* desc, uint64_t seed,
+                                  int64_t kmax, double rel_tol, int refine, int64_t* request_id) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e && desc && request_id, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(kmax >= 1 && kmax <= kEngMaxK, MB_ERR_INVALID_ARG, "kmax must be in [1, 512]");
+    MB_REQUIRE(desc->ndim >= 1 && desc->ndim <= 3, MB_ERR_INVALID_ARG, "ndim must be 1..3");
+    MB_REQUIRE(!(desc->t * desc->t < kTol * kTol), MB_ERR_INVALID_ARG, "t must be non-zero");
+    int64_t need = 0;
+    int rc = mb_engine_footprint(desc, &need);
+    if (rc) throw Error(rc, mb_last_error());
+    MB_REQUIRE(e->in_use + need <= e->budget, MB_ERR_CAPACITY,
+               "device-memory budget full: retry after a step retires requests");
+    auto s = std::make_unique<EngineSlot>();
+    s->tables = get_tables(e, *desc);
+    s->t = desc->t;
+    s->u = desc->u;
+    s->seed = seed;
+    s->kmax = std::min<int64_t>(kmax, s->tables->basis.dim);
+    s->rel_tol = rel_tol;
+    s->refine = refine;
+    s->Du = s->tables->basis.up.D;
+    s->Dd = s->tables->basis.down.D;
+    s->dim = s->tables->basis.dim;
+    s->bytes = need;
+    s->vecs = std::make_unique<EngBuf>(4 * 8 * (size_t)s->dim);
+    s->scal = std::make_unique<EngBuf>(3 * 8 * (size_t)kEngMaxK);
+    s->id = e->next_id++;
+    s->t_submit = std::chrono::steady_clock::now();
+    e->in_use += need;
+    // append, keeping the progress of the others
+    std::vector<SlotDesc> old = e->h_slots;
+    e->slots.push_back(std::move(s));
+    e->dirty = true;
+    rebuild(e);
+    for (auto& nd : e->h_slots)
+      for (auto& od : old)
+        if (od.buf[0] == nd.buf[0]) {
+          nd.k = od.k;
+          nd.mode = od.mode;
+          nd.steps = od.steps;
+        }
+    EngineSlot& ns = *e->slots.back();
+    arm_slot(e, ns, e->h_slots.back(), false);
+    push_slots(e);
+    *request_id = ns.id;
+  });
+}
+
+int mb_engine_step(mb_engine_t eng, int n_steps, int* n_active) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e && n_steps >= 0, MB_ERR_INVALID_ARG, "bad argument");
+    for (int i = 0; i < n_steps && !e->slots.empty(); ++i) {
+      rebuild(e);
+      launch_step(e);
+      after_step(e);
+    }
+    if (n_active) *n_active = (int)e->slots.size();
+  });
+}
+
+int mb_engine_poll(mb_engine_t eng, int64_t id, int* done, double* e0, double* e0_raw,
+                   int64_t* steps, double* latency_s) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e && done, MB_ERR_INVALID_ARG, "NULL argument");
+    auto it = e->done.find(id);
+    if (it == e->done.end()) {
+      *done = 0;
+      return;
+    }
+    const EngineSlot& s = *it->second;
+    *done = 1;
+    if (e0) *e0 = s.e0;
+    if (e0_raw) *e0_raw = s.e_raw;
+    if (steps) *steps = s.m;
+    if (latency_s) *latency_s = std::chrono::duration<double>(s.t_done - s.t_submit).count();
+  });
+}
+
+int mb_engine_set_warps(mb_engine_t eng, int warps_per_block) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e, MB_ERR_INVALID_ARG, "NULL engine");
+    MB_REQUIRE(warps_per_block == 2 || warps_per_block == 4 || warps_per_block == 8 ||
+                   warps_per_block == 16,
+               MB_ERR_INVALID_ARG, "warps per block must be 2, 4, 8 or 16");
+    e->warps = warps_per_block;
+  });
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// n_steps engine steps without host round trips (no convergence checks in
+// between), optionally as one captured CUDA graph replayed n_steps times;
+// then one round of bookkeeping.  For fixed-length batches.
+int mb_engine_step_fixed(mb_engine_t eng, int n_steps, int use_graph, int* n_active) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e && n_steps >= 0, MB_ERR_INVALID_ARG, "bad argument");
+    if (!e->slots.empty() && n_steps > 0) {
+      rebuild(e);
+      if (use_graph) {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        MB_CUDA(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
+        launch_step(e);
+        MB_CUDA(cudaStreamEndCapture(e->st, &g));
+        MB_CUDA(cudaGraphInstantiate(&ge, g, 0));
+        for (int i = 0; i < n_steps; ++i) MB_CUDA(cudaGraphLaunch(ge, e->st));
+        MB_CUDA(cudaStreamSynchronize(e->st));
+        cudaGraphExecDestroy(ge);
+        cudaGraphDestroy(g);
+      } else {
+        for (int i = 0; i < n_steps; ++i) launch_step(e);
+      }
+      after_step(e);
+    }
+    if (n_active) *n_active = (int)e->slots.size();
+  });
+}
+
+// Autotuner: times the grouped apply kernel at 2, 4, 8 and 16 warps per
+// block on the current set of requests and keeps the fastest.  The timed
+// launches write only the w buffers, which the next real step overwrites.
+int mb_engine_autotune(mb_engine_t eng, int* chosen, double* ms) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e, MB_ERR_INVALID_ARG, "NULL engine");
+    if (e->slots.empty()) {
+      if (chosen) *chosen = e->warps;
+      return;
+    }
+    rebuild(e);
+    const SlotDesc* ds = (const SlotDesc*)e->d_slots->p;
+    const int2* it = (const int2*)e->d_items->p;
+    double* part = (double*)e->d_part->p;
+    const int n = e->n_items;
+    cudaEvent_t a, b;
+    MB_CUDA(cudaEventCreate(&a));
+    MB_CUDA(cudaEventCreate(&b));
+    int best = e->warps;
+    float best_ms = 1e30f;
+    const int cand[4] = {2, 4, 8, 16};
+    for (int ci = 0; ci < 4; ++ci) {
+      const int W = cand[ci];
+      auto run = [&] {
+        const int g = eng_grid(n, W);
+        switch (W) {
+          case 2: k_eng_apply<2><<<g, 64, 0, e->st>>>(ds, it, n, part); break;
+          case 4: k_eng_apply<4><<<g, 128, 0, e->st>>>(ds, it, n, part); break;
+          case 8: k_eng_apply<8><<<g, 256, 0, e->st>>>(ds, it, n, part); break;
+          default: k_eng_apply<16><<<g, 512, 0, e->st>>>(ds, it, n, part); break;
+        }
+      };
+      run();
+      MB_CUDA(cudaEventRecord(a, e->st));
+      for (int rep = 0; rep < 3; ++rep) run();
+      MB_CUDA(cudaEventRecord(b, e->st));
+      MB_CUDA(cudaEventSynchronize(b));
+      float t = 0.f;
+      MB_CUDA(cudaEventElapsedTime(&t, a, b));
+      if (t < best_ms) {
+        best_ms = t;
+        best = W;
+      }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    MB_CUDA(cudaGetLastError());
+    e->warps = best;
+    if (chosen) *chosen = best;
+    if (ms) *ms = best_ms / 3.0;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,107 @@
+"""Batched / served ground states (mb_engine_*): many sectors of uneven size
+advanced together, complex64 vectors with FP64 alpha/beta, replay + FP64
+Rayleigh-quotient refinement.
+
+Tolerances: refined energies |dE0| <= 1e-8 |E0| (the spec bar);
+unrefined Ritz values <= 1e-5 |E0|; a request gives bit-identical results
+alone and in any mix (per-request fixed-order reductions).
+"""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+SECTORS = [  # (dims, n_up, n_down, U)
+    ((6,), 3, 3, 4.0),
+    ((6,), 2, 2, 1.5),
+    ((8,), 4, 4, 4.0),
+    ((8,), 3, 3, 7.0),
+    ((2, 3), 2, 2, 3.0),
+    ((3, 3), 2, 2, 8.0),
+    ((4,), 2, 2, 0.5),
+    ((2, 4), 2, 1, 2.0),
+]
+
+
+def exact_e0(dims, nu, nd, u):
+    H = oracle.hubbard_csc(list(dims), 1.0, u, nu, nd)
+    return np.linalg.eigvalsh(H.to_dense())[0]
+
+
+@pytest.fixture(scope="module")
+def exact():
+    return [exact_e0(*s) for s in SECTORS]
+
+
+def descs(mb):
+    return [mb.sector(d, nu, nd, 1.0, u) for d, nu, nd, u in SECTORS]
+
+
+def test_batch_matches_exact(mb, cuda, exact):
+    res = mb.batch_ground_states(descs(mb), seeds=list(range(len(SECTORS))), kmax=150)
+    for r, e in zip(res, exact):
+        assert r is not None
+        assert abs(r.e0 - e) <= 1e-8 * abs(e), (r.e0, e)
+        assert abs(r.e0_raw - e) <= 1e-5 * abs(e), (r.e0_raw, e)
+
+
+def test_same_result_alone_and_in_mix(mb, cuda):
+    d = descs(mb)
+    mixed = mb.batch_ground_states(d, seeds=[7] * len(d), kmax=120, autotune=False)
+    for i in (0, 2, 5):
+        alone = mb.batch_ground_states([d[i]], seeds=[7], kmax=120, autotune=False)[0]
+        assert alone.e0 == mixed[i].e0 and alone.e0_raw == mixed[i].e0_raw
+        assert alone.steps == mixed[i].steps
+
+
+def test_graph_and_eager_agree(mb, cuda):
+    d = descs(mb)[:4]
+    a = mb.batch_ground_states(d, kmax=100, use_graph=True, autotune=False)
+    b = mb.batch_ground_states(d, kmax=100, use_graph=False, autotune=False)
+    assert [x.e0 for x in a] == [x.e0 for x in b]
+
+
+def test_continuous_admission_and_convergence(mb, cuda, exact):
+    """Budget for ~2 requests: later ones are admitted as earlier ones retire;
+    each stops on its own convergence test."""
+    d = descs(mb)
+    foot = max(mb.Engine.footprint(x) for x in d)
+    eng = mb.Engine(device_bytes_budget=2 * foot + 1)
+    pending = list(range(len(d)))
+    ids = {}
+    rounds = 0
+    while pending or any(eng.poll(r) is None for r in ids.values()):
+        while pending:
+            rid = eng.try_submit(d[pending[0]], seed=3, kmax=300, rel_tol=1e-12)
+            if rid is None:
+                break
+            ids[pending.pop(0)] = rid
+        eng.step(5)
+        rounds += 1
+        assert rounds < 2000
+    for i, rid in ids.items():
+        r = eng.poll(rid)
+        assert abs(r.e0 - exact[i]) <= 1e-8 * abs(exact[i])
+        assert r.latency_s > 0
+    assert len(ids) == len(d)
+
+
+def test_autotune_picks_a_valid_shape(mb, cuda):
+    eng = mb.Engine()
+    for x in descs(mb):
+        assert eng.try_submit(x, 1, 50) is not None
+    w, ms = eng.autotune()
+    assert w in (2, 4, 8, 16) and ms > 0
+    eng.set_warps(4)
+    with pytest.raises(mb.MbError):
+        eng.set_warps(3)
+
+
+def test_engine_rejects_bad_requests(mb, cuda):
+    eng = mb.Engine()
+    with pytest.raises(mb.MbError):
+        eng.try_submit(mb.sector((1, 4), 1, 1, 1.0, 1.0), 0, 10)   # size-1 dimension
+    with pytest.raises(mb.MbError):
+        eng.try_submit(mb.sector((6,), 3, 3, 1.0, 1.0), 0, 10000)  # kmax > 512
