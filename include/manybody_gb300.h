@@ -277,6 +277,17 @@ int mb_engine_footprint(const mb_sector_desc* desc, int64_t* bytes);
  * mb_engine_step retires requests). */
 int mb_engine_submit_ground_state(mb_engine_t engine, const mb_sector_desc* desc, uint64_t seed,
                                   int64_t kmax, double rel_tol, int refine, int64_t* request_id);
+/* Density-of-states moments of one sector: spectral bounds from 40 Lanczos
+ * steps on H (extremal Ritz values widened by their residual bounds), then
+ * (H - b)/a with (a, b) = rescaling::from_bounds(E_min, E_max, padding)
+ * (rescaling.h:33-38) and n_probes random-phase probes (Philox stream
+ * 1 + probe), n_moments/2 Chebyshev steps each with the doubling identities.
+ * The result is mu[n] = (1/R) sum_r <r|T_n|r> / D. */
+int mb_engine_submit_dos(mb_engine_t engine, const mb_sector_desc* desc, int64_t n_moments,
+                         int64_t n_probes, uint64_t seed, double padding, int64_t* request_id);
+/* *done = 1 once finished; mu receives n_moments values; the bounds used. */
+int mb_engine_poll_dos(mb_engine_t engine, int64_t request_id, int* done, double* mu,
+                       double* e_min, double* e_max, double* latency_s);
 /* Run up to n_steps engine steps; *n_active = requests still running. */
 int mb_engine_step(mb_engine_t engine, int n_steps, int* n_active);
 /* *done = 1 once the request finished: energy (refined if asked), the

@@ -130,6 +130,9 @@ SIGNATURES = {
     "mb_engine_footprint": (C.c_int, [C.POINTER(SectorDesc), _i64p]),
     "mb_engine_submit_ground_state": (C.c_int, [_vp, C.POINTER(SectorDesc), C.c_uint64, _i64,
                                                 C.c_double, C.c_int, _i64p]),
+    "mb_engine_submit_dos": (C.c_int, [_vp, C.POINTER(SectorDesc), _i64, _i64, C.c_uint64,
+                                       C.c_double, _i64p]),
+    "mb_engine_poll_dos": (C.c_int, [_vp, _i64, C.POINTER(C.c_int), _dp, _dp, _dp, _dp]),
     "mb_engine_step": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
     "mb_engine_step_fixed": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "mb_engine_poll": (C.c_int, [_vp, _i64, C.POINTER(C.c_int), _dp, _dp, _i64p, _dp]),
@@ -499,9 +502,9 @@ class EigenPair:
 
 
 def _eigenpair(fn, op, k, seed, order, reorth, basis_precision, conv_tol, check_every,
-               want_vector):
+               want_vector, refine=False):
     _sync_torch()
-    opts = LanczosOpts(int(reorth), basis_precision, conv_tol, check_every, 0)
+    opts = LanczosOpts(int(reorth), basis_precision, conv_tol, check_every, int(refine))
     e = C.c_double()
     steps = C.c_int64()
     vec = op.empty() if want_vector else None
@@ -512,12 +515,14 @@ def _eigenpair(fn, op, k, seed, order, reorth, basis_precision, conv_tol, check_
 
 def find_min_eigenpair(op: GpuHubbardOperator, k: int, seed=None, order: int = ORDER_REFERENCE,
                        reorth: bool = False, basis_precision: int = -1, conv_tol: float = 0.0,
-                       check_every: int = 10, want_vector: bool = True) -> EigenPair:
-    """find_min_eigenpair (src/numerics/lanczos.h:283-290) from a seeded start vector."""
+                       check_every: int = 10, want_vector: bool = True,
+                       refine: bool = False) -> EigenPair:
+    """find_min_eigenpair (src/numerics/lanczos.h:283-290) from a seeded start vector.
+    refine (FP32 operators): the energy is the FP64 Rayleigh quotient of the Ritz vector."""
     if seed is None:
         seed = op.seed_vector(0, order=order)
     return _eigenpair(lib().mb_find_min_eigenpair, op, k, seed, order, reorth, basis_precision,
-                      conv_tol, check_every, want_vector)
+                      conv_tol, check_every, want_vector, refine)
 
 
 def find_max_eigenpair(op: GpuHubbardOperator, k: int, seed=None, order: int = ORDER_REFERENCE,
@@ -657,6 +662,29 @@ class Engine:
             return None
         _check(rc)
         return rid.value
+
+    def try_submit_dos(self, desc: SectorDesc, n_moments: int = 512, n_probes: int = 1,
+                       seed: int = 0, padding: float = 0.01):
+        """DOS-moment request id, or None when the device-memory budget is full."""
+        rid = C.c_int64()
+        rc = lib().mb_engine_submit_dos(self._h, C.byref(desc), n_moments, n_probes, seed, padding,
+                                        C.byref(rid))
+        if rc == MB_ERR_CAPACITY:
+            return None
+        _check(rc)
+        self._dos_moments = getattr(self, "_dos_moments", {})
+        self._dos_moments[rid.value] = n_moments
+        return rid.value
+
+    def poll_dos(self, rid: int):
+        """(mu, e_min, e_max, latency_s) once finished, else None."""
+        n = self._dos_moments[rid]
+        mu = np.zeros(n)
+        done = C.c_int()
+        lo, hi, lat = C.c_double(), C.c_double(), C.c_double()
+        _check(lib().mb_engine_poll_dos(self._h, rid, C.byref(done), mu.ctypes.data_as(_dp),
+                                        C.byref(lo), C.byref(hi), C.byref(lat)))
+        return (mu, lo.value, hi.value, lat.value) if done.value else None
 
     def step(self, n: int = 1) -> int:
         a = C.c_int()

@@ -48,7 +48,9 @@ struct SlotDesc {
   double* yk;       // Ritz coefficients for the replay pass [kEngMaxK]
   float ufold[kMaxOrbitals + 1];
   float t;
-  float scale;      // -1: Negated H (ground state), +1: H
+  float scale;      // Lanczos: -1 Negated H (ground state), +1 H
+  float cheb_a;     // Chebyshev mode: Ht = (H - cheb_b) / cheb_a
+  float cheb_b;
   int kmax;         // pass one: steps to run at most
   int k;            // this slot's step counter
   int mode;         // kModeIdle, kModeLanczos, kModeReplay
@@ -59,6 +61,7 @@ struct SlotDesc {
 constexpr int kModeIdle = 0;
 constexpr int kModeLanczos = 1;
 constexpr int kModeReplay = 2;
+constexpr int kModeCheb = 3;   // T_{k+1} = 2 Ht T_k - T_{k-1} (T_1 = Ht T_0)
 
 // ---------------------------------------------------------------------------
 // Kernels.  One warp per (slot, row) item; lanes stride over the row.
@@ -66,24 +69,30 @@ constexpr int kModeReplay = 2;
 template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32)
 k_eng_apply(const SlotDesc* __restrict__ slots, const int2* __restrict__ items, int n_items,
-            double* __restrict__ part) {
+            double* __restrict__ part, double* __restrict__ part2) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int it = blockIdx.x * WARPS + warp; it < n_items; it += gridDim.x * WARPS) {
     const int2 item = items[it];
     const SlotDesc& s = slots[item.x];
     const int k = s.k;
     const bool replay = s.mode == kModeReplay;
-    double dxy = 0.0;
-    if ((s.mode == kModeLanczos && k < s.kmax) || (replay && k + 1 < s.steps)) {
+    const bool cheb = s.mode == kModeCheb;
+    double dxy = 0.0, dyy = 0.0;
+    if ((s.mode == kModeLanczos && k < s.kmax) || (replay && k + 1 < s.steps) ||
+        (cheb && k < s.kmax)) {
       const int64_t r = item.y, Dd = s.Dd;
       const float2* v = s.buf[(k + 1) % 3] + r * Dd;
       const float2* x = s.buf[(k + 1) % 3];
       const float2* z = s.buf[k % 3] + r * Dd;
       float2* w = s.buf[(k + 2) % 3] + r * Dd;
-      // w = scale (H v) - beta_{k-1} v_prev   (lanczos.h:25-31)
-      const double bprev = k > 0 ? s.beta[k - 1] : 0.0;
+      // Lanczos: w = scale (H v) - beta_{k-1} v_prev   (lanczos.h:25-31)
+      // Chebyshev: w = c (H - b) v - [k > 0] v_prev, c = 1/a (k = 0) or 2/a (kpm.h:218-223)
+      const double bprev = cheb ? 1.0 : (k > 0 ? s.beta[k - 1] : 0.0);
       const float beta = (float)(-bprev);
-      const float hop = -s.t * s.scale;
+      const float sc = cheb ? (k == 0 ? 1.f : 2.f) / s.cheb_a : s.scale;
+      const float shift = cheb ? s.cheb_b : 0.f;
+      const float hop = -s.t * sc;
+      float hi2 = 0.f, lo2 = 0.f;
       const uint32_t um = s.up_mask[r];
       const int u0 = s.up_off[r], u1 = s.up_off[r + 1];
       float hi = 0.f, lo = 0.f;
@@ -106,7 +115,7 @@ k_eng_apply(const SlotDesc* __restrict__ slots, const int2* __restrict__ items, 
           ai = fmaf(wgt, val.y, ai);
         }
         const float2 xv = v[c];
-        const float d = s.scale * s.ufold[__popc(um & s.dn_mask[c])];
+        const float d = sc * (s.ufold[__popc(um & s.dn_mask[c])] - shift);
         float2 o;
         o.x = fmaf(hop, ar, d * xv.x);
         o.y = fmaf(hop, ai, d * xv.y);
@@ -129,34 +138,66 @@ k_eng_apply(const SlotDesc* __restrict__ slots, const int2* __restrict__ items, 
           lo += ((hi - (s1 - bp)) + (p - bp)) + pe;
           hi = s1;
         }
+        if (cheb) {  // <T_{k+1}, T_{k+1}>
+          float p = o.x * o.x, pe = fmaf(o.x, o.x, -p);
+          float s1 = hi2 + p, bp = s1 - hi2;
+          lo2 += ((hi2 - (s1 - bp)) + (p - bp)) + pe;
+          hi2 = s1;
+          p = o.y * o.y;
+          pe = fmaf(o.y, o.y, -p);
+          s1 = hi2 + p;
+          bp = s1 - hi2;
+          lo2 += ((hi2 - (s1 - bp)) + (p - bp)) + pe;
+          hi2 = s1;
+        }
       }
       dxy = (double)hi + (double)lo;
+      dyy = (double)hi2 + (double)lo2;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) dxy += __shfl_down_sync(0xffffffffu, dxy, o);
+      for (int o = 16; o > 0; o >>= 1) {
+        dxy += __shfl_down_sync(0xffffffffu, dxy, o);
+        dyy += __shfl_down_sync(0xffffffffu, dyy, o);
+      }
     }
-    if (lane == 0 && part) part[it] = dxy;
+    if (lane == 0 && part) {
+      part[it] = dxy;
+      part2[it] = dyy;
+    }
   }
 }
 
 // Per-slot fixed-order sum of item partials into alpha[k] (what = 0) or
 // beta[k] = sqrt(sum) (what = 1).
 __global__ void k_eng_seg_reduce(SlotDesc* __restrict__ slots, int n_slots,
-                                 const double* __restrict__ part, int what) {
+                                 const double* __restrict__ part, const double* __restrict__ part2,
+                                 int what) {
   for (int si = blockIdx.x; si < n_slots; si += gridDim.x) {
     SlotDesc& s = slots[si];
     const int k = s.k;
-    __shared__ double red[256];
-    double a = 0.0;
-    for (int it = s.item0 + threadIdx.x; it < s.item1; it += blockDim.x) a += part[it];
+    const bool cheb = s.mode == kModeCheb && what == 0;
+    __shared__ double red[256], red2[256];
+    double a = 0.0, b = 0.0;
+    for (int it = s.item0 + threadIdx.x; it < s.item1; it += blockDim.x) {
+      a += part[it];
+      if (cheb) b += part2[it];
+    }
     red[threadIdx.x] = a;
+    red2[threadIdx.x] = b;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      if (threadIdx.x < w) {
+        red[threadIdx.x] += red[threadIdx.x + w];
+        red2[threadIdx.x] += red2[threadIdx.x + w];
+      }
       __syncthreads();
     }
     if (threadIdx.x == 0 && s.mode == kModeLanczos && k < s.kmax) {
       if (what == 0) s.alpha[k] = red[0];
       else s.beta[k] = sqrt(fmax(red[0], 0.0));
+    }
+    if (threadIdx.x == 0 && cheb && k < s.kmax) {
+      s.alpha[k] = red[0];   // Re<T_k, T_{k+1}>
+      s.beta[k] = red2[0];   // <T_{k+1}, T_{k+1}>
     }
     __syncthreads();
   }
@@ -274,7 +315,27 @@ __global__ void k_eng_advance(SlotDesc* __restrict__ slots, int n_slots) {
       if (k + 2 >= s.steps) s.mode = kModeIdle;
     } else if (s.mode == kModeReplay) {
       s.mode = kModeIdle;
+    } else if (s.mode == kModeCheb && k < s.kmax) {
+      s.k = k + 1;
+      s.steps = k + 1;
+      if (k + 1 >= s.kmax) s.mode = kModeIdle;
     }
+  }
+}
+
+__device__ __forceinline__ void eng_philox(uint32_t c[4], uint32_t k0, uint32_t k1);
+
+// Random-phase probe exp(2 pi i u), u ~ U[0,1) from Philox (stream 1 + probe).
+__global__ void k_eng_seed_phase(float2* __restrict__ v, int64_t n, uint64_t seed, uint32_t stream_id) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t c[4] = {(uint32_t)i, (uint32_t)((uint64_t)i >> 32), stream_id, 0u};
+    eng_philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const uint64_t m0 = ((((uint64_t)c[0]) << 32) | c[1]) >> 12;
+    const double u = (__longlong_as_double((long long)(0x4000000000000000ull | m0)) - 3.0 + 1.0) * 0.5;
+    float sn, cs;
+    sincospif((float)(2.0 * u), &sn, &cs);
+    v[i] = make_float2(cs, sn);
   }
 }
 
@@ -430,7 +491,12 @@ struct EngineSlot {
   std::unique_ptr<EngBuf> scal;   // alpha, beta, yk (double x kEngMaxK each)
   int64_t dim = 0, Du = 0, Dd = 0;
   int64_t bytes = 0;
-  int phase = 0;                  // 0 pass one, 1 replay, 2 done
+  int phase = 0;                  // 0 pass one, 1 replay, 2 done, 10 DOS bounds, 11 DOS Chebyshev
+  int kind = 0;                   // 0 ground state, 1 DOS moments
+  float scale = -1.f;             // Lanczos scale (-1: ground state; +1: spectral bounds)
+  int n_moments = 0, n_probes = 0, probe = 0;
+  double padding = 0.01, emin = 0.0, emax = 0.0, mu0 = 0.0;
+  std::vector<double> mu;         // accumulated DOS moments
   double b_norm = 0.0;
   double last_ritz = 0.0;
   bool have_ritz = false;
@@ -529,7 +595,7 @@ void rebuild(mb_engine_s* e) {
     const std::vector<double> uf = u_fold_table(s.u, !(s.u * s.u < kTol * kTol), ts.basis.L);
     for (int kk = 0; kk <= kMaxOrbitals; ++kk) d.ufold[kk] = kk < (int)uf.size() ? (float)uf[(size_t)kk] : 0.f;
     d.t = (float)s.t;
-    d.scale = -1.f;
+    d.scale = s.scale;
     d.kmax = (int)s.kmax;
     d.item0 = (int)items.size();
     for (int64_t r = 0; r < s.Du; ++r) items.push_back(make_int2((int)e->h_slots.size(), (int)r));
@@ -539,7 +605,7 @@ void rebuild(mb_engine_s* e) {
   e->n_items = (int)items.size();
   e->d_slots = std::make_unique<EngBuf>(sizeof(SlotDesc) * std::max<size_t>(e->h_slots.size(), 1));
   e->d_items = std::make_unique<EngBuf>(sizeof(int2) * std::max<size_t>(items.size(), 1));
-  e->d_part = std::make_unique<EngBuf>(sizeof(double) * std::max<size_t>(items.size(), 1));
+  e->d_part = std::make_unique<EngBuf>(2 * sizeof(double) * std::max<size_t>(items.size(), 1));
   if (!items.empty())
     MB_CUDA(cudaMemcpyAsync(e->d_items->p, items.data(), sizeof(int2) * items.size(),
                             cudaMemcpyHostToDevice, e->st));
@@ -581,12 +647,13 @@ void step_kernels(mb_engine_s* e) {
   const int2* it = (const int2*)e->d_items->p;
   double* part = (double*)e->d_part->p;
   const int n = e->n_items, ns = (int)e->h_slots.size();
+  double* part2 = part + n;
   const int g = eng_grid(n, W);
-  k_eng_apply<W><<<g, W * 32, 0, e->st>>>(ds, it, n, part);
-  k_eng_seg_reduce<<<std::min(ns, 1024), 256, 0, e->st>>>(dsm, ns, part, 0);
+  k_eng_apply<W><<<g, W * 32, 0, e->st>>>(ds, it, n, part, part2);
+  k_eng_seg_reduce<<<std::min(ns, 1024), 256, 0, e->st>>>(dsm, ns, part, part2, 0);
   k_eng_update<W><<<g, W * 32, 0, e->st>>>(ds, it, n, part);
   k_eng_replay_update<W><<<g, W * 32, 0, e->st>>>(ds, it, n);
-  k_eng_seg_reduce<<<std::min(ns, 1024), 256, 0, e->st>>>(dsm, ns, part, 1);
+  k_eng_seg_reduce<<<std::min(ns, 1024), 256, 0, e->st>>>(dsm, ns, part, part2, 1);
   k_eng_normalize<W><<<g, W * 32, 0, e->st>>>(ds, it, n);
   k_eng_advance<<<(ns + 255) / 256, 256, 0, e->st>>>(dsm, ns);
 }
@@ -669,6 +736,71 @@ double rayleigh_fp64(mb_engine_s* e, EngineSlot& s, const SlotDesc& d) {
   return h[0] / h[2];  // <x, H x> / <x, x>
 }
 
+// Seed probe `p` of a DOS request into buf[1] and arm Chebyshev mode.
+void arm_probe(mb_engine_s* e, EngineSlot& s, SlotDesc& d) {
+  k_eng_seed_phase<<<256, 256, 0, e->st>>>(d.buf[1], s.dim, s.seed, (uint32_t)(1 + s.probe));
+  EngBuf nb(sizeof(double));
+  k_eng_norm2<<<1, 256, 0, e->st>>>(d.buf[1], s.dim, (double*)nb.p);
+  MB_CUDA(cudaMemcpyAsync(&s.mu0, nb.p, sizeof(double), cudaMemcpyDeviceToHost, e->st));
+  MB_CUDA(cudaMemsetAsync(d.buf[0], 0, 8 * (size_t)s.dim, e->st));
+  MB_CUDA(cudaStreamSynchronize(e->st));
+  const double a = (s.emax - s.emin) / 2.0 * (1.0 + s.padding);  // rescaling.h:33-38
+  const double b = (s.emax + s.emin) / 2.0;
+  d.cheb_a = (float)a;
+  d.cheb_b = (float)b;
+  d.mode = kModeCheb;
+  d.k = 0;
+  d.steps = 0;
+  d.kmax = std::max(s.n_moments / 2, 1);
+}
+
+// DOS bookkeeping when a slot's device phase went idle.
+void dos_transition(mb_engine_s* e, EngineSlot& s, SlotDesc& d, bool& changed) {
+  if (s.phase == 10) {
+    // spectral bounds: extremal Ritz values of pass one on H, widened by
+    // their residual bounds beta_m |z_m|
+    const int m = d.steps;
+    std::vector<double> a((size_t)m), b((size_t)m);
+    MB_CUDA(cudaMemcpy(a.data(), d.alpha, sizeof(double) * m, cudaMemcpyDeviceToHost));
+    MB_CUDA(cudaMemcpy(b.data(), d.beta, sizeof(double) * m, cudaMemcpyDeviceToHost));
+    std::vector<double> dd(a), z, ee(b.begin(), b.begin() + std::max(m - 1, 0));
+    MB_REQUIRE(tridiag_eig(m, dd, ee, &z), MB_ERR_EIG_FAILED, "Eigenvalue decomposition of T_k failed");
+    const double bm = b[(size_t)m - 1];
+    const double rlo = bm * std::fabs(z[(size_t)0 * m + (m - 1)]);
+    const double rhi = bm * std::fabs(z[(size_t)(m - 1) * m + (m - 1)]);
+    s.emin = dd[0] - rlo;
+    s.emax = dd[(size_t)m - 1] + rhi;
+    if (!(s.emax > s.emin)) s.emax = s.emin + 1.0;
+    s.mu.assign((size_t)s.n_moments, 0.0);
+    s.probe = 0;
+    arm_probe(e, s, d);
+    s.phase = 11;
+    changed = true;
+  } else if (s.phase == 11) {
+    const int ns = d.steps;
+    std::vector<double> a((size_t)ns), b((size_t)ns);
+    MB_CUDA(cudaMemcpy(a.data(), d.alpha, sizeof(double) * ns, cudaMemcpyDeviceToHost));
+    MB_CUDA(cudaMemcpy(b.data(), d.beta, sizeof(double) * ns, cudaMemcpyDeviceToHost));
+    // mu_0 = <T0,T0>, mu_1 = <T0,T1>, mu_2n = 2<Tn,Tn> - mu_0, mu_2n+1 = 2<Tn+1,Tn> - mu_1
+    const double mu0 = s.mu0, mu1 = ns > 0 ? a[0] : 0.0;
+    s.mu[0] += mu0;
+    if (s.n_moments > 1) s.mu[1] += mu1;
+    for (int n = 1; 2 * n < s.n_moments; ++n) {
+      s.mu[(size_t)(2 * n)] += 2.0 * b[(size_t)n - 1] - mu0;
+      if (2 * n + 1 < s.n_moments) s.mu[(size_t)(2 * n + 1)] += 2.0 * a[(size_t)n] - mu1;
+    }
+    s.probe += 1;
+    if (s.probe < s.n_probes) {
+      arm_probe(e, s, d);
+    } else {
+      const double norm = 1.0 / ((double)s.n_probes * (double)s.dim);
+      for (auto& v : s.mu) v *= norm;
+      s.phase = 2;
+    }
+    changed = true;
+  }
+}
+
 // Host bookkeeping after a step: convergence, replay, refinement, retirement.
 void after_step(mb_engine_s* e) {
   fetch_slots(e);
@@ -676,7 +808,7 @@ void after_step(mb_engine_s* e) {
   for (size_t i = 0; i < e->slots.size(); ++i) {
     EngineSlot& s = *e->slots[i];
     SlotDesc& d = e->h_slots[i];
-    if (s.phase == 0) {
+    if (s.phase == 0 && s.kind == 0) {
       const int m = d.steps;
       bool finished = d.mode == kModeIdle;
       if (!finished && s.rel_tol > 0.0 && m >= 2 && (m % s.check_every) == 0) {
@@ -714,6 +846,8 @@ void after_step(mb_engine_s* e) {
       s.e0 = rayleigh_fp64(e, s, d);
       s.phase = 2;
       changed = true;
+    } else if ((s.phase == 10 || s.phase == 11) && d.mode == kModeIdle) {
+      dos_transition(e, s, d, changed);
     }
   }
   // retire finished slots
@@ -745,6 +879,9 @@ void after_step(mb_engine_s* e) {
           nd.k = od.k;
           nd.mode = od.mode;
           nd.steps = od.steps;
+          nd.kmax = od.kmax;
+          nd.cheb_a = od.cheb_a;
+          nd.cheb_b = od.cheb_b;
         }
     push_slots(e);
   }
@@ -833,11 +970,91 @@ int mb_engine_submit_ground_state(mb_engine_t eng, const mb_sector_desc* desc, u
           nd.k = od.k;
           nd.mode = od.mode;
           nd.steps = od.steps;
+          nd.kmax = od.kmax;
+          nd.cheb_a = od.cheb_a;
+          nd.cheb_b = od.cheb_b;
         }
     EngineSlot& ns = *e->slots.back();
     arm_slot(e, ns, e->h_slots.back(), false);
     push_slots(e);
     *request_id = ns.id;
+  });
+}
+
+int mb_engine_submit_dos(mb_engine_t eng, const mb_sector_desc* desc, int64_t n_moments,
+                         int64_t n_probes, uint64_t seed, double padding, int64_t* request_id) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e && desc && request_id, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(n_moments >= 2 && n_moments <= 2 * kEngMaxK, MB_ERR_INVALID_ARG,
+               "n_moments must be in [2, 1024]");
+    MB_REQUIRE(n_probes >= 1, MB_ERR_INVALID_ARG, "n_probes must be >= 1");
+    MB_REQUIRE(desc->ndim >= 1 && desc->ndim <= 3, MB_ERR_INVALID_ARG, "ndim must be 1..3");
+    MB_REQUIRE(!(desc->t * desc->t < kTol * kTol), MB_ERR_INVALID_ARG, "t must be non-zero");
+    int64_t need = 0;
+    int rc = mb_engine_footprint(desc, &need);
+    if (rc) throw Error(rc, mb_last_error());
+    MB_REQUIRE(e->in_use + need <= e->budget, MB_ERR_CAPACITY,
+               "device-memory budget full: retry after a step retires requests");
+    auto s = std::make_unique<EngineSlot>();
+    s->tables = get_tables(e, *desc);
+    s->kind = 1;
+    s->scale = 1.f;
+    s->t = desc->t;
+    s->u = desc->u;
+    s->seed = seed;
+    s->Du = s->tables->basis.up.D;
+    s->Dd = s->tables->basis.down.D;
+    s->dim = s->tables->basis.dim;
+    s->kmax = std::min<int64_t>(40, s->dim);  // Lanczos steps for the spectral bounds
+    s->n_moments = (int)n_moments;
+    s->n_probes = (int)n_probes;
+    s->padding = padding;
+    s->bytes = need;
+    s->vecs = std::make_unique<EngBuf>(4 * 8 * (size_t)s->dim);
+    s->scal = std::make_unique<EngBuf>(3 * 8 * (size_t)kEngMaxK);
+    s->id = e->next_id++;
+    s->t_submit = std::chrono::steady_clock::now();
+    s->phase = 10;
+    e->in_use += need;
+    std::vector<SlotDesc> old = e->h_slots;
+    e->slots.push_back(std::move(s));
+    e->dirty = true;
+    rebuild(e);
+    for (auto& nd : e->h_slots)
+      for (auto& od : old)
+        if (od.buf[0] == nd.buf[0]) {
+          nd.k = od.k;
+          nd.mode = od.mode;
+          nd.steps = od.steps;
+          nd.kmax = od.kmax;
+          nd.cheb_a = od.cheb_a;
+          nd.cheb_b = od.cheb_b;
+        }
+    EngineSlot& ns = *e->slots.back();
+    arm_slot(e, ns, e->h_slots.back(), false);
+    push_slots(e);
+    *request_id = ns.id;
+  });
+}
+
+int mb_engine_poll_dos(mb_engine_t eng, int64_t id, int* done, double* mu, double* e_min,
+                       double* e_max, double* latency_s) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e && done, MB_ERR_INVALID_ARG, "NULL argument");
+    auto it = e->done.find(id);
+    if (it == e->done.end()) {
+      *done = 0;
+      return;
+    }
+    const EngineSlot& s = *it->second;
+    MB_REQUIRE(s.kind == 1, MB_ERR_INVALID_ARG, "request is not a DOS request");
+    *done = 1;
+    if (mu) std::copy(s.mu.begin(), s.mu.end(), mu);
+    if (e_min) *e_min = s.emin;
+    if (e_max) *e_max = s.emax;
+    if (latency_s) *latency_s = std::chrono::duration<double>(s.t_done - s.t_submit).count();
   });
 }
 
@@ -944,10 +1161,10 @@ int mb_engine_autotune(mb_engine_t eng, int* chosen, double* ms) {
       auto run = [&] {
         const int g = eng_grid(n, W);
         switch (W) {
-          case 2: k_eng_apply<2><<<g, 64, 0, e->st>>>(ds, it, n, part); break;
-          case 4: k_eng_apply<4><<<g, 128, 0, e->st>>>(ds, it, n, part); break;
-          case 8: k_eng_apply<8><<<g, 256, 0, e->st>>>(ds, it, n, part); break;
-          default: k_eng_apply<16><<<g, 512, 0, e->st>>>(ds, it, n, part); break;
+          case 2: k_eng_apply<2><<<g, 64, 0, e->st>>>(ds, it, n, part, part + n); break;
+          case 4: k_eng_apply<4><<<g, 128, 0, e->st>>>(ds, it, n, part, part + n); break;
+          case 8: k_eng_apply<8><<<g, 256, 0, e->st>>>(ds, it, n, part, part + n); break;
+          default: k_eng_apply<16><<<g, 512, 0, e->st>>>(ds, it, n, part, part + n); break;
         }
       };
       run();

@@ -511,7 +511,8 @@ static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
   MB_REQUIRE(tridiag_eig((int)m, d, e, &z), MB_ERR_EIG_FAILED,
              "Eigenvalue decomposition of T_k failed");
   *e_out = sign * d[(size_t)m - 1];
-  if (vec) {
+  const bool refine = o.refine && op->precision == MB_PREC_F32;
+  if (vec || refine) {
     std::vector<std::complex<double>> y((size_t)m);
     for (int64_t i = 0; i < m; ++i) y[(size_t)i] = z[(size_t)(m - 1) * m + i] * b_norm;
     DevBuf xt(kr.vb);
@@ -520,7 +521,17 @@ static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
     } else {
       kr.pass_two(bt.p, m, sign, alphas, betas, b_norm, y, xt.p);
     }
-    from_tensor(op, xt.p, vec, order, st);
+    if (refine) {
+      // One FP64 Rayleigh-quotient sweep on the FP32 Ritz vector x:
+      // E = <x, H x> / <x, x> with FP64 vectors and arithmetic.
+      DevBuf x64(16 * (size_t)op->dim), y64(16 * (size_t)op->dim);
+      launch_convert(MB_PREC_F32, MB_PREC_F64, op->dim, xt.p, x64.p, st);
+      launch_apply(op->view, MB_PREC_F64, x64.p, y64.p, 1.0, 0.0, 0.0, nullptr, kr.red.p(), 7, st);
+      const double* h = kr.red.fetch(kr.grid_apply, 3, st);
+      MB_REQUIRE(h[2] > 0.0, MB_ERR_ZERO_NORM, "Ritz vector has zero norm");
+      *e_out = h[0] / h[2];
+    }
+    if (vec) from_tensor(op, xt.p, vec, order, st);
   }
   MB_CUDA(cudaStreamSynchronize(st));
 }

@@ -105,3 +105,37 @@ def test_engine_rejects_bad_requests(mb, cuda):
         eng.try_submit(mb.sector((1, 4), 1, 1, 1.0, 1.0), 0, 10)   # size-1 dimension
     with pytest.raises(mb.MbError):
         eng.try_submit(mb.sector((6,), 3, 3, 1.0, 1.0), 0, 10000)  # kmax > 512
+
+
+def test_dos_requests_match_oracle_and_mix_with_ground_states(mb, cuda):
+    """KPM DOS requests (complex64 Chebyshev, FP64 moment sums) next to ground-
+    state requests in one engine: moments within 1e-4 of the oracle's FP64
+    moments with the same bounds and probes; spectrum inside the bounds."""
+    eng = mb.Engine()
+    d_dos = mb.sector((6,), 3, 3, 1.0, 4.0)
+    d_gs = mb.sector((8,), 4, 4, 1.0, 4.0)
+    M, R = 64, 2
+    rid = eng.try_submit_dos(d_dos, n_moments=M, n_probes=R, seed=5)
+    gid = eng.try_submit(d_gs, seed=1, kmax=200, rel_tol=1e-12)
+    while eng.step(4):
+        pass
+    mu, lo, hi, lat = eng.poll_dos(rid)
+    H = oracle.hubbard_csc([6], 1.0, 4.0, 3, 3)
+    E = np.linalg.eigvalsh(H.to_dense())
+    assert lo <= E[0] + 1e-9 and hi >= E[-1] - 1e-9          # bounds enclose the spectrum
+    a = (hi - lo) / 2 * 1.01
+    b = (hi + lo) / 2
+    basis = mb.FermionBasis.with_fixed_particle_number_and_spin(6, 6, 0)
+    perm = basis.permutation()
+    ref = np.zeros(M)
+    for p in range(R):
+        rt = oracle.philox_phase(5, H.dim, 1 + p)
+        r = np.empty_like(rt)
+        r[perm] = rt
+        ref += H.kpm_dos_moments(r, M, a, b)
+    ref /= R * H.dim
+    assert abs(mu[0] - 1.0) < 1e-6
+    assert np.max(np.abs(mu - ref)) <= 1e-4
+    g = eng.poll(gid)
+    e_exact = exact_e0((8,), 4, 4, 4.0)
+    assert abs(g.e0 - e_exact) <= 1e-8 * abs(e_exact)

@@ -324,3 +324,14 @@ def test_full_size_operator_properties(mb, cuda, dims, n):
     hx32 = op32.apply(x32, order=mb.ORDER_TENSOR)
     rel = float(torch.linalg.norm(hx32.to(torch.complex128) - hx)) / float(torch.linalg.norm(hx))
     assert rel < 2e-6
+
+
+def test_fp32_lanczos_with_fp64_refinement(mb, cuda):
+    """Precision path: complex64 vectors, FP64 alpha/beta and re-orthogonalisation
+    coefficients, one FP64 Rayleigh-quotient sweep: |dE0| <= 1e-8 |E0|."""
+    _, _, op = make(mb, [3, 3], 1.0, 8.0, 3, 2, prec=1)
+    E = np.linalg.eigvalsh(oracle.hubbard_csc([3, 3], 1.0, 8.0, 3, 2).to_dense())
+    raw = mb.find_min_eigenpair(op, 150, reorth=True, want_vector=False)
+    ref = mb.find_min_eigenpair(op, 150, reorth=True, want_vector=False, refine=True)
+    assert abs(raw.value - E[0]) <= 1e-5 * abs(E[0])
+    assert abs(ref.value - E[0]) <= 1e-8 * abs(E[0])
