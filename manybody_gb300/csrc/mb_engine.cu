@@ -724,16 +724,10 @@ double rayleigh_fp64(mb_engine_s* e, EngineSlot& s, const SlotDesc& d) {
   EngBuf duf(sizeof(double) * uf.size());
   MB_CUDA(cudaMemcpy(duf.p, uf.data(), sizeof(double) * uf.size(), cudaMemcpyHostToDevice));
   v.u_fold = (const double*)duf.p;
-  EngBuf xd(16 * (size_t)s.dim), yd(16 * (size_t)s.dim);
+  EngBuf xd(16 * (size_t)s.dim);
   k_f32_to_f64<<<256, 256, 0, e->st>>>(d.xacc, (double2*)xd.p, s.dim);
-  const int g = apply_grid(v, MB_PREC_F64);
-  EngBuf part(sizeof(double) * 3 * (size_t)std::max(g, 1)), out(sizeof(double) * 3);
-  launch_apply(v, MB_PREC_F64, xd.p, yd.p, 1.0, 0.0, 0.0, nullptr, (double*)part.p, 7, e->st);
-  launch_reduce((const double*)part.p, g, 3, (double*)out.p, e->st);
-  double h[3];
-  MB_CUDA(cudaMemcpyAsync(h, out.p, sizeof(h), cudaMemcpyDeviceToHost, e->st));
-  MB_CUDA(cudaStreamSynchronize(e->st));
-  return h[0] / h[2];  // <x, H x> / <x, x>
+  // Rayleigh-Ritz on span{x, Hx, H^2 x} in FP64 (first step: <x,Hx>/<x,x>)
+  return fp64_ritz_refine(v, xd.p, 3, e->st);
 }
 
 // Seed probe `p` of a DOS request into buf[1] and arm Chebyshev mode.

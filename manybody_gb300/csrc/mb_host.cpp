@@ -95,6 +95,38 @@ HopTable build_hop_table(const SpinSector& s, const mb_model_s& m) {
   return t;
 }
 
+std::vector<int32_t> rcm_order(const HopTable& t, int64_t D) {
+  std::vector<int32_t> order;
+  order.reserve((size_t)D);
+  std::vector<char> seen((size_t)D, 0);
+  auto deg = [&](int64_t r) { return t.off[(size_t)r + 1] - t.off[(size_t)r]; };
+  std::vector<int32_t> nb;
+  for (int64_t start = 0; (int64_t)order.size() < D; ++start) {
+    if (seen[(size_t)start]) continue;
+    // the first unvisited state roots a breadth-first sweep of its component
+    size_t head = order.size();
+    seen[(size_t)start] = 1;
+    order.push_back((int32_t)start);
+    while (head < order.size()) {
+      const int32_t r = order[head++];
+      nb.clear();
+      for (int32_t j = t.off[(size_t)r]; j < t.off[(size_t)r + 1]; ++j) {
+        const int32_t q = (int32_t)(t.ent[(size_t)j] >> 8);
+        if (!seen[(size_t)q]) {
+          seen[(size_t)q] = 1;
+          nb.push_back(q);
+        }
+      }
+      std::sort(nb.begin(), nb.end(), [&](int32_t a, int32_t b) {
+        return deg(a) != deg(b) ? deg(a) < deg(b) : a < b;
+      });
+      order.insert(order.end(), nb.begin(), nb.end());
+    }
+  }
+  std::reverse(order.begin(), order.end());
+  return order;
+}
+
 std::vector<double> u_fold_table(double u, bool has_u, int L) {
   std::vector<double> f((size_t)L + 1, 0.0);
   double acc = 0.0;

@@ -160,6 +160,10 @@ struct HopTable {
 };
 HopTable build_hop_table(const SpinSector& s, const mb_model_s& m);
 
+// Reverse Cuthill-McKee order of the states of a hop table (BFS from a
+// low-degree state, neighbours by increasing degree, reversed).
+std::vector<int32_t> rcm_order(const HopTable& t, int64_t D);
+
 // Left fold U + U + ... (k terms), the order-independent value the reference
 // accumulates for k doubly occupied sites (matrix_elements.h:85-96).
 std::vector<double> u_fold_table(double u, bool has_u, int L);
@@ -190,6 +194,9 @@ struct OpView {
   // mask, the mask of sites strictly between its ends, its multiplicity;
   // colex-rank tables in 8-bit chunks: rank(m) = sum_k
   // dn_rank[(k*(n+1) + cb_k)*256 + byte_k(m)], cb_k = set bits below chunk k.
+  // Row processing order of the fused apply (reverse Cuthill-McKee of the
+  // up-hop graph): rows processed together share more neighbour rows in L2.
+  const int32_t* row_sched;
   const unsigned long long* dn_vmask;
   const uint32_t* bond_pair;
   const uint32_t* bond_between;
@@ -214,6 +221,7 @@ struct mb_op_s {
   mb::OpView view{};
   std::vector<void*> allocations;  // device buffers owned by the op
   int32_t* perm = nullptr;         // tensor -> reference index (lazy)
+  int32_t* iperm = nullptr;        // reference -> tensor index (lazy)
   std::mutex mu;
   struct Scratch {
     void* a = nullptr;  // tensor-order copies for reference-order calls
@@ -275,6 +283,15 @@ void launch_csr_fill(const OpView& v, const int32_t* perm, const int64_t* row_pt
 void upload_binomials(cudaStream_t st);
 // tensor -> reference index table of an operator, built on first use
 int32_t* op_perm(mb_op_s* op);
+// reference -> tensor index table (inverse of op_perm), built on first use
+int32_t* op_iperm(mb_op_s* op);
+void launch_invert_perm(int64_t n, const int32_t* perm, int32_t* iperm, cudaStream_t st);
+
+// FP64 refinement of a ground-state estimate: Rayleigh-Ritz on the Krylov
+// space span{x, Hx, ..., H^(steps-1) x} with FP64 vectors and arithmetic
+// (Lanczos with full re-orthogonalisation), x complex128 in tensor order.
+// Returns the lowest Ritz value.
+double fp64_ritz_refine(const OpView& v, const void* x64, int steps, cudaStream_t st);
 
 // Host tridiagonal eigensolver (implicit QL, mb_tridiag.cpp).
 bool tridiag_eig(int n, std::vector<double>& d, const std::vector<double>& e,

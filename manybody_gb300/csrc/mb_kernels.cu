@@ -146,7 +146,8 @@ k_apply(OpView v, const typename C2<T>::type* __restrict__ x, typename C2<T>::ty
   const int64_t Dd = v.Dd;
   DotAcc<T> a_xy, a_yy, a_xx;
 
-  for (int64_t r = blockIdx.x; r < v.Du; r += gridDim.x) {
+  for (int64_t ri = blockIdx.x; ri < v.Du; ri += gridDim.x) {
+    const int64_t r = v.row_sched ? (int64_t)v.row_sched[ri] : ri;
     const V2* xrow = x + r * Dd;
     __syncthreads();
     const int u0 = v.up_off[r], nup = v.up_off[r + 1] - u0;
@@ -593,6 +594,17 @@ __global__ void k_perm(OpView v, int32_t* __restrict__ perm) {
     const int64_t ru = i / v.Dd, rd = i - ru * v.Dd;
     perm[i] = (int32_t)reference_rank(sb, v.up_mask[ru], v.dn_mask[rd], v.L);
   }
+}
+
+__global__ void k_invert_perm(int64_t n, const int32_t* __restrict__ perm, int32_t* __restrict__ iperm) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    iperm[perm[i]] = (int32_t)i;
+}
+
+void launch_invert_perm(int64_t n, const int32_t* perm, int32_t* iperm, cudaStream_t st) {
+  k_invert_perm<<<blas_grid(n), kBlasThreads, 0, st>>>(n, perm, iperm);
+  MB_CUDA(cudaGetLastError());
 }
 
 void launch_perm(const OpView& v, int32_t* perm, cudaStream_t st) {

@@ -142,6 +142,7 @@ static void build_op(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m) {
   }
   v.max_up_degree = tu.max_degree;
   v.max_dn_degree = td.max_degree;
+  v.row_sched = upload(op, rcm_order(tu, op->Du));
   {
     // slot-major copy of the down-hop table (coalesced across columns)
     MB_REQUIRE(td.max_degree <= 255, MB_ERR_CAPACITY, "more than 255 hops from one state");
@@ -255,6 +256,20 @@ int32_t* op_perm(mb_op_s* op) {
   return op->perm;
 }
 
+int32_t* op_iperm(mb_op_s* op) {
+  ensure_perm(op);
+  std::lock_guard<std::mutex> lk(op->mu);
+  if (!op->iperm) {
+    void* p = nullptr;
+    MB_CUDA(cudaMalloc(&p, sizeof(int32_t) * (size_t)op->dim));
+    op->allocations.push_back(p);
+    launch_invert_perm(op->dim, op->perm, (int32_t*)p, 0);
+    MB_CUDA(cudaStreamSynchronize(0));
+    op->iperm = (int32_t*)p;
+  }
+  return op->iperm;
+}
+
 static void to_tensor(mb_op_s* op, const void* src, void* dst, int order, cudaStream_t st) {
   if (order == MB_ORDER_TENSOR) {
     if (src != dst)
@@ -273,8 +288,8 @@ static void from_tensor(mb_op_s* op, const void* src, void* dst, int order, cuda
                               cudaMemcpyDeviceToDevice, st));
     return;
   }
-  ensure_perm(op);
-  launch_scatter(op->precision, op->dim, op->perm, src, dst, st);
+  // y_ref[i] = y_tensor[iperm[i]]: coalesced writes, random reads
+  launch_gather(op->precision, op->dim, op_iperm(op), src, dst, st);
 }
 
 static void check_order(int order) {
@@ -471,6 +486,47 @@ struct Krylov {
   }
 };
 
+double fp64_ritz_refine(const OpView& v, const void* x64, int steps, cudaStream_t st) {
+  const int64_t n = v.dim;
+  const size_t vb = 16 * (size_t)n;
+  steps = std::max(1, std::min(steps, 8));
+  const int ga = apply_grid(v, MB_PREC_F64), gb = blas_grid(n);
+  Reducer red(std::max(std::max(ga, gb), multi_dot_grid(n)), 2 * 8 + 4);
+  DevBuf basis(vb * (size_t)steps), w(vb), coef(sizeof(double) * 2 * 8);
+  auto col = [&](int j) { return (char*)basis.p + vb * (size_t)j; };
+  // v0 = x / ||x||
+  launch_dot(MB_PREC_F64, n, x64, x64, red.p(), st);
+  const double nx = std::sqrt(red.fetch(gb, 3, st)[2]);
+  MB_REQUIRE(nx > 0.0, MB_ERR_ZERO_NORM, "refinement start vector has zero norm");
+  launch_axpby(MB_PREC_F64, n, 1.0 / nx, 0.0, x64, 0.0, 0.0, col(0), nullptr, 0, st);
+  std::vector<double> alpha, beta;
+  for (int j = 0; j < steps; ++j) {
+    const double bprev = j ? beta.back() : 0.0;
+    launch_apply(v, MB_PREC_F64, col(j), w.p, 1.0, 0.0, -bprev, j ? col(j - 1) : nullptr,
+                 red.p(), 1, st);
+    const double a = red.fetch(ga, 3, st)[0];
+    alpha.push_back(a);
+    launch_axpby(MB_PREC_F64, n, -a, 0.0, col(j), 1.0, 0.0, w.p, nullptr, 0, st);
+    double nn = 0.0;
+    for (int pass = 0; pass < 2; ++pass) {  // CGS2 against the j+1 basis vectors
+      launch_multi_dot(MB_PREC_F64, MB_PREC_F64, n, basis.p, n, j + 1, w.p, red.p(), st);
+      launch_reduce(red.p(), multi_dot_grid(n), 2 * (j + 1), (double*)coef.p, st);
+      launch_multi_axpy(MB_PREC_F64, MB_PREC_F64, n, basis.p, n, j + 1, (const double*)coef.p, w.p,
+                        red.p(), st);
+      nn = red.fetch(gb, 3, st)[1];
+    }
+    const double b = std::sqrt(nn);
+    if (j + 1 == steps || !(b > kTol)) break;
+    beta.push_back(b);
+    launch_axpby(MB_PREC_F64, n, 1.0 / b, 0.0, w.p, 0.0, 0.0, col(j + 1), nullptr, 0, st);
+  }
+  const int m = (int)alpha.size();
+  std::vector<double> d(alpha), e(beta);
+  e.resize((size_t)std::max(m - 1, 0));
+  MB_REQUIRE(tridiag_eig(m, d, e, nullptr), MB_ERR_EIG_FAILED, "Eigenvalue decomposition of T_k failed");
+  return d[0];
+}
+
 static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
                       const mb_lanczos_opts* opts, double sign, double* e_out, void* vec,
                       int64_t* steps_out) {
@@ -522,14 +578,13 @@ static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
       kr.pass_two(bt.p, m, sign, alphas, betas, b_norm, y, xt.p);
     }
     if (refine) {
-      // One FP64 Rayleigh-quotient sweep on the FP32 Ritz vector x:
-      // E = <x, H x> / <x, x> with FP64 vectors and arithmetic.
-      DevBuf x64(16 * (size_t)op->dim), y64(16 * (size_t)op->dim);
+      // FP64 refinement of the FP32 Ritz vector x: Rayleigh-Ritz on
+      // span{x, Hx, H^2 x} with FP64 vectors and arithmetic (its first step is
+      // the Rayleigh quotient <x,Hx>/<x,x>; two more Krylov directions remove
+      // the FP32 error of x to second order).
+      DevBuf x64(16 * (size_t)op->dim);
       launch_convert(MB_PREC_F32, MB_PREC_F64, op->dim, xt.p, x64.p, st);
-      launch_apply(op->view, MB_PREC_F64, x64.p, y64.p, 1.0, 0.0, 0.0, nullptr, kr.red.p(), 7, st);
-      const double* h = kr.red.fetch(kr.grid_apply, 3, st);
-      MB_REQUIRE(h[2] > 0.0, MB_ERR_ZERO_NORM, "Ritz vector has zero norm");
-      *e_out = h[0] / h[2];
+      *e_out = fp64_ritz_refine(op->view, x64.p, 3, st);
     }
     if (vec) from_tensor(op, xt.p, vec, order, st);
   }

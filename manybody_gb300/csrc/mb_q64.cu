@@ -162,7 +162,8 @@ k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlon
   __int128 a_xy = 0, a_yy = 0;
   unsigned long long mor = 0;
 
-  for (int64_t r = blockIdx.x; r < v.Du; r += gridDim.x) {
+  for (int64_t ri = blockIdx.x; ri < v.Du; ri += gridDim.x) {
+    const int64_t r = v.row_sched ? (int64_t)v.row_sched[ri] : ri;
     const longlong2* xrow = x + r * Dd;
     __syncthreads();
     const int u0 = v.up_off[r], nup = v.up_off[r + 1] - u0;
@@ -647,14 +648,15 @@ __global__ void k_to_fixed(int64_t n, const double2* __restrict__ src, const int
   }
 }
 
+// dst[i] = value(src[iperm ? iperm[i] : i]) (iperm: reference -> tensor index)
 __global__ void k_from_fixed(int64_t n, const longlong2* __restrict__ src,
-                             const int32_t* __restrict__ perm, const int* __restrict__ ey,
+                             const int32_t* __restrict__ iperm, const int* __restrict__ ey,
                              double2* __restrict__ dst) {
   const int E = *ey;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const longlong2 q = src[i];
-    dst[perm ? (int64_t)perm[i] : i] = make_double2(fixed_to_f64(q.x, E), fixed_to_f64(q.y, E));
+    const longlong2 q = src[iperm ? (int64_t)iperm[i] : i];
+    dst[i] = make_double2(fixed_to_f64(q.x, E), fixed_to_f64(q.y, E));
   }
 }
 
@@ -675,9 +677,9 @@ void launch_f64_to_q(int64_t n, const void* src, const int32_t* perm, int qbits,
   MB_CUDA(cudaGetLastError());
 }
 
-void launch_q_to_f64(int64_t n, const void* src, const int32_t* perm, const int* e_dev, void* dst,
+void launch_q_to_f64(int64_t n, const void* src, const int32_t* iperm, const int* e_dev, void* dst,
                      cudaStream_t st) {
-  k_from_fixed<<<q_blas_grid(n), kQBlas, 0, st>>>(n, (const longlong2*)src, perm, e_dev,
+  k_from_fixed<<<q_blas_grid(n), kQBlas, 0, st>>>(n, (const longlong2*)src, iperm, e_dev,
                                                    (double2*)dst);
   MB_CUDA(cudaGetLastError());
 }

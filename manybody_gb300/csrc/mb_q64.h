@@ -57,7 +57,9 @@ int q_multi_dot_grid(int64_t n);
 // (max biased exponent, resulting E).
 void launch_f64_to_q(int64_t n, const void* src, const int32_t* perm, int qbits, int* scratch_int2,
                      void* dst, cudaStream_t st);
-void launch_q_to_f64(int64_t n, const void* src, const int32_t* perm, const int* e_dev, void* dst,
+// Q64 (tensor order) -> FP64; with iperm (reference -> tensor index) the
+// output is in reference order.
+void launch_q_to_f64(int64_t n, const void* src, const int32_t* iperm, const int* e_dev, void* dst,
                      cudaStream_t st);
 void launch_q_plan(const QPlanInput& in, const int* ex_dev, QParams* p_dev, cudaStream_t st);
 void launch_q_lincomb(int64_t n, const void* a, long long ar, long long ai, const void* b,

@@ -108,6 +108,7 @@ void q_apply_affine(mb_op_s* op, const void* x, void* y, double scale, double sh
                     const void* z, int order, cudaStream_t st) {
   auto& s = qscratch_for(op, st);
   int32_t* perm = order == MB_ORDER_REFERENCE ? op_perm(op) : nullptr;
+  int32_t* iperm = order == MB_ORDER_REFERENCE ? op_iperm(op) : nullptr;
   launch_f64_to_q(op->dim, x, perm, op->q_qbits, s.ints, s.xq, st);
   launch_q_plan(plan_input(op, scale, shift, 0.0, 0, 0, false), s.ints + 1, (QParams*)s.prm, st);
   launch_apply_q2(op->view, op->q_has_double, s.xq, s.yq, nullptr, s.sq, (const QParams*)s.prm,
@@ -115,13 +116,13 @@ void q_apply_affine(mb_op_s* op, const void* x, void* y, double scale, double sh
   // the output exponent sits in the planned QParams (field ey)
   const int* ey = (const int*)((const char*)s.prm + offsetof(QParams, ey));
   if (!z) {
-    launch_q_to_f64(op->dim, s.yq, perm, ey, y, st);
+    launch_q_to_f64(op->dim, s.yq, iperm, ey, y, st);
     return;
   }
   // y = beta z + (Q64 result): z may alias y; convert into a tensor-order
   // temporary, then combine with the FP64 vector kernel.
   QBuf tmp(sizeof(double2) * (size_t)op->dim);
-  launch_q_to_f64(op->dim, s.yq, perm, ey, tmp.p, st);
+  launch_q_to_f64(op->dim, s.yq, iperm, ey, tmp.p, st);
   launch_axpby(MB_PREC_F64, op->dim, beta, 0.0, z, 1.0, 0.0, tmp.p, nullptr, 0, st);
   MB_CUDA(cudaMemcpyAsync(y, tmp.p, sizeof(double2) * (size_t)op->dim, cudaMemcpyDeviceToDevice, st));
   MB_CUDA(cudaStreamSynchronize(st));
@@ -399,10 +400,10 @@ struct QKrylov {
   }
 
   void store(const QRef& x, int order, void* dst) {
-    int32_t* perm = order == MB_ORDER_REFERENCE ? op_perm(op) : nullptr;
+    int32_t* iperm = order == MB_ORDER_REFERENCE ? op_iperm(op) : nullptr;
     QBuf e(sizeof(int));
     MB_CUDA(cudaMemcpyAsync(e.p, &x.E, sizeof(int), cudaMemcpyHostToDevice, st));
-    launch_q_to_f64(n, x.p, perm, (const int*)e.p, dst, st);
+    launch_q_to_f64(n, x.p, iperm, (const int*)e.p, dst, st);
     MB_CUDA(cudaStreamSynchronize(st));
   }
 };
@@ -516,10 +517,10 @@ int mb_q64_to_f64(mb_op_t op, const void* xq_dev, int exponent, int order, void*
     MB_REQUIRE(order == MB_ORDER_REFERENCE || order == MB_ORDER_TENSOR, MB_ERR_INVALID_ARG,
                "bad order");
     cudaStream_t st = (cudaStream_t)stream;
-    int32_t* perm = order == MB_ORDER_REFERENCE ? op_perm(op) : nullptr;
+    int32_t* iperm = order == MB_ORDER_REFERENCE ? op_iperm(op) : nullptr;
     QBuf e(sizeof(int));
     MB_CUDA(cudaMemcpyAsync(e.p, &exponent, sizeof(int), cudaMemcpyHostToDevice, st));
-    launch_q_to_f64(op->dim, xq_dev, perm, (const int*)e.p, x_dev, st);
+    launch_q_to_f64(op->dim, xq_dev, iperm, (const int*)e.p, x_dev, st);
     MB_CUDA(cudaStreamSynchronize(st));
   });
 }
