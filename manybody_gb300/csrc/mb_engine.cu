@@ -501,6 +501,7 @@ struct EngineSlot {
   double last_ritz = 0.0;
   bool have_ritz = false;
   int m = 0;                      // pass-one steps
+  int m_ritz = 0;                 // steps replayed for the Ritz vector
   double e_raw = 0.0, e0 = 0.0;
   std::chrono::steady_clock::time_point t_submit, t_done;
 };
@@ -684,7 +685,7 @@ void arm_slot(mb_engine_s* e, EngineSlot& s, SlotDesc& d, bool replay) {
   d.k = 0;
   if (replay) {
     d.mode = kModeReplay;
-    d.steps = s.m;
+    d.steps = s.m_ritz;
   } else {
     d.mode = kModeLanczos;
     d.steps = 0;
@@ -819,11 +820,15 @@ void after_step(mb_engine_s* e) {
         std::vector<double> a((size_t)m), b((size_t)m), y;
         MB_CUDA(cudaMemcpy(a.data(), d.alpha, sizeof(double) * m, cudaMemcpyDeviceToHost));
         MB_CUDA(cudaMemcpy(b.data(), d.beta, sizeof(double) * m, cudaMemcpyDeviceToHost));
-        s.e_raw = -ritz_min(a, b, m, s.refine ? &y : nullptr);
+        s.e_raw = -ritz_min(a, b, m, nullptr);
         s.e0 = s.e_raw;
         if (s.refine && m > 0) {
+          // Ritz vector from the first converged checkpoint, before a ghost
+          // copy of the ground state can enter T_m
+          s.m_ritz = ritz_vector_steps(a, b, m, s.check_every, 1e-9);
+          ritz_min(a, b, s.m_ritz, &y);
           for (auto& yv : y) yv *= s.b_norm;
-          MB_CUDA(cudaMemcpy(d.yk, y.data(), sizeof(double) * m, cudaMemcpyHostToDevice));
+          MB_CUDA(cudaMemcpy(d.yk, y.data(), sizeof(double) * s.m_ritz, cudaMemcpyHostToDevice));
           arm_slot(e, s, d, true);
           // x = y_0 v_0, v_prev = 0
           const int2* it = (const int2*)e->d_items->p;

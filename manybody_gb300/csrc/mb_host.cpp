@@ -127,6 +127,111 @@ std::vector<int32_t> rcm_order(const HopTable& t, int64_t D) {
   return order;
 }
 
+SignedLists signed_lists(const HopTable& t, int64_t D) {
+  SignedLists s;
+  s.off.resize((size_t)D + 1);
+  s.pos.resize((size_t)D);
+  s.list.reserve(t.ent.size() + 1);
+  s.off[0] = 0;
+  for (int64_t r = 0; r < D; ++r) {
+    const size_t start = s.list.size();
+    for (int neg = 0; neg < 2; ++neg) {
+      for (int32_t j = t.off[(size_t)r]; j < t.off[(size_t)r + 1]; ++j) {
+        const uint32_t e = t.ent[(size_t)j];
+        if ((int)(e & 1u) != neg) continue;
+        s.list.push_back(e >> 8);
+        if (e & 2u) s.list.push_back(e >> 8);
+      }
+      if (!neg) s.pos[(size_t)r] = (int32_t)(s.list.size() - start);
+    }
+    MB_REQUIRE(s.list.size() < (size_t)INT32_MAX, MB_ERR_CAPACITY, "hop table too large");
+    s.off[(size_t)r + 1] = (int32_t)s.list.size();
+    s.max_len = std::max(s.max_len, (int)(s.list.size() - start));
+  }
+  if (s.list.empty()) s.list.push_back(0u);
+  return s;
+}
+
+SlicedTable sliced_table(const HopTable& t, int64_t D) {
+  MB_REQUIRE(D < (int64_t(1) << 27), MB_ERR_CAPACITY, "sector too large for the sliced table");
+  SlicedTable s;
+  const int64_t ng = (D + 31) / 32;
+  s.grp.resize((size_t)(2 * ng));
+  s.nneg.assign((size_t)D, 0);
+  const uint32_t pad = (uint32_t)(16 * D);
+  std::vector<uint32_t> col;
+  for (int64_t g = 0; g < ng; ++g) {
+    int k = 0;
+    for (int64_t c = 32 * g; c < std::min(D, 32 * g + 32); ++c) {
+      int n = 0;
+      for (int32_t j = t.off[(size_t)c]; j < t.off[(size_t)c + 1]; ++j) n += (t.ent[(size_t)j] & 2u) ? 2 : 1;
+      k = std::max(k, n);
+    }
+    const size_t base = s.ent.size();
+    MB_REQUIRE(base + (size_t)32 * k < (size_t)INT32_MAX, MB_ERR_CAPACITY, "hop table too large");
+    s.grp[(size_t)(2 * g)] = (int32_t)base;
+    s.grp[(size_t)(2 * g + 1)] = k;
+    s.ent.resize(base + (size_t)32 * k, pad);
+    for (int64_t c = 32 * g; c < std::min(D, 32 * g + 32); ++c) {
+      col.clear();
+      for (int32_t j = t.off[(size_t)c]; j < t.off[(size_t)c + 1]; ++j) {
+        const uint32_t e = t.ent[(size_t)j];
+        const uint32_t w = (16u * (e >> 8)) | ((e & 1u) << 31);
+        col.push_back(w);
+        if (e & 2u) col.push_back(w);
+        s.nneg[(size_t)c] += (uint8_t)((e & 1u) * ((e & 2u) ? 2 : 1));
+      }
+      for (size_t j = 0; j < col.size(); ++j) s.ent[base + 32 * j + (size_t)(c - 32 * g)] = col[j];
+    }
+  }
+  if (s.ent.empty()) s.ent.push_back(pad);
+  return s;
+}
+
+// Largest eigenvalue of the symmetric tridiagonal T_m (diagonal a, off-
+// diagonal b) by bisection on the Sturm count (number of eigenvalues below x
+// = number of negative pivots of the LDL^T factorisation of T - x).
+double tridiag_max_eig(const double* a, const double* b, int m) {
+  double lo = a[0], hi = a[0];
+  for (int i = 0; i < m; ++i) {
+    const double r = (i > 0 ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < m ? std::fabs(b[i]) : 0.0);
+    lo = std::min(lo, a[i] - r);
+    hi = std::max(hi, a[i] + r);
+  }
+  const double tiny = 1e-300;
+  for (int it = 0; it < 200; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (!(mid > lo && mid < hi)) break;
+    int below = 0;
+    double q = 1.0;
+    for (int i = 0; i < m; ++i) {
+      q = a[i] - mid - (i > 0 ? b[i - 1] * b[i - 1] / q : 0.0);
+      if (q == 0.0) q = -tiny;
+      if (q < 0.0) ++below;
+    }
+    if (below == m) hi = mid;
+    else lo = mid;
+  }
+  return hi;
+}
+
+int ritz_vector_steps(const std::vector<double>& a, const std::vector<double>& b, int m,
+                      int every, double tol) {
+  if (every <= 0) every = 10;
+  double prev = 0.0;
+  bool have = false;
+  int loose = 0;  // first checkpoint within the FP32 rounding level
+  for (int k = every; k < m; k += every) {
+    const double th = tridiag_max_eig(a.data(), b.data(), k);
+    const double moved = std::fabs(th - prev);
+    if (have && moved <= tol * std::fabs(th)) return k;
+    if (have && !loose && moved <= 1e-7 * std::fabs(th)) loose = k;
+    prev = th;
+    have = true;
+  }
+  return loose ? loose : m;
+}
+
 std::vector<double> u_fold_table(double u, bool has_u, int L) {
   std::vector<double> f((size_t)L + 1, 0.0);
   double acc = 0.0;

@@ -164,6 +164,43 @@ HopTable build_hop_table(const SpinSector& s, const mb_model_s& m);
 // low-degree state, neighbours by increasing degree, reversed).
 std::vector<int32_t> rcm_order(const HopTable& t, int64_t D);
 
+// Largest eigenvalue of the symmetric tridiagonal matrix (a[0..m), b[0..m-1)).
+double tridiag_max_eig(const double* a, const double* b, int m);
+
+// Steps of a finished Lanczos run (on an operator whose extremal eigenvalue
+// sought is the largest) to build the Ritz vector from.  Without full re-
+// orthogonalisation, and with FP32 vectors early, the recurrence loses
+// orthogonality once that Ritz value has converged, and some steps later a
+// second copy of it appears in T_m; a Ritz vector from T_m past that point
+// can be a near-cancelling mix of the two copies.  Returns the first
+// checkpoint k (multiples of `every`) whose largest Ritz value moved by at
+// most tol * |value| since the previous checkpoint, else the first that
+// moved by at most 1e-7 * |value|, else m.
+int ritz_vector_steps(const std::vector<double>& a, const std::vector<double>& b, int m,
+                      int every, double tol);
+
+// Hop lists of the fused block-floating-point apply, signs resolved ahead:
+// per state the target ranks with the positive hops first and doubled bonds
+// listed twice (so the kernel needs neither a sign nor a weight per hop).
+struct SignedLists {
+  std::vector<uint32_t> list;  // target ranks
+  std::vector<int32_t> off;    // [D+1]
+  std::vector<int32_t> pos;    // [D] number of positive hops
+  int max_len = 0;
+};
+SignedLists signed_lists(const HopTable& t, int64_t D);
+
+// Sliced-ELL copy of a hop table over groups of 32 consecutive states:
+// group g's slot j for lane l is ent[grp[2g] + 32 j + l] = 16 * target |
+// (negative << 31), doubled bonds listed twice, padding 16 * D (one zero
+// element past the row); grp[2g+1] = slots of group g.
+struct SlicedTable {
+  std::vector<uint32_t> ent;
+  std::vector<int32_t> grp;
+  std::vector<uint8_t> nneg;  // [D] negative entries per state
+};
+SlicedTable sliced_table(const HopTable& t, int64_t D);
+
 // Left fold U + U + ... (k terms), the order-independent value the reference
 // accumulates for k doubly occupied sites (matrix_elements.h:85-96).
 std::vector<double> u_fold_table(double u, bool has_u, int L);
@@ -184,27 +221,18 @@ struct OpView {
   const float* u_fold_f;    // float copies for complex64 operators
   const float* self_up_f;
   const float* self_dn_f;
-  // Down hops again in slot-major ("ELL") layout for coalesced reads:
-  // dn_ell[j * Dd + c] is column c's j-th entry, j < dn_cnt[c] <= dn_ell_k.
-  const uint32_t* dn_ell;
-  const uint8_t* dn_cnt;
-  int dn_ell_k;
-  // On-the-fly down hops (lattices with <= 64 bonds): per down state the
-  // bitmask of bonds with exactly one occupied end; per bond its two-site
-  // mask, the mask of sites strictly between its ends, its multiplicity;
-  // colex-rank tables in 8-bit chunks: rank(m) = sum_k
-  // dn_rank[(k*(n+1) + cb_k)*256 + byte_k(m)], cb_k = set bits below chunk k.
-  // Row processing order of the fused apply (reverse Cuthill-McKee of the
-  // up-hop graph): rows processed together share more neighbour rows in L2.
+  // Row processing order of the fused applies (reverse Cuthill-McKee of the
+  // up-hop graph): rows in flight together share more neighbour rows in L2.
   const int32_t* row_sched;
-  const unsigned long long* dn_vmask;
-  const uint32_t* bond_pair;
-  const uint32_t* bond_between;
-  const uint32_t* bond_mult;
-  const int32_t* dn_rank;
-  int n_bonds;
-  int dn_nchunks;
-  int dn_n;
+  // Sign-resolved hop lists of the fused block-floating-point apply (see
+  // SignedLists / SlicedTable): up hops by row, down hops sliced by column.
+  const uint32_t* up_list;
+  const int32_t* up_loff;
+  const int32_t* up_lpos;
+  const uint32_t* dn_sell;
+  const int32_t* dn_sgrp;
+  const uint8_t* dn_nneg;  // per down state: number of negative hops (doubled twice)
+  int max_up_list;
   double t;
   int max_up_degree;
   int max_dn_degree;
@@ -238,7 +266,6 @@ struct mb_op_s {
   struct QScratch {
     void* xq = nullptr;
     void* yq = nullptr;
-    void* sq = nullptr;    // down-hop partial sums of the two-pass apply
     void* prm = nullptr;   // QParams
     int* ints = nullptr;   // [max exp, Ex, unused, unused]
   };

@@ -143,66 +143,6 @@ static void build_op(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m) {
   v.max_up_degree = tu.max_degree;
   v.max_dn_degree = td.max_degree;
   v.row_sched = upload(op, rcm_order(tu, op->Du));
-  {
-    // slot-major copy of the down-hop table (coalesced across columns)
-    MB_REQUIRE(td.max_degree <= 255, MB_ERR_CAPACITY, "more than 255 hops from one state");
-    const int K = std::max(td.max_degree, 1);
-    std::vector<uint32_t> ell((size_t)K * (size_t)op->Dd, 0u);
-    std::vector<uint8_t> cnt((size_t)op->Dd, 0);
-    for (int64_t c = 0; c < op->Dd; ++c) {
-      const int32_t o0 = td.off[(size_t)c], o1 = td.off[(size_t)c + 1];
-      cnt[(size_t)c] = (uint8_t)(o1 - o0);
-      for (int32_t j = o0; j < o1; ++j) ell[(size_t)(j - o0) * (size_t)op->Dd + (size_t)c] = td.ent[(size_t)j];
-    }
-    v.dn_ell = upload(op, ell);
-    v.dn_cnt = upload(op, cnt);
-    v.dn_ell_k = K;
-  }
-  if (m->has_hop && !m->bonds.empty() && m->bonds.size() <= 64) {
-    // on-the-fly down hops: bonds, per-state valid-bond masks, rank tables
-    const int nb = (int)m->bonds.size();
-    std::vector<uint32_t> pair((size_t)nb), betw((size_t)nb), mult((size_t)nb);
-    for (int b = 0; b < nb; ++b) {
-      const auto& bd = m->bonds[(size_t)b];
-      pair[(size_t)b] = (1u << bd.a) | (1u << bd.b);
-      betw[(size_t)b] = ((1u << bd.b) - 1u) & ~((2u << bd.a) - 1u);
-      mult[(size_t)b] = (uint32_t)bd.mult;
-    }
-    const SpinSector& dsec = b->down;
-    std::vector<unsigned long long> vm((size_t)dsec.D, 0ull);
-    for (int64_t r = 0; r < dsec.D; ++r) {
-      const uint32_t d = dsec.masks[(size_t)r];
-      unsigned long long bits = 0ull;
-      for (int bb = 0; bb < nb; ++bb) {
-        const uint32_t t = d & pair[(size_t)bb];
-        if (t != 0u && t != pair[(size_t)bb]) bits |= 1ull << bb;
-      }
-      vm[(size_t)r] = bits;
-    }
-    const int n = dsec.n, nchunks = (op->L + 7) / 8;
-    const Binom& B = binom_table();
-    std::vector<int32_t> rt((size_t)nchunks * (size_t)(n + 1) * 256, 0);
-    for (int k = 0; k < nchunks; ++k)
-      for (int cb = 0; cb <= n; ++cb)
-        for (int byte = 0; byte < 256; ++byte) {
-          int64_t sum = 0;
-          int idx = 0;
-          for (int i = 0; i < 8; ++i)
-            if ((byte >> i) & 1) {
-              ++idx;
-              sum += binom_at(B, 8 * k + i, cb + idx);
-            }
-          rt[((size_t)k * (size_t)(n + 1) + (size_t)cb) * 256 + (size_t)byte] = (int32_t)sum;
-        }
-    v.dn_vmask = upload(op, vm);
-    v.bond_pair = upload(op, pair);
-    v.bond_between = upload(op, betw);
-    v.bond_mult = upload(op, mult);
-    v.dn_rank = upload(op, rt);
-    v.n_bonds = nb;
-    v.dn_nchunks = nchunks;
-    v.dn_n = n;
-  }
   const std::vector<double> uf = u_fold_table(m->u, m->has_u, op->L);
   v.u_fold = upload(op, uf);
   v.u_fold_f = upload(op, std::vector<float>(uf.begin(), uf.end()));
@@ -220,7 +160,18 @@ static void build_op(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m) {
     }
   }
   ensure_binomials();
-  if (op->precision == MB_PREC_Q64) q_op_prepare(op, m, tu, td);
+  if (op->precision == MB_PREC_Q64) {
+    const SignedLists ul = signed_lists(tu, op->Du);
+    v.up_list = upload(op, ul.list);
+    v.up_loff = upload(op, ul.off);
+    v.up_lpos = upload(op, ul.pos);
+    v.max_up_list = ul.max_len;
+    const SlicedTable sd = sliced_table(td, op->Dd);
+    v.dn_sell = upload(op, sd.ent);
+    v.dn_sgrp = upload(op, sd.grp);
+    v.dn_nneg = upload(op, sd.nneg);
+    q_op_prepare(op, m, tu, td);
+  }
 }
 
 static mb_op_s::Scratch& scratch_for(mb_op_s* op, cudaStream_t st, int nvec) {
@@ -569,13 +520,26 @@ static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
   *e_out = sign * d[(size_t)m - 1];
   const bool refine = o.refine && op->precision == MB_PREC_F32;
   if (vec || refine) {
-    std::vector<std::complex<double>> y((size_t)m);
-    for (int64_t i = 0; i < m; ++i) y[(size_t)i] = z[(size_t)(m - 1) * m + i] * b_norm;
+    // An FP32 run without re-orthogonalisation takes its Ritz vector from
+    // the first converged checkpoint, before a ghost copy of the eigenvalue
+    // can enter T_m; every other run from T_m as the reference does.
+    int64_t mv = m;
+    if (refine && !reorth) {
+      mv = ritz_vector_steps(alphas, betas, (int)m, o.check_every, 1e-9);
+      if (mv != m) {
+        d.assign(alphas.begin(), alphas.begin() + mv);
+        e.assign(betas.begin(), betas.begin() + (mv - 1));
+        MB_REQUIRE(tridiag_eig((int)mv, d, e, &z), MB_ERR_EIG_FAILED,
+                   "Eigenvalue decomposition of T_k failed");
+      }
+    }
+    std::vector<std::complex<double>> y((size_t)mv);
+    for (int64_t i = 0; i < mv; ++i) y[(size_t)i] = z[(size_t)(mv - 1) * mv + i] * b_norm;
     DevBuf xt(kr.vb);
     if (reorth) {
       kr.combine_basis(m, y, xt.p);
     } else {
-      kr.pass_two(bt.p, m, sign, alphas, betas, b_norm, y, xt.p);
+      kr.pass_two(bt.p, mv, sign, alphas, betas, b_norm, y, xt.p);
     }
     if (refine) {
       // FP64 refinement of the FP32 Ritz vector x: Rayleigh-Ritz on

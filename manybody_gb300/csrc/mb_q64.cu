@@ -132,23 +132,33 @@ __device__ void q_block_reduce(double (&v)[NC], unsigned long long magor, double
 // The Q64 apply: y = scale (H - shift) x + beta z on mantissas.
 //   P = c1 * S + cq[popc(up & down)] * x_q + c3 * z_q      (128-bit)
 //   y_q = round(P / 2^sh)
-// S = sum over hops of +-x_q (or 2x for doubled bonds), exact in int64.
-// Same row-staged structure as the floating-point kernel: one CTA per row
-// r_up at a time, the row in shared memory for the down hops, coalesced
-// 16-byte loads of the neighbour rows for the up hops.
+// S = sum over hops of +-x_q (doubled bonds listed twice), exact in int64.
 // dots (DOTS bit0): Re<x,y> and <y,y> as exact integer sums >> 32.
+//
+// One CTA of 1024 threads per SM walks the rows r_up in the row schedule's
+// order (reverse Cuthill-McKee: rows in flight together share neighbour rows
+// in L2).  Per row: the row x[r,:] and one zero element go to shared memory,
+// then warp w takes the 32-column groups g = w, w + 32, ...:
+//   down hops: sliced table, one coalesced 4-byte entry per lane and slot =
+//     byte offset of the neighbour in the staged row | sign << 31; padding
+//     reads the zero element.  A negative hop adds v ^ -1 (= -v - 1); the
+//     column's count of negative hops is added back once;
+//   up hops: the row's sign-sorted target list (uniform across the CTA):
+//     coalesced 16-byte loads x[r',c], summed then subtracted, no sign work;
+//     the lines of the warp's next group are prefetched into L2 first.
+// Hops are summed in pairs (three-operand 64-bit adds).
 // ---------------------------------------------------------------------------
 constexpr int kQThreads = 1024;
 
-template <bool STAGED, int DOTS, bool HAS_Z, bool DBL>
-__global__ void __launch_bounds__(kQThreads)
+template <bool STAGED, int DOTS, bool HAS_Z>
+__global__ void __launch_bounds__(kQThreads, 1)
 k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlong2* z,
           const QParams* __restrict__ prm, double* __restrict__ partials,
           unsigned long long* __restrict__ max_or) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int up_words = (v.max_up_degree + 3) & ~3;
-  uint32_t* s_upn = reinterpret_cast<uint32_t*>(smem);
-  longlong2* s_row = reinterpret_cast<longlong2*>(smem + sizeof(uint32_t) * up_words);
+  const int64_t Dd = v.Dd;
+  const uint32_t row_bytes = (uint32_t)(16 * Dd);
+  uint32_t* s_up = reinterpret_cast<uint32_t*>(smem + (STAGED ? row_bytes + 16 : 0));
   __shared__ long long s_cq[kMaxOrbitals + 1];
   __shared__ long long s_c1, s_c3;
   __shared__ int s_sh;
@@ -157,52 +167,99 @@ k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlon
     s_c1 = prm->c1;
     s_c3 = prm->c3;
     s_sh = prm->sh;
+    if (STAGED) *reinterpret_cast<longlong2*>(smem + row_bytes) = make_longlong2(0, 0);
   }
-  const int64_t Dd = v.Dd;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int64_t ngroups = (Dd + 31) >> 5;
   __int128 a_xy = 0, a_yy = 0;
   unsigned long long mor = 0;
+  // a down neighbour by table entry: staged row, or the row in global memory
+  auto dn_val = [&](const longlong2* xrow, uint32_t e) -> longlong2 {
+    const uint32_t off = e & 0x7FFFFFF0u;
+    if (STAGED) return *reinterpret_cast<const longlong2*>(smem + off);
+    return off < row_bytes
+               ? __ldg(reinterpret_cast<const longlong2*>(reinterpret_cast<const char*>(xrow) + off))
+               : make_longlong2(0, 0);
+  };
 
   for (int64_t ri = blockIdx.x; ri < v.Du; ri += gridDim.x) {
     const int64_t r = v.row_sched ? (int64_t)v.row_sched[ri] : ri;
     const longlong2* xrow = x + r * Dd;
     __syncthreads();
-    const int u0 = v.up_off[r], nup = v.up_off[r + 1] - u0;
-    for (int j = threadIdx.x; j < nup; j += blockDim.x) s_upn[j] = v.up_ent[u0 + j];
+    const int u0 = __ldg(&v.up_loff[r]), nu = __ldg(&v.up_loff[r + 1]) - u0;
+    const int npos = __ldg(&v.up_lpos[r]);
+    for (int j = threadIdx.x; j < nu; j += blockDim.x) s_up[j] = __ldg(&v.up_list[u0 + j]);
     if (STAGED)
-      for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) s_row[c] = xrow[c];
+      for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x)
+        reinterpret_cast<longlong2*>(smem)[c] = xrow[c];
     __syncthreads();
     const uint32_t um = v.up_mask[r];
     const long long c1 = s_c1, c3 = s_c3;
     const int sh = s_sh;
-    for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) {
+    for (int64_t g = warp; g < ngroups; g += nwarps) {
+      const int64_t c = (g << 5) + lane;
+      const bool live = c < Dd;
+      const int64_t cl = live ? c : Dd - 1;
+      if (g + nwarps < ngroups) {
+        // the up-hop lines of this warp's next group, into L2 ahead of use
+        const int64_t cn = min(((g + nwarps) << 5) + lane, Dd - 1);
+        const char* xn = reinterpret_cast<const char*>(x + cn);
+        for (int k = 0; k < nu; ++k)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(xn + (uint64_t)s_up[k] * row_bytes));
+      }
       long long sr = 0, si = 0;
-      int negs = 0;
-      const int d0 = v.dn_off[c], d1 = v.dn_off[c + 1];
-      for (int j = d0; j < d1; ++j) {
-        const uint32_t e = __ldg(&v.dn_ent[j]);
-        const longlong2 val = STAGED ? s_row[e >> 8] : __ldg(&xrow[e >> 8]);
-        const long long m = -(long long)(e & 1u);   // 0 or -1
-        long long tr = val.x ^ m, ti = val.y ^ m;   // -v = (v ^ -1) + 1: the +1s are counted
-        if (DBL && (e & 2u)) { tr = tr + tr + (m & 1); ti = ti + ti + (m & 1); }
-        sr += tr;
-        si += ti;
-        negs += (int)(e & 1u);
+      const int2 gi = __ldg(reinterpret_cast<const int2*>(v.dn_sgrp) + g);
+      const uint32_t* ep = v.dn_sell + gi.x + lane;
+      int j = 0;
+#pragma unroll 2
+      for (; j + 2 <= gi.y; j += 2) {
+        const uint32_t e0 = __ldg(ep + 32 * j), e1 = __ldg(ep + 32 * j + 32);
+        const long long m0 = (int)e0 >> 31, m1 = (int)e1 >> 31;  // 0 or -1
+        const longlong2 v0 = dn_val(xrow, e0), v1 = dn_val(xrow, e1);
+        sr += (v0.x ^ m0) + (v1.x ^ m1);
+        si += (v0.y ^ m0) + (v1.y ^ m1);
       }
-#pragma unroll 4
-      for (int j = 0; j < nup; ++j) {
-        const uint32_t e = s_upn[j];
-        const longlong2 val = __ldg(&x[(int64_t)(e >> 8) * Dd + c]);
-        const long long m = -(long long)(e & 1u);
-        long long tr = val.x ^ m, ti = val.y ^ m;
-        if (DBL && (e & 2u)) { tr = tr + tr + (m & 1); ti = ti + ti + (m & 1); }
-        sr += tr;
-        si += ti;
-        negs += (int)(e & 1u);
+      if (j < gi.y) {
+        const uint32_t e0 = __ldg(ep + 32 * j);
+        const long long m0 = (int)e0 >> 31;
+        const longlong2 v0 = dn_val(xrow, e0);
+        sr += v0.x ^ m0;
+        si += v0.y ^ m0;
       }
-      sr += negs;
-      si += negs;
-      const longlong2 xv = STAGED ? s_row[c] : xrow[c];
-      const long long dq = s_cq[__popc(um & v.dn_mask[c])];
+      const int nneg = __ldg(&v.dn_nneg[cl]);
+      sr += nneg;
+      si += nneg;
+      const char* xc = reinterpret_cast<const char*>(x + cl);
+      auto up_val = [&](int k) {
+        return __ldg(reinterpret_cast<const longlong2*>(xc + (uint64_t)s_up[k] * row_bytes));
+      };
+      j = 0;
+#pragma unroll 2
+      for (; j + 2 <= npos; j += 2) {
+        const longlong2 v0 = up_val(j), v1 = up_val(j + 1);
+        sr += v0.x + v1.x;
+        si += v0.y + v1.y;
+      }
+      if (j < npos) {
+        const longlong2 v0 = up_val(j);
+        sr += v0.x;
+        si += v0.y;
+      }
+      j = npos;
+#pragma unroll 2
+      for (; j + 2 <= nu; j += 2) {
+        const longlong2 v0 = up_val(j), v1 = up_val(j + 1);
+        sr -= v0.x + v1.x;
+        si -= v0.y + v1.y;
+      }
+      if (j < nu) {
+        const longlong2 v0 = up_val(j);
+        sr -= v0.x;
+        si -= v0.y;
+      }
+      if (!live) continue;
+      const longlong2 xv = STAGED ? reinterpret_cast<const longlong2*>(smem)[c] : xrow[c];
+      const long long dq = s_cq[__popc(um & __ldg(&v.dn_mask[c]))];
       __int128 pr = (__int128)c1 * sr + (__int128)dq * xv.x;
       __int128 pi = (__int128)c1 * si + (__int128)dq * xv.y;
       const int64_t idx = r * Dd + c;
@@ -252,321 +309,37 @@ int q_apply_grid(const OpView& v) {
   return (int)std::max<int64_t>(g, 1);
 }
 
-template <bool STAGED, int DOTS, bool HAS_Z, bool DBL>
+template <bool STAGED, int DOTS, bool HAS_Z>
 static void q_apply_t(const OpView& v, const void* x, void* y, const void* z, const QParams* prm,
                       double* partials, unsigned long long* max_or, cudaStream_t st) {
-  const int up_words = (v.max_up_degree + 3) & ~3;
-  size_t smem = sizeof(uint32_t) * (size_t)up_words;
-  if (STAGED) smem += sizeof(longlong2) * (size_t)v.Dd;
-  auto kern = k_apply_q<STAGED, DOTS, HAS_Z, DBL>;
+  size_t smem = sizeof(uint32_t) * (size_t)((v.max_up_list + 3) & ~3);
+  if (STAGED) smem += sizeof(longlong2) * (size_t)(v.Dd + 1);
+  auto kern = k_apply_q<STAGED, DOTS, HAS_Z>;
   MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<q_apply_grid(v), kQThreads, smem, st>>>(v, (const longlong2*)x, (longlong2*)y,
                                                    (const longlong2*)z, prm, partials, max_or);
   MB_CUDA(cudaGetLastError());
 }
 
-template <bool STAGED, bool DBL>
+template <bool STAGED>
 static void q_apply_sel(const OpView& v, const void* x, void* y, const void* z,
                         const QParams* prm, double* partials, unsigned long long* max_or,
                         int dots, cudaStream_t st) {
   if (z) {
-    if (dots) q_apply_t<STAGED, 7, true, DBL>(v, x, y, z, prm, partials, max_or, st);
-    else q_apply_t<STAGED, 0, true, DBL>(v, x, y, z, prm, partials, max_or, st);
+    if (dots) q_apply_t<STAGED, 7, true>(v, x, y, z, prm, partials, max_or, st);
+    else q_apply_t<STAGED, 0, true>(v, x, y, z, prm, partials, max_or, st);
   } else {
-    if (dots) q_apply_t<STAGED, 7, false, DBL>(v, x, y, z, prm, partials, max_or, st);
-    else q_apply_t<STAGED, 0, false, DBL>(v, x, y, z, prm, partials, max_or, st);
+    if (dots) q_apply_t<STAGED, 7, false>(v, x, y, z, prm, partials, max_or, st);
+    else q_apply_t<STAGED, 0, false>(v, x, y, z, prm, partials, max_or, st);
   }
 }
 
-void launch_apply_q(const OpView& v, bool has_double_bonds, const void* x, void* y, const void* z,
-                    const QParams* prm, double* partials, unsigned long long* max_or, int dots,
-                    cudaStream_t st) {
-  const size_t need = sizeof(uint32_t) * (size_t)((v.max_up_degree + 3) & ~3) +
-                      sizeof(longlong2) * (size_t)v.Dd + 2048;
-  const bool staged = need <= (size_t)smem_optin();
-  if (staged) {
-    if (has_double_bonds) q_apply_sel<true, true>(v, x, y, z, prm, partials, max_or, dots, st);
-    else q_apply_sel<true, false>(v, x, y, z, prm, partials, max_or, dots, st);
-  } else {
-    if (has_double_bonds) q_apply_sel<false, true>(v, x, y, z, prm, partials, max_or, dots, st);
-    else q_apply_sel<false, false>(v, x, y, z, prm, partials, max_or, dots, st);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Split apply for large sectors: the up hops read whole neighbour rows, and
-// with ~16 neighbours per row spread over the sector (the hop graph is an
-// expander) no row order keeps them in L2 -- the fused kernel re-reads each
-// row ~6x from DRAM.  So the apply runs as two streaming passes:
-//   K1 (rows):    S[r,:] = sum over down hops of +-x[r,c'] (exact int64),
-//                 the row staged in shared memory;
-//   K2 (columns): work items (column block b, row r) in b-major order, so
-//                 all CTAs sweep one 256-column slab of every row at a time
-//                 (D_up * 4 KB, L2-resident) and each neighbour segment
-//                 x[r',b] comes from L2; it adds the up hops to S and does
-//                 the 128-bit epilogue of the fused kernel.
-// DRAM: K1 reads x, writes S; K2 reads S, x (once, via L2), writes y.
-// ---------------------------------------------------------------------------
-constexpr int kK1Threads = 1024;
-constexpr int kK2Threads = 256;
-
-template <bool STAGED, bool DBL>
-__global__ void __launch_bounds__(kK1Threads, 1)
-k_q_down_rows(OpView v, const longlong2* __restrict__ x, longlong2* __restrict__ s_out) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  longlong2* s_row = reinterpret_cast<longlong2*>(smem);
-  const int64_t Dd = v.Dd;
-  for (int64_t r = blockIdx.x; r < v.Du; r += gridDim.x) {
-    const longlong2* xrow = x + r * Dd;
-    if (STAGED) {
-      __syncthreads();
-      for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) s_row[c] = xrow[c];
-      __syncthreads();
-    }
-    for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) {
-      long long sr = 0, si = 0;
-      int negs = 0;
-      const int cnt = __ldg(&v.dn_cnt[c]);
-#pragma unroll 4
-      for (int j = 0; j < cnt; ++j) {
-        const uint32_t e = __ldg(&v.dn_ell[(int64_t)j * Dd + c]);
-        const longlong2 val = STAGED ? s_row[e >> 8] : __ldg(&xrow[e >> 8]);
-        const long long m = -(long long)(e & 1u);
-        long long tr = val.x ^ m, ti = val.y ^ m;
-        if (DBL && (e & 2u)) { tr = tr + tr + (m & 1); ti = ti + ti + (m & 1); }
-        sr += tr;
-        si += ti;
-        negs += (int)(e & 1u);
-      }
-      __stcs(&s_out[r * Dd + c], make_longlong2(sr + negs, si + negs));
-    }
-  }
-}
-
-// K1 with the down hops computed on the fly: no per-row table stream.
-// Shared memory: rank tables, bond masks, then the staged row.
-__device__ __forceinline__ int otf_rank(const int32_t* s_rank, uint32_t m, int nchunks,
-                                         int stride) {
-  int r = 0, cb = 0;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    if (k < nchunks) {
-      const uint32_t byte = (m >> (8 * k)) & 0xFFu;
-      r += s_rank[(k * stride + cb) * 256 + (int)byte];
-      cb += __popc(byte);
-    }
-  }
-  return r;
-}
-
-static size_t otf_prefix_bytes(const OpView& v) {
-  return sizeof(int32_t) * (size_t)v.dn_nchunks * (size_t)(v.dn_n + 1) * 256 + 3 * 64 * sizeof(uint32_t);
-}
-
-template <bool DBL>
-__global__ void __launch_bounds__(kK1Threads, 1)
-k_q_down_rows_otf(OpView v, const longlong2* __restrict__ x, longlong2* __restrict__ s_out) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int stride = v.dn_n + 1;
-  const int rank_words = v.dn_nchunks * stride * 256;
-  int32_t* s_rank = reinterpret_cast<int32_t*>(smem);
-  uint32_t* s_pair = reinterpret_cast<uint32_t*>(s_rank + rank_words);
-  uint32_t* s_betw = s_pair + 64;
-  uint32_t* s_mult = s_betw + 64;
-  longlong2* s_row = reinterpret_cast<longlong2*>(s_mult + 64);
-  for (int i = threadIdx.x; i < rank_words; i += blockDim.x) s_rank[i] = v.dn_rank[i];
-  for (int i = threadIdx.x; i < v.n_bonds; i += blockDim.x) {
-    s_pair[i] = v.bond_pair[i];
-    s_betw[i] = v.bond_between[i];
-    s_mult[i] = v.bond_mult[i];
-  }
-  const int64_t Dd = v.Dd;
-  const int nch = v.dn_nchunks;
-  for (int64_t r = blockIdx.x; r < v.Du; r += gridDim.x) {
-    const longlong2* xrow = x + r * Dd;
-    __syncthreads();
-    for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) s_row[c] = xrow[c];
-    __syncthreads();
-    for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) {
-      const uint32_t d = __ldg(&v.dn_mask[c]);
-      unsigned long long vm = __ldg(&v.dn_vmask[c]);
-      long long sr = 0, si = 0;
-      int negs = 0;
-      while (vm) {
-        const int bnd = __ffsll((long long)vm) - 1;
-        vm &= vm - 1ull;
-        const uint32_t d2 = d ^ s_pair[bnd];
-        const int neg = __popc(d & s_betw[bnd]) & 1;
-        const longlong2 val = s_row[otf_rank(s_rank, d2, nch, stride)];
-        const long long m = -(long long)neg;
-        long long tr = val.x ^ m, ti = val.y ^ m;
-        if (DBL && s_mult[bnd] == 2u) { tr = tr + tr + (m & 1); ti = ti + ti + (m & 1); }
-        sr += tr;
-        si += ti;
-        negs += neg;
-      }
-      __stcs(&s_out[r * Dd + c], make_longlong2(sr + negs, si + negs));
-    }
-  }
-}
-
-constexpr int kK2Cols = 2;  // columns per thread (two independent hop chains)
-
-template <int DOTS, bool HAS_Z, bool DBL>
-__global__ void __launch_bounds__(kK2Threads)
-k_q_up_cols(OpView v, const longlong2* __restrict__ x, const longlong2* __restrict__ s_in,
-            longlong2* y, const longlong2* z, const QParams* __restrict__ prm,
-            double* __restrict__ partials, unsigned long long* __restrict__ max_or) {
-  __shared__ long long s_cq[kMaxOrbitals + 1];
-  if (threadIdx.x <= (unsigned)v.L) s_cq[threadIdx.x] = prm->cq[threadIdx.x];
-  __syncthreads();
-  const long long c1 = prm->c1, c3 = prm->c3;
-  const int sh = prm->sh;
-  const int64_t Dd = v.Dd, Du = v.Du;
-  constexpr int W = kK2Threads * kK2Cols;
-  const int64_t nblk = (Dd + W - 1) / W;
-  const int64_t items = nblk * Du;
-  __int128 a_xy = 0, a_yy = 0;
-  unsigned long long mor = 0;
-  for (int64_t it = blockIdx.x; it < items; it += gridDim.x) {
-    const int64_t b = it / Du, r = it - b * Du;
-    const int64_t c0 = b * W + threadIdx.x;
-    const int u0 = __ldg(&v.up_off[r]), u1 = __ldg(&v.up_off[r + 1]);
-    const uint32_t um = __ldg(&v.up_mask[r]);
-    long long sr[kK2Cols], si[kK2Cols];
-    bool ok[kK2Cols];
-#pragma unroll
-    for (int q = 0; q < kK2Cols; ++q) {
-      const int64_t c = c0 + q * kK2Threads;
-      ok[q] = c < Dd;
-      const longlong2 s0 = ok[q] ? __ldcs(&s_in[r * Dd + c]) : make_longlong2(0, 0);
-      sr[q] = s0.x;
-      si[q] = s0.y;
-    }
-    int negs = 0;
-#pragma unroll 4
-    for (int j = u0; j < u1; ++j) {
-      const uint32_t e = __ldg(&v.up_ent[j]);
-      const longlong2* xr = x + (int64_t)(e >> 8) * Dd;
-      const long long m = -(long long)(e & 1u);
-#pragma unroll
-      for (int q = 0; q < kK2Cols; ++q) {
-        const longlong2 val = ok[q] ? __ldg(&xr[c0 + q * kK2Threads]) : make_longlong2(0, 0);
-        long long tr = val.x ^ m, ti = val.y ^ m;
-        if (DBL && (e & 2u)) { tr = tr + tr + (m & 1); ti = ti + ti + (m & 1); }
-        sr[q] += tr;
-        si[q] += ti;
-      }
-      negs += (int)(e & 1u);
-    }
-#pragma unroll
-    for (int q = 0; q < kK2Cols; ++q) {
-      if (!ok[q]) continue;
-      const int64_t c = c0 + q * kK2Threads;
-      const int64_t idx = r * Dd + c;
-      const long long srq = sr[q] + negs, siq = si[q] + negs;
-      const longlong2 xv = x[idx];
-      const long long dq = s_cq[__popc(um & __ldg(&v.dn_mask[c]))];
-      __int128 pr = (__int128)c1 * srq + (__int128)dq * xv.x;
-      __int128 pi = (__int128)c1 * siq + (__int128)dq * xv.y;
-      if (HAS_Z) {
-        const longlong2 zv = z[idx];
-        pr += (__int128)c3 * zv.x;
-        pi += (__int128)c3 * zv.y;
-      }
-      longlong2 out;
-      out.x = round_shift(pr, sh);
-      out.y = round_shift(pi, sh);
-      __stcs(&y[idx], out);  // streamed: keep the x slab resident in L2
-      if (DOTS & 1) a_xy += prod_hi(xv.x, out.x) + prod_hi(xv.y, out.y);
-      if (DOTS & 2) a_yy += prod_hi(out.x, out.x) + prod_hi(out.y, out.y);
-      if (DOTS & 4) mor |= mag(out.x) | mag(out.y);
-    }
-  }
-  if (DOTS) {
-    double vals[2] = {i128_to_f64(a_xy), i128_to_f64(a_yy)};
-    q_block_reduce<2>(vals, mor, partials, max_or);
-  }
-}
-
-static int q_split_grid() { return sm_count() * 8; }
-
-// Up-hop grid size used by the split apply (partials are per block).
-int q_apply_split_grid() { return q_split_grid(); }
-
-template <int DOTS, bool HAS_Z, bool DBL>
-static void q_split_t(const OpView& v, const void* x, void* y, const void* z, void* s_scratch,
-                      const QParams* prm, double* partials, unsigned long long* max_or,
-                      cudaStream_t st) {
-  const size_t row_bytes = sizeof(longlong2) * (size_t)v.Dd;
-  const bool staged = row_bytes + 2048 <= (size_t)smem_optin();
-  int g1 = sm_count();
-  if (g1 > v.Du) g1 = (int)v.Du;
-  const size_t otf_bytes = v.dn_vmask ? otf_prefix_bytes(v) + row_bytes : 0;
-  if (v.dn_vmask && otf_bytes + 1024 <= (size_t)smem_optin()) {
-    auto k1 = k_q_down_rows_otf<DBL>;
-    MB_CUDA(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)otf_bytes));
-    k1<<<g1, kK1Threads, otf_bytes, st>>>(v, (const longlong2*)x, (longlong2*)s_scratch);
-  } else if (staged) {
-    auto k1 = k_q_down_rows<true, DBL>;
-    MB_CUDA(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_bytes));
-    k1<<<g1, kK1Threads, row_bytes, st>>>(v, (const longlong2*)x, (longlong2*)s_scratch);
-  } else {
-    k_q_down_rows<false, DBL><<<g1, kK1Threads, 0, st>>>(v, (const longlong2*)x,
-                                                         (longlong2*)s_scratch);
-  }
-  MB_CUDA(cudaGetLastError());
-  k_q_up_cols<DOTS, HAS_Z, DBL><<<q_split_grid(), kK2Threads, 0, st>>>(
-      v, (const longlong2*)x, (const longlong2*)s_scratch, (longlong2*)y, (const longlong2*)z,
-      prm, partials, max_or);
-  MB_CUDA(cudaGetLastError());
-}
-
-template <bool DBL>
-static void q_split_sel(const OpView& v, const void* x, void* y, const void* z, void* s,
-                        const QParams* prm, double* partials, unsigned long long* max_or,
-                        int dots, cudaStream_t st) {
-  if (z) {
-    if (dots) q_split_t<7, true, DBL>(v, x, y, z, s, prm, partials, max_or, st);
-    else q_split_t<0, true, DBL>(v, x, y, z, s, prm, partials, max_or, st);
-  } else {
-    if (dots) q_split_t<7, false, DBL>(v, x, y, z, s, prm, partials, max_or, st);
-    else q_split_t<0, false, DBL>(v, x, y, z, s, prm, partials, max_or, st);
-  }
-}
-
-// Sectors at least this large use the split apply when scratch is given.
-constexpr int64_t kSplitMinDim = int64_t(1) << 22;
-
-// MB_APPLY_VARIANT=fused|split overrides the size rule (tuning knob).
-bool q_use_split(const OpView& v) {
-  static const int forced = [] {
-    const char* e = getenv("MB_APPLY_VARIANT");
-    if (!e) return -1;
-    if (!strcmp(e, "fused")) return 0;
-    if (!strcmp(e, "split")) return 1;
-    return -1;
-  }();
-  if (forced >= 0) return forced == 1;
-  // Measured on GB300 (4x4 and 1D L=16 sectors): the fused kernel is faster
-  // than the two-pass split at every size tried, so it is the default.
-  (void)v;
-  return false;
-}
-
-void launch_apply_q2(const OpView& v, bool has_double_bonds, const void* x, void* y,
-                     const void* z, void* s_scratch, const QParams* prm, double* partials,
-                     unsigned long long* max_or, int dots, cudaStream_t st) {
-  if (!s_scratch || !q_use_split(v)) {
-    launch_apply_q(v, has_double_bonds, x, y, z, prm, partials, max_or, dots, st);
-    return;
-  }
-  if (has_double_bonds) q_split_sel<true>(v, x, y, z, s_scratch, prm, partials, max_or, dots, st);
-  else q_split_sel<false>(v, x, y, z, s_scratch, prm, partials, max_or, dots, st);
-}
-
-int q_apply_grid_for(const OpView& v, bool split) {
-  return split ? q_split_grid() : q_apply_grid(v);
+void launch_apply_q(const OpView& v, const void* x, void* y, const void* z, const QParams* prm,
+                    double* partials, unsigned long long* max_or, int dots, cudaStream_t st) {
+  const size_t need = sizeof(uint32_t) * (size_t)((v.max_up_list + 3) & ~3) +
+                      sizeof(longlong2) * (size_t)(v.Dd + 1) + 2048;
+  if (need <= (size_t)smem_optin()) q_apply_sel<true>(v, x, y, z, prm, partials, max_or, dots, st);
+  else q_apply_sel<false>(v, x, y, z, prm, partials, max_or, dots, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -36,19 +36,11 @@ struct QPlanInput {
 
 __host__ __device__ void q_plan(QParams* p, const QPlanInput& in);
 
-void launch_apply_q(const OpView& v, bool has_double_bonds, const void* x, void* y, const void* z,
-                    const QParams* prm_dev, double* partials, unsigned long long* max_or, int dots,
-                    cudaStream_t st);
+// The fused apply (one pass over x; see mb_q64.cu).  y must not alias x or z.
+void launch_apply_q(const OpView& v, const void* x, void* y, const void* z, const QParams* prm_dev,
+                    double* partials, unsigned long long* max_or, int dots, cudaStream_t st);
+// blocks that write dot partials for an apply
 int q_apply_grid(const OpView& v);
-// Two-pass apply (down hops by rows, up hops by L2-resident column blocks)
-// for sectors of >= 2^22 states when s_scratch (one Q64 vector) is given;
-// otherwise the fused single-pass kernel.
-void launch_apply_q2(const OpView& v, bool has_double_bonds, const void* x, void* y,
-                     const void* z, void* s_scratch, const QParams* prm_dev, double* partials,
-                     unsigned long long* max_or, int dots, cudaStream_t st);
-bool q_use_split(const OpView& v);
-// blocks that write dot partials for an apply (split or fused)
-int q_apply_grid_for(const OpView& v, bool split);
 int q_blas_grid(int64_t n);
 int q_multi_dot_grid(int64_t n);
 

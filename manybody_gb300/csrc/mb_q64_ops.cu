@@ -65,7 +65,7 @@ void q_op_prepare(mb_op_s* op, const mb_model_s* m, const HopTable& tu, const Ho
 
 void q_op_release(mb_op_s* op) {
   for (auto& kv : op->qscratch) {
-    for (void* p : {kv.second.xq, kv.second.yq, kv.second.sq, kv.second.prm, (void*)kv.second.ints})
+    for (void* p : {kv.second.xq, kv.second.yq, kv.second.prm, (void*)kv.second.ints})
       if (p) cudaFree(p);
   }
   op->qscratch.clear();
@@ -94,7 +94,6 @@ static mb_op_s::QScratch& qscratch_for(mb_op_s* op, cudaStream_t st) {
     const size_t vb = sizeof(longlong2) * (size_t)op->dim;
     MB_CUDA(cudaMalloc(&s.xq, vb));
     MB_CUDA(cudaMalloc(&s.yq, vb));
-    if (q_use_split(op->view)) MB_CUDA(cudaMalloc(&s.sq, vb));
     MB_CUDA(cudaMalloc(&s.prm, sizeof(QParams)));
     MB_CUDA(cudaMalloc((void**)&s.ints, 4 * sizeof(int)));
   }
@@ -111,8 +110,7 @@ void q_apply_affine(mb_op_s* op, const void* x, void* y, double scale, double sh
   int32_t* iperm = order == MB_ORDER_REFERENCE ? op_iperm(op) : nullptr;
   launch_f64_to_q(op->dim, x, perm, op->q_qbits, s.ints, s.xq, st);
   launch_q_plan(plan_input(op, scale, shift, 0.0, 0, 0, false), s.ints + 1, (QParams*)s.prm, st);
-  launch_apply_q2(op->view, op->q_has_double, s.xq, s.yq, nullptr, s.sq, (const QParams*)s.prm,
-                  nullptr, nullptr, 0, st);
+  launch_apply_q(op->view, s.xq, s.yq, nullptr, (const QParams*)s.prm, nullptr, nullptr, 0, st);
   // the output exponent sits in the planned QParams (field ey)
   const int* ey = (const int*)((const char*)s.prm + offsetof(QParams, ey));
   if (!z) {
@@ -151,7 +149,7 @@ struct QKrylov {
   cudaStream_t st;
   int64_t n;
   int qbits;
-  QBuf partials, red_out, maxor, prm, sbuf;
+  QBuf partials, red_out, maxor, prm;
   double* host = nullptr;      // pinned: reduce outputs, then the max word
   QParams* hprm = nullptr;     // pinned
   int grid_apply, grid_blas, grid_md;
@@ -165,13 +163,12 @@ struct QKrylov {
   QKrylov(mb_op_s* o, cudaStream_t s)
       : op(o), st(s), n(o->dim), qbits(o->q_qbits),
         partials(sizeof(double) *
-                 (size_t)std::max(std::max(q_apply_grid_for(o->view, true), q_apply_grid(o->view)) * 2,
+                 (size_t)std::max(q_apply_grid(o->view) * 2,
                                   std::max(q_blas_grid(o->dim) * 2,
                                            q_multi_dot_grid(o->dim) * 2 * kQMaxBasis))),
         red_out(sizeof(double) * 2 * kQMaxBasis), maxor(sizeof(unsigned long long)),
         prm(sizeof(QParams)),
-        sbuf(q_use_split(o->view) ? sizeof(longlong2) * (size_t)o->dim : 0),
-        grid_apply(q_apply_grid_for(o->view, q_use_split(o->view))), grid_blas(q_blas_grid(o->dim)),
+        grid_apply(q_apply_grid(o->view)), grid_blas(q_blas_grid(o->dim)),
         grid_md(q_multi_dot_grid(o->dim)), coef(sizeof(long long) * 2 * kQMaxBasis) {
     MB_CUDA(cudaMallocHost((void**)&host, sizeof(double) * (2 * kQMaxBasis + 8)));
     MB_CUDA(cudaMallocHost((void**)&hprm, sizeof(QParams)));
@@ -236,8 +233,8 @@ struct QKrylov {
     q_plan(hprm, plan_input(op, scale, 0.0, -beta_prev, v.E, hz ? v_prev->E : v.E, hz));
     MB_CUDA(cudaMemcpyAsync(prm.p, hprm, sizeof(QParams), cudaMemcpyHostToDevice, st));
     zero_max();
-    launch_apply_q2(op->view, op->q_has_double, v.p, w.p, hz ? v_prev->p : nullptr, sbuf.p,
-                    (const QParams*)prm.p, part(), mor(), 1, st);
+    launch_apply_q(op->view, v.p, w.p, hz ? v_prev->p : nullptr, (const QParams*)prm.p, part(),
+                   mor(), 1, st);
     double mq = 0.0;
     const double* h = fetch(grid_apply, 2, &mq);
     w.E = hprm->ey;
@@ -538,8 +535,8 @@ int mb_op_apply_q64(mb_op_t op, const void* xq_dev, int x_exponent, void* yq_dev
     // a plan per call: the parameter block lives in per-stream scratch, and
     // the copy is ordered before the kernel on the same stream.
     MB_CUDA(cudaMemcpyAsync(s.prm, &p, sizeof(QParams), cudaMemcpyHostToDevice, st));
-    launch_apply_q2(op->view, op->q_has_double, xq_dev, yq_dev, nullptr, s.sq,
-                    (const QParams*)s.prm, nullptr, nullptr, 0, st);
+    launch_apply_q(op->view, xq_dev, yq_dev, nullptr, (const QParams*)s.prm, nullptr, nullptr, 0,
+                   st);
     *y_exponent = p.ey;
   });
 }
