@@ -169,8 +169,10 @@ typedef struct {
   double conv_tol;      /* > 0: stop early once the extremal Ritz value changes by
                            less than conv_tol * |E| between checks (0 = run k steps) */
   int check_every;      /* Ritz check period in steps when conv_tol > 0 (default 10) */
-  int refine;           /* MB_PREC_F32 operators: 1 = finish with an FP64 Rayleigh-quotient
-                           refinement of the Ritz vector on an FP64 operator */
+  int refine;           /* MB_PREC_F32 operators: 1 = finish with an FP64 Rayleigh-Ritz
+                           refinement (3 FP64 Lanczos steps from the Ritz vector; a plain
+                           run that used all k steps takes the vector from its first
+                           settled checkpoint, before ghost copies of E0 form) */
 } mb_lanczos_opts;
 
 /* lanczos_pass_one (lanczos.h:130-175) on the operator scaled by `scale`
@@ -252,7 +254,7 @@ int mb_op_apply_q64(mb_op_t op, const void* xq_dev, int x_exponent, void* yq_dev
  * An engine advances many independent sectors of uneven size together: one
  * Lanczos step of every active request per engine step, complex64 vectors with
  * FP64 alpha/beta, an optional replay pass that rebuilds the Ritz vector and
- * an FP64 Rayleigh-quotient refinement of the energy.  Requests are admitted
+ * an FP64 Rayleigh-Ritz refinement of the energy.  Requests are admitted
  * while the device-memory budget allows and retire when converged, so new
  * requests join while others run.  No counterpart in the reference (its
  * closest analogue are the OpenMP sample loops over independent vectors,
@@ -272,9 +274,12 @@ int mb_engine_footprint(const mb_sector_desc* desc, int64_t* bytes);
 /* Ground state of one sector: Lanczos on -H from the Philox start vector of
  * `seed` (tensor order), until the lowest Ritz value changes by less than
  * rel_tol * |E| between checks (every 10 steps; rel_tol 0: run kmax steps),
- * at most kmax <= 512 steps; refine = 1 adds the replay pass and the FP64
- * Rayleigh quotient.  MB_ERR_CAPACITY when the budget is full (retry after
- * mb_engine_step retires requests). */
+ * at most kmax <= 512 steps; refine = 1 adds the replay pass that rebuilds
+ * the Ritz vector (from T_m; for a run that reached kmax, from its first
+ * checkpoint whose Ritz value had settled to 1e-9, before ghost copies of E0
+ * form) and an FP64 Rayleigh-Ritz refinement of the energy (3 FP64 Lanczos
+ * steps from that vector).  MB_ERR_CAPACITY when the budget is full (retry
+ * after mb_engine_step retires requests). */
 int mb_engine_submit_ground_state(mb_engine_t engine, const mb_sector_desc* desc, uint64_t seed,
                                   int64_t kmax, double rel_tol, int refine, int64_t* request_id);
 /* Density-of-states moments of one sector: spectral bounds from 40 Lanczos

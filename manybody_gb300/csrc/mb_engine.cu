@@ -462,6 +462,7 @@ struct TableSet {
   const uint32_t *up_mask = nullptr, *dn_mask = nullptr, *up_ent = nullptr, *dn_ent = nullptr;
   const int32_t *up_off = nullptr, *dn_off = nullptr;
   int max_up_deg = 0, max_dn_deg = 0;
+  OpView fused{};  // tables of the fused FP64 apply (refinement)
   int64_t bytes = 0;
   int refs = 0;
 };
@@ -563,6 +564,16 @@ std::shared_ptr<TableSet> get_tables(mb_engine_s* e, const mb_sector_desc& d) {
   ts->dn_ent = tupload(*ts, td.ent);
   ts->max_up_deg = tu.max_degree;
   ts->max_dn_deg = td.max_degree;
+  TableSet* tsp = ts.get();
+  fill_fused_tables(ts->fused, tu, td, ts->basis.up.D, ts->basis.down.D,
+                    [tsp](const void* h, size_t bytes) -> const void* {
+                      auto b = std::make_unique<EngBuf>(std::max<size_t>(bytes, 16));
+                      if (bytes) MB_CUDA(cudaMemcpy(b->p, h, bytes, cudaMemcpyHostToDevice));
+                      tsp->bytes += (int64_t)b->bytes;
+                      const void* p = b->p;
+                      tsp->bufs.push_back(std::move(b));
+                      return p;
+                    });
   e->tables[key] = ts;
   return ts;
 }
@@ -707,7 +718,7 @@ double ritz_min(const std::vector<double>& a, const std::vector<double>& b, int 
 // FP64 Rayleigh quotient of the slot's Ritz vector on an FP64 operator view.
 double rayleigh_fp64(mb_engine_s* e, EngineSlot& s, const SlotDesc& d) {
   const TableSet& ts = *s.tables;
-  OpView v{};
+  OpView v = ts.fused;
   v.Du = s.Du;
   v.Dd = s.Dd;
   v.dim = s.dim;
@@ -805,13 +816,13 @@ void after_step(mb_engine_s* e) {
     SlotDesc& d = e->h_slots[i];
     if (s.phase == 0 && s.kind == 0) {
       const int m = d.steps;
-      bool finished = d.mode == kModeIdle;
+      bool finished = d.mode == kModeIdle, converged = false;
       if (!finished && s.rel_tol > 0.0 && m >= 2 && (m % s.check_every) == 0) {
         std::vector<double> a((size_t)m), b((size_t)m);
         MB_CUDA(cudaMemcpy(a.data(), d.alpha, sizeof(double) * m, cudaMemcpyDeviceToHost));
         MB_CUDA(cudaMemcpy(b.data(), d.beta, sizeof(double) * m, cudaMemcpyDeviceToHost));
         const double r = ritz_min(a, b, m, nullptr);
-        if (s.have_ritz && std::fabs(r - s.last_ritz) <= s.rel_tol * std::fabs(r)) finished = true;
+        if (s.have_ritz && std::fabs(r - s.last_ritz) <= s.rel_tol * std::fabs(r)) finished = converged = true;
         s.last_ritz = r;
         s.have_ritz = true;
       }
@@ -823,9 +834,10 @@ void after_step(mb_engine_s* e) {
         s.e_raw = -ritz_min(a, b, m, nullptr);
         s.e0 = s.e_raw;
         if (s.refine && m > 0) {
-          // Ritz vector from the first converged checkpoint, before a ghost
-          // copy of the ground state can enter T_m
-          s.m_ritz = ritz_vector_steps(a, b, m, s.check_every, 1e-9);
+          // a run that stopped on its convergence test ends before a ghost
+          // copy of the ground state can enter T_m; one that ran to kmax
+          // takes its Ritz vector from the first converged checkpoint
+          s.m_ritz = converged ? m : ritz_vector_steps(a, b, m, s.check_every, 1e-9);
           ritz_min(a, b, s.m_ritz, &y);
           for (auto& yv : y) yv *= s.b_norm;
           MB_CUDA(cudaMemcpy(d.yk, y.data(), sizeof(double) * s.m_ritz, cudaMemcpyHostToDevice));

@@ -6,6 +6,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "mb_internal.h"
@@ -158,7 +159,7 @@ SlicedTable sliced_table(const HopTable& t, int64_t D) {
   const int64_t ng = (D + 31) / 32;
   s.grp.resize((size_t)(2 * ng));
   s.nneg.assign((size_t)D, 0);
-  const uint32_t pad = (uint32_t)(16 * D);
+  const uint32_t pad = (uint32_t)D;
   std::vector<uint32_t> col;
   for (int64_t g = 0; g < ng; ++g) {
     int k = 0;
@@ -176,7 +177,7 @@ SlicedTable sliced_table(const HopTable& t, int64_t D) {
       col.clear();
       for (int32_t j = t.off[(size_t)c]; j < t.off[(size_t)c + 1]; ++j) {
         const uint32_t e = t.ent[(size_t)j];
-        const uint32_t w = (16u * (e >> 8)) | ((e & 1u) << 31);
+        const uint32_t w = (e >> 8) | ((e & 1u) << 31);
         col.push_back(w);
         if (e & 2u) col.push_back(w);
         s.nneg[(size_t)c] += (uint8_t)((e & 1u) * ((e & 2u) ? 2 : 1));
@@ -230,6 +231,25 @@ int ritz_vector_steps(const std::vector<double>& a, const std::vector<double>& b
     have = true;
   }
   return loose ? loose : m;
+}
+
+void fill_fused_tables(OpView& v, const HopTable& tu, const HopTable& td, int64_t Du, int64_t Dd,
+                       const TableUpload& upload) {
+  auto put = [&](const auto& vec) {
+    using T = typename std::decay_t<decltype(vec)>::value_type;
+    return (const T*)upload(vec.data(), sizeof(T) * vec.size());
+  };
+  const std::vector<int32_t> sched = rcm_order(tu, Du);
+  v.row_sched = put(sched);
+  const SignedLists ul = signed_lists(tu, Du);
+  v.up_list = put(ul.list);
+  v.up_loff = put(ul.off);
+  v.up_lpos = put(ul.pos);
+  v.max_up_list = ul.max_len;
+  const SlicedTable sd = sliced_table(td, Dd);
+  v.dn_sell = put(sd.ent);
+  v.dn_sgrp = put(sd.grp);
+  v.dn_nneg = put(sd.nneg);
 }
 
 std::vector<double> u_fold_table(double u, bool has_u, int L) {

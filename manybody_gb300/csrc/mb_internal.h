@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <cstdio>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -191,9 +192,9 @@ struct SignedLists {
 SignedLists signed_lists(const HopTable& t, int64_t D);
 
 // Sliced-ELL copy of a hop table over groups of 32 consecutive states:
-// group g's slot j for lane l is ent[grp[2g] + 32 j + l] = 16 * target |
-// (negative << 31), doubled bonds listed twice, padding 16 * D (one zero
-// element past the row); grp[2g+1] = slots of group g.
+// group g's slot j for lane l is ent[grp[2g] + 32 j + l] = target |
+// (negative << 31), doubled bonds listed twice, padding D (one zero element
+// past the row); grp[2g+1] = slots of group g.
 struct SlicedTable {
   std::vector<uint32_t> ent;
   std::vector<int32_t> grp;
@@ -237,6 +238,13 @@ struct OpView {
   int max_up_degree;
   int max_dn_degree;
 };
+
+// Fills the tables of the fused applies (row schedule, sign-sorted up lists,
+// sliced down table) into v; `upload` copies host bytes to the device and
+// returns the device address.
+using TableUpload = std::function<const void*(const void* host, size_t bytes)>;
+void fill_fused_tables(OpView& v, const HopTable& tu, const HopTable& td, int64_t Du, int64_t Dd,
+                       const TableUpload& upload);
 
 }  // namespace mb
 

@@ -117,65 +117,106 @@ static int max_smem_optin() {
 // ---------------------------------------------------------------------------
 // The matrix-free apply:  y = scale * (H - shift) x + beta * z
 // with optional fused dot products (dot_mode bit0: Re<x,y>, bit1: <y,y>,
-// bit2: <x,x>).  One CTA processes whole rows r_up (grid-stride): it stages
-// the row X[r_up, :] in shared memory (when it fits), so the down hops, which
-// stay inside the row, gather from shared memory, while the up hops read the
-// neighbour rows X[r_up', c] straight from HBM/L2 with coalesced 8/16-byte
-// loads (consecutive threads take consecutive columns).  The up-neighbour
-// list of the row (same for every column) sits in shared memory.
+// bit2: <x,x>).  One CTA per SM walks the rows r_up in the row schedule's
+// order; it stages the row X[r_up, :] (and one zero element) in shared
+// memory when it fits, so the down hops, which stay inside the row, gather
+// from shared memory through the sliced table (one coalesced 4-byte entry
+// per lane and slot: neighbour index | sign << 31, padding = the zero
+// element), while the up hops read the neighbour rows X[r_up', c] from
+// L2/HBM with coalesced 8/16-byte loads, the row's sign-sorted target list
+// in shared memory (added, then subtracted).  Warp w takes the 32-column
+// groups w, w + 32, ... and prefetches its next group's up-hop lines into L2.
 // ---------------------------------------------------------------------------
 constexpr int kApplyThreads = 1024;
 
-template <typename T>
-__device__ __forceinline__ T hop_weight(uint32_t e) {
-  T w = (e & 2u) ? T(2) : T(1);
-  return (e & 1u) ? -w : w;
+// +-1 from the sign bit of a table entry
+__device__ __forceinline__ double unit_sign(uint32_t e, double) {
+  return __hiloint2double((int)(0x3ff00000u | (e & 0x80000000u)), 0);
+}
+__device__ __forceinline__ float unit_sign(uint32_t e, float) {
+  return __int_as_float((int)(0x3f800000u | (e & 0x80000000u)));
 }
 
 template <typename T, bool STAGED, int DOTS>
-__global__ void __launch_bounds__(kApplyThreads)
+__global__ void __launch_bounds__(kApplyThreads, 1)
 k_apply(OpView v, const typename C2<T>::type* __restrict__ x, typename C2<T>::type* y,
         T hop_coef, T dscale, T shift, T beta, const typename C2<T>::type* z,
         const T* __restrict__ ufold, const T* __restrict__ self_up, const T* __restrict__ self_dn,
         double* __restrict__ partials) {
   using V2 = typename C2<T>::type;
+  constexpr int kShift = sizeof(V2) == 16 ? 4 : 3;
   extern __shared__ __align__(16) unsigned char smem[];
-  const int up_words = (v.max_up_degree + 3) & ~3;
-  uint32_t* s_upn = reinterpret_cast<uint32_t*>(smem);
-  V2* s_row = reinterpret_cast<V2*>(smem + sizeof(uint32_t) * up_words);
   const int64_t Dd = v.Dd;
+  const uint32_t row_bytes = (uint32_t)(sizeof(V2) * Dd);
+  uint32_t* s_up = reinterpret_cast<uint32_t*>(smem + (STAGED ? row_bytes + sizeof(V2) : 0));
+  if (STAGED && threadIdx.x == 0) {
+    V2 zero;
+    zero.x = T(0);
+    zero.y = T(0);
+    *reinterpret_cast<V2*>(smem + row_bytes) = zero;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int64_t ngroups = (Dd + 31) >> 5;
   DotAcc<T> a_xy, a_yy, a_xx;
 
   for (int64_t ri = blockIdx.x; ri < v.Du; ri += gridDim.x) {
     const int64_t r = v.row_sched ? (int64_t)v.row_sched[ri] : ri;
     const V2* xrow = x + r * Dd;
     __syncthreads();
-    const int u0 = v.up_off[r], nup = v.up_off[r + 1] - u0;
-    for (int j = threadIdx.x; j < nup; j += blockDim.x) s_upn[j] = v.up_ent[u0 + j];
+    const int u0 = __ldg(&v.up_loff[r]), nu = __ldg(&v.up_loff[r + 1]) - u0;
+    const int npos = __ldg(&v.up_lpos[r]);
+    for (int j = threadIdx.x; j < nu; j += blockDim.x) s_up[j] = __ldg(&v.up_list[u0 + j]);
     if (STAGED)
-      for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) s_row[c] = xrow[c];
+      for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x)
+        reinterpret_cast<V2*>(smem)[c] = xrow[c];
     __syncthreads();
     const uint32_t um = v.up_mask[r];
     const T su = self_up ? self_up[r] : T(0);
-    for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) {
+    for (int64_t g = warp; g < ngroups; g += nwarps) {
+      const int64_t c = (g << 5) + lane;
+      const bool live = c < Dd;
+      const int64_t cl = live ? c : Dd - 1;
+      if (g + nwarps < ngroups) {
+        const int64_t cn = min(((g + nwarps) << 5) + lane, Dd - 1);
+        const char* xn = reinterpret_cast<const char*>(x + cn);
+        for (int k = 0; k < nu; ++k)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(xn + (uint64_t)s_up[k] * row_bytes));
+      }
       T ar = T(0), ai = T(0);
-      const int d0 = v.dn_off[c], d1 = v.dn_off[c + 1];
-      for (int j = d0; j < d1; ++j) {
-        const uint32_t e = __ldg(&v.dn_ent[j]);
-        const V2 val = STAGED ? s_row[e >> 8] : __ldg(&xrow[e >> 8]);
-        const T w = hop_weight<T>(e);
+      const int2 gi = __ldg(reinterpret_cast<const int2*>(v.dn_sgrp) + g);
+      const uint32_t* ep = v.dn_sell + gi.x + lane;
+#pragma unroll 4
+      for (int j = 0; j < gi.y; ++j) {
+        const uint32_t e = __ldg(ep + 32 * j);
+        const uint32_t off = e << kShift;  // the sign bit shifts out
+        V2 val;
+        if (STAGED) {
+          val = *reinterpret_cast<const V2*>(smem + off);
+        } else if (off < row_bytes) {
+          val = __ldg(reinterpret_cast<const V2*>(reinterpret_cast<const char*>(xrow) + off));
+        } else {
+          val.x = T(0);
+          val.y = T(0);
+        }
+        const T w = unit_sign(e, T(0));
         ar = fma(w, val.x, ar);
         ai = fma(w, val.y, ai);
+      }
+      const char* xc = reinterpret_cast<const char*>(x + cl);
+#pragma unroll 4
+      for (int j = 0; j < npos; ++j) {
+        const V2 val = __ldg(reinterpret_cast<const V2*>(xc + (uint64_t)s_up[j] * row_bytes));
+        ar += val.x;
+        ai += val.y;
       }
 #pragma unroll 4
-      for (int j = 0; j < nup; ++j) {
-        const uint32_t e = s_upn[j];
-        const V2 val = __ldg(&x[(int64_t)(e >> 8) * Dd + c]);
-        const T w = hop_weight<T>(e);
-        ar = fma(w, val.x, ar);
-        ai = fma(w, val.y, ai);
+      for (int j = npos; j < nu; ++j) {
+        const V2 val = __ldg(reinterpret_cast<const V2*>(xc + (uint64_t)s_up[j] * row_bytes));
+        ar -= val.x;
+        ai -= val.y;
       }
-      const V2 xv = STAGED ? s_row[c] : xrow[c];
+      if (!live) continue;
+      const V2 xv = STAGED ? reinterpret_cast<const V2*>(smem)[c] : xrow[c];
       T dv = ufold[__popc(um & v.dn_mask[c])] + su;
       if (self_dn) dv += self_dn[c];
       const T ds = dscale * (dv - shift);
@@ -201,9 +242,9 @@ k_apply(OpView v, const typename C2<T>::type* __restrict__ x, typename C2<T>::ty
 }
 
 static size_t apply_smem(const OpView& v, int precision, bool staged) {
-  const int up_words = (v.max_up_degree + 3) & ~3;
+  const int up_words = (v.max_up_list + 3) & ~3;
   size_t s = sizeof(uint32_t) * (size_t)up_words;
-  if (staged) s += elem_bytes(precision) * (size_t)v.Dd;
+  if (staged) s += elem_bytes(precision) * (size_t)(v.Dd + 1);
   return s;
 }
 

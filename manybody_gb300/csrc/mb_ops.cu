@@ -25,6 +25,8 @@ void q_eigenpair(mb_op_s* op, int64_t k, const void* seed, int order, const mb_l
                  double sign, double* e_out, void* vec, int64_t* steps_out);
 void q_evolve(mb_op_s* op, const void* psi0, int order, double t, int64_t krylov_steps,
               int imaginary, void* out);
+void q_kpm_dos_moments(mb_op_s* op, int64_t n_moments, int64_t n_probes, uint64_t seed, double a,
+                       double b, double* mu);
 int32_t* op_perm(mb_op_s* op);
 
 namespace {
@@ -142,7 +144,13 @@ static void build_op(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m) {
   }
   v.max_up_degree = tu.max_degree;
   v.max_dn_degree = td.max_degree;
-  v.row_sched = upload(op, rcm_order(tu, op->Du));
+  fill_fused_tables(v, tu, td, op->Du, op->Dd, [op](const void* h, size_t bytes) -> const void* {
+    void* p = nullptr;
+    MB_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+    op->allocations.push_back(p);
+    if (bytes) MB_CUDA(cudaMemcpy(p, h, bytes, cudaMemcpyHostToDevice));
+    return p;
+  });
   const std::vector<double> uf = u_fold_table(m->u, m->has_u, op->L);
   v.u_fold = upload(op, uf);
   v.u_fold_f = upload(op, std::vector<float>(uf.begin(), uf.end()));
@@ -160,18 +168,7 @@ static void build_op(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m) {
     }
   }
   ensure_binomials();
-  if (op->precision == MB_PREC_Q64) {
-    const SignedLists ul = signed_lists(tu, op->Du);
-    v.up_list = upload(op, ul.list);
-    v.up_loff = upload(op, ul.off);
-    v.up_lpos = upload(op, ul.pos);
-    v.max_up_list = ul.max_len;
-    const SlicedTable sd = sliced_table(td, op->Dd);
-    v.dn_sell = upload(op, sd.ent);
-    v.dn_sgrp = upload(op, sd.grp);
-    v.dn_nneg = upload(op, sd.nneg);
-    q_op_prepare(op, m, tu, td);
-  }
+  if (op->precision == MB_PREC_Q64) q_op_prepare(op, m, tu, td);
 }
 
 static mb_op_s::Scratch& scratch_for(mb_op_s* op, cudaStream_t st, int nvec) {
@@ -520,11 +517,12 @@ static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
   *e_out = sign * d[(size_t)m - 1];
   const bool refine = o.refine && op->precision == MB_PREC_F32;
   if (vec || refine) {
-    // An FP32 run without re-orthogonalisation takes its Ritz vector from
-    // the first converged checkpoint, before a ghost copy of the eigenvalue
-    // can enter T_m; every other run from T_m as the reference does.
+    // An FP32 run without re-orthogonalisation that ran all k steps takes
+    // its Ritz vector from the first converged checkpoint, before a ghost
+    // copy of the eigenvalue can enter T_m; every other run (including one
+    // that stopped on its convergence test) from T_m as the reference does.
     int64_t mv = m;
-    if (refine && !reorth) {
+    if (refine && !reorth && m == k) {
       mv = ritz_vector_steps(alphas, betas, (int)m, o.check_every, 1e-9);
       if (mv != m) {
         d.assign(alphas.begin(), alphas.begin() + mv);
@@ -888,6 +886,10 @@ int mb_kpm_dos_moments(mb_op_t op, int64_t n_moments, int64_t n_probes, uint64_t
     MB_REQUIRE(e_max > e_min, MB_ERR_INVALID_ARG, "e_max must exceed e_min");
     const double a = (e_max - e_min) / 2.0 * (1.0 + padding);  // rescaling.h:33-38
     const double b = (e_max + e_min) / 2.0;
+    if (op->precision == MB_PREC_Q64) {
+      q_kpm_dos_moments(op, n_moments, n_probes, seed, a, b, mu);
+      return;
+    }
     cudaStream_t st = 0;
     const size_t vb = elem_bytes(op->precision) * (size_t)op->dim;
     DevBuf t0(vb), t1(vb);

@@ -140,8 +140,8 @@ __device__ void q_block_reduce(double (&v)[NC], unsigned long long magor, double
 // in L2).  Per row: the row x[r,:] and one zero element go to shared memory,
 // then warp w takes the 32-column groups g = w, w + 32, ...:
 //   down hops: sliced table, one coalesced 4-byte entry per lane and slot =
-//     byte offset of the neighbour in the staged row | sign << 31; padding
-//     reads the zero element.  A negative hop adds v ^ -1 (= -v - 1); the
+//     neighbour index in the staged row | sign << 31; padding reads the zero
+//     element.  A negative hop adds v ^ -1 (= -v - 1); the
 //     column's count of negative hops is added back once;
 //   up hops: the row's sign-sorted target list (uniform across the CTA):
 //     coalesced 16-byte loads x[r',c], summed then subtracted, no sign work;
@@ -175,7 +175,7 @@ k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlon
   unsigned long long mor = 0;
   // a down neighbour by table entry: staged row, or the row in global memory
   auto dn_val = [&](const longlong2* xrow, uint32_t e) -> longlong2 {
-    const uint32_t off = e & 0x7FFFFFF0u;
+    const uint32_t off = e << 4;  // byte offset; the sign bit shifts out
     if (STAGED) return *reinterpret_cast<const longlong2*>(smem + off);
     return off < row_bytes
                ? __ldg(reinterpret_cast<const longlong2*>(reinterpret_cast<const char*>(xrow) + off))

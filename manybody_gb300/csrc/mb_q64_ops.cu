@@ -229,11 +229,17 @@ struct QKrylov {
   // w = scale H v - beta_prev v_prev; returns (Re<v,w>, ||w||^2).
   std::pair<double, double> apply(QRef& w, const QRef& v, double scale, double beta_prev,
                                   const QRef* v_prev) {
-    const bool hz = v_prev && beta_prev != 0.0;
-    q_plan(hprm, plan_input(op, scale, 0.0, -beta_prev, v.E, hz ? v_prev->E : v.E, hz));
+    return apply_affine(w, v, scale, 0.0, -beta_prev, v_prev);
+  }
+
+  // w = scale (H - shift) v + beta z; returns (Re<v,w>, ||w||^2).
+  std::pair<double, double> apply_affine(QRef& w, const QRef& v, double scale, double shift,
+                                         double beta, const QRef* z) {
+    const bool hz = z && beta != 0.0;
+    q_plan(hprm, plan_input(op, scale, shift, beta, v.E, hz ? z->E : v.E, hz));
     MB_CUDA(cudaMemcpyAsync(prm.p, hprm, sizeof(QParams), cudaMemcpyHostToDevice, st));
     zero_max();
-    launch_apply_q(op->view, v.p, w.p, hz ? v_prev->p : nullptr, (const QParams*)prm.p, part(),
+    launch_apply_q(op->view, v.p, w.p, hz ? z->p : nullptr, (const QParams*)prm.p, part(),
                    mor(), 1, st);
     double mq = 0.0;
     const double* h = fetch(grid_apply, 2, &mq);
@@ -445,6 +451,51 @@ void q_eigenpair(mb_op_s* op, int64_t k, const void* seed, int order, const mb_l
     else kr.pass_two(b.r, b_norm, m, sign, alphas, betas, y, x.r, &vp.r, &vc.r, &w.r);
     kr.store(x.r, order, vec);
   }
+}
+
+// DOS Chebyshev moments on Q64 vectors: per probe (random phases, Philox
+// stream 1 + p, tensor order) T_0 = r, T_1 = Ht T_0, T_{s+1} = 2 Ht T_s -
+// T_{s-1} with Ht = (H - b) / a, each step one fused apply whose exact dots
+// give <T_s, T_{s+1}> and <T_{s+1}, T_{s+1}>; moments by the doubling
+// identities mu_2s = 2<T_s,T_s> - mu_0, mu_2s+1 = 2<T_s,T_{s+1}> - mu_1.
+void q_kpm_dos_moments(mb_op_s* op, int64_t n_moments, int64_t n_probes, uint64_t seed, double a,
+                       double b, double* mu) {
+  cudaStream_t st = 0;
+  QKrylov kr(op, st);
+  const int64_t n = op->dim;
+  QVec v0(n), v1(n), v2(n);
+  QBuf probe(sizeof(double2) * (size_t)n);
+  const int64_t nsteps = std::max<int64_t>(n_moments / 2, 1);
+  std::vector<double> acc((size_t)n_moments, 0.0), self((size_t)nsteps + 1), cross((size_t)nsteps);
+  for (int64_t p = 0; p < n_probes; ++p) {
+    launch_fill_rng(MB_PREC_F64, op->Du, op->Dd, seed, (uint32_t)(1 + p), 1, probe.p, st);
+    const double nrm = kr.load(probe.p, MB_ORDER_TENSOR, v0.r);
+    QRef* prev = &v0.r;
+    QRef* cur = &v1.r;
+    QRef* nxt = &v2.r;
+    const double mu0 = nrm * nrm;
+    const auto first = kr.apply_affine(*cur, *prev, 1.0 / a, b, 0.0, nullptr);
+    cross[0] = first.first;
+    self[1] = first.second;
+    for (int64_t s = 1; s < nsteps; ++s) {
+      const auto r = kr.apply_affine(*nxt, *cur, 2.0 / a, b, -1.0, prev);
+      cross[(size_t)s] = r.first;
+      self[(size_t)s + 1] = r.second;
+      QRef* old = prev;
+      prev = cur;
+      cur = nxt;
+      nxt = old;
+    }
+    const double mu1 = cross[0];
+    acc[0] += mu0;
+    if (n_moments > 1) acc[1] += mu1;
+    for (int64_t s = 1; 2 * s < n_moments; ++s) {
+      acc[(size_t)(2 * s)] += 2.0 * self[(size_t)s] - mu0;
+      if (2 * s + 1 < n_moments) acc[(size_t)(2 * s + 1)] += 2.0 * cross[(size_t)s] - mu1;
+    }
+  }
+  const double norm = 1.0 / ((double)n_probes * (double)n);
+  for (int64_t i = 0; i < n_moments; ++i) mu[i] = acc[(size_t)i] * norm;
 }
 
 void q_evolve(mb_op_s* op, const void* psi0, int order, double t, int64_t krylov_steps,

@@ -335,3 +335,23 @@ def test_fp32_lanczos_with_fp64_refinement(mb, cuda):
     ref = mb.find_min_eigenpair(op, 150, reorth=True, want_vector=False, refine=True)
     assert abs(raw.value - E[0]) <= 1e-5 * abs(E[0])
     assert abs(ref.value - E[0]) <= 1e-8 * abs(E[0])
+
+
+def test_fp32_refinement_past_convergence(mb, cuda):
+    """Plain (not re-orthogonalised) FP32 Lanczos run well past convergence:
+    a ghost copy of E0 enters T_k, and a Ritz vector taken from T_k can be a
+    near-cancelling mix of the two copies.  The refined energy takes its Ritz
+    vector from the first converged checkpoint: |dE0| <= 1e-8 |E0| (the
+    unrefined Ritz value only to FP32-level 1e-6)."""
+    u = 5.2292243302455415
+    _, _, op = make(mb, [8], 1.0, u, 4, 4, prec=1)
+    H = oracle.hubbard_csc([8], 1.0, u, 4, 4)
+    e_ref = H.find_min_eigenpair(oracle.philox_uniform(1, H.dim), 200, reorth=True,
+                                 want_vec=False)[0]
+    seed = op.seed_vector(0, order=mb.ORDER_TENSOR)
+    raw = mb.find_min_eigenpair(op, 150, seed, order=mb.ORDER_TENSOR, want_vector=False)
+    ref = mb.find_min_eigenpair(op, 150, seed, order=mb.ORDER_TENSOR, want_vector=False,
+                                refine=True)
+    assert raw.steps == 150
+    assert abs(raw.value - e_ref) <= 1e-6 * abs(e_ref)
+    assert abs(ref.value - e_ref) <= 1e-8 * abs(e_ref)
