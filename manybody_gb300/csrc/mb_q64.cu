@@ -362,7 +362,7 @@ __host__ __device__ void q_plan(QParams* p, const QPlanInput& in) {
   }
   const double c3r = in.has_z ? in.beta * ldexp(1.0, in.ez - in.ex) : 0.0;
   const double maxc = fmax(fmax(fabs(c1r), maxcq), fabs(c3r));
-  const double bound = fabs(c1r) * in.w_max + maxcq + fabs(c3r);
+  const double bound = (fabs(c1r) * in.w_max + maxcq) * in.x_frac + fabs(c3r) * in.z_frac;
   int G = 60;
   if (maxc > 0.0) G = 61 - ceil_log2_pos(maxc);
   int ey = in.ex;

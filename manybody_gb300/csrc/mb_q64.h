@@ -29,6 +29,9 @@ struct QPlanInput {
   double t, scale, shift, beta;
   double ufold[kMaxOrbitals + 1];
   double w_max;  // largest sum of |hop weights| of one state (both spins)
+  // bounds on max |x_q|, max |z_q| as fractions of 2^qbits (1 when unknown);
+  // the output exponent follows them, so chained applies keep their bits
+  double x_frac, z_frac;
   int L;
   int ex, ez;
   int has_z;

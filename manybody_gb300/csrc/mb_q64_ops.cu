@@ -72,8 +72,10 @@ void q_op_release(mb_op_s* op) {
 }
 
 static QPlanInput plan_input(const mb_op_s* op, double scale, double shift, double beta, int ex,
-                             int ez, bool has_z) {
+                             int ez, bool has_z, double x_frac = 1.0, double z_frac = 1.0) {
   QPlanInput in{};
+  in.x_frac = std::min(x_frac, 1.0);
+  in.z_frac = std::min(z_frac, 1.0);
   in.t = op->t;
   in.scale = scale;
   in.shift = shift;
@@ -236,7 +238,9 @@ struct QKrylov {
   std::pair<double, double> apply_affine(QRef& w, const QRef& v, double scale, double shift,
                                          double beta, const QRef* z) {
     const bool hz = z && beta != 0.0;
-    q_plan(hprm, plan_input(op, scale, shift, beta, v.E, hz ? z->E : v.E, hz));
+    const double full = std::ldexp(1.0, qbits);
+    q_plan(hprm, plan_input(op, scale, shift, beta, v.E, hz ? z->E : v.E, hz, v.maxq / full,
+                            hz ? z->maxq / full : 1.0));
     MB_CUDA(cudaMemcpyAsync(prm.p, hprm, sizeof(QParams), cudaMemcpyHostToDevice, st));
     zero_max();
     launch_apply_q(op->view, v.p, w.p, hz ? z->p : nullptr, (const QParams*)prm.p, part(),

@@ -4,7 +4,7 @@ with integer arithmetic on GB300.
 Tolerances: the apply is compared with the reference CSR at the FP64 bar,
 ||y - y_ref|| <= 1e-13 ||y_ref|| (mantissas keep >= 56 bits relative to the
 largest element); ground-state energies |dE0| <= 1e-10 |E0|; Krylov
-evolution <= 1e-10 relative.
+evolution <= 1e-10 relative; DOS moments <= 1e-10 absolute.
 """
 import numpy as np
 import pytest
@@ -123,6 +123,29 @@ def test_q64_time_evolution(mb, cuda, imaginary):
     out = fn(op, psi, 0.25).cpu().numpy()
     ref = H.time_evolve(psi.cpu().numpy(), 0.25, 30, imaginary)
     assert np.linalg.norm(out - ref) <= 1e-10 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("dims,nu,nd", [([6], 3, 3), ([2, 4], 2, 2)])
+def test_q64_kpm_dos_moments_match_oracle(mb, cuda, dims, nu, nd):
+    """DOS Chebyshev moments on Q64 vectors (exact integer dot products)
+    against the oracle's FP64 recurrence with the same probes: <= 1e-10."""
+    _, _, op = make(mb, dims, 1.0, 4.0, nu, nd)
+    H = oracle.hubbard_csc(dims, 1.0, 4.0, nu, nd)
+    E = np.linalg.eigvalsh(H.to_dense())
+    M, R = 64, 3
+    mu = mb.kpm_dos_moments(op, M, R, 11, E[0], E[-1], 0.01)
+    a = (E[-1] - E[0]) / 2 * 1.01
+    b = (E[-1] + E[0]) / 2
+    perm = op.basis.permutation()
+    ref = np.zeros(M)
+    for p in range(R):
+        rt = oracle.philox_phase(11, op.dimension(), 1 + p)
+        r = np.empty_like(rt)
+        r[perm] = rt
+        ref += H.kpm_dos_moments(r, M, a, b)
+    ref /= R * op.dimension()
+    assert abs(mu[0] - 1.0) < 1e-12
+    assert np.max(np.abs(mu - ref)) <= 1e-10
 
 
 def test_q64_full_size_4x4_matches_f64(mb, cuda):
