@@ -380,7 +380,7 @@ def run_batch_extra(mb, torch):
     errs_fp64_150 = [abs(a - r) / abs(r) for a, r in zip(ref, conv)]
     return {
         "instances": len(secs), "lanczos_steps": 150, "vectors": "complex64",
-        "recurrence": "FP64 alpha/beta + FP64 Rayleigh-quotient refinement",
+        "recurrence": "FP64 alpha/beta + FP64 Rayleigh-Ritz refinement",
         "solves_per_s": round(len(secs) / t_batch, 2),
         "fp64_per_instance_solves_per_s": round(1.0 / t_ref, 2),
         "speedup_vs_fp64_per_instance": round((len(secs) / t_batch) * t_ref, 2),
@@ -458,6 +458,21 @@ def run_precision_extra(mb, torch):
             "steps_fp32": r32.steps, "steps_q64": rq.steps,
             "seconds_fp32_refined": round(t32, 3), "seconds_q64": round(tq, 3),
         }
+        if u == 4.0:
+            # the plain FP64 GPU solver on the same problem, same stopping rule
+            op64 = mb.GpuHubbardOperator(b, model, mb.PREC_F64)
+            s64 = op64.seed_vector(0, order=mb.ORDER_TENSOR)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r64 = mb.find_min_eigenpair(op64, 300, s64, order=mb.ORDER_TENSOR, conv_tol=1e-12,
+                                        check_every=10, want_vector=False)
+            t64 = time.perf_counter() - t0
+            del op64, s64
+            torch.cuda.empty_cache()
+            out[f"U={u:g}"].update({
+                "e0_fp64": r64.value, "steps_fp64": r64.steps, "seconds_fp64": round(t64, 3),
+                "rel_dE0_fp64_vs_fp64class": abs(r64.value - rq.value) / abs(rq.value),
+                "speedup_fp32_refined_vs_fp64": round(t64 / t32, 2)})
     return {"workload": "1D L=16 N_up=N_down=8 (165,636,900 states)",
             "note": "plain Lanczos to Ritz stability (1e-10); re-orthogonalised runs are "
                     "covered by the tests at smaller sizes", "runs": out}
