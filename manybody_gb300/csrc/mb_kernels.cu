@@ -117,8 +117,8 @@ static int max_smem_optin() {
 // ---------------------------------------------------------------------------
 // The matrix-free apply:  y = scale * (H - shift) x + beta * z
 // with optional fused dot products (dot_mode bit0: Re<x,y>, bit1: <y,y>,
-// bit2: <x,x>).  One CTA per SM walks the rows r_up in the row schedule's
-// order; it stages the row X[r_up, :] (and one zero element) in shared
+// bit2: <x,x>).  One CTA per SM (two for complex64) walks the rows r_up in
+// the row schedule's order; it stages the row X[r_up, :] (and one zero element) in shared
 // memory when it fits, so the down hops, which stay inside the row, gather
 // from shared memory through the sliced table (one coalesced 4-byte entry
 // per lane and slot: neighbour index | sign << 31, padding = the zero
@@ -128,6 +128,10 @@ static int max_smem_optin() {
 // groups w, w + 32, ... and prefetches its next group's up-hop lines into L2.
 // ---------------------------------------------------------------------------
 constexpr int kApplyThreads = 1024;
+// CTAs per SM: complex64 rows are half the size, and two CTAs per SM (32
+// registers a thread) beat one with 64 registers (measured 2.03 -> 1.75 ms at
+// 4x4 6+6, 3.41 -> 2.98 ms at 1D L=16 8+8); complex128 keeps one.
+template <typename T> constexpr int kApplyCtasPerSm = sizeof(T) == 4 ? 2 : 1;
 
 // +-1 from the sign bit of a table entry
 __device__ __forceinline__ double unit_sign(uint32_t e, double) {
@@ -138,7 +142,7 @@ __device__ __forceinline__ float unit_sign(uint32_t e, float) {
 }
 
 template <typename T, bool STAGED, int DOTS>
-__global__ void __launch_bounds__(kApplyThreads, 1)
+__global__ void __launch_bounds__(kApplyThreads, kApplyCtasPerSm<T>)
 k_apply(OpView v, const typename C2<T>::type* __restrict__ x, typename C2<T>::type* y,
         T hop_coef, T dscale, T shift, T beta, const typename C2<T>::type* z,
         const T* __restrict__ ufold, const T* __restrict__ self_up, const T* __restrict__ self_dn,
@@ -252,8 +256,8 @@ static bool apply_staged(const OpView& v, int precision) {
   return apply_smem(v, precision, true) + 1024 <= (size_t)max_smem_optin();
 }
 
-int apply_grid(const OpView& v, int /*precision*/) {
-  int64_t g = (int64_t)num_sms();
+int apply_grid(const OpView& v, int precision) {
+  int64_t g = (int64_t)num_sms() * (precision == MB_PREC_F32 ? kApplyCtasPerSm<float> : 1);
   if (g > v.Du) g = v.Du;
   return (int)(g > 0 ? g : 1);
 }
@@ -268,7 +272,7 @@ static void apply_t(const OpView& v, const void* x, void* y, double scale, doubl
   const T* uf = sizeof(T) == 8 ? (const T*)v.u_fold : (const T*)v.u_fold_f;
   const T* su = sizeof(T) == 8 ? (const T*)v.self_up : (const T*)v.self_up_f;
   const T* sd = sizeof(T) == 8 ? (const T*)v.self_dn : (const T*)v.self_dn_f;
-  const int grid = apply_grid(v, 0);
+  const int grid = apply_grid(v, sizeof(T) == 4 ? MB_PREC_F32 : MB_PREC_F64);
   kern<<<grid, kApplyThreads, smem, st>>>(v, (const V2*)x, (V2*)y, (T)(-v.t * scale), (T)scale,
                                           (T)shift, (T)beta, (const V2*)z, uf, su, sd, partials);
   MB_CUDA(cudaGetLastError());
