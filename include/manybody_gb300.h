@@ -117,10 +117,37 @@ int mb_model_term_count(mb_model_t model, int64_t* n_terms);
 int mb_compute_matrix_elements_csr(mb_basis_t basis, mb_model_t model, int64_t* nnz,
                                    int64_t* row_ptr, int64_t* col_idx, double* values);
 
+/* ---- the reference's sparse-matrix cache format ---------------------------- *
+ * Hamiltonian caches are cereal binary archives of arma::sp_cx_mat
+ * (src/utils/arma_cereal.h:9-30; written and read by
+ * examples/hubbard_momentum_optical_conductivity.cpp:185-203): uint32 version
+ * 0, uint64 n_rows, n_cols, n_nonzero, then per non-zero in column-major order
+ * uint64 row, uint64 col and the value as two float64, little-endian.
+ * CSR here: row_ptr n_rows+1 entries, col_idx and values (interleaved
+ * complex128) nnz entries, host arrays.
+ * Write: entries go out in column-major order.  Read: two calls, first with
+ * row_ptr == NULL for the sizes; loading follows arma's t(row, col) = value
+ * (a later duplicate wins, an explicit zero stores nothing), rows sorted by
+ * column. */
+int mb_cereal_write_csr(const char* path, int64_t n_rows, int64_t n_cols, const int64_t* row_ptr,
+                        const int64_t* col_idx, const double* values);
+int mb_cereal_read_csr(const char* path, int64_t* n_rows, int64_t* n_cols, int64_t* nnz,
+                       int64_t* row_ptr, int64_t* col_idx, double* values);
+
 /* ---- operator: SparseComplexMatrixOperator (src/numerics/linear_operator.h:81-91)
  * replaced by a matrix-free operator on the GPU.  The operator holds the
  * sector tables on the device; it never stores H. */
 int mb_op_create(mb_basis_t basis, mb_model_t model, int precision, mb_op_t* out);
+/* SparseComplexMatrixOperator itself (src/numerics/linear_operator.h:81-91):
+ * an operator from any square complex sparse matrix in CSR (host arrays, as
+ * mb_cereal_read_csr gives them), applied on the GPU by a CSR kernel, for
+ * Hamiltonians built elsewhere (the reference's cached momentum-space or
+ * correlator matrices).  MB_PREC_F64 or MB_PREC_F32; its index order is the
+ * matrix's own, so MB_ORDER_REFERENCE and MB_ORDER_TENSOR coincide.  Every
+ * driver below takes it (apply, Lanczos, KPM, evolution); the Q64 and
+ * allocation-free entry points take lattice operators only. */
+int mb_op_create_csr(int64_t n, const int64_t* row_ptr, const int64_t* col_idx,
+                     const double* values, int precision, mb_op_t* out);
 int mb_op_destroy(mb_op_t op);
 /* LinearOperator::dimension() (linear_operator.h:42). */
 int mb_op_dimension(mb_op_t op, int64_t* dim);

@@ -94,6 +94,9 @@ SIGNATURES = {
     "mb_model_term_count": (C.c_int, [_vp, _i64p]),
     "mb_compute_matrix_elements_csr": (C.c_int, [_vp, _vp, _i64p, _i64p, _i64p, _dp]),
     "mb_op_create": (C.c_int, [_vp, _vp, C.c_int, C.POINTER(_vp)]),
+    "mb_op_create_csr": (C.c_int, [_i64, _i64p, _i64p, _dp, C.c_int, C.POINTER(_vp)]),
+    "mb_cereal_write_csr": (C.c_int, [C.c_char_p, _i64, _i64, _i64p, _i64p, _dp]),
+    "mb_cereal_read_csr": (C.c_int, [C.c_char_p, _i64p, _i64p, _i64p, _i64p, _i64p, _dp]),
     "mb_op_destroy": (C.c_int, [_vp]),
     "mb_op_dimension": (C.c_int, [_vp, _i64p]),
     "mb_op_precision": (C.c_int, [_vp, C.POINTER(C.c_int)]),
@@ -298,19 +301,53 @@ class HubbardModel3D(_Hubbard):
 
 @dataclass
 class CsrMatrix:
-    """Reference-order sparse H: row_ptr (dim+1), col_idx, values (complex128)."""
+    """Reference-order sparse H: row_ptr (dim+1), col_idx, values (complex128);
+    n_cols = 0 means square."""
     dim: int
     row_ptr: np.ndarray
     col_idx: np.ndarray
     values: np.ndarray
+    n_cols: int = 0
 
     @property
     def nnz(self) -> int:
         return int(self.row_ptr[-1])
 
+    @property
+    def cols(self) -> int:
+        return self.n_cols or self.dim
+
     def to_scipy(self):
         import scipy.sparse as sp
-        return sp.csr_matrix((self.values, self.col_idx, self.row_ptr), shape=(self.dim, self.dim))
+        return sp.csr_matrix((self.values, self.col_idx, self.row_ptr), shape=(self.dim, self.cols))
+
+
+def write_cereal(path: str, m: CsrMatrix) -> None:
+    """Writes m in the reference's sparse-matrix cache format (cereal binary
+    archive of arma::sp_cx_mat, src/utils/arma_cereal.h:9-30)."""
+    rp = np.ascontiguousarray(m.row_ptr, np.int64)
+    ci = np.ascontiguousarray(m.col_idx, np.int64)
+    vals = np.ascontiguousarray(m.values, np.complex128)
+    if ci.size == 0:
+        ci = np.zeros(1, np.int64)
+        vals = np.zeros(1, np.complex128)
+    _check(lib().mb_cereal_write_csr(os.fsencode(path), m.dim, m.cols, rp.ctypes.data_as(_i64p),
+                                     ci.ctypes.data_as(_i64p), vals.view(np.float64).ctypes.data_as(_dp)))
+
+
+def read_cereal(path: str) -> CsrMatrix:
+    """Reads a matrix in the reference's sparse-matrix cache format."""
+    r, c, nz = C.c_int64(), C.c_int64(), C.c_int64()
+    _check(lib().mb_cereal_read_csr(os.fsencode(path), C.byref(r), C.byref(c), C.byref(nz), None,
+                                    None, None))
+    rp = np.zeros(r.value + 1, np.int64)
+    ci = np.zeros(max(nz.value, 1), np.int64)
+    vals = np.zeros(max(nz.value, 1), np.complex128)
+    _check(lib().mb_cereal_read_csr(os.fsencode(path), C.byref(r), C.byref(c), C.byref(nz),
+                                    rp.ctypes.data_as(_i64p), ci.ctypes.data_as(_i64p),
+                                    vals.view(np.float64).ctypes.data_as(_dp)))
+    n = nz.value
+    return CsrMatrix(r.value, rp, ci[:n], vals[:n], 0 if c.value == r.value else c.value)
 
 
 def compute_matrix_elements(basis: FermionBasis, model: _Hubbard) -> CsrMatrix:
@@ -451,6 +488,32 @@ class GpuHubbardOperator:
         r = C.c_double()
         _check(lib().mb_norm(self._h, _ptr(x), C.byref(r)))
         return r.value
+
+
+class GpuSparseOperator(GpuHubbardOperator):
+    """SparseComplexMatrixOperator (src/numerics/linear_operator.h:81-91) on the GPU:
+    any square complex sparse matrix (a CsrMatrix, e.g. from read_cereal), with
+    the same apply / Krylov / KPM / evolution drivers.  Its index order is the
+    matrix's own (reference and tensor order coincide)."""
+
+    def __init__(self, m: CsrMatrix, precision: int = PREC_F64):
+        if m.cols != m.dim:
+            raise ValueError("a sparse operator needs a square matrix")
+        rp = np.ascontiguousarray(m.row_ptr, np.int64)
+        ci = np.ascontiguousarray(m.col_idx, np.int64)
+        vals = np.ascontiguousarray(m.values, np.complex128)
+        if ci.size == 0:
+            ci = np.zeros(1, np.int64)
+            vals = np.zeros(1, np.complex128)
+        h = C.c_void_p()
+        _check(lib().mb_op_create_csr(m.dim, rp.ctypes.data_as(_i64p), ci.ctypes.data_as(_i64p),
+                                      vals.view(np.float64).ctypes.data_as(_dp), precision,
+                                      C.byref(h)))
+        self._h = h
+        self.precision = precision
+        self.basis = None
+        self.model = None
+        self._dim = m.dim
 
 
 def _sync_torch():

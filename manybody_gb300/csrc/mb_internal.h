@@ -234,6 +234,12 @@ struct OpView {
   const int32_t* dn_sgrp;
   const uint8_t* dn_nneg;  // per down state: number of negative hops (doubled twice)
   int max_up_list;
+  // Operators made from a sparse matrix instead of a lattice (mb_op_create_csr):
+  // CSR on the device, values complex128 (and complex64 copies for MB_PREC_F32).
+  const int64_t* csr_row;
+  const int32_t* csr_col;
+  const double2* csr_val;
+  const float2* csr_val_f;
   double t;
   int max_up_degree;
   int max_dn_degree;
@@ -255,6 +261,7 @@ struct mb_op_s {
   int64_t Du = 0, Dd = 0, dim = 0;
   double t = 0.0, u = 0.0;
   mb::OpView view{};
+  bool natural_order = false;      // a sparse-matrix operator: reference order = its own index
   std::vector<void*> allocations;  // device buffers owned by the op
   int32_t* perm = nullptr;         // tensor -> reference index (lazy)
   int32_t* iperm = nullptr;        // reference -> tensor index (lazy)

@@ -256,7 +256,10 @@ static bool apply_staged(const OpView& v, int precision) {
   return apply_smem(v, precision, true) + 1024 <= (size_t)max_smem_optin();
 }
 
+static int csr_grid(int64_t n);
+
 int apply_grid(const OpView& v, int precision) {
+  if (v.csr_row) return csr_grid(v.dim);
   int64_t g = (int64_t)num_sms() * (precision == MB_PREC_F32 ? kApplyCtasPerSm<float> : 1);
   if (g > v.Du) g = v.Du;
   return (int)(g > 0 ? g : 1);
@@ -292,9 +295,100 @@ static void apply_dots(const OpView& v, const void* x, void* y, double scale, do
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same contract for an operator given as a sparse matrix (CSR): one warp
+// per row (rows grid-strided over a fixed grid), lanes over the row's
+// entries, complex products, a fixed-order shuffle sum, then the affine
+// epilogue and the fused dots in lane 0.  Deterministic.
+// ---------------------------------------------------------------------------
+constexpr int kCsrThreads = 256;
+
+template <typename T, int DOTS>
+__global__ void __launch_bounds__(kCsrThreads)
+k_csr_apply(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+            const typename C2<T>::type* __restrict__ val, const typename C2<T>::type* __restrict__ x,
+            typename C2<T>::type* y, T scale, T shift, T beta, const typename C2<T>::type* z,
+            double* __restrict__ partials) {
+  using V2 = typename C2<T>::type;
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  DotAcc<T> a_xy, a_yy, a_xx;
+  for (int64_t row = w0; row < n; row += nw) {
+    T ar = T(0), ai = T(0);
+    for (int64_t k = rp[row] + lane; k < rp[row + 1]; k += 32) {
+      const V2 a = val[k], b = x[ci[k]];
+      ar = fma(a.x, b.x, fma(-a.y, b.y, ar));
+      ai = fma(a.x, b.y, fma(a.y, b.x, ai));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ar += __shfl_xor_sync(0xffffffffu, ar, o);
+      ai += __shfl_xor_sync(0xffffffffu, ai, o);
+    }
+    if (lane == 0) {
+      const V2 xv = x[row];
+      V2 out;
+      out.x = scale * (ar - shift * xv.x);
+      out.y = scale * (ai - shift * xv.y);
+      if (z) {
+        const V2 zv = z[row];
+        out.x = fma(beta, zv.x, out.x);
+        out.y = fma(beta, zv.y, out.y);
+      }
+      y[row] = out;
+      if (DOTS & 1) { a_xy.add_prod(xv.x, out.x); a_xy.add_prod(xv.y, out.y); }
+      if (DOTS & 2) { a_yy.add_prod(out.x, out.x); a_yy.add_prod(out.y, out.y); }
+      if (DOTS & 4) { a_xx.add_prod(xv.x, xv.x); a_xx.add_prod(xv.y, xv.y); }
+    }
+  }
+  if (DOTS) {
+    double vals[3] = {a_xy.value(), a_yy.value(), a_xx.value()};
+    block_reduce_store<3>(vals, partials);
+  }
+}
+
+static int csr_grid(int64_t n) {
+  const int64_t rows_per_block = kCsrThreads / 32;
+  int64_t g = (n + rows_per_block - 1) / rows_per_block;
+  const int64_t cap = (int64_t)num_sms() * 16;
+  if (g > cap) g = cap;
+  return (int)(g > 0 ? g : 1);
+}
+
+template <typename T, int DOTS>
+static void csr_apply_t(const OpView& v, const void* x, void* y, double scale, double shift,
+                        double beta, const void* z, double* partials, cudaStream_t st) {
+  using V2 = typename C2<T>::type;
+  const V2* val = sizeof(T) == 8 ? (const V2*)v.csr_val : (const V2*)v.csr_val_f;
+  k_csr_apply<T, DOTS><<<csr_grid(v.dim), kCsrThreads, 0, st>>>(
+      v.dim, v.csr_row, v.csr_col, val, (const V2*)x, (V2*)y, (T)scale, (T)shift, (T)beta,
+      (const V2*)z, partials);
+  MB_CUDA(cudaGetLastError());
+}
+
+template <typename T>
+static void csr_apply_dots(const OpView& v, const void* x, void* y, double scale, double shift,
+                           double beta, const void* z, double* partials, int dot_mode,
+                           cudaStream_t st) {
+  switch (dot_mode) {
+    case 0: csr_apply_t<T, 0>(v, x, y, scale, shift, beta, z, partials, st); break;
+    case 1: csr_apply_t<T, 1>(v, x, y, scale, shift, beta, z, partials, st); break;
+    case 2: csr_apply_t<T, 2>(v, x, y, scale, shift, beta, z, partials, st); break;
+    case 3: csr_apply_t<T, 3>(v, x, y, scale, shift, beta, z, partials, st); break;
+    case 5: csr_apply_t<T, 5>(v, x, y, scale, shift, beta, z, partials, st); break;
+    default: csr_apply_t<T, 7>(v, x, y, scale, shift, beta, z, partials, st); break;
+  }
+}
+
 void launch_apply(const OpView& v, int precision, const void* x, void* y, double scale,
                   double shift, double beta, const void* z, double* partials, int dot_mode,
                   cudaStream_t st) {
+  if (v.csr_row) {
+    if (precision == MB_PREC_F32) csr_apply_dots<float>(v, x, y, scale, shift, beta, z, partials, dot_mode, st);
+    else csr_apply_dots<double>(v, x, y, scale, shift, beta, z, partials, dot_mode, st);
+    return;
+  }
   const bool staged = apply_staged(v, precision);
   if (precision == MB_PREC_F32) {
     if (staged) apply_dots<float, true>(v, x, y, scale, shift, beta, z, partials, dot_mode, st);

@@ -219,7 +219,7 @@ int32_t* op_iperm(mb_op_s* op) {
 }
 
 static void to_tensor(mb_op_s* op, const void* src, void* dst, int order, cudaStream_t st) {
-  if (order == MB_ORDER_TENSOR) {
+  if (order == MB_ORDER_TENSOR || op->natural_order) {
     if (src != dst)
       MB_CUDA(cudaMemcpyAsync(dst, src, elem_bytes(op->precision) * (size_t)op->dim,
                               cudaMemcpyDeviceToDevice, st));
@@ -230,7 +230,7 @@ static void to_tensor(mb_op_s* op, const void* src, void* dst, int order, cudaSt
 }
 
 static void from_tensor(mb_op_s* op, const void* src, void* dst, int order, cudaStream_t st) {
-  if (order == MB_ORDER_TENSOR) {
+  if (order == MB_ORDER_TENSOR || op->natural_order) {
     if (src != dst)
       MB_CUDA(cudaMemcpyAsync(dst, src, elem_bytes(op->precision) * (size_t)op->dim,
                               cudaMemcpyDeviceToDevice, st));
@@ -653,6 +653,55 @@ int mb_op_create(mb_basis_t basis, mb_model_t model, int precision, mb_op_t* out
     op->precision = precision;
     try {
       build_op(op.get(), basis, model);
+    } catch (...) {
+      for (void* p : op->allocations) cudaFree(p);
+      throw;
+    }
+    *out = op.release();
+  });
+}
+
+int mb_op_create_csr(int64_t n, const int64_t* row_ptr, const int64_t* col_idx,
+                     const double* values, int precision, mb_op_t* out) {
+  return guard([&] {
+    MB_REQUIRE(row_ptr && out && n > 0, MB_ERR_INVALID_ARG, "NULL argument or empty matrix");
+    *out = nullptr;
+    MB_REQUIRE(precision == MB_PREC_F64 || precision == MB_PREC_F32, MB_ERR_INVALID_ARG,
+               "a sparse-matrix operator takes MB_PREC_F64 or MB_PREC_F32");
+    MB_REQUIRE(n < (int64_t(1) << 31), MB_ERR_CAPACITY, "matrix dimension above 2^31 - 1");
+    MB_REQUIRE(row_ptr[0] == 0, MB_ERR_INVALID_ARG, "row_ptr[0] must be 0");
+    for (int64_t i = 0; i < n; ++i)
+      MB_REQUIRE(row_ptr[i + 1] >= row_ptr[i], MB_ERR_INVALID_ARG, "row_ptr must not decrease");
+    const int64_t nnz = row_ptr[n];
+    MB_REQUIRE(nnz == 0 || (col_idx && values), MB_ERR_INVALID_ARG, "NULL col_idx or values");
+    std::vector<int32_t> col((size_t)std::max<int64_t>(nnz, 1), 0);
+    for (int64_t k = 0; k < nnz; ++k) {
+      MB_REQUIRE(col_idx[k] >= 0 && col_idx[k] < n, MB_ERR_INVALID_ARG, "column index out of range");
+      col[(size_t)k] = (int32_t)col_idx[k];
+    }
+    require_device();
+    auto op = std::make_unique<mb_op_s>();
+    op->precision = precision;
+    op->natural_order = true;
+    try {
+      MB_CUDA(cudaGetDevice(&op->device));
+      op->Du = n;
+      op->Dd = 1;
+      op->dim = n;
+      OpView& v = op->view;
+      v.Du = n;
+      v.Dd = 1;
+      v.dim = n;
+      v.csr_row = upload(op.get(), std::vector<int64_t>(row_ptr, row_ptr + n + 1));
+      v.csr_col = upload(op.get(), col);
+      std::vector<double2> val((size_t)std::max<int64_t>(nnz, 1), make_double2(0.0, 0.0));
+      for (int64_t k = 0; k < nnz; ++k) val[(size_t)k] = make_double2(values[2 * k], values[2 * k + 1]);
+      v.csr_val = upload(op.get(), val);
+      if (precision == MB_PREC_F32) {
+        std::vector<float2> vf(val.size());
+        for (size_t k = 0; k < val.size(); ++k) vf[k] = make_float2((float)val[k].x, (float)val[k].y);
+        v.csr_val_f = upload(op.get(), vf);
+      }
     } catch (...) {
       for (void* p : op->allocations) cudaFree(p);
       throw;

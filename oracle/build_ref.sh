@@ -6,7 +6,9 @@
 # The stock value caps a monomial at 7 operators, which silently drops
 # every Hubbard term acting on a sector with more than 3 particles
 # (src/algebra/expression_base.h:182-186); 128 gives a 55-operator cap.
-# The copy and the binary live only under oracle/_ref/ (git-ignored).
+# Also builds oracle/_ref/cereal_pin (oracle/cereal_pin.cpp against the
+# reference's vendored cereal headers).
+# The copy and the binaries live only under oracle/_ref/ (git-ignored).
 # Test infrastructure: the product never calls anything built here.
 set -e
 REF=${MANYBODY_REFERENCE:-/root/reference}
@@ -33,3 +35,6 @@ ${CXX:-g++} -std=c++20 -O2 -fopenmp -DNDEBUG \
   "$OUT/src/utils/xxhash_impl.cpp" \
   -o "$OUT/ref_dump"
 echo "built $OUT/ref_dump"
+# The cache-format pin: the vendored cereal library only (no reference code).
+${CXX:-g++} -std=c++17 -O2 -I"$REF/third-party" "$HERE/cereal_pin.cpp" -o "$OUT/cereal_pin"
+echo "built $OUT/cereal_pin"
