@@ -82,6 +82,15 @@ int mb_synchronize(void);
  * <= 32 and C(L,N_up), C(L,N_down) <= 2^23. */
 int mb_basis_create_fixed_spin(int64_t orbitals, int64_t particles, int spin_projection,
                                mb_basis_t* out);
+/* BasisImpl::with_fixed_particle_number_spin_momentum (src/algebra/basis.cpp:128-185,
+ * 304-356): the states of one total momentum K on a periodic lattice of sizes
+ * dims[0..ndim) (orbital k has coordinates k_d, first dimension fastest;
+ * total momentum = sum of the occupied orbitals' coordinates mod the sizes),
+ * in the reference's index order (its depth-first order filtered by K).
+ * mb_basis_size / export / index_of work as for the full sector; the
+ * permutation is the identity (operators on it use reference order). */
+int mb_basis_create_momentum(const int64_t* dims, int ndim, int64_t particles,
+                             int spin_projection, const int64_t* momentum, mb_basis_t* out);
 int mb_basis_destroy(mb_basis_t basis);
 /* basis.set.size() (compute_basis_size_spin, src/algebra/basis.cpp:39-50). */
 int mb_basis_size(mb_basis_t basis, int64_t* dim);
@@ -105,6 +114,15 @@ int mb_basis_permutation(mb_basis_t basis, int64_t* ref_of_tensor);
  * as the reference's merged expression does (tests/algebra/test_model.cpp:58-74).
  * Coefficients with |c| < 1000*eps are dropped (src/utils/tolerances.h:7-10). */
 int mb_hubbard_create(const int64_t* dims, int ndim, double t, double u, mb_model_t* out);
+/* HubbardModelMomentum (src/algebra/fermion/model/hubbard_model_momentum.h:19-180):
+ * H = sum_{k,s} eps(k) n_{k,s} + (U/N) sum_{k1,k2,q} c+_{k1+q,up} c+_{k2-q,dn}
+ * c_{k2,dn} c_{k1,up}, eps(k) = -2t sum_d cos(2 pi k_d / L_d), on momentum
+ * orbitals (same lattice indexing).  With a momentum-sector basis it gives
+ * the sector's H: mb_compute_matrix_elements_csr (built on the GPU) and
+ * mb_op_create (MB_PREC_F64 / MB_PREC_F32: the sector's H kept on the device
+ * in signed-column sparse form; reference order). */
+int mb_hubbard_momentum_create(const int64_t* dims, int ndim, double t, double u,
+                               mb_model_t* out);
 int mb_model_destroy(mb_model_t model);
 /* FermionExpression::size() of hamiltonian(): number of distinct terms. */
 int mb_model_term_count(mb_model_t model, int64_t* n_terms);

@@ -95,6 +95,8 @@ SIGNATURES = {
     "mb_compute_matrix_elements_csr": (C.c_int, [_vp, _vp, _i64p, _i64p, _i64p, _dp]),
     "mb_op_create": (C.c_int, [_vp, _vp, C.c_int, C.POINTER(_vp)]),
     "mb_op_create_csr": (C.c_int, [_i64, _i64p, _i64p, _dp, C.c_int, C.POINTER(_vp)]),
+    "mb_basis_create_momentum": (C.c_int, [_i64p, C.c_int, _i64, C.c_int, _i64p, C.POINTER(_vp)]),
+    "mb_hubbard_momentum_create": (C.c_int, [_i64p, C.c_int, C.c_double, C.c_double, C.POINTER(_vp)]),
     "mb_cereal_write_csr": (C.c_int, [C.c_char_p, _i64, _i64, _i64p, _i64p, _dp]),
     "mb_cereal_read_csr": (C.c_int, [C.c_char_p, _i64p, _i64p, _i64p, _i64p, _i64p, _dp]),
     "mb_op_destroy": (C.c_int, [_vp]),
@@ -202,6 +204,25 @@ class FermionBasis:
         _check(lib().mb_basis_create_fixed_spin(orbitals, particles, spin_projection, C.byref(h)))
         return cls(h, orbitals, particles)
 
+    @classmethod
+    def with_fixed_particle_number_spin_momentum(cls, orbitals: int, particles: int,
+                                                 spin_projection: int, dims,
+                                                 momentum) -> "FermionBasis":
+        """with_fixed_particle_number_spin_momentum (src/algebra/basis.cpp:128-185):
+        the states of total momentum `momentum` on the periodic lattice `dims`."""
+        dims = tuple(int(d) for d in dims)
+        momentum = tuple(int(k) for k in momentum)
+        if int(np.prod(dims)) != orbitals or len(momentum) != len(dims):
+            raise ValueError("orbitals must equal the lattice size, momentum one entry per dimension")
+        d = (C.c_int64 * len(dims))(*dims)
+        k = (C.c_int64 * len(dims))(*momentum)
+        h = C.c_void_p()
+        _check(lib().mb_basis_create_momentum(d, len(dims), particles, spin_projection, k,
+                                              C.byref(h)))
+        b = cls(h, orbitals, particles)
+        b.dims, b.momentum = dims, momentum
+        return b
+
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
             _lib.mb_basis_destroy(self._h)
@@ -257,11 +278,13 @@ class FermionBasis:
 # HubbardModel / 2D / 3D (src/algebra/fermion/model/hubbard_model.h)
 # ---------------------------------------------------------------------------
 class _Hubbard:
+    _create = "mb_hubbard_create"
+
     def __init__(self, t: float, u: float, dims):
         self.t, self.u, self.dims = float(t), float(u), tuple(int(d) for d in dims)
         d = (C.c_int64 * len(self.dims))(*self.dims)
         h = C.c_void_p()
-        _check(lib().mb_hubbard_create(d, len(self.dims), self.t, self.u, C.byref(h)))
+        _check(getattr(lib(), self._create)(d, len(self.dims), self.t, self.u, C.byref(h)))
         self._h = h
 
     def __del__(self):
@@ -297,6 +320,16 @@ class HubbardModel2D(_Hubbard):
 class HubbardModel3D(_Hubbard):
     def __init__(self, t, u, size_x, size_y, size_z):
         super().__init__(t, u, (size_x, size_y, size_z))
+
+
+class HubbardModelMomentum(_Hubbard):
+    """HubbardModelMomentum (src/algebra/fermion/model/hubbard_model_momentum.h:19-180):
+    the Hubbard model on momentum orbitals; with a momentum-sector basis it
+    gives that sector's H (compute_matrix_elements, GpuHubbardOperator)."""
+    _create = "mb_hubbard_momentum_create"
+
+    def __init__(self, t, u, size):
+        super().__init__(t, u, tuple(size))
 
 
 @dataclass

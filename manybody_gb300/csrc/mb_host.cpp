@@ -343,6 +343,45 @@ bool tridiag_eig(int n, std::vector<double>& d, const std::vector<double>& e_in,
 
 using namespace mb;
 
+// Momentum (flat orbital index) of a set of occupied orbitals on a periodic
+// lattice: the componentwise sum of the orbitals' coordinates modulo the
+// sizes, first dimension fastest (src/utils/index.h:69-100).
+namespace mb {
+
+static int64_t mask_momentum(uint32_t mask, const std::vector<int64_t>& dims) {
+  std::vector<int64_t> tot(dims.size(), 0);
+  while (mask) {
+    const int k = __builtin_ctz(mask);
+    mask &= mask - 1;
+    int64_t rest = k;
+    for (size_t d = 0; d < dims.size(); ++d) {
+      tot[d] = (tot[d] + rest % dims[d]) % dims[d];
+      rest /= dims[d];
+    }
+  }
+  int64_t flat = 0, stride = 1;
+  for (size_t d = 0; d < dims.size(); ++d) {
+    flat += tot[d] * stride;
+    stride *= dims[d];
+  }
+  return flat;
+}
+
+// Flat index of k + sign * q on the lattice.
+int64_t momentum_add(int64_t k, int64_t q, int sign, const std::vector<int64_t>& dims) {
+  int64_t flat = 0, stride = 1;
+  for (size_t d = 0; d < dims.size(); ++d) {
+    const int64_t kd = k % dims[d], qd = q % dims[d];
+    flat += ((kd + sign * qd + dims[d]) % dims[d]) * stride;
+    k /= dims[d];
+    q /= dims[d];
+    stride *= dims[d];
+  }
+  return flat;
+}
+
+}  // namespace mb
+
 extern "C" {
 
 int mb_version(void) { return 10000; }
@@ -377,6 +416,56 @@ int mb_basis_create_fixed_spin(int64_t orbitals, int64_t particles, int spin_pro
   });
 }
 
+int mb_basis_create_momentum(const int64_t* dims, int ndim, int64_t particles,
+                             int spin_projection, const int64_t* momentum, mb_basis_t* out) {
+  return guard([&] {
+    MB_REQUIRE(dims && momentum && out && ndim >= 1 && ndim <= 3, MB_ERR_INVALID_ARG,
+               "NULL argument or ndim outside 1..3");
+    *out = nullptr;
+    int64_t L = 1;
+    std::vector<int64_t> kd(dims, dims + ndim), kv(momentum, momentum + ndim);
+    for (int d = 0; d < ndim; ++d) {
+      MB_REQUIRE(dims[d] >= 1, MB_ERR_INVALID_ARG, "lattice sizes must be >= 1");
+      MB_REQUIRE(momentum[d] >= 0 && momentum[d] < dims[d], MB_ERR_INVALID_ARG,
+                 "momentum component outside [0, size)");
+      L *= dims[d];
+      MB_REQUIRE(L <= kMaxOrbitals, MB_ERR_CAPACITY, "more than 32 orbitals");
+    }
+    mb_basis_t full = nullptr;
+    const int rc = mb_basis_create_fixed_spin(L, particles, spin_projection, &full);
+    if (rc) throw Error(rc, mb_last_error());
+    std::unique_ptr<mb_basis_s> b(full);
+    b->kdims = kd;
+    b->kvec = kv;
+    int64_t K = 0, stride = 1;
+    for (int d = 0; d < ndim; ++d) {
+      K += kv[(size_t)d] * stride;
+      stride *= kd[(size_t)d];
+    }
+    // down states grouped by momentum
+    std::vector<std::vector<uint32_t>> dn_by_p((size_t)L);
+    for (uint32_t m : b->down.masks) dn_by_p[(size_t)mask_momentum(m, kd)].push_back(m);
+    const Binom& B = binom_table();
+    std::vector<std::pair<int64_t, std::pair<uint32_t, uint32_t>>> states;
+    for (uint32_t u : b->up.masks) {
+      const int64_t pu = mask_momentum(u, kd);
+      const auto& group = dn_by_p[(size_t)momentum_add(K, pu, -1, kd)];
+      for (uint32_t d : group) states.push_back({reference_rank(B, u, d, b->L), {u, d}});
+    }
+    std::sort(states.begin(), states.end());
+    b->dim = (int64_t)states.size();
+    b->kup.resize(states.size());
+    b->kdown.resize(states.size());
+    b->kfull.resize(states.size());
+    for (size_t i = 0; i < states.size(); ++i) {
+      b->kfull[i] = states[i].first;
+      b->kup[i] = states[i].second.first;
+      b->kdown[i] = states[i].second.second;
+    }
+    *out = b.release();
+  });
+}
+
 int mb_basis_destroy(mb_basis_t basis) {
   delete basis;
   return MB_OK;
@@ -404,6 +493,13 @@ int mb_basis_sector(mb_basis_t basis, int64_t* orbitals, int64_t* n_up, int64_t*
 int mb_basis_export_reference_order(mb_basis_t basis, uint64_t* up_masks, uint64_t* down_masks) {
   return guard([&] {
     MB_REQUIRE(basis && up_masks && down_masks, MB_ERR_INVALID_ARG, "NULL argument");
+    if (basis->momentum()) {
+      for (int64_t i = 0; i < basis->dim; ++i) {
+        up_masks[i] = basis->kup[(size_t)i];
+        down_masks[i] = basis->kdown[(size_t)i];
+      }
+      return;
+    }
     const Binom& B = binom_table();
     const int64_t Dd = basis->down.D;
 #pragma omp parallel for schedule(static)
@@ -425,12 +521,22 @@ int mb_basis_index_of(mb_basis_t basis, uint64_t up_mask, uint64_t down_mask, in
                    __builtin_popcountll(down_mask) == basis->n_down,
                MB_ERR_INVALID_ARG, "key is not in the basis");
     *index = reference_rank(binom_table(), (uint32_t)up_mask, (uint32_t)down_mask, basis->L);
+    if (basis->momentum()) {
+      const auto it = std::lower_bound(basis->kfull.begin(), basis->kfull.end(), *index);
+      MB_REQUIRE(it != basis->kfull.end() && *it == *index, MB_ERR_INVALID_ARG,
+                 "key is not in the basis (other total momentum)");
+      *index = it - basis->kfull.begin();
+    }
   });
 }
 
 int mb_basis_permutation(mb_basis_t basis, int64_t* ref_of_tensor) {
   return guard([&] {
     MB_REQUIRE(basis && ref_of_tensor, MB_ERR_INVALID_ARG, "NULL argument");
+    if (basis->momentum()) {  // operators on a momentum sector index it in reference order
+      for (int64_t i = 0; i < basis->dim; ++i) ref_of_tensor[i] = i;
+      return;
+    }
     const Binom& B = binom_table();
     const int64_t Dd = basis->down.D;
 #pragma omp parallel for schedule(static)
@@ -498,6 +604,50 @@ int mb_hubbard_create(const int64_t* dims, int ndim, double t, double u, mb_mode
 int mb_model_destroy(mb_model_t model) {
   delete model;
   return MB_OK;
+}
+
+int mb_hubbard_momentum_create(const int64_t* dims, int ndim, double t, double u,
+                               mb_model_t* out) {
+  return guard([&] {
+    MB_REQUIRE(out && dims, MB_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    MB_REQUIRE(ndim >= 1 && ndim <= 3, MB_ERR_INVALID_ARG, "ndim must be 1, 2 or 3");
+    int64_t L = 1;
+    for (int d = 0; d < ndim; ++d) {
+      MB_REQUIRE(dims[d] >= 1, MB_ERR_INVALID_ARG, "lattice dimension of size zero");
+      L *= dims[d];
+      MB_REQUIRE(L <= kMaxOrbitals, MB_ERR_CAPACITY, "more than 32 sites");
+    }
+    MB_REQUIRE(std::isfinite(t) && std::isfinite(u), MB_ERR_INVALID_ARG, "t and U must be finite");
+    auto m = std::make_unique<mb_model_s>();
+    m->dims.assign(dims, dims + ndim);
+    m->L = (int)L;
+    m->t = t;
+    m->u = u;
+    m->momentum = true;
+    m->eps.assign((size_t)L, 0.0);
+    int64_t kinetic = 0;
+    for (int64_t k = 0; k < L; ++k) {
+      // epsilon(k) = -2t sum_d cos(2 pi k_d / L_d), accumulated as the
+      // reference does (hubbard_model_momentum.h:28-36)
+      double e = 0.0;
+      int64_t rest = k;
+      for (int d = 0; d < ndim; ++d) {
+        const double phase = 2.0 * 3.14159265358979323846 * (double)(rest % dims[d]) / (double)dims[d];
+        e += -2.0 * t * std::cos(phase);
+        rest /= dims[d];
+      }
+      if (e * e < kTol * kTol) e = 0.0;  // the expression drops |c| < 1000 eps
+      m->eps[(size_t)k] = e;
+      kinetic += e != 0.0 ? 2 : 0;
+    }
+    const double uon = u / (double)L;
+    m->u_over_n = uon * uon < kTol * kTol ? 0.0 : uon;
+    m->has_hop = kinetic > 0;
+    m->has_u = m->u_over_n != 0.0;
+    m->n_terms = kinetic + (m->has_u ? L * L * L : 0);
+    *out = m.release();
+  });
 }
 
 int mb_model_term_count(mb_model_t model, int64_t* n_terms) {

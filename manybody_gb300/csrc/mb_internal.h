@@ -130,6 +130,13 @@ struct mb_basis_s {
   int L = 0, n_up = 0, n_down = 0;
   int64_t dim = 0;
   mb::SpinSector up, down;
+  // A total-momentum sector (with_fixed_particle_number_spin_momentum): its
+  // states' masks in reference order, their full-(N_up, N_down)-sector
+  // reference ranks (ascending), the lattice and the momentum.
+  std::vector<int64_t> kdims, kvec;
+  std::vector<uint32_t> kup, kdown;
+  std::vector<int64_t> kfull;
+  bool momentum() const { return !kdims.empty(); }
 };
 
 struct mb_model_s {
@@ -144,6 +151,11 @@ struct mb_model_s {
   // self_mult[i] = number of hopping(i, i) calls (a dimension of size 1).
   std::vector<int> self_mult;
   int64_t n_terms = 0;
+  // The momentum-space model (HubbardModelMomentum): dispersion per orbital
+  // and U/N, each 0 where the expression's 1000 eps zero drop removes it.
+  bool momentum = false;
+  std::vector<double> eps;
+  double u_over_n = 0.0;
 };
 
 namespace mb {
@@ -240,6 +252,10 @@ struct OpView {
   const int32_t* csr_col;
   const double2* csr_val;
   const float2* csr_val_f;
+  // Signed-column form (csr_val == nullptr): an entry is +-csr_off by bit 31
+  // of its column, plus a separate diagonal (the momentum-sector operators).
+  const double* csr_diag;
+  double csr_off;
   double t;
   int max_up_degree;
   int max_dn_degree;
@@ -288,6 +304,28 @@ struct mb_op_s {
 };
 
 namespace mb {
+
+// Flat orbital index of momentum k + sign * q on a periodic lattice (first
+// dimension fastest).
+int64_t momentum_add(int64_t k, int64_t q, int sign, const std::vector<int64_t>& dims);
+
+// A momentum sector's Hamiltonian on the device (see mb_kernels.cu): the
+// states, the momentum arithmetic of the lattice and the model's numbers.
+struct MomTables {
+  int64_t n;
+  int L, n_up, n_down;
+  const uint32_t* up;     // masks, reference order
+  const uint32_t* dn;
+  const int64_t* full;    // full-sector reference ranks, ascending
+  const double* eps;      // [L]
+  const uint8_t* kadd;    // [L*L]: orbital of momentum k + q
+  const uint8_t* ksub;    // [L*L]: orbital of momentum k - q
+  double u_over_n;
+};
+// Per row: the diagonal (0 when dropped) and the number of off-diagonal
+// entries; then the off-diagonal columns (index | negative << 31).
+void launch_mom_count(const MomTables& m, int32_t* count, double* diag, cudaStream_t st);
+void launch_mom_fill(const MomTables& m, const int64_t* row_ptr, int32_t* col, cudaStream_t st);
 
 // Kernel launchers (mb_kernels.cu).  All asynchronous on `st`.
 size_t elem_bytes(int precision);

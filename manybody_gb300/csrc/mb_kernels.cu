@@ -299,16 +299,17 @@ static void apply_dots(const OpView& v, const void* x, void* y, double scale, do
 // The same contract for an operator given as a sparse matrix (CSR): one warp
 // per row (rows grid-strided over a fixed grid), lanes over the row's
 // entries, complex products, a fixed-order shuffle sum, then the affine
-// epilogue and the fused dots in lane 0.  Deterministic.
+// epilogue and the fused dots in lane 0.  Deterministic.  In the signed-
+// column form (no values) every entry is +-off and the diagonal comes apart.
 // ---------------------------------------------------------------------------
 constexpr int kCsrThreads = 256;
 
 template <typename T, int DOTS>
 __global__ void __launch_bounds__(kCsrThreads)
 k_csr_apply(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
-            const typename C2<T>::type* __restrict__ val, const typename C2<T>::type* __restrict__ x,
-            typename C2<T>::type* y, T scale, T shift, T beta, const typename C2<T>::type* z,
-            double* __restrict__ partials) {
+            const typename C2<T>::type* __restrict__ val, const double* __restrict__ diag, T off,
+            const typename C2<T>::type* __restrict__ x, typename C2<T>::type* y, T scale, T shift,
+            T beta, const typename C2<T>::type* z, double* __restrict__ partials) {
   using V2 = typename C2<T>::type;
   const int lane = threadIdx.x & 31;
   const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -316,10 +317,24 @@ k_csr_apply(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict
   DotAcc<T> a_xy, a_yy, a_xx;
   for (int64_t row = w0; row < n; row += nw) {
     T ar = T(0), ai = T(0);
-    for (int64_t k = rp[row] + lane; k < rp[row + 1]; k += 32) {
-      const V2 a = val[k], b = x[ci[k]];
-      ar = fma(a.x, b.x, fma(-a.y, b.y, ar));
-      ai = fma(a.x, b.y, fma(a.y, b.x, ai));
+    if (val) {
+      for (int64_t k = rp[row] + lane; k < rp[row + 1]; k += 32) {
+        const V2 a = val[k], b = x[ci[k]];
+        ar = fma(a.x, b.x, fma(-a.y, b.y, ar));
+        ai = fma(a.x, b.y, fma(a.y, b.x, ai));
+      }
+    } else {  // signed columns: entries +-1 (times off below), diagonal apart
+      for (int64_t k = rp[row] + lane; k < rp[row + 1]; k += 32) {
+        const uint32_t e = (uint32_t)ci[k];
+        const V2 b = x[e & 0x7FFFFFFFu];
+        if (e >> 31) {
+          ar -= b.x;
+          ai -= b.y;
+        } else {
+          ar += b.x;
+          ai += b.y;
+        }
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -328,6 +343,11 @@ k_csr_apply(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict
     }
     if (lane == 0) {
       const V2 xv = x[row];
+      if (!val) {
+        const T d = (T)diag[row];
+        ar = fma(off, ar, d * xv.x);
+        ai = fma(off, ai, d * xv.y);
+      }
       V2 out;
       out.x = scale * (ar - shift * xv.x);
       out.y = scale * (ai - shift * xv.y);
@@ -362,8 +382,8 @@ static void csr_apply_t(const OpView& v, const void* x, void* y, double scale, d
   using V2 = typename C2<T>::type;
   const V2* val = sizeof(T) == 8 ? (const V2*)v.csr_val : (const V2*)v.csr_val_f;
   k_csr_apply<T, DOTS><<<csr_grid(v.dim), kCsrThreads, 0, st>>>(
-      v.dim, v.csr_row, v.csr_col, val, (const V2*)x, (V2*)y, (T)scale, (T)shift, (T)beta,
-      (const V2*)z, partials);
+      v.dim, v.csr_row, v.csr_col, val, v.csr_diag, (T)v.csr_off, (const V2*)x, (V2*)y,
+      (T)scale, (T)shift, (T)beta, (const V2*)z, partials);
   MB_CUDA(cudaGetLastError());
 }
 
@@ -763,6 +783,92 @@ __device__ __forceinline__ double diag_value(const OpView& v, int64_t ru, int64_
 // Row of the reference-order CSR for tensor state i: hops from both spin
 // tables (value -t * weight), plus the diagonal unless |d| < 1000*eps (the
 // reference drops such coefficients, expression_base.h:79-97).
+// ---------------------------------------------------------------------------
+// Momentum-sector Hamiltonian (HubbardModelMomentum on one total momentum,
+// src/algebra/fermion/model/hubbard_model_momentum.h:19-180):
+//   H = sum_{k,s} eps(k) n_{k,s} + (U/N) sum_q rho_{q,up} rho_{-q,down},
+//   rho_{q,s} = sum_k c+_{k+q,s} c_{k,s}
+// (the reference's term c+_{k1+q,up} c+_{k2-q,dn} c_{k2,dn} c_{k1,up} equals
+// (c+_{k1+q,up} c_{k1,up})(c+_{k2-q,dn} c_{k2,dn}) with sign +1).  Per row:
+// diagonal = sum of eps over the occupied orbitals + (U/N) N_up N_down
+// (the q = 0 terms), dropped below 1000 eps as the reference's expression
+// does; off-diagonal = (U/N) * hop sign (up) * hop sign (down) for every
+// q != 0, up electron k1 -> k1+q and down electron k2 -> k2-q into empty
+// orbitals.  A column is the row of (up', down') in the sector: its
+// full-sector reference rank, then a binary search in the sector's ranks.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int64_t mom_find(const MomTables& m, const Binom& b, uint32_t up,
+                                            uint32_t dn) {
+  const int64_t r = reference_rank(b, up, dn, m.L);
+  int64_t lo = 0, hi = m.n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (m.full[mid] < r) lo = mid + 1;
+    else hi = mid;
+  }
+  return (lo < m.n && m.full[lo] == r) ? lo : -1;
+}
+
+__device__ __forceinline__ uint32_t between_bits(int a, int b) {
+  const int lo = min(a, b), hi = max(a, b);
+  return ((1u << hi) - 1u) & ~((2u << lo) - 1u);
+}
+
+template <bool FILL>
+__global__ void k_mom_rows(MomTables m, int32_t* __restrict__ cnt, double* __restrict__ diag,
+                           const int64_t* __restrict__ row_ptr, int32_t* __restrict__ col) {
+  __shared__ Binom sb;
+  for (int i = threadIdx.x; i < (int)(sizeof(Binom) / sizeof(int64_t)); i += blockDim.x)
+    (&sb.c[0][0])[i] = (&c_binom.c[0][0])[i];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t up = m.up[i], dn = m.dn[i];
+    if (!FILL) {
+      double d = 0.0;
+      for (uint32_t b = up; b; b &= b - 1) d += m.eps[__ffs(b) - 1];
+      for (uint32_t b = dn; b; b &= b - 1) d += m.eps[__ffs(b) - 1];
+      if (m.u_over_n != 0.0) d += m.u_over_n * (double)(m.n_up * m.n_down);
+      diag[i] = (d * d < kTol * kTol) ? 0.0 : d;
+    }
+    int c = 0;
+    int64_t out = FILL ? row_ptr[i] : 0;
+    if (m.u_over_n != 0.0) {
+      for (int q = 1; q < m.L; ++q) {
+        for (uint32_t bu = up; bu; bu &= bu - 1) {
+          const int k1 = __ffs(bu) - 1, a = m.kadd[k1 * m.L + q];
+          if ((up >> a) & 1u) continue;
+          const uint32_t up2 = up ^ (1u << k1) ^ (1u << a);
+          const uint32_t su = __popc(up & between_bits(k1, a)) & 1u;
+          for (uint32_t bd = dn; bd; bd &= bd - 1) {
+            const int k2 = __ffs(bd) - 1, b = m.ksub[k2 * m.L + q];
+            if ((dn >> b) & 1u) continue;
+            const uint32_t dn2 = dn ^ (1u << k2) ^ (1u << b);
+            const int64_t j = mom_find(m, sb, up2, dn2);
+            if (j < 0) continue;  // not in the sector (cannot happen: momentum is conserved)
+            if (FILL) {
+              const uint32_t sd = __popc(dn & between_bits(k2, b)) & 1u;
+              col[out++] = (int32_t)((uint32_t)j | ((su ^ sd) << 31));
+            }
+            ++c;
+          }
+        }
+      }
+    }
+    if (!FILL) cnt[i] = c;
+  }
+}
+
+void launch_mom_count(const MomTables& m, int32_t* count, double* diag, cudaStream_t st) {
+  k_mom_rows<false><<<blas_grid(m.n), kBlasThreads, 0, st>>>(m, count, diag, nullptr, nullptr);
+  MB_CUDA(cudaGetLastError());
+}
+
+void launch_mom_fill(const MomTables& m, const int64_t* row_ptr, int32_t* col, cudaStream_t st) {
+  k_mom_rows<true><<<blas_grid(m.n), kBlasThreads, 0, st>>>(m, nullptr, nullptr, row_ptr, col);
+  MB_CUDA(cudaGetLastError());
+}
+
 __global__ void k_csr_count(OpView v, const int32_t* __restrict__ perm, int32_t* __restrict__ cnt) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < v.dim;
        i += (int64_t)gridDim.x * blockDim.x) {

@@ -171,6 +171,69 @@ static void build_op(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m) {
   if (op->precision == MB_PREC_Q64) q_op_prepare(op, m, tu, td);
 }
 
+// A momentum-sector operator: the sector's Hamiltonian built on the device
+// in signed-column form (row_ptr, column | sign << 31, diagonal, U/N); its
+// rows are the sector's reference order.
+struct MomBuild {
+  int64_t n = 0, nnz = 0;
+  std::vector<int64_t> row_ptr;
+  int32_t* col = nullptr;  // device
+  double* diag = nullptr;  // device
+};
+
+static void build_momentum(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m, MomBuild& out) {
+  MB_REQUIRE(b->momentum() && m->momentum, MB_ERR_INVALID_ARG,
+             "a momentum-sector basis needs the momentum-space model (and the reverse)");
+  MB_REQUIRE(b->kdims == m->dims, MB_ERR_DIM_MISMATCH, "basis and model lattices differ");
+  const int L = b->L;
+  std::vector<uint8_t> kadd((size_t)L * L), ksub((size_t)L * L);
+  for (int k = 0; k < L; ++k)
+    for (int q = 0; q < L; ++q) {
+      kadd[(size_t)k * L + q] = (uint8_t)momentum_add(k, q, +1, b->kdims);
+      ksub[(size_t)k * L + q] = (uint8_t)momentum_add(k, q, -1, b->kdims);
+    }
+  MomTables t{};
+  t.n = b->dim;
+  t.L = L;
+  t.n_up = b->n_up;
+  t.n_down = b->n_down;
+  t.up = upload(op, b->kup.empty() ? std::vector<uint32_t>{0u} : b->kup);
+  t.dn = upload(op, b->kdown.empty() ? std::vector<uint32_t>{0u} : b->kdown);
+  t.full = upload(op, b->kfull.empty() ? std::vector<int64_t>{0} : b->kfull);
+  t.eps = upload(op, m->eps);
+  t.kadd = upload(op, kadd);
+  t.ksub = upload(op, ksub);
+  t.u_over_n = m->u_over_n;
+  ensure_binomials();
+  cudaStream_t st = 0;
+  out.n = b->dim;
+  out.row_ptr.assign((size_t)out.n + 1, 0);
+  if (out.n == 0) return;
+  DevBuf cnt(sizeof(int32_t) * (size_t)out.n);
+  void* dg = nullptr;
+  MB_CUDA(cudaMalloc(&dg, sizeof(double) * (size_t)out.n));
+  op->allocations.push_back(dg);
+  out.diag = (double*)dg;
+  launch_mom_count(t, (int32_t*)cnt.p, out.diag, st);
+  std::vector<int32_t> hc((size_t)out.n);
+  MB_CUDA(cudaMemcpy(hc.data(), cnt.p, sizeof(int32_t) * (size_t)out.n, cudaMemcpyDeviceToHost));
+  for (int64_t i = 0; i < out.n; ++i) out.row_ptr[(size_t)i + 1] = out.row_ptr[(size_t)i] + hc[(size_t)i];
+  out.nnz = out.row_ptr[(size_t)out.n];
+  const int64_t* drp = upload(op, out.row_ptr);
+  void* dc = nullptr;
+  MB_CUDA(cudaMalloc(&dc, sizeof(int32_t) * (size_t)std::max<int64_t>(out.nnz, 1)));
+  op->allocations.push_back(dc);
+  out.col = (int32_t*)dc;
+  launch_mom_fill(t, drp, out.col, st);
+  MB_CUDA(cudaStreamSynchronize(st));
+  OpView& v = op->view;
+  v.csr_row = drp;
+  v.csr_col = out.col;
+  v.csr_val = nullptr;
+  v.csr_diag = out.diag;
+  v.csr_off = m->u_over_n;
+}
+
 static mb_op_s::Scratch& scratch_for(mb_op_s* op, cudaStream_t st, int nvec) {
   std::lock_guard<std::mutex> lk(op->mu);
   auto& s = op->scratch[st];
@@ -652,7 +715,28 @@ int mb_op_create(mb_basis_t basis, mb_model_t model, int precision, mb_op_t* out
     auto op = std::make_unique<mb_op_s>();
     op->precision = precision;
     try {
-      build_op(op.get(), basis, model);
+      if (basis->momentum() || model->momentum) {
+        MB_REQUIRE(precision != MB_PREC_Q64, MB_ERR_INVALID_ARG,
+                   "momentum-sector operators take MB_PREC_F64 or MB_PREC_F32");
+        MB_CUDA(cudaGetDevice(&op->device));
+        op->L = basis->L;
+        op->n_up = basis->n_up;
+        op->n_down = basis->n_down;
+        op->Du = basis->dim;
+        op->Dd = 1;
+        op->dim = basis->dim;
+        op->t = model->t;
+        op->u = model->u;
+        op->natural_order = true;
+        op->view.Du = basis->dim;
+        op->view.Dd = 1;
+        op->view.dim = basis->dim;
+        op->view.L = basis->L;
+        MomBuild mbld;
+        build_momentum(op.get(), basis, model, mbld);
+      } else {
+        build_op(op.get(), basis, model);
+      }
     } catch (...) {
       for (void* p : op->allocations) cudaFree(p);
       throw;
@@ -813,6 +897,48 @@ int mb_compute_matrix_elements_csr(mb_basis_t basis, mb_model_t model, int64_t* 
         for (void* p : o.allocations) cudaFree(p);
       }
     } cleanup{tmp};
+    if (basis->momentum() || model->momentum) {
+      MomBuild mb;
+      build_momentum(&tmp, basis, model, mb);
+      const int64_t n = mb.n;
+      std::vector<int32_t> hcol((size_t)std::max<int64_t>(mb.nnz, 1));
+      std::vector<double> hdiag((size_t)std::max<int64_t>(n, 1));
+      if (mb.nnz) MB_CUDA(cudaMemcpy(hcol.data(), mb.col, sizeof(int32_t) * (size_t)mb.nnz, cudaMemcpyDeviceToHost));
+      if (n) MB_CUDA(cudaMemcpy(hdiag.data(), mb.diag, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost));
+      std::vector<int64_t> rp((size_t)n + 1, 0);
+      for (int64_t i = 0; i < n; ++i)
+        rp[(size_t)i + 1] = rp[(size_t)i] + (mb.row_ptr[(size_t)i + 1] - mb.row_ptr[(size_t)i]) +
+                            (hdiag[(size_t)i] != 0.0 ? 1 : 0);
+      const int64_t total = rp[(size_t)n];
+      if (!col_idx) {
+        *nnz = total;
+        if (row_ptr) std::memcpy(row_ptr, rp.data(), sizeof(int64_t) * rp.size());
+        return;
+      }
+      MB_REQUIRE(*nnz >= total, MB_ERR_CAPACITY, "nnz capacity smaller than the matrix");
+      MB_REQUIRE(row_ptr && values, MB_ERR_INVALID_ARG, "NULL row_ptr or values");
+      const double off = tmp.view.csr_off;
+#pragma omp parallel for schedule(dynamic, 64)
+      for (int64_t i = 0; i < n; ++i) {
+        std::vector<std::pair<int64_t, double>> row;
+        for (int64_t k = mb.row_ptr[(size_t)i]; k < mb.row_ptr[(size_t)i + 1]; ++k) {
+          const uint32_t e = (uint32_t)hcol[(size_t)k];
+          row.push_back({(int64_t)(e & 0x7FFFFFFFu), (e >> 31) ? -off : off});
+        }
+        if (hdiag[(size_t)i] != 0.0) row.push_back({i, hdiag[(size_t)i]});
+        std::sort(row.begin(), row.end());
+        int64_t o = rp[(size_t)i];
+        for (const auto& [c, v] : row) {
+          col_idx[o] = c;
+          values[2 * o] = v;
+          values[2 * o + 1] = 0.0;
+          ++o;
+        }
+      }
+      std::memcpy(row_ptr, rp.data(), sizeof(int64_t) * rp.size());
+      *nnz = total;
+      return;
+    }
     build_op(&tmp, basis, model);
     ensure_perm(&tmp);
     const int64_t dim = tmp.dim;

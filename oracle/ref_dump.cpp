@@ -3,6 +3,11 @@
 //
 //   ref_dump <dims> <t> <U> <particles> <spin_projection> <out.bin>
 //     dims: "8" (1D chain), "4x4" (2D), "2x2x2" (3D), all periodic.
+//   ref_dump --momentum <dims> <t> <U> <particles> <spin_projection> <K> <out.bin>
+//     the momentum-space model on one total-momentum sector K ("1", "1x0"):
+//     FermionBasis::with_fixed_particle_number_spin_momentum
+//     (src/algebra/basis.cpp:128-185,304-356) and HubbardModelMomentum
+//     (src/algebra/fermion/model/hubbard_model_momentum.h:19-180).
 //
 // Calls, unchanged, the reference's
 //   FermionBasis::with_fixed_particle_number_and_spin   (src/algebra/basis.cpp:91-126)
@@ -25,6 +30,8 @@
 #include "algebra/fermion/basis.h"
 #include "algebra/fermion/expression.h"
 #include "algebra/fermion/model/hubbard_model.h"
+#include "algebra/fermion/model/hubbard_model_momentum.h"
+#include "utils/index.h"
 #include "algebra/matrix_elements.h"
 
 namespace {
@@ -53,35 +60,47 @@ std::vector<size_t> parse_dims(const std::string& s) {
 }  // namespace
 
 int main(int argc, char** argv) {
-  if (argc != 7) {
-    std::fprintf(stderr, "usage: ref_dump <dims> <t> <U> <particles> <spin_projection> <out>\n");
+  const bool momentum = argc == 9 && std::string(argv[1]) == "--momentum";
+  if (argc != 7 && !momentum) {
+    std::fprintf(stderr,
+                 "usage: ref_dump <dims> <t> <U> <particles> <spin_projection> <out>\n"
+                 "       ref_dump --momentum <dims> <t> <U> <particles> <spin_projection> <K> <out>\n");
     return 2;
   }
-  const std::vector<size_t> dims = parse_dims(argv[1]);
-  const double t = std::atof(argv[2]);
-  const double u = std::atof(argv[3]);
-  const size_t particles = std::stoul(argv[4]);
-  const int sz = std::atoi(argv[5]);
+  char** a = momentum ? argv + 1 : argv;
+  const std::vector<size_t> dims = parse_dims(a[1]);
+  const double t = std::atof(a[2]);
+  const double u = std::atof(a[3]);
+  const size_t particles = std::stoul(a[4]);
+  const int sz = std::atoi(a[5]);
+  const char* out_path = momentum ? argv[8] : argv[6];
 
   size_t orbitals = 1;
   for (size_t d : dims) orbitals *= d;
 
   FermionExpression h;
-  if (dims.size() == 1) {
-    h = HubbardModel(t, u, dims[0]).hamiltonian();
-  } else if (dims.size() == 2) {
-    h = HubbardModel2D(t, u, dims[0], dims[1]).hamiltonian();
-  } else if (dims.size() == 3) {
-    h = HubbardModel3D(t, u, dims[0], dims[1], dims[2]).hamiltonian();
+  FermionBasis basis;
+  if (momentum) {
+    const std::vector<size_t> k = parse_dims(argv[7]);
+    h = HubbardModelMomentum(t, u, dims).hamiltonian();
+    basis = FermionBasis::with_fixed_particle_number_spin_momentum(orbitals, particles, sz,
+                                                                   Index(dims), k);
   } else {
-    std::fprintf(stderr, "ref_dump: 1 to 3 dimensions\n");
-    return 2;
+    if (dims.size() == 1) {
+      h = HubbardModel(t, u, dims[0]).hamiltonian();
+    } else if (dims.size() == 2) {
+      h = HubbardModel2D(t, u, dims[0], dims[1]).hamiltonian();
+    } else if (dims.size() == 3) {
+      h = HubbardModel3D(t, u, dims[0], dims[1], dims[2]).hamiltonian();
+    } else {
+      std::fprintf(stderr, "ref_dump: 1 to 3 dimensions\n");
+      return 2;
+    }
+    basis = FermionBasis::with_fixed_particle_number_and_spin(orbitals, particles, sz);
   }
-
-  FermionBasis basis = FermionBasis::with_fixed_particle_number_and_spin(orbitals, particles, sz);
   CooMatrix m = compute_matrix_elements<CooMatrix>(basis, h);
 
-  FILE* f = std::fopen(argv[6], "wb");
+  FILE* f = std::fopen(out_path, "wb");
   if (!f) return 3;
   std::fwrite("MBREF001", 1, 8, f);
   const uint64_t n_terms = h.size();

@@ -17,10 +17,15 @@ def pytest_configure(config):
 
 
 def golden_cases():
-    """The Hubbard sectors dumped from the reference (cereal_* fixtures are
-    cache-format pins, not sectors)."""
+    """The real-space Hubbard sectors dumped from the reference (cereal_*
+    fixtures are cache-format pins, mom_* momentum-space sectors)."""
     return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(f).startswith("cereal_"))
+                  if not os.path.basename(f).startswith(("cereal_", "mom_")))
+
+
+def momentum_cases():
+    """The momentum-space model on total-momentum sectors, from the reference."""
+    return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "mom_*.npz")))
 
 
 def load_golden(name):

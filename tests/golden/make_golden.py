@@ -1,5 +1,8 @@
 """Regenerates the golden Hubbard fixtures in tests/golden/ from the reference.
 
+The real-space sectors (CASES) and, as mom_*.npz, the momentum-space model on
+total-momentum sectors (MOMENTUM_CASES; their npz adds the K vector).
+
 Runs oracle/_ref/ref_dump (built by oracle/build_ref.sh from the reference
 sources: its basis enumeration, HubbardModel{,2D,3D} and
 compute_matrix_elements) for each case below and stores, per case, the
@@ -52,12 +55,31 @@ CASES = [
 
 TERM_COUNT_CASES = [("1", 2), ("2x2", 2), ("2x2x2", 3)]
 
+# Momentum-space model on one total-momentum sector (ref_dump --momentum):
+# (name, dims, t, U, particles, spin_projection, K)
+MOMENTUM_CASES = [
+    ("mom_chain4_n2_k0", "4", 1.0, 2.0, 2, 0, "0"),
+    ("mom_chain4_n4_k1", "4", 1.0, 4.0, 4, 0, "1"),
+    ("mom_chain4_n4_u0_k2", "4", 1.0, 0.0, 4, 0, "2"),    # U = 0: diagonal only
+    ("mom_chain6_n4_k2", "6", 1.0, 4.0, 4, 0, "2"),
+    ("mom_chain6_n4_t0_k0", "6", 0.0, 4.0, 4, 0, "0"),    # t = 0: no kinetic terms
+    ("mom_chain6_n3_sz1_k3", "6", 0.7, 3.0, 3, 1, "3"),
+    ("mom_chain8_n4_k0", "8", 1.0, 4.0, 4, 0, "0"),
+    ("mom_sq2x2_n4_k10", "2x2", 1.0, 2.0, 4, 0, "1x0"),
+    ("mom_sq3x3_n4_k11", "3x3", 1.0, 8.0, 4, 0, "1x1"),
+    ("mom_rect2x3_n4_k01", "2x3", 0.5, 6.0, 4, 0, "0x1"),
+    ("mom_cube2x2x2_n4_k101", "2x2x2", 1.0, 2.0, 4, 0, "1x0x1"),
+]
 
-def dump(dims, t, U, n, sz):
+
+def dump(dims, t, U, n, sz, momentum=None):
     with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
         path = f.name
     try:
-        subprocess.run([REF_DUMP, dims, repr(t), repr(U), str(n), str(sz), path], check=True)
+        args = [dims, repr(t), repr(U), str(n), str(sz)]
+        if momentum is not None:
+            args = ["--momentum", *args, momentum]
+        subprocess.run([REF_DUMP, *args, path], check=True)
         b = open(path, "rb").read()
     finally:
         os.unlink(path)
@@ -84,6 +106,16 @@ def main():
                             t=t, U=U, particles=n, spin_projection=sz, n_terms=n_terms,
                             up=up, down=dn, row=rec["r"].astype(np.int32),
                             col=rec["c"].astype(np.int32), val=rec["re"].copy())
+        print(f"{name}: dim={len(up)} nnz={len(rec)} terms={n_terms}")
+    for name, dims, t, U, n, sz, k in MOMENTUM_CASES:
+        n_terms, up, dn, rec = dump(dims, t, U, n, sz, k)
+        dvec = [int(x) for x in dims.split("x")]
+        kvec = [int(x) for x in k.split("x")]
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), dims=np.array(dvec, np.int32),
+                            t=t, U=U, particles=n, spin_projection=sz,
+                            momentum=np.array(kvec, np.int32), n_terms=n_terms, up=up, down=dn,
+                            row=rec["r"].astype(np.int32), col=rec["c"].astype(np.int32),
+                            val=rec["re"].copy())
         print(f"{name}: dim={len(up)} nnz={len(rec)} terms={n_terms}")
 
 

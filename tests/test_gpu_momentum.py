@@ -1,0 +1,108 @@
+"""Momentum-space Hubbard sectors on the GPU: the sector's H built on the
+device (compute_matrix_elements of HubbardModelMomentum on
+with_fixed_particle_number_spin_momentum) against the reference's own
+matrices (tests/golden/mom_*.npz), and the sector operators through the
+Krylov drivers.
+
+Tolerances: structure and off-diagonal values (+-U/N) bit-exact; diagonal
+values <= 1e-14 |H|max (the reference sums the same terms in its own order);
+apply <= 1e-13 ||y|| (FP64), <= 2e-6 ||y|| (FP32); E0 <= 1e-10 |E0|.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import load_golden, momentum_cases
+
+pytestmark = pytest.mark.gpu
+
+
+def make(mb, g, prec=0):
+    dims = [int(d) for d in g["dims"]]
+    basis = mb.FermionBasis.with_fixed_particle_number_spin_momentum(
+        int(np.prod(dims)), int(g["particles"]), int(g["spin_projection"]), dims,
+        [int(k) for k in g["momentum"]])
+    model = mb.HubbardModelMomentum(float(g["t"]), float(g["U"]), dims)
+    return basis, model
+
+
+def ref_csr(g):
+    import scipy.sparse as sp
+    n = len(g["up"])
+    return sp.csr_matrix((g["val"], (g["row"], g["col"])), shape=(n, n))
+
+
+@pytest.mark.parametrize("name", momentum_cases())
+def test_momentum_matrix_elements_match_reference(mb, cuda, name):
+    g = load_golden(name)
+    basis, model = make(mb, g)
+    H = mb.compute_matrix_elements(basis, model)
+    rows = np.repeat(np.arange(H.dim), np.diff(H.row_ptr))
+    assert H.nnz == len(g["row"])
+    assert np.array_equal(rows, g["row"]) and np.array_equal(H.col_idx, g["col"])
+    off = rows != H.col_idx
+    assert np.array_equal(H.values.real[off], g["val"][off])
+    scale = max(np.abs(g["val"]).max(), 1.0)
+    assert np.max(np.abs(H.values.real[~off] - g["val"][~off]), initial=0.0) <= 1e-14 * scale
+    assert not H.values.imag.any()
+
+
+@pytest.mark.parametrize("name", momentum_cases())
+@pytest.mark.parametrize("prec,tol", [(0, 1e-13), (1, 2e-6)])
+def test_momentum_operator_apply(mb, cuda, name, prec, tol):
+    torch = cuda
+    g = load_golden(name)
+    basis, model = make(mb, g)
+    op = mb.GpuHubbardOperator(basis, model, prec)
+    n = op.dimension()
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)
+    dt = torch.complex64 if prec else torch.complex128
+    y = op.apply(torch.tensor(x, dtype=dt, device="cuda")).cpu().numpy()
+    ref = ref_csr(g) @ x
+    assert np.linalg.norm(y - ref) <= tol * max(np.linalg.norm(ref), 1e-300)
+
+
+def test_momentum_sectors_reproduce_the_real_space_spectrum(mb, cuda):
+    """1D L=6, 2+2: the union over K of the sector spectra is the spectrum
+    of the real-space Hamiltonian (the Fourier transform is unitary)."""
+    dims, n = [6], 4
+    E_real = np.linalg.eigvalsh(oracle.hubbard_csc(dims, 1.0, 3.0, 2, 2).to_dense())
+    model = mb.HubbardModelMomentum(1.0, 3.0, dims)
+    parts = []
+    for k in range(6):
+        b = mb.FermionBasis.with_fixed_particle_number_spin_momentum(6, n, 0, dims, [k])
+        parts.append(np.linalg.eigvalsh(mb.compute_matrix_elements(b, model).to_scipy().toarray()))
+    E_mom = np.sort(np.concatenate(parts))
+    assert len(E_mom) == len(E_real)
+    assert np.max(np.abs(E_mom - E_real)) <= 1e-10 * np.abs(E_real).max()
+
+
+def test_momentum_ground_state_matches_real_space(mb, cuda):
+    """3x3, 3+3 (dim 7056 real space): the lowest sector ground state over
+    all nine momenta equals the real-space ground state (Lanczos on both)."""
+    dims = [3, 3]
+    real = mb.GpuHubbardOperator(mb.FermionBasis.with_fixed_particle_number_and_spin(9, 6, 0),
+                                 mb.HubbardModel2D(1.0, 4.0, 3, 3))
+    e_real = mb.find_min_eigenpair(real, 200, reorth=True, want_vector=False).value
+    model = mb.HubbardModelMomentum(1.0, 4.0, dims)
+    best = None
+    for kx in range(3):
+        for ky in range(3):
+            b = mb.FermionBasis.with_fixed_particle_number_spin_momentum(9, 6, 0, dims, (kx, ky))
+            op = mb.GpuHubbardOperator(b, model)
+            e = mb.find_min_eigenpair(op, min(200, op.dimension()), reorth=True,
+                                      want_vector=False).value
+            best = e if best is None else min(best, e)
+    assert abs(best - e_real) <= 1e-10 * abs(e_real)
+
+
+def test_momentum_operator_rejects_q64_and_mixed_models(mb, cuda):
+    b = mb.FermionBasis.with_fixed_particle_number_spin_momentum(4, 2, 0, [4], [0])
+    with pytest.raises(mb.MbError):
+        mb.GpuHubbardOperator(b, mb.HubbardModelMomentum(1.0, 2.0, [4]), mb.PREC_Q64)
+    with pytest.raises(mb.MbError):
+        mb.GpuHubbardOperator(b, mb.HubbardModel(1.0, 2.0, 4))
+    with pytest.raises(mb.MbError):
+        mb.compute_matrix_elements(mb.FermionBasis.with_fixed_particle_number_and_spin(4, 2, 0),
+                                   mb.HubbardModelMomentum(1.0, 2.0, [4]))
