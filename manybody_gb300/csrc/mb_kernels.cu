@@ -304,6 +304,14 @@ static void apply_dots(const OpView& v, const void* x, void* y, double scale, do
 // ---------------------------------------------------------------------------
 constexpr int kCsrThreads = 256;
 
+// v with its sign flipped when bit 31 of e is set
+__device__ __forceinline__ double flip_sign(double v, uint32_t e) {
+  return __longlong_as_double(__double_as_longlong(v) ^ ((long long)(e >> 31) << 63));
+}
+__device__ __forceinline__ float flip_sign(float v, uint32_t e) {
+  return __int_as_float(__float_as_int(v) ^ (int)(e & 0x80000000u));
+}
+
 template <typename T, int DOTS>
 __global__ void __launch_bounds__(kCsrThreads)
 k_csr_apply(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
@@ -324,17 +332,31 @@ k_csr_apply(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict
         ai = fma(a.x, b.y, fma(a.y, b.x, ai));
       }
     } else {  // signed columns: entries +-1 (times off below), diagonal apart
-      for (int64_t k = rp[row] + lane; k < rp[row + 1]; k += 32) {
-        const uint32_t e = (uint32_t)ci[k];
-        const V2 b = x[e & 0x7FFFFFFFu];
-        if (e >> 31) {
-          ar -= b.x;
-          ai -= b.y;
-        } else {
-          ar += b.x;
-          ai += b.y;
-        }
+      // the sign goes onto the sign bit, so no lane branches per entry; for
+      // complex64 two independent sums (even / odd strides) halve the add
+      // chains (measured at 4x4 6+6, K=0: 3.19 -> 2.81 ms), for complex128
+      // one (9.1 ms, against 12.9 ms with two)
+      T br = T(0), bi = T(0);
+      const int64_t k1 = rp[row + 1];
+      int64_t k = rp[row] + lane;
+#pragma unroll 4
+      for (; sizeof(T) == 4 && k + 32 < k1; k += 64) {
+        const uint32_t e0 = (uint32_t)__ldg(&ci[k]), e1 = (uint32_t)__ldg(&ci[k + 32]);
+        const V2 b0 = __ldg(&x[e0 & 0x7FFFFFFFu]), b1 = __ldg(&x[e1 & 0x7FFFFFFFu]);
+        ar += flip_sign(b0.x, e0);
+        ai += flip_sign(b0.y, e0);
+        br += flip_sign(b1.x, e1);
+        bi += flip_sign(b1.y, e1);
       }
+#pragma unroll 4
+      for (; k < k1; k += 32) {
+        const uint32_t e0 = (uint32_t)__ldg(&ci[k]);
+        const V2 b0 = __ldg(&x[e0 & 0x7FFFFFFFu]);
+        ar += flip_sign(b0.x, e0);
+        ai += flip_sign(b0.y, e0);
+      }
+      ar += br;
+      ai += bi;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
