@@ -267,7 +267,8 @@ def run_gpu(args):
         torch.cuda.empty_cache()
 
     if not args.no_extras:
-        for name, fn in (("cfg2_solve", run_cfg2_extra), ("batch", run_batch_extra),
+        for name, fn in (("cfg2_solve", run_cfg2_extra), ("momentum", run_momentum_extra),
+                         ("batch", run_batch_extra),
                          ("precision", run_precision_extra), ("serve", run_serve_extra)):
             try:
                 extras[name] = fn(mb, torch)
@@ -425,6 +426,40 @@ def run_cfg2_extra(mb, torch, n_probes=2, n_moments=1024):
                 "projected_seconds_16_probes": round(16 * t_kpm / n_probes, 2),
                 "mu0": float(mu[0]), "mu_1_to_4": [float(v) for v in mu[1:5]]},
     }
+
+
+def run_momentum_extra(mb, torch):
+    """4x4, 6+6, U=8 on the total-momentum sector K = (0, 0) (the sector of the
+    ground state): the sector basis and its H built on the GPU, the apply in
+    FP64 and FP32, the ground state by plain Lanczos to Ritz stability 1e-12."""
+    dims = (4, 4)
+    model = mb.HubbardModelMomentum(1.0, 8.0, dims)
+    t0 = time.perf_counter()
+    basis = mb.FermionBasis.with_fixed_particle_number_spin_momentum(16, 12, 0, dims, (0, 0))
+    t_basis = time.perf_counter() - t0
+    out = {"workload": "2D 4x4, U=8, N_up=N_down=6, total momentum (0,0)", "dim": basis.size(),
+           "basis_seconds": round(t_basis, 3)}
+    stream = torch.cuda.current_stream()
+    for name, prec in (("f64", mb.PREC_F64), ("f32", mb.PREC_F32)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        op = mb.GpuHubbardOperator(basis, model, prec)
+        torch.cuda.synchronize()
+        t_build = time.perf_counter() - t0
+        x = op.seed_vector(0)
+        y = op.empty()
+        _, per = time_loop(torch, stream, lambda: op.apply(x, out=y, stream=stream.cuda_stream), 10, 3)
+        out[f"{name}_build_seconds"] = round(t_build, 3)
+        out[f"{name}_apply_ms"] = round(statistics.mean(per), 3)
+        if prec == mb.PREC_F64:
+            t0 = time.perf_counter()
+            r = mb.find_min_eigenpair(op, 300, x, conv_tol=1e-12, check_every=10,
+                                      want_vector=False)
+            out.update({"e0": r.value, "lanczos_steps": r.steps,
+                        "e0_seconds": round(time.perf_counter() - t0, 3)})
+        del op, x, y
+        torch.cuda.empty_cache()
+    return out
 
 
 def run_precision_extra(mb, torch):

@@ -295,6 +295,39 @@ int mb_q64_to_f64(mb_op_t op, const void* xq_dev, int exponent, int order, void*
 int mb_op_apply_q64(mb_op_t op, const void* xq_dev, int x_exponent, void* yq_dev,
                     int* y_exponent, void* stream);
 
+/* ---- operators between momentum sectors; the current correlator ---------- *
+ * The current operator J_d(Q) = sum_{k,s} v_d(k) c+_{k+Q,s} c_{k,s},
+ * v_d(k) = 2t (2 pi / L_d) sin(2 pi k_d / L_d)
+ * (HubbardModelMomentum::current, src/algebra/fermion/model/
+ * hubbard_model_momentum.h:38-90), maps the sector of momentum K to K+Q. */
+int mb_current_create(const int64_t* dims, int ndim, double t, const int64_t* transfer,
+                      int direction, mb_model_t* out);
+/* compute_rectangular_matrix_elements (src/algebra/matrix_elements.h:107-167):
+ * rows in row_basis (sector K+Q), columns in col_basis (sector K), built on
+ * the GPU; two calls as mb_compute_matrix_elements_csr. */
+int mb_compute_rectangular_matrix_elements_csr(mb_basis_t row_basis, mb_basis_t col_basis,
+                                               mb_model_t model, int64_t* nnz, int64_t* row_ptr,
+                                               int64_t* col_idx, double* values);
+/* J and J+ on the device (MB_PREC_F64 / MB_PREC_F32 vectors, reference
+ * order): y = J x (x in sector K, y in K+Q), or with adjoint = 1 y = J+ x. */
+typedef struct mb_rect_op_s* mb_rect_op_t;
+int mb_rect_op_create(mb_basis_t row_basis, mb_basis_t col_basis, mb_model_t model, int precision,
+                      mb_rect_op_t* out);
+int mb_rect_op_destroy(mb_rect_op_t op);
+int mb_rect_op_dims(mb_rect_op_t op, int64_t* n_rows, int64_t* n_cols);
+int mb_rect_op_apply(mb_rect_op_t op, const void* x_dev, void* y_dev, int adjoint, void* stream);
+/* The stochastic current-current correlator of the reference's optical-
+ * conductivity driver (examples/hubbard_momentum_optical_conductivity.cpp:
+ * 340-410), on the device: per sample a probe |v> in sector K (random phases,
+ * Philox stream 1 + s; the example draws complex Gaussians), |v_b> =
+ * exp(-beta H_K / 2)|v>, Z = <v_b|v_b>, phi1 = v_b, phi2 = J v_b, then for
+ * each step C[i] += <phi1| J+ |phi2> / Z, phi1 <- exp(-i H_K dt) phi1,
+ * phi2 <- exp(-i H_{K+Q} dt) phi2 (Krylov, krylov_steps); C averaged over the
+ * samples.  correlator: 2 * steps doubles (re, im). */
+int mb_current_correlator(mb_op_t op_k, mb_op_t op_kq, mb_rect_op_t current, int64_t n_samples,
+                          uint64_t seed, double beta, double dt, int64_t steps,
+                          int64_t krylov_steps, double* correlator);
+
 /* ---- batched / served solves ------------------------------------------------ *
  * An engine advances many independent sectors of uneven size together: one
  * Lanczos step of every active request per engine step, complex64 vectors with

@@ -96,6 +96,14 @@ SIGNATURES = {
     "mb_op_create": (C.c_int, [_vp, _vp, C.c_int, C.POINTER(_vp)]),
     "mb_op_create_csr": (C.c_int, [_i64, _i64p, _i64p, _dp, C.c_int, C.POINTER(_vp)]),
     "mb_basis_create_momentum": (C.c_int, [_i64p, C.c_int, _i64, C.c_int, _i64p, C.POINTER(_vp)]),
+    "mb_current_create": (C.c_int, [_i64p, C.c_int, C.c_double, _i64p, C.c_int, C.POINTER(_vp)]),
+    "mb_compute_rectangular_matrix_elements_csr": (C.c_int, [_vp, _vp, _vp, _i64p, _i64p, _i64p, _dp]),
+    "mb_rect_op_create": (C.c_int, [_vp, _vp, _vp, C.c_int, C.POINTER(_vp)]),
+    "mb_rect_op_destroy": (C.c_int, [_vp]),
+    "mb_rect_op_dims": (C.c_int, [_vp, _i64p, _i64p]),
+    "mb_rect_op_apply": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
+    "mb_current_correlator": (C.c_int, [_vp, _vp, _vp, _i64, C.c_uint64, C.c_double, C.c_double,
+                                        _i64, _i64, _dp]),
     "mb_hubbard_momentum_create": (C.c_int, [_i64p, C.c_int, C.c_double, C.c_double, C.POINTER(_vp)]),
     "mb_cereal_write_csr": (C.c_int, [C.c_char_p, _i64, _i64, _i64p, _i64p, _dp]),
     "mb_cereal_read_csr": (C.c_int, [C.c_char_p, _i64p, _i64p, _i64p, _i64p, _i64p, _dp]),
@@ -353,6 +361,97 @@ class CsrMatrix:
     def to_scipy(self):
         import scipy.sparse as sp
         return sp.csr_matrix((self.values, self.col_idx, self.row_ptr), shape=(self.dim, self.cols))
+
+
+class CurrentOperator:
+    """HubbardModelMomentum::current(Q, direction)
+    (src/algebra/fermion/model/hubbard_model_momentum.h:52-90): J_d(Q), from
+    the momentum sector K to K+Q."""
+
+    def __init__(self, t: float, size, transfer, direction: int):
+        self.t, self.dims = float(t), tuple(int(d) for d in size)
+        self.transfer, self.direction = tuple(int(q) for q in transfer), int(direction)
+        d = (C.c_int64 * len(self.dims))(*self.dims)
+        q = (C.c_int64 * len(self.dims))(*self.transfer)
+        h = C.c_void_p()
+        _check(lib().mb_current_create(d, len(self.dims), self.t, q, self.direction, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.mb_model_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def term_count(self) -> int:
+        n = C.c_int64()
+        _check(lib().mb_model_term_count(self._h, C.byref(n)))
+        return n.value
+
+
+def compute_rectangular_matrix_elements(row_basis: FermionBasis, col_basis: FermionBasis,
+                                        op: CurrentOperator) -> CsrMatrix:
+    """compute_rectangular_matrix_elements (src/algebra/matrix_elements.h:107-167), on GPU."""
+    nnz = C.c_int64()
+    n = row_basis.size()
+    rp = np.zeros(n + 1, np.int64)
+    _check(lib().mb_compute_rectangular_matrix_elements_csr(row_basis.handle, col_basis.handle,
+                                                            op.handle, C.byref(nnz),
+                                                            rp.ctypes.data_as(_i64p), None, None))
+    ci = np.zeros(max(nnz.value, 1), np.int64)
+    vals = np.zeros(max(nnz.value, 1), np.complex128)
+    _check(lib().mb_compute_rectangular_matrix_elements_csr(
+        row_basis.handle, col_basis.handle, op.handle, C.byref(nnz), rp.ctypes.data_as(_i64p),
+        ci.ctypes.data_as(_i64p), vals.view(np.float64).ctypes.data_as(_dp)))
+    k = nnz.value
+    return CsrMatrix(n, rp, ci[:k], vals[:k], col_basis.size())
+
+
+class GpuCurrentOperator:
+    """J and J+ between two momentum sectors on the GPU (reference order)."""
+
+    def __init__(self, row_basis: FermionBasis, col_basis: FermionBasis, op: CurrentOperator,
+                 precision: int = PREC_F64):
+        h = C.c_void_p()
+        _check(lib().mb_rect_op_create(row_basis.handle, col_basis.handle, op.handle, precision,
+                                       C.byref(h)))
+        self._h = h
+        self.precision = precision
+        self.shape = (row_basis.size(), col_basis.size())
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.mb_rect_op_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def apply(self, x, adjoint: bool = False, out=None):
+        import torch
+        n = self.shape[1] if adjoint else self.shape[0]
+        dt = torch.complex64 if self.precision == PREC_F32 else torch.complex128
+        y = torch.empty(n, dtype=dt, device="cuda") if out is None else out
+        _check(lib().mb_rect_op_apply(self._h, _ptr(x), _ptr(y), int(adjoint),
+                                      C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        return y
+
+
+def current_correlator(op_k: GpuHubbardOperator, op_kq: GpuHubbardOperator,
+                       current: GpuCurrentOperator, n_samples: int, seed: int, beta: float,
+                       dt: float, steps: int, krylov_steps: int = 30) -> np.ndarray:
+    """The optical-conductivity driver's stochastic current-current correlator
+    (examples/hubbard_momentum_optical_conductivity.cpp:340-410), on the GPU."""
+    _sync_torch()
+    c = np.zeros(2 * steps)
+    _check(lib().mb_current_correlator(op_k.handle, op_kq.handle, current.handle, n_samples,
+                                       seed, beta, dt, steps, krylov_steps,
+                                       c.ctypes.data_as(_dp)))
+    return c[0::2] + 1j * c[1::2]
 
 
 def write_cereal(path: str, m: CsrMatrix) -> None:

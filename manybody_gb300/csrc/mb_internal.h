@@ -153,9 +153,14 @@ struct mb_model_s {
   int64_t n_terms = 0;
   // The momentum-space model (HubbardModelMomentum): dispersion per orbital
   // and U/N, each 0 where the expression's 1000 eps zero drop removes it.
+  // For a current operator J_d(Q) (current = true) eps holds the velocity
+  // v_d(k) per orbital instead, with the transfer Q and the direction d.
   bool momentum = false;
   std::vector<double> eps;
   double u_over_n = 0.0;
+  bool current = false;
+  std::vector<int64_t> transfer;
+  int direction = 0;
 };
 
 namespace mb {

@@ -3,6 +3,12 @@
 //
 //   ref_dump <dims> <t> <U> <particles> <spin_projection> <out.bin>
 //     dims: "8" (1D chain), "4x4" (2D), "2x2x2" (3D), all periodic.
+//   ref_dump --current <dims> <t> <particles> <spin_projection> <K> <Q> <direction> <out.bin>
+//     the current operator J_d(Q) (hubbard_model_momentum.h:52-90) from sector K
+//     to sector K+Q through compute_rectangular_matrix_elements
+//     (src/algebra/matrix_elements.h:107-167); output "MBREF002", u64 n_terms,
+//     u64 rows, u64 cols, the row basis masks (up, down), the column basis
+//     masks, u64 nnz, records as below.
 //   ref_dump --momentum <dims> <t> <U> <particles> <spin_projection> <K> <out.bin>
 //     the momentum-space model on one total-momentum sector K ("1", "1x0"):
 //     FermionBasis::with_fixed_particle_number_spin_momentum
@@ -59,7 +65,59 @@ std::vector<size_t> parse_dims(const std::string& s) {
 
 }  // namespace
 
+void put_masks(FILE* f, const FermionBasis& basis) {
+  const size_t dim = basis.set.size();
+  std::vector<uint64_t> up(dim, 0), down(dim, 0);
+  for (size_t i = 0; i < dim; ++i) {
+    for (const auto& op : basis.set[i]) {
+      if (op.spin() == FermionOperator::Spin::Up)
+        up[i] |= uint64_t{1} << op.value();
+      else
+        down[i] |= uint64_t{1} << op.value();
+    }
+  }
+  std::fwrite(up.data(), 8, dim, f);
+  std::fwrite(down.data(), 8, dim, f);
+}
+
+int dump_current(char** argv) {
+  const std::vector<size_t> dims = parse_dims(argv[2]);
+  const double t = std::atof(argv[3]);
+  const size_t particles = std::stoul(argv[4]);
+  const int sz = std::atoi(argv[5]);
+  const std::vector<size_t> k = parse_dims(argv[6]), q = parse_dims(argv[7]);
+  const size_t direction = std::stoul(argv[8]);
+  size_t orbitals = 1;
+  for (size_t d : dims) orbitals *= d;
+  std::vector<size_t> kq(dims.size());
+  for (size_t d = 0; d < dims.size(); ++d) kq[d] = (k[d] + q[d]) % dims[d];
+  const FermionExpression j = HubbardModelMomentum(t, 0.0, dims).current(q, direction);
+  FermionBasis col = FermionBasis::with_fixed_particle_number_spin_momentum(orbitals, particles, sz,
+                                                                           Index(dims), k);
+  FermionBasis row = FermionBasis::with_fixed_particle_number_spin_momentum(orbitals, particles, sz,
+                                                                           Index(dims), kq);
+  CooMatrix m = compute_rectangular_matrix_elements<CooMatrix>(row, col, j);
+  FILE* f = std::fopen(argv[9], "wb");
+  if (!f) return 3;
+  std::fwrite("MBREF002", 1, 8, f);
+  const uint64_t head[3] = {j.size(), row.set.size(), col.set.size()};
+  std::fwrite(head, 8, 3, f);
+  put_masks(f, row);
+  put_masks(f, col);
+  const uint64_t nnz = m.entries.size();
+  std::fwrite(&nnz, 8, 1, f);
+  for (const auto& [ij, v] : m.entries) {
+    const int64_t rc[2] = {static_cast<int64_t>(ij.first), static_cast<int64_t>(ij.second)};
+    const double re_im[2] = {v.real(), v.imag()};
+    std::fwrite(rc, 8, 2, f);
+    std::fwrite(re_im, 8, 2, f);
+  }
+  std::fclose(f);
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc == 10 && std::string(argv[1]) == "--current") return dump_current(argv);
   const bool momentum = argc == 9 && std::string(argv[1]) == "--momentum";
   if (argc != 7 && !momentum) {
     std::fprintf(stderr,

@@ -20,7 +20,12 @@ def golden_cases():
     """The real-space Hubbard sectors dumped from the reference (cereal_*
     fixtures are cache-format pins, mom_* momentum-space sectors)."""
     return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(f).startswith(("cereal_", "mom_")))
+                  if not os.path.basename(f).startswith(("cereal_", "mom_", "cur_")))
+
+
+def current_cases():
+    """The current operator J_d(Q) between momentum sectors, from the reference."""
+    return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "cur_*.npz")))
 
 
 def momentum_cases():

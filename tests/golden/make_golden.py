@@ -1,7 +1,8 @@
 """Regenerates the golden Hubbard fixtures in tests/golden/ from the reference.
 
-The real-space sectors (CASES) and, as mom_*.npz, the momentum-space model on
-total-momentum sectors (MOMENTUM_CASES; their npz adds the K vector).
+The real-space sectors (CASES); as mom_*.npz, the momentum-space model on
+total-momentum sectors (MOMENTUM_CASES; their npz adds the K vector); as
+cur_*.npz, the current operator between two sectors (CURRENT_CASES).
 
 Runs oracle/_ref/ref_dump (built by oracle/build_ref.sh from the reference
 sources: its basis enumeration, HubbardModel{,2D,3D} and
@@ -71,6 +72,43 @@ MOMENTUM_CASES = [
     ("mom_cube2x2x2_n4_k101", "2x2x2", 1.0, 2.0, 4, 0, "1x0x1"),
 ]
 
+# Current operator J_d(Q) from sector K to K+Q (ref_dump --current):
+# (name, dims, t, particles, spin_projection, K, Q, direction)
+CURRENT_CASES = [
+    ("cur_chain4_n2_k0_q1", "4", 1.0, 2, 0, "0", "1", 0),
+    ("cur_chain6_n4_k2_q1", "6", 1.0, 4, 0, "2", "1", 0),
+    ("cur_chain6_n4_k2_q0", "6", 1.0, 4, 0, "2", "0", 0),
+    ("cur_chain6_n3_sz1_k1_q3", "6", 0.7, 3, 1, "1", "3", 0),
+    ("cur_chain8_n4_k0_q2", "8", 1.0, 4, 0, "0", "2", 0),
+    ("cur_sq3x3_n4_k11_q10_d0", "3x3", 1.0, 4, 0, "1x1", "1x0", 0),
+    ("cur_sq3x3_n4_k11_q10_d1", "3x3", 1.0, 4, 0, "1x1", "1x0", 1),
+    ("cur_rect2x4_n4_k00_q01_d1", "2x4", 1.0, 4, 0, "0x0", "0x1", 1),
+]
+
+
+def dump_current(dims, t, n, sz, k, q, d):
+    with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
+        path = f.name
+    try:
+        subprocess.run([REF_DUMP, "--current", dims, repr(t), str(n), str(sz), k, q, str(d), path],
+                       check=True)
+        b = open(path, "rb").read()
+    finally:
+        os.unlink(path)
+    assert b[:8] == b"MBREF002"
+    n_terms, nr, nc = (int(v) for v in np.frombuffer(b[8:32], "<u8"))
+    o = 32
+    parts = []
+    for n_ in (nr, nr, nc, nc):
+        parts.append(np.frombuffer(b[o:o + 8 * n_], "<u8").copy())
+        o += 8 * n_
+    nnz = int(np.frombuffer(b[o:o + 8], "<u8")[0])
+    rec = np.frombuffer(b[o + 8:], np.dtype([("r", "<i8"), ("c", "<i8"), ("re", "<f8"),
+                                             ("im", "<f8")]))
+    assert len(rec) == nnz
+    assert np.all(rec["im"] == 0.0)
+    return n_terms, parts, rec
+
 
 def dump(dims, t, U, n, sz, momentum=None):
     with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
@@ -117,6 +155,17 @@ def main():
                             row=rec["r"].astype(np.int32), col=rec["c"].astype(np.int32),
                             val=rec["re"].copy())
         print(f"{name}: dim={len(up)} nnz={len(rec)} terms={n_terms}")
+    for name, dims, t, n, sz, k, q, d in CURRENT_CASES:
+        n_terms, (ru, rd, cu, cd), rec = dump_current(dims, t, n, sz, k, q, d)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"),
+                            dims=np.array([int(x) for x in dims.split("x")], np.int32), t=t,
+                            particles=n, spin_projection=sz,
+                            momentum=np.array([int(x) for x in k.split("x")], np.int32),
+                            transfer=np.array([int(x) for x in q.split("x")], np.int32),
+                            direction=d, n_terms=n_terms, row_up=ru, row_down=rd, col_up=cu,
+                            col_down=cd, row=rec["r"].astype(np.int32),
+                            col=rec["c"].astype(np.int32), val=rec["re"].copy())
+        print(f"{name}: {len(ru)}x{len(cu)} nnz={len(rec)} terms={n_terms}")
 
 
 if __name__ == "__main__":

@@ -61,3 +61,11 @@ def test_momentum_argument_checks(mb):
         mb.FermionBasis.with_fixed_particle_number_spin_momentum(4, 3, 0, (4,), (0,))
     with pytest.raises(ValueError):
         mb.FermionBasis.with_fixed_particle_number_spin_momentum(4, 2, 0, (2, 2), (0,))
+
+
+@pytest.mark.parametrize("name", __import__("conftest").current_cases())
+def test_current_operator_term_count(mb, name):
+    g = load_golden(name)
+    dims = [int(d) for d in g["dims"]]
+    j = mb.CurrentOperator(float(g["t"]), dims, [int(q) for q in g["transfer"]], int(g["direction"]))
+    assert j.term_count() == int(g["n_terms"])
