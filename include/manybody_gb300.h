@@ -82,6 +82,14 @@ int mb_synchronize(void);
  * <= 32 and C(L,N_up), C(L,N_down) <= 2^23. */
 int mb_basis_create_fixed_spin(int64_t orbitals, int64_t particles, int spin_projection,
                                mb_basis_t* out);
+/* BasisImpl::with_fixed_particle_number (src/algebra/basis.cpp:69-89,248-266):
+ * all spin projections for `particles` fermions, in the reference's index
+ * order (its depth-first enumeration without per-spin counts).  Operators on
+ * it (mb_op_create with a real-space model; MB_PREC_F64 / MB_PREC_F32) are
+ * block diagonal: one (N_up, N_down) block per spin projection, each the
+ * matrix-free kernel on its slice of the tensor layout (blocks by N_up
+ * ascending).  mb_basis_sector reports n_up = n_down = -1. */
+int mb_basis_create_fixed_number(int64_t orbitals, int64_t particles, mb_basis_t* out);
 /* BasisImpl::with_fixed_particle_number_spin_momentum (src/algebra/basis.cpp:128-185,
  * 304-356): the states of one total momentum K on a periodic lattice of sizes
  * dims[0..ndim) (orbital k has coordinates k_d, first dimension fastest;

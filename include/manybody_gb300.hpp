@@ -3,10 +3,12 @@
 //
 //   reference                                        here
 //   FermionBasis::with_fixed_particle_number_and_spin mbgpu::FermionBasis::with_fixed_particle_number_and_spin
-//     (src/algebra/basis.cpp:91-126)
+//     (src/algebra/basis.cpp:91-126); also with_fixed_particle_number (:69-89)
+//     and with_fixed_particle_number_spin_momentum (:128-185)
 //   basis.set.size() / index_of / contains            size() / index_of() / contains()
 //   HubbardModel / 2D / 3D (t, u, sizes...)           mbgpu::HubbardModel / 2D / 3D
 //     (src/algebra/fermion/model/hubbard_model.h)
+//   HubbardModelMomentum (t, u, sizes)                mbgpu::HubbardModelMomentum
 //   compute_matrix_elements<sp_cx_mat>(basis, H)      mbgpu::compute_matrix_elements(basis, model)
 //     (src/algebra/matrix_elements.h:74-105)
 //   SparseComplexMatrixOperator (linear_operator.h:81-91)
@@ -54,6 +56,24 @@ class FermionBasis {
     check(mb_basis_create_fixed_spin((int64_t)orbitals, (int64_t)particles, spin_projection, &h));
     return FermionBasis(h, orbitals, particles);
   }
+  // with_fixed_particle_number (src/algebra/basis.cpp:69-89): all spin projections
+  static FermionBasis with_fixed_particle_number(size_t orbitals, size_t particles) {
+    mb_basis_t h = nullptr;
+    check(mb_basis_create_fixed_number((int64_t)orbitals, (int64_t)particles, &h));
+    return FermionBasis(h, orbitals, particles);
+  }
+  // with_fixed_particle_number_spin_momentum (src/algebra/basis.cpp:128-185); the
+  // reference passes an Index of the lattice sizes
+  static FermionBasis with_fixed_particle_number_spin_momentum(
+      size_t orbitals, size_t particles, int spin_projection, const std::vector<size_t>& sizes,
+      const std::vector<size_t>& momentum) {
+    std::vector<int64_t> d(sizes.begin(), sizes.end()), k(momentum.begin(), momentum.end());
+    mb_basis_t h = nullptr;
+    check(mb_basis_create_momentum(d.data(), (int)d.size(), (int64_t)particles, spin_projection,
+                                   k.data(), &h));
+    (void)orbitals;
+    return FermionBasis(h, orbitals, particles);
+  }
   FermionBasis(FermionBasis&& o) noexcept : h_(std::exchange(o.h_, nullptr)),
                                             orbitals(o.orbitals), particles(o.particles) {}
   FermionBasis& operator=(FermionBasis&& o) noexcept {
@@ -99,8 +119,10 @@ class FermionBasis {
 
 class HubbardModelBase {
  public:
-  HubbardModelBase(double t, double u, std::vector<int64_t> dims) : t(t), u(u) {
-    check(mb_hubbard_create(dims.data(), (int)dims.size(), t, u, &h_));
+  HubbardModelBase(double t, double u, std::vector<int64_t> dims, bool momentum = false)
+      : t(t), u(u) {
+    if (momentum) check(mb_hubbard_momentum_create(dims.data(), (int)dims.size(), t, u, &h_));
+    else check(mb_hubbard_create(dims.data(), (int)dims.size(), t, u, &h_));
   }
   HubbardModelBase(HubbardModelBase&& o) noexcept : t(o.t), u(o.u), h_(std::exchange(o.h_, nullptr)) {}
   HubbardModelBase(const HubbardModelBase&) = delete;
@@ -129,6 +151,11 @@ struct HubbardModel2D : HubbardModelBase {
 struct HubbardModel3D : HubbardModelBase {
   HubbardModel3D(double t, double u, size_t sx, size_t sy, size_t sz)
       : HubbardModelBase(t, u, {(int64_t)sx, (int64_t)sy, (int64_t)sz}) {}
+};
+// HubbardModelMomentum (src/algebra/fermion/model/hubbard_model_momentum.h:19-180)
+struct HubbardModelMomentum : HubbardModelBase {
+  HubbardModelMomentum(double t, double u, const std::vector<size_t>& size)
+      : HubbardModelBase(t, u, std::vector<int64_t>(size.begin(), size.end()), true) {}
 };
 
 // Reference-order CSR of H, values complex<double>.

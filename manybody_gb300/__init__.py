@@ -96,6 +96,7 @@ SIGNATURES = {
     "mb_op_create": (C.c_int, [_vp, _vp, C.c_int, C.POINTER(_vp)]),
     "mb_op_create_csr": (C.c_int, [_i64, _i64p, _i64p, _dp, C.c_int, C.POINTER(_vp)]),
     "mb_basis_create_momentum": (C.c_int, [_i64p, C.c_int, _i64, C.c_int, _i64p, C.POINTER(_vp)]),
+    "mb_basis_create_fixed_number": (C.c_int, [_i64, _i64, C.POINTER(_vp)]),
     "mb_current_create": (C.c_int, [_i64p, C.c_int, C.c_double, _i64p, C.c_int, C.POINTER(_vp)]),
     "mb_compute_rectangular_matrix_elements_csr": (C.c_int, [_vp, _vp, _vp, _i64p, _i64p, _i64p, _dp]),
     "mb_rect_op_create": (C.c_int, [_vp, _vp, _vp, C.c_int, C.POINTER(_vp)]),
@@ -210,6 +211,13 @@ class FermionBasis:
                                             spin_projection: int) -> "FermionBasis":
         h = C.c_void_p()
         _check(lib().mb_basis_create_fixed_spin(orbitals, particles, spin_projection, C.byref(h)))
+        return cls(h, orbitals, particles)
+
+    @classmethod
+    def with_fixed_particle_number(cls, orbitals: int, particles: int) -> "FermionBasis":
+        """with_fixed_particle_number (src/algebra/basis.cpp:69-89): all spin projections."""
+        h = C.c_void_p()
+        _check(lib().mb_basis_create_fixed_number(orbitals, particles, C.byref(h)))
         return cls(h, orbitals, particles)
 
     @classmethod

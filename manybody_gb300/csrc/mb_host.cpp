@@ -30,6 +30,10 @@ const Binom& binom_table() {
 }
 
 // Masks with n of L bits set, in increasing numeric order (= colex order).
+static SpinSector make_sector(int L, int n);
+
+SpinSector make_spin_sector(int L, int n) { return make_sector(L, n); }
+
 static SpinSector make_sector(int L, int n) {
   SpinSector s;
   s.L = L;
@@ -416,6 +420,35 @@ int mb_basis_create_fixed_spin(int64_t orbitals, int64_t particles, int spin_pro
   });
 }
 
+int mb_basis_create_fixed_number(int64_t orbitals, int64_t particles, mb_basis_t* out) {
+  return guard([&] {
+    MB_REQUIRE(out, MB_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    MB_REQUIRE(orbitals >= 1 && orbitals <= kMaxOrbitals, MB_ERR_CAPACITY,
+               "orbitals must be in [1, 32]");
+    MB_REQUIRE(particles >= 0 && particles <= 2 * orbitals, MB_ERR_INVALID_ARG,
+               "particles must be in [0, 2*orbitals]");
+    auto b = std::make_unique<mb_basis_s>();
+    b->L = (int)orbitals;
+    b->particles = (int)particles;
+    b->n_up = -1;
+    b->n_down = -1;
+    const Binom& B = binom_table();
+    b->sz_off.push_back(0);
+    for (int64_t nu = std::max<int64_t>(0, particles - orbitals); nu <= std::min(particles, orbitals); ++nu) {
+      const int64_t d = binom_at(B, (int)orbitals, (int)nu) * binom_at(B, (int)orbitals, (int)(particles - nu));
+      MB_REQUIRE(binom_at(B, (int)orbitals, (int)nu) <= kMaxSectorDim &&
+                     binom_at(B, (int)orbitals, (int)(particles - nu)) <= kMaxSectorDim,
+                 MB_ERR_CAPACITY, "a spin sector exceeds 2^23 states");
+      b->sz_nup.push_back((int)nu);
+      b->sz_off.push_back(b->sz_off.back() + d);
+    }
+    b->dim = b->sz_off.back();
+    MB_REQUIRE(b->dim < (int64_t)INT32_MAX, MB_ERR_CAPACITY, "basis dimension exceeds 2^31");
+    *out = b.release();
+  });
+}
+
 int mb_basis_create_momentum(const int64_t* dims, int ndim, int64_t particles,
                              int spin_projection, const int64_t* momentum, mb_basis_t* out) {
   return guard([&] {
@@ -500,6 +533,21 @@ int mb_basis_export_reference_order(mb_basis_t basis, uint64_t* up_masks, uint64
       }
       return;
     }
+    if (basis->all_sz()) {
+      const Binom& B = binom_table();
+      for (size_t blk = 0; blk < basis->sz_nup.size(); ++blk) {
+        const SpinSector su = make_sector(basis->L, basis->sz_nup[blk]);
+        const SpinSector sd = make_sector(basis->L, basis->particles - basis->sz_nup[blk]);
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < su.D * sd.D; ++i) {
+          const uint32_t u = su.masks[(size_t)(i / sd.D)], d = sd.masks[(size_t)(i % sd.D)];
+          const int64_t r = reference_rank_all(B, u, d, basis->L);
+          up_masks[r] = u;
+          down_masks[r] = d;
+        }
+      }
+      return;
+    }
     const Binom& B = binom_table();
     const int64_t Dd = basis->down.D;
 #pragma omp parallel for schedule(static)
@@ -516,6 +564,13 @@ int mb_basis_index_of(mb_basis_t basis, uint64_t up_mask, uint64_t down_mask, in
   return guard([&] {
     MB_REQUIRE(basis && index, MB_ERR_INVALID_ARG, "NULL argument");
     const uint64_t lim = basis->L >= 64 ? ~uint64_t(0) : ((uint64_t(1) << basis->L) - 1);
+    if (basis->all_sz()) {
+      MB_REQUIRE((up_mask & ~lim) == 0 && (down_mask & ~lim) == 0 &&
+                     __builtin_popcountll(up_mask) + __builtin_popcountll(down_mask) == basis->particles,
+                 MB_ERR_INVALID_ARG, "key is not in the basis");
+      *index = reference_rank_all(binom_table(), (uint32_t)up_mask, (uint32_t)down_mask, basis->L);
+      return;
+    }
     MB_REQUIRE((up_mask & ~lim) == 0 && (down_mask & ~lim) == 0 &&
                    __builtin_popcountll(up_mask) == basis->n_up &&
                    __builtin_popcountll(down_mask) == basis->n_down,
@@ -535,6 +590,19 @@ int mb_basis_permutation(mb_basis_t basis, int64_t* ref_of_tensor) {
     MB_REQUIRE(basis && ref_of_tensor, MB_ERR_INVALID_ARG, "NULL argument");
     if (basis->momentum()) {  // operators on a momentum sector index it in reference order
       for (int64_t i = 0; i < basis->dim; ++i) ref_of_tensor[i] = i;
+      return;
+    }
+    if (basis->all_sz()) {  // the sectors' tensor blocks, concatenated
+      const Binom& B = binom_table();
+      for (size_t blk = 0; blk < basis->sz_nup.size(); ++blk) {
+        const SpinSector su = make_sector(basis->L, basis->sz_nup[blk]);
+        const SpinSector sd = make_sector(basis->L, basis->particles - basis->sz_nup[blk]);
+        const int64_t off = basis->sz_off[blk];
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < su.D * sd.D; ++i)
+          ref_of_tensor[off + i] = reference_rank_all(B, su.masks[(size_t)(i / sd.D)],
+                                                      sd.masks[(size_t)(i % sd.D)], basis->L);
+      }
       return;
     }
     const Binom& B = binom_table();

@@ -115,6 +115,42 @@ __host__ __device__ inline int64_t reference_rank(const Binom& B, uint32_t up, u
   return r;
 }
 
+// Reference index of the state (up, down) in the basis of all spin
+// projections, with_fixed_particle_number (src/algebra/basis.cpp:69-89,
+// 248-266): the same depth-first enumeration without the per-spin counts, so
+// the index counts the sequences of occupied slots (orbital-major, Up before
+// Down) that are lexicographically smaller under the element order (spin,
+// orbital).  At each position every valid smaller alternative e' contributes
+// C(#slots after e', particles left), where the slots after (o', Up) are
+// 1 + 2 (L-1-o') and after (o', Down) are 2 (L-1-o').
+__host__ __device__ inline int64_t reference_rank_all(const Binom& B, uint32_t up, uint32_t down,
+                                                      int L) {
+#ifdef __CUDA_ARCH__
+  const int n = __popc(up) + __popc(down);
+#else
+  const int n = __builtin_popcount(up) + __builtin_popcount(down);
+#endif
+  int64_t r = 0;
+  int t = 0, last_o = -1, last_s = 1;
+  for (int o = 0; o < L; ++o) {
+    for (int s = 0; s < 2; ++s) {
+      if (!(((s ? down : up) >> o) & 1u)) continue;
+      const int rem = n - t - 1;
+      for (int s2 = 0; s2 <= s; ++s2) {
+        const int hi = s2 < s ? L : o;
+        for (int o2 = 0; o2 < hi; ++o2) {
+          if (!(o2 > last_o || (o2 == last_o && s2 > last_s))) continue;
+          r += binom_at(B, (s2 == 0 ? 1 : 0) + 2 * (L - 1 - o2), rem);
+        }
+      }
+      ++t;
+      last_o = o;
+      last_s = s;
+    }
+  }
+  return r;
+}
+
 // ---------------------------------------------------------------------------
 // Host objects behind the opaque handles.
 // ---------------------------------------------------------------------------
@@ -137,6 +173,13 @@ struct mb_basis_s {
   std::vector<uint32_t> kup, kdown;
   std::vector<int64_t> kfull;
   bool momentum() const { return !kdims.empty(); }
+  // All spin projections (with_fixed_particle_number): the sectors N_up =
+  // sz_nup[b], N_down = particles - N_up, concatenated in the tensor layout
+  // (block b at sz_off[b], its own r_up * D_down + r_down inside).
+  int particles = 0;
+  std::vector<int> sz_nup;
+  std::vector<int64_t> sz_off;
+  bool all_sz() const { return !sz_nup.empty(); }
 };
 
 struct mb_model_s {
@@ -177,6 +220,9 @@ struct HopTable {
   bool has_self = false;
 };
 HopTable build_hop_table(const SpinSector& s, const mb_model_s& m);
+
+// The masks of one spin sector (n of L orbitals) in colex order.
+SpinSector make_spin_sector(int L, int n);
 
 // Reverse Cuthill-McKee order of the states of a hop table (BFS from a
 // low-degree state, neighbours by increasing degree, reversed).
@@ -261,6 +307,12 @@ struct OpView {
   // of its column, plus a separate diagonal (the momentum-sector operators).
   const double* csr_diag;
   double csr_off;
+  // Block-diagonal operators (all spin projections): n_blocks sub-views on
+  // consecutive slices of the vector, sub_off[b] their element offsets (host
+  // arrays; launch_apply loops over them).
+  int n_blocks;
+  const OpView* sub;
+  const int64_t* sub_off;
   double t;
   int max_up_degree;
   int max_dn_degree;
@@ -283,6 +335,9 @@ struct mb_op_s {
   double t = 0.0, u = 0.0;
   mb::OpView view{};
   bool natural_order = false;      // a sparse-matrix operator: reference order = its own index
+  std::vector<std::unique_ptr<mb_op_s>> subs;  // blocks of an all-spin-projection operator
+  std::vector<mb::OpView> sub_views;
+  std::vector<int64_t> sub_offsets;
   std::vector<void*> allocations;  // device buffers owned by the op
   int32_t* perm = nullptr;         // tensor -> reference index (lazy)
   int32_t* iperm = nullptr;        // reference -> tensor index (lazy)

@@ -259,6 +259,11 @@ static bool apply_staged(const OpView& v, int precision) {
 static int csr_grid(int64_t n);
 
 int apply_grid(const OpView& v, int precision) {
+  if (v.n_blocks) {
+    int g = 0;
+    for (int b = 0; b < v.n_blocks; ++b) g += apply_grid(v.sub[b], precision);
+    return g;
+  }
   if (v.csr_row) return csr_grid(v.dim);
   int64_t g = (int64_t)num_sms() * (precision == MB_PREC_F32 ? kApplyCtasPerSm<float> : 1);
   if (g > v.Du) g = v.Du;
@@ -426,6 +431,18 @@ static void csr_apply_dots(const OpView& v, const void* x, void* y, double scale
 void launch_apply(const OpView& v, int precision, const void* x, void* y, double scale,
                   double shift, double beta, const void* z, double* partials, int dot_mode,
                   cudaStream_t st) {
+  if (v.n_blocks) {  // block-diagonal: each block on its slice, partials one after another
+    const size_t es = elem_bytes(precision);
+    int64_t first = 0;
+    for (int b = 0; b < v.n_blocks; ++b) {
+      const size_t off = es * (size_t)v.sub_off[b];
+      launch_apply(v.sub[b], precision, (const char*)x + off, (char*)y + off, scale, shift, beta,
+                   z ? (const char*)z + off : nullptr, partials ? partials + 3 * first : nullptr,
+                   dot_mode, st);
+      first += apply_grid(v.sub[b], precision);
+    }
+    return;
+  }
   if (v.csr_row) {
     if (precision == MB_PREC_F32) csr_apply_dots<float>(v, x, y, scale, shift, beta, z, partials, dot_mode, st);
     else csr_apply_dots<double>(v, x, y, scale, shift, beta, z, partials, dot_mode, st);

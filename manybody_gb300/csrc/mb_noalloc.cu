@@ -112,8 +112,8 @@ extern "C" int mb_op_apply_noalloc(mb_op_t op, const void* x_dev, void* y_dev, v
   return guard([&] {
     MB_REQUIRE(op && x_dev && y_dev, MB_ERR_INVALID_ARG, "NULL argument");
     MB_REQUIRE(x_dev != y_dev, MB_ERR_INVALID_ARG, "x and y must not overlap");
-    MB_REQUIRE(!op->natural_order, MB_ERR_INVALID_ARG,
-               "mb_op_apply_noalloc takes lattice operators (mb_op_create)");
+    MB_REQUIRE(!op->natural_order && !op->view.n_blocks, MB_ERR_INVALID_ARG,
+               "mb_op_apply_noalloc takes lattice operators of one (N_up, N_down) sector");
     MB_REQUIRE(op->dim <= kNoAllocMaxDim, MB_ERR_CAPACITY,
                "mb_op_apply_noalloc handles at most 1048576 basis states; this sector has " +
                    std::to_string(op->dim) + " (use mb_op_apply)");

@@ -171,6 +171,85 @@ static void build_op(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m) {
   if (op->precision == MB_PREC_Q64) q_op_prepare(op, m, tu, td);
 }
 
+// One (N_up, N_down) block of an all-spin-projection basis as a basis.
+static mb_basis_s sector_of(const mb_basis_s* b, size_t blk) {
+  mb_basis_s s;
+  s.L = b->L;
+  s.n_up = b->sz_nup[blk];
+  s.n_down = b->particles - s.n_up;
+  s.up = make_spin_sector(s.L, s.n_up);
+  s.down = make_spin_sector(s.L, s.n_down);
+  s.dim = s.up.D * s.down.D;
+  return s;
+}
+
+// Reference indices (all spin projections) of one block's tensor order.
+static std::vector<int32_t> block_perm(const mb_basis_s& s) {
+  std::vector<int32_t> p((size_t)s.dim);
+  const Binom& B = binom_table();
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < s.dim; ++i)
+    p[(size_t)i] = (int32_t)reference_rank_all(B, s.up.masks[(size_t)(i / s.down.D)],
+                                               s.down.masks[(size_t)(i % s.down.D)], s.L);
+  return p;
+}
+
+static void free_op_memory(mb_op_s* op) {
+  for (auto& kv : op->scratch) {
+    for (void* p : {kv.second.a, kv.second.b, kv.second.hx, kv.second.hy})
+      if (p) cudaFree(p);
+  }
+  op->scratch.clear();
+  for (auto& sub : op->subs) free_op_memory(sub.get());
+  for (void* p : op->allocations) cudaFree(p);
+  op->allocations.clear();
+}
+
+// The block-diagonal operator of an all-spin-projection basis: one lattice
+// operator per (N_up, N_down) block on consecutive slices, the permutation
+// to the reference order (reference_rank_all) computed here.
+static void build_all_sz(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m) {
+  MB_REQUIRE(!m->momentum && !m->current, MB_ERR_INVALID_ARG,
+             "an all-spin-projection basis takes the real-space model");
+  MB_REQUIRE(op->precision != MB_PREC_Q64, MB_ERR_INVALID_ARG,
+             "all-spin-projection operators take MB_PREC_F64 or MB_PREC_F32");
+  MB_CUDA(cudaGetDevice(&op->device));
+  op->L = b->L;
+  op->n_up = -1;
+  op->n_down = -1;
+  op->dim = b->dim;
+  op->Du = b->dim;
+  op->Dd = 1;
+  op->t = m->t;
+  op->u = m->u;
+  std::vector<int32_t> perm((size_t)b->dim);
+  for (size_t blk = 0; blk < b->sz_nup.size(); ++blk) {
+    const mb_basis_s s = sector_of(b, blk);
+    auto sub = std::make_unique<mb_op_s>();
+    sub->precision = op->precision;
+    try {
+      build_op(sub.get(), &s, m);
+    } catch (...) {
+      free_op_memory(sub.get());
+      throw;
+    }
+    op->sub_views.push_back(sub->view);
+    op->subs.push_back(std::move(sub));
+    const std::vector<int32_t> p = block_perm(s);
+    std::copy(p.begin(), p.end(), perm.begin() + b->sz_off[blk]);
+  }
+  op->sub_offsets = b->sz_off;
+  OpView& v = op->view;
+  v.Du = b->dim;
+  v.Dd = 1;
+  v.dim = b->dim;
+  v.L = b->L;
+  v.n_blocks = (int)op->subs.size();
+  v.sub = op->sub_views.data();
+  v.sub_off = op->sub_offsets.data();
+  op->perm = upload(op, perm.empty() ? std::vector<int32_t>{0} : perm);
+}
+
 // A momentum-sector operator: the sector's Hamiltonian built on the device
 // in signed-column form (row_ptr, column | sign << 31, diagonal, U/N); its
 // rows are the sector's reference order.
@@ -715,7 +794,9 @@ int mb_op_create(mb_basis_t basis, mb_model_t model, int precision, mb_op_t* out
     auto op = std::make_unique<mb_op_s>();
     op->precision = precision;
     try {
-      if (basis->momentum() || model->momentum) {
+      if (basis->all_sz()) {
+        build_all_sz(op.get(), basis, model);
+      } else if (basis->momentum() || model->momentum) {
         MB_REQUIRE(precision != MB_PREC_Q64, MB_ERR_INVALID_ARG,
                    "momentum-sector operators take MB_PREC_F64 or MB_PREC_F32");
         MB_CUDA(cudaGetDevice(&op->device));
@@ -738,7 +819,7 @@ int mb_op_create(mb_basis_t basis, mb_model_t model, int precision, mb_op_t* out
         build_op(op.get(), basis, model);
       }
     } catch (...) {
-      for (void* p : op->allocations) cudaFree(p);
+      free_op_memory(op.get());
       throw;
     }
     *out = op.release();
@@ -798,12 +879,8 @@ int mb_op_destroy(mb_op_t op) {
   if (!op) return MB_OK;
   cudaSetDevice(op->device);
   cudaDeviceSynchronize();
-  for (auto& kv : op->scratch) {
-    for (void* p : {kv.second.a, kv.second.b, kv.second.hx, kv.second.hy})
-      if (p) cudaFree(p);
-  }
   q_op_release(op);
-  for (void* p : op->allocations) cudaFree(p);
+  free_op_memory(op);
   delete op;
   return MB_OK;
 }
@@ -897,6 +974,53 @@ int mb_compute_matrix_elements_csr(mb_basis_t basis, mb_model_t model, int64_t* 
         for (void* p : o.allocations) cudaFree(p);
       }
     } cleanup{tmp};
+    if (basis->all_sz()) {
+      MB_REQUIRE(!model->momentum && !model->current, MB_ERR_INVALID_ARG,
+                 "an all-spin-projection basis takes the real-space model");
+      cudaStream_t st = 0;
+      const int64_t dim = basis->dim;
+      DevBuf cnt(sizeof(int32_t) * (size_t)std::max<int64_t>(dim, 1));
+      std::vector<mb_basis_s> secs;
+      std::vector<std::unique_ptr<mb_op_s>> ops;
+      std::vector<int32_t*> perms;
+      for (size_t blk = 0; blk < basis->sz_nup.size(); ++blk) {
+        secs.push_back(sector_of(basis, blk));
+        ops.push_back(std::make_unique<mb_op_s>());
+        ops.back()->precision = MB_PREC_F64;
+        build_op(ops.back().get(), &secs.back(), model);
+        perms.push_back(upload(&tmp, block_perm(secs.back())));
+        launch_csr_count(ops.back()->view, perms.back(), (int32_t*)cnt.p, st);
+      }
+      struct FreeOps {
+        std::vector<std::unique_ptr<mb_op_s>>& o;
+        ~FreeOps() {
+          for (auto& p : o) free_op_memory(p.get());
+        }
+      } free_ops{ops};
+      std::vector<int32_t> hc((size_t)dim);
+      if (dim) MB_CUDA(cudaMemcpy(hc.data(), cnt.p, sizeof(int32_t) * (size_t)dim, cudaMemcpyDeviceToHost));
+      std::vector<int64_t> rp((size_t)dim + 1, 0);
+      for (int64_t i = 0; i < dim; ++i) rp[(size_t)i + 1] = rp[(size_t)i] + hc[(size_t)i];
+      const int64_t total = rp[(size_t)dim];
+      if (!col_idx) {
+        *nnz = total;
+        if (row_ptr) std::memcpy(row_ptr, rp.data(), sizeof(int64_t) * rp.size());
+        return;
+      }
+      MB_REQUIRE(*nnz >= total, MB_ERR_CAPACITY, "nnz capacity smaller than the matrix");
+      MB_REQUIRE(row_ptr && values, MB_ERR_INVALID_ARG, "NULL row_ptr or values");
+      DevBuf drp(sizeof(int64_t) * rp.size()), dci(sizeof(int64_t) * (size_t)std::max<int64_t>(total, 1)),
+          dv(sizeof(double) * 2 * (size_t)std::max<int64_t>(total, 1));
+      MB_CUDA(cudaMemcpy(drp.p, rp.data(), sizeof(int64_t) * rp.size(), cudaMemcpyHostToDevice));
+      for (size_t blk = 0; blk < ops.size(); ++blk)
+        launch_csr_fill(ops[blk]->view, perms[blk], (const int64_t*)drp.p, (int64_t*)dci.p,
+                        (double*)dv.p, st);
+      std::memcpy(row_ptr, rp.data(), sizeof(int64_t) * rp.size());
+      MB_CUDA(cudaMemcpy(col_idx, dci.p, sizeof(int64_t) * (size_t)total, cudaMemcpyDeviceToHost));
+      MB_CUDA(cudaMemcpy(values, dv.p, sizeof(double) * 2 * (size_t)total, cudaMemcpyDeviceToHost));
+      *nnz = total;
+      return;
+    }
     if (basis->momentum() || model->momentum) {
       MomBuild mb;
       build_momentum(&tmp, basis, model, mb);

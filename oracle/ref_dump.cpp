@@ -9,6 +9,9 @@
 //     (src/algebra/matrix_elements.h:107-167); output "MBREF002", u64 n_terms,
 //     u64 rows, u64 cols, the row basis masks (up, down), the column basis
 //     masks, u64 nnz, records as below.
+//   ref_dump --all <dims> <t> <U> <particles> <out.bin>
+//     all spin projections: FermionBasis::with_fixed_particle_number
+//     (src/algebra/basis.cpp:69-89,248-266) with the real-space model.
 //   ref_dump --momentum <dims> <t> <U> <particles> <spin_projection> <K> <out.bin>
 //     the momentum-space model on one total-momentum sector K ("1", "1x0"):
 //     FermionBasis::with_fixed_particle_number_spin_momentum
@@ -118,6 +121,19 @@ int dump_current(char** argv) {
 
 int main(int argc, char** argv) {
   if (argc == 10 && std::string(argv[1]) == "--current") return dump_current(argv);
+  const bool all_sz = argc == 7 && std::string(argv[1]) == "--all";
+  if (all_sz) {  // same layout as the fixed-spin dump below, spin projection unused
+    static char zero[] = "0";
+    static char* shifted[8];
+    shifted[0] = argv[0];
+    shifted[1] = argv[2];
+    shifted[2] = argv[3];
+    shifted[3] = argv[4];
+    shifted[4] = argv[5];
+    shifted[5] = zero;
+    shifted[6] = argv[6];
+    argv = shifted;
+  }
   const bool momentum = argc == 9 && std::string(argv[1]) == "--momentum";
   if (argc != 7 && !momentum) {
     std::fprintf(stderr,
@@ -154,7 +170,8 @@ int main(int argc, char** argv) {
       std::fprintf(stderr, "ref_dump: 1 to 3 dimensions\n");
       return 2;
     }
-    basis = FermionBasis::with_fixed_particle_number_and_spin(orbitals, particles, sz);
+    basis = all_sz ? FermionBasis::with_fixed_particle_number(orbitals, particles)
+                   : FermionBasis::with_fixed_particle_number_and_spin(orbitals, particles, sz);
   }
   CooMatrix m = compute_matrix_elements<CooMatrix>(basis, h);
 

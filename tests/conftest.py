@@ -20,7 +20,12 @@ def golden_cases():
     """The real-space Hubbard sectors dumped from the reference (cereal_*
     fixtures are cache-format pins, mom_* momentum-space sectors)."""
     return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(f).startswith(("cereal_", "mom_", "cur_")))
+                  if not os.path.basename(f).startswith(("cereal_", "mom_", "cur_", "all_")))
+
+
+def all_sz_cases():
+    """All spin projections (with_fixed_particle_number), from the reference."""
+    return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "all_*.npz")))
 
 
 def current_cases():
@@ -37,10 +42,11 @@ def load_golden(name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     d = {k: z[k] for k in z.files}
     n = int(d["particles"])
-    sz = int(d["spin_projection"])
-    d["n_up"] = (n + sz) // 2
-    d["n_down"] = n - d["n_up"]
     d["L"] = int(np.prod(d["dims"]))
+    if "spin_projection" in d:  # all_* fixtures span every spin projection
+        sz = int(d["spin_projection"])
+        d["n_up"] = (n + sz) // 2
+        d["n_down"] = n - d["n_up"]
     return d
 
 

@@ -2,7 +2,8 @@
 
 The real-space sectors (CASES); as mom_*.npz, the momentum-space model on
 total-momentum sectors (MOMENTUM_CASES; their npz adds the K vector); as
-cur_*.npz, the current operator between two sectors (CURRENT_CASES).
+cur_*.npz, the current operator between two sectors (CURRENT_CASES); as
+all_*.npz, all spin projections (ALL_SZ_CASES).
 
 Runs oracle/_ref/ref_dump (built by oracle/build_ref.sh from the reference
 sources: its basis enumeration, HubbardModel{,2D,3D} and
@@ -72,6 +73,17 @@ MOMENTUM_CASES = [
     ("mom_cube2x2x2_n4_k101", "2x2x2", 1.0, 2.0, 4, 0, "1x0x1"),
 ]
 
+# All spin projections, real-space model (ref_dump --all): (name, dims, t, U, particles)
+ALL_SZ_CASES = [
+    ("all_chain1_n1", "1", 1.0, 3.0, 1),
+    ("all_chain4_n2", "4", 1.0, 4.0, 2),
+    ("all_chain4_n4", "4", 1.0, 4.0, 4),
+    ("all_chain5_n5", "5", 0.7, 3.0, 5),
+    ("all_chain6_n3", "6", 1.0, 2.0, 3),
+    ("all_sq2x2_n3", "2x2", 1.0, 2.0, 3),
+    ("all_rect2x3_n4", "2x3", 1.0, 6.0, 4),
+]
+
 # Current operator J_d(Q) from sector K to K+Q (ref_dump --current):
 # (name, dims, t, particles, spin_projection, K, Q, direction)
 CURRENT_CASES = [
@@ -110,13 +122,15 @@ def dump_current(dims, t, n, sz, k, q, d):
     return n_terms, parts, rec
 
 
-def dump(dims, t, U, n, sz, momentum=None):
+def dump(dims, t, U, n, sz, momentum=None, all_sz=False):
     with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
         path = f.name
     try:
         args = [dims, repr(t), repr(U), str(n), str(sz)]
         if momentum is not None:
             args = ["--momentum", *args, momentum]
+        if all_sz:
+            args = ["--all", dims, repr(t), repr(U), str(n)]
         subprocess.run([REF_DUMP, *args, path], check=True)
         b = open(path, "rb").read()
     finally:
@@ -152,6 +166,14 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), dims=np.array(dvec, np.int32),
                             t=t, U=U, particles=n, spin_projection=sz,
                             momentum=np.array(kvec, np.int32), n_terms=n_terms, up=up, down=dn,
+                            row=rec["r"].astype(np.int32), col=rec["c"].astype(np.int32),
+                            val=rec["re"].copy())
+        print(f"{name}: dim={len(up)} nnz={len(rec)} terms={n_terms}")
+    for name, dims, t, U, n in ALL_SZ_CASES:
+        n_terms, up, dn, rec = dump(dims, t, U, n, 0, all_sz=True)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"),
+                            dims=np.array([int(x) for x in dims.split("x")], np.int32), t=t, U=U,
+                            particles=n, n_terms=n_terms, up=up, down=dn,
                             row=rec["r"].astype(np.int32), col=rec["c"].astype(np.int32),
                             val=rec["re"].copy())
         print(f"{name}: dim={len(up)} nnz={len(rec)} terms={n_terms}")

@@ -69,3 +69,20 @@ def test_current_operator_term_count(mb, name):
     dims = [int(d) for d in g["dims"]]
     j = mb.CurrentOperator(float(g["t"]), dims, [int(q) for q in g["transfer"]], int(g["direction"]))
     assert j.term_count() == int(g["n_terms"])
+
+
+@pytest.mark.parametrize("name", __import__("conftest").all_sz_cases())
+def test_all_spin_projection_basis_matches_reference(mb, name):
+    """with_fixed_particle_number (src/algebra/basis.cpp:69-89,248-266): keys in
+    the reference's order, index_of, and the block permutation."""
+    g = load_golden(name)
+    L = int(np.prod([int(d) for d in g["dims"]]))
+    b = mb.FermionBasis.with_fixed_particle_number(L, int(g["particles"]))
+    up, dn = b.keys()
+    assert b.size() == len(g["up"])
+    assert np.array_equal(up, g["up"].astype(np.uint64))
+    assert np.array_equal(dn, g["down"].astype(np.uint64))
+    for i in range(0, len(up), max(1, len(up) // 13)):
+        assert b.index_of(int(up[i]), int(dn[i])) == i
+    perm = b.permutation()
+    assert np.array_equal(np.sort(perm), np.arange(len(up)))
