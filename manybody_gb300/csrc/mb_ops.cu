@@ -922,8 +922,17 @@ int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
     cudaStream_t st = 0;
     auto& s = scratch_for(op, st, 4);
     MB_CUDA(cudaMemcpyAsync(s.hx, x_host, vb, cudaMemcpyHostToDevice, st));
-    apply_affine(op, s.hx, s.hy, 1.0, 0.0, 0.0, nullptr, order, st);
-    MB_CUDA(cudaMemcpyAsync(y_host, s.hy, vb, cudaMemcpyDeviceToHost, st));
+    // A page-locked y (cudaHostAlloc / cudaHostRegister) is written in place by
+    // the last kernel (the order / format change), so the result crosses the
+    // host link once, while it is produced, instead of after a device copy.
+    void* y_dev = s.hy;
+    cudaPointerAttributes at{};
+    const bool direct = cudaPointerGetAttributes(&at, y_host) == cudaSuccess &&
+                        at.type == cudaMemoryTypeHost && at.devicePointer != nullptr;
+    if (!direct) cudaGetLastError();  // clear a failed query on pageable memory
+    if (direct) y_dev = at.devicePointer;
+    apply_affine(op, s.hx, y_dev, 1.0, 0.0, 0.0, nullptr, order, st);
+    if (!direct) MB_CUDA(cudaMemcpyAsync(y_host, s.hy, vb, cudaMemcpyDeviceToHost, st));
     MB_CUDA(cudaStreamSynchronize(st));
   });
 }
