@@ -186,7 +186,8 @@ int mb_op_apply(mb_op_t op, const void* x_dev, void* y_dev, int order, void* str
  * the Chebyshev step 2*Ht*T_n - T_{n-1} (kpm.h:222) in one pass. */
 int mb_op_apply_affine(mb_op_t op, const void* x_dev, void* y_dev, double scale, double shift,
                        double beta, const void* z_dev, int order, void* stream);
-/* apply() with host buffers: copies x in, applies, copies y out, then waits. */
+/* apply() with host buffers: copies x in, applies, copies y out, then waits.
+ * Safe from several host threads; calls on one operator run one at a time. */
 int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order);
 
 /* y = H x on device buffers in REFERENCE order, without allocating: no

@@ -342,6 +342,7 @@ struct mb_op_s {
   int32_t* perm = nullptr;         // tensor -> reference index (lazy)
   int32_t* iperm = nullptr;        // reference -> tensor index (lazy)
   std::mutex mu;
+  std::mutex host_mu;  // host-buffer calls: one at a time (shared staging, stream 0)
   struct Scratch {
     void* a = nullptr;  // tensor-order copies for reference-order calls
     void* b = nullptr;

@@ -920,6 +920,9 @@ int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
     check_order(order);
     const size_t vb = elem_bytes(op->precision) * (size_t)op->dim;
     cudaStream_t st = 0;
+    // host threads share the staging buffers and the stream: serialise whole
+    // calls, or one thread's upload could land between another's copy and apply
+    std::lock_guard<std::mutex> lk(op->host_mu);
     auto& s = scratch_for(op, st, 4);
     MB_CUDA(cudaMemcpyAsync(s.hx, x_host, vb, cudaMemcpyHostToDevice, st));
     // A page-locked y (cudaHostAlloc / cudaHostRegister) is written in place by

@@ -295,6 +295,48 @@ def test_concurrent_apply_on_streams(mb, cuda):
         assert np.linalg.norm(y.cpu().numpy() - ref) <= 1e-13 * np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_concurrent_apply_from_host_threads(mb, cuda, prec):
+    """Several host threads share one operator: each applies on its own stream
+    in reference order (per-stream scratch) and through host buffers (calls
+    serialised on the operator)."""
+    import threading
+    torch = cuda
+    g = load_golden("sq3x3_n5_sz1")
+    _, _, op = make(mb, [3, 3], 1.0, 8.0, g["n_up"], g["n_down"], prec)
+    H = ref_csr(g)
+    tol = 2e-6 if prec == 1 else 1e-13
+    n = op.dimension()
+    errors = []
+
+    def work(k):
+        try:
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                x = op.seed_vector(10 + k)
+                for _ in range(20):
+                    y = op.apply(x, stream=s.cuda_stream)
+            s.synchronize()
+            ref = H @ x.cpu().numpy()
+            errors.append(np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref))
+            xh = x.cpu().numpy()
+            yh = np.zeros_like(xh)
+            op.apply_host(xh, yh)
+            errors.append(np.linalg.norm(yh - ref) / np.linalg.norm(ref))
+        except Exception as exc:  # reported to the main thread
+            errors.append(exc)
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(6)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert len(errors) == 12
+    for e in errors:
+        assert not isinstance(e, Exception), e
+        assert e <= tol
+
+
 @pytest.mark.parametrize("dims,n", [((4, 4), 6), ((16,), 8)])
 def test_full_size_operator_properties(mb, cuda, dims, n):
     """The 4x4 6+6 and 1D L=16 8+8 sectors at full size (64.1M / 165.6M
