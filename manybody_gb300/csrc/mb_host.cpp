@@ -2,6 +2,7 @@
 // per-spin hop tables, the tridiagonal eigensolver, and the basis / model
 // entry points of the C ABI.
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -157,28 +158,100 @@ SignedLists signed_lists(const HopTable& t, int64_t D) {
   return s;
 }
 
+namespace {
+
+// Orders the entries of one quarter warp (8 lanes) over k slots: in each slot
+// a maximum matching of lanes to bank groups (target mod 8), lanes that must
+// take an entry now (as many left as slots) first, entries of the groups with
+// the most entries left preferred (the greedy form of Koenig's edge
+// colouring).  A lane left unmatched takes a padding zero element of a group
+// no entry uses in that slot, or, if it must take an entry, its first one.
+void order_quarter(std::vector<uint32_t> (&lst)[8], int k, uint32_t D, uint32_t* out) {
+  constexpr uint32_t kIdx = 0x7FFFFFFFu;
+  for (int j = 0; j < k; ++j) {
+    const int left = k - j;
+    int gdeg[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (auto& l : lst)
+      for (uint32_t w : l) ++gdeg[(w & kIdx) & 7u];
+    int order[8];
+    for (int l = 0; l < 8; ++l) order[l] = l;
+    std::stable_sort(order, order + 8, [&](int a, int b) {
+      const bool fa = (int)lst[a].size() >= left, fb = (int)lst[b].size() >= left;
+      if (fa != fb) return fa;
+      return lst[a].size() > lst[b].size();
+    });
+    int match_g[8], pick[8];
+    for (int i = 0; i < 8; ++i) match_g[i] = pick[i] = -1;
+    // Kuhn's augmenting paths; candidates by descending group degree
+    std::function<bool(int, unsigned&)> augment = [&](int l, unsigned& seen) -> bool {
+      int cand[64];
+      int nc = 0;
+      for (int i = 0; i < (int)lst[l].size() && nc < 64; ++i) cand[nc++] = i;
+      std::stable_sort(cand, cand + nc, [&](int a, int b) {
+        return gdeg[(lst[l][(size_t)a] & kIdx) & 7u] > gdeg[(lst[l][(size_t)b] & kIdx) & 7u];
+      });
+      for (int ci = 0; ci < nc; ++ci) {
+        const int g = (int)((lst[l][(size_t)cand[ci]] & kIdx) & 7u);
+        if (seen & (1u << g)) continue;
+        seen |= 1u << g;
+        if (match_g[g] < 0 || augment(match_g[g], seen)) {
+          match_g[g] = l;
+          pick[l] = cand[ci];
+          return true;
+        }
+      }
+      return false;
+    };
+    for (int oi = 0; oi < 8; ++oi) {
+      const int l = order[oi];
+      if (lst[l].empty()) continue;
+      unsigned seen = 0;
+      augment(l, seen);
+    }
+    unsigned used = 0;
+    uint32_t slot[8];
+    bool taken[8] = {false, false, false, false, false, false, false, false};
+    for (int l = 0; l < 8; ++l) {
+      if (pick[l] < 0 && !lst[l].empty() && (int)lst[l].size() >= left) pick[l] = 0;
+      if (pick[l] >= 0) {
+        slot[l] = lst[l][(size_t)pick[l]];
+        used |= 1u << ((slot[l] & kIdx) & 7u);
+        taken[l] = true;
+      }
+    }
+    // one padding element for every unmatched lane (same address: a broadcast)
+    int pg = 0;
+    while (pg < 8 && (used & (1u << pg))) ++pg;
+    if (pg == 8) pg = 0;
+    const uint32_t pad = D + ((uint32_t)pg + 8u - (D & 7u)) % 8u;
+    for (int l = 0; l < 8; ++l) {
+      if (taken[l]) {
+        lst[l].erase(lst[l].begin() + pick[l]);
+      } else {
+        slot[l] = pad;
+      }
+      out[(size_t)32 * j + (size_t)l] = slot[l];
+    }
+  }
+}
+
+}  // namespace
+
 SlicedTable sliced_table(const HopTable& t, int64_t D) {
-  MB_REQUIRE(D < (int64_t(1) << 27), MB_ERR_CAPACITY, "sector too large for the sliced table");
+  MB_REQUIRE(D + kSlicedPads < (int64_t(1) << 27), MB_ERR_CAPACITY,
+             "sector too large for the sliced table");
   SlicedTable s;
   const int64_t ng = (D + 31) / 32;
   s.grp.resize((size_t)(2 * ng));
   s.nneg.assign((size_t)D, 0);
-  const uint32_t pad = (uint32_t)D;
-  std::vector<uint32_t> col;
+  std::vector<uint32_t> lst[4][8];
   for (int64_t g = 0; g < ng; ++g) {
     int k = 0;
-    for (int64_t c = 32 * g; c < std::min(D, 32 * g + 32); ++c) {
-      int n = 0;
-      for (int32_t j = t.off[(size_t)c]; j < t.off[(size_t)c + 1]; ++j) n += (t.ent[(size_t)j] & 2u) ? 2 : 1;
-      k = std::max(k, n);
-    }
-    const size_t base = s.ent.size();
-    MB_REQUIRE(base + (size_t)32 * k < (size_t)INT32_MAX, MB_ERR_CAPACITY, "hop table too large");
-    s.grp[(size_t)(2 * g)] = (int32_t)base;
-    s.grp[(size_t)(2 * g + 1)] = k;
-    s.ent.resize(base + (size_t)32 * k, pad);
-    for (int64_t c = 32 * g; c < std::min(D, 32 * g + 32); ++c) {
+    for (int l = 0; l < 32; ++l) {
+      auto& col = lst[l >> 3][l & 7];
       col.clear();
+      const int64_t c = 32 * g + l;
+      if (c >= D) continue;
       for (int32_t j = t.off[(size_t)c]; j < t.off[(size_t)c + 1]; ++j) {
         const uint32_t e = t.ent[(size_t)j];
         const uint32_t w = (e >> 8) | ((e & 1u) << 31);
@@ -186,10 +259,16 @@ SlicedTable sliced_table(const HopTable& t, int64_t D) {
         if (e & 2u) col.push_back(w);
         s.nneg[(size_t)c] += (uint8_t)((e & 1u) * ((e & 2u) ? 2 : 1));
       }
-      for (size_t j = 0; j < col.size(); ++j) s.ent[base + 32 * j + (size_t)(c - 32 * g)] = col[j];
+      k = std::max(k, (int)col.size());
     }
+    const size_t base = s.ent.size();
+    MB_REQUIRE(base + (size_t)32 * k < (size_t)INT32_MAX, MB_ERR_CAPACITY, "hop table too large");
+    s.grp[(size_t)(2 * g)] = (int32_t)base;
+    s.grp[(size_t)(2 * g + 1)] = k;
+    s.ent.resize(base + (size_t)32 * k, (uint32_t)D);
+    for (int q = 0; q < 4; ++q) order_quarter(lst[q], k, (uint32_t)D, s.ent.data() + base + 8 * q);
   }
-  if (s.ent.empty()) s.ent.push_back(pad);
+  if (s.ent.empty()) s.ent.push_back((uint32_t)D);
   return s;
 }
 

@@ -256,8 +256,14 @@ SignedLists signed_lists(const HopTable& t, int64_t D);
 
 // Sliced-ELL copy of a hop table over groups of 32 consecutive states:
 // group g's slot j for lane l is ent[grp[2g] + 32 j + l] = target |
-// (negative << 31), doubled bonds listed twice, padding D (one zero element
-// past the row); grp[2g+1] = slots of group g.
+// (negative << 31), doubled bonds listed twice, padding D + k (one of
+// kSlicedPads zero elements past the row); grp[2g+1] = slots of group g.
+// Within a group each lane's entries are ordered (the hop sum does not
+// depend on the order) so that in every slot the eight lanes of a quarter
+// warp read distinct 16-byte shared-memory bank groups (index mod 8): a
+// warp's 16-byte gather from the staged row then takes 4 wavefronts, not
+// the ~8 of the hop order.  Padding takes a zero element in a free group.
+constexpr int kSlicedPads = 8;
 struct SlicedTable {
   std::vector<uint32_t> ent;
   std::vector<int32_t> grp;

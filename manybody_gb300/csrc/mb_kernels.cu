@@ -118,11 +118,11 @@ static int max_smem_optin() {
 // The matrix-free apply:  y = scale * (H - shift) x + beta * z
 // with optional fused dot products (dot_mode bit0: Re<x,y>, bit1: <y,y>,
 // bit2: <x,x>).  One CTA per SM (two for complex64) walks the rows r_up in
-// the row schedule's order; it stages the row X[r_up, :] (and one zero element) in shared
+// the row schedule's order; it stages the row X[r_up, :] (and eight zero elements) in shared
 // memory when it fits, so the down hops, which stay inside the row, gather
 // from shared memory through the sliced table (one coalesced 4-byte entry
-// per lane and slot: neighbour index | sign << 31, padding = the zero
-// element), while the up hops read the neighbour rows X[r_up', c] from
+// per lane and slot: neighbour index | sign << 31, padding = one of the zero
+// elements past the row), while the up hops read the neighbour rows X[r_up', c] from
 // L2/HBM with coalesced 8/16-byte loads, the row's sign-sorted target list
 // in shared memory (added, then subtracted).  Warp w takes the 32-column
 // groups w, w + 32, ... and prefetches its next group's up-hop lines into L2.
@@ -152,12 +152,13 @@ k_apply(OpView v, const typename C2<T>::type* __restrict__ x, typename C2<T>::ty
   extern __shared__ __align__(16) unsigned char smem[];
   const int64_t Dd = v.Dd;
   const uint32_t row_bytes = (uint32_t)(sizeof(V2) * Dd);
-  uint32_t* s_up = reinterpret_cast<uint32_t*>(smem + (STAGED ? row_bytes + sizeof(V2) : 0));
-  if (STAGED && threadIdx.x == 0) {
+  uint32_t* s_up =
+      reinterpret_cast<uint32_t*>(smem + (STAGED ? row_bytes + sizeof(V2) * kSlicedPads : 0));
+  if (STAGED && threadIdx.x < kSlicedPads) {
     V2 zero;
     zero.x = T(0);
     zero.y = T(0);
-    *reinterpret_cast<V2*>(smem + row_bytes) = zero;
+    reinterpret_cast<V2*>(smem + row_bytes)[threadIdx.x] = zero;
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int64_t ngroups = (Dd + 31) >> 5;
@@ -248,7 +249,7 @@ k_apply(OpView v, const typename C2<T>::type* __restrict__ x, typename C2<T>::ty
 static size_t apply_smem(const OpView& v, int precision, bool staged) {
   const int up_words = (v.max_up_list + 3) & ~3;
   size_t s = sizeof(uint32_t) * (size_t)up_words;
-  if (staged) s += elem_bytes(precision) * (size_t)(v.Dd + 1);
+  if (staged) s += elem_bytes(precision) * (size_t)(v.Dd + kSlicedPads);
   return s;
 }
 

@@ -137,10 +137,11 @@ __device__ void q_block_reduce(double (&v)[NC], unsigned long long magor, double
 //
 // One CTA of 1024 threads per SM walks the rows r_up in the row schedule's
 // order (reverse Cuthill-McKee: rows in flight together share neighbour rows
-// in L2).  Per row: the row x[r,:] and one zero element go to shared memory,
-// then warp w takes the 32-column groups g = w, w + 32, ...:
+// in L2).  Per row: the row x[r,:] and eight zero elements go to shared
+// memory, then warp w takes the 32-column groups g = w, w + 32, ...:
 //   down hops: sliced table, one coalesced 4-byte entry per lane and slot =
-//     neighbour index in the staged row | sign << 31; padding reads the zero
+//     neighbour index in the staged row | sign << 31, in an order that keeps
+//     each quarter warp on distinct bank groups; padding reads a zero
 //     element.  A negative hop adds v ^ -1 (= -v - 1); the
 //     column's count of negative hops is added back once;
 //   up hops: the row's sign-sorted target list (uniform across the CTA):
@@ -158,16 +159,17 @@ k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlon
   extern __shared__ __align__(16) unsigned char smem[];
   const int64_t Dd = v.Dd;
   const uint32_t row_bytes = (uint32_t)(16 * Dd);
-  uint32_t* s_up = reinterpret_cast<uint32_t*>(smem + (STAGED ? row_bytes + 16 : 0));
+  uint32_t* s_up = reinterpret_cast<uint32_t*>(smem + (STAGED ? row_bytes + 16 * kSlicedPads : 0));
   __shared__ long long s_cq[kMaxOrbitals + 1];
   __shared__ long long s_c1, s_c3;
   __shared__ int s_sh;
   if (threadIdx.x <= (unsigned)v.L) s_cq[threadIdx.x] = prm->cq[threadIdx.x];
+  if (STAGED && threadIdx.x < kSlicedPads)
+    reinterpret_cast<longlong2*>(smem + row_bytes)[threadIdx.x] = make_longlong2(0, 0);
   if (threadIdx.x == 0) {
     s_c1 = prm->c1;
     s_c3 = prm->c3;
     s_sh = prm->sh;
-    if (STAGED) *reinterpret_cast<longlong2*>(smem + row_bytes) = make_longlong2(0, 0);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int64_t ngroups = (Dd + 31) >> 5;
@@ -313,7 +315,7 @@ template <bool STAGED, int DOTS, bool HAS_Z>
 static void q_apply_t(const OpView& v, const void* x, void* y, const void* z, const QParams* prm,
                       double* partials, unsigned long long* max_or, cudaStream_t st) {
   size_t smem = sizeof(uint32_t) * (size_t)((v.max_up_list + 3) & ~3);
-  if (STAGED) smem += sizeof(longlong2) * (size_t)(v.Dd + 1);
+  if (STAGED) smem += sizeof(longlong2) * (size_t)(v.Dd + kSlicedPads);
   auto kern = k_apply_q<STAGED, DOTS, HAS_Z>;
   MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<q_apply_grid(v), kQThreads, smem, st>>>(v, (const longlong2*)x, (longlong2*)y,
@@ -337,7 +339,7 @@ static void q_apply_sel(const OpView& v, const void* x, void* y, const void* z,
 void launch_apply_q(const OpView& v, const void* x, void* y, const void* z, const QParams* prm,
                     double* partials, unsigned long long* max_or, int dots, cudaStream_t st) {
   const size_t need = sizeof(uint32_t) * (size_t)((v.max_up_list + 3) & ~3) +
-                      sizeof(longlong2) * (size_t)(v.Dd + 1) + 2048;
+                      sizeof(longlong2) * (size_t)(v.Dd + kSlicedPads) + 2048;
   if (need <= (size_t)smem_optin()) q_apply_sel<true>(v, x, y, z, prm, partials, max_or, dots, st);
   else q_apply_sel<false>(v, x, y, z, prm, partials, max_or, dots, st);
 }

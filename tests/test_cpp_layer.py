@@ -8,6 +8,7 @@ import pytest
 from conftest import ROOT
 
 SRC = os.path.join(ROOT, "tests", "cpp", "hpp_check.cpp")
+SLICED = os.path.join(ROOT, "tests", "cpp", "sliced_check.cpp")
 
 
 @pytest.fixture(scope="module")
@@ -28,4 +29,18 @@ def test_cpp_layer_host(hpp_binary):
 @pytest.mark.gpu
 def test_cpp_layer_gpu(hpp_binary, cuda):
     r = subprocess.run([hpp_binary, "gpu"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_sliced_table_order(tmp_path, mb):
+    """The sliced down table keeps every hop of every state, pads with the zero
+    elements past the row, and orders slots so a quarter warp's 16-byte
+    shared-memory gathers hit distinct bank groups (host-side tables only)."""
+    out = str(tmp_path / "sliced_check")
+    libdir = os.path.dirname(mb.LIB_PATH)
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", cuda_inc, SLICED,
+                    "-L", libdir, "-lmanybody_gb300", f"-Wl,-rpath,{libdir}", "-o", out],
+                   check=True)
+    r = subprocess.run([out], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
