@@ -245,6 +245,7 @@ SlicedTable sliced_table(const HopTable& t, int64_t D) {
   s.grp.resize((size_t)(2 * ng));
   s.nneg.assign((size_t)D, 0);
   std::vector<uint32_t> lst[4][8];
+  std::vector<uint32_t> slots;
   for (int64_t g = 0; g < ng; ++g) {
     int k = 0;
     for (int l = 0; l < 32; ++l) {
@@ -262,11 +263,18 @@ SlicedTable sliced_table(const HopTable& t, int64_t D) {
       k = std::max(k, (int)col.size());
     }
     const size_t base = s.ent.size();
-    MB_REQUIRE(base + (size_t)32 * k < (size_t)INT32_MAX, MB_ERR_CAPACITY, "hop table too large");
+    const int k4 = (k + 3) & ~3;
+    MB_REQUIRE(base + (size_t)32 * k4 < (size_t)INT32_MAX, MB_ERR_CAPACITY, "hop table too large");
     s.grp[(size_t)(2 * g)] = (int32_t)base;
     s.grp[(size_t)(2 * g + 1)] = k;
-    s.ent.resize(base + (size_t)32 * k, (uint32_t)D);
-    for (int q = 0; q < 4; ++q) order_quarter(lst[q], k, (uint32_t)D, s.ent.data() + base + 8 * q);
+    slots.assign((size_t)32 * k, (uint32_t)D);
+    for (int q = 0; q < 4; ++q) order_quarter(lst[q], k, (uint32_t)D, slots.data() + 8 * q);
+    // slots 4i..4i+3 of a lane are one 16-byte word; the last word is padded
+    s.ent.resize(base + (size_t)32 * k4, (uint32_t)D);
+    for (int j = 0; j < k; ++j)
+      for (int l = 0; l < 32; ++l)
+        s.ent[base + 128 * (size_t)(j >> 2) + 4 * (size_t)l + (size_t)(j & 3)] =
+            slots[(size_t)32 * j + (size_t)l];
   }
   if (s.ent.empty()) s.ent.push_back((uint32_t)D);
   return s;

@@ -255,9 +255,11 @@ struct SignedLists {
 SignedLists signed_lists(const HopTable& t, int64_t D);
 
 // Sliced-ELL copy of a hop table over groups of 32 consecutive states:
-// group g's slot j for lane l is ent[grp[2g] + 32 j + l] = target |
-// (negative << 31), doubled bonds listed twice, padding D + k (one of
-// kSlicedPads zero elements past the row); grp[2g+1] = slots of group g.
+// group g's slot j for lane l is ent[grp[2g] + 128 (j / 4) + 4 l + j % 4] =
+// target | (negative << 31) (a lane loads four slots as one 16-byte word, a
+// warp 512 contiguous bytes), doubled bonds listed twice, padding D + k (one
+// of kSlicedPads zero elements past the row); grp[2g+1] = slots of group g,
+// stored rounded up to a multiple of 4 with padding.
 // Within a group each lane's entries are ordered (the hop sum does not
 // depend on the order) so that in every slot the eight lanes of a quarter
 // warp read distinct 16-byte shared-memory bank groups (index mod 8): a

@@ -120,9 +120,9 @@ static int max_smem_optin() {
 // bit2: <x,x>).  One CTA per SM (two for complex64) walks the rows r_up in
 // the row schedule's order; it stages the row X[r_up, :] (and eight zero elements) in shared
 // memory when it fits, so the down hops, which stay inside the row, gather
-// from shared memory through the sliced table (one coalesced 4-byte entry
-// per lane and slot: neighbour index | sign << 31, padding = one of the zero
-// elements past the row), while the up hops read the neighbour rows X[r_up', c] from
+// from shared memory through the sliced table (one coalesced 16-byte load
+// per lane for four slots: neighbour index | sign << 31, padding = one of the
+// zero elements past the row), while the up hops read the neighbour rows X[r_up', c] from
 // L2/HBM with coalesced 8/16-byte loads, the row's sign-sorted target list
 // in shared memory (added, then subtracted).  Warp w takes the 32-column
 // groups w, w + 32, ... and prefetches its next group's up-hop lines into L2.
@@ -189,10 +189,7 @@ k_apply(OpView v, const typename C2<T>::type* __restrict__ x, typename C2<T>::ty
       }
       T ar = T(0), ai = T(0);
       const int2 gi = __ldg(reinterpret_cast<const int2*>(v.dn_sgrp) + g);
-      const uint32_t* ep = v.dn_sell + gi.x + lane;
-#pragma unroll 4
-      for (int j = 0; j < gi.y; ++j) {
-        const uint32_t e = __ldg(ep + 32 * j);
+      auto hop = [&](uint32_t e) {
         const uint32_t off = e << kShift;  // the sign bit shifts out
         V2 val;
         if (STAGED) {
@@ -206,6 +203,15 @@ k_apply(OpView v, const typename C2<T>::type* __restrict__ x, typename C2<T>::ty
         const T w = unit_sign(e, T(0));
         ar = fma(w, val.x, ar);
         ai = fma(w, val.y, ai);
+      };
+      // four slots per 16-byte load; the last word's unused slots are padding
+      const uint4* ep = reinterpret_cast<const uint4*>(v.dn_sell + gi.x) + lane;
+      for (int j = 0; j < gi.y; j += 4) {
+        const uint4 e = __ldg(ep + 8 * j);
+        hop(e.x);
+        hop(e.y);
+        hop(e.z);
+        hop(e.w);
       }
       const char* xc = reinterpret_cast<const char*>(x + cl);
 #pragma unroll 4

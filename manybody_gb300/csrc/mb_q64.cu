@@ -139,10 +139,10 @@ __device__ void q_block_reduce(double (&v)[NC], unsigned long long magor, double
 // order (reverse Cuthill-McKee: rows in flight together share neighbour rows
 // in L2).  Per row: the row x[r,:] and eight zero elements go to shared
 // memory, then warp w takes the 32-column groups g = w, w + 32, ...:
-//   down hops: sliced table, one coalesced 4-byte entry per lane and slot =
-//     neighbour index in the staged row | sign << 31, in an order that keeps
-//     each quarter warp on distinct bank groups; padding reads a zero
-//     element.  A negative hop adds v ^ -1 (= -v - 1); the
+//   down hops: sliced table, one coalesced 16-byte load per lane for four
+//     slots; entry = neighbour index in the staged row | sign << 31, in an
+//     order that keeps each quarter warp on distinct bank groups; padding
+//     reads a zero element.  A negative hop adds v ^ -1 (= -v - 1); the
 //     column's count of negative hops is added back once;
 //   up hops: the row's sign-sorted target list (uniform across the CTA):
 //     coalesced 16-byte loads x[r',c], summed then subtracted, no sign work;
@@ -211,22 +211,18 @@ k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlon
       }
       long long sr = 0, si = 0;
       const int2 gi = __ldg(reinterpret_cast<const int2*>(v.dn_sgrp) + g);
-      const uint32_t* ep = v.dn_sell + gi.x + lane;
-      int j = 0;
-#pragma unroll 2
-      for (; j + 2 <= gi.y; j += 2) {
-        const uint32_t e0 = __ldg(ep + 32 * j), e1 = __ldg(ep + 32 * j + 32);
-        const long long m0 = (int)e0 >> 31, m1 = (int)e1 >> 31;  // 0 or -1
-        const longlong2 v0 = dn_val(xrow, e0), v1 = dn_val(xrow, e1);
+      // four slots per 16-byte load; the last word's unused slots are padding
+      const uint4* ep = reinterpret_cast<const uint4*>(v.dn_sell + gi.x) + lane;
+      for (int j = 0; j < gi.y; j += 4) {
+        const uint4 e = __ldg(ep + 8 * j);
+        const long long m0 = (int)e.x >> 31, m1 = (int)e.y >> 31;  // 0 or -1
+        const long long m2 = (int)e.z >> 31, m3 = (int)e.w >> 31;
+        const longlong2 v0 = dn_val(xrow, e.x), v1 = dn_val(xrow, e.y);
+        const longlong2 v2 = dn_val(xrow, e.z), v3 = dn_val(xrow, e.w);
         sr += (v0.x ^ m0) + (v1.x ^ m1);
         si += (v0.y ^ m0) + (v1.y ^ m1);
-      }
-      if (j < gi.y) {
-        const uint32_t e0 = __ldg(ep + 32 * j);
-        const long long m0 = (int)e0 >> 31;
-        const longlong2 v0 = dn_val(xrow, e0);
-        sr += v0.x ^ m0;
-        si += v0.y ^ m0;
+        sr += (v2.x ^ m2) + (v3.x ^ m3);
+        si += (v2.y ^ m2) + (v3.y ^ m3);
       }
       const int nneg = __ldg(&v.dn_nneg[cl]);
       sr += nneg;
@@ -235,7 +231,7 @@ k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlon
       auto up_val = [&](int k) {
         return __ldg(reinterpret_cast<const longlong2*>(xc + (uint64_t)s_up[k] * row_bytes));
       };
-      j = 0;
+      int j = 0;
 #pragma unroll 2
       for (; j + 2 <= npos; j += 2) {
         const longlong2 v0 = up_val(j), v1 = up_val(j + 1);

@@ -1,6 +1,7 @@
 // Checks the sliced-ELL down table against the hop table it is built from:
 // every state's entries (doubled bonds twice) appear exactly once in its
-// lane, padding points at the zero elements past the row, and the slot order
+// lane (slots 4i..4i+3 of a lane form one 16-byte word), padding points at
+// the zero elements past the row, and the slot order
 // keeps the eight lanes of each quarter warp on distinct 16-byte bank groups
 // (index mod 8).  Prints the shared-memory wavefronts of one warp's gathers
 // per slot against the minimum of 4.
@@ -49,6 +50,11 @@ mb::HopTable hops(int L, int n, const std::vector<std::pair<int, int>>& bonds, b
   return t;
 }
 
+// entry of slot j, lane l in a group starting at base
+uint32_t at(const mb::SlicedTable& s, int32_t base, int j, int l) {
+  return s.ent[(size_t)base + 128 * (size_t)(j >> 2) + 4 * (size_t)l + (size_t)(j & 3)];
+}
+
 int check(const char* name, int L, int n, const std::vector<std::pair<int, int>>& bonds,
           bool double_some, double max_ratio) {
   const mb::HopTable t = hops(L, n, bonds, double_some);
@@ -58,6 +64,10 @@ int check(const char* name, int L, int n, const std::vector<std::pair<int, int>>
   long long wave = 0, ideal = 0;
   for (int64_t g = 0; g < ng; ++g) {
     const int32_t base = s.grp[(size_t)(2 * g)], k = s.grp[(size_t)(2 * g + 1)];
+    if (base % 4) {
+      std::printf("%s: group %lld not 16-byte aligned\n", name, (long long)g);
+      return 1;
+    }
     for (int l = 0; l < 32; ++l) {
       const int64_t c = 32 * g + l;
       std::multiset<uint32_t> want, got;
@@ -71,8 +81,8 @@ int check(const char* name, int L, int n, const std::vector<std::pair<int, int>>
           nneg += (int)(e & 1u) * mult;
         }
       }
-      for (int j = 0; j < k; ++j) {
-        const uint32_t w = s.ent[(size_t)base + 32 * (size_t)j + (size_t)l];
+      for (int j = 0; j < ((k + 3) & ~3); ++j) {
+        const uint32_t w = at(s, base, j, l);
         const uint32_t idx = w & 0x7FFFFFFFu;
         if (idx >= (uint32_t)D) {
           if (w >> 31 || idx >= (uint32_t)(D + mb::kSlicedPads)) {
@@ -92,7 +102,7 @@ int check(const char* name, int L, int n, const std::vector<std::pair<int, int>>
       for (int q = 0; q < 4; ++q) {
         std::map<uint32_t, std::set<uint32_t>> banks;
         for (int l = 8 * q; l < 8 * q + 8; ++l) {
-          const uint32_t idx = s.ent[(size_t)base + 32 * (size_t)j + (size_t)l] & 0x7FFFFFFFu;
+          const uint32_t idx = at(s, base, j, l) & 0x7FFFFFFFu;
           banks[idx & 7u].insert(idx);
         }
         size_t worst = 0;
