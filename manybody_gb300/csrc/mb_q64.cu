@@ -232,7 +232,7 @@ k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlon
         return __ldg(reinterpret_cast<const longlong2*>(xc + (uint64_t)s_up[k] * row_bytes));
       };
       int j = 0;
-#pragma unroll 2
+#pragma unroll 4
       for (; j + 2 <= npos; j += 2) {
         const longlong2 v0 = up_val(j), v1 = up_val(j + 1);
         sr += v0.x + v1.x;
@@ -244,7 +244,7 @@ k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlon
         si += v0.y;
       }
       j = npos;
-#pragma unroll 2
+#pragma unroll 4
       for (; j + 2 <= nu; j += 2) {
         const longlong2 v0 = up_val(j), v1 = up_val(j + 1);
         sr -= v0.x + v1.x;

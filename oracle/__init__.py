@@ -47,6 +47,10 @@ def lib():
                                              C.c_int, _i64p, _i64p, _dp, _dp, C.c_int64]
         L.or_csc_apply.restype = None
         L.or_csc_apply.argtypes = [C.c_int64, _i64p, _i64p, _dp, _dp, _dp, _dp]
+        L.or_csc_apply_hermitian_parallel.restype = None
+        L.or_csc_apply_hermitian_parallel.argtypes = [C.c_int64, _i64p, _i64p, _dp, _dp, _dp, _dp]
+        L.or_max_threads.restype = C.c_int
+        L.or_max_threads.argtypes = []
         L.or_philox_uniform_pm1.restype = None
         L.or_philox_uniform_pm1.argtypes = [C.c_uint64, C.c_uint32, C.c_int64, _dp]
         L.or_philox_phase.restype = None
@@ -119,6 +123,15 @@ class CscMatrix:
         lib().or_csc_apply(*self._args(), _p(x.view(np.float64), _dp), _p(y.view(np.float64), _dp))
         return y
 
+    def apply_parallel(self, x: np.ndarray) -> np.ndarray:
+        """Multi-core row gather for Hermitian H (column i is the conjugate of
+        row i): best-effort CPU context, not the reference's serial scatter."""
+        x = np.ascontiguousarray(x, np.complex128)
+        y = np.empty(self.dim, np.complex128)
+        lib().or_csc_apply_hermitian_parallel(*self._args(), _p(x.view(np.float64), _dp),
+                                              _p(y.view(np.float64), _dp))
+        return y
+
     def to_dense(self) -> np.ndarray:
         H = np.zeros((self.dim, self.dim), np.complex128)
         for j in range(self.dim):
@@ -181,6 +194,11 @@ def hubbard_csc(dims, t, U, nup, ndn) -> CscMatrix:
                                        _p(row_idx, _i64p), _p(re, _dp), _p(im, _dp), nnz)
     assert got == nnz
     return CscMatrix(dim, col_ptr, row_idx[:nnz], re[:nnz], im[:nnz])
+
+
+def max_threads() -> int:
+    """OpenMP threads the oracle's parallel loops use."""
+    return int(lib().or_max_threads())
 
 
 def philox_uniform(seed: int, n: int, stream: int = 0) -> np.ndarray:

@@ -21,6 +21,9 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define OR_TYPE_BIT 0x8000u
 #define OR_SPIN_BIT 0x4000u
@@ -441,6 +444,36 @@ void or_csc_apply(int64_t dim, const int64_t* col_ptr, const int64_t* row_idx, c
       y[2 * i + 1] += re[p] * xi + im[p] * xr;
     }
   }
+}
+
+/* Best-effort multi-core y = H x for a Hermitian H held as CSC: column i of H
+ * is the conjugate of row i, so y_i = sum_p conj(H_{row(p), i}) x_{row(p)}
+ * over column i's entries, a gather that splits over rows with no write
+ * conflicts.  Not the reference's algorithm (Armadillo's serial column
+ * scatter, or_csc_apply above); a multi-core CPU figure for context. */
+void or_csc_apply_hermitian_parallel(int64_t dim, const int64_t* col_ptr, const int64_t* row_idx,
+                                     const double* re, const double* im, const double* x,
+                                     double* y) {
+#pragma omp parallel for schedule(static, 1024)
+  for (int64_t i = 0; i < dim; ++i) {
+    double yr = 0.0, yi = 0.0;
+    for (int64_t p = col_ptr[i]; p < col_ptr[i + 1]; ++p) {
+      const int64_t j = row_idx[p];
+      const double xr = x[2 * j], xi = x[2 * j + 1];
+      yr += re[p] * xr + im[p] * xi;
+      yi += re[p] * xi - im[p] * xr;
+    }
+    y[2 * i] = yr;
+    y[2 * i + 1] = yi;
+  }
+}
+
+int or_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
 }
 
 /* ------------------------------------------------------------------------ */
