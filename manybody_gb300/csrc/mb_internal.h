@@ -351,6 +351,12 @@ struct mb_op_s {
   int32_t* iperm = nullptr;        // reference -> tensor index (lazy)
   std::mutex mu;
   std::mutex host_mu;  // host-buffer calls: one at a time (shared staging, stream 0)
+  // Pipelined host-buffer apply (MB_PREC_Q64, reference order): the row
+  // schedule split into rows whose up state holds orbital 0 (reference
+  // indices [0, rows_a * Dd)) and the rest; two non-blocking streams.
+  int32_t* split_sched = nullptr;
+  int64_t split_rows_a = 0;
+  cudaStream_t host_streams[2] = {nullptr, nullptr};
   struct Scratch {
     void* a = nullptr;  // tensor-order copies for reference-order calls
     void* b = nullptr;

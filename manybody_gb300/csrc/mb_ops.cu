@@ -19,6 +19,8 @@ namespace mb {
 // Q64 hooks (mb_q64_ops.cu)
 void q_op_prepare(mb_op_s* op, const mb_model_s* m, const HopTable& tu, const HopTable& td);
 void q_op_release(mb_op_s* op);
+void q_apply_host_reference(mb_op_s* op, const void* x_host, const void* x_mapped, void* y_host,
+                            void* y_mapped, void* x_stage, void* y_stage);
 void q_apply_affine(mb_op_s* op, const void* x, void* y, double scale, double shift, double beta,
                     const void* z, int order, cudaStream_t st);
 void q_eigenpair(mb_op_s* op, int64_t k, const void* seed, int order, const mb_lanczos_opts* opts,
@@ -195,6 +197,10 @@ static std::vector<int32_t> block_perm(const mb_basis_s& s) {
 }
 
 static void free_op_memory(mb_op_s* op) {
+  for (cudaStream_t& h : op->host_streams) {
+    if (h) cudaStreamDestroy(h);
+    h = nullptr;
+  }
   for (auto& kv : op->scratch) {
     for (void* p : {kv.second.a, kv.second.b, kv.second.hx, kv.second.hy})
       if (p) cudaFree(p);
@@ -924,7 +930,6 @@ int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
     // calls, or one thread's upload could land between another's copy and apply
     std::lock_guard<std::mutex> lk(op->host_mu);
     auto& s = scratch_for(op, st, 4);
-    MB_CUDA(cudaMemcpyAsync(s.hx, x_host, vb, cudaMemcpyHostToDevice, st));
     // A page-locked y (cudaHostAlloc / cudaHostRegister) is written in place by
     // the last kernel (the order / format change), so the result crosses the
     // host link once, while it is produced, instead of after a device copy.
@@ -934,6 +939,20 @@ int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
                         at.type == cudaMemoryTypeHost && at.devicePointer != nullptr;
     if (!direct) cudaGetLastError();  // clear a failed query on pageable memory
     if (direct) y_dev = at.devicePointer;
+    if (op->precision == MB_PREC_Q64 && order == MB_ORDER_REFERENCE && !op->natural_order &&
+        !op->view.n_blocks && !op->view.csr_row) {
+      // x lands in chunks, each scattered to tensor order while the next is
+      // in flight; the result's first reference block goes back while the
+      // rest of the apply runs
+      cudaPointerAttributes ax{};
+      const bool x_locked = cudaPointerGetAttributes(&ax, x_host) == cudaSuccess &&
+                            ax.type == cudaMemoryTypeHost && ax.devicePointer != nullptr;
+      if (!x_locked) cudaGetLastError();
+      q_apply_host_reference(op, x_host, x_locked ? ax.devicePointer : nullptr, y_host,
+                             direct ? at.devicePointer : nullptr, s.hx, s.hy);
+      return;
+    }
+    MB_CUDA(cudaMemcpyAsync(s.hx, x_host, vb, cudaMemcpyHostToDevice, st));
     apply_affine(op, s.hx, y_dev, 1.0, 0.0, 0.0, nullptr, order, st);
     if (!direct) MB_CUDA(cudaMemcpyAsync(y_host, s.hy, vb, cudaMemcpyDeviceToHost, st));
     MB_CUDA(cudaStreamSynchronize(st));

@@ -431,6 +431,38 @@ __global__ void k_from_fixed(int64_t n, const longlong2* __restrict__ src,
   }
 }
 
+// Reference-order chunk -> tensor order (dst[iperm[i]] = src[i]), with the
+// chunk's largest biased exponent folded into *emax: the landing step of a
+// host-buffer apply, run on each chunk while the next one is in flight.
+__global__ void k_scatter_maxexp(int64_t n, const double2* __restrict__ src,
+                                 const int32_t* __restrict__ iperm, double2* __restrict__ dst,
+                                 int* __restrict__ emax) {
+  int m = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = src[i];
+    dst[iperm[i]] = v;
+    const int ea = (int)(((unsigned long long)__double_as_longlong(v.x) >> 52) & 0x7FF);
+    const int eb = (int)(((unsigned long long)__double_as_longlong(v.y) >> 52) & 0x7FF);
+    m = max(m, max(ea, eb));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(emax, m);
+}
+
+// complex128 -> Q64 in place (the same 16 bytes per element)
+__global__ void k_to_fixed_inplace(int64_t n, void* buf, const int* __restrict__ ex) {
+  const int E = *ex;
+  double2* d = reinterpret_cast<double2*>(buf);
+  longlong2* q = reinterpret_cast<longlong2*>(buf);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = d[i];
+    q[i] = make_longlong2(f64_to_fixed(v.x, E), f64_to_fixed(v.y, E));
+  }
+}
+
 // One-thread planner on the device (keeps mb_op_apply asynchronous).
 __global__ void k_plan(QPlanInput in, const int* __restrict__ ex, QParams* __restrict__ p) {
   in.ex = *ex;
@@ -445,6 +477,20 @@ void launch_f64_to_q(int64_t n, const void* src, const int32_t* perm, int qbits,
   k_exp_from_max<<<1, 1, 0, st>>>(scratch_int2, qbits, scratch_int2 + 1);
   k_to_fixed<<<q_blas_grid(n), kQBlas, 0, st>>>(n, (const double2*)src, perm, scratch_int2 + 1,
                                                  (longlong2*)dst);
+  MB_CUDA(cudaGetLastError());
+}
+
+void launch_scatter_maxexp(int64_t n, const void* src, const int32_t* iperm, void* dst,
+                           int* emax, cudaStream_t st) {
+  if (n <= 0) return;
+  k_scatter_maxexp<<<q_blas_grid(n), kQBlas, 0, st>>>(n, (const double2*)src, iperm,
+                                                       (double2*)dst, emax);
+  MB_CUDA(cudaGetLastError());
+}
+
+void launch_f64_to_q_inplace(int64_t n, void* buf, int qbits, int* scratch_int2, cudaStream_t st) {
+  k_exp_from_max<<<1, 1, 0, st>>>(scratch_int2, qbits, scratch_int2 + 1);
+  k_to_fixed_inplace<<<q_blas_grid(n), kQBlas, 0, st>>>(n, buf, scratch_int2 + 1);
   MB_CUDA(cudaGetLastError());
 }
 

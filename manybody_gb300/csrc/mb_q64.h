@@ -52,6 +52,13 @@ int q_multi_dot_grid(int64_t n);
 // (max biased exponent, resulting E).
 void launch_f64_to_q(int64_t n, const void* src, const int32_t* perm, int qbits, int* scratch_int2,
                      void* dst, cudaStream_t st);
+// dst[iperm[i]] = src[i] for a reference-order complex128 chunk, its largest
+// biased exponent folded into *emax (atomic max; zero it before the first).
+void launch_scatter_maxexp(int64_t n, const void* src, const int32_t* iperm, void* dst,
+                           int* emax, cudaStream_t st);
+// complex128 -> Q64 in place, the exponent from scratch_int2[0] (the largest
+// biased exponent) written to scratch_int2[1].
+void launch_f64_to_q_inplace(int64_t n, void* buf, int qbits, int* scratch_int2, cudaStream_t st);
 // Q64 (tensor order) -> FP64; with iperm (reference -> tensor index) the
 // output is in reference order.
 void launch_q_to_f64(int64_t n, const void* src, const int32_t* iperm, const int* e_dev, void* dst,

@@ -129,6 +129,138 @@ void q_apply_affine(mb_op_s* op, const void* x, void* y, double scale, double sh
 }
 
 // ---------------------------------------------------------------------------
+// The host-buffer apply in reference order, pipelined over the host link.
+//
+// The reference order lists first every state whose up configuration holds
+// orbital 0 (its operator (0, up) sorts before all others): reference indices
+// [0, rows_a * Dd) are exactly the tensor rows r_up with bit 0 set, all
+// columns.  So the apply runs those rows first, and their results go back to
+// the host on the copy engine while the remaining rows are computed.  On the
+// way in, a page-locked x is read over the link by the kernel that scatters it
+// to tensor order (with its largest exponent); a pageable x arrives in chunks,
+// each scattered while the next one is in flight.  The vector is converted to
+// Q64 in place once all of it has landed.  The arithmetic
+// is that of mb_op_apply (same exponent, same kernel per row), so the result
+// is bit-identical to the device-buffer call.
+// ---------------------------------------------------------------------------
+static void ensure_host_split(mb_op_s* op) {
+  std::lock_guard<std::mutex> lk(op->mu);
+  if (op->split_sched) return;
+  const int64_t Du = op->Du;
+  std::vector<int32_t> sched((size_t)Du);
+  std::vector<uint32_t> um((size_t)Du);
+  if (op->view.row_sched) {
+    MB_CUDA(cudaMemcpy(sched.data(), op->view.row_sched, sizeof(int32_t) * (size_t)Du,
+                       cudaMemcpyDeviceToHost));
+  } else {
+    for (int64_t r = 0; r < Du; ++r) sched[(size_t)r] = (int32_t)r;
+  }
+  MB_CUDA(cudaMemcpy(um.data(), op->view.up_mask, sizeof(uint32_t) * (size_t)Du,
+                     cudaMemcpyDeviceToHost));
+  std::vector<int32_t> split;
+  split.reserve((size_t)Du);
+  for (int32_t r : sched)
+    if (um[(size_t)r] & 1u) split.push_back(r);
+  const int64_t rows_a = (int64_t)split.size();
+  for (int32_t r : sched)
+    if (!(um[(size_t)r] & 1u)) split.push_back(r);
+  void* p = nullptr;
+  MB_CUDA(cudaMalloc(&p, sizeof(int32_t) * (size_t)std::max<int64_t>(Du, 1)));
+  op->allocations.push_back(p);
+  MB_CUDA(cudaMemcpy(p, split.data(), sizeof(int32_t) * (size_t)Du, cudaMemcpyHostToDevice));
+  for (cudaStream_t& h : op->host_streams)
+    if (!h) MB_CUDA(cudaStreamCreateWithFlags(&h, cudaStreamNonBlocking));
+  op->split_rows_a = rows_a;
+  op->split_sched = (int32_t*)p;
+}
+
+namespace {
+struct Events {
+  std::vector<cudaEvent_t> ev;
+  explicit Events(int n) : ev((size_t)n, nullptr) {
+    for (auto& e : ev) MB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  ~Events() {
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+  cudaEvent_t operator[](int i) const { return ev[(size_t)i]; }
+};
+}  // namespace
+
+void q_apply_host_reference(mb_op_s* op, const void* x_host, const void* x_mapped, void* y_host,
+                            void* y_mapped, void* x_stage, void* y_stage) {
+  ensure_host_split(op);
+  cudaStream_t comp = op->host_streams[0], copy = op->host_streams[1];
+  auto& q = qscratch_for(op, comp);
+  int32_t* iperm = op_iperm(op);
+  const int64_t n = op->dim;
+  const int64_t n_a = op->split_rows_a * op->Dd;  // reference indices [0, n_a)
+  constexpr size_t es = sizeof(double2);
+  constexpr int kChunks = 8;    // pageable x: upload chunks
+  constexpr int kPieces = 4;    // first block: gather / download pieces
+  Events ev(kChunks + kPieces + 1);
+  MB_CUDA(cudaMemsetAsync(q.ints, 0, sizeof(int), comp));
+  if (x_mapped) {
+    // page-locked x: the scatter kernel reads it over the link directly
+    launch_scatter_maxexp(n, x_mapped, iperm, q.xq, q.ints, comp);
+  } else {
+    const int64_t step = (n + kChunks - 1) / kChunks;
+    for (int c = 0; c < kChunks; ++c) {
+      const int64_t i0 = std::min<int64_t>(n, c * step), i1 = std::min<int64_t>(n, i0 + step);
+      if (i1 > i0)
+        MB_CUDA(cudaMemcpyAsync((char*)x_stage + es * (size_t)i0,
+                                (const char*)x_host + es * (size_t)i0, es * (size_t)(i1 - i0),
+                                cudaMemcpyHostToDevice, copy));
+      MB_CUDA(cudaEventRecord(ev[c], copy));
+      MB_CUDA(cudaStreamWaitEvent(comp, ev[c], 0));
+      launch_scatter_maxexp(i1 - i0, (const char*)x_stage + es * (size_t)i0, iperm + i0, q.xq,
+                            q.ints, comp);
+    }
+  }
+  launch_f64_to_q_inplace(n, q.xq, op->q_qbits, q.ints, comp);
+  launch_q_plan(plan_input(op, 1.0, 0.0, 0.0, 0, 0, false), q.ints + 1, (QParams*)q.prm, comp);
+  const int* ey = (const int*)((const char*)q.prm + offsetof(QParams, ey));
+  OpView va = op->view, vb = op->view;
+  va.row_sched = op->split_sched;
+  va.Du = op->split_rows_a;
+  vb.row_sched = op->split_sched + op->split_rows_a;
+  vb.Du = op->Du - op->split_rows_a;
+  if (va.Du > 0)
+    launch_apply_q(va, q.xq, q.yq, nullptr, (const QParams*)q.prm, nullptr, nullptr, 0, comp);
+  // the first block back in pieces: each piece's download starts as soon as
+  // it is gathered, and runs on the copy engine while the rest is computed
+  const int64_t piece = (n_a + kPieces - 1) / kPieces;
+  for (int k = 0; k < kPieces; ++k) {
+    const int64_t i0 = std::min<int64_t>(n_a, k * piece), i1 = std::min<int64_t>(n_a, i0 + piece);
+    if (i1 > i0)
+      launch_q_to_f64(i1 - i0, q.yq, iperm + i0, ey, (char*)y_stage + es * (size_t)i0, comp);
+    MB_CUDA(cudaEventRecord(ev[kChunks + k], comp));
+  }
+  if (vb.Du > 0)
+    launch_apply_q(vb, q.xq, q.yq, nullptr, (const QParams*)q.prm, nullptr, nullptr, 0, comp);
+  // the rest straight into a page-locked y (over the link as it is produced),
+  // or into the staging buffer for a copy
+  void* y_b = y_mapped ? (char*)y_mapped + es * (size_t)n_a : (char*)y_stage + es * (size_t)n_a;
+  if (n > n_a) launch_q_to_f64(n - n_a, q.yq, iperm + n_a, ey, y_b, comp);
+  MB_CUDA(cudaEventRecord(ev[kChunks + kPieces], comp));
+  for (int k = 0; k < kPieces; ++k) {
+    const int64_t i0 = std::min<int64_t>(n_a, k * piece), i1 = std::min<int64_t>(n_a, i0 + piece);
+    MB_CUDA(cudaStreamWaitEvent(copy, ev[kChunks + k], 0));
+    if (i1 > i0)
+      MB_CUDA(cudaMemcpyAsync((char*)y_host + es * (size_t)i0, (char*)y_stage + es * (size_t)i0,
+                              es * (size_t)(i1 - i0), cudaMemcpyDeviceToHost, copy));
+  }
+  if (!y_mapped && n > n_a) {
+    MB_CUDA(cudaStreamWaitEvent(copy, ev[kChunks + kPieces], 0));
+    MB_CUDA(cudaMemcpyAsync((char*)y_host + es * (size_t)n_a, (char*)y_stage + es * (size_t)n_a,
+                            es * (size_t)(n - n_a), cudaMemcpyDeviceToHost, copy));
+  }
+  MB_CUDA(cudaStreamSynchronize(copy));
+  MB_CUDA(cudaStreamSynchronize(comp));
+}
+
+// ---------------------------------------------------------------------------
 // Q64 Krylov machinery.
 // ---------------------------------------------------------------------------
 namespace {

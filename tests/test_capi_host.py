@@ -104,3 +104,17 @@ def test_gpu_calls_fail_loudly_without_device(mb):
     with pytest.raises(mb.MbError) as e:
         mb.GpuHubbardOperator(b, m)
     assert e.value.status == mb.MB_ERR_NO_DEVICE
+
+
+@pytest.mark.parametrize("L,nu,nd", [(12, 4, 4), (9, 3, 2), (8, 1, 4), (6, 0, 3), (5, 5, 2)])
+def test_reference_order_leads_with_orbital_zero_up(mb, L, nu, nd):
+    """The pipelined host-buffer apply returns the reference indices
+    [0, C(L-1, N_up-1) * D_down) first: exactly the states whose up
+    configuration holds orbital 0 (the operator (0, up) sorts first)."""
+    from math import comb
+    basis = mb.FermionBasis.with_fixed_particle_number_and_spin(L, nu + nd, nu - nd)
+    up, dn = basis.keys()
+    n_a = (comb(L - 1, nu - 1) if nu > 0 else 0) * comb(L, nd)
+    holds = (up & np.uint64(1)) != 0
+    assert holds[:n_a].all() and not holds[n_a:].any()
+    assert int(holds.sum()) == n_a

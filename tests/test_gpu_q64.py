@@ -49,6 +49,15 @@ def test_q64_apply_matches_reference_csr(mb, cuda, name):
     perm = op.basis.permutation()
     yt = op.apply(torch.tensor(x[perm], device="cuda"), order=mb.ORDER_TENSOR).cpu().numpy()
     assert np.linalg.norm(yt - y_ref[perm]) <= 1e-13 * scale + 1e-300
+    # host buffers (pipelined: chunked upload, split row schedule): the same
+    # arithmetic as the device call, so bit-identical; pageable and page-locked
+    yh = np.zeros(n, np.complex128)
+    op.apply_host(x, yh)
+    assert np.array_equal(yh, y)
+    xp = torch.tensor(x).pin_memory()
+    yp = torch.zeros(n, dtype=torch.complex128).pin_memory()
+    op.apply_host(xp, yp)
+    assert np.array_equal(yp.numpy(), y)
 
 
 def test_q64_roundtrip_and_native_apply(mb, cuda):
@@ -164,3 +173,20 @@ def test_q64_full_size_4x4_matches_f64(mb, cuda):
     y = opq.q64_to_f64(yq, ey, order=mb.ORDER_TENSOR)
     rel = float(torch.linalg.norm(y - y64)) / float(torch.linalg.norm(y64))
     assert rel <= 1e-13
+
+
+def test_q64_host_apply_full_size_bit_identical(mb, cuda):
+    """4x4, 6+6: the pipelined host-buffer apply (page-locked buffers) equals
+    the device-buffer apply in reference order bit for bit."""
+    torch = cuda
+    basis = mb.FermionBasis.with_fixed_particle_number_and_spin(16, 12, 0)
+    model = mb.HubbardModel2D(1.0, 8.0, 4, 4)
+    op = mb.GpuHubbardOperator(basis, model, mb.PREC_Q64)
+    x = op.seed_vector(3)
+    y = op.apply(x).cpu()
+    xh = x.cpu().pin_memory()
+    yh = torch.empty_like(xh).pin_memory()
+    op.apply_host(xh, yh)
+    assert torch.equal(yh, y)
+    del x, y
+    torch.cuda.empty_cache()
