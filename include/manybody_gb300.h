@@ -128,7 +128,12 @@ int mb_hubbard_create(const int64_t* dims, int ndim, double t, double u, mb_mode
  * orbitals (same lattice indexing).  With a momentum-sector basis it gives
  * the sector's H: mb_compute_matrix_elements_csr (built on the GPU) and
  * mb_op_create (MB_PREC_F64 / MB_PREC_F32: the sector's H kept on the device
- * in signed-column sparse form; reference order). */
+ * in signed-column sparse form; reference order).  With a whole (N_up,
+ * N_down) basis (mb_basis_create_fixed_spin) it gives the operator of the
+ * reference's HubbardMomentumFactorized (src/numerics/
+ * hubbard_momentum_factorized.h:32-249, t sum eps(k) n_k + (U/N) sum_q
+ * rho_{q,up} rho_{-q,down}): block diagonal over the total momentum, one
+ * sector operator per K, in the whole basis's reference order. */
 int mb_hubbard_momentum_create(const int64_t* dims, int ndim, double t, double u,
                                mb_model_t* out);
 int mb_model_destroy(mb_model_t model);

@@ -9,6 +9,8 @@
 //   HubbardModel / 2D / 3D (t, u, sizes...)           mbgpu::HubbardModel / 2D / 3D
 //     (src/algebra/fermion/model/hubbard_model.h)
 //   HubbardModelMomentum (t, u, sizes)                mbgpu::HubbardModelMomentum
+//   HubbardMomentumFactorized (basis, sizes, t, U)    mbgpu::HubbardMomentumFactorized<V>
+//     (src/numerics/hubbard_momentum_factorized.h:32-249)
 //   compute_matrix_elements<sp_cx_mat>(basis, H)      mbgpu::compute_matrix_elements(basis, model)
 //     (src/algebra/matrix_elements.h:74-105)
 //   SparseComplexMatrixOperator (linear_operator.h:81-91)
@@ -209,6 +211,18 @@ class GpuHubbardOperator {
  private:
   mb_op_t h_ = nullptr;
   int64_t dim_ = 0;
+};
+
+// HubbardMomentumFactorized (src/numerics/hubbard_momentum_factorized.h:32-249):
+// the momentum-space Hubbard operator on a whole (N_up, N_down) basis,
+// constructed as the reference's (basis, lattice_size, t, U); on the GPU it
+// is block diagonal over the total momentum (one sector operator per K).
+template <class Vector>
+class HubbardMomentumFactorized : public GpuHubbardOperator<Vector> {
+ public:
+  HubbardMomentumFactorized(const FermionBasis& basis, const std::vector<size_t>& lattice_size,
+                            double t, double U, int precision = MB_PREC_F64)
+      : GpuHubbardOperator<Vector>(basis, HubbardModelMomentum(t, U, lattice_size), precision) {}
 };
 
 // Device-resident find_min_eigenpair (lanczos.h:283-290) from a device seed

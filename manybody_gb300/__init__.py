@@ -341,7 +341,9 @@ class HubbardModel3D(_Hubbard):
 class HubbardModelMomentum(_Hubbard):
     """HubbardModelMomentum (src/algebra/fermion/model/hubbard_model_momentum.h:19-180):
     the Hubbard model on momentum orbitals; with a momentum-sector basis it
-    gives that sector's H (compute_matrix_elements, GpuHubbardOperator)."""
+    gives that sector's H (compute_matrix_elements, GpuHubbardOperator), with
+    a whole (N_up, N_down) basis the union of its sectors (the operator of
+    HubbardMomentumFactorized)."""
     _create = "mb_hubbard_momentum_create"
 
     def __init__(self, t, u, size):
@@ -628,6 +630,23 @@ class GpuHubbardOperator:
         r = C.c_double()
         _check(lib().mb_norm(self._h, _ptr(x), C.byref(r)))
         return r.value
+
+
+class HubbardMomentumFactorized(GpuHubbardOperator):
+    """HubbardMomentumFactorized (src/numerics/hubbard_momentum_factorized.h:32-249):
+    H = t sum_k eps(k) n_k + (U/N) sum_q rho_{q,up} rho_{-q,down} on a whole
+    (N_up, N_down) basis of momentum orbitals, constructed as the reference's
+    (basis, lattice_size, t, U).  On the GPU it is block diagonal over the
+    total momentum (one sector operator per K) in the basis's reference order;
+    every driver takes it."""
+
+    def __init__(self, basis: FermionBasis, lattice_size, t: float, U: float,
+                 precision: int = PREC_F64):
+        if not len(lattice_size):
+            raise MbError(MB_ERR_INVALID_ARG,
+                          "HubbardMomentumFactorized requires at least one dimension")
+        self.lattice_size = tuple(int(d) for d in lattice_size)
+        super().__init__(basis, HubbardModelMomentum(t, U, self.lattice_size), precision)
 
 
 class GpuSparseOperator(GpuHubbardOperator):

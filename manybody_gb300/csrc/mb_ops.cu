@@ -319,6 +319,99 @@ static void build_momentum(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m
   v.csr_off = m->u_over_n;
 }
 
+// A momentum-sector operator: natural (sector reference) order, signed-column
+// CSR on the device.
+static void build_momentum_op(mb_op_s* op, const mb_basis_s* basis, const mb_model_s* model) {
+  MB_REQUIRE(op->precision != MB_PREC_Q64, MB_ERR_INVALID_ARG,
+             "momentum-sector operators take MB_PREC_F64 or MB_PREC_F32");
+  MB_CUDA(cudaGetDevice(&op->device));
+  op->L = basis->L;
+  op->n_up = basis->n_up;
+  op->n_down = basis->n_down;
+  op->Du = basis->dim;
+  op->Dd = 1;
+  op->dim = basis->dim;
+  op->t = model->t;
+  op->u = model->u;
+  op->natural_order = true;
+  op->view.Du = basis->dim;
+  op->view.Dd = 1;
+  op->view.dim = basis->dim;
+  op->view.L = basis->L;
+  MomBuild mbld;
+  build_momentum(op, basis, model, mbld);
+}
+
+// The total-momentum sectors of a whole (N_up, N_down) basis on the model's
+// lattice, K in flat order (first dimension fastest); empty sectors skipped.
+static std::vector<std::unique_ptr<mb_basis_s>> momentum_sectors(const mb_basis_s* b,
+                                                                 const mb_model_s* m) {
+  const int ndim = (int)m->dims.size();
+  std::vector<std::unique_ptr<mb_basis_s>> out;
+  for (int64_t K = 0; K < b->L; ++K) {
+    int64_t kv[3] = {0, 0, 0}, rest = K;
+    for (int d = 0; d < ndim; ++d) {
+      kv[d] = rest % m->dims[(size_t)d];
+      rest /= m->dims[(size_t)d];
+    }
+    mb_basis_t h = nullptr;
+    const int rc = mb_basis_create_momentum(m->dims.data(), ndim, b->n_up + b->n_down,
+                                            b->n_up - b->n_down, kv, &h);
+    if (rc) throw Error(rc, mb_last_error());
+    std::unique_ptr<mb_basis_s> sec(h);
+    if (sec->dim > 0) out.push_back(std::move(sec));
+  }
+  return out;
+}
+
+// The momentum-space model on a whole (N_up, N_down) basis: the matrix the
+// reference's HubbardMomentumFactorized applies
+// (src/numerics/hubbard_momentum_factorized.h:32-249), H = t sum eps(k) n_k +
+// (U/N) sum_q rho_{q,up} rho_{-q,down}.  H conserves the total momentum, so
+// the operator is block diagonal: one sector operator per K on consecutive
+// slices, and the permutation to the whole basis's reference order is each
+// sector's list of full-basis reference ranks.
+static void build_momentum_all(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m) {
+  MB_REQUIRE(op->precision != MB_PREC_Q64, MB_ERR_INVALID_ARG,
+             "momentum-space operators take MB_PREC_F64 or MB_PREC_F32");
+  MB_CUDA(cudaGetDevice(&op->device));
+  op->L = b->L;
+  op->n_up = b->n_up;
+  op->n_down = b->n_down;
+  op->dim = b->dim;
+  op->Du = b->dim;
+  op->Dd = 1;
+  op->t = m->t;
+  op->u = m->u;
+  std::vector<int32_t> perm((size_t)b->dim);
+  int64_t off = 0;
+  for (auto& sec : momentum_sectors(b, m)) {
+    auto sub = std::make_unique<mb_op_s>();
+    sub->precision = op->precision;
+    try {
+      build_momentum_op(sub.get(), sec.get(), m);
+    } catch (...) {
+      free_op_memory(sub.get());
+      throw;
+    }
+    op->sub_views.push_back(sub->view);
+    op->subs.push_back(std::move(sub));
+    op->sub_offsets.push_back(off);
+    for (int64_t i = 0; i < sec->dim; ++i) perm[(size_t)(off + i)] = (int32_t)sec->kfull[(size_t)i];
+    off += sec->dim;
+  }
+  MB_REQUIRE(off == b->dim, MB_ERR_INVALID_ARG, "momentum sectors do not cover the basis");
+  OpView& v = op->view;
+  v.Du = b->dim;
+  v.Dd = 1;
+  v.dim = b->dim;
+  v.L = b->L;
+  v.n_blocks = (int)op->subs.size();
+  v.sub = op->sub_views.data();
+  v.sub_off = op->sub_offsets.data();
+  op->perm = upload(op, perm.empty() ? std::vector<int32_t>{0} : perm);
+}
+
 static mb_op_s::Scratch& scratch_for(mb_op_s* op, cudaStream_t st, int nvec) {
   std::lock_guard<std::mutex> lk(op->mu);
   auto& s = op->scratch[st];
@@ -802,25 +895,10 @@ int mb_op_create(mb_basis_t basis, mb_model_t model, int precision, mb_op_t* out
     try {
       if (basis->all_sz()) {
         build_all_sz(op.get(), basis, model);
+      } else if (model->momentum && !model->current && !basis->momentum()) {
+        build_momentum_all(op.get(), basis, model);
       } else if (basis->momentum() || model->momentum) {
-        MB_REQUIRE(precision != MB_PREC_Q64, MB_ERR_INVALID_ARG,
-                   "momentum-sector operators take MB_PREC_F64 or MB_PREC_F32");
-        MB_CUDA(cudaGetDevice(&op->device));
-        op->L = basis->L;
-        op->n_up = basis->n_up;
-        op->n_down = basis->n_down;
-        op->Du = basis->dim;
-        op->Dd = 1;
-        op->dim = basis->dim;
-        op->t = model->t;
-        op->u = model->u;
-        op->natural_order = true;
-        op->view.Du = basis->dim;
-        op->view.Dd = 1;
-        op->view.dim = basis->dim;
-        op->view.L = basis->L;
-        MomBuild mbld;
-        build_momentum(op.get(), basis, model, mbld);
+        build_momentum_op(op.get(), basis, model);
       } else {
         build_op(op.get(), basis, model);
       }
@@ -991,6 +1069,50 @@ int mb_fill_phase(mb_op_t op, uint64_t seed, uint32_t stream_id, void* v_dev, in
   });
 }
 
+// One momentum sector's H as CSR in the sector's reference order, each row's
+// columns ascending (off-diagonals +-U/N, the diagonal where non-zero).
+static void momentum_csr(const mb_basis_s* b, const mb_model_s* m, std::vector<int64_t>& rp,
+                         std::vector<int64_t>& cols, std::vector<double>& vals) {
+  mb_op_s tmp;
+  tmp.precision = MB_PREC_F64;
+  struct Cleanup {
+    mb_op_s& o;
+    ~Cleanup() {
+      for (void* p : o.allocations) cudaFree(p);
+    }
+  } cleanup{tmp};
+  MomBuild mb;
+  build_momentum(&tmp, b, m, mb);
+  const int64_t n = mb.n;
+  std::vector<int32_t> hcol((size_t)std::max<int64_t>(mb.nnz, 1));
+  std::vector<double> hdiag((size_t)std::max<int64_t>(n, 1));
+  if (mb.nnz) MB_CUDA(cudaMemcpy(hcol.data(), mb.col, sizeof(int32_t) * (size_t)mb.nnz, cudaMemcpyDeviceToHost));
+  if (n) MB_CUDA(cudaMemcpy(hdiag.data(), mb.diag, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost));
+  rp.assign((size_t)n + 1, 0);
+  for (int64_t i = 0; i < n; ++i)
+    rp[(size_t)i + 1] = rp[(size_t)i] + (mb.row_ptr[(size_t)i + 1] - mb.row_ptr[(size_t)i]) +
+                        (hdiag[(size_t)i] != 0.0 ? 1 : 0);
+  cols.resize((size_t)rp[(size_t)n]);
+  vals.resize((size_t)rp[(size_t)n]);
+  const double off = tmp.view.csr_off;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < n; ++i) {
+    std::vector<std::pair<int64_t, double>> row;
+    for (int64_t k = mb.row_ptr[(size_t)i]; k < mb.row_ptr[(size_t)i + 1]; ++k) {
+      const uint32_t e = (uint32_t)hcol[(size_t)k];
+      row.push_back({(int64_t)(e & 0x7FFFFFFFu), (e >> 31) ? -off : off});
+    }
+    if (hdiag[(size_t)i] != 0.0) row.push_back({i, hdiag[(size_t)i]});
+    std::sort(row.begin(), row.end());
+    int64_t o = rp[(size_t)i];
+    for (const auto& [c, v] : row) {
+      cols[(size_t)o] = c;
+      vals[(size_t)o] = v;
+      ++o;
+    }
+  }
+}
+
 int mb_compute_matrix_elements_csr(mb_basis_t basis, mb_model_t model, int64_t* nnz,
                                    int64_t* row_ptr, int64_t* col_idx, double* values) {
   return guard([&] {
@@ -1053,18 +1175,46 @@ int mb_compute_matrix_elements_csr(mb_basis_t basis, mb_model_t model, int64_t* 
       return;
     }
     if (basis->momentum() || model->momentum) {
-      MomBuild mb;
-      build_momentum(&tmp, basis, model, mb);
-      const int64_t n = mb.n;
-      std::vector<int32_t> hcol((size_t)std::max<int64_t>(mb.nnz, 1));
-      std::vector<double> hdiag((size_t)std::max<int64_t>(n, 1));
-      if (mb.nnz) MB_CUDA(cudaMemcpy(hcol.data(), mb.col, sizeof(int32_t) * (size_t)mb.nnz, cudaMemcpyDeviceToHost));
-      if (n) MB_CUDA(cudaMemcpy(hdiag.data(), mb.diag, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost));
-      std::vector<int64_t> rp((size_t)n + 1, 0);
-      for (int64_t i = 0; i < n; ++i)
-        rp[(size_t)i + 1] = rp[(size_t)i] + (mb.row_ptr[(size_t)i + 1] - mb.row_ptr[(size_t)i]) +
-                            (hdiag[(size_t)i] != 0.0 ? 1 : 0);
-      const int64_t total = rp[(size_t)n];
+      // a momentum sector, or the whole basis as the union of its sectors
+      // (rows and columns mapped to the whole basis's reference ranks)
+      MB_REQUIRE(basis->momentum() || !model->current, MB_ERR_INVALID_ARG,
+                 "the current operator maps between sectors: use "
+                 "mb_compute_rectangular_matrix_elements_csr");
+      std::vector<int64_t> rp, cols;
+      std::vector<double> vals;
+      if (basis->momentum()) {
+        momentum_csr(basis, model, rp, cols, vals);
+      } else {
+        const int64_t dim = basis->dim;
+        std::vector<std::vector<std::pair<int64_t, double>>> rows((size_t)dim);
+        for (auto& sec : momentum_sectors(basis, model)) {
+          std::vector<int64_t> srp, scol;
+          std::vector<double> sval;
+          momentum_csr(sec.get(), model, srp, scol, sval);
+          for (int64_t i = 0; i < sec->dim; ++i) {
+            auto& row = rows[(size_t)sec->kfull[(size_t)i]];
+            for (int64_t k = srp[(size_t)i]; k < srp[(size_t)i + 1]; ++k)
+              row.push_back({sec->kfull[(size_t)scol[(size_t)k]], sval[(size_t)k]});
+          }
+        }
+        rp.assign((size_t)dim + 1, 0);
+        for (int64_t i = 0; i < dim; ++i) {
+          auto& row = rows[(size_t)i];
+          std::sort(row.begin(), row.end());
+          rp[(size_t)i + 1] = rp[(size_t)i] + (int64_t)row.size();
+        }
+        cols.resize((size_t)rp[(size_t)dim]);
+        vals.resize((size_t)rp[(size_t)dim]);
+        for (int64_t i = 0; i < dim; ++i) {
+          int64_t o = rp[(size_t)i];
+          for (const auto& [c, v] : rows[(size_t)i]) {
+            cols[(size_t)o] = c;
+            vals[(size_t)o] = v;
+            ++o;
+          }
+        }
+      }
+      const int64_t total = rp.back();
       if (!col_idx) {
         *nnz = total;
         if (row_ptr) std::memcpy(row_ptr, rp.data(), sizeof(int64_t) * rp.size());
@@ -1072,23 +1222,10 @@ int mb_compute_matrix_elements_csr(mb_basis_t basis, mb_model_t model, int64_t* 
       }
       MB_REQUIRE(*nnz >= total, MB_ERR_CAPACITY, "nnz capacity smaller than the matrix");
       MB_REQUIRE(row_ptr && values, MB_ERR_INVALID_ARG, "NULL row_ptr or values");
-      const double off = tmp.view.csr_off;
-#pragma omp parallel for schedule(dynamic, 64)
-      for (int64_t i = 0; i < n; ++i) {
-        std::vector<std::pair<int64_t, double>> row;
-        for (int64_t k = mb.row_ptr[(size_t)i]; k < mb.row_ptr[(size_t)i + 1]; ++k) {
-          const uint32_t e = (uint32_t)hcol[(size_t)k];
-          row.push_back({(int64_t)(e & 0x7FFFFFFFu), (e >> 31) ? -off : off});
-        }
-        if (hdiag[(size_t)i] != 0.0) row.push_back({i, hdiag[(size_t)i]});
-        std::sort(row.begin(), row.end());
-        int64_t o = rp[(size_t)i];
-        for (const auto& [c, v] : row) {
-          col_idx[o] = c;
-          values[2 * o] = v;
-          values[2 * o + 1] = 0.0;
-          ++o;
-        }
+      for (int64_t k = 0; k < total; ++k) {
+        col_idx[k] = cols[(size_t)k];
+        values[2 * k] = vals[(size_t)k];
+        values[2 * k + 1] = 0.0;
       }
       std::memcpy(row_ptr, rp.data(), sizeof(int64_t) * rp.size());
       *nnz = total;

@@ -256,3 +256,63 @@ def expm_tridiag_first_column(alphas, betas, t, imaginary=False):
     if rc:
         raise RuntimeError("expm failed")
     return (yr + 1j * yi)[:n]
+
+
+def momentum_factorized_matrix(dims, t: float, U: float, up_masks, down_masks) -> np.ndarray:
+    """Dense H of the reference's HubbardMomentumFactorized
+    (src/numerics/hubbard_momentum_factorized.h:32-249) on the given basis
+    (occupation masks over momentum orbitals, reference order):
+    H = t diag(sum_k eps(k) n_k) + (U/N) sum_q rho_{q,up} rho_{-q,down}, with
+    eps(k) = -2 sum_d cos(2 pi k_d / L_d) (:107-133) and rho_{q,s} =
+    sum_k c+_{k+q,s} c_{k,s} built per column as :136-237 does: the key lists
+    the up creators then the down creators, each by ascending orbital; moving
+    k -> k+q costs (-1)^(op_idx + insert_pos).  Flat momentum index: first
+    dimension fastest (src/utils/index.h).  Pure Python, small bases only."""
+    dims = [int(d) for d in dims]
+    N = int(np.prod(dims))
+    strides = np.cumprod([1] + dims[:-1])
+
+    def coords(k):
+        return [(k // strides[d]) % dims[d] for d in range(len(dims))]
+
+    def flat(c):
+        return int(sum(c[d] * strides[d] for d in range(len(dims))))
+
+    def add(k, q, sign):
+        a, b = coords(k), coords(q)
+        return flat([(a[d] + sign * b[d]) % dims[d] for d in range(len(dims))])
+
+    eps = [-2.0 * sum(np.cos(2.0 * np.pi * c / dims[d]) for d, c in enumerate(coords(k)))
+           for k in range(N)]
+    keys = list(zip((int(u) for u in up_masks), (int(d) for d in down_masks)))
+    index = {k: i for i, k in enumerate(keys)}
+    n = len(keys)
+
+    def rho(q, spin):
+        R = np.zeros((n, n))
+        for j, (um, dm) in enumerate(keys):
+            mine = um if spin == 0 else dm
+            orbs = [o for o in range(N) if (mine >> o) & 1]
+            before = 0 if spin == 0 else bin(um).count("1")  # up creators precede down ones
+            for pos, k in enumerate(orbs):
+                kq = add(k, q, +1)
+                if kq == k:
+                    R[j, j] += 1.0
+                    continue
+                if (mine >> kq) & 1:
+                    continue
+                rest = mine & ~(1 << k)
+                insert = before + bin(rest & ((1 << kq) - 1)).count("1")
+                sign = -1.0 if (before + pos + insert) % 2 else 1.0
+                new = rest | (1 << kq)
+                key = (new, dm) if spin == 0 else (um, new)
+                if key in index:
+                    R[index[key], j] += sign
+        return R
+
+    H = np.diag([t * sum(eps[o] for o in range(N) if (um >> o) & 1) +
+                 t * sum(eps[o] for o in range(N) if (dm >> o) & 1) for um, dm in keys])
+    if abs(U) > 1e-15:
+        for q in range(N):
+            H = H + (U / N) * (rho(q, 0) @ rho(add(0, q, -1), 1))
+    return H

@@ -17,6 +17,12 @@
 //     FermionBasis::with_fixed_particle_number_spin_momentum
 //     (src/algebra/basis.cpp:128-185,304-356) and HubbardModelMomentum
 //     (src/algebra/fermion/model/hubbard_model_momentum.h:19-180).
+//   ref_dump --momentum-full <dims> <t> <U> <particles> <spin_projection> <out.bin>
+//     the momentum-space model on the whole (N_up, N_down) basis
+//     (with_fixed_particle_number_and_spin, every total momentum): the matrix
+//     the reference's HubbardMomentumFactorized applies
+//     (src/numerics/hubbard_momentum_factorized.h:32-249), as its own test
+//     builds it (tests/numerics/test_hubbard_momentum_factorized.cpp:54-130).
 //
 // Calls, unchanged, the reference's
 //   FermionBasis::with_fixed_particle_number_and_spin   (src/algebra/basis.cpp:91-126)
@@ -134,6 +140,13 @@ int main(int argc, char** argv) {
     shifted[6] = argv[6];
     argv = shifted;
   }
+  const bool momentum_full = argc == 8 && std::string(argv[1]) == "--momentum-full";
+  if (momentum_full) {  // the fixed-spin layout below, momentum-space model
+    static char* shifted[8];
+    for (int i = 0; i < 7; ++i) shifted[i] = argv[i + (i ? 1 : 0)];
+    argv = shifted;
+    argc = 7;
+  }
   const bool momentum = argc == 9 && std::string(argv[1]) == "--momentum";
   if (argc != 7 && !momentum) {
     std::fprintf(stderr,
@@ -159,6 +172,9 @@ int main(int argc, char** argv) {
     h = HubbardModelMomentum(t, u, dims).hamiltonian();
     basis = FermionBasis::with_fixed_particle_number_spin_momentum(orbitals, particles, sz,
                                                                    Index(dims), k);
+  } else if (momentum_full) {
+    h = HubbardModelMomentum(t, u, dims).hamiltonian();
+    basis = FermionBasis::with_fixed_particle_number_and_spin(orbitals, particles, sz);
   } else {
     if (dims.size() == 1) {
       h = HubbardModel(t, u, dims[0]).hamiltonian();

@@ -18,9 +18,16 @@ def pytest_configure(config):
 
 def golden_cases():
     """The real-space Hubbard sectors dumped from the reference (cereal_*
-    fixtures are cache-format pins, mom_* momentum-space sectors)."""
+    fixtures are cache-format pins, mom_* momentum-space sectors, mfull_*
+    the momentum-space model on whole bases)."""
     return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(f).startswith(("cereal_", "mom_", "cur_", "all_")))
+                  if not os.path.basename(f).startswith(("cereal_", "mom_", "cur_", "all_",
+                                                         "mfull_")))
+
+
+def momentum_full_cases():
+    """The momentum-space model on whole (N_up, N_down) bases, from the reference."""
+    return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "mfull_*.npz")))
 
 
 def all_sz_cases():

@@ -103,6 +103,14 @@ int main(int argc, char** argv) {
   const double e0 = mbgpu::find_min_eigenpair(op, 200, seed);
   std::printf("E0 = %.12f\n", e0);
   CHECK(std::fabs(e0 - (-4.603526299989141)) < 1e-9);
+  // HubbardMomentumFactorized, constructed as the reference's (basis, sizes,
+  // t, U): the real-space ground state, reached in another orbital basis
+  mbgpu::HubbardMomentumFactorized<CxVec> fact(basis, {8}, 1.0, 4.0);
+  CHECK(fact.dimension() == 4900);
+  mbgpu::check(mb_fill_uniform(fact.handle(), 0, 0, seed, MB_ORDER_REFERENCE, nullptr));
+  const double e0k = mbgpu::find_min_eigenpair(fact, 200, seed);
+  std::printf("E0 (momentum space) = %.12f\n", e0k);
+  CHECK(std::fabs(e0k - e0) < 1e-9);
   mb_free(seed);
   return 0;
 }

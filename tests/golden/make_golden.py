@@ -3,7 +3,8 @@
 The real-space sectors (CASES); as mom_*.npz, the momentum-space model on
 total-momentum sectors (MOMENTUM_CASES; their npz adds the K vector); as
 cur_*.npz, the current operator between two sectors (CURRENT_CASES); as
-all_*.npz, all spin projections (ALL_SZ_CASES).
+all_*.npz, all spin projections (ALL_SZ_CASES); as mfull_*.npz, the
+momentum-space model on a whole (N_up, N_down) basis (MOMENTUM_FULL_CASES).
 
 Runs oracle/_ref/ref_dump (built by oracle/build_ref.sh from the reference
 sources: its basis enumeration, HubbardModel{,2D,3D} and
@@ -73,6 +74,19 @@ MOMENTUM_CASES = [
     ("mom_cube2x2x2_n4_k101", "2x2x2", 1.0, 2.0, 4, 0, "1x0x1"),
 ]
 
+# Momentum-space model on the whole (N_up, N_down) basis, every total momentum
+# (ref_dump --momentum-full): the matrix HubbardMomentumFactorized applies.
+# (name, dims, t, U, particles, spin_projection)
+MOMENTUM_FULL_CASES = [
+    ("mfull_chain2_n2_t0", "2", 0.0, 3.0, 2, 0),      # interaction only
+    ("mfull_chain4_n2", "4", 1.0, 4.0, 2, 0),
+    ("mfull_chain6_n4_u0", "6", 1.5, 0.0, 4, 0),      # kinetic only
+    ("mfull_chain6_n3_sz1", "6", 1.0, -2.0, 3, 1),    # attractive U, 2 up + 1 down
+    ("mfull_sq2x2_n3_sz1", "2x2", 1.0, 2.0, 3, 1),
+    ("mfull_rect2x3_n4", "2x3", 1.0, 4.0, 4, 0),
+    ("mfull_sq3x3_n3_sz1", "3x3", 1.0, 8.0, 3, 1),
+]
+
 # All spin projections, real-space model (ref_dump --all): (name, dims, t, U, particles)
 ALL_SZ_CASES = [
     ("all_chain1_n1", "1", 1.0, 3.0, 1),
@@ -122,13 +136,15 @@ def dump_current(dims, t, n, sz, k, q, d):
     return n_terms, parts, rec
 
 
-def dump(dims, t, U, n, sz, momentum=None, all_sz=False):
+def dump(dims, t, U, n, sz, momentum=None, all_sz=False, momentum_full=False):
     with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
         path = f.name
     try:
         args = [dims, repr(t), repr(U), str(n), str(sz)]
         if momentum is not None:
             args = ["--momentum", *args, momentum]
+        if momentum_full:
+            args = ["--momentum-full", *args]
         if all_sz:
             args = ["--all", dims, repr(t), repr(U), str(n)]
         subprocess.run([REF_DUMP, *args, path], check=True)
@@ -166,6 +182,14 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), dims=np.array(dvec, np.int32),
                             t=t, U=U, particles=n, spin_projection=sz,
                             momentum=np.array(kvec, np.int32), n_terms=n_terms, up=up, down=dn,
+                            row=rec["r"].astype(np.int32), col=rec["c"].astype(np.int32),
+                            val=rec["re"].copy())
+        print(f"{name}: dim={len(up)} nnz={len(rec)} terms={n_terms}")
+    for name, dims, t, U, n, sz in MOMENTUM_FULL_CASES:
+        n_terms, up, dn, rec = dump(dims, t, U, n, sz, momentum_full=True)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"),
+                            dims=np.array([int(x) for x in dims.split("x")], np.int32), t=t, U=U,
+                            particles=n, spin_projection=sz, n_terms=n_terms, up=up, down=dn,
                             row=rec["r"].astype(np.int32), col=rec["c"].astype(np.int32),
                             val=rec["re"].copy())
         print(f"{name}: dim={len(up)} nnz={len(rec)} terms={n_terms}")

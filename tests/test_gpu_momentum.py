@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 import oracle
-from conftest import load_golden, momentum_cases
+from conftest import load_golden, momentum_cases, momentum_full_cases
 
 pytestmark = pytest.mark.gpu
 
@@ -103,6 +103,75 @@ def test_momentum_operator_rejects_q64_and_mixed_models(mb, cuda):
         mb.GpuHubbardOperator(b, mb.HubbardModelMomentum(1.0, 2.0, [4]), mb.PREC_Q64)
     with pytest.raises(mb.MbError):
         mb.GpuHubbardOperator(b, mb.HubbardModel(1.0, 2.0, 4))
-    with pytest.raises(mb.MbError):
-        mb.compute_matrix_elements(mb.FermionBasis.with_fixed_particle_number_and_spin(4, 2, 0),
-                                   mb.HubbardModelMomentum(1.0, 2.0, [4]))
+    with pytest.raises(mb.MbError):  # a whole basis as well: no Q64 for momentum space
+        mb.HubbardMomentumFactorized(mb.FermionBasis.with_fixed_particle_number_and_spin(4, 2, 0),
+                                     [4], 1.0, 2.0, mb.PREC_Q64)
+    with pytest.raises(mb.MbError):  # lattice of 4 sites, basis of 6 orbitals
+        mb.HubbardMomentumFactorized(mb.FermionBasis.with_fixed_particle_number_and_spin(6, 2, 0),
+                                     [4], 1.0, 2.0)
+
+
+def make_full(mb, g):
+    dims = [int(d) for d in g["dims"]]
+    basis = mb.FermionBasis.with_fixed_particle_number_and_spin(
+        int(np.prod(dims)), int(g["particles"]), int(g["spin_projection"]))
+    return basis, dims
+
+
+@pytest.mark.parametrize("name", momentum_full_cases())
+def test_whole_basis_momentum_matrix_matches_reference(mb, cuda, name):
+    """compute_matrix_elements of HubbardModelMomentum on a whole (N_up, N_down)
+    basis (the matrix of HubbardMomentumFactorized), union of the K sectors."""
+    g = load_golden(name)
+    basis, dims = make_full(mb, g)
+    H = mb.compute_matrix_elements(basis, mb.HubbardModelMomentum(float(g["t"]), float(g["U"]), dims))
+    rows = np.repeat(np.arange(H.dim), np.diff(H.row_ptr))
+    assert H.nnz == len(g["row"])
+    assert np.array_equal(rows, g["row"]) and np.array_equal(H.col_idx, g["col"])
+    off = rows != H.col_idx
+    assert np.array_equal(H.values.real[off], g["val"][off])
+    scale = max(np.abs(g["val"]).max(), 1.0)
+    assert np.max(np.abs(H.values.real[~off] - g["val"][~off]), initial=0.0) <= 1e-14 * scale
+    assert not H.values.imag.any()
+
+
+@pytest.mark.parametrize("name", momentum_full_cases())
+@pytest.mark.parametrize("prec,tol", [(0, 1e-13), (1, 2e-6)])
+def test_factorized_operator_apply(mb, cuda, name, prec, tol):
+    """HubbardMomentumFactorized(basis, lattice_size, t, U).apply against the
+    reference's matrix, on device and host buffers (reference order)."""
+    torch = cuda
+    g = load_golden(name)
+    basis, dims = make_full(mb, g)
+    op = mb.HubbardMomentumFactorized(basis, dims, float(g["t"]), float(g["U"]), prec)
+    n = op.dimension()
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)
+    dt = torch.complex64 if prec else torch.complex128
+    ref = ref_csr(g) @ x
+    scale = max(np.linalg.norm(ref), 1e-300)
+    y = op.apply(torch.tensor(x, dtype=dt, device="cuda")).cpu().numpy()
+    assert np.linalg.norm(y - ref) <= tol * scale
+    yh = np.zeros(n, np.complex64 if prec else np.complex128)
+    op.apply_host(x.astype(yh.dtype), yh)
+    assert np.linalg.norm(yh - ref) <= tol * scale
+
+
+def test_factorized_operator_spectrum_and_ground_state(mb, cuda):
+    """The factorized momentum-space operator is the real-space Hamiltonian in
+    another single-particle basis: 1D L=6, 2+2 spectra agree (dense), and at
+    3x3, 3+3 (7056 states) Lanczos on it gives the real-space ground state."""
+    dims = [6]
+    E_real = np.linalg.eigvalsh(oracle.hubbard_csc(dims, 1.0, 3.0, 2, 2).to_dense())
+    basis = mb.FermionBasis.with_fixed_particle_number_and_spin(6, 4, 0)
+    H = mb.compute_matrix_elements(basis, mb.HubbardModelMomentum(1.0, 3.0, dims))
+    E_mom = np.linalg.eigvalsh(H.to_scipy().toarray())
+    assert np.max(np.abs(E_mom - E_real)) <= 1e-10 * np.abs(E_real).max()
+    real = mb.GpuHubbardOperator(mb.FermionBasis.with_fixed_particle_number_and_spin(9, 6, 0),
+                                 mb.HubbardModel2D(1.0, 4.0, 3, 3))
+    e_real = mb.find_min_eigenpair(real, 200, reorth=True, want_vector=False).value
+    fact = mb.HubbardMomentumFactorized(mb.FermionBasis.with_fixed_particle_number_and_spin(9, 6, 0),
+                                        [3, 3], 1.0, 4.0)
+    assert fact.dimension() == 7056
+    e_fact = mb.find_min_eigenpair(fact, 200, reorth=True, want_vector=False).value
+    assert abs(e_fact - e_real) <= 1e-10 * abs(e_real)

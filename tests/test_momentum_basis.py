@@ -8,7 +8,8 @@ reference order and the term count, bit-exact.
 import numpy as np
 import pytest
 
-from conftest import load_golden, momentum_cases
+import oracle
+from conftest import load_golden, momentum_cases, momentum_full_cases
 
 
 def make(mb, g):
@@ -86,3 +87,26 @@ def test_all_spin_projection_basis_matches_reference(mb, name):
         assert b.index_of(int(up[i]), int(dn[i])) == i
     perm = b.permutation()
     assert np.array_equal(np.sort(perm), np.arange(len(up)))
+
+
+@pytest.mark.parametrize("name", momentum_full_cases())
+def test_factorized_restatement_matches_reference_matrix(mb, name):
+    """The oracle's restatement of HubbardMomentumFactorized (rho_q products
+    with the (-1)^(op_idx + insert_pos) rule) equals the reference's
+    compute_matrix_elements of HubbardModelMomentum on the whole basis (what
+    the reference's own test asserts), and the basis is the real-space one."""
+    g = load_golden(name)
+    n = len(g["up"])
+    H_ref = np.zeros((n, n))
+    H_ref[g["row"], g["col"]] = g["val"]
+    H = oracle.momentum_factorized_matrix(g["dims"], float(g["t"]), float(g["U"]), g["up"],
+                                          g["down"])
+    assert np.abs(H - H_ref).max() <= 1e-12 * max(1.0, np.abs(H_ref).max())
+    L = int(np.prod(g["dims"]))
+    basis = mb.FermionBasis.with_fixed_particle_number_and_spin(L, int(g["particles"]),
+                                                                int(g["spin_projection"]))
+    up, dn = basis.keys()
+    assert np.array_equal(up, g["up"].astype(np.uint64))
+    assert np.array_equal(dn, g["down"].astype(np.uint64))
+    model = mb.HubbardModelMomentum(float(g["t"]), float(g["U"]), [int(d) for d in g["dims"]])
+    assert model.term_count() == int(g["n_terms"])
