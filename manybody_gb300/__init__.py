@@ -716,6 +716,18 @@ def lanczos_pass_two(op: GpuHubbardOperator, b, decomp: LanczosDecomposition, y_
     return x
 
 
+def solve(op: GpuHubbardOperator, b, k: int, solver, order: int = ORDER_REFERENCE, out=None):
+    """solve (src/numerics/lanczos.h:220-237): pass one, y_k = solver(alphas,
+    betas) on the host, scaled by |b|, then pass two; zeros if no step ran."""
+    decomp = lanczos_pass_one(op, b, k, order=order)
+    if decomp.steps_taken == 0:
+        x = op.empty() if out is None else out
+        x.zero_()
+        return x
+    y = np.asarray(solver(decomp.alphas, decomp.betas), np.complex128) * decomp.b_norm
+    return lanczos_pass_two(op, b, decomp, y, order=order, out=out)
+
+
 @dataclass
 class EigenPair:
     value: float

@@ -397,3 +397,26 @@ def test_fp32_refinement_past_convergence(mb, cuda):
     assert raw.steps == 150
     assert abs(raw.value - e_ref) <= 1e-6 * abs(e_ref)
     assert abs(ref.value - e_ref) <= 1e-8 * abs(e_ref)
+
+
+def test_solve_linear_system(mb, cuda):
+    """solve(op, b, k, solver) (lanczos.h:220-237) with a tridiagonal solver
+    T y = e1: over the full Krylov space x = H^-1 b."""
+    torch = cuda
+    g = load_golden("rect2x3_n4")  # nonsingular: |eigenvalues| >= 0.089
+    _, _, op = make(mb, [2, 3], float(g["t"]), float(g["U"]), g["n_up"], g["n_down"])
+    n = op.dimension()
+    H = ref_csr(g).toarray()
+    rng = np.random.default_rng(4)
+    b = rng.normal(size=n) + 1j * rng.normal(size=n)
+
+    def tridiag_solve(a, be):
+        T = np.diag(a) + np.diag(be, 1) + np.diag(be, -1)
+        e1 = np.zeros(len(a))
+        e1[0] = 1.0
+        return np.linalg.solve(T, e1)
+
+    x = mb.solve(op, torch.tensor(b, device="cuda"), n, tridiag_solve).cpu().numpy()
+    assert np.linalg.norm(H @ x - b) <= 1e-7 * np.linalg.norm(b)
+    zero = mb.solve(op, torch.zeros(n, dtype=torch.complex128, device="cuda"), n, tridiag_solve)
+    assert not zero.abs().max().item()
