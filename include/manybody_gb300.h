@@ -393,6 +393,12 @@ int mb_engine_poll(mb_engine_t engine, int64_t request_id, int* done, double* e0
                    int64_t* steps, double* latency_s);
 /* Warps per block of the grouped kernels (2, 4, 8, 16): the autotuner's knob. */
 int mb_engine_set_warps(mb_engine_t engine, int warps_per_block);
+/* Requests on sectors of at least min_states states step through the fused
+ * complex64 apply (rows staged in shared memory, sliced tables), one launch
+ * per such request; smaller ones share the grouped warp-per-row kernels.
+ * Default 1,048,576 (a launch per large request pays off; many medium
+ * requests run faster together); 1 sends every request through it. */
+int mb_engine_set_fused_threshold(mb_engine_t engine, int64_t min_states);
 /* Times the grouped apply at each block shape on the current requests and
  * keeps the fastest; *chosen = warps per block, *ms = its time per apply. */
 int mb_engine_autotune(mb_engine_t engine, int* chosen, double* ms);

@@ -151,6 +151,7 @@ SIGNATURES = {
     "mb_engine_step_fixed": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "mb_engine_poll": (C.c_int, [_vp, _i64, C.POINTER(C.c_int), _dp, _dp, _i64p, _dp]),
     "mb_engine_set_warps": (C.c_int, [_vp, C.c_int]),
+    "mb_engine_set_fused_threshold": (C.c_int, [_vp, C.c_int64]),
     "mb_engine_autotune": (C.c_int, [_vp, C.POINTER(C.c_int), _dp]),
     "mb_dot_re": (C.c_int, [_vp, _vp, _vp, _dp]),
     "mb_norm": (C.c_int, [_vp, _vp, _dp]),
@@ -941,6 +942,10 @@ class Engine:
     def set_warps(self, w: int):
         _check(lib().mb_engine_set_warps(self._h, w))
 
+    def set_fused_threshold(self, min_states: int):
+        """Sectors of at least min_states states use the fused complex64 apply."""
+        _check(lib().mb_engine_set_fused_threshold(self._h, min_states))
+
     def autotune(self):
         w, ms = C.c_int(), C.c_double()
         _check(lib().mb_engine_autotune(self._h, C.byref(w), C.byref(ms)))
@@ -948,9 +953,11 @@ class Engine:
 
 
 def batch_ground_states(descs, seeds=None, kmax: int = 150, refine: bool = True,
-                        use_graph: bool = True, autotune: bool = True):
+                        use_graph: bool = True, autotune: bool = True, fused_threshold=None):
     """Fixed-length batched Lanczos for many sectors: returns [EngineResult]."""
     eng = Engine()
+    if fused_threshold is not None:
+        eng.set_fused_threshold(fused_threshold)
     seeds = seeds if seeds is not None else [0] * len(descs)
     ids = []
     for d, s in zip(descs, seeds):

@@ -56,12 +56,13 @@ struct SlotDesc {
   int mode;         // kModeIdle, kModeLanczos, kModeReplay
   int steps;        // pass-one steps taken (m)
   int item0, item1; // this slot's range of work items
+  int fused;        // applied by the fused kernel (large sectors), not k_eng_apply
 };
 
-constexpr int kModeIdle = 0;
-constexpr int kModeLanczos = 1;
-constexpr int kModeReplay = 2;
-constexpr int kModeCheb = 3;   // T_{k+1} = 2 Ht T_k - T_{k-1} (T_1 = Ht T_0)
+constexpr int kModeIdle = kEngIdle;
+constexpr int kModeLanczos = kEngLanczos;
+constexpr int kModeReplay = kEngReplay;
+constexpr int kModeCheb = kEngCheb;   // T_{k+1} = 2 Ht T_k - T_{k-1} (T_1 = Ht T_0)
 
 // ---------------------------------------------------------------------------
 // Kernels.  One warp per (slot, row) item; lanes stride over the row.
@@ -74,6 +75,7 @@ k_eng_apply(const SlotDesc* __restrict__ slots, const int2* __restrict__ items, 
   for (int it = blockIdx.x * WARPS + warp; it < n_items; it += gridDim.x * WARPS) {
     const int2 item = items[it];
     const SlotDesc& s = slots[item.x];
+    if (s.fused) continue;  // its partials come from the fused kernel
     const int k = s.k;
     const bool replay = s.mode == kModeReplay;
     const bool cheb = s.mode == kModeCheb;
@@ -522,6 +524,11 @@ struct mb_engine_s {
   std::vector<mb::SlotDesc> h_slots;
   int n_items = 0;
   bool dirty = true;
+  // slots of at least fused_min states step through the fused complex64
+  // apply (staged rows, sliced tables) instead of the warp-per-row kernel
+  int64_t fused_min = 1048576;
+  std::vector<std::pair<mb::OpView, mb::EngFusedArgs>> fused;
+  std::vector<std::unique_ptr<mb::EngBuf>> fused_scratch;
   cudaStream_t st = nullptr;
   ~mb_engine_s() {
     if (st) cudaStreamDestroy(st);
@@ -581,6 +588,26 @@ std::shared_ptr<TableSet> get_tables(mb_engine_s* e, const mb_sector_desc& d) {
 // Device bytes of one slot: 4 complex64 vectors plus 3 x kEngMaxK doubles.
 int64_t slot_bytes(int64_t dim) { return 4 * 8 * dim + 3 * 8 * kEngMaxK; }
 
+// The fused-apply view of a slot's sector (tables shared by its TableSet).
+OpView slot_view(const EngineSlot& s) {
+  const TableSet& ts = *s.tables;
+  OpView v = ts.fused;
+  v.Du = s.Du;
+  v.Dd = s.Dd;
+  v.dim = s.dim;
+  v.L = ts.basis.L;
+  v.up_mask = ts.up_mask;
+  v.dn_mask = ts.dn_mask;
+  v.up_off = ts.up_off;
+  v.up_ent = ts.up_ent;
+  v.dn_off = ts.dn_off;
+  v.dn_ent = ts.dn_ent;
+  v.max_up_degree = ts.max_up_deg;
+  v.max_dn_degree = ts.max_dn_deg;
+  v.t = s.t;
+  return v;
+}
+
 void rebuild(mb_engine_s* e) {
   if (!e->dirty) return;
   e->h_slots.clear();
@@ -612,12 +639,44 @@ void rebuild(mb_engine_s* e) {
     d.item0 = (int)items.size();
     for (int64_t r = 0; r < s.Du; ++r) items.push_back(make_int2((int)e->h_slots.size(), (int)r));
     d.item1 = (int)items.size();
+    d.fused = s.dim >= e->fused_min ? 1 : 0;
     e->h_slots.push_back(d);
   }
   e->n_items = (int)items.size();
   e->d_slots = std::make_unique<EngBuf>(sizeof(SlotDesc) * std::max<size_t>(e->h_slots.size(), 1));
   e->d_items = std::make_unique<EngBuf>(sizeof(int2) * std::max<size_t>(items.size(), 1));
   e->d_part = std::make_unique<EngBuf>(2 * sizeof(double) * std::max<size_t>(items.size(), 1));
+  // fused slots: device addresses of their step state in the new slot array
+  e->fused.clear();
+  e->fused_scratch.clear();
+  SlotDesc* dsl = (SlotDesc*)e->d_slots->p;
+  double* part = (double*)e->d_part->p;
+  for (size_t i = 0; i < e->h_slots.size(); ++i) {
+    const SlotDesc& d = e->h_slots[i];
+    if (!d.fused) continue;
+    const OpView v = slot_view(*e->slots[i]);
+    EngFusedArgs a{};
+    a.k = &dsl[i].k;
+    a.mode = &dsl[i].mode;
+    a.kmax = &dsl[i].kmax;
+    a.steps = &dsl[i].steps;
+    a.beta = d.beta;
+    a.ufold = dsl[i].ufold;
+    for (int q = 0; q < 3; ++q) a.buf[q] = d.buf[q];
+    a.t = d.t;
+    a.scale = d.scale;
+    a.cheb_a = &dsl[i].cheb_a;
+    a.cheb_b = &dsl[i].cheb_b;
+    a.part = part;
+    a.part2 = part + items.size();  // the second half of d_part, as step_kernels uses it
+    a.item0 = d.item0;
+    a.n_items = d.item1 - d.item0;
+    e->fused_scratch.push_back(
+        std::make_unique<EngBuf>(3 * sizeof(double) * (size_t)std::max(eng_fused_blocks(v), 1)));
+    a.scratch = (double*)e->fused_scratch.back()->p;
+    e->fused.push_back({v, a});
+  }
+  if (!e->fused.empty()) prepare_eng_fused();
   if (!items.empty())
     MB_CUDA(cudaMemcpyAsync(e->d_items->p, items.data(), sizeof(int2) * items.size(),
                             cudaMemcpyHostToDevice, e->st));
@@ -662,6 +721,7 @@ void step_kernels(mb_engine_s* e) {
   double* part2 = part + n;
   const int g = eng_grid(n, W);
   k_eng_apply<W><<<g, W * 32, 0, e->st>>>(ds, it, n, part, part2);
+  for (const auto& [v, a] : e->fused) launch_eng_fused(v, a, e->st);
   k_eng_seg_reduce<<<std::min(ns, 1024), 256, 0, e->st>>>(dsm, ns, part, part2, 0);
   k_eng_update<W><<<g, W * 32, 0, e->st>>>(ds, it, n, part);
   k_eng_replay_update<W><<<g, W * 32, 0, e->st>>>(ds, it, n);
@@ -718,20 +778,7 @@ double ritz_min(const std::vector<double>& a, const std::vector<double>& b, int 
 // FP64 Rayleigh quotient of the slot's Ritz vector on an FP64 operator view.
 double rayleigh_fp64(mb_engine_s* e, EngineSlot& s, const SlotDesc& d) {
   const TableSet& ts = *s.tables;
-  OpView v = ts.fused;
-  v.Du = s.Du;
-  v.Dd = s.Dd;
-  v.dim = s.dim;
-  v.L = ts.basis.L;
-  v.up_mask = ts.up_mask;
-  v.dn_mask = ts.dn_mask;
-  v.up_off = ts.up_off;
-  v.up_ent = ts.up_ent;
-  v.dn_off = ts.dn_off;
-  v.dn_ent = ts.dn_ent;
-  v.max_up_degree = ts.max_up_deg;
-  v.max_dn_degree = ts.max_dn_deg;
-  v.t = s.t;
+  OpView v = slot_view(s);
   const std::vector<double> uf = u_fold_table(s.u, !(s.u * s.u < kTol * kTol), ts.basis.L);
   EngBuf duf(sizeof(double) * uf.size());
   MB_CUDA(cudaMemcpy(duf.p, uf.data(), sizeof(double) * uf.size(), cudaMemcpyHostToDevice));
@@ -1098,6 +1145,30 @@ int mb_engine_poll(mb_engine_t eng, int64_t id, int* done, double* e0, double* e
     if (e0_raw) *e0_raw = s.e_raw;
     if (steps) *steps = s.m;
     if (latency_s) *latency_s = std::chrono::duration<double>(s.t_done - s.t_submit).count();
+  });
+}
+
+int mb_engine_set_fused_threshold(mb_engine_t eng, int64_t min_states) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e && min_states >= 1, MB_ERR_INVALID_ARG, "NULL engine or threshold below 1");
+    // mid-run changes keep each slot's progress: only the kernel that applies it changes
+    if (!e->h_slots.empty()) fetch_slots(e);
+    const std::vector<SlotDesc> old = e->h_slots;
+    e->fused_min = min_states;
+    e->dirty = true;
+    rebuild(e);
+    for (auto& nd : e->h_slots)
+      for (auto& od : old)
+        if (od.buf[0] == nd.buf[0]) {
+          nd.k = od.k;
+          nd.mode = od.mode;
+          nd.steps = od.steps;
+          nd.kmax = od.kmax;
+          nd.cheb_a = od.cheb_a;
+          nd.cheb_b = od.cheb_b;
+        }
+    push_slots(e);
   });
 }
 

@@ -329,6 +329,33 @@ struct OpView {
 // Fills the tables of the fused applies (row schedule, sign-sorted up lists,
 // sliced down table) into v; `upload` copies host bytes to the device and
 // returns the device address.
+// Engine slot modes (device side of mb_engine.cu's batched solves).
+enum EngMode { kEngIdle = 0, kEngLanczos = 1, kEngReplay = 2, kEngCheb = 3 };
+
+// One large engine slot applied by the fused complex64 kernel: device
+// addresses of the slot's step state (read every step) and its fixed data.
+struct EngFusedArgs {
+  const int* k;
+  const int* mode;
+  const int* kmax;
+  const int* steps;
+  const double* beta;   // beta[k - 1] scales v_prev
+  const float* ufold;   // [L + 1] U fold of the slot
+  float2* buf[3];       // v_prev = buf[k % 3], v = buf[(k + 1) % 3], w = buf[(k + 2) % 3]
+  const float* cheb_a;  // Chebyshev rescaling (H - b) / a of the current probe
+  const float* cheb_b;
+  float t, scale;
+  double* part;         // per-item partials of the engine (Re<v,w>)
+  double* part2;        // (<w,w>)
+  int item0, n_items;   // the slot's item range
+  double* scratch;      // [blocks * 3] block partials
+};
+// Launches the slot's step (apply + partial placement) on `st`; graph-safe
+// once prepare_eng_fused() has run (outside any capture).
+void prepare_eng_fused();
+void launch_eng_fused(const OpView& v, const EngFusedArgs& a, cudaStream_t st);
+int eng_fused_blocks(const OpView& v);
+
 using TableUpload = std::function<const void*(const void* host, size_t bytes)>;
 void fill_fused_tables(OpView& v, const HopTable& tu, const HopTable& td, int64_t Du, int64_t Dd,
                        const TableUpload& upload);

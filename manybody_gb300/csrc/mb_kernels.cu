@@ -142,11 +142,11 @@ __device__ __forceinline__ float unit_sign(uint32_t e, float) {
 }
 
 template <typename T, bool STAGED, int DOTS>
-__global__ void __launch_bounds__(kApplyThreads, kApplyCtasPerSm<T>)
-k_apply(OpView v, const typename C2<T>::type* __restrict__ x, typename C2<T>::type* y,
-        T hop_coef, T dscale, T shift, T beta, const typename C2<T>::type* z,
-        const T* __restrict__ ufold, const T* __restrict__ self_up, const T* __restrict__ self_dn,
-        double* __restrict__ partials) {
+__device__ __forceinline__ void apply_rows(
+    const OpView& v, const typename C2<T>::type* __restrict__ x, typename C2<T>::type* y,
+    T hop_coef, T dscale, T shift, T beta, const typename C2<T>::type* z,
+    const T* __restrict__ ufold, const T* __restrict__ self_up, const T* __restrict__ self_dn,
+    double* __restrict__ partials) {
   using V2 = typename C2<T>::type;
   constexpr int kShift = sizeof(V2) == 16 ? 4 : 3;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -249,6 +249,54 @@ k_apply(OpView v, const typename C2<T>::type* __restrict__ x, typename C2<T>::ty
   if (DOTS) {
     double vals[3] = {a_xy.value(), a_yy.value(), a_xx.value()};
     block_reduce_store<3>(vals, partials);
+  }
+}
+
+template <typename T, bool STAGED, int DOTS>
+__global__ void __launch_bounds__(kApplyThreads, kApplyCtasPerSm<T>)
+k_apply(OpView v, const typename C2<T>::type* __restrict__ x, typename C2<T>::type* y,
+        T hop_coef, T dscale, T shift, T beta, const typename C2<T>::type* z,
+        const T* __restrict__ ufold, const T* __restrict__ self_up, const T* __restrict__ self_dn,
+        double* __restrict__ partials) {
+  apply_rows<T, STAGED, DOTS>(v, x, y, hop_coef, dscale, shift, beta, z, ufold, self_up, self_dn,
+                              partials);
+}
+
+// One engine step of a large slot through the fused complex64 apply: the
+// slot's mode and step counter are read on the device, so the launch can sit
+// in a captured graph.  Lanczos / replay: w = scale H v - beta_{k-1} v_prev;
+// Chebyshev: w = c (H - b) v - [k > 0] T_{k-1}, c = (k ? 2 : 1) / a.
+// Block partials (Re<v,w>, <w,w>) go to a.scratch.
+template <bool STAGED>
+__global__ void __launch_bounds__(kApplyThreads, kApplyCtasPerSm<float>)
+k_eng_fused(OpView v, EngFusedArgs a) {
+  const int k = *a.k, mode = *a.mode;
+  float sc, shift = 0.f, beta = 0.f;
+  if ((mode == kEngLanczos && k < *a.kmax) || (mode == kEngReplay && k + 1 < *a.steps)) {
+    sc = a.scale;
+    if (k > 0) beta = -(float)a.beta[k - 1];
+  } else if (mode == kEngCheb && k < *a.kmax) {
+    sc = (k == 0 ? 1.f : 2.f) / *a.cheb_a;
+    shift = *a.cheb_b;
+    if (k > 0) beta = -1.f;
+  } else {
+    return;  // idle this step: k_eng_fused_place writes zero partials
+  }
+  apply_rows<float, STAGED, 3>(v, a.buf[(k + 1) % 3], a.buf[(k + 2) % 3], -a.t * sc, sc, shift,
+                               beta, k > 0 ? a.buf[k % 3] : nullptr, a.ufold, nullptr, nullptr,
+                               a.scratch);
+}
+
+// The fused slot's block partials into the engine's per-item partial arrays
+// (its items [item0, item0 + n_items)), zeros where there is no block.
+__global__ void k_eng_fused_place(EngFusedArgs a, int nblocks) {
+  const int k = *a.k, mode = *a.mode;
+  const bool ran = (mode == kEngLanczos && k < *a.kmax) || (mode == kEngReplay && k + 1 < *a.steps) ||
+                   (mode == kEngCheb && k < *a.kmax);
+  for (int i = threadIdx.x; i < a.n_items; i += blockDim.x) {
+    const bool b = ran && i < nblocks;
+    a.part[a.item0 + i] = b ? a.scratch[3 * i] : 0.0;
+    a.part2[a.item0 + i] = b ? a.scratch[3 * i + 1] : 0.0;
   }
 }
 
@@ -463,6 +511,34 @@ void launch_apply(const OpView& v, int precision, const void* x, void* y, double
     if (staged) apply_dots<double, true>(v, x, y, scale, shift, beta, z, partials, dot_mode, st);
     else apply_dots<double, false>(v, x, y, scale, shift, beta, z, partials, dot_mode, st);
   }
+}
+
+int eng_fused_blocks(const OpView& v) { return apply_grid(v, MB_PREC_F32); }
+
+void prepare_eng_fused() {
+  // the launch limit on dynamic shared memory, set outside any stream capture
+  static bool done = false;
+  if (done) return;
+  // the opt-in maximum less each kernel's static shared memory
+  auto allow = [](const void* f) {
+    cudaFuncAttributes fa{};
+    MB_CUDA(cudaFuncGetAttributes(&fa, f));
+    MB_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 max_smem_optin() - (int)fa.sharedSizeBytes));
+  };
+  allow((const void*)k_eng_fused<true>);
+  allow((const void*)k_eng_fused<false>);
+  done = true;
+}
+
+void launch_eng_fused(const OpView& v, const EngFusedArgs& a, cudaStream_t st) {
+  const bool staged = apply_staged(v, MB_PREC_F32);
+  const size_t smem = apply_smem(v, MB_PREC_F32, staged);
+  const int grid = apply_grid(v, MB_PREC_F32);
+  if (staged) k_eng_fused<true><<<grid, kApplyThreads, smem, st>>>(v, a);
+  else k_eng_fused<false><<<grid, kApplyThreads, smem, st>>>(v, a);
+  k_eng_fused_place<<<1, 256, 0, st>>>(a, grid);
+  MB_CUDA(cudaGetLastError());
 }
 
 // ---------------------------------------------------------------------------

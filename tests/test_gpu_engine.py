@@ -139,3 +139,51 @@ def test_dos_requests_match_oracle_and_mix_with_ground_states(mb, cuda):
     g = eng.poll(gid)
     e_exact = exact_e0((8,), 4, 4, 4.0)
     assert abs(g.e0 - e_exact) <= 1e-8 * abs(e_exact)
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_fused_apply_path_matches_grouped(mb, cuda, exact, use_graph):
+    """Every request through the fused complex64 apply (threshold 1) against
+    none (threshold above every sector): the same refined energies, and the
+    fused path alone equals it in the mix bit for bit."""
+    d = descs(mb)
+    big = 1 << 62
+    grouped = mb.batch_ground_states(d, seeds=list(range(len(d))), kmax=150, autotune=False,
+                                     use_graph=use_graph, fused_threshold=big)
+    fused = mb.batch_ground_states(d, seeds=list(range(len(d))), kmax=150, autotune=False,
+                                   use_graph=use_graph, fused_threshold=1)
+    for g, f, e in zip(grouped, fused, exact):
+        assert abs(f.e0 - e) <= 1e-8 * abs(e), (f.e0, e)
+        assert abs(f.e0 - g.e0) <= 1e-9 * abs(e)
+        assert abs(f.e0_raw - e) <= 1e-5 * abs(e)
+    alone = mb.batch_ground_states([d[3]], seeds=[3], kmax=150, autotune=False,
+                                   use_graph=use_graph, fused_threshold=1)[0]
+    assert alone.e0 == fused[3].e0 and alone.e0_raw == fused[3].e0_raw
+
+
+def test_fused_dos_and_mid_run_switch(mb, cuda):
+    """DOS moments through the fused apply match the grouped path's; switching
+    the threshold while requests run keeps their progress."""
+    res = []
+    for thr in (1 << 62, 1):
+        eng = mb.Engine()
+        eng.set_fused_threshold(thr)
+        rid = eng.try_submit_dos(mb.sector((8,), 4, 4, 1.0, 4.0), n_moments=64, n_probes=1, seed=9)
+        while eng.step(4):
+            pass
+        res.append(eng.poll_dos(rid))
+    (mu_g, lo_g, hi_g, _), (mu_f, lo_f, hi_f, _) = res
+    assert abs(lo_f - lo_g) <= 1e-4 * abs(lo_g) and abs(hi_f - hi_g) <= 1e-4 * abs(hi_g)
+    assert np.max(np.abs(mu_f - mu_g)) <= 1e-4
+    eng = mb.Engine()
+    gid = eng.try_submit(mb.sector((8,), 4, 4, 1.0, 4.0), seed=1, kmax=300, rel_tol=1e-12)
+    eng.step(20)
+    eng.set_fused_threshold(1)
+    eng.step(20)
+    eng.set_fused_threshold(1 << 62)
+    while eng.step(10):
+        pass
+    e_exact = exact_e0((8,), 4, 4, 4.0)
+    assert abs(eng.poll(gid).e0 - e_exact) <= 1e-8 * abs(e_exact)
+    with pytest.raises(mb.MbError):
+        eng.set_fused_threshold(0)

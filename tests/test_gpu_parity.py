@@ -418,5 +418,7 @@ def test_solve_linear_system(mb, cuda):
 
     x = mb.solve(op, torch.tensor(b, device="cuda"), n, tridiag_solve).cpu().numpy()
     assert np.linalg.norm(H @ x - b) <= 1e-7 * np.linalg.norm(b)
-    zero = mb.solve(op, torch.zeros(n, dtype=torch.complex128, device="cuda"), n, tridiag_solve)
-    assert not zero.abs().max().item()
+    # a zero right-hand side is an error, as in lanczos_pass_one (lanczos.h:144)
+    with pytest.raises(mb.MbError) as e:
+        mb.solve(op, torch.zeros(n, dtype=torch.complex128, device="cuda"), n, tridiag_solve)
+    assert e.value.status == mb.MB_ERR_ZERO_NORM
