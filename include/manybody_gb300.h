@@ -391,6 +391,14 @@ int mb_engine_step(mb_engine_t engine, int n_steps, int* n_active);
  * unrefined Ritz value, Lanczos steps and submit-to-finish seconds. */
 int mb_engine_poll(mb_engine_t engine, int64_t request_id, int* done, double* e0, double* e0_raw,
                    int64_t* steps, double* latency_s);
+/* Ids of the requests (ground state or DOS) that finished since the last
+ * call, oldest first, at most `capacity` of them (the rest stay queued);
+ * *n = how many were written.  Lets a serving loop poll only those. */
+int mb_engine_completed(mb_engine_t engine, int64_t* ids, int64_t capacity, int64_t* n);
+/* Totals over mb_engine_step calls: steps run, their wall time and the
+ * device time of their kernels (ms), for the host / device split. */
+int mb_engine_stats(mb_engine_t engine, int64_t* steps, double* step_wall_ms,
+                    double* step_device_ms);
 /* Warps per block of the grouped kernels (2, 4, 8, 16): the autotuner's knob. */
 int mb_engine_set_warps(mb_engine_t engine, int warps_per_block);
 /* Requests on sectors of at least min_states states step through the fused

@@ -152,6 +152,8 @@ SIGNATURES = {
     "mb_engine_poll": (C.c_int, [_vp, _i64, C.POINTER(C.c_int), _dp, _dp, _i64p, _dp]),
     "mb_engine_set_warps": (C.c_int, [_vp, C.c_int]),
     "mb_engine_set_fused_threshold": (C.c_int, [_vp, C.c_int64]),
+    "mb_engine_completed": (C.c_int, [_vp, _i64p, C.c_int64, _i64p]),
+    "mb_engine_stats": (C.c_int, [_vp, _i64p, _dp, _dp]),
     "mb_engine_autotune": (C.c_int, [_vp, C.POINTER(C.c_int), _dp]),
     "mb_dot_re": (C.c_int, [_vp, _vp, _vp, _dp]),
     "mb_norm": (C.c_int, [_vp, _vp, _dp]),
@@ -941,6 +943,20 @@ class Engine:
 
     def set_warps(self, w: int):
         _check(lib().mb_engine_set_warps(self._h, w))
+
+    def completed(self, capacity: int = 4096):
+        """Ids of requests finished since the last call (oldest first)."""
+        ids = np.zeros(capacity, np.int64)
+        n = C.c_int64()
+        _check(lib().mb_engine_completed(self._h, ids.ctypes.data_as(_i64p), capacity, C.byref(n)))
+        return [int(i) for i in ids[:n.value]]
+
+    def stats(self):
+        """(steps, wall ms, device ms) summed over step() calls."""
+        st = C.c_int64()
+        w, d = C.c_double(), C.c_double()
+        _check(lib().mb_engine_stats(self._h, C.byref(st), C.byref(w), C.byref(d)))
+        return st.value, w.value, d.value
 
     def set_fused_threshold(self, min_states: int):
         """Sectors of at least min_states states use the fused complex64 apply."""

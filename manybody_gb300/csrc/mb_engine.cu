@@ -530,7 +530,16 @@ struct mb_engine_s {
   std::vector<std::pair<mb::OpView, mb::EngFusedArgs>> fused;
   std::vector<std::unique_ptr<mb::EngBuf>> fused_scratch;
   cudaStream_t st = nullptr;
+  // ids retired since the last mb_engine_completed call
+  std::vector<int64_t> newly_done;
+  // step statistics: steps run, wall time of the step calls, device time of
+  // the step kernels (events around each step's launches)
+  int64_t stat_steps = 0;
+  double stat_wall_ms = 0.0, stat_dev_ms = 0.0;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
   ~mb_engine_s() {
+    for (cudaEvent_t x : ev)
+      if (x) cudaEventDestroy(x);
     if (st) cudaStreamDestroy(st);
   }
 };
@@ -917,6 +926,7 @@ void after_step(mb_engine_s* e) {
       sp->vecs.reset();
       sp->scal.reset();
       sp->tables.reset();
+      e->newly_done.push_back(sp->id);
       e->done[sp->id] = std::move(sp);
       e->slots.erase(e->slots.begin() + (long)i);
       changed = true;
@@ -963,6 +973,7 @@ int mb_engine_create(int64_t device_bytes_budget, mb_engine_t* out) {
     MB_CUDA(cudaMemGetInfo(&free_b, &total_b));
     e->budget = device_bytes_budget > 0 ? device_bytes_budget : (int64_t)(free_b * 0.8);
     MB_CUDA(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
+    for (cudaEvent_t& x : e->ev) MB_CUDA(cudaEventCreate(&x));
     *out = (mb_engine_t)e.release();
   });
 }
@@ -1121,9 +1132,18 @@ int mb_engine_step(mb_engine_t eng, int n_steps, int* n_active) {
     auto* e = (mb_engine_s*)eng;
     MB_REQUIRE(e && n_steps >= 0, MB_ERR_INVALID_ARG, "bad argument");
     for (int i = 0; i < n_steps && !e->slots.empty(); ++i) {
+      const auto t0 = std::chrono::steady_clock::now();
       rebuild(e);
+      MB_CUDA(cudaEventRecord(e->ev[0], e->st));
       launch_step(e);
-      after_step(e);
+      MB_CUDA(cudaEventRecord(e->ev[1], e->st));
+      after_step(e);  // waits on the stream: both events have completed
+      float ms = 0.f;
+      MB_CUDA(cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]));
+      e->stat_dev_ms += ms;
+      e->stat_wall_ms +=
+          std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      ++e->stat_steps;
     }
     if (n_active) *n_active = (int)e->slots.size();
   });
@@ -1145,6 +1165,28 @@ int mb_engine_poll(mb_engine_t eng, int64_t id, int* done, double* e0, double* e
     if (e0_raw) *e0_raw = s.e_raw;
     if (steps) *steps = s.m;
     if (latency_s) *latency_s = std::chrono::duration<double>(s.t_done - s.t_submit).count();
+  });
+}
+
+int mb_engine_completed(mb_engine_t eng, int64_t* ids, int64_t capacity, int64_t* n) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e && n && (ids || capacity == 0) && capacity >= 0, MB_ERR_INVALID_ARG,
+               "NULL argument or negative capacity");
+    const int64_t k = std::min<int64_t>(capacity, (int64_t)e->newly_done.size());
+    std::copy(e->newly_done.begin(), e->newly_done.begin() + k, ids);
+    e->newly_done.erase(e->newly_done.begin(), e->newly_done.begin() + k);
+    *n = k;
+  });
+}
+
+int mb_engine_stats(mb_engine_t eng, int64_t* steps, double* step_wall_ms, double* step_device_ms) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e, MB_ERR_INVALID_ARG, "NULL engine");
+    if (steps) *steps = e->stat_steps;
+    if (step_wall_ms) *step_wall_ms = e->stat_wall_ms;
+    if (step_device_ms) *step_device_ms = e->stat_dev_ms;
   });
 }
 

@@ -187,3 +187,20 @@ def test_fused_dos_and_mid_run_switch(mb, cuda):
     assert abs(eng.poll(gid).e0 - e_exact) <= 1e-8 * abs(e_exact)
     with pytest.raises(mb.MbError):
         eng.set_fused_threshold(0)
+
+
+def test_completed_queue_and_stats(mb, cuda):
+    """completed() hands back each finished request once, oldest first; the
+    step statistics count the steps run."""
+    eng = mb.Engine()
+    ids = [eng.try_submit(x, seed=2, kmax=60) for x in descs(mb)[:4]]
+    seen = []
+    while eng.step(3):
+        seen += eng.completed()
+    seen += eng.completed()
+    assert sorted(seen) == sorted(ids) and len(set(seen)) == len(seen)
+    assert eng.completed() == []
+    for rid in seen:
+        assert eng.poll(rid) is not None
+    steps, wall_ms, dev_ms = eng.stats()
+    assert steps > 0 and wall_ms > 0 and 0 < dev_ms <= wall_ms
