@@ -874,10 +874,12 @@ void after_step(mb_engine_s* e) {
       const int m = d.steps;
       bool finished = d.mode == kModeIdle, converged = false;
       if (!finished && s.rel_tol > 0.0 && m >= 2 && (m % s.check_every) == 0) {
-        std::vector<double> a((size_t)m), b((size_t)m);
-        MB_CUDA(cudaMemcpy(a.data(), d.alpha, sizeof(double) * m, cudaMemcpyDeviceToHost));
-        MB_CUDA(cudaMemcpy(b.data(), d.beta, sizeof(double) * m, cudaMemcpyDeviceToHost));
-        const double r = ritz_min(a, b, m, nullptr);
+        // alpha and beta sit kEngMaxK apart in one buffer: one copy; the
+        // extreme Ritz value by Sturm bisection (O(m) a sweep), not a full
+        // eigensolve of T_m
+        std::vector<double> ab((size_t)(kEngMaxK + m));
+        MB_CUDA(cudaMemcpy(ab.data(), d.alpha, sizeof(double) * ab.size(), cudaMemcpyDeviceToHost));
+        const double r = tridiag_max_eig(ab.data(), ab.data() + kEngMaxK, m);
         if (s.have_ritz && std::fabs(r - s.last_ritz) <= s.rel_tol * std::fabs(r)) finished = converged = true;
         s.last_ritz = r;
         s.have_ritz = true;
