@@ -393,11 +393,15 @@ __global__ void k_eng_seed(float2* __restrict__ v, int64_t n, uint64_t seed, dou
   }
 }
 
-// ||b||^2 of one slot's start vector (compensated), single block.
-__global__ void k_eng_norm2(const float2* __restrict__ v, int64_t n, double* __restrict__ out) {
+// ||b||^2 of one slot's start vector (compensated): block b sums the
+// elements [b * n / nb, (b + 1) * n / nb) into part[b], then k_eng_sum adds
+// the nb partials in order (nb depends on n only: the same bits alone or in
+// any mix of requests).
+__global__ void k_eng_norm2(const float2* __restrict__ v, int64_t n, double* __restrict__ part) {
   __shared__ double red[256];
+  const int64_t i0 = n * blockIdx.x / gridDim.x, i1 = n * (blockIdx.x + 1) / gridDim.x;
   float hi = 0.f, lo = 0.f;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
     const float2 a = v[i];
     float p = a.x * a.x, pe = fmaf(a.x, a.x, -p);
     float s1 = hi + p, bp = s1 - hi;
@@ -416,7 +420,13 @@ __global__ void k_eng_norm2(const float2* __restrict__ v, int64_t n, double* __r
     if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) *out = red[0];
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void k_eng_sum(const double* __restrict__ part, int nb, double* __restrict__ out) {
+  double a = 0.0;
+  for (int b = 0; b < nb; ++b) a += part[b];
+  *out = a;
 }
 
 __global__ void k_eng_scale(float2* __restrict__ v, int64_t n, float s) {
@@ -619,6 +629,10 @@ OpView slot_view(const EngineSlot& s) {
 
 void rebuild(mb_engine_s* e) {
   if (!e->dirty) return;
+  // h_slots holds the device state of the previous list (fetched after the
+  // last step, host edits since): keep each surviving slot's progress
+  std::map<const float2*, SlotDesc> old;
+  for (const SlotDesc& od : e->h_slots) old[od.buf[0]] = od;
   e->h_slots.clear();
   std::vector<int2> items;
   for (auto& sp : e->slots) {
@@ -649,6 +663,19 @@ void rebuild(mb_engine_s* e) {
     for (int64_t r = 0; r < s.Du; ++r) items.push_back(make_int2((int)e->h_slots.size(), (int)r));
     d.item1 = (int)items.size();
     d.fused = s.dim >= e->fused_min ? 1 : 0;
+    auto o = old.find(d.buf[0]);
+    if (o != old.end()) {
+      d.k = o->second.k;
+      d.mode = o->second.mode;
+      d.steps = o->second.steps;
+      d.kmax = o->second.kmax;
+      d.cheb_a = o->second.cheb_a;
+      d.cheb_b = o->second.cheb_b;
+    } else {  // admitted since: its vectors were seeded at submission
+      d.k = 0;
+      d.mode = kModeLanczos;
+      d.steps = 0;
+    }
     e->h_slots.push_back(d);
   }
   e->n_items = (int)items.size();
@@ -686,6 +713,9 @@ void rebuild(mb_engine_s* e) {
     e->fused.push_back({v, a});
   }
   if (!e->fused.empty()) prepare_eng_fused();
+  if (!e->h_slots.empty())
+    MB_CUDA(cudaMemcpyAsync(e->d_slots->p, e->h_slots.data(), sizeof(SlotDesc) * e->h_slots.size(),
+                            cudaMemcpyHostToDevice, e->st));
   if (!items.empty())
     MB_CUDA(cudaMemcpyAsync(e->d_items->p, items.data(), sizeof(int2) * items.size(),
                             cudaMemcpyHostToDevice, e->st));
@@ -750,18 +780,30 @@ void launch_step(mb_engine_s* e) {
 }
 
 // Seed, normalise and arm a slot for pass one (or replay).
-void arm_slot(mb_engine_s* e, EngineSlot& s, SlotDesc& d, bool replay) {
-  float2* b1 = d.buf[1];
+// ||v||^2 into out[0] (out holds kEngNormBlocks + 1 doubles of scratch).
+constexpr int kEngNormBlocks = 128;
+void eng_norm2(mb_engine_s* e, const float2* v, int64_t n, double* out) {
+  const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(kEngNormBlocks, (n + 8191) / 8192));
+  k_eng_norm2<<<nb, 256, 0, e->st>>>(v, n, out + 1);
+  k_eng_sum<<<1, 1, 0, e->st>>>(out + 1, nb, out);
+}
+
+// Seeds v = buf[1] (normalised start vector) and zeroes v_prev = buf[0].
+void seed_vectors(mb_engine_s* e, EngineSlot& s, float2* b0, float2* b1) {
   k_eng_seed<<<256, 256, 0, e->st>>>(b1, s.dim, s.seed, 1.0);
-  EngBuf nb(sizeof(double));
-  k_eng_norm2<<<1, 256, 0, e->st>>>(b1, s.dim, (double*)nb.p);
+  EngBuf nb(sizeof(double) * (kEngNormBlocks + 1));
+  eng_norm2(e, b1, s.dim, (double*)nb.p);
   double n2 = 0.0;
   MB_CUDA(cudaMemcpyAsync(&n2, nb.p, sizeof(double), cudaMemcpyDeviceToHost, e->st));
   MB_CUDA(cudaStreamSynchronize(e->st));
   s.b_norm = std::sqrt(n2);
   MB_REQUIRE(s.b_norm > kTol, MB_ERR_ZERO_NORM, "Input vector has zero norm");
   k_eng_scale<<<256, 256, 0, e->st>>>(b1, s.dim, (float)(1.0 / s.b_norm));
-  MB_CUDA(cudaMemsetAsync(d.buf[0], 0, 8 * (size_t)s.dim, e->st));
+  MB_CUDA(cudaMemsetAsync(b0, 0, 8 * (size_t)s.dim, e->st));
+}
+
+void arm_slot(mb_engine_s* e, EngineSlot& s, SlotDesc& d, bool replay) {
+  seed_vectors(e, s, d.buf[0], d.buf[1]);
   d.k = 0;
   if (replay) {
     d.mode = kModeReplay;
@@ -801,8 +843,8 @@ double rayleigh_fp64(mb_engine_s* e, EngineSlot& s, const SlotDesc& d) {
 // Seed probe `p` of a DOS request into buf[1] and arm Chebyshev mode.
 void arm_probe(mb_engine_s* e, EngineSlot& s, SlotDesc& d) {
   k_eng_seed_phase<<<256, 256, 0, e->st>>>(d.buf[1], s.dim, s.seed, (uint32_t)(1 + s.probe));
-  EngBuf nb(sizeof(double));
-  k_eng_norm2<<<1, 256, 0, e->st>>>(d.buf[1], s.dim, (double*)nb.p);
+  EngBuf nb(sizeof(double) * (kEngNormBlocks + 1));
+  eng_norm2(e, d.buf[1], s.dim, (double*)nb.p);
   MB_CUDA(cudaMemcpyAsync(&s.mu0, nb.p, sizeof(double), cudaMemcpyDeviceToHost, e->st));
   MB_CUDA(cudaMemsetAsync(d.buf[0], 0, 8 * (size_t)s.dim, e->st));
   MB_CUDA(cudaStreamSynchronize(e->st));
@@ -936,24 +978,9 @@ void after_step(mb_engine_s* e) {
       ++i;
     }
   }
-  if (changed) {
-    // keep device-side progress (k, mode) of the surviving slots
-    std::vector<SlotDesc> keep;
+  if (changed) {  // new work lists; rebuild keeps the survivors' progress
     e->dirty = true;
-    std::vector<SlotDesc> old = e->h_slots;
     rebuild(e);
-    // rebuild() reset per-slot fields: copy progress over by buffer identity
-    for (auto& nd : e->h_slots)
-      for (auto& od : old)
-        if (od.buf[0] == nd.buf[0]) {
-          nd.k = od.k;
-          nd.mode = od.mode;
-          nd.steps = od.steps;
-          nd.kmax = od.kmax;
-          nd.cheb_a = od.cheb_a;
-          nd.cheb_b = od.cheb_b;
-        }
-    push_slots(e);
   }
 }
 
@@ -1029,26 +1056,13 @@ int mb_engine_submit_ground_state(mb_engine_t eng, const mb_sector_desc* desc, u
     s->scal = std::make_unique<EngBuf>(3 * 8 * (size_t)kEngMaxK);
     s->id = e->next_id++;
     s->t_submit = std::chrono::steady_clock::now();
+    float2* base = (float2*)s->vecs->p;
+    seed_vectors(e, *s, base, base + s->dim);
     e->in_use += need;
-    // append, keeping the progress of the others
-    std::vector<SlotDesc> old = e->h_slots;
+    *request_id = s->id;
+    // joins at the next step (rebuild keeps the others' progress)
     e->slots.push_back(std::move(s));
     e->dirty = true;
-    rebuild(e);
-    for (auto& nd : e->h_slots)
-      for (auto& od : old)
-        if (od.buf[0] == nd.buf[0]) {
-          nd.k = od.k;
-          nd.mode = od.mode;
-          nd.steps = od.steps;
-          nd.kmax = od.kmax;
-          nd.cheb_a = od.cheb_a;
-          nd.cheb_b = od.cheb_b;
-        }
-    EngineSlot& ns = *e->slots.back();
-    arm_slot(e, ns, e->h_slots.back(), false);
-    push_slots(e);
-    *request_id = ns.id;
   });
 }
 
@@ -1087,25 +1101,12 @@ int mb_engine_submit_dos(mb_engine_t eng, const mb_sector_desc* desc, int64_t n_
     s->id = e->next_id++;
     s->t_submit = std::chrono::steady_clock::now();
     s->phase = 10;
+    float2* base = (float2*)s->vecs->p;
+    seed_vectors(e, *s, base, base + s->dim);
     e->in_use += need;
-    std::vector<SlotDesc> old = e->h_slots;
+    *request_id = s->id;
     e->slots.push_back(std::move(s));
     e->dirty = true;
-    rebuild(e);
-    for (auto& nd : e->h_slots)
-      for (auto& od : old)
-        if (od.buf[0] == nd.buf[0]) {
-          nd.k = od.k;
-          nd.mode = od.mode;
-          nd.steps = od.steps;
-          nd.kmax = od.kmax;
-          nd.cheb_a = od.cheb_a;
-          nd.cheb_b = od.cheb_b;
-        }
-    EngineSlot& ns = *e->slots.back();
-    arm_slot(e, ns, e->h_slots.back(), false);
-    push_slots(e);
-    *request_id = ns.id;
   });
 }
 
@@ -1197,22 +1198,9 @@ int mb_engine_set_fused_threshold(mb_engine_t eng, int64_t min_states) {
     auto* e = (mb_engine_s*)eng;
     MB_REQUIRE(e && min_states >= 1, MB_ERR_INVALID_ARG, "NULL engine or threshold below 1");
     // mid-run changes keep each slot's progress: only the kernel that applies it changes
-    if (!e->h_slots.empty()) fetch_slots(e);
-    const std::vector<SlotDesc> old = e->h_slots;
     e->fused_min = min_states;
     e->dirty = true;
     rebuild(e);
-    for (auto& nd : e->h_slots)
-      for (auto& od : old)
-        if (od.buf[0] == nd.buf[0]) {
-          nd.k = od.k;
-          nd.mode = od.mode;
-          nd.steps = od.steps;
-          nd.kmax = od.kmax;
-          nd.cheb_a = od.cheb_a;
-          nd.cheb_b = od.cheb_b;
-        }
-    push_slots(e);
   });
 }
 
