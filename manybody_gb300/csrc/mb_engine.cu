@@ -55,8 +55,15 @@ struct SlotDesc {
   int k;            // this slot's step counter
   int mode;         // kModeIdle, kModeLanczos, kModeReplay
   int steps;        // pass-one steps taken (m)
-  int item0, item1; // this slot's range of work items
+  int item0, item1; // this slot's range of work items (partials at item0 + row)
   int fused;        // applied by the fused kernel (large sectors), not k_eng_apply
+  // the sector's fused-apply tables (row-staged kernel): sign-sorted up
+  // lists and the sliced down table
+  const uint32_t* up_list;
+  const int32_t* up_loff;
+  const int32_t* up_lpos;
+  const uint32_t* dn_sell;
+  const int32_t* dn_sgrp;
 };
 
 constexpr int kModeIdle = kEngIdle;
@@ -162,8 +169,162 @@ k_eng_apply(const SlotDesc* __restrict__ slots, const int2* __restrict__ items, 
       }
     }
     if (lane == 0 && part) {
-      part[it] = dxy;
-      part2[it] = dyy;
+      part[s.item0 + item.y] = dxy;
+      part2[s.item0 + item.y] = dyy;
+    }
+  }
+}
+
+// Rows of medium sectors, a block per (slot, row), as the operators' fused
+// apply does it: the row of v (and the zero padding elements) and the row's
+// sign-sorted up list staged in shared memory; warps take the row's 32-column
+// groups; down hops gather from the staged row through the sliced table (four
+// slots per 16-byte load), up hops are coalesced loads of the listed rows,
+// added then subtracted; the step arithmetic and compensated partials of
+// k_eng_apply.
+constexpr int kEngRowWarps = 8;
+constexpr int64_t kEngRowMinCols = 256;  // rows this wide and wider
+
+__global__ void __launch_bounds__(kEngRowWarps * 32)
+k_eng_apply_rows(const SlotDesc* __restrict__ slots, const int2* __restrict__ items, int n_items,
+                 int max_cols, double* __restrict__ part, double* __restrict__ part2) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2* srow = reinterpret_cast<float2*>(smem);
+  uint32_t* s_up = reinterpret_cast<uint32_t*>(smem + sizeof(float2) * (max_cols + kSlicedPads));
+  __shared__ double red[kEngRowWarps][2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const int2 item = items[it];
+    const SlotDesc& s = slots[item.x];
+    const int k = s.k;
+    const bool lanczos = s.mode == kModeLanczos && k < s.kmax;
+    const bool replay = s.mode == kModeReplay && k + 1 < s.steps;
+    const bool cheb = s.mode == kModeCheb && k < s.kmax;
+    const int64_t pidx = s.item0 + item.y;
+    if (!(lanczos || replay || cheb)) {  // uniform over the block
+      if (threadIdx.x == 0) {
+        part[pidx] = 0.0;
+        part2[pidx] = 0.0;
+      }
+      continue;
+    }
+    const int64_t r = item.y, Dd = s.Dd;
+    const uint64_t row_bytes = sizeof(float2) * (uint64_t)Dd;
+    const float2* x = s.buf[(k + 1) % 3];
+    const float2* v = x + r * Dd;
+    const float2* z = s.buf[k % 3] + r * Dd;
+    float2* w = s.buf[(k + 2) % 3] + r * Dd;
+    const double bprev = cheb ? 1.0 : (k > 0 ? s.beta[k - 1] : 0.0);
+    const float beta = (float)(-bprev);
+    const float sc = cheb ? (k == 0 ? 1.f : 2.f) / s.cheb_a : s.scale;
+    const float shift = cheb ? s.cheb_b : 0.f;
+    const float hop = -s.t * sc;
+    const uint32_t um = s.up_mask[r];
+    const int u0 = __ldg(&s.up_loff[r]), nu = __ldg(&s.up_loff[r + 1]) - u0;
+    const int npos = __ldg(&s.up_lpos[r]);
+    __syncthreads();  // the previous item's readers are done with srow / s_up
+    for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) srow[c] = v[c];
+    if (threadIdx.x < kSlicedPads) srow[Dd + threadIdx.x] = make_float2(0.f, 0.f);
+    for (int j = threadIdx.x; j < nu; j += blockDim.x) s_up[j] = __ldg(&s.up_list[u0 + j]);
+    __syncthreads();
+    float hi = 0.f, lo = 0.f, hi2 = 0.f, lo2 = 0.f;
+    const int64_t ngroups = (Dd + 31) >> 5;
+    for (int64_t g = warp; g < ngroups; g += kEngRowWarps) {
+      const int64_t c = (g << 5) + lane;
+      const bool live = c < Dd;
+      const int64_t cl = live ? c : Dd - 1;
+      float ar = 0.f, ai = 0.f;
+      const int2 gi = __ldg(reinterpret_cast<const int2*>(s.dn_sgrp) + g);
+      const uint4* ep = reinterpret_cast<const uint4*>(s.dn_sell + gi.x) + lane;
+      auto dn = [&](uint32_t e) {
+        const float2 val = srow[e & 0x7FFFFFFFu];
+        const float wgt = __int_as_float((int)(0x3f800000u | (e & 0x80000000u)));
+        ar = fmaf(wgt, val.x, ar);
+        ai = fmaf(wgt, val.y, ai);
+      };
+      for (int j = 0; j < gi.y; j += 4) {
+        const uint4 e = __ldg(ep + 8 * j);
+        dn(e.x);
+        dn(e.y);
+        dn(e.z);
+        dn(e.w);
+      }
+      const char* xc = reinterpret_cast<const char*>(x + cl);
+      auto up = [&](int q) {
+        return __ldg(reinterpret_cast<const float2*>(xc + (uint64_t)s_up[q] * row_bytes));
+      };
+      float pr = 0.f, pi = 0.f, nr = 0.f, ni = 0.f;
+      int j = 0;
+#pragma unroll 4
+      for (; j < npos; ++j) {
+        const float2 val = up(j);
+        pr += val.x;
+        pi += val.y;
+      }
+#pragma unroll 4
+      for (; j < nu; ++j) {
+        const float2 val = up(j);
+        nr += val.x;
+        ni += val.y;
+      }
+      ar += pr - nr;
+      ai += pi - ni;
+      if (!live) continue;
+      const float2 xv = srow[c];
+      const float d = sc * (s.ufold[__popc(um & s.dn_mask[c])] - shift);
+      float2 o;
+      o.x = fmaf(hop, ar, d * xv.x);
+      o.y = fmaf(hop, ai, d * xv.y);
+      if (k > 0) {
+        const float2 zv = z[c];
+        o.x = fmaf(beta, zv.x, o.x);
+        o.y = fmaf(beta, zv.y, o.y);
+      }
+      w[c] = o;
+      if (!replay) {  // compensated Re<v, w> (exact float products, TwoSum)
+        float p = xv.x * o.x, pe = fmaf(xv.x, o.x, -p);
+        float s1 = hi + p, bp = s1 - hi;
+        lo += ((hi - (s1 - bp)) + (p - bp)) + pe;
+        hi = s1;
+        p = xv.y * o.y;
+        pe = fmaf(xv.y, o.y, -p);
+        s1 = hi + p;
+        bp = s1 - hi;
+        lo += ((hi - (s1 - bp)) + (p - bp)) + pe;
+        hi = s1;
+      }
+      if (cheb) {  // <T_{k+1}, T_{k+1}>
+        float p = o.x * o.x, pe = fmaf(o.x, o.x, -p);
+        float s1 = hi2 + p, bp = s1 - hi2;
+        lo2 += ((hi2 - (s1 - bp)) + (p - bp)) + pe;
+        hi2 = s1;
+        p = o.y * o.y;
+        pe = fmaf(o.y, o.y, -p);
+        s1 = hi2 + p;
+        bp = s1 - hi2;
+        lo2 += ((hi2 - (s1 - bp)) + (p - bp)) + pe;
+        hi2 = s1;
+      }
+    }
+    double dxy = (double)hi + (double)lo, dyy = (double)hi2 + (double)lo2;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      dxy += __shfl_down_sync(0xffffffffu, dxy, o);
+      dyy += __shfl_down_sync(0xffffffffu, dyy, o);
+    }
+    if (lane == 0) {
+      red[warp][0] = dxy;
+      red[warp][1] = dyy;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {  // fixed order over the warps
+      double a = 0.0, b = 0.0;
+      for (int q = 0; q < kEngRowWarps; ++q) {
+        a += red[q][0];
+        b += red[q][1];
+      }
+      part[pidx] = a;
+      part2[pidx] = b;
     }
   }
 }
@@ -531,6 +692,13 @@ struct mb_engine_s {
   int64_t next_id = 1;
   // device work lists
   std::unique_ptr<mb::EngBuf> d_slots, d_items, d_part;
+  // the apply's work lists: rows of small sectors (warp per row) and rows of
+  // medium ones (block per row, staged); large sectors use the fused kernel
+  std::unique_ptr<mb::EngBuf> d_items_warp, d_items_rows;
+  int n_warp = 0, n_rows = 0;
+  int row_cols = 0;     // widest staged row
+  size_t row_smem = 0;  // its row plus the longest up list
+  int row_grid = 1;
   std::vector<mb::SlotDesc> h_slots;
   int n_items = 0;
   bool dirty = true;
@@ -634,7 +802,9 @@ void rebuild(mb_engine_s* e) {
   std::map<const float2*, SlotDesc> old;
   for (const SlotDesc& od : e->h_slots) old[od.buf[0]] = od;
   e->h_slots.clear();
-  std::vector<int2> items;
+  std::vector<int2> items, items_warp, items_rows;
+  int max_list = 0;
+  e->row_cols = 0;
   for (auto& sp : e->slots) {
     EngineSlot& s = *sp;
     SlotDesc d{};
@@ -663,6 +833,20 @@ void rebuild(mb_engine_s* e) {
     for (int64_t r = 0; r < s.Du; ++r) items.push_back(make_int2((int)e->h_slots.size(), (int)r));
     d.item1 = (int)items.size();
     d.fused = s.dim >= e->fused_min ? 1 : 0;
+    d.up_list = ts.fused.up_list;
+    d.up_loff = ts.fused.up_loff;
+    d.up_lpos = ts.fused.up_lpos;
+    d.dn_sell = ts.fused.dn_sell;
+    d.dn_sgrp = ts.fused.dn_sgrp;
+    if (!d.fused) {
+      const bool rows = s.Dd >= kEngRowMinCols;
+      auto& list = rows ? items_rows : items_warp;
+      for (int64_t r = 0; r < s.Du; ++r) list.push_back(make_int2((int)e->h_slots.size(), (int)r));
+      if (rows) {
+        e->row_cols = std::max(e->row_cols, (int)s.Dd);
+        max_list = std::max(max_list, ts.fused.max_up_list);
+      }
+    }
     auto o = old.find(d.buf[0]);
     if (o != old.end()) {
       d.k = o->second.k;
@@ -719,6 +903,28 @@ void rebuild(mb_engine_s* e) {
   if (!items.empty())
     MB_CUDA(cudaMemcpyAsync(e->d_items->p, items.data(), sizeof(int2) * items.size(),
                             cudaMemcpyHostToDevice, e->st));
+  e->n_warp = (int)items_warp.size();
+  e->n_rows = (int)items_rows.size();
+  e->d_items_warp = std::make_unique<EngBuf>(sizeof(int2) * std::max<size_t>(items_warp.size(), 1));
+  e->d_items_rows = std::make_unique<EngBuf>(sizeof(int2) * std::max<size_t>(items_rows.size(), 1));
+  if (!items_warp.empty())
+    MB_CUDA(cudaMemcpyAsync(e->d_items_warp->p, items_warp.data(),
+                            sizeof(int2) * items_warp.size(), cudaMemcpyHostToDevice, e->st));
+  if (!items_rows.empty()) {
+    MB_CUDA(cudaMemcpyAsync(e->d_items_rows->p, items_rows.data(),
+                            sizeof(int2) * items_rows.size(), cudaMemcpyHostToDevice, e->st));
+    // launch shape, set outside any capture: shared memory and resident blocks
+    e->row_smem = sizeof(float2) * (size_t)(e->row_cols + kSlicedPads) +
+                  sizeof(uint32_t) * (size_t)((max_list + 3) & ~3);
+    MB_CUDA(cudaFuncSetAttribute(k_eng_apply_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)e->row_smem));
+    int bps = 0, sms = 0, dev = 0;
+    MB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_eng_apply_rows,
+                                                          kEngRowWarps * 32, e->row_smem));
+    MB_CUDA(cudaGetDevice(&dev));
+    MB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    e->row_grid = std::max(1, std::min(e->n_rows, std::max(bps, 1) * sms));
+  }
   MB_CUDA(cudaStreamSynchronize(e->st));
   e->dirty = false;
 }
@@ -759,7 +965,12 @@ void step_kernels(mb_engine_s* e) {
   const int n = e->n_items, ns = (int)e->h_slots.size();
   double* part2 = part + n;
   const int g = eng_grid(n, W);
-  k_eng_apply<W><<<g, W * 32, 0, e->st>>>(ds, it, n, part, part2);
+  if (e->n_warp)
+    k_eng_apply<W><<<eng_grid(e->n_warp, W), W * 32, 0, e->st>>>(
+        ds, (const int2*)e->d_items_warp->p, e->n_warp, part, part2);
+  if (e->n_rows)
+    k_eng_apply_rows<<<e->row_grid, kEngRowWarps * 32, e->row_smem, e->st>>>(
+        ds, (const int2*)e->d_items_rows->p, e->n_rows, e->row_cols, part, part2);
   for (const auto& [v, a] : e->fused) launch_eng_fused(v, a, e->st);
   k_eng_seg_reduce<<<std::min(ns, 1024), 256, 0, e->st>>>(dsm, ns, part, part2, 0);
   k_eng_update<W><<<g, W * 32, 0, e->st>>>(ds, it, n, part);
@@ -1261,9 +1472,15 @@ int mb_engine_autotune(mb_engine_t eng, int* chosen, double* ms) {
     }
     rebuild(e);
     const SlotDesc* ds = (const SlotDesc*)e->d_slots->p;
-    const int2* it = (const int2*)e->d_items->p;
+    const int2* it = (const int2*)e->d_items_warp->p;
     double* part = (double*)e->d_part->p;
-    const int n = e->n_items;
+    double* part2 = part + e->n_items;
+    const int n = e->n_warp;
+    if (n == 0) {  // every request runs through the row-staged or fused kernels
+      if (chosen) *chosen = e->warps;
+      if (ms) *ms = 0.0;
+      return;
+    }
     cudaEvent_t a, b;
     MB_CUDA(cudaEventCreate(&a));
     MB_CUDA(cudaEventCreate(&b));
@@ -1275,10 +1492,10 @@ int mb_engine_autotune(mb_engine_t eng, int* chosen, double* ms) {
       auto run = [&] {
         const int g = eng_grid(n, W);
         switch (W) {
-          case 2: k_eng_apply<2><<<g, 64, 0, e->st>>>(ds, it, n, part, part + n); break;
-          case 4: k_eng_apply<4><<<g, 128, 0, e->st>>>(ds, it, n, part, part + n); break;
-          case 8: k_eng_apply<8><<<g, 256, 0, e->st>>>(ds, it, n, part, part + n); break;
-          default: k_eng_apply<16><<<g, 512, 0, e->st>>>(ds, it, n, part, part + n); break;
+          case 2: k_eng_apply<2><<<g, 64, 0, e->st>>>(ds, it, n, part, part2); break;
+          case 4: k_eng_apply<4><<<g, 128, 0, e->st>>>(ds, it, n, part, part2); break;
+          case 8: k_eng_apply<8><<<g, 256, 0, e->st>>>(ds, it, n, part, part2); break;
+          default: k_eng_apply<16><<<g, 512, 0, e->st>>>(ds, it, n, part, part2); break;
         }
       };
       run();
