@@ -122,11 +122,17 @@ class FermionBasis {
 class HubbardModelBase {
  public:
   HubbardModelBase(double t, double u, std::vector<int64_t> dims, bool momentum = false)
-      : t(t), u(u) {
+      : t(t), u(u), dims_(dims), momentum_(momentum) {
     if (momentum) check(mb_hubbard_momentum_create(dims.data(), (int)dims.size(), t, u, &h_));
     else check(mb_hubbard_create(dims.data(), (int)dims.size(), t, u, &h_));
   }
-  HubbardModelBase(HubbardModelBase&& o) noexcept : t(o.t), u(o.u), h_(std::exchange(o.h_, nullptr)) {}
+  // kinetic() / interaction() (hubbard_model.h:13-32): the hopping terms
+  // alone (U = 0) or the U n_up n_down terms alone (t = 0), as models
+  HubbardModelBase kinetic() const { return HubbardModelBase(t, 0.0, dims_, momentum_); }
+  HubbardModelBase interaction() const { return HubbardModelBase(0.0, u, dims_, momentum_); }
+  HubbardModelBase(HubbardModelBase&& o) noexcept
+      : t(o.t), u(o.u), dims_(std::move(o.dims_)), momentum_(o.momentum_),
+        h_(std::exchange(o.h_, nullptr)) {}
   HubbardModelBase(const HubbardModelBase&) = delete;
   HubbardModelBase& operator=(const HubbardModelBase&) = delete;
   ~HubbardModelBase() { mb_model_destroy(h_); }
@@ -140,6 +146,8 @@ class HubbardModelBase {
   double t, u;
 
  private:
+  std::vector<int64_t> dims_;
+  bool momentum_ = false;
   mb_model_t h_ = nullptr;
 };
 

@@ -325,6 +325,25 @@ class _Hubbard:
         _check(lib().mb_model_term_count(self._h, C.byref(n)))
         return n.value
 
+    def _part(self, t: float, u: float) -> "_Hubbard":
+        m = _Hubbard.__new__(type(self))
+        _Hubbard.__init__(m, t, u, self.dims)
+        return m
+
+    def kinetic(self) -> "_Hubbard":
+        """kinetic() (hubbard_model.h:13-22, :69-84, :141-161): the hopping
+        terms alone, as a model (U = 0)."""
+        return self._part(self.t, 0.0)
+
+    def interaction(self) -> "_Hubbard":
+        """interaction() (hubbard_model.h:24-32, :86-97, :163-176): the
+        U n_up n_down terms alone, as a model (t = 0)."""
+        return self._part(0.0, self.u)
+
+    def hamiltonian(self) -> "_Hubbard":
+        """hamiltonian() = kinetic() + interaction() (hubbard_model.h:34-38)."""
+        return self
+
 
 class HubbardModel(_Hubbard):
     def __init__(self, t, u, size):

@@ -54,6 +54,8 @@ int main(int argc, char** argv) {
   CHECK(mbgpu::HubbardModel(1.0, 2.0, 2).term_count() == 6);
   CHECK(mbgpu::HubbardModel2D(1.0, 2.0, 2, 2).term_count() == 20);
   CHECK(mbgpu::HubbardModel3D(1.0, 2.0, 2, 2, 2).term_count() == 56);
+  CHECK(chain.kinetic().term_count() + chain.interaction().term_count() == chain.term_count());
+  CHECK(chain.kinetic().u == 0.0 && chain.interaction().t == 0.0);
   auto all = mbgpu::FermionBasis::with_fixed_particle_number(8, 8);
   CHECK(all.size() == 12870);  // C(16, 8): every spin projection
   auto ksec = mbgpu::FermionBasis::with_fixed_particle_number_spin_momentum(8, 4, 0, {8}, {0});

@@ -118,3 +118,19 @@ def test_reference_order_leads_with_orbital_zero_up(mb, L, nu, nd):
     holds = (up & np.uint64(1)) != 0
     assert holds[:n_a].all() and not holds[n_a:].any()
     assert int(holds.sum()) == n_a
+
+
+def test_model_parts_match_reference_term_counts(mb):
+    """kinetic() / interaction() as models: their term counts add up to the
+    hamiltonian's (the parts share no term) and the U = 0 / t = 0 golden
+    sectors are their matrices' term counts."""
+    for dims in ((8,), (2, 2), (3, 3), (2, 2, 2)):
+        m = mb._Hubbard(1.0, 4.0, dims)
+        assert m.kinetic().term_count() + m.interaction().term_count() == m.term_count()
+        assert m.kinetic().u == 0.0 and m.interaction().t == 0.0
+        assert type(m.kinetic()) is type(m) and m.hamiltonian() is m
+    g = load_golden("chain4_n4_u0")
+    assert mb.HubbardModel(float(g["t"]), 4.0, 4).kinetic().term_count() == int(g["n_terms"])
+    mm = mb.HubbardModelMomentum(1.0, 3.0, [2])
+    g = load_golden("mfull_chain2_n2_t0")
+    assert mm.interaction().term_count() == int(g["n_terms"])
