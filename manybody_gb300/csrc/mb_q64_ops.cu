@@ -188,9 +188,24 @@ struct Events {
 };
 }  // namespace
 
+static void q_apply_host_pipeline(mb_op_s* op, const void* x_host, const void* x_mapped,
+                                  void* y_host, void* y_mapped, void* x_stage, void* y_stage);
+
 void q_apply_host_reference(mb_op_s* op, const void* x_host, const void* x_mapped, void* y_host,
                             void* y_mapped, void* x_stage, void* y_stage) {
   ensure_host_split(op);
+  try {
+    q_apply_host_pipeline(op, x_host, x_mapped, y_host, y_mapped, x_stage, y_stage);
+  } catch (...) {
+    // nothing may still read or write the caller's buffers once it sees the error
+    cudaStreamSynchronize(op->host_streams[1]);
+    cudaStreamSynchronize(op->host_streams[0]);
+    throw;
+  }
+}
+
+static void q_apply_host_pipeline(mb_op_s* op, const void* x_host, const void* x_mapped,
+                                  void* y_host, void* y_mapped, void* x_stage, void* y_stage) {
   cudaStream_t comp = op->host_streams[0], copy = op->host_streams[1];
   auto& q = qscratch_for(op, comp);
   int32_t* iperm = op_iperm(op);
