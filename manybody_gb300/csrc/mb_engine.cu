@@ -795,6 +795,15 @@ OpView slot_view(const EngineSlot& s) {
   return v;
 }
 
+// Work-list buffers only grow (by half again), so admissions and
+// retirements do not free and reallocate device memory every time.
+void reserve(std::unique_ptr<EngBuf>& b, size_t bytes) {
+  if (b && b->bytes >= bytes) return;
+  const size_t want = b ? std::max(bytes, b->bytes + b->bytes / 2) : bytes;
+  b.reset();
+  b = std::make_unique<EngBuf>(want);
+}
+
 void rebuild(mb_engine_s* e) {
   if (!e->dirty) return;
   // h_slots holds the device state of the previous list (fetched after the
@@ -863,9 +872,9 @@ void rebuild(mb_engine_s* e) {
     e->h_slots.push_back(d);
   }
   e->n_items = (int)items.size();
-  e->d_slots = std::make_unique<EngBuf>(sizeof(SlotDesc) * std::max<size_t>(e->h_slots.size(), 1));
-  e->d_items = std::make_unique<EngBuf>(sizeof(int2) * std::max<size_t>(items.size(), 1));
-  e->d_part = std::make_unique<EngBuf>(2 * sizeof(double) * std::max<size_t>(items.size(), 1));
+  reserve(e->d_slots, sizeof(SlotDesc) * std::max<size_t>(e->h_slots.size(), 1));
+  reserve(e->d_items, sizeof(int2) * std::max<size_t>(items.size(), 1));
+  reserve(e->d_part, 2 * sizeof(double) * std::max<size_t>(items.size(), 1));
   // fused slots: device addresses of their step state in the new slot array
   e->fused.clear();
   e->fused_scratch.clear();
@@ -905,8 +914,8 @@ void rebuild(mb_engine_s* e) {
                             cudaMemcpyHostToDevice, e->st));
   e->n_warp = (int)items_warp.size();
   e->n_rows = (int)items_rows.size();
-  e->d_items_warp = std::make_unique<EngBuf>(sizeof(int2) * std::max<size_t>(items_warp.size(), 1));
-  e->d_items_rows = std::make_unique<EngBuf>(sizeof(int2) * std::max<size_t>(items_rows.size(), 1));
+  reserve(e->d_items_warp, sizeof(int2) * std::max<size_t>(items_warp.size(), 1));
+  reserve(e->d_items_rows, sizeof(int2) * std::max<size_t>(items_rows.size(), 1));
   if (!items_warp.empty())
     MB_CUDA(cudaMemcpyAsync(e->d_items_warp->p, items_warp.data(),
                             sizeof(int2) * items_warp.size(), cudaMemcpyHostToDevice, e->st));
