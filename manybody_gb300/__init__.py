@@ -567,6 +567,40 @@ class GpuHubbardOperator:
         import torch
         return torch.empty(self._dim, dtype=self.dtype, device="cuda")
 
+    def _v(self, t):
+        """Device pointer of a vector of this operator (None passes): a
+        contiguous CUDA tensor of its dtype and dimension, else an error
+        before the library reads or writes past it."""
+        if t is None or isinstance(t, int):
+            return _ptr(t)
+        if not t.is_cuda or t.dtype != self.dtype or t.numel() != self._dim:
+            raise MbError(MB_ERR_INVALID_ARG,
+                          f"expected a CUDA {self.dtype} vector of {self._dim} elements, got "
+                          f"{t.dtype} {tuple(t.shape)} on {t.device}")
+        return _ptr(t)
+
+    def _f64(self, t):
+        """Device pointer of a complex128 vector of this operator's dimension."""
+        import torch
+        if t is None or isinstance(t, int):
+            return _ptr(t)
+        if not t.is_cuda or t.dtype != torch.complex128 or t.numel() != self._dim:
+            raise MbError(MB_ERR_INVALID_ARG,
+                          f"expected a CUDA complex128 vector of {self._dim} elements, got "
+                          f"{t.dtype} {tuple(t.shape)} on {t.device}")
+        return _ptr(t)
+
+    def _q(self, t):
+        """Device pointer of a Q64 vector (int64 mantissa pairs) of this operator."""
+        import torch
+        if t is None or isinstance(t, int):
+            return _ptr(t)
+        if not t.is_cuda or t.dtype != torch.int64 or t.numel() != 2 * self._dim:
+            raise MbError(MB_ERR_INVALID_ARG,
+                          f"expected a CUDA int64 ({self._dim}, 2) Q64 vector, got "
+                          f"{t.dtype} {tuple(t.shape)} on {t.device}")
+        return _ptr(t)
+
     def _stream(self, stream):
         if stream is None:
             import torch
@@ -576,13 +610,13 @@ class GpuHubbardOperator:
     def apply(self, x, out=None, order: int = ORDER_REFERENCE, stream=None):
         """y = H x (LinearOperator::apply, linear_operator.h:41)."""
         y = self.empty() if out is None else out
-        _check(lib().mb_op_apply(self._h, _ptr(x), _ptr(y), order, self._stream(stream)))
+        _check(lib().mb_op_apply(self._h, self._v(x), self._v(y), order, self._stream(stream)))
         return y
 
     def apply_affine(self, x, scale=1.0, shift=0.0, beta=0.0, z=None, out=None,
                      order: int = ORDER_REFERENCE, stream=None):
         y = self.empty() if out is None else out
-        _check(lib().mb_op_apply_affine(self._h, _ptr(x), _ptr(y), scale, shift, beta, _ptr(z),
+        _check(lib().mb_op_apply_affine(self._h, self._v(x), self._v(y), scale, shift, beta, self._v(z),
                                         order, self._stream(stream)))
         return y
 
@@ -590,7 +624,7 @@ class GpuHubbardOperator:
         """Reference-order y = H x that allocates nothing inside the library:
         for callers that own all device memory (see mb_op_apply_noalloc)."""
         y = self.empty() if out is None else out
-        _check(lib().mb_op_apply_noalloc(self._h, _ptr(x), _ptr(y), self._stream(stream)))
+        _check(lib().mb_op_apply_noalloc(self._h, self._v(x), self._v(y), self._stream(stream)))
         return y
 
     def apply_host(self, x: np.ndarray, y: np.ndarray, order: int = ORDER_REFERENCE):
@@ -603,13 +637,13 @@ class GpuHubbardOperator:
     def seed_vector(self, seed: int = 0, stream_id: int = 0, order: int = ORDER_REFERENCE,
                     out=None):
         v = self.empty() if out is None else out
-        _check(lib().mb_fill_uniform(self._h, seed, stream_id, _ptr(v), order,
+        _check(lib().mb_fill_uniform(self._h, seed, stream_id, self._v(v), order,
                                      self._stream(None)))
         return v
 
     def phase_vector(self, seed: int, stream_id: int = 0, order: int = ORDER_REFERENCE, out=None):
         v = self.empty() if out is None else out
-        _check(lib().mb_fill_phase(self._h, seed, stream_id, _ptr(v), order, self._stream(None)))
+        _check(lib().mb_fill_phase(self._h, seed, stream_id, self._v(v), order, self._stream(None)))
         return v
 
     # --- block-floating-point (PREC_Q64) vectors: int64 mantissas + exponent ---
@@ -620,13 +654,13 @@ class GpuHubbardOperator:
     def q64_from_f64(self, x, order: int = ORDER_REFERENCE, out=None, stream=None):
         q = self.q64_empty() if out is None else out
         e = C.c_int()
-        _check(lib().mb_q64_from_f64(self._h, _ptr(x), order, _ptr(q), C.byref(e),
+        _check(lib().mb_q64_from_f64(self._h, self._f64(x), order, self._q(q), C.byref(e),
                                      self._stream(stream)))
         return q, e.value
 
     def q64_to_f64(self, q, exponent: int, order: int = ORDER_REFERENCE, out=None, stream=None):
         y = self.empty() if out is None else out
-        _check(lib().mb_q64_to_f64(self._h, _ptr(q), exponent, order, _ptr(y),
+        _check(lib().mb_q64_to_f64(self._h, self._q(q), exponent, order, self._f64(y),
                                    self._stream(stream)))
         return y
 
@@ -634,7 +668,7 @@ class GpuHubbardOperator:
         """H applied to a Q64 vector (tensor order); returns (mantissas, exponent)."""
         y = self.q64_empty() if out is None else out
         e = C.c_int()
-        _check(lib().mb_op_apply_q64(self._h, _ptr(q), exponent, _ptr(y), C.byref(e),
+        _check(lib().mb_op_apply_q64(self._h, self._q(q), exponent, self._q(y), C.byref(e),
                                      self._stream(stream)))
         return y, e.value
 
@@ -645,12 +679,12 @@ class GpuHubbardOperator:
 
     def dot_re(self, x, y) -> float:
         r = C.c_double()
-        _check(lib().mb_dot_re(self._h, _ptr(x), _ptr(y), C.byref(r)))
+        _check(lib().mb_dot_re(self._h, self._v(x), self._v(y), C.byref(r)))
         return r.value
 
     def norm(self, x) -> float:
         r = C.c_double()
-        _check(lib().mb_norm(self._h, _ptr(x), C.byref(r)))
+        _check(lib().mb_norm(self._h, self._v(x), C.byref(r)))
         return r.value
 
 
@@ -718,7 +752,7 @@ def lanczos_pass_one(op: GpuHubbardOperator, b, k: int, scale: float = 1.0,
     bb = np.zeros(max(k, 1))
     steps = C.c_int64()
     bn = C.c_double()
-    _check(lib().mb_lanczos_pass_one(op.handle, _ptr(b), order, k, scale, a.ctypes.data_as(_dp),
+    _check(lib().mb_lanczos_pass_one(op.handle, op._v(b), order, k, scale, a.ctypes.data_as(_dp),
                                      bb.ctypes.data_as(_dp), C.byref(steps), C.byref(bn)))
     m = steps.value
     return LanczosDecomposition(a[:m].copy(), bb[:max(m - 1, 0)].copy(), m, bn.value)
@@ -732,9 +766,9 @@ def lanczos_pass_two(op: GpuHubbardOperator, b, decomp: LanczosDecomposition, y_
     y = np.ascontiguousarray(np.asarray(y_k, np.complex128))
     al = np.ascontiguousarray(decomp.alphas, np.float64)
     be = np.ascontiguousarray(decomp.betas if len(decomp.betas) else np.zeros(1), np.float64)
-    _check(lib().mb_lanczos_pass_two(op.handle, _ptr(b), order, scale, al.ctypes.data_as(_dp),
+    _check(lib().mb_lanczos_pass_two(op.handle, op._v(b), order, scale, al.ctypes.data_as(_dp),
                                      be.ctypes.data_as(_dp), decomp.steps_taken, decomp.b_norm,
-                                     y.view(np.float64).ctypes.data_as(_dp), _ptr(x)))
+                                     y.view(np.float64).ctypes.data_as(_dp), op._v(x)))
     return x
 
 
@@ -764,7 +798,7 @@ def _eigenpair(fn, op, k, seed, order, reorth, basis_precision, conv_tol, check_
     e = C.c_double()
     steps = C.c_int64()
     vec = op.empty() if want_vector else None
-    _check(fn(op.handle, k, _ptr(seed), order, C.byref(opts), C.byref(e), _ptr(vec),
+    _check(fn(op.handle, k, op._v(seed), order, C.byref(opts), C.byref(e), op._v(vec),
               C.byref(steps)))
     return EigenPair(e.value, vec, steps.value)
 
@@ -796,7 +830,7 @@ def time_evolve_state(op: GpuHubbardOperator, psi0, t: float, krylov_steps: int 
     """time_evolve_state (src/numerics/evolve_state.h:164-178): exp(-i t H) psi0."""
     _sync_torch()
     y = op.empty() if out is None else out
-    _check(lib().mb_time_evolve(op.handle, _ptr(psi0), order, t, krylov_steps, 0, _ptr(y)))
+    _check(lib().mb_time_evolve(op.handle, op._v(psi0), order, t, krylov_steps, 0, op._v(y)))
     return y
 
 
@@ -805,7 +839,7 @@ def imaginary_time_evolve_state(op: GpuHubbardOperator, psi0, t: float, krylov_s
     """imaginary_time_evolve_state (src/numerics/evolve_state.h): exp(-t H) psi0."""
     _sync_torch()
     y = op.empty() if out is None else out
-    _check(lib().mb_time_evolve(op.handle, _ptr(psi0), order, t, krylov_steps, 1, _ptr(y)))
+    _check(lib().mb_time_evolve(op.handle, op._v(psi0), order, t, krylov_steps, 1, op._v(y)))
     return y
 
 
@@ -813,7 +847,7 @@ def time_evolve_state_steps(op: GpuHubbardOperator, psi, t0: float, t1: float, d
                             krylov_steps: int = 30, order: int = ORDER_REFERENCE):
     """time_evolve_state_steps (src/numerics/evolve_state.h:204-231), in place."""
     _sync_torch()
-    _check(lib().mb_time_evolve_steps(op.handle, _ptr(psi), order, t0, t1, dt, krylov_steps))
+    _check(lib().mb_time_evolve_steps(op.handle, op._v(psi), order, t0, t1, dt, krylov_steps))
     return psi
 
 
@@ -854,7 +888,7 @@ class SparseKPMProjector:
         _sync_torch()
         y = self.op.empty() if out is None else out
         _check(lib().mb_kpm_projector_apply(self.op.handle, self.M, self.e_min, self.e_max,
-                                            self.e_fermi, self.padding, _ptr(v), order, _ptr(y)))
+                                            self.e_fermi, self.padding, self.op._v(v), order, self.op._v(y)))
         return y
 
 
