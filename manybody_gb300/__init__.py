@@ -844,11 +844,47 @@ def imaginary_time_evolve_state(op: GpuHubbardOperator, psi0, t: float, krylov_s
 
 
 def time_evolve_state_steps(op: GpuHubbardOperator, psi, t0: float, t1: float, dt: float,
-                            krylov_steps: int = 30, order: int = ORDER_REFERENCE):
-    """time_evolve_state_steps (src/numerics/evolve_state.h:204-231), in place."""
+                            krylov_steps: int = 30, order: int = ORDER_REFERENCE, callback=None):
+    """time_evolve_state_steps (src/numerics/evolve_state.h:204-231), in place.
+    With a callback(t, psi), it is called at t0 and after every step (steps of
+    dt, the last one shortened to end on t1), as the reference does; without
+    one the whole loop runs in the library."""
     _sync_torch()
-    _check(lib().mb_time_evolve_steps(op.handle, op._v(psi), order, t0, t1, dt, krylov_steps))
+    if callback is None:
+        _check(lib().mb_time_evolve_steps(op.handle, op._v(psi), order, t0, t1, dt,
+                                          krylov_steps))
+        return psi
+    if dt == 0.0 or t1 - t0 == 0.0:
+        callback(t0, psi)
+        return psi
+    direction = 1.0 if t1 >= t0 else -1.0
+    dt = abs(dt) * direction
+    t = t0
+    callback(t, psi)
+    while (direction > 0 and t < t1) or (direction < 0 and t > t1):
+        step = min(dt, t1 - t) if direction > 0 else max(dt, t1 - t)
+        psi.copy_(time_evolve_state(op, psi, step, krylov_steps, order))
+        t += step
+        callback(t, psi)
     return psi
+
+
+@dataclass
+class Rescaling:
+    """rescaling::Rescaling (src/numerics/rescaling.h:9-18): H_scaled = (H - b) / a."""
+    a: float
+    b: float
+
+    def rescale(self, e: float) -> float:
+        return (e - self.b) / self.a
+
+    def inverse(self, e_scaled: float) -> float:
+        return e_scaled * self.a + self.b
+
+
+def rescaling_from_bounds(e_min: float, e_max: float, padding: float = 0.01) -> Rescaling:
+    """rescaling::from_bounds (src/numerics/rescaling.h:33-38), the KPM drivers' map."""
+    return Rescaling((e_max - e_min) / 2.0 * (1.0 + padding), (e_max + e_min) / 2.0)
 
 
 def kpm_dos_moments(op: GpuHubbardOperator, n_moments: int, n_probes: int, seed: int,

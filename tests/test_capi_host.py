@@ -134,3 +134,15 @@ def test_model_parts_match_reference_term_counts(mb):
     mm = mb.HubbardModelMomentum(1.0, 3.0, [2])
     g = load_golden("mfull_chain2_n2_t0")
     assert mm.interaction().term_count() == int(g["n_terms"])
+
+
+def test_rescaling_from_bounds(mb):
+    """rescaling_from_bounds_* and rescale/inverse (test_rescaling.cpp:9-92), host side."""
+    r = mb.rescaling_from_bounds(-3.0, 5.0, 0.0)
+    assert r.a == 4.0 and r.b == 1.0
+    assert r.rescale(-3.0) == -1.0 and r.rescale(5.0) == 1.0 and r.inverse(0.5) == 3.0
+    for e in (-2.5, 0.0, 4.75):
+        assert abs(r.inverse(r.rescale(e)) - e) < 1e-14
+    rp = mb.rescaling_from_bounds(-3.0, 5.0, 0.1)
+    assert abs(rp.a - 4.4) < 1e-14 and rp.b == 1.0
+    assert -1.0 < rp.rescale(-3.0) < rp.rescale(5.0) < 1.0

@@ -135,3 +135,76 @@ def test_vectors_of_the_wrong_type_or_size_are_refused(mb, cuda):
         assert e.value.status == mb.MB_ERR_INVALID_ARG
         with pytest.raises(mb.MbError):
             mb.find_min_eigenpair(op, 3, v)
+
+
+def exact_evolution(A, psi, t, imaginary=False):
+    E, V = np.linalg.eigh(A)
+    f = np.exp(-t * E) if imaginary else np.exp(-1j * t * E)
+    return V @ (f * (V.conj().T @ psi))
+
+
+def test_stepped_evolution_with_callback_matches_exact(mb, cuda):
+    """time_evolve_state_steps_calls_callback_and_matches_exact_expm
+    (test_evolve_state.cpp:67-98): 2x2 diagonal, 2 Krylov steps, t 0 -> 0.3 by
+    0.1: four callbacks from t0 to t1, state within 1e-8 of exp(-i t H)."""
+    torch = cuda
+    A = np.diag([0.5, 1.5])
+    op = op_of(mb, A)
+    psi0 = np.array([0.3 - 0.4j, 0.2 + 0.1j])
+    psi = torch.tensor(psi0, dtype=torch.complex128, device="cuda")
+    times = []
+    mb.time_evolve_state_steps(op, psi, 0.0, 0.3, 0.1, krylov_steps=2,
+                               callback=lambda t, v: times.append(t))
+    assert len(times) == 4 and abs(times[0]) < 1e-12 and abs(times[-1] - 0.3) < 1e-12
+    ref = exact_evolution(A, psi0, 0.3)
+    assert np.linalg.norm(psi.cpu().numpy() - ref) / np.linalg.norm(ref) < 1e-8
+    # the library's own loop, no callback (time_evolve_state_steps_matches_exact_expm)
+    A2 = np.diag([1.0, 2.0])
+    p2 = torch.tensor([1.0, 1j], dtype=torch.complex128, device="cuda")
+    mb.time_evolve_state_steps(op_of(mb, A2), p2, 0.0, 0.3, 0.1, krylov_steps=2)
+    ref2 = exact_evolution(A2, np.array([1.0, 1j]), 0.3)
+    assert np.linalg.norm(p2.cpu().numpy() - ref2) / np.linalg.norm(ref2) < 1e-8
+
+
+def test_imaginary_time_evolution_matches_exact(mb, cuda):
+    """imaginary_time_evolve_state_matches_exact_expm (test_evolve_state.cpp:100-121)."""
+    torch = cuda
+    A = np.diag([0.2, 1.1])
+    psi0 = np.array([0.6 + 0.1j, -0.3 + 0.2j])
+    y = mb.imaginary_time_evolve_state(op_of(mb, A), torch.tensor(psi0, device="cuda"), 0.7,
+                                       krylov_steps=2).cpu().numpy()
+    ref = exact_evolution(A, psi0, 0.7, imaginary=True)
+    assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < 1e-8
+
+
+def test_lanczos_exp_solver_matches_direct_expm(mb, cuda):
+    """lanczos_exp_solver_matches_direct_expm (test_lanczos.cpp:104-134): solve()
+    with y = exp(T) e1 over the full Krylov space is exp(A) b."""
+    torch = cuda
+    rng = np.random.default_rng(2)
+    M = rng.normal(size=(5, 5))
+    A = (M + M.T) / 4.0
+    b = rng.normal(size=5)
+
+    def exp_solver(a, be):
+        T = np.diag(a) + np.diag(be, 1) + np.diag(be, -1)
+        E, V = np.linalg.eigh(T)
+        return V @ (np.exp(E) * V[0])
+
+    x = mb.solve(op_of(mb, A), torch.tensor(b + 0j, device="cuda"), 5, exp_solver).cpu().numpy()
+    E, V = np.linalg.eigh(A)
+    ref = V @ (np.exp(E) * (V.T @ b))
+    assert np.linalg.norm(x - ref) / np.linalg.norm(ref) < 1e-8
+
+
+def test_kpm_projector_apply_matches_its_matrix(mb, cuda):
+    """kpm_projector_apply_matches_matrix (test_kpm.cpp:103-121): a 6-site chain."""
+    torch = cuda
+    A = -(np.diag(np.ones(5), 1) + np.diag(np.ones(5), -1))
+    P = projector_matrix(mb, torch, A, 100, 0.0)
+    v = np.random.default_rng(6).normal(size=6)
+    E = np.linalg.eigvalsh(A)
+    proj = mb.SparseKPMProjector(op_of(mb, A), 100, float(E[0]), float(E[-1]), 0.0)
+    pv = proj.apply(torch.tensor(v + 0j, device="cuda")).cpu().numpy()
+    assert np.linalg.norm(P @ v - pv) < 1e-10
+
