@@ -267,7 +267,10 @@ def run_gpu(args):
         torch.cuda.empty_cache()
 
     if not args.no_extras:
-        for name, fn in (("cfg2_solve", run_cfg2_extra), ("momentum", run_momentum_extra),
+        runs = [("cfg2_solve", run_cfg2_extra)]
+        if args.cfg2_reorth:  # ~2.5 minutes: off by default
+            runs.append(("cfg2_reorth", run_cfg2_reorth_extra))
+        for name, fn in (*runs, ("momentum", run_momentum_extra),
                          ("batch", run_batch_extra),
                          ("precision", run_precision_extra), ("serve", run_serve_extra)):
             try:
@@ -426,6 +429,26 @@ def run_cfg2_extra(mb, torch, n_probes=2, n_moments=1024):
                 "projected_seconds_16_probes": round(16 * t_kpm / n_probes, 2),
                 "mu0": float(mu[0]), "mu_1_to_4": [float(v) for v in mu[1:5]]},
     }
+
+
+def run_cfg2_reorth_extra(mb, torch, k=300):
+    """4x4, 6+6, U=8: Lanczos with full re-orthogonalisation (CGS2 against every
+    stored Krylov vector) for all 300 steps, as the 4x4 configuration names it.
+    300 complex128 or Q64 vectors would be 308 GB, so the FP64 operator keeps
+    its Krylov basis in complex64 (154 GB); the recurrence, the projections
+    and the tridiagonal eigensolve stay FP64."""
+    basis = mb.FermionBasis.with_fixed_particle_number_and_spin(16, 12, 0)
+    op = mb.GpuHubbardOperator(basis, mb.HubbardModel2D(1.0, 8.0, 4, 4), mb.PREC_F64)
+    seed = op.seed_vector(0, order=mb.ORDER_TENSOR)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = mb.find_min_eigenpair(op, k, seed, order=mb.ORDER_TENSOR, reorth=True,
+                              basis_precision=mb.PREC_F32, want_vector=False)
+    t = time.perf_counter() - t0
+    del seed, op
+    return {"workload": "2D 4x4 periodic, t=1, U=8, N_up=N_down=6, FP64 operator",
+            "lanczos_steps": r.steps, "reorth": "CGS2 against every stored vector",
+            "krylov_basis": "complex64, 154 GB", "e0": r.value, "seconds": round(t, 3)}
 
 
 def run_momentum_extra(mb, torch):
@@ -730,6 +753,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batching / precision / serving extras")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--cfg2-reorth", action="store_true",
+                    help="also run 300 Lanczos steps with full re-orthogonalisation at 4x4 6+6")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
