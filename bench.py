@@ -395,7 +395,7 @@ def run_batch_extra(mb, torch):
     }
 
 
-def run_cfg2_extra(mb, torch, n_probes=2, n_moments=1024):
+def run_cfg2_extra(mb, torch, n_probes=16, n_moments=1024):
     """4x4, 6+6, U=8 on Q64 vectors: the ground state by plain Lanczos (the
     reference's find_min_eigenpair) to Ritz stability 1e-12, at most 300 steps;
     the top of the spectrum the same way; then DOS Chebyshev moments with
@@ -426,7 +426,6 @@ def run_cfg2_extra(mb, torch, n_probes=2, n_moments=1024):
         "e_max": hi.value, "e_max_lanczos_steps": hi.steps, "e_max_seconds": round(t_hi, 3),
         "kpm": {"moments": n_moments, "probes": n_probes, "seconds": round(t_kpm, 3),
                 "seconds_per_probe": round(t_kpm / n_probes, 3),
-                "projected_seconds_16_probes": round(16 * t_kpm / n_probes, 2),
                 "mu0": float(mu[0]), "mu_1_to_4": [float(v) for v in mu[1:5]]},
     }
 
