@@ -268,7 +268,7 @@ def run_gpu(args):
 
     if not args.no_extras:
         runs = [("cfg2_solve", run_cfg2_extra)]
-        if args.cfg2_reorth:  # ~2.5 minutes: off by default
+        if args.cfg2_reorth:  # about a minute: off by default
             runs.append(("cfg2_reorth", run_cfg2_reorth_extra))
         for name, fn in (*runs, ("momentum", run_momentum_extra),
                          ("batch", run_batch_extra),

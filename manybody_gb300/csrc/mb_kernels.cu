@@ -636,6 +636,11 @@ k_multi_dot(int64_t n, const typename C2<TV>::type* __restrict__ V, int64_t ld, 
   using VW = typename C2<TW>::type;
   __shared__ double acc[2 * kMaxBasis];
   __shared__ double2 sw[kMdChunk];
+  // a complex64 basis against a complex128 w: w split into float hi + lo
+  // parts, products on the FP32 pipe (exact products, compensated sums),
+  // FP64 per chunk; the FP64 pipe runs at 1/57 of the FP32 rate here
+  constexpr bool kSplit = sizeof(TV) == 4 && sizeof(TW) == 8;
+  __shared__ float4 swf[kSplit ? kMdChunk : 1];
   for (int j = threadIdx.x; j < 2 * m; j += blockDim.x) acc[j] = 0.0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int64_t base = (int64_t)blockIdx.x * kMdChunk; base < n; base += (int64_t)gridDim.x * kMdChunk) {
@@ -643,20 +648,43 @@ k_multi_dot(int64_t n, const typename C2<TV>::type* __restrict__ V, int64_t ld, 
     __syncthreads();
     for (int i = threadIdx.x; i < len; i += blockDim.x) {
       const VW a = w[base + i];
-      sw[i] = make_double2((double)a.x, (double)a.y);
+      if constexpr (kSplit) {
+        const float hx = (float)a.x, hy = (float)a.y;
+        swf[i] = make_float4(hx, hy, (float)((double)a.x - (double)hx),
+                             (float)((double)a.y - (double)hy));
+      } else {
+        sw[i] = make_double2((double)a.x, (double)a.y);
+      }
     }
     __syncthreads();
     for (int j = warp; j < m; j += nwarps) {
       const VV* vj = V + (int64_t)j * ld + base;
       double cr = 0.0, ci = 0.0;
-      for (int i = lane; i < len; i += 32) {
-        const VV a = vj[i];
-        const double ar = (double)a.x, ai = (double)a.y;
-        const double2 b = sw[i];
-        cr = fma(ar, b.x, cr);
-        cr = fma(ai, b.y, cr);
-        ci = fma(ar, b.y, ci);
-        ci = fma(-ai, b.x, ci);
+      if constexpr (kSplit) {
+        DotAcc<float> pr, pi;
+        float lr = 0.f, li = 0.f;
+        for (int i = lane; i < len; i += 32) {
+          const VV a = vj[i];
+          const float4 b = swf[i];
+          pr.add_prod(a.x, b.x);
+          pr.add_prod(a.y, b.y);
+          pi.add_prod(a.x, b.y);
+          pi.add_prod(-a.y, b.x);
+          lr = fmaf(a.x, b.z, fmaf(a.y, b.w, lr));
+          li = fmaf(a.x, b.w, fmaf(-a.y, b.z, li));
+        }
+        cr = pr.value() + (double)lr;
+        ci = pi.value() + (double)li;
+      } else {
+        for (int i = lane; i < len; i += 32) {
+          const VV a = vj[i];
+          const double ar = (double)a.x, ai = (double)a.y;
+          const double2 b = sw[i];
+          cr = fma(ar, b.x, cr);
+          cr = fma(ai, b.y, cr);
+          ci = fma(ar, b.y, ci);
+          ci = fma(-ai, b.x, ci);
+        }
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -706,16 +734,36 @@ k_multi_axpy(int64_t n, const typename C2<TV>::type* __restrict__ V, int64_t ld,
   __shared__ double sc[2 * kMaxBasis];
   for (int j = threadIdx.x; j < 2 * m; j += blockDim.x) sc[j] = c[j];
   __syncthreads();
+  // a complex64 basis under a complex128 w: the correction sum_j c_j V_j on
+  // the FP32 pipe (it is small next to w: the projections measure lost
+  // orthogonality), subtracted in FP64
+  constexpr bool kSplit = sizeof(TV) == 4 && sizeof(TW) == 8;
+  __shared__ float scf[kSplit ? 2 * kMaxBasis : 1];
+  if constexpr (kSplit)
+    for (int j = threadIdx.x; j < 2 * m; j += blockDim.x) scf[j] = (float)c[j];
+  __syncthreads();
   DotAcc<double> ww;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const VW wv = w[i];
     double sr = (double)wv.x, si = (double)wv.y;
-    for (int j = 0; j < m; ++j) {
-      const VV a = V[(int64_t)j * ld + i];
-      const double cr = sc[2 * j], ci = sc[2 * j + 1];
-      sr -= cr * (double)a.x - ci * (double)a.y;
-      si -= cr * (double)a.y + ci * (double)a.x;
+    if constexpr (kSplit) {
+      float fr = 0.f, fi = 0.f;
+      for (int j = 0; j < m; ++j) {
+        const VV a = V[(int64_t)j * ld + i];
+        const float cr = scf[2 * j], ci = scf[2 * j + 1];
+        fr = fmaf(cr, a.x, fmaf(-ci, a.y, fr));
+        fi = fmaf(cr, a.y, fmaf(ci, a.x, fi));
+      }
+      sr -= (double)fr;
+      si -= (double)fi;
+    } else {
+      for (int j = 0; j < m; ++j) {
+        const VV a = V[(int64_t)j * ld + i];
+        const double cr = sc[2 * j], ci = sc[2 * j + 1];
+        sr -= cr * (double)a.x - ci * (double)a.y;
+        si -= cr * (double)a.y + ci * (double)a.x;
+      }
     }
     VW o;
     o.x = (decltype(o.x))sr;
