@@ -268,7 +268,7 @@ def run_gpu(args):
 
     if not args.no_extras:
         runs = [("cfg2_solve", run_cfg2_extra)]
-        if args.cfg2_reorth:  # about a minute: off by default
+        if not args.skip_cfg2_reorth:  # about a minute
             runs.append(("cfg2_reorth", run_cfg2_reorth_extra))
         for name, fn in (*runs, ("momentum", run_momentum_extra),
                          ("batch", run_batch_extra),
@@ -752,8 +752,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batching / precision / serving extras")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--cfg2-reorth", action="store_true",
-                    help="also run 300 Lanczos steps with full re-orthogonalisation at 4x4 6+6")
+    ap.add_argument("--skip-cfg2-reorth", action="store_true",
+                    help="leave out the 300-step fully re-orthogonalised Lanczos at 4x4 6+6")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
