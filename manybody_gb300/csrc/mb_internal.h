@@ -467,6 +467,23 @@ void upload_binomials(cudaStream_t st);
 int32_t* op_perm(mb_op_s* op);
 // reference -> tensor index table (inverse of op_perm), built on first use
 int32_t* op_iperm(mb_op_s* op);
+// split row schedule and streams of the pipelined host-buffer applies
+void ensure_host_split(mb_op_s* op);
+
+// CUDA events without timing, destroyed with the owner.
+struct Events {
+  std::vector<cudaEvent_t> ev;
+  explicit Events(int n) : ev((size_t)n, nullptr) {
+    for (auto& e : ev) MB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  ~Events() {
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+  Events(const Events&) = delete;
+  Events& operator=(const Events&) = delete;
+  cudaEvent_t operator[](int i) const { return ev[(size_t)i]; }
+};
 void launch_invert_perm(int64_t n, const int32_t* perm, int32_t* iperm, cudaStream_t st);
 
 // FP64 refinement of a ground-state estimate: Rayleigh-Ritz on the Krylov

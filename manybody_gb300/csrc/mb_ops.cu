@@ -481,6 +481,42 @@ static void from_tensor(mb_op_s* op, const void* src, void* dst, int order, cuda
   launch_gather(op->precision, op->dim, op_iperm(op), src, dst, st);
 }
 
+// The row schedule split for pipelined host-buffer applies: the rows whose up
+// configuration holds orbital 0 (the reference order's first block, indices
+// [0, rows_a * Dd)) in schedule order, then the rest; and two non-blocking
+// streams.  Built on the first host-buffer call.
+void ensure_host_split(mb_op_s* op) {
+  std::lock_guard<std::mutex> lk(op->mu);
+  if (op->split_sched) return;
+  const int64_t Du = op->Du;
+  std::vector<int32_t> sched((size_t)Du);
+  std::vector<uint32_t> um((size_t)Du);
+  if (op->view.row_sched) {
+    MB_CUDA(cudaMemcpy(sched.data(), op->view.row_sched, sizeof(int32_t) * (size_t)Du,
+                       cudaMemcpyDeviceToHost));
+  } else {
+    for (int64_t r = 0; r < Du; ++r) sched[(size_t)r] = (int32_t)r;
+  }
+  MB_CUDA(cudaMemcpy(um.data(), op->view.up_mask, sizeof(uint32_t) * (size_t)Du,
+                     cudaMemcpyDeviceToHost));
+  std::vector<int32_t> split;
+  split.reserve((size_t)Du);
+  for (int32_t r : sched)
+    if (um[(size_t)r] & 1u) split.push_back(r);
+  const int64_t rows_a = (int64_t)split.size();
+  for (int32_t r : sched)
+    if (!(um[(size_t)r] & 1u)) split.push_back(r);
+  void* p = nullptr;
+  MB_CUDA(cudaMalloc(&p, sizeof(int32_t) * (size_t)std::max<int64_t>(Du, 1)));
+  op->allocations.push_back(p);
+  MB_CUDA(cudaMemcpy(p, split.data(), sizeof(int32_t) * (size_t)Du, cudaMemcpyHostToDevice));
+  for (cudaStream_t& h : op->host_streams)
+    if (!h) MB_CUDA(cudaStreamCreateWithFlags(&h, cudaStreamNonBlocking));
+  op->split_rows_a = rows_a;
+  op->split_sched = (int32_t*)p;
+}
+
+
 static void check_order(int order) {
   MB_REQUIRE(order == MB_ORDER_REFERENCE || order == MB_ORDER_TENSOR, MB_ERR_INVALID_ARG,
              "order must be MB_ORDER_REFERENCE or MB_ORDER_TENSOR");
@@ -998,6 +1034,72 @@ int mb_op_apply_affine(mb_op_t op, const void* x_dev, void* y_dev, double scale,
   });
 }
 
+// The host-buffer apply of a complex128 / complex64 lattice operator in
+// reference order, pipelined over the host link as the Q64 one is: x lands
+// scattered to tensor order (a page-locked x read over the link by the
+// scatter kernel, a pageable one in chunks), the rows holding orbital 0 (the
+// reference order's first block) are applied first and their results go
+// back in pieces on the copy engine while the other rows are applied.  Same
+// kernels and arithmetic as mb_op_apply, so the same bits.
+static void host_apply_pipeline(mb_op_s* op, const void* x_host, const void* x_mapped,
+                                void* y_host, void* y_mapped, mb_op_s::Scratch& s) {
+  cudaStream_t comp = op->host_streams[0], copy = op->host_streams[1];
+  int32_t* iperm = op_iperm(op);
+  const int prec = op->precision;
+  const size_t es = elem_bytes(prec);
+  const int64_t n = op->dim, n_a = op->split_rows_a * op->Dd;
+  char* xt = (char*)s.a;  // tensor order
+  char* yt = (char*)s.b;
+  char* xs = (char*)s.hx;  // landing / staging, reference order
+  char* ys = (char*)s.hy;
+  constexpr int kChunks = 8, kPieces = 4;
+  Events ev(kChunks + kPieces + 1);
+  if (x_mapped) {
+    launch_scatter(prec, n, iperm, x_mapped, xt, comp);
+  } else {
+    const int64_t step = (n + kChunks - 1) / kChunks;
+    for (int c = 0; c < kChunks; ++c) {
+      const int64_t i0 = std::min<int64_t>(n, c * step), i1 = std::min<int64_t>(n, i0 + step);
+      if (i1 > i0)
+        MB_CUDA(cudaMemcpyAsync(xs + es * (size_t)i0, (const char*)x_host + es * (size_t)i0,
+                                es * (size_t)(i1 - i0), cudaMemcpyHostToDevice, copy));
+      MB_CUDA(cudaEventRecord(ev[c], copy));
+      MB_CUDA(cudaStreamWaitEvent(comp, ev[c], 0));
+      if (i1 > i0) launch_scatter(prec, i1 - i0, iperm + i0, xs + es * (size_t)i0, xt, comp);
+    }
+  }
+  OpView va = op->view, vb = op->view;
+  va.row_sched = op->split_sched;
+  va.Du = op->split_rows_a;
+  vb.row_sched = op->split_sched + op->split_rows_a;
+  vb.Du = op->Du - op->split_rows_a;
+  if (va.Du > 0) launch_apply(va, prec, xt, yt, 1.0, 0.0, 0.0, nullptr, nullptr, 0, comp);
+  const int64_t piece = (n_a + kPieces - 1) / kPieces;
+  for (int k = 0; k < kPieces; ++k) {
+    const int64_t i0 = std::min<int64_t>(n_a, k * piece), i1 = std::min<int64_t>(n_a, i0 + piece);
+    if (i1 > i0) launch_gather(prec, i1 - i0, iperm + i0, yt, ys + es * (size_t)i0, comp);
+    MB_CUDA(cudaEventRecord(ev[kChunks + k], comp));
+  }
+  if (vb.Du > 0) launch_apply(vb, prec, xt, yt, 1.0, 0.0, 0.0, nullptr, nullptr, 0, comp);
+  char* y_b = y_mapped ? (char*)y_mapped + es * (size_t)n_a : ys + es * (size_t)n_a;
+  if (n > n_a) launch_gather(prec, n - n_a, iperm + n_a, yt, y_b, comp);
+  MB_CUDA(cudaEventRecord(ev[kChunks + kPieces], comp));
+  for (int k = 0; k < kPieces; ++k) {
+    const int64_t i0 = std::min<int64_t>(n_a, k * piece), i1 = std::min<int64_t>(n_a, i0 + piece);
+    MB_CUDA(cudaStreamWaitEvent(copy, ev[kChunks + k], 0));
+    if (i1 > i0)
+      MB_CUDA(cudaMemcpyAsync((char*)y_host + es * (size_t)i0, ys + es * (size_t)i0,
+                              es * (size_t)(i1 - i0), cudaMemcpyDeviceToHost, copy));
+  }
+  if (!y_mapped && n > n_a) {
+    MB_CUDA(cudaStreamWaitEvent(copy, ev[kChunks + kPieces], 0));
+    MB_CUDA(cudaMemcpyAsync((char*)y_host + es * (size_t)n_a, ys + es * (size_t)n_a,
+                            es * (size_t)(n - n_a), cudaMemcpyDeviceToHost, copy));
+  }
+  MB_CUDA(cudaStreamSynchronize(copy));
+  MB_CUDA(cudaStreamSynchronize(comp));
+}
+
 int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
   return guard([&] {
     MB_REQUIRE(op && x_host && y_host, MB_ERR_INVALID_ARG, "NULL argument");
@@ -1017,17 +1119,29 @@ int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
                         at.type == cudaMemoryTypeHost && at.devicePointer != nullptr;
     if (!direct) cudaGetLastError();  // clear a failed query on pageable memory
     if (direct) y_dev = at.devicePointer;
-    if (op->precision == MB_PREC_Q64 && order == MB_ORDER_REFERENCE && !op->natural_order &&
-        !op->view.n_blocks && !op->view.csr_row) {
-      // x lands in chunks, each scattered to tensor order while the next is
-      // in flight; the result's first reference block goes back while the
-      // rest of the apply runs
+    if (order == MB_ORDER_REFERENCE && !op->natural_order && !op->view.n_blocks &&
+        !op->view.csr_row) {
+      // x lands scattered to tensor order as it arrives; the result's first
+      // reference block goes back while the rest of the apply runs
       cudaPointerAttributes ax{};
       const bool x_locked = cudaPointerGetAttributes(&ax, x_host) == cudaSuccess &&
                             ax.type == cudaMemoryTypeHost && ax.devicePointer != nullptr;
       if (!x_locked) cudaGetLastError();
-      q_apply_host_reference(op, x_host, x_locked ? ax.devicePointer : nullptr, y_host,
-                             direct ? at.devicePointer : nullptr, s.hx, s.hy);
+      const void* x_mapped = x_locked ? ax.devicePointer : nullptr;
+      void* y_mapped = direct ? at.devicePointer : nullptr;
+      if (op->precision == MB_PREC_Q64) {
+        q_apply_host_reference(op, x_host, x_mapped, y_host, y_mapped, s.hx, s.hy);
+        return;
+      }
+      ensure_host_split(op);
+      try {
+        host_apply_pipeline(op, x_host, x_mapped, y_host, y_mapped, s);
+      } catch (...) {
+        // nothing may still read or write the caller's buffers once it sees the error
+        cudaStreamSynchronize(op->host_streams[1]);
+        cudaStreamSynchronize(op->host_streams[0]);
+        throw;
+      }
       return;
     }
     MB_CUDA(cudaMemcpyAsync(s.hx, x_host, vb, cudaMemcpyHostToDevice, st));

@@ -143,50 +143,6 @@ void q_apply_affine(mb_op_s* op, const void* x, void* y, double scale, double sh
 // is that of mb_op_apply (same exponent, same kernel per row), so the result
 // is bit-identical to the device-buffer call.
 // ---------------------------------------------------------------------------
-static void ensure_host_split(mb_op_s* op) {
-  std::lock_guard<std::mutex> lk(op->mu);
-  if (op->split_sched) return;
-  const int64_t Du = op->Du;
-  std::vector<int32_t> sched((size_t)Du);
-  std::vector<uint32_t> um((size_t)Du);
-  if (op->view.row_sched) {
-    MB_CUDA(cudaMemcpy(sched.data(), op->view.row_sched, sizeof(int32_t) * (size_t)Du,
-                       cudaMemcpyDeviceToHost));
-  } else {
-    for (int64_t r = 0; r < Du; ++r) sched[(size_t)r] = (int32_t)r;
-  }
-  MB_CUDA(cudaMemcpy(um.data(), op->view.up_mask, sizeof(uint32_t) * (size_t)Du,
-                     cudaMemcpyDeviceToHost));
-  std::vector<int32_t> split;
-  split.reserve((size_t)Du);
-  for (int32_t r : sched)
-    if (um[(size_t)r] & 1u) split.push_back(r);
-  const int64_t rows_a = (int64_t)split.size();
-  for (int32_t r : sched)
-    if (!(um[(size_t)r] & 1u)) split.push_back(r);
-  void* p = nullptr;
-  MB_CUDA(cudaMalloc(&p, sizeof(int32_t) * (size_t)std::max<int64_t>(Du, 1)));
-  op->allocations.push_back(p);
-  MB_CUDA(cudaMemcpy(p, split.data(), sizeof(int32_t) * (size_t)Du, cudaMemcpyHostToDevice));
-  for (cudaStream_t& h : op->host_streams)
-    if (!h) MB_CUDA(cudaStreamCreateWithFlags(&h, cudaStreamNonBlocking));
-  op->split_rows_a = rows_a;
-  op->split_sched = (int32_t*)p;
-}
-
-namespace {
-struct Events {
-  std::vector<cudaEvent_t> ev;
-  explicit Events(int n) : ev((size_t)n, nullptr) {
-    for (auto& e : ev) MB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  }
-  ~Events() {
-    for (auto& e : ev)
-      if (e) cudaEventDestroy(e);
-  }
-  cudaEvent_t operator[](int i) const { return ev[(size_t)i]; }
-};
-}  // namespace
 
 static void q_apply_host_pipeline(mb_op_s* op, const void* x_host, const void* x_mapped,
                                   void* y_host, void* y_mapped, void* x_stage, void* y_stage);

@@ -295,6 +295,32 @@ def test_concurrent_apply_on_streams(mb, cuda):
         assert np.linalg.norm(y.cpu().numpy() - ref) <= 1e-13 * np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("pinned", [True, False])
+@pytest.mark.parametrize("dims,n_up,n_down", [
+    ((4, 4), 5, 5),  # 19,079,424 states: every landing chunk and download piece in use
+    ((8,), 0, 3),    # no up electron: the first reference block is empty
+    ((6,), 6, 2),    # every up configuration holds orbital 0
+    ((3, 2), 2, 3),
+])
+def test_host_apply_bit_identical(mb, cuda, prec, pinned, dims, n_up, n_down):
+    """The pipelined host-buffer apply of a complex128 / complex64 operator in
+    reference order equals the device-buffer apply bit for bit, with page-locked
+    and with pageable host buffers."""
+    torch = cuda
+    _, _, op = make(mb, dims, 1.0, 8.0, n_up, n_down, prec)
+    x = op.seed_vector(5)
+    y = op.apply(x).cpu()
+    xh = x.cpu()
+    yh = torch.full_like(xh, float("nan"))
+    if pinned:
+        xh, yh = xh.pin_memory(), yh.pin_memory()
+    op.apply_host(xh, yh)
+    assert torch.equal(yh, y)
+    del x, y
+    torch.cuda.empty_cache()
+
+
 @pytest.mark.parametrize("prec", [0, 1, 2])
 def test_concurrent_apply_from_host_threads(mb, cuda, prec):
     """Several host threads share one operator: each applies on its own stream
