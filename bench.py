@@ -651,14 +651,21 @@ def run_serve_extra(mb, torch, n_requests=400, rate=200.0):
 # CSC apply), on a bounded sample.
 # ---------------------------------------------------------------------------
 def cpu_sample_matrix():
+    """The sample's H by the restated compute_matrix_elements (normal ordering
+    of H|key_j>, OpenMP over columns), with that build's wall time: the
+    reference's CPU path is this build once, then serial applies."""
     import oracle
     # same lattice and interaction, a sector small enough to build in seconds
-    return oracle.hubbard_csc([4, 4], 1.0, 8.0, 3, 3), "4x4 U=8 sector N_up=N_down=3 (313,600 states)"
+    t0 = time.perf_counter()
+    H = oracle.hubbard_csc([4, 4], 1.0, 8.0, 3, 3)
+    build = {"build_seconds": round(time.perf_counter() - t0, 3),
+             "build_cores": oracle.max_threads()}
+    return H, "4x4 U=8 sector N_up=N_down=3 (313,600 states)", build
 
 
 def cpu_baseline(seconds: float = 10.0):
     import numpy as np
-    H, sample = cpu_sample_matrix()
+    H, sample, build = cpu_sample_matrix()
     x = np.ascontiguousarray(
         np.random.default_rng(0).uniform(-1, 1, H.dim) + 1j * np.random.default_rng(1).uniform(-1, 1, H.dim))
     H.apply(x)
@@ -674,6 +681,7 @@ def cpu_baseline(seconds: float = 10.0):
             "kind": "port",
             "sample": f"{sample}; serial CSC column-scatter apply, {n} applies in {el:.1f}s, "
                       f"nnz={H.nnz}",
+            **build,
             "best_effort_all_cores": cpu_parallel(H, x, sample, seconds / 2)}
 
 
@@ -701,7 +709,7 @@ def run_reference(args):
     if rank != 0:
         return
     import numpy as np
-    H, sample = cpu_sample_matrix()
+    H, sample, build = cpu_sample_matrix()
     x = np.ascontiguousarray(np.random.default_rng(0).uniform(-1, 1, H.dim) + 0j)
     for _ in range(args.warmup):
         H.apply(x)
@@ -732,6 +740,7 @@ def run_reference(args):
                                    f"(restated) applied by a serial CSC column scatter "
                                    f"(Armadillo sp_cx_mat*cx_vec with ARMA_OPENMP_THREADS=1: "
                                    f"the reference's apply uses one thread)",
+                         **build,
                          "best_effort_all_cores": cpu_parallel(H, x, sample, 5.0)},
         "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
