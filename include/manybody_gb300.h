@@ -192,9 +192,10 @@ int mb_op_apply(mb_op_t op, const void* x_dev, void* y_dev, int order, void* str
 int mb_op_apply_affine(mb_op_t op, const void* x_dev, void* y_dev, double scale, double shift,
                        double beta, const void* z_dev, int order, void* stream);
 /* apply() with host buffers: copies x in, applies, copies y out, then waits.
- * In reference order on a lattice operator the copies overlap the apply (the
- * first reference block is computed first and goes back while the rest runs);
- * page-locked buffers are read and written over the link by the kernels.
+ * In reference order on a lattice operator the copies overlap the apply: rows
+ * run in groups ordered by where their states first appear in the reference
+ * order, and each finished prefix of y goes back while later groups run; a
+ * page-locked x is read over the link by the kernel that scatters it.
  * Safe from several host threads; calls on one operator run one at a time. */
 int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order);
 

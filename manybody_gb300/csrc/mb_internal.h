@@ -378,11 +378,14 @@ struct mb_op_s {
   int32_t* iperm = nullptr;        // reference -> tensor index (lazy)
   std::mutex mu;
   std::mutex host_mu;  // host-buffer calls: one at a time (shared staging, stream 0)
-  // Pipelined host-buffer apply (MB_PREC_Q64, reference order): the row
-  // schedule split into rows whose up state holds orbital 0 (reference
-  // indices [0, rows_a * Dd)) and the rest; two non-blocking streams.
-  int32_t* split_sched = nullptr;
-  int64_t split_rows_a = 0;
+  // Pipelined host-buffer apply (lattice operators, reference order): the
+  // rows in groups by the first reference index among their states, each
+  // group in the row schedule's order, so that once groups 0..g are applied
+  // the reference indices [0, host_ready[g]) are final; group g is
+  // host_sched[host_row0[g], host_row0[g+1]).  Two non-blocking streams.
+  int32_t* host_sched = nullptr;
+  std::vector<int64_t> host_row0;
+  std::vector<int64_t> host_ready;
   cudaStream_t host_streams[2] = {nullptr, nullptr};
   struct Scratch {
     void* a = nullptr;  // tensor-order copies for reference-order calls
@@ -467,8 +470,19 @@ void upload_binomials(cudaStream_t st);
 int32_t* op_perm(mb_op_s* op);
 // reference -> tensor index table (inverse of op_perm), built on first use
 int32_t* op_iperm(mb_op_s* op);
-// split row schedule and streams of the pipelined host-buffer applies
-void ensure_host_split(mb_op_s* op);
+// first[r] = the smallest reference index of tensor row r's states
+void launch_row_first(int64_t Du, int64_t Dd, const int32_t* perm, int32_t* first,
+                      cudaStream_t st);
+// row groups and streams of the pipelined host-buffer applies
+void ensure_host_groups(mb_op_s* op);
+// The result side of a pipelined host-buffer apply, on the operator's host
+// streams: per row group, apply_rows(view of the group's rows) and
+// gather(i0, i1, dst) (reference indices [i0, i1) of the result to dst) on the
+// compute stream; each finished reference range goes from y_stage to y_host on
+// the copy stream while later groups run.  Returns once y_host is written.
+void host_groups_run(mb_op_s* op, size_t elem, void* y_host, void* y_stage,
+                     const std::function<void(const OpView&)>& apply_rows,
+                     const std::function<void(int64_t, int64_t, void*)>& gather);
 
 // CUDA events without timing, destroyed with the owner.
 struct Events {

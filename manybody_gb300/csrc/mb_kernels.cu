@@ -941,6 +941,33 @@ void launch_perm(const OpView& v, int32_t* perm, cudaStream_t st) {
   MB_CUDA(cudaGetLastError());
 }
 
+// first[r] = the smallest reference index among the states of tensor row r
+// (min of perm over the row's Dd columns); one block per row.
+__global__ void k_row_first(int64_t Du, int64_t Dd, const int32_t* __restrict__ perm,
+                            int32_t* __restrict__ first) {
+  __shared__ int32_t s_min[kBlasThreads / 32];
+  for (int64_t r = blockIdx.x; r < Du; r += gridDim.x) {
+    int32_t m = INT32_MAX;
+    for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) m = min(m, perm[r * Dd + c]);
+    for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      m = threadIdx.x < blockDim.x / 32 ? s_min[threadIdx.x] : INT32_MAX;
+      for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+      if (threadIdx.x == 0) first[r] = m;
+    }
+    __syncthreads();
+  }
+}
+
+void launch_row_first(int64_t Du, int64_t Dd, const int32_t* perm, int32_t* first,
+                      cudaStream_t st) {
+  const int grid = (int)std::min<int64_t>(std::max<int64_t>(Du, 1), 65535);
+  k_row_first<<<grid, kBlasThreads, 0, st>>>(Du, Dd, perm, first);
+  MB_CUDA(cudaGetLastError());
+}
+
 constexpr int kMaxRowNnz = 256;
 
 __device__ __forceinline__ double diag_value(const OpView& v, int64_t ru, int64_t rd) {

@@ -20,7 +20,8 @@ namespace mb {
 void q_op_prepare(mb_op_s* op, const mb_model_s* m, const HopTable& tu, const HopTable& td);
 void q_op_release(mb_op_s* op);
 void q_apply_host_reference(mb_op_s* op, const void* x_host, const void* x_mapped, void* y_host,
-                            void* y_mapped, void* x_stage, void* y_stage);
+                            void* x_stage, void* y_stage);
+int q_apply_grid(const OpView& v);
 void q_apply_affine(mb_op_s* op, const void* x, void* y, double scale, double shift, double beta,
                     const void* z, int order, cudaStream_t st);
 void q_eigenpair(mb_op_s* op, int64_t k, const void* seed, int order, const mb_lanczos_opts* opts,
@@ -481,41 +482,103 @@ static void from_tensor(mb_op_s* op, const void* src, void* dst, int order, cuda
   launch_gather(op->precision, op->dim, op_iperm(op), src, dst, st);
 }
 
-// The row schedule split for pipelined host-buffer applies: the rows whose up
-// configuration holds orbital 0 (the reference order's first block, indices
-// [0, rows_a * Dd)) in schedule order, then the rest; and two non-blocking
-// streams.  Built on the first host-buffer call.
-void ensure_host_split(mb_op_s* op) {
-  std::lock_guard<std::mutex> lk(op->mu);
-  if (op->split_sched) return;
+// The row groups of the pipelined host-buffer applies.  Rows are ordered by
+// the first reference index among their states and cut into at most
+// kHostGroups groups; once groups 0..g are applied, every reference index
+// below the first one of a later group's rows is final, so that prefix can go
+// back while the later groups run.  Group sizes are whole multiples of the
+// apply's grid (each CTA takes one row per wave), so the groups together run
+// no more waves than one launch over every row.  Within a group the rows keep
+// the row schedule's order (its L2 locality).  Built on the first host-buffer
+// call.
+constexpr int64_t kHostGroups = 8;
+
+void ensure_host_groups(mb_op_s* op) {
+  {
+    std::lock_guard<std::mutex> lk(op->mu);
+    if (op->host_sched) return;
+  }
+  const int32_t* perm = op_perm(op);
   const int64_t Du = op->Du;
-  std::vector<int32_t> sched((size_t)Du);
-  std::vector<uint32_t> um((size_t)Du);
+  std::vector<int32_t> first((size_t)Du), sched((size_t)Du);
+  {
+    DevBuf d_first(sizeof(int32_t) * (size_t)Du);
+    launch_row_first(Du, op->Dd, perm, (int32_t*)d_first.p, 0);
+    MB_CUDA(cudaMemcpy(first.data(), d_first.p, sizeof(int32_t) * (size_t)Du,
+                       cudaMemcpyDeviceToHost));
+  }
   if (op->view.row_sched) {
     MB_CUDA(cudaMemcpy(sched.data(), op->view.row_sched, sizeof(int32_t) * (size_t)Du,
                        cudaMemcpyDeviceToHost));
   } else {
     for (int64_t r = 0; r < Du; ++r) sched[(size_t)r] = (int32_t)r;
   }
-  MB_CUDA(cudaMemcpy(um.data(), op->view.up_mask, sizeof(uint32_t) * (size_t)Du,
-                     cudaMemcpyDeviceToHost));
-  std::vector<int32_t> split;
-  split.reserve((size_t)Du);
-  for (int32_t r : sched)
-    if (um[(size_t)r] & 1u) split.push_back(r);
-  const int64_t rows_a = (int64_t)split.size();
-  for (int32_t r : sched)
-    if (!(um[(size_t)r] & 1u)) split.push_back(r);
+  std::vector<int64_t> pos((size_t)Du);
+  for (int64_t i = 0; i < Du; ++i) pos[(size_t)sched[(size_t)i]] = i;
+  std::vector<int32_t> order((size_t)Du);
+  for (int64_t r = 0; r < Du; ++r) order[(size_t)r] = (int32_t)r;
+  std::sort(order.begin(), order.end(),
+            [&](int32_t a, int32_t b) { return first[(size_t)a] < first[(size_t)b]; });
+  const int64_t wave =
+      op->precision == MB_PREC_Q64 ? q_apply_grid(op->view) : apply_grid(op->view, op->precision);
+  const int64_t waves = (Du + wave - 1) / wave;
+  const int64_t G = std::min<int64_t>(kHostGroups, waves);
+  std::vector<int64_t> row0((size_t)G + 1), ready((size_t)G);
+  for (int64_t g = 0; g <= G; ++g)
+    row0[(size_t)g] = std::min<int64_t>(Du, (g * waves + G / 2) / G * wave);
+  row0[(size_t)G] = Du;
+  for (int64_t g = 0; g < G; ++g)
+    ready[(size_t)g] = g + 1 < G ? (int64_t)first[(size_t)order[(size_t)row0[(size_t)g + 1]]]
+                                 : op->dim;
+  for (int64_t g = 0; g < G; ++g)
+    std::sort(order.begin() + row0[(size_t)g], order.begin() + row0[(size_t)g + 1],
+              [&](int32_t a, int32_t b) { return pos[(size_t)a] < pos[(size_t)b]; });
+  // callers hold host_mu, so no other thread builds the groups meanwhile
+  std::lock_guard<std::mutex> lk(op->mu);
   void* p = nullptr;
   MB_CUDA(cudaMalloc(&p, sizeof(int32_t) * (size_t)std::max<int64_t>(Du, 1)));
   op->allocations.push_back(p);
-  MB_CUDA(cudaMemcpy(p, split.data(), sizeof(int32_t) * (size_t)Du, cudaMemcpyHostToDevice));
+  MB_CUDA(cudaMemcpy(p, order.data(), sizeof(int32_t) * (size_t)Du, cudaMemcpyHostToDevice));
   for (cudaStream_t& h : op->host_streams)
     if (!h) MB_CUDA(cudaStreamCreateWithFlags(&h, cudaStreamNonBlocking));
-  op->split_rows_a = rows_a;
-  op->split_sched = (int32_t*)p;
+  op->host_row0 = std::move(row0);
+  op->host_ready = std::move(ready);
+  op->host_sched = (int32_t*)p;
 }
 
+void host_groups_run(mb_op_s* op, size_t elem, void* y_host, void* y_stage,
+                     const std::function<void(const OpView&)>& apply_rows,
+                     const std::function<void(int64_t, int64_t, void*)>& gather) {
+  cudaStream_t comp = op->host_streams[0], copy = op->host_streams[1];
+  const int64_t G = (int64_t)op->host_ready.size();
+  Events ev((int)G);
+  int64_t done = 0;
+  for (int64_t g = 0; g < G; ++g) {
+    OpView v = op->view;
+    v.row_sched = op->host_sched + op->host_row0[(size_t)g];
+    v.Du = op->host_row0[(size_t)g + 1] - op->host_row0[(size_t)g];
+    apply_rows(v);
+    const int64_t ready = op->host_ready[(size_t)g];
+    if (ready > done) gather(done, ready, (char*)y_stage + elem * (size_t)done);
+    MB_CUDA(cudaEventRecord(ev[(int)g], comp));
+    done = ready;
+  }
+  // every compute launch is queued before the first download: a download to
+  // pageable memory returns only when it has finished
+  done = 0;
+  for (int64_t g = 0; g < G; ++g) {
+    const int64_t ready = op->host_ready[(size_t)g];
+    if (ready > done) {
+      MB_CUDA(cudaStreamWaitEvent(copy, ev[(int)g], 0));
+      MB_CUDA(cudaMemcpyAsync((char*)y_host + elem * (size_t)done,
+                              (const char*)y_stage + elem * (size_t)done,
+                              elem * (size_t)(ready - done), cudaMemcpyDeviceToHost, copy));
+    }
+    done = ready;
+  }
+  MB_CUDA(cudaStreamSynchronize(copy));
+  MB_CUDA(cudaStreamSynchronize(comp));
+}
 
 static void check_order(int order) {
   MB_REQUIRE(order == MB_ORDER_REFERENCE || order == MB_ORDER_TENSOR, MB_ERR_INVALID_ARG,
@@ -1037,26 +1100,25 @@ int mb_op_apply_affine(mb_op_t op, const void* x_dev, void* y_dev, double scale,
 // The host-buffer apply of a complex128 / complex64 lattice operator in
 // reference order, pipelined over the host link as the Q64 one is: x lands
 // scattered to tensor order (a page-locked x read over the link by the
-// scatter kernel, a pageable one in chunks), the rows holding orbital 0 (the
-// reference order's first block) are applied first and their results go
-// back in pieces on the copy engine while the other rows are applied.  Same
-// kernels and arithmetic as mb_op_apply, so the same bits.
+// scatter kernel, a pageable one in chunks, each scattered while the next is
+// in flight), then the rows are applied group by group and each finished
+// prefix of the reference order goes back on the copy engine while the later
+// groups run.  Same kernels and arithmetic as mb_op_apply, so the same bits.
 static void host_apply_pipeline(mb_op_s* op, const void* x_host, const void* x_mapped,
-                                void* y_host, void* y_mapped, mb_op_s::Scratch& s) {
+                                void* y_host, mb_op_s::Scratch& s) {
   cudaStream_t comp = op->host_streams[0], copy = op->host_streams[1];
   int32_t* iperm = op_iperm(op);
   const int prec = op->precision;
   const size_t es = elem_bytes(prec);
-  const int64_t n = op->dim, n_a = op->split_rows_a * op->Dd;
+  const int64_t n = op->dim;
   char* xt = (char*)s.a;  // tensor order
   char* yt = (char*)s.b;
-  char* xs = (char*)s.hx;  // landing / staging, reference order
-  char* ys = (char*)s.hy;
-  constexpr int kChunks = 8, kPieces = 4;
-  Events ev(kChunks + kPieces + 1);
+  char* xs = (char*)s.hx;  // landing, reference order
+  constexpr int kChunks = 8;
   if (x_mapped) {
     launch_scatter(prec, n, iperm, x_mapped, xt, comp);
   } else {
+    Events ev(kChunks);
     const int64_t step = (n + kChunks - 1) / kChunks;
     for (int c = 0; c < kChunks; ++c) {
       const int64_t i0 = std::min<int64_t>(n, c * step), i1 = std::min<int64_t>(n, i0 + step);
@@ -1068,36 +1130,14 @@ static void host_apply_pipeline(mb_op_s* op, const void* x_host, const void* x_m
       if (i1 > i0) launch_scatter(prec, i1 - i0, iperm + i0, xs + es * (size_t)i0, xt, comp);
     }
   }
-  OpView va = op->view, vb = op->view;
-  va.row_sched = op->split_sched;
-  va.Du = op->split_rows_a;
-  vb.row_sched = op->split_sched + op->split_rows_a;
-  vb.Du = op->Du - op->split_rows_a;
-  if (va.Du > 0) launch_apply(va, prec, xt, yt, 1.0, 0.0, 0.0, nullptr, nullptr, 0, comp);
-  const int64_t piece = (n_a + kPieces - 1) / kPieces;
-  for (int k = 0; k < kPieces; ++k) {
-    const int64_t i0 = std::min<int64_t>(n_a, k * piece), i1 = std::min<int64_t>(n_a, i0 + piece);
-    if (i1 > i0) launch_gather(prec, i1 - i0, iperm + i0, yt, ys + es * (size_t)i0, comp);
-    MB_CUDA(cudaEventRecord(ev[kChunks + k], comp));
-  }
-  if (vb.Du > 0) launch_apply(vb, prec, xt, yt, 1.0, 0.0, 0.0, nullptr, nullptr, 0, comp);
-  char* y_b = y_mapped ? (char*)y_mapped + es * (size_t)n_a : ys + es * (size_t)n_a;
-  if (n > n_a) launch_gather(prec, n - n_a, iperm + n_a, yt, y_b, comp);
-  MB_CUDA(cudaEventRecord(ev[kChunks + kPieces], comp));
-  for (int k = 0; k < kPieces; ++k) {
-    const int64_t i0 = std::min<int64_t>(n_a, k * piece), i1 = std::min<int64_t>(n_a, i0 + piece);
-    MB_CUDA(cudaStreamWaitEvent(copy, ev[kChunks + k], 0));
-    if (i1 > i0)
-      MB_CUDA(cudaMemcpyAsync((char*)y_host + es * (size_t)i0, ys + es * (size_t)i0,
-                              es * (size_t)(i1 - i0), cudaMemcpyDeviceToHost, copy));
-  }
-  if (!y_mapped && n > n_a) {
-    MB_CUDA(cudaStreamWaitEvent(copy, ev[kChunks + kPieces], 0));
-    MB_CUDA(cudaMemcpyAsync((char*)y_host + es * (size_t)n_a, ys + es * (size_t)n_a,
-                            es * (size_t)(n - n_a), cudaMemcpyDeviceToHost, copy));
-  }
-  MB_CUDA(cudaStreamSynchronize(copy));
-  MB_CUDA(cudaStreamSynchronize(comp));
+  host_groups_run(
+      op, es, y_host, s.hy,
+      [&](const OpView& v) {
+        launch_apply(v, prec, xt, yt, 1.0, 0.0, 0.0, nullptr, nullptr, 0, comp);
+      },
+      [&](int64_t i0, int64_t i1, void* dst) {
+        launch_gather(prec, i1 - i0, iperm + i0, yt, dst, comp);
+      });
 }
 
 int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
@@ -1121,21 +1161,20 @@ int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
     if (direct) y_dev = at.devicePointer;
     if (order == MB_ORDER_REFERENCE && !op->natural_order && !op->view.n_blocks &&
         !op->view.csr_row) {
-      // x lands scattered to tensor order as it arrives; the result's first
-      // reference block goes back while the rest of the apply runs
+      // x lands scattered to tensor order as it arrives; each finished prefix
+      // of the result (reference order) goes back while later rows run
       cudaPointerAttributes ax{};
       const bool x_locked = cudaPointerGetAttributes(&ax, x_host) == cudaSuccess &&
                             ax.type == cudaMemoryTypeHost && ax.devicePointer != nullptr;
       if (!x_locked) cudaGetLastError();
       const void* x_mapped = x_locked ? ax.devicePointer : nullptr;
-      void* y_mapped = direct ? at.devicePointer : nullptr;
       if (op->precision == MB_PREC_Q64) {
-        q_apply_host_reference(op, x_host, x_mapped, y_host, y_mapped, s.hx, s.hy);
+        q_apply_host_reference(op, x_host, x_mapped, y_host, s.hx, s.hy);
         return;
       }
-      ensure_host_split(op);
+      ensure_host_groups(op);
       try {
-        host_apply_pipeline(op, x_host, x_mapped, y_host, y_mapped, s);
+        host_apply_pipeline(op, x_host, x_mapped, y_host, s);
       } catch (...) {
         // nothing may still read or write the caller's buffers once it sees the error
         cudaStreamSynchronize(op->host_streams[1]);

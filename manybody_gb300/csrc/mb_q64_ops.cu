@@ -131,27 +131,26 @@ void q_apply_affine(mb_op_s* op, const void* x, void* y, double scale, double sh
 // ---------------------------------------------------------------------------
 // The host-buffer apply in reference order, pipelined over the host link.
 //
-// The reference order lists first every state whose up configuration holds
-// orbital 0 (its operator (0, up) sorts before all others): reference indices
-// [0, rows_a * Dd) are exactly the tensor rows r_up with bit 0 set, all
-// columns.  So the apply runs those rows first, and their results go back to
-// the host on the copy engine while the remaining rows are computed.  On the
-// way in, a page-locked x is read over the link by the kernel that scatters it
-// to tensor order (with its largest exponent); a pageable x arrives in chunks,
-// each scattered while the next one is in flight.  The vector is converted to
-// Q64 in place once all of it has landed.  The arithmetic
-// is that of mb_op_apply (same exponent, same kernel per row), so the result
-// is bit-identical to the device-buffer call.
+// On the way in, a page-locked x is read over the link by the kernel that
+// scatters it to tensor order (with its largest exponent); a pageable x
+// arrives in chunks, each scattered while the next one is in flight.  The
+// vector is converted to Q64 in place once all of it has landed.  On the way
+// out, the rows are applied in groups ordered by the first reference index
+// among their states, so each group finishes a prefix of the reference order,
+// which is converted back and downloaded on the copy engine while the later
+// groups run (host_groups_run).  The arithmetic is that of mb_op_apply (same
+// exponent, same kernel per row), so the result is bit-identical to the
+// device-buffer call.
 // ---------------------------------------------------------------------------
 
 static void q_apply_host_pipeline(mb_op_s* op, const void* x_host, const void* x_mapped,
-                                  void* y_host, void* y_mapped, void* x_stage, void* y_stage);
+                                  void* y_host, void* x_stage, void* y_stage);
 
 void q_apply_host_reference(mb_op_s* op, const void* x_host, const void* x_mapped, void* y_host,
-                            void* y_mapped, void* x_stage, void* y_stage) {
-  ensure_host_split(op);
+                            void* x_stage, void* y_stage) {
+  ensure_host_groups(op);
   try {
-    q_apply_host_pipeline(op, x_host, x_mapped, y_host, y_mapped, x_stage, y_stage);
+    q_apply_host_pipeline(op, x_host, x_mapped, y_host, x_stage, y_stage);
   } catch (...) {
     // nothing may still read or write the caller's buffers once it sees the error
     cudaStreamSynchronize(op->host_streams[1]);
@@ -161,21 +160,19 @@ void q_apply_host_reference(mb_op_s* op, const void* x_host, const void* x_mappe
 }
 
 static void q_apply_host_pipeline(mb_op_s* op, const void* x_host, const void* x_mapped,
-                                  void* y_host, void* y_mapped, void* x_stage, void* y_stage) {
+                                  void* y_host, void* x_stage, void* y_stage) {
   cudaStream_t comp = op->host_streams[0], copy = op->host_streams[1];
   auto& q = qscratch_for(op, comp);
   int32_t* iperm = op_iperm(op);
   const int64_t n = op->dim;
-  const int64_t n_a = op->split_rows_a * op->Dd;  // reference indices [0, n_a)
   constexpr size_t es = sizeof(double2);
-  constexpr int kChunks = 8;    // pageable x: upload chunks
-  constexpr int kPieces = 4;    // first block: gather / download pieces
-  Events ev(kChunks + kPieces + 1);
+  constexpr int kChunks = 8;  // pageable x: upload chunks
   MB_CUDA(cudaMemsetAsync(q.ints, 0, sizeof(int), comp));
   if (x_mapped) {
     // page-locked x: the scatter kernel reads it over the link directly
     launch_scatter_maxexp(n, x_mapped, iperm, q.xq, q.ints, comp);
   } else {
+    Events ev(kChunks);
     const int64_t step = (n + kChunks - 1) / kChunks;
     for (int c = 0; c < kChunks; ++c) {
       const int64_t i0 = std::min<int64_t>(n, c * step), i1 = std::min<int64_t>(n, i0 + step);
@@ -192,43 +189,14 @@ static void q_apply_host_pipeline(mb_op_s* op, const void* x_host, const void* x
   launch_f64_to_q_inplace(n, q.xq, op->q_qbits, q.ints, comp);
   launch_q_plan(plan_input(op, 1.0, 0.0, 0.0, 0, 0, false), q.ints + 1, (QParams*)q.prm, comp);
   const int* ey = (const int*)((const char*)q.prm + offsetof(QParams, ey));
-  OpView va = op->view, vb = op->view;
-  va.row_sched = op->split_sched;
-  va.Du = op->split_rows_a;
-  vb.row_sched = op->split_sched + op->split_rows_a;
-  vb.Du = op->Du - op->split_rows_a;
-  if (va.Du > 0)
-    launch_apply_q(va, q.xq, q.yq, nullptr, (const QParams*)q.prm, nullptr, nullptr, 0, comp);
-  // the first block back in pieces: each piece's download starts as soon as
-  // it is gathered, and runs on the copy engine while the rest is computed
-  const int64_t piece = (n_a + kPieces - 1) / kPieces;
-  for (int k = 0; k < kPieces; ++k) {
-    const int64_t i0 = std::min<int64_t>(n_a, k * piece), i1 = std::min<int64_t>(n_a, i0 + piece);
-    if (i1 > i0)
-      launch_q_to_f64(i1 - i0, q.yq, iperm + i0, ey, (char*)y_stage + es * (size_t)i0, comp);
-    MB_CUDA(cudaEventRecord(ev[kChunks + k], comp));
-  }
-  if (vb.Du > 0)
-    launch_apply_q(vb, q.xq, q.yq, nullptr, (const QParams*)q.prm, nullptr, nullptr, 0, comp);
-  // the rest straight into a page-locked y (over the link as it is produced),
-  // or into the staging buffer for a copy
-  void* y_b = y_mapped ? (char*)y_mapped + es * (size_t)n_a : (char*)y_stage + es * (size_t)n_a;
-  if (n > n_a) launch_q_to_f64(n - n_a, q.yq, iperm + n_a, ey, y_b, comp);
-  MB_CUDA(cudaEventRecord(ev[kChunks + kPieces], comp));
-  for (int k = 0; k < kPieces; ++k) {
-    const int64_t i0 = std::min<int64_t>(n_a, k * piece), i1 = std::min<int64_t>(n_a, i0 + piece);
-    MB_CUDA(cudaStreamWaitEvent(copy, ev[kChunks + k], 0));
-    if (i1 > i0)
-      MB_CUDA(cudaMemcpyAsync((char*)y_host + es * (size_t)i0, (char*)y_stage + es * (size_t)i0,
-                              es * (size_t)(i1 - i0), cudaMemcpyDeviceToHost, copy));
-  }
-  if (!y_mapped && n > n_a) {
-    MB_CUDA(cudaStreamWaitEvent(copy, ev[kChunks + kPieces], 0));
-    MB_CUDA(cudaMemcpyAsync((char*)y_host + es * (size_t)n_a, (char*)y_stage + es * (size_t)n_a,
-                            es * (size_t)(n - n_a), cudaMemcpyDeviceToHost, copy));
-  }
-  MB_CUDA(cudaStreamSynchronize(copy));
-  MB_CUDA(cudaStreamSynchronize(comp));
+  host_groups_run(
+      op, es, y_host, y_stage,
+      [&](const OpView& v) {
+        launch_apply_q(v, q.xq, q.yq, nullptr, (const QParams*)q.prm, nullptr, nullptr, 0, comp);
+      },
+      [&](int64_t i0, int64_t i1, void* dst) {
+        launch_q_to_f64(i1 - i0, q.yq, iperm + i0, ey, dst, comp);
+      });
 }
 
 // ---------------------------------------------------------------------------

@@ -298,15 +298,18 @@ def test_concurrent_apply_on_streams(mb, cuda):
 @pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("pinned", [True, False])
 @pytest.mark.parametrize("dims,n_up,n_down", [
-    ((4, 4), 5, 5),  # 19,079,424 states: every landing chunk and download piece in use
-    ((8,), 0, 3),    # no up electron: the first reference block is empty
-    ((6,), 6, 2),    # every up configuration holds orbital 0
+    ((4, 4), 5, 5),  # 19,079,424 states: eight row groups, eight landing chunks
+    ((14,), 4, 3),   # 1,001 rows: seven (FP64) or four (FP32) groups, the last wave partial
+    ((12,), 3, 3),   # 220 rows: two groups (FP64), one (FP32)
+    ((8,), 0, 3),    # one up configuration: a single row group
+    ((6,), 6, 2),    # a full up band: a single row group
     ((3, 2), 2, 3),
 ])
 def test_host_apply_bit_identical(mb, cuda, prec, pinned, dims, n_up, n_down):
     """The pipelined host-buffer apply of a complex128 / complex64 operator in
-    reference order equals the device-buffer apply bit for bit, with page-locked
-    and with pageable host buffers."""
+    reference order (rows applied in groups, each finished reference prefix
+    downloaded while later groups run) equals the device-buffer apply bit for
+    bit, with page-locked and with pageable host buffers."""
     torch = cuda
     _, _, op = make(mb, dims, 1.0, 8.0, n_up, n_down, prec)
     x = op.seed_vector(5)

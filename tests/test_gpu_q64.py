@@ -175,6 +175,32 @@ def test_q64_full_size_4x4_matches_f64(mb, cuda):
     assert rel <= 1e-13
 
 
+@pytest.mark.parametrize("pinned", [True, False])
+@pytest.mark.parametrize("dims,n_up,n_down", [
+    ((4, 4), 5, 5),  # eight row groups
+    ((14,), 4, 3),   # 1,001 rows: seven groups, the last wave partial
+    ((12,), 3, 3),   # 220 rows: two groups
+    ((8,), 0, 3),    # a single row group
+    ((3, 2), 2, 3),
+])
+def test_q64_host_apply_groups_bit_identical(mb, cuda, pinned, dims, n_up, n_down):
+    """The pipelined host-buffer apply of a Q64 operator (rows in groups, each
+    finished reference prefix downloaded while later groups run) equals the
+    device-buffer apply bit for bit, page-locked and pageable."""
+    torch = cuda
+    L = int(np.prod(dims))
+    basis = mb.FermionBasis.with_fixed_particle_number_and_spin(L, n_up + n_down, n_up - n_down)
+    op = mb.GpuHubbardOperator(basis, mb._Hubbard(1.0, 8.0, list(dims)), mb.PREC_Q64)
+    x = op.seed_vector(11)
+    y = op.apply(x).cpu()
+    xh = x.cpu()
+    yh = torch.full_like(xh, float("nan"))
+    if pinned:
+        xh, yh = xh.pin_memory(), yh.pin_memory()
+    op.apply_host(xh, yh)
+    assert torch.equal(yh, y)
+
+
 def test_q64_host_apply_full_size_bit_identical(mb, cuda):
     """4x4, 6+6: the pipelined host-buffer apply (page-locked buffers) equals
     the device-buffer apply in reference order bit for bit."""
