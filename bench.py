@@ -4,12 +4,14 @@ Workload (N=1 line): 2D square-lattice Hubbard 4x4 periodic, t=1, U=8,
 N_up = N_down = 6 -- 64,128,064 states, 16-byte complex elements (1.026 GB
 per vector).  A step is one H|psi> over the whole sector on device-resident
 block-floating-point vectors (int64 mantissas, one exponent per vector: the
-engine's FP64-class format; plain FP64 arithmetic runs at 1/64 rate on this
-GPU and is reported beside it in `extras`).  `value` is the algorithmic
+engine's FP64-class format; plain FP64 arithmetic runs at 1/57 of the FP32
+rate on this GPU and is reported beside it in `extras`).  `value` is the algorithmic
 bandwidth 2 * 16 B * dim / (device time per apply); `e2e` is the same metric
 through the reference-facing C-ABI call with complex128 host buffers in
-reference order (mb_op_apply_host: host->device copy, permutation + FP64->Q64
-conversion, apply, conversion + inverse permutation, device->host copy).
+reference order (mb_op_apply_host: x read over the host link and scattered to
+tensor order, FP64->Q64 conversion, the apply in row groups, each finished
+reference-order prefix converted back and copied to the host while later
+groups run).
 
 Inputs (1 GB each) are larger than the 129 MB L2, so no flush is needed.
 
