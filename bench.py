@@ -433,8 +433,9 @@ def run_cfg2_extra(mb, torch, n_probes=16, n_moments=1024):
 
 
 def run_cfg2_reorth_extra(mb, torch, k=300):
-    """4x4, 6+6, U=8: Lanczos with full re-orthogonalisation (CGS2 against every
-    stored Krylov vector) for all 300 steps, as the 4x4 configuration names it.
+    """4x4, 6+6, U=8: Lanczos with full re-orthogonalisation (classical
+    Gram-Schmidt against every stored Krylov vector, a second pass by the DGKS
+    test) for all 300 steps, as the 4x4 configuration names it.
     300 complex128 or Q64 vectors would be 308 GB, so the FP64 operator keeps
     its Krylov basis in complex64 (154 GB); the recurrence, the projections
     and the tridiagonal eigensolve stay FP64."""
@@ -448,7 +449,7 @@ def run_cfg2_reorth_extra(mb, torch, k=300):
     t = time.perf_counter() - t0
     del seed, op
     return {"workload": "2D 4x4 periodic, t=1, U=8, N_up=N_down=6, FP64 operator",
-            "lanczos_steps": r.steps, "reorth": "CGS2 against every stored vector",
+            "lanczos_steps": r.steps, "reorth": "classical Gram-Schmidt against every stored vector, second pass by the DGKS test",
             "krylov_basis": "complex64, 154 GB", "e0": r.value, "seconds": round(t, 3)}
 
 

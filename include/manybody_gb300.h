@@ -226,7 +226,9 @@ int mb_fill_phase(mb_op_t op, uint64_t seed, uint32_t stream_id, void* v_dev, in
 /* ---- Lanczos (src/numerics/lanczos.h) ------------------------------------ */
 typedef struct {
   int reorth;           /* 0: plain three-term recurrence (the reference's); 1: full
-                           re-orthogonalisation (classical Gram-Schmidt, twice) */
+                           re-orthogonalisation (classical Gram-Schmidt against every
+                           stored vector; a second pass when the first one takes ||w||
+                           below 1/sqrt(2) of its norm, the DGKS test) */
   int basis_precision;  /* storage of the Krylov basis for reorth: MB_PREC_F64 or MB_PREC_F32;
                            -1 = F64 when it fits in free device memory, else F32 */
   double conv_tol;      /* > 0: stop early once the extremal Ritz value changes by

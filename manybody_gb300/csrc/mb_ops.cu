@@ -661,15 +661,22 @@ struct Krylov {
     return (char*)basis.p + elem_bytes(basis_prec) * (size_t)n * (size_t)j;
   }
 
-  // CGS2: two passes of w -= V (V^H w); returns ||w||^2 after the last pass.
-  double reorth(int m) {
-    double nrm2 = 0.0;
+  // Full re-orthogonalisation of w (squared norm nrm2) against the m stored
+  // vectors: classical Gram-Schmidt, w -= V (V^H w), with the DGKS test
+  // (Daniel, Gragg, Kaufman and Stewart, Math. Comp. 30 (1976); Parlett's
+  // "twice is enough"): a second pass runs only when the first one took w
+  // below 1/sqrt(2) of its norm, where cancellation can leave components
+  // along V.  A Lanczos vector is already nearly orthogonal to V, so one pass
+  // is the rule.  Returns ||w||^2 after the last pass.
+  double reorth(int m, double nrm2) {
     for (int pass = 0; pass < 2; ++pass) {
+      const double before = nrm2;
       launch_multi_dot(basis_prec, prec, n, basis.p, n, m, w.p, red.p(), st);
       launch_reduce(red.p(), multi_dot_grid(n), 2 * m, (double*)coef.p, st);
       launch_multi_axpy(basis_prec, prec, n, basis.p, n, m, (const double*)coef.p, w.p, red.p(),
                         st);
       nrm2 = red.fetch(grid_blas, 3, st)[1];
+      if (nrm2 >= 0.5 * before) break;
     }
     return nrm2;
   }
@@ -699,7 +706,7 @@ struct Krylov {
       // w -= alpha v ; beta = ||w||                             (lanczos.h:34-36)
       launch_axpby(prec, n, -alpha, 0.0, v_curr.p, 1.0, 0.0, w.p, red.p(), 1, st);
       double nrm2 = red.fetch(grid_blas, 3, st)[1];
-      if (reorth) nrm2 = this->reorth((int)(it + 1));
+      if (reorth) nrm2 = this->reorth((int)(it + 1), nrm2);
       const double beta = std::sqrt(nrm2);
       alphas.push_back(alpha);
       steps += 1;

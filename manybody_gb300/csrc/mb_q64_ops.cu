@@ -351,11 +351,13 @@ struct QKrylov {
     basis_max.push_back(v.maxq);
   }
 
-  // Classical Gram-Schmidt, twice: w -= V (V^H w).  Returns ||w||^2.
-  double reorth(QRef& w) {
+  // Classical Gram-Schmidt, w -= V (V^H w), with the DGKS test (a second
+  // pass only when the first took w below 1/sqrt(2) of its norm, nrm2 on
+  // entry).  Returns ||w||^2.
+  double reorth(QRef& w, double nrm2) {
     const int m = (int)basis_E.size();
-    double nrm2 = 0.0;
     for (int pass = 0; pass < 2; ++pass) {
+      const double before = nrm2;
       launch_q_multi_dot(n, basis.p, n, m, w.p, part(), st);
       const double* h = fetch(grid_md, 2 * m, nullptr);
       std::vector<std::complex<double>> c((size_t)m);
@@ -380,6 +382,7 @@ struct QKrylov {
       w.E += shw;
       w.maxq = std::max(mq, 1.0);
       nrm2 = h2[0] * std::ldexp(1.0, 2 * w.E + 32);
+      if (nrm2 >= 0.5 * before) break;
     }
     return nrm2;
   }
@@ -401,7 +404,7 @@ struct QKrylov {
       const double alpha = apply(*ww, *vc, scale, beta_prev, beta_prev != 0.0 ? vp : nullptr).first;
       QRef wv = *ww;
       double nrm2 = lincomb(*ww, vc, -alpha, &wv, 1.0);  // w -= alpha v
-      if (reorth_on) nrm2 = reorth(*ww);
+      if (reorth_on) nrm2 = reorth(*ww, nrm2);
       const double beta = std::sqrt(nrm2);
       alphas.push_back(alpha);
       steps += 1;
