@@ -626,6 +626,7 @@ void launch_dot(int precision, int64_t n, const void* x, const void* y, double* 
 // ---------------------------------------------------------------------------
 constexpr int kMdChunk = 1024;
 constexpr int kMdThreads = 256;
+constexpr int kMdBatch = 8;  // loads in flight per lane in the multi-vector kernels
 constexpr int kMaxBasis = 1024;
 
 template <typename TV, typename TW>
@@ -660,30 +661,46 @@ k_multi_dot(int64_t n, const typename C2<TV>::type* __restrict__ V, int64_t ld, 
     for (int j = warp; j < m; j += nwarps) {
       const VV* vj = V + (int64_t)j * ld + base;
       double cr = 0.0, ci = 0.0;
+      // the basis elements of kMdBatch iterations are loaded before any is
+      // used, so a warp has that many HBM loads in flight instead of one
       if constexpr (kSplit) {
         DotAcc<float> pr, pi;
         float lr = 0.f, li = 0.f;
-        for (int i = lane; i < len; i += 32) {
-          const VV a = vj[i];
-          const float4 b = swf[i];
-          pr.add_prod(a.x, b.x);
-          pr.add_prod(a.y, b.y);
-          pi.add_prod(a.x, b.y);
-          pi.add_prod(-a.y, b.x);
-          lr = fmaf(a.x, b.z, fmaf(a.y, b.w, lr));
-          li = fmaf(a.x, b.w, fmaf(-a.y, b.z, li));
+        for (int i0 = lane; i0 < len; i0 += 32 * kMdBatch) {
+          VV a[kMdBatch];
+#pragma unroll
+          for (int u = 0; u < kMdBatch; ++u)
+            if (i0 + 32 * u < len) a[u] = vj[i0 + 32 * u];
+#pragma unroll
+          for (int u = 0; u < kMdBatch; ++u) {
+            if (i0 + 32 * u >= len) break;
+            const float4 b = swf[i0 + 32 * u];
+            pr.add_prod(a[u].x, b.x);
+            pr.add_prod(a[u].y, b.y);
+            pi.add_prod(a[u].x, b.y);
+            pi.add_prod(-a[u].y, b.x);
+            lr = fmaf(a[u].x, b.z, fmaf(a[u].y, b.w, lr));
+            li = fmaf(a[u].x, b.w, fmaf(-a[u].y, b.z, li));
+          }
         }
         cr = pr.value() + (double)lr;
         ci = pi.value() + (double)li;
       } else {
-        for (int i = lane; i < len; i += 32) {
-          const VV a = vj[i];
-          const double ar = (double)a.x, ai = (double)a.y;
-          const double2 b = sw[i];
-          cr = fma(ar, b.x, cr);
-          cr = fma(ai, b.y, cr);
-          ci = fma(ar, b.y, ci);
-          ci = fma(-ai, b.x, ci);
+        for (int i0 = lane; i0 < len; i0 += 32 * kMdBatch) {
+          VV a[kMdBatch];
+#pragma unroll
+          for (int u = 0; u < kMdBatch; ++u)
+            if (i0 + 32 * u < len) a[u] = vj[i0 + 32 * u];
+#pragma unroll
+          for (int u = 0; u < kMdBatch; ++u) {
+            if (i0 + 32 * u >= len) break;
+            const double ar = (double)a[u].x, ai = (double)a[u].y;
+            const double2 b = sw[i0 + 32 * u];
+            cr = fma(ar, b.x, cr);
+            cr = fma(ai, b.y, cr);
+            ci = fma(ar, b.y, ci);
+            ci = fma(-ai, b.x, ci);
+          }
         }
       }
 #pragma unroll
@@ -701,7 +718,9 @@ k_multi_dot(int64_t n, const typename C2<TV>::type* __restrict__ V, int64_t ld, 
 
 static int md_grid(int64_t n) {
   int64_t g = (n + kMdChunk - 1) / kMdChunk;
-  const int64_t cap = (int64_t)num_sms() * 2;
+  // four CTAs per SM fit (64 registers x 256 threads, 32 KB of shared memory
+  // each): twice the loads in flight of two
+  const int64_t cap = (int64_t)num_sms() * 4;
   if (g > cap) g = cap;
   return (int)(g > 0 ? g : 1);
 }
@@ -747,22 +766,38 @@ k_multi_axpy(int64_t n, const typename C2<TV>::type* __restrict__ V, int64_t ld,
        i += (int64_t)gridDim.x * blockDim.x) {
     const VW wv = w[i];
     double sr = (double)wv.x, si = (double)wv.y;
+    // kMdBatch basis vectors' elements are loaded before any is used (HBM
+    // loads in flight); the sums run in the same order as one at a time
     if constexpr (kSplit) {
       float fr = 0.f, fi = 0.f;
-      for (int j = 0; j < m; ++j) {
-        const VV a = V[(int64_t)j * ld + i];
-        const float cr = scf[2 * j], ci = scf[2 * j + 1];
-        fr = fmaf(cr, a.x, fmaf(-ci, a.y, fr));
-        fi = fmaf(cr, a.y, fmaf(ci, a.x, fi));
+      for (int j0 = 0; j0 < m; j0 += kMdBatch) {
+        VV a[kMdBatch];
+#pragma unroll
+        for (int u = 0; u < kMdBatch; ++u)
+          if (j0 + u < m) a[u] = V[(int64_t)(j0 + u) * ld + i];
+#pragma unroll
+        for (int u = 0; u < kMdBatch; ++u) {
+          if (j0 + u >= m) break;
+          const float cr = scf[2 * (j0 + u)], ci = scf[2 * (j0 + u) + 1];
+          fr = fmaf(cr, a[u].x, fmaf(-ci, a[u].y, fr));
+          fi = fmaf(cr, a[u].y, fmaf(ci, a[u].x, fi));
+        }
       }
       sr -= (double)fr;
       si -= (double)fi;
     } else {
-      for (int j = 0; j < m; ++j) {
-        const VV a = V[(int64_t)j * ld + i];
-        const double cr = sc[2 * j], ci = sc[2 * j + 1];
-        sr -= cr * (double)a.x - ci * (double)a.y;
-        si -= cr * (double)a.y + ci * (double)a.x;
+      for (int j0 = 0; j0 < m; j0 += kMdBatch) {
+        VV a[kMdBatch];
+#pragma unroll
+        for (int u = 0; u < kMdBatch; ++u)
+          if (j0 + u < m) a[u] = V[(int64_t)(j0 + u) * ld + i];
+#pragma unroll
+        for (int u = 0; u < kMdBatch; ++u) {
+          if (j0 + u >= m) break;
+          const double cr = sc[2 * (j0 + u)], ci = sc[2 * (j0 + u) + 1];
+          sr -= cr * (double)a[u].x - ci * (double)a[u].y;
+          si -= cr * (double)a[u].y + ci * (double)a[u].x;
+        }
       }
     }
     VW o;

@@ -572,6 +572,7 @@ void launch_q_dot(int64_t n, const void* a, const void* b, double* partials, cud
 // per column).  c_j = <V_j, w> per block partials [blocks][2m].
 constexpr int kQmdChunk = 512;
 constexpr int kQmdThreads = 256;
+constexpr int kQmdBatch = 8;  // loads in flight per lane in the multi-vector kernels
 
 __global__ void __launch_bounds__(kQmdThreads)
 k_q_multi_dot(int64_t n, const longlong2* __restrict__ V, int64_t ld, int m,
@@ -589,10 +590,19 @@ k_q_multi_dot(int64_t n, const longlong2* __restrict__ V, int64_t ld, int m,
     for (int j = warp; j < m; j += nwarps) {
       const longlong2* vj = V + (int64_t)j * ld + base;
       __int128 cr = 0, ci = 0;
-      for (int i = lane; i < len; i += 32) {
-        const longlong2 a = vj[i], b = sw[i];
-        cr += prod_hi(a.x, b.x) + prod_hi(a.y, b.y);
-        ci += prod_hi(a.x, b.y) - prod_hi(a.y, b.x);
+      // kQmdBatch basis elements loaded before any is used: HBM loads in flight
+      for (int i0 = lane; i0 < len; i0 += 32 * kQmdBatch) {
+        longlong2 a[kQmdBatch];
+#pragma unroll
+        for (int u = 0; u < kQmdBatch; ++u)
+          if (i0 + 32 * u < len) a[u] = vj[i0 + 32 * u];
+#pragma unroll
+        for (int u = 0; u < kQmdBatch; ++u) {
+          if (i0 + 32 * u >= len) break;
+          const longlong2 b = sw[i0 + 32 * u];
+          cr += prod_hi(a[u].x, b.x) + prod_hi(a[u].y, b.y);
+          ci += prod_hi(a[u].x, b.y) - prod_hi(a[u].y, b.x);
+        }
       }
       double dr = i128_to_f64(cr), di = i128_to_f64(ci);
 #pragma unroll
@@ -613,7 +623,7 @@ k_q_multi_dot(int64_t n, const longlong2* __restrict__ V, int64_t ld, int m,
 
 int q_multi_dot_grid(int64_t n) {
   int64_t g = (n + kQmdChunk - 1) / kQmdChunk;
-  const int64_t cap = (int64_t)sm_count() * 2;
+  const int64_t cap = (int64_t)sm_count() * 3;  // three CTAs per SM fit (80 registers)
   if (g > cap) g = cap;
   return (int)std::max<int64_t>(g, 1);
 }
@@ -641,11 +651,18 @@ k_q_multi_axpy(int64_t n, const longlong2* __restrict__ V, int64_t ld, int m,
        i += (int64_t)gridDim.x * blockDim.x) {
     const longlong2 wv = w[i];
     __int128 sr = (__int128)wv.x << G, si = (__int128)wv.y << G;
-    for (int j = 0; j < m; ++j) {
-      const longlong2 a = V[(int64_t)j * ld + i];
-      const long long cr = sc[2 * j], ci = sc[2 * j + 1];
-      sr -= (__int128)cr * a.x - (__int128)ci * a.y;
-      si -= (__int128)cr * a.y + (__int128)ci * a.x;
+    for (int j0 = 0; j0 < m; j0 += kQmdBatch) {
+      longlong2 a[kQmdBatch];
+#pragma unroll
+      for (int u = 0; u < kQmdBatch; ++u)
+        if (j0 + u < m) a[u] = V[(int64_t)(j0 + u) * ld + i];
+#pragma unroll
+      for (int u = 0; u < kQmdBatch; ++u) {
+        if (j0 + u >= m) break;
+        const long long cr = sc[2 * (j0 + u)], ci = sc[2 * (j0 + u) + 1];
+        sr -= (__int128)cr * a[u].x - (__int128)ci * a[u].y;
+        si -= (__int128)cr * a[u].y + (__int128)ci * a[u].x;
+      }
     }
     longlong2 o;
     o.x = round_shift(sr, G + shw);
