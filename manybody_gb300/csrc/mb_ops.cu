@@ -413,7 +413,9 @@ static void build_momentum_all(mb_op_s* op, const mb_basis_s* b, const mb_model_
   op->perm = upload(op, perm.empty() ? std::vector<int32_t>{0} : perm);
 }
 
-static mb_op_s::Scratch& scratch_for(mb_op_s* op, cudaStream_t st, int nvec) {
+// Per-stream scratch vectors: nvec = 1 gives a, 2 gives a and b; staging
+// adds the host-buffer staging pair hx, hy.  Each is allocated on first use.
+static mb_op_s::Scratch& scratch_for(mb_op_s* op, cudaStream_t st, int nvec, bool staging = false) {
   std::lock_guard<std::mutex> lk(op->mu);
   auto& s = op->scratch[st];
   const size_t vb = elem_bytes(op->precision) * (size_t)op->dim;
@@ -423,7 +425,7 @@ static mb_op_s::Scratch& scratch_for(mb_op_s* op, cudaStream_t st, int nvec) {
   if (nvec >= 2 && !s.b) {
     MB_CUDA(cudaMalloc(&s.b, vb));
   }
-  if (nvec >= 4 && !s.hx) {
+  if (staging && !s.hx) {
     MB_CUDA(cudaMalloc(&s.hx, vb));
     MB_CUDA(cudaMalloc(&s.hy, vb));
   }
@@ -1156,7 +1158,7 @@ int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
     // host threads share the staging buffers and the stream: serialise whole
     // calls, or one thread's upload could land between another's copy and apply
     std::lock_guard<std::mutex> lk(op->host_mu);
-    auto& s = scratch_for(op, st, 4);
+    auto& s = scratch_for(op, st, 0, true);  // the staging pair; a, b where a path needs them
     // A page-locked y (cudaHostAlloc / cudaHostRegister) is written in place by
     // the last kernel (the order / format change), so the result crosses the
     // host link once, while it is produced, instead of after a device copy.
@@ -1180,6 +1182,7 @@ int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
         return;
       }
       ensure_host_groups(op);
+      scratch_for(op, st, 2);  // a, b: x and y in tensor order
       try {
         host_apply_pipeline(op, x_host, x_mapped, y_host, s);
       } catch (...) {
