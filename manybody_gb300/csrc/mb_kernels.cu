@@ -311,7 +311,7 @@ static bool apply_staged(const OpView& v, int precision) {
   return apply_smem(v, precision, true) + 1024 <= (size_t)max_smem_optin();
 }
 
-static int csr_grid(int64_t n);
+static int csr_grid(int64_t n, int precision);
 
 int apply_grid(const OpView& v, int precision) {
   if (v.n_blocks) {
@@ -319,7 +319,7 @@ int apply_grid(const OpView& v, int precision) {
     for (int b = 0; b < v.n_blocks; ++b) g += apply_grid(v.sub[b], precision);
     return g;
   }
-  if (v.csr_row) return csr_grid(v.dim);
+  if (v.csr_row) return csr_grid(v.dim, precision);
   int64_t g = (int64_t)num_sms() * (precision == MB_PREC_F32 ? kApplyCtasPerSm<float> : 1);
   if (g > v.Du) g = v.Du;
   return (int)(g > 0 ? g : 1);
@@ -363,6 +363,12 @@ static void apply_dots(const OpView& v, const void* x, void* y, double scale, do
 // column form (no values) every entry is +-off and the diagonal comes apart.
 // ---------------------------------------------------------------------------
 constexpr int kCsrThreads = 256;
+// Lanes per CSR row: a row's partial sums meet in a log2(lanes)-step shuffle
+// reduction, which on this GPU's slow FP64 pipe cost as much as the row's own
+// adds at 32 lanes.  Measured at 4x4 6+6, K = (0,0) (~210 entries a row):
+// complex128 10.85 / 6.72 / 5.11 / 4.47 ms at 32 / 16 / 8 / 4 lanes,
+// complex64 2.95 / 2.32 / 2.02 / 2.07 ms.
+template <typename T> constexpr int csr_lanes() { return sizeof(T) == 8 ? 4 : 8; }
 
 // v with its sign flipped when bit 31 of e is set
 __device__ __forceinline__ double flip_sign(double v, uint32_t e) {
@@ -372,21 +378,28 @@ __device__ __forceinline__ float flip_sign(float v, uint32_t e) {
   return __int_as_float(__float_as_int(v) ^ (int)(e & 0x80000000u));
 }
 
-template <typename T, int DOTS>
+template <typename T, int DOTS, int LPR>
 __global__ void __launch_bounds__(kCsrThreads)
 k_csr_apply(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
             const typename C2<T>::type* __restrict__ val, const double* __restrict__ diag, T off,
             const typename C2<T>::type* __restrict__ x, typename C2<T>::type* y, T scale, T shift,
             T beta, const typename C2<T>::type* z, double* __restrict__ partials) {
   using V2 = typename C2<T>::type;
-  const int lane = threadIdx.x & 31;
+  // LPR lanes per row, 32 / LPR rows per warp; the warp steps through its rows
+  // together (the shuffles need every lane), groups past the last row idle
+  constexpr int RPW = 32 / LPR;
+  const int lane = threadIdx.x & (LPR - 1);
+  const int sub = (threadIdx.x & 31) / LPR;
   const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   DotAcc<T> a_xy, a_yy, a_xx;
-  for (int64_t row = w0; row < n; row += nw) {
+  for (int64_t rb = w0 * RPW; rb < n; rb += nw * RPW) {
+    const int64_t row = rb + sub;
+    const bool live = row < n;
     T ar = T(0), ai = T(0);
-    if (val) {
-      for (int64_t k = rp[row] + lane; k < rp[row + 1]; k += 32) {
+    if (!live) {
+    } else if (val) {
+      for (int64_t k = rp[row] + lane; k < rp[row + 1]; k += LPR) {
         const V2 a = val[k], b = x[ci[k]];
         ar = fma(a.x, b.x, fma(-a.y, b.y, ar));
         ai = fma(a.x, b.y, fma(a.y, b.x, ai));
@@ -394,14 +407,14 @@ k_csr_apply(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict
     } else {  // signed columns: entries +-1 (times off below), diagonal apart
       // the sign goes onto the sign bit, so no lane branches per entry; for
       // complex64 two independent sums (even / odd strides) halve the add
-      // chains (measured at 4x4 6+6, K=0: 3.19 -> 2.81 ms), for complex128
-      // one (9.1 ms, against 12.9 ms with two)
+      // chains (measured at 4x4 6+6, K=0, 32 lanes a row: 3.19 -> 2.81 ms),
+      // for complex128 one (9.1 ms, against 12.9 ms with two)
       T br = T(0), bi = T(0);
       const int64_t k1 = rp[row + 1];
       int64_t k = rp[row] + lane;
 #pragma unroll 4
-      for (; sizeof(T) == 4 && k + 32 < k1; k += 64) {
-        const uint32_t e0 = (uint32_t)__ldg(&ci[k]), e1 = (uint32_t)__ldg(&ci[k + 32]);
+      for (; sizeof(T) == 4 && k + LPR < k1; k += 2 * LPR) {
+        const uint32_t e0 = (uint32_t)__ldg(&ci[k]), e1 = (uint32_t)__ldg(&ci[k + LPR]);
         const V2 b0 = __ldg(&x[e0 & 0x7FFFFFFFu]), b1 = __ldg(&x[e1 & 0x7FFFFFFFu]);
         ar += flip_sign(b0.x, e0);
         ai += flip_sign(b0.y, e0);
@@ -409,7 +422,7 @@ k_csr_apply(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict
         bi += flip_sign(b1.y, e1);
       }
 #pragma unroll 4
-      for (; k < k1; k += 32) {
+      for (; k < k1; k += LPR) {
         const uint32_t e0 = (uint32_t)__ldg(&ci[k]);
         const V2 b0 = __ldg(&x[e0 & 0x7FFFFFFFu]);
         ar += flip_sign(b0.x, e0);
@@ -419,11 +432,11 @@ k_csr_apply(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict
       ai += bi;
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = LPR / 2; o > 0; o >>= 1) {
       ar += __shfl_xor_sync(0xffffffffu, ar, o);
       ai += __shfl_xor_sync(0xffffffffu, ai, o);
     }
-    if (lane == 0) {
+    if (live && lane == 0) {
       const V2 xv = x[row];
       if (!val) {
         const T d = (T)diag[row];
@@ -450,8 +463,9 @@ k_csr_apply(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict
   }
 }
 
-static int csr_grid(int64_t n) {
-  const int64_t rows_per_block = kCsrThreads / 32;
+static int csr_grid(int64_t n, int precision) {
+  const int64_t rows_per_block =
+      kCsrThreads / (precision == MB_PREC_F32 ? csr_lanes<float>() : csr_lanes<double>());
   int64_t g = (n + rows_per_block - 1) / rows_per_block;
   const int64_t cap = (int64_t)num_sms() * 16;
   if (g > cap) g = cap;
@@ -463,7 +477,8 @@ static void csr_apply_t(const OpView& v, const void* x, void* y, double scale, d
                         double beta, const void* z, double* partials, cudaStream_t st) {
   using V2 = typename C2<T>::type;
   const V2* val = sizeof(T) == 8 ? (const V2*)v.csr_val : (const V2*)v.csr_val_f;
-  k_csr_apply<T, DOTS><<<csr_grid(v.dim), kCsrThreads, 0, st>>>(
+  k_csr_apply<T, DOTS, csr_lanes<T>()><<<csr_grid(v.dim, sizeof(T) == 4 ? MB_PREC_F32 : MB_PREC_F64),
+                                         kCsrThreads, 0, st>>>(
       v.dim, v.csr_row, v.csr_col, val, v.csr_diag, (T)v.csr_off, (const V2*)x, (V2*)y,
       (T)scale, (T)shift, (T)beta, (const V2*)z, partials);
   MB_CUDA(cudaGetLastError());
