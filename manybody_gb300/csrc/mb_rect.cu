@@ -173,27 +173,38 @@ int64_t build_rows(mb_rect_op_s* op, int which, const MoveTables& m) {
   return nnz;
 }
 
-// y[row] = sum val * x[col] (real values, complex vectors); warp per row.
+// y[row] = sum val * x[col] (real values, complex vectors).  A row of the
+// current operator has about one entry per electron, so kRowLanes lanes take
+// a row (32 / kRowLanes rows a warp): the partial sums meet in a two-step
+// shuffle instead of five FP64 steps at a warp per row.  The warp steps
+// through its rows together (the shuffles need every lane).
+constexpr int kRowLanes = 4;
+
 template <typename V2>
 __global__ void k_real_csr_apply(int64_t n, const int64_t* __restrict__ rp,
                                  const int32_t* __restrict__ ci, const double* __restrict__ val,
                                  const V2* __restrict__ x, V2* __restrict__ y) {
-  const int lane = threadIdx.x & 31;
+  constexpr int RPW = 32 / kRowLanes;
+  const int lane = threadIdx.x & (kRowLanes - 1);
+  const int sub = (threadIdx.x & 31) / kRowLanes;
   const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t row = w0; row < n; row += nw) {
+  for (int64_t rb = w0 * RPW; rb < n; rb += nw * RPW) {
+    const int64_t row = rb + sub;
+    const bool live = row < n;
     double ar = 0.0, ai = 0.0;
-    for (int64_t k = rp[row] + lane; k < rp[row + 1]; k += 32) {
-      const V2 b = x[ci[k]];
-      ar = fma(val[k], (double)b.x, ar);
-      ai = fma(val[k], (double)b.y, ai);
-    }
+    if (live)
+      for (int64_t k = rp[row] + lane; k < rp[row + 1]; k += kRowLanes) {
+        const V2 b = x[ci[k]];
+        ar = fma(val[k], (double)b.x, ar);
+        ai = fma(val[k], (double)b.y, ai);
+      }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = kRowLanes / 2; o > 0; o >>= 1) {
       ar += __shfl_xor_sync(0xffffffffu, ar, o);
       ai += __shfl_xor_sync(0xffffffffu, ai, o);
     }
-    if (lane == 0) {
+    if (live && lane == 0) {
       V2 out;
       out.x = (decltype(out.x))ar;
       out.y = (decltype(out.y))ai;
@@ -233,7 +244,9 @@ __global__ void k_cdot(int64_t n, const V2* __restrict__ a, const V2* __restrict
 void rect_apply(const mb_rect_op_s* op, const void* x, void* y, int adjoint, cudaStream_t st) {
   const int w = adjoint ? 1 : 0;
   const int64_t n = adjoint ? op->n_cols : op->n_rows;
-  const int g = (int)std::min<int64_t>(std::max<int64_t>((n + 7) / 8, 1), 152 * 16);
+  const int64_t rows_per_block = kThreads / kRowLanes;
+  const int g = (int)std::min<int64_t>(
+      std::max<int64_t>((n + rows_per_block - 1) / rows_per_block, 1), 152 * 16);
   if (op->precision == MB_PREC_F32)
     k_real_csr_apply<float2><<<g, kThreads, 0, st>>>(n, op->rp[w], op->col[w], op->val[w],
                                                      (const float2*)x, (float2*)y);
