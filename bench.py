@@ -655,8 +655,8 @@ def run_serve_extra(mb, torch, n_requests=400, rate=200.0):
 # ---------------------------------------------------------------------------
 def cpu_sample_matrix():
     """The sample's H by the restated compute_matrix_elements (normal ordering
-    of H|key_j>, OpenMP over columns), with that build's wall time: the
-    reference's CPU path is this build once, then serial applies."""
+    of H|key_j>, OpenMP over columns), with the wall time of building it: the
+    reference's CPU path builds H once, then applies it serially."""
     import oracle
     # same lattice and interaction, a sector small enough to build in seconds
     t0 = time.perf_counter()

@@ -1,8 +1,8 @@
 """ctypes front end of the CPU oracle (oracle/oracle.c).
 
 Test infrastructure only: tests/, __graft_entry__.smoke() and the CPU legs of
-bench.py use it as the checker or as the timed CPU baseline.  The GPU product
-(manybody_gb300) never imports it.
+bench.py use it to verify results or as the timed CPU baseline.  The GPU
+product (manybody_gb300) never imports it.
 """
 from __future__ import annotations
 

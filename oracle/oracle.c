@@ -2,8 +2,8 @@
  * oracle.c -- CPU restatement of the reference library's Hubbard hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
- * cpu_baseline / reference arm of bench.py load this library, and only as
- * the checker or as the timed CPU baseline.  The GPU product never calls it.
+ * cpu_baseline / reference arm of bench.py load this library, and only to
+ * verify results or as the timed CPU baseline.  The GPU product never calls it.
  *
  * Parity pins: the basis order and the sparse Hamiltonian produced here are
  * compared bit-for-bit against outputs of the reference's own code

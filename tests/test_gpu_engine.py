@@ -2,7 +2,7 @@
 advanced together, complex64 vectors with FP64 alpha/beta, replay + FP64
 Rayleigh-quotient refinement.
 
-Tolerances: refined energies |dE0| <= 1e-8 |E0| (the north-star bar);
+Tolerances: refined energies |dE0| <= 1e-8 |E0| (the batch and serving accuracy bar);
 unrefined Ritz values <= 1e-5 |E0|; a request gives bit-identical results
 alone and in any mix (per-request fixed-order reductions).
 """
