@@ -451,3 +451,21 @@ def test_solve_linear_system(mb, cuda):
     with pytest.raises(mb.MbError) as e:
         mb.solve(op, torch.zeros(n, dtype=torch.complex128, device="cuda"), n, tridiag_solve)
     assert e.value.status == mb.MB_ERR_ZERO_NORM
+
+
+@pytest.mark.parametrize("prec", [0, 2])
+def test_reorth_lanczos_through_breakdown(mb, cuda, prec):
+    """More Lanczos steps than the sector has states, with full
+    re-orthogonalisation: the Krylov space fills the sector, w becomes
+    (numerically) dependent on the stored vectors, so the Gram-Schmidt pass
+    cancels most of it and the second pass runs (the DGKS test).  The
+    recurrence must stop at the breakdown (beta <= 1000 eps, lanczos.h:106-110)
+    within dim steps, with E0 exact to 1e-12."""
+    _, _, op = make(mb, [4], 1.0, 4.0, 2, 1, prec)
+    n = op.dimension()
+    assert n == 24
+    H = oracle.hubbard_csc([4], 1.0, 4.0, 2, 1)
+    E = np.linalg.eigvalsh(H.to_dense())
+    res = mb.find_min_eigenpair(op, 3 * n, reorth=True)
+    assert res.steps <= n
+    assert abs(res.value - E[0]) <= 1e-12 * abs(E[0])
