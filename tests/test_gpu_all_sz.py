@@ -67,3 +67,26 @@ def test_all_sz_ground_state(mb, cuda):
     hv = op.apply(res.vector)
     lam = op.dot_re(res.vector, hv) / op.dot_re(res.vector, res.vector)
     assert abs(lam - res.value) <= 1e-9 * abs(res.value)
+
+
+@pytest.mark.parametrize("kind", ["all_sz", "momentum_factorized"])
+@pytest.mark.parametrize("pinned", [True, False])
+def test_block_diagonal_host_apply_bit_identical(mb, cuda, kind, pinned):
+    """Block-diagonal operators (one block per (N_up, N_down), or per total
+    momentum) through the host-buffer call equal the device-buffer call bit for
+    bit, with page-locked and pageable buffers."""
+    torch = cuda
+    if kind == "all_sz":
+        op = mb.GpuHubbardOperator(mb.FermionBasis.with_fixed_particle_number(8, 8),
+                                   mb.HubbardModel(1.0, 4.0, 8))
+    else:
+        op = mb.HubbardMomentumFactorized(mb.FermionBasis.with_fixed_particle_number_and_spin(8, 8, 0),
+                                          [8], 1.0, 4.0)
+    x = op.seed_vector(3)
+    y = op.apply(x).cpu()
+    xh = x.cpu()
+    yh = torch.full_like(xh, float("nan"))
+    if pinned:
+        xh, yh = xh.pin_memory(), yh.pin_memory()
+    op.apply_host(xh, yh)
+    assert torch.equal(yh, y)
