@@ -198,7 +198,11 @@ def run_gpu(args):
     model = mb._Hubbard(w["t"], w["U"], w["lattice"])
     opq = mb.GpuHubbardOperator(basis, model, mb.PREC_Q64)
     dim = opq.dimension()
+    # the apply's kernel shape from the project's autotuner (every candidate
+    # timed on this GPU; all give the same bits)
+    apply_shape, _ = opq.autotune()
     w.update(dim=dim, lattice="x".join(str(d) for d in w["lattice"]), order="tensor",
+             apply_shape=apply_shape,
              vector="16-byte complex elements (int64 mantissa pairs)",
              l2=f"inputs ({16 * dim / 1e9:.2f} GB) larger than L2 (129 MB); no flush")
     stream = torch.cuda.current_stream()
@@ -256,6 +260,7 @@ def run_gpu(args):
     extras = {}
     for name, prec, nbytes in (("f64_fp64_pipe", mb.PREC_F64, 16), ("c64_fp32", mb.PREC_F32, 8)):
         op = mb.GpuHubbardOperator(basis, model, prec)
+        shape, _ = op.autotune()
         xv = op.seed_vector(0, order=mb.ORDER_TENSOR)
         yv = op.empty()
         n_steps = 3 if prec == mb.PREC_F64 else max(5, args.steps // 2)
@@ -264,7 +269,7 @@ def run_gpu(args):
         ms = statistics.mean(pr)
         gbs = 2 * nbytes * dim / (ms * 1e-3) / 1e9
         extras[name] = {"ms_per_apply": round(ms, 4), "GBps": round(gbs, 2),
-                        "frac_of_hbm": round(gbs / peak, 4)}
+                        "frac_of_hbm": round(gbs / peak, 4), "apply_shape": shape}
         del op, xv, yv
         torch.cuda.empty_cache()
 
@@ -372,18 +377,24 @@ def run_batch_extra(mb, torch):
     mb.batch_ground_states(descs[:8], seeds[:8], kmax=20)  # warm up tables / kernels
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    res = mb.batch_ground_states(descs, seeds, kmax=150, refine=True, use_graph=True)
+    eng = []
+    res = mb.batch_ground_states(descs, seeds, kmax=150, refine=True, use_graph=True,
+                                 engine_out=eng)
     t_batch = time.perf_counter() - t0
-    # the plain per-instance FP64 GPU solver on a sample (same 150 steps), and
-    # a converged FP64 reference for the accuracy check
+    engine_shape = eng[0].shape()
+    del eng
+    # the plain per-instance FP64 GPU solver timed on a sample (same 150
+    # steps); every instance checked against a converged FP64 solve
     idx = list(range(0, len(secs), 64))
     t0 = time.perf_counter()
     ref = [fp64_solve(mb, *secs[i], 150, i) for i in idx]
     t_ref = (time.perf_counter() - t0) / len(idx)
-    conv = [fp64_solve(mb, *secs[i], 500, i, conv_tol=1e-13) for i in idx]
+    t0 = time.perf_counter()
+    conv = [fp64_solve(mb, *secs[i], 500, i, conv_tol=1e-13) for i in range(len(secs))]
+    t_check = time.perf_counter() - t0
     errs = [abs(res[i].e0 - r) / abs(r) for i, r in zip(idx, ref)]
-    errs_conv = [abs(res[i].e0 - r) / abs(r) for i, r in zip(idx, conv)]
-    errs_fp64_150 = [abs(a - r) / abs(r) for a, r in zip(ref, conv)]
+    errs_conv = [abs(r.e0 - c) / abs(c) for r, c in zip(res, conv)]
+    errs_fp64_150 = [abs(a - conv[i]) / abs(conv[i]) for i, a in zip(idx, ref)]
     return {
         "instances": len(secs), "lanczos_steps": 150, "vectors": "complex64",
         "recurrence": "FP64 alpha/beta + FP64 Rayleigh-Ritz refinement",
@@ -393,7 +404,14 @@ def run_batch_extra(mb, torch):
         "max_rel_dE0_vs_fp64_same_steps": float(max(errs)),
         "max_rel_dE0_vs_converged_fp64": float(max(errs_conv)),
         "fp64_150_steps_max_rel_dE0_vs_converged": float(max(errs_fp64_150)),
-        "sample_checked": len(idx), "cuda_graph": True, "autotuned": True,
+        "instances_checked": len(errs_conv),
+        "instances_within_1e-8": int(sum(e <= 1e-8 for e in errs_conv)),
+        "check_seconds": round(t_check, 2),
+        "fp64_timing_sample": len(idx), "cuda_graph": True, "autotuned": True,
+        "engine_shape": engine_shape,
+        "step": "one persistent cooperative launch of the fused step kernel per fixed-length "
+                "phase (all its steps), captured as a CUDA graph" if engine_shape["persistent"]
+                else "grouped kernels per step, captured as a CUDA graph",
     }
 
 
@@ -487,55 +505,64 @@ def run_momentum_extra(mb, torch):
     return out
 
 
-def run_precision_extra(mb, torch):
+def run_precision_extra(mb, torch, k=150):
+    """1D L=16, N_up=N_down=8 (165,636,900 states), U in {2, 4, 8}: FP32
+    (complex64) vectors and apply, Lanczos with full re-orthogonalisation
+    against a complex64 Krylov basis (k vectors, 1.33 GB each) with FP64
+    alpha/beta and projections, one FP64 Rayleigh-Ritz refinement; against
+    the plain FP64 GPU solver (complex128, FP64 arithmetic, Ritz stability
+    1e-12) on the same problem, timed at every U.  The FP32 run without
+    re-orthogonalisation is reported beside them."""
     out = {}
     b = mb.FermionBasis.with_fixed_particle_number_and_spin(16, 16, 0)
     for u in (2.0, 4.0, 8.0):
         model = mb.HubbardModel(1.0, u, 16)
+        op64 = mb.GpuHubbardOperator(b, model, mb.PREC_F64)
+        s64 = op64.seed_vector(0, order=mb.ORDER_TENSOR)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r64 = mb.find_min_eigenpair(op64, 400, s64, order=mb.ORDER_TENSOR, conv_tol=1e-12,
+                                    check_every=10, want_vector=False)
+        t64 = time.perf_counter() - t0
+        del op64, s64
+        torch.cuda.empty_cache()
         op32 = mb.GpuHubbardOperator(b, model, mb.PREC_F32)
         s32 = op32.seed_vector(0, order=mb.ORDER_TENSOR)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r32 = mb.find_min_eigenpair(op32, 300, s32, order=mb.ORDER_TENSOR, conv_tol=1e-10,
-                                    check_every=10, want_vector=False, refine=True)
-        t32 = time.perf_counter() - t0
-        raw = mb.find_min_eigenpair(op32, r32.steps, s32, order=mb.ORDER_TENSOR,
-                                    want_vector=False).value
+        rr = mb.find_min_eigenpair(op32, k, s32, order=mb.ORDER_TENSOR, reorth=True,
+                                   basis_precision=mb.PREC_F32, conv_tol=1e-10, check_every=10,
+                                   want_vector=False, refine=True)
+        t_re = time.perf_counter() - t0
+        torch.cuda.empty_cache()
+        t0 = time.perf_counter()
+        rp = mb.find_min_eigenpair(op32, 300, s32, order=mb.ORDER_TENSOR, conv_tol=1e-10,
+                                   check_every=10, want_vector=False, refine=True)
+        t_plain = time.perf_counter() - t0
+        raw = mb.find_min_eigenpair(op32, rr.steps, s32, order=mb.ORDER_TENSOR, reorth=True,
+                                    basis_precision=mb.PREC_F32, want_vector=False).value
         del op32, s32
         torch.cuda.empty_cache()
-        opq = mb.GpuHubbardOperator(b, model, mb.PREC_Q64)
-        sq = opq.seed_vector(0, order=mb.ORDER_TENSOR)
-        t0 = time.perf_counter()
-        rq = mb.find_min_eigenpair(opq, 300, sq, order=mb.ORDER_TENSOR, conv_tol=1e-12,
-                                   check_every=10, want_vector=False)
-        tq = time.perf_counter() - t0
-        del opq, sq
-        torch.cuda.empty_cache()
+        e = r64.value
         out[f"U={u:g}"] = {
-            "e0_fp64class": rq.value, "e0_fp32_refined": r32.value, "e0_fp32_raw": raw,
-            "rel_dE0_refined": abs(r32.value - rq.value) / abs(rq.value),
-            "rel_dE0_raw": abs(raw - rq.value) / abs(rq.value),
-            "steps_fp32": r32.steps, "steps_q64": rq.steps,
-            "seconds_fp32_refined": round(t32, 3), "seconds_q64": round(tq, 3),
+            "e0_fp64": e, "steps_fp64": r64.steps, "seconds_fp64": round(t64, 3),
+            "e0_fp32_reorth_refined": rr.value, "steps_fp32_reorth": rr.steps,
+            "seconds_fp32_reorth_refined": round(t_re, 3),
+            "rel_dE0_fp32_reorth_refined_vs_fp64": abs(rr.value - e) / abs(e),
+            "e0_fp32_reorth_unrefined": raw,
+            "rel_dE0_fp32_reorth_unrefined_vs_fp64": abs(raw - e) / abs(e),
+            "e0_fp32_plain_refined": rp.value, "steps_fp32_plain": rp.steps,
+            "seconds_fp32_plain_refined": round(t_plain, 3),
+            "rel_dE0_fp32_plain_refined_vs_fp64": abs(rp.value - e) / abs(e),
+            "speedup_fp32_reorth_refined_vs_fp64": round(t64 / t_re, 2),
+            "speedup_fp32_plain_refined_vs_fp64": round(t64 / t_plain, 2),
         }
-        if u == 4.0:
-            # the plain FP64 GPU solver on the same problem, same stopping rule
-            op64 = mb.GpuHubbardOperator(b, model, mb.PREC_F64)
-            s64 = op64.seed_vector(0, order=mb.ORDER_TENSOR)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            r64 = mb.find_min_eigenpair(op64, 300, s64, order=mb.ORDER_TENSOR, conv_tol=1e-12,
-                                        check_every=10, want_vector=False)
-            t64 = time.perf_counter() - t0
-            del op64, s64
-            torch.cuda.empty_cache()
-            out[f"U={u:g}"].update({
-                "e0_fp64": r64.value, "steps_fp64": r64.steps, "seconds_fp64": round(t64, 3),
-                "rel_dE0_fp64_vs_fp64class": abs(r64.value - rq.value) / abs(rq.value),
-                "speedup_fp32_refined_vs_fp64": round(t64 / t32, 2)})
-    return {"workload": "1D L=16 N_up=N_down=8 (165,636,900 states)",
-            "note": "plain Lanczos to Ritz stability (1e-10); re-orthogonalised runs are "
-                    "covered by the tests at smaller sizes", "runs": out}
+    return {"workload": "1D L=16 N_up=N_down=8 (165,636,900 states), t=1",
+            "fp32_reorth": f"full re-orthogonalisation, complex64 basis of at most {k} vectors "
+                           "(1.33 GB each), FP64 alpha/beta/projections, stop at Ritz stability "
+                           "1e-10, then FP64 Rayleigh-Ritz on span{x, Hx, H^2 x}",
+            "fp64": "plain Lanczos on complex128 with FP64 arithmetic, Ritz stability 1e-12",
+            "runs": out}
 
 
 SERVE_LATTICES = [(6,), (7,), (8,), (9,), (10,), (11,), (12,), (13,), (14,), (3, 3), (2, 4), (3, 4)]
@@ -574,11 +601,22 @@ def fp64_dos(mb, dims, nn, u, n_moments, seed):
     return mb.kpm_dos_moments(op, n_moments, 1, seed, lo - pad, hi + pad, 0.01)
 
 
+def q64_dos(mb, dims, nn, u, n_moments, seed, lo, hi, padding=0.01):
+    """DOS moments of one probe (Philox stream 1, key `seed`: the engine's
+    probe) on an FP64-class (Q64) operator with the given bounds."""
+    L = 1
+    for d in dims:
+        L *= d
+    b = mb.FermionBasis.with_fixed_particle_number_and_spin(L, 2 * nn, 0)
+    op = mb.GpuHubbardOperator(b, mb._Hubbard(1.0, u, dims), mb.PREC_Q64)
+    return mb.kpm_dos_moments(op, n_moments, 1, seed, lo, hi, padding)
+
+
 def run_serve_extra(mb, torch, n_requests=400, rate=200.0):
     import numpy as np
     reqs = serve_requests(n_requests, rate)
     eng = mb.Engine()
-    pending, live, lat, e_served = [], {}, {}, {}
+    pending, live, lat, e_served, dos_served = [], {}, {}, {}, {}
     nxt = 0
     t0 = time.perf_counter()
     while len(lat) < len(reqs):
@@ -603,6 +641,8 @@ def run_serve_extra(mb, torch, n_requests=400, rate=200.0):
                 lat[i] = (time.perf_counter() - t0) - a
                 if kind == 0:
                     e_served[i] = r.e0
+                else:
+                    dos_served[i] = (np.asarray(r[0]), r[1], r[2])
         elif nxt < len(reqs):
             time.sleep(max(0.0, reqs[nxt][0] - (time.perf_counter() - t0)))
     wall = time.perf_counter() - t0
@@ -622,14 +662,22 @@ def run_serve_extra(mb, torch, n_requests=400, rate=200.0):
         lat_ref.append((time.perf_counter() - t0) - a)
     wall_ref = time.perf_counter() - t0
     lr = np.array(sorted(lat_ref))
-    # accuracy against a converged FP64 reference on a sample of the ground states
+    # accuracy of every result: each ground state against a converged FP64
+    # solve; each DOS request's moments against the FP64-class (Q64) Chebyshev
+    # moments of the same probe with the bounds the engine used
     by_idx = {r[5]: r for r in reqs}
-    check = sorted(e_served)[::4]
+    t_chk = time.perf_counter()
     dE = []
-    for i in check:
+    for i in sorted(e_served):
         a, dims, nn, u, kind, _ = by_idx[i]
         e_conv = fp64_solve(mb, dims, nn, nn, u, 500, i, conv_tol=1e-13)
         dE.append(abs(e_served[i] - e_conv) / max(abs(e_conv), 1e-300))
+    dmu = []
+    for i in sorted(dos_served):
+        a, dims, nn, u, kind, _ = by_idx[i]
+        mu, lo, hi = dos_served[i]
+        dmu.append(float(np.max(np.abs(mu - q64_dos(mb, dims, nn, u, len(mu), i, lo, hi)))))
+    t_chk = time.perf_counter() - t_chk
     return {
         "requests": len(reqs), "arrival_rate_per_s": rate,
         "mix": "50 % ground state (Ritz stability 1e-10 + FP64 Rayleigh refinement), "
@@ -646,6 +694,11 @@ def run_serve_extra(mb, torch, n_requests=400, rate=200.0):
         "solves_per_s_ratio": round(wall_ref / wall, 2),
         "max_rel_dE0_vs_converged_fp64": float(max(dE)) if dE else None,
         "ground_states_checked": len(dE),
+        "ground_states_within_1e-8": int(sum(x <= 1e-8 for x in dE)),
+        "max_abs_dmu_vs_fp64class": float(max(dmu)) if dmu else None,
+        "dos_requests_checked": len(dmu),
+        "dos_within_1e-4": int(sum(x <= 1e-4 for x in dmu)),
+        "check_seconds": round(t_chk, 2),
     }
 
 
@@ -751,6 +804,70 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Kernel probes for profiling captures: a few launches of one kernel's
+# workload, nothing timed (ncu measures).  Each prints one JSON line.
+# ---------------------------------------------------------------------------
+PROBES = ("q64_apply", "fp64_apply", "fp32_apply", "engine_persistent", "engine_grouped",
+          "momentum_csr")
+
+
+def run_probe(args):
+    import torch
+
+    import manybody_gb300 as mb
+    torch.cuda.set_device(0)
+    name = args.probe
+    if name in ("q64_apply", "fp64_apply", "fp32_apply"):
+        w = CASES[args.case]
+        L = 1
+        for d in w["lattice"]:
+            L *= d
+        basis = mb.FermionBasis.with_fixed_particle_number_and_spin(L, w["n_up"] + w["n_down"],
+                                                                    w["n_up"] - w["n_down"])
+        prec = {"q64_apply": mb.PREC_Q64, "fp64_apply": mb.PREC_F64,
+                "fp32_apply": mb.PREC_F32}[name]
+        op = mb.GpuHubbardOperator(basis, mb._Hubbard(w["t"], w["U"], w["lattice"]), prec)
+        shape, _ = op.autotune()
+        x = op.seed_vector(0, order=mb.ORDER_TENSOR)
+        if prec == mb.PREC_Q64:
+            xq, ex = op.q64_from_f64(x, order=mb.ORDER_TENSOR)
+            yq = op.q64_empty()
+            for _ in range(args.steps):
+                op.apply_q64(xq, ex, out=yq)
+        else:
+            y = op.empty()
+            for _ in range(args.steps):
+                op.apply(x, out=y, order=mb.ORDER_TENSOR)
+        torch.cuda.synchronize()
+        out = {"probe": name, "case": args.case, "dim": op.dimension(), "apply_shape": shape,
+               "launches": args.steps}
+    elif name in ("engine_persistent", "engine_grouped"):
+        secs = batch_sectors(n=64)
+        descs = [mb.sector(d, nu, nd, 1.0, u) for d, nu, nd, u in secs]
+        eng = mb.Engine()
+        eng.set_persistent(name == "engine_persistent")
+        for i, d in enumerate(descs):
+            eng.try_submit(d, seed=i, kmax=150, rel_tol=0.0)
+        eng.step(args.steps)
+        torch.cuda.synchronize()
+        import math
+        states = sum(math.comb(d[0], nu) * math.comb(d[0], nd) for d, nu, nd, _ in secs)
+        out = {"probe": name, "requests": len(descs), "steps": args.steps, "states": states,
+               "shape": eng.shape()}
+    else:  # momentum_csr: the K = (0, 0) sector of 4x4, N_up = N_down = 4
+        dims = (4, 4)
+        basis = mb.FermionBasis.with_fixed_particle_number_spin_momentum(16, 8, 0, dims, (0, 0))
+        op = mb.GpuHubbardOperator(basis, mb.HubbardModelMomentum(1.0, 8.0, dims), mb.PREC_F64)
+        x = op.seed_vector(0)
+        y = op.empty()
+        for _ in range(args.steps):
+            op.apply(x, out=y)
+        torch.cuda.synchronize()
+        out = {"probe": name, "dim": op.dimension(), "launches": args.steps}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -766,9 +883,15 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--skip-cfg2-reorth", action="store_true",
                     help="leave out the 300-step fully re-orthogonalised Lanczos at 4x4 6+6")
+    ap.add_argument("--probe", choices=PROBES,
+                    help="run a few launches of one kernel's workload for a profiler "
+                         "(--steps launches; nothing timed, no bench line)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.probe:
+        run_probe(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

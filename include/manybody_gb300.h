@@ -196,7 +196,13 @@ int mb_op_apply_affine(mb_op_t op, const void* x_dev, void* y_dev, double scale,
  * run in groups ordered by where their states first appear in the reference
  * order, and each finished prefix of y goes back while later groups run; a
  * page-locked x is read over the link by the kernel that scatters it.
- * Safe from several host threads; calls on one operator run one at a time. */
+ * Calls on one operator from several host threads overlap: each runs on its
+ * own lane (two streams and its own staging buffers, about four vectors of
+ * device memory, made on first use and kept with the operator; at most 8
+ * lanes, further callers wait for one), with the bits a call alone gets.
+ * Pageable vectors (an Armadillo vector's memory) pass through the lane's own
+ * two 16 MiB page-locked bounce buffers; calls on page-locked vectors, each of
+ * which runs the host link at its full rate alone, take turns. */
 int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order);
 
 /* y = H x on device buffers in REFERENCE order, without allocating: no
@@ -206,12 +212,57 @@ int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order);
  * latency-critical loop that cannot afford cudaMalloc's implicit device
  * synchronisation).  mb_op_apply's permutation scratch comes instead from one
  * fixed 32 MiB array inside the library (two vectors of up to 1,048,576
- * complex128 elements), held on every GPU that loads the library until exit;
- * larger sectors return MB_ERR_CAPACITY.  The first call on a device sets up
- * (looks up the array's address, uploads a small table) with the operator's
- * device current; make it before any stream capture.  All calls on a device
- * share the array: calls that overlap on the GPU race; serialise them. */
+ * complex128 elements); larger sectors return MB_ERR_CAPACITY.  The array is
+ * part of the library's device code, which CUDA loads into a device lazily
+ * (the default since CUDA 12.2): the first call on a device loads it there,
+ * taking the 32 MiB on that device until the process exits, looks up the
+ * array's address and uploads a small table, with the operator's device
+ * current.  Make that first call during set-up, before any stream capture;
+ * later calls allocate nothing.  MB_PREC_F64, MB_PREC_F32 and MB_PREC_Q64
+ * operators (Q64 takes the steps of mb_op_apply on it: the same bits).  All
+ * calls on a device share the array: calls that overlap on the GPU race;
+ * serialise them. */
 int mb_op_apply_noalloc(mb_op_t op, const void* x_dev, void* y_dev, void* stream);
+
+/* ---- apply kernel shapes ------------------------------------------------- *
+ * No counterpart in the reference.  How a lattice operator's H|psi> runs on
+ * the GPU.  Every shape gives the same result bits on an MB_PREC_Q64
+ * operator (its hop sums are exact integers in any order).  Shapes other than
+ * the default {1, 1, 32} apply to MB_PREC_Q64 lattice operators.
+ *  passes     1: one pass over the rows r_up; each row staged in shared
+ *                memory for the down hops, the up hops read from x in global
+ *                memory;
+ *             2: first a column pass (each column r_down staged in shared
+ *                memory, the up hops gathered there, their exact sums written
+ *                to scratch: one vector per stream, allocated on first use),
+ *                then the row pass adds them (sectors whose column fits);
+ *  row_split  1, 2 or 4 CTAs share a row (each stages it and takes every
+ *             row_split-th column group): fewer rows in flight, so the up-hop
+ *             rows they read stay in L2;
+ *  table_bits 32 or 16: width of the down/up hop-table entries (16 needs
+ *             sectors below 32760 states per spin). */
+typedef struct {
+  int passes;
+  int row_split;
+  int table_bits;
+  int prefetch;   /* 1: each warp prefetches its next column group's up-hop
+                     lines into L2 (any lattice operator) */
+  int table_stage; /* 1: each warp copies its next column group's down-table
+                      words into its own shared buffer (cp.async) while it
+                      finishes the current one (MB_PREC_Q64, one pass, 32-bit
+                      entries, where the buffers fit beside the row) */
+  int reserved[3];
+} mb_apply_shape;
+int mb_op_get_apply_shape(mb_op_t op, mb_apply_shape* shape);
+int mb_op_set_apply_shape(mb_op_t op, const mb_apply_shape* shape);
+/* The apply autotuner: times every candidate shape of the operator on the
+ * live GPU (tensor-order device vectors, CUDA events on `stream`, median of 7
+ * applies after 2 warm-up ones), keeps the fastest and returns it with its
+ * time.  Choices are cached per (lattice, N_up, N_down, precision) for the
+ * process: a later operator of the same sector takes the cached shape without
+ * timing.  Operators without shapes (sparse matrix, block diagonal) keep the
+ * default and report 0 ms.  Allocates two (Q64: three) vectors while it runs. */
+int mb_op_autotune(mb_op_t op, void* stream, mb_apply_shape* chosen, double* best_ms);
 
 /* ---- seeded start vectors ----------------------------------------------- *
  * v[i] = (u1, u2), u ~ U[-1,1) from Philox4x32-10 (Salmon et al., SC'11) with
@@ -413,12 +464,46 @@ int mb_engine_set_warps(mb_engine_t engine, int warps_per_block);
  * Default 1,048,576 (a launch per large request pays off; many medium
  * requests run faster together); 1 sends every request through it. */
 int mb_engine_set_fused_threshold(mb_engine_t engine, int64_t min_states);
-/* Times the grouped apply at each block shape on the current requests and
- * keeps the fastest; *chosen = warps per block, *ms = its time per apply. */
+/* Times the step's apply at each shape on the current requests and keeps the
+ * fastest; *ms = its time per apply.  Persistent step: row_min_cols in
+ * {64, 128, 256} x ctas_per_sm in {all that fit, 2, 1}, timed with apply-only
+ * launches (they change no request's progress); grouped kernels: warps per
+ * block in {2, 4, 8, 16}.  *chosen = the grouped kernels' warps per block. */
 int mb_engine_autotune(mb_engine_t engine, int* chosen, double* ms);
-/* n_steps steps with no host round trip between them (fixed-length batches),
- * optionally as one captured CUDA graph replayed n_steps times. */
+/* n_steps steps with no host round trip between them (fixed-length batches).
+ * Persistent step (the default): ONE cooperative launch of the fused kernel
+ * runs all n_steps (with use_graph, captured as a CUDA graph and launched);
+ * grouped kernels: the step's launches captured once and the graph replayed
+ * n_steps times. */
 int mb_engine_step_fixed(mb_engine_t engine, int n_steps, int use_graph, int* n_active);
+
+/* The persistent step (default on): one cooperative launch runs whole engine
+ * steps of every request, the apply (rows of wide or large sectors block per
+ * row, staged in shared memory with the sliced tables; the others warp per
+ * row), the per-request fixed-order alpha and beta reductions, the update, the
+ * normalisation and the step counters, its phases separated by grid barriers.
+ * Off: each step is the grouped kernels (apply, reduce, update, reduce,
+ * normalise, advance).  Requests keep their progress across a switch, and get
+ * the same bits through both for sectors applied warp per row or row-staged
+ * in both; a large sector (>= the fused threshold) runs its rows through the
+ * block-per-row body here and the fused kernel there. */
+int mb_engine_set_persistent(mb_engine_t engine, int on);
+/* Budget in clock64 cycles of one grid-barrier wait of the persistent step
+ * (default 2^32, about two seconds).  A wait that runs past it sets the
+ * step's status word; every block then returns at its next barrier and the
+ * step fails with MB_ERR_TIMEOUT.  The requests in flight are lost then: the
+ * step stopped part-way, and the engine refuses further work (destroy it). */
+int mb_engine_set_wait_budget(mb_engine_t engine, int64_t cycles);
+typedef struct {
+  int persistent;    /* 1: the persistent step; 0: the grouped kernels */
+  int row_min_cols;  /* persistent: rows this wide or wider block per row (<= 256) */
+  int ctas_per_sm;   /* persistent: co-resident blocks per SM (0: all that fit) */
+  int grid;          /* persistent: blocks of the last launch shape (read only) */
+  int warps;         /* grouped kernels: warps per block (2, 4, 8, 16) */
+  int reserved[3];
+} mb_engine_shape;
+int mb_engine_get_shape(mb_engine_t engine, mb_engine_shape* shape);
+int mb_engine_set_shape(mb_engine_t engine, const mb_engine_shape* shape);
 
 /* ---- block reductions on device vectors (for drivers above this ABI) ---- */
 /* *out = Re <x, y> (arma::cdot real part), FP64 accumulation, deterministic. */

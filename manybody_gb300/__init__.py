@@ -73,6 +73,18 @@ class LanczosOpts(C.Structure):
                 ("check_every", C.c_int), ("refine", C.c_int)]
 
 
+class EngineShape(C.Structure):
+    """mb_engine_shape: the engine step's launch shape."""
+    _fields_ = [("persistent", C.c_int), ("row_min_cols", C.c_int), ("ctas_per_sm", C.c_int),
+                ("grid", C.c_int), ("warps", C.c_int), ("reserved", C.c_int * 3)]
+
+
+class ApplyShape(C.Structure):
+    """mb_apply_shape: how a lattice operator's H|psi> runs on the GPU."""
+    _fields_ = [("passes", C.c_int), ("row_split", C.c_int), ("table_bits", C.c_int),
+                ("prefetch", C.c_int), ("table_stage", C.c_int), ("reserved", C.c_int * 3)]
+
+
 # name -> (restype, argtypes); every exported symbol of include/manybody_gb300.h.
 SIGNATURES = {
     "mb_version": (C.c_int, []),
@@ -155,6 +167,13 @@ SIGNATURES = {
     "mb_engine_completed": (C.c_int, [_vp, _i64p, C.c_int64, _i64p]),
     "mb_engine_stats": (C.c_int, [_vp, _i64p, _dp, _dp]),
     "mb_engine_autotune": (C.c_int, [_vp, C.POINTER(C.c_int), _dp]),
+    "mb_engine_set_persistent": (C.c_int, [_vp, C.c_int]),
+    "mb_engine_set_wait_budget": (C.c_int, [_vp, C.c_int64]),
+    "mb_engine_get_shape": (C.c_int, [_vp, C.POINTER(EngineShape)]),
+    "mb_engine_set_shape": (C.c_int, [_vp, C.POINTER(EngineShape)]),
+    "mb_op_get_apply_shape": (C.c_int, [_vp, C.POINTER(ApplyShape)]),
+    "mb_op_set_apply_shape": (C.c_int, [_vp, C.POINTER(ApplyShape)]),
+    "mb_op_autotune": (C.c_int, [_vp, _vp, C.POINTER(ApplyShape), _dp]),
     "mb_dot_re": (C.c_int, [_vp, _vp, _vp, _dp]),
     "mb_norm": (C.c_int, [_vp, _vp, _dp]),
 }
@@ -672,6 +691,30 @@ class GpuHubbardOperator:
                                      self._stream(stream)))
         return y, e.value
 
+    def apply_shape(self) -> dict:
+        """The kernel shape of this operator's apply (mb_op_get_apply_shape)."""
+        sh = ApplyShape()
+        _check(lib().mb_op_get_apply_shape(self._h, C.byref(sh)))
+        return {"passes": sh.passes, "row_split": sh.row_split, "table_bits": sh.table_bits,
+                "prefetch": sh.prefetch, "table_stage": sh.table_stage}
+
+    def set_apply_shape(self, passes: int = 1, row_split: int = 1, table_bits: int = 32,
+                        prefetch: int = 0, table_stage: int = 0):
+        """Choose the apply's kernel shape (mb_op_set_apply_shape)."""
+        sh = ApplyShape()
+        sh.passes, sh.row_split, sh.table_bits = passes, row_split, table_bits
+        sh.prefetch, sh.table_stage = prefetch, table_stage
+        _check(lib().mb_op_set_apply_shape(self._h, C.byref(sh)))
+
+    def autotune(self, stream=None):
+        """Time every candidate shape on the GPU and keep the fastest
+        (mb_op_autotune); returns (shape dict, ms per apply)."""
+        sh = ApplyShape()
+        ms = C.c_double()
+        _check(lib().mb_op_autotune(self._h, self._stream(stream), C.byref(sh), C.byref(ms)))
+        return ({"passes": sh.passes, "row_split": sh.row_split, "table_bits": sh.table_bits,
+                 "prefetch": sh.prefetch, "table_stage": sh.table_stage}, ms.value)
+
     def q64_mantissa_bits(self) -> int:
         b = C.c_int()
         _check(lib().mb_q64_mantissa_bits(self._h, C.byref(b)))
@@ -1047,6 +1090,29 @@ class Engine:
         _check(lib().mb_engine_stats(self._h, C.byref(st), C.byref(w), C.byref(d)))
         return st.value, w.value, d.value
 
+    def set_persistent(self, on: bool):
+        """The persistent fused step (default) or the grouped kernels."""
+        _check(lib().mb_engine_set_persistent(self._h, int(bool(on))))
+
+    def set_wait_budget(self, cycles: int):
+        """clock64 budget of one grid-barrier wait of the persistent step."""
+        _check(lib().mb_engine_set_wait_budget(self._h, int(cycles)))
+
+    def shape(self) -> dict:
+        sh = EngineShape()
+        _check(lib().mb_engine_get_shape(self._h, C.byref(sh)))
+        return {"persistent": sh.persistent, "row_min_cols": sh.row_min_cols,
+                "ctas_per_sm": sh.ctas_per_sm, "grid": sh.grid, "warps": sh.warps}
+
+    def set_shape(self, persistent=None, row_min_cols=None, ctas_per_sm=None, warps=None):
+        cur = self.shape()
+        sh = EngineShape()
+        sh.persistent = cur["persistent"] if persistent is None else int(bool(persistent))
+        sh.row_min_cols = cur["row_min_cols"] if row_min_cols is None else row_min_cols
+        sh.ctas_per_sm = cur["ctas_per_sm"] if ctas_per_sm is None else ctas_per_sm
+        sh.warps = cur["warps"] if warps is None else warps
+        _check(lib().mb_engine_set_shape(self._h, C.byref(sh)))
+
     def set_fused_threshold(self, min_states: int):
         """Sectors of at least min_states states use the fused complex64 apply."""
         _check(lib().mb_engine_set_fused_threshold(self._h, min_states))
@@ -1058,9 +1124,14 @@ class Engine:
 
 
 def batch_ground_states(descs, seeds=None, kmax: int = 150, refine: bool = True,
-                        use_graph: bool = True, autotune: bool = True, fused_threshold=None):
+                        use_graph: bool = True, autotune: bool = True, fused_threshold=None,
+                        persistent: bool = True, engine_out=None):
     """Fixed-length batched Lanczos for many sectors: returns [EngineResult]."""
     eng = Engine()
+    if engine_out is not None:
+        engine_out.append(eng)
+    if not persistent:
+        eng.set_persistent(False)
     if fused_threshold is not None:
         eng.set_fused_threshold(fused_threshold)
     seeds = seeds if seeds is not None else [0] * len(descs)

@@ -64,6 +64,10 @@ struct SlotDesc {
   const int32_t* up_lpos;
   const uint32_t* dn_sell;
   const int32_t* dn_sgrp;
+  // diagonal self energies of lattices with a size-1 dimension (t times the
+  // sector's t = 1 values, per up / down state), else nullptr
+  const float* self_up;
+  const float* self_dn;
 };
 
 constexpr int kModeIdle = kEngIdle;
@@ -124,7 +128,8 @@ k_eng_apply(const SlotDesc* __restrict__ slots, const int2* __restrict__ items, 
           ai = fmaf(wgt, val.y, ai);
         }
         const float2 xv = v[c];
-        const float d = sc * (s.ufold[__popc(um & s.dn_mask[c])] - shift);
+        const float d = sc * (s.ufold[__popc(um & s.dn_mask[c])] +
+                            (s.self_up ? s.self_up[r] + s.self_dn[c] : 0.f) - shift);
         float2 o;
         o.x = fmaf(hop, ar, d * xv.x);
         o.y = fmaf(hop, ai, d * xv.y);
@@ -271,7 +276,8 @@ k_eng_apply_rows(const SlotDesc* __restrict__ slots, const int2* __restrict__ it
       ai += pi - ni;
       if (!live) continue;
       const float2 xv = srow[c];
-      const float d = sc * (s.ufold[__popc(um & s.dn_mask[c])] - shift);
+      const float d = sc * (s.ufold[__popc(um & s.dn_mask[c])] +
+                            (s.self_up ? s.self_up[r] + s.self_dn[c] : 0.f) - shift);
       float2 o;
       o.x = fmaf(hop, ar, d * xv.x);
       o.y = fmaf(hop, ai, d * xv.y);
@@ -606,6 +612,529 @@ __global__ void k_f32_to_f64(const float2* __restrict__ a, double2* __restrict__
   }
 }
 
+
+// ===========================================================================
+// The persistent engine step.  One cooperative launch runs `steps` engine
+// steps of every active request, the phases of a step separated by a grid
+// barrier:
+//   A  apply: rows of staged sectors block per row (the row and its sign-
+//      sorted up list in shared memory, the sliced down table), rows of small
+//      sectors warp per row (the row staged in the warp's own shared memory,
+//      CSR down table) -> per-row partials Re<v,w>, <w,w>;
+//   B  per-request fixed-order sum of the partials -> alpha_k (Chebyshev:
+//      Re<T_k,T_k+1> and <T_k+1,T_k+1>);
+//   C  w -= alpha_k v and per-row ||w||^2 (Lanczos); w = (w - alpha v) / beta,
+//      x += y w (replay);
+//   D  per-request sum -> beta_k;
+//   E  v_k+1 = w / beta_k;
+//   F  step counters, breakdown (beta <= 1000 eps) and completion.
+// The arithmetic of every phase is that of the grouped kernels above (same
+// operation order, same fixed-order reductions over 256 threads), so a request
+// gets the same bits alone, in any mix, and through either path.  Data that
+// other CTAs of the launch write is read after a grid barrier (release fence
+// and atomic arrival, gpu-scope acquire of the generation, then the block
+// barrier) with ordinary loads, never through the read-only path; the step
+// state (counters, alpha, beta, partials) through L2.  A barrier wait that runs past its clock64
+// budget sets the status word, and every CTA then returns at its next barrier:
+// the step fails with MB_ERR_TIMEOUT instead of hanging.
+// ===========================================================================
+struct EngGrid {
+  unsigned int count;
+  unsigned int gen;
+  int status;   // 0: running; 1: a barrier wait ran out of its budget
+  int pad;
+};
+
+struct EngPersistArgs {
+  SlotDesc* slots;
+  int n_slots;
+  const int2* items;       // every (slot, row); item index = slot's item0 + row
+  int n_items;
+  const int2* items_rows;  // rows applied block per row (staged)
+  int n_rows;
+  const int2* items_warp;  // rows applied warp per row
+  int n_warp;
+  double* part;            // [n_items]
+  double* part2;           // [n_items]
+  int row_cols;            // widest staged row
+  int steps;
+  int apply_only;          // 1: phase A only (the autotuner's timing runs)
+  EngGrid* grid;
+  long long budget;        // clock64 cycles one barrier wait may take
+};
+
+constexpr int kEngPWarps = 8;             // 256 threads: the reductions' width
+constexpr int kEngWarpRowCols = 256;      // widest row of the warp-per-row items
+
+__device__ __forceinline__ unsigned eng_ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int eng_ld_relaxed(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void eng_st_release(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid barrier with a bounded wait; false once any CTA has given up.
+__device__ bool eng_grid_sync(EngGrid* g, long long budget) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    const unsigned gen = eng_ld_acquire(&g->gen);
+    if (atomicAdd(&g->count, 1u) == gridDim.x - 1) {
+      atomicExch(&g->count, 0u);
+      __threadfence();
+      eng_st_release(&g->gen, gen + 1u);
+    } else {
+      const long long t0 = clock64();
+      while (eng_ld_acquire(&g->gen) == gen) {
+        if (eng_ld_relaxed(&g->status) != 0) {
+          ok = 0;
+          break;
+        }
+        if (clock64() - t0 > budget) {
+          atomicExch(&g->status, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    if (ok && eng_ld_relaxed(&g->status) != 0) ok = 0;
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+struct SlotNow {
+  int k, mode, kmax, steps;
+};
+__device__ __forceinline__ SlotNow slot_now(const SlotDesc& s) {
+  SlotNow n;
+  n.k = __ldcg(&s.k);
+  n.mode = __ldcg(&s.mode);
+  n.kmax = __ldcg(&s.kmax);
+  n.steps = __ldcg(&s.steps);
+  return n;
+}
+
+// compensated float accumulation of a * b (exact product, TwoSum)
+__device__ __forceinline__ void eng_acc(float& hi, float& lo, float a, float b) {
+  const float p = a * b, pe = fmaf(a, b, -p);
+  const float s1 = hi + p, bp = s1 - hi;
+  lo += ((hi - (s1 - bp)) + (p - bp)) + pe;
+  hi = s1;
+}
+
+// Phase A, one staged row (block-level): the arithmetic of k_eng_apply_rows.
+__device__ void p_apply_row(const SlotDesc& s, const SlotNow& n, int64_t r, int64_t pidx,
+                            double* part, double* part2, float2* srow, uint32_t* s_up,
+                            double (*red)[2]) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = n.k;
+  const bool lanczos = n.mode == kModeLanczos && k < n.kmax;
+  const bool replay = n.mode == kModeReplay && k + 1 < n.steps;
+  const bool cheb = n.mode == kModeCheb && k < n.kmax;
+  if (!(lanczos || replay || cheb)) {  // uniform over the block
+    if (threadIdx.x == 0) {
+      part[pidx] = 0.0;
+      part2[pidx] = 0.0;
+    }
+    return;
+  }
+  const int64_t Dd = s.Dd;
+  const uint64_t row_bytes = sizeof(float2) * (uint64_t)Dd;
+  const float2* x = s.buf[(k + 1) % 3];
+  const float2* v = x + r * Dd;
+  const float2* z = s.buf[k % 3] + r * Dd;
+  float2* w = s.buf[(k + 2) % 3] + r * Dd;
+  const double bprev = cheb ? 1.0 : (k > 0 ? __ldcg(&s.beta[k - 1]) : 0.0);
+  const float beta = (float)(-bprev);
+  const float sc = cheb ? (k == 0 ? 1.f : 2.f) / s.cheb_a : s.scale;
+  const float shift = cheb ? s.cheb_b : 0.f;
+  const float hop = -s.t * sc;
+  const uint32_t um = s.up_mask[r];
+  const int u0 = __ldg(&s.up_loff[r]), nu = __ldg(&s.up_loff[r + 1]) - u0;
+  const int npos = __ldg(&s.up_lpos[r]);
+  __syncthreads();  // the previous item's readers are done with srow / s_up
+  for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) srow[c] = v[c];
+  if (threadIdx.x < kSlicedPads) srow[Dd + threadIdx.x] = make_float2(0.f, 0.f);
+  for (int j = threadIdx.x; j < nu; j += blockDim.x) s_up[j] = __ldg(&s.up_list[u0 + j]);
+  __syncthreads();
+  float hi = 0.f, lo = 0.f, hi2 = 0.f, lo2 = 0.f;
+  const int64_t ngroups = (Dd + 31) >> 5;
+  for (int64_t g = warp; g < ngroups; g += kEngPWarps) {
+    const int64_t c = (g << 5) + lane;
+    const bool live = c < Dd;
+    const int64_t cl = live ? c : Dd - 1;
+    float ar = 0.f, ai = 0.f;
+    const int2 gi = __ldg(reinterpret_cast<const int2*>(s.dn_sgrp) + g);
+    const uint4* ep = reinterpret_cast<const uint4*>(s.dn_sell + gi.x) + lane;
+    auto dn = [&](uint32_t e) {
+      const float2 val = srow[e & 0x7FFFFFFFu];
+      const float wgt = __int_as_float((int)(0x3f800000u | (e & 0x80000000u)));
+      ar = fmaf(wgt, val.x, ar);
+      ai = fmaf(wgt, val.y, ai);
+    };
+    for (int j = 0; j < gi.y; j += 4) {
+      const uint4 e = __ldg(ep + 8 * j);
+      dn(e.x);
+      dn(e.y);
+      dn(e.z);
+      dn(e.w);
+    }
+    const char* xc = reinterpret_cast<const char*>(x + cl);
+    auto up = [&](int q) {
+      return *reinterpret_cast<const float2*>(xc + (uint64_t)s_up[q] * row_bytes);
+    };
+    float pr = 0.f, pi = 0.f, nr = 0.f, ni = 0.f;
+    int j = 0;
+#pragma unroll 4
+    for (; j < npos; ++j) {
+      const float2 val = up(j);
+      pr += val.x;
+      pi += val.y;
+    }
+#pragma unroll 4
+    for (; j < nu; ++j) {
+      const float2 val = up(j);
+      nr += val.x;
+      ni += val.y;
+    }
+    ar += pr - nr;
+    ai += pi - ni;
+    if (!live) continue;
+    const float2 xv = srow[c];
+    const float d = sc * (s.ufold[__popc(um & s.dn_mask[c])] +
+                          (s.self_up ? s.self_up[r] + s.self_dn[c] : 0.f) - shift);
+    float2 o;
+    o.x = fmaf(hop, ar, d * xv.x);
+    o.y = fmaf(hop, ai, d * xv.y);
+    if (k > 0) {
+      const float2 zv = z[c];
+      o.x = fmaf(beta, zv.x, o.x);
+      o.y = fmaf(beta, zv.y, o.y);
+    }
+    w[c] = o;
+    if (!replay) {
+      eng_acc(hi, lo, xv.x, o.x);
+      eng_acc(hi, lo, xv.y, o.y);
+    }
+    if (cheb) {
+      eng_acc(hi2, lo2, o.x, o.x);
+      eng_acc(hi2, lo2, o.y, o.y);
+    }
+  }
+  double dxy = (double)hi + (double)lo, dyy = (double)hi2 + (double)lo2;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    dxy += __shfl_down_sync(0xffffffffu, dxy, o);
+    dyy += __shfl_down_sync(0xffffffffu, dyy, o);
+  }
+  if (lane == 0) {
+    red[warp][0] = dxy;
+    red[warp][1] = dyy;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // fixed order over the warps
+    double a = 0.0, b = 0.0;
+    for (int q = 0; q < kEngPWarps; ++q) {
+      a += red[q][0];
+      b += red[q][1];
+    }
+    part[pidx] = a;
+    part2[pidx] = b;
+  }
+}
+
+// Phase A, one small row (warp-level, the row staged in the warp's shared
+// memory): the arithmetic of k_eng_apply.
+__device__ void p_apply_warp_row(const SlotDesc& s, const SlotNow& n, int64_t r, int64_t pidx,
+                                 double* part, double* part2, float2* wrow) {
+  const int lane = threadIdx.x & 31;
+  const int k = n.k;
+  const bool replay = n.mode == kModeReplay;
+  const bool cheb = n.mode == kModeCheb;
+  double dxy = 0.0, dyy = 0.0;
+  if ((n.mode == kModeLanczos && k < n.kmax) || (replay && k + 1 < n.steps) ||
+      (cheb && k < n.kmax)) {
+    const int64_t Dd = s.Dd;
+    const float2* v = s.buf[(k + 1) % 3] + r * Dd;
+    const float2* x = s.buf[(k + 1) % 3];
+    const float2* z = s.buf[k % 3] + r * Dd;
+    float2* w = s.buf[(k + 2) % 3] + r * Dd;
+    __syncwarp();  // the warp's previous row is no longer read
+    for (int64_t c = lane; c < Dd; c += 32) wrow[c] = v[c];
+    __syncwarp();
+    const double bprev = cheb ? 1.0 : (k > 0 ? __ldcg(&s.beta[k - 1]) : 0.0);
+    const float beta = (float)(-bprev);
+    const float sc = cheb ? (k == 0 ? 1.f : 2.f) / s.cheb_a : s.scale;
+    const float shift = cheb ? s.cheb_b : 0.f;
+    const float hop = -s.t * sc;
+    float hi2 = 0.f, lo2 = 0.f;
+    const uint32_t um = s.up_mask[r];
+    const int u0 = s.up_off[r], u1 = s.up_off[r + 1];
+    float hi = 0.f, lo = 0.f;
+    for (int64_t c = lane; c < Dd; c += 32) {
+      float ar = 0.f, ai = 0.f;
+      for (int j = s.dn_off[c]; j < s.dn_off[c + 1]; ++j) {
+        const uint32_t e = __ldg(&s.dn_ent[j]);
+        const float2 val = wrow[e >> 8];
+        float wgt = (e & 2u) ? 2.f : 1.f;
+        if (e & 1u) wgt = -wgt;
+        ar = fmaf(wgt, val.x, ar);
+        ai = fmaf(wgt, val.y, ai);
+      }
+      for (int j = u0; j < u1; ++j) {
+        const uint32_t e = __ldg(&s.up_ent[j]);
+        const float2 val = x[(int64_t)(e >> 8) * Dd + c];
+        float wgt = (e & 2u) ? 2.f : 1.f;
+        if (e & 1u) wgt = -wgt;
+        ar = fmaf(wgt, val.x, ar);
+        ai = fmaf(wgt, val.y, ai);
+      }
+      const float2 xv = wrow[c];
+      const float d = sc * (s.ufold[__popc(um & s.dn_mask[c])] +
+                            (s.self_up ? s.self_up[r] + s.self_dn[c] : 0.f) - shift);
+      float2 o;
+      o.x = fmaf(hop, ar, d * xv.x);
+      o.y = fmaf(hop, ai, d * xv.y);
+      if (k > 0) {
+        const float2 zv = z[c];
+        o.x = fmaf(beta, zv.x, o.x);
+        o.y = fmaf(beta, zv.y, o.y);
+      }
+      w[c] = o;
+      if (!replay) {
+        eng_acc(hi, lo, xv.x, o.x);
+        eng_acc(hi, lo, xv.y, o.y);
+      }
+      if (cheb) {
+        eng_acc(hi2, lo2, o.x, o.x);
+        eng_acc(hi2, lo2, o.y, o.y);
+      }
+    }
+    dxy = (double)hi + (double)lo;
+    dyy = (double)hi2 + (double)lo2;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      dxy += __shfl_down_sync(0xffffffffu, dxy, o);
+      dyy += __shfl_down_sync(0xffffffffu, dyy, o);
+    }
+  }
+  if (lane == 0) {
+    part[pidx] = dxy;
+    part2[pidx] = dyy;
+  }
+}
+
+// Phases B and D, one request (block-level): the sum of k_eng_seg_reduce.
+__device__ void p_seg_reduce(SlotDesc& s, const double* part, const double* part2, int what,
+                             double* red, double* red2) {
+  const SlotNow n = slot_now(s);
+  const int k = n.k;
+  const bool cheb = n.mode == kModeCheb && what == 0;
+  double a = 0.0, b = 0.0;
+  for (int it = s.item0 + threadIdx.x; it < s.item1; it += blockDim.x) {
+    a += __ldcg(part + it);
+    if (cheb) b += __ldcg(part2 + it);
+  }
+  __syncthreads();  // the previous request's sums are read
+  red[threadIdx.x] = a;
+  red2[threadIdx.x] = b;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      red[threadIdx.x] += red[threadIdx.x + w];
+      red2[threadIdx.x] += red2[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && n.mode == kModeLanczos && k < n.kmax) {
+    if (what == 0) s.alpha[k] = red[0];
+    else s.beta[k] = sqrt(fmax(red[0], 0.0));
+  }
+  if (threadIdx.x == 0 && cheb && k < n.kmax) {
+    s.alpha[k] = red[0];
+    s.beta[k] = red2[0];
+  }
+}
+
+// Phase C, one row (warp-level): k_eng_update and k_eng_replay_update.
+__device__ void p_update_row(const SlotDesc& s, const SlotNow& n, int64_t r, int it, double* part) {
+  const int lane = threadIdx.x & 31;
+  const int k = n.k;
+  const int64_t Dd = s.Dd;
+  if (n.mode == kModeLanczos && k < n.kmax) {
+    const float2* v = s.buf[(k + 1) % 3] + r * Dd;
+    float2* w = s.buf[(k + 2) % 3] + r * Dd;
+    const float a = (float)__ldcg(&s.alpha[k]);
+    float hi = 0.f, lo = 0.f;
+    // four elements a lane in flight (half the threads of the grouped
+    // kernels run here), summed in the same order
+    int64_t c = lane;
+    for (; c + 96 < Dd; c += 128) {
+      float2 o[4], xv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        o[q] = w[c + 32 * q];
+        xv[q] = v[c + 32 * q];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        o[q].x = fmaf(-a, xv[q].x, o[q].x);
+        o[q].y = fmaf(-a, xv[q].y, o[q].y);
+        w[c + 32 * q] = o[q];
+        eng_acc(hi, lo, o[q].x, o[q].x);
+        eng_acc(hi, lo, o[q].y, o[q].y);
+      }
+    }
+    for (; c < Dd; c += 32) {
+      float2 o = w[c];
+      const float2 xv = v[c];
+      o.x = fmaf(-a, xv.x, o.x);
+      o.y = fmaf(-a, xv.y, o.y);
+      w[c] = o;
+      eng_acc(hi, lo, o.x, o.x);
+      eng_acc(hi, lo, o.y, o.y);
+    }
+    double nn = (double)hi + (double)lo;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nn += __shfl_down_sync(0xffffffffu, nn, o);
+    if (lane == 0) part[it] = nn;
+    return;
+  }
+  if (lane == 0) part[it] = 0.0;
+  if (n.mode == kModeReplay && k + 1 < n.steps) {
+    const float2* v = s.buf[(k + 1) % 3] + r * Dd;
+    float2* w = s.buf[(k + 2) % 3] + r * Dd;
+    float2* xa = s.xacc + r * Dd;
+    const float a = (float)__ldcg(&s.alpha[k]), ib = (float)(1.0 / __ldcg(&s.beta[k]));
+    const float y = (float)s.yk[k + 1];
+    for (int64_t c = lane; c < Dd; c += 32) {
+      float2 o = w[c];
+      const float2 xv = v[c];
+      o.x = (o.x - a * xv.x) * ib;
+      o.y = (o.y - a * xv.y) * ib;
+      w[c] = o;
+      float2 acc = xa[c];
+      acc.x = fmaf(y, o.x, acc.x);
+      acc.y = fmaf(y, o.y, acc.y);
+      xa[c] = acc;
+    }
+  }
+}
+
+// Phase E, one row (warp-level): k_eng_normalize.
+__device__ void p_normalize_row(const SlotDesc& s, const SlotNow& n, int64_t r) {
+  const int lane = threadIdx.x & 31;
+  const int k = n.k;
+  if (!(n.mode == kModeLanczos && k < n.kmax)) return;
+  const double b = __ldcg(&s.beta[k]);
+  if (!(b > kTol)) return;
+  const int64_t Dd = s.Dd;
+  float2* w = s.buf[(k + 2) % 3] + r * Dd;
+  const float ib = (float)(1.0 / b);
+  int64_t c = lane;
+  for (; c + 96 < Dd; c += 128) {
+    float2 o[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = w[c + 32 * q];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) w[c + 32 * q] = make_float2(o[q].x * ib, o[q].y * ib);
+  }
+  for (; c < Dd; c += 32) {
+    float2 o = w[c];
+    o.x *= ib;
+    o.y *= ib;
+    w[c] = o;
+  }
+}
+
+// Phase F, one request: k_eng_advance.
+__device__ void p_advance(SlotDesc& s) {
+  const SlotNow n = slot_now(s);
+  const int k = n.k;
+  if (n.mode == kModeLanczos && k < n.kmax) {
+    s.steps = k + 1;
+    s.k = k + 1;
+    if (!(__ldcg(&s.beta[k]) > kTol) || k + 1 >= n.kmax) s.mode = kModeIdle;
+  } else if (n.mode == kModeReplay && k + 1 < n.steps) {
+    s.k = k + 1;
+    if (k + 2 >= n.steps) s.mode = kModeIdle;
+  } else if (n.mode == kModeReplay) {
+    s.mode = kModeIdle;
+  } else if (n.mode == kModeCheb && k < n.kmax) {
+    s.k = k + 1;
+    s.steps = k + 1;
+    if (k + 1 >= n.kmax) s.mode = kModeIdle;
+  }
+}
+
+__global__ void __launch_bounds__(kEngPWarps * 32)
+k_eng_persistent(EngPersistArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double red[kEngPWarps][2];
+  __shared__ double sred[kEngPWarps * 32], sred2[kEngPWarps * 32];
+  const int warp = threadIdx.x >> 5;
+  float2* srow = reinterpret_cast<float2*>(smem);
+  uint32_t* s_up = reinterpret_cast<uint32_t*>(smem + sizeof(float2) * (a.row_cols + kSlicedPads));
+  float2* wrow = reinterpret_cast<float2*>(smem) + (size_t)warp * kEngWarpRowCols;
+  const int gw = blockIdx.x * kEngPWarps + warp, nw = gridDim.x * kEngPWarps;
+  for (int step = 0; step < a.steps; ++step) {
+    // A: apply
+    for (int it = blockIdx.x; it < a.n_rows; it += gridDim.x) {
+      const int2 item = a.items_rows[it];
+      const SlotDesc& s = a.slots[item.x];
+      p_apply_row(s, slot_now(s), item.y, s.item0 + item.y, a.part, a.part2, srow, s_up, red);
+    }
+    __syncthreads();  // the row items' shared memory becomes the warps' rows
+    for (int it = gw; it < a.n_warp; it += nw) {
+      const int2 item = a.items_warp[it];
+      const SlotDesc& s = a.slots[item.x];
+      p_apply_warp_row(s, slot_now(s), item.y, s.item0 + item.y, a.part, a.part2, wrow);
+    }
+    if (a.apply_only) return;
+    if (!eng_grid_sync(a.grid, a.budget)) return;
+    // B: alpha
+    for (int si = blockIdx.x; si < a.n_slots; si += gridDim.x)
+      p_seg_reduce(a.slots[si], a.part, a.part2, 0, sred, sred2);
+    if (!eng_grid_sync(a.grid, a.budget)) return;
+    // C: update (and the replay accumulation)
+    for (int it = gw; it < a.n_items; it += nw) {
+      const int2 item = a.items[it];
+      const SlotDesc& s = a.slots[item.x];
+      p_update_row(s, slot_now(s), item.y, it, a.part);
+    }
+    if (!eng_grid_sync(a.grid, a.budget)) return;
+    // D: beta
+    for (int si = blockIdx.x; si < a.n_slots; si += gridDim.x)
+      p_seg_reduce(a.slots[si], a.part, a.part2, 1, sred, sred2);
+    if (!eng_grid_sync(a.grid, a.budget)) return;
+    // E: normalise
+    for (int it = gw; it < a.n_items; it += nw) {
+      const int2 item = a.items[it];
+      const SlotDesc& s = a.slots[item.x];
+      p_normalize_row(s, slot_now(s), item.y);
+    }
+    if (!eng_grid_sync(a.grid, a.budget)) return;
+    // F: advance
+    for (int si = blockIdx.x * blockDim.x + threadIdx.x; si < a.n_slots;
+         si += gridDim.x * blockDim.x)
+      p_advance(a.slots[si]);
+    if (step + 1 < a.steps && !eng_grid_sync(a.grid, a.budget)) return;
+  }
+}
+
 }  // namespace mb
 
 // ===========================================================================
@@ -636,6 +1165,9 @@ struct TableSet {
   const int32_t *up_off = nullptr, *dn_off = nullptr;
   int max_up_deg = 0, max_dn_deg = 0;
   OpView fused{};  // tables of the fused FP64 apply (refinement)
+  // self energies at t = 1 (lattices with a size-1 dimension): per up state,
+  // per down state; empty otherwise
+  std::vector<double> self_up1, self_dn1;
   int64_t bytes = 0;
   int refs = 0;
 };
@@ -663,6 +1195,7 @@ struct EngineSlot {
   int refine = 1;
   std::unique_ptr<EngBuf> vecs;   // 4 vectors: buf0..2, xacc (complex64)
   std::unique_ptr<EngBuf> scal;   // alpha, beta, yk (double x kEngMaxK each)
+  std::unique_ptr<EngBuf> selfe;  // self energies times t, float: [Du] up, [Dd] down (or none)
   int64_t dim = 0, Du = 0, Dd = 0;
   int64_t bytes = 0;
   int phase = 0;                  // 0 pass one, 1 replay, 2 done, 10 DOS bounds, 11 DOS Chebyshev
@@ -708,6 +1241,19 @@ struct mb_engine_s {
   std::vector<std::pair<mb::OpView, mb::EngFusedArgs>> fused;
   std::vector<std::unique_ptr<mb::EngBuf>> fused_scratch;
   cudaStream_t st = nullptr;
+  // The persistent step (k_eng_persistent, cooperative launch): on by
+  // default; rows of at least p_row_min_cols columns (and every row of a
+  // sector of fused_min states or more) are applied block per row, the others
+  // warp per row; p_ctas_per_sm CTAs per SM (0: as many as fit).
+  bool persistent = true;
+  int p_row_min_cols = 256;
+  int p_ctas_per_sm = 0;
+  int p_grid = 1;
+  int p_bps = 1, p_sms = 1;  // co-resident blocks per SM of the last launch shape, SMs
+  size_t p_smem = 0;
+  long long wait_budget = 1LL << 32;  // clock64 cycles one barrier wait may take
+  std::unique_ptr<mb::EngBuf> d_grid;  // barrier state and status (mb::EngGrid)
+  bool broken = false;                 // a barrier wait ran out: requests are lost
   // ids retired since the last mb_engine_completed call
   std::vector<int64_t> newly_done;
   // step statistics: steps run, wall time of the step calls, device time of
@@ -746,10 +1292,14 @@ std::shared_ptr<TableSet> get_tables(mb_engine_s* e, const mb_sector_desc& d) {
   ts->model = *m;
   mb_basis_destroy(b);
   mb_model_destroy(m);
-  for (int v : ts->model.self_mult)
-    MB_REQUIRE(!v, MB_ERR_INVALID_ARG, "the engine needs lattices without size-1 dimensions");
   const HopTable tu = build_hop_table(ts->basis.up, ts->model);
   const HopTable td = build_hop_table(ts->basis.down, ts->model);
+  // a size-1 dimension: hopping(i, i) self bonds, a diagonal term per spin
+  // (HubbardModel2D/3D with a size-1 side, hubbard_model.h:61-129)
+  if (tu.has_self || td.has_self) {
+    ts->self_up1 = tu.has_self ? tu.self_energy : std::vector<double>((size_t)ts->basis.up.D, 0.0);
+    ts->self_dn1 = td.has_self ? td.self_energy : std::vector<double>((size_t)ts->basis.down.D, 0.0);
+  }
   ts->up_mask = tupload(*ts, ts->basis.up.masks);
   ts->dn_mask = tupload(*ts, ts->basis.down.masks);
   ts->up_off = tupload(*ts, tu.off);
@@ -776,6 +1326,18 @@ std::shared_ptr<TableSet> get_tables(mb_engine_s* e, const mb_sector_desc& d) {
 int64_t slot_bytes(int64_t dim) { return 4 * 8 * dim + 3 * 8 * kEngMaxK; }
 
 // The fused-apply view of a slot's sector (tables shared by its TableSet).
+// The slot's self energies (t times the sector's t = 1 values) as float.
+void upload_self_energies(EngineSlot& s) {
+  const TableSet& ts = *s.tables;
+  if (ts.self_up1.empty()) return;
+  std::vector<float> h;
+  h.reserve(ts.self_up1.size() + ts.self_dn1.size());
+  for (double x : ts.self_up1) h.push_back((float)(s.t * x));
+  for (double x : ts.self_dn1) h.push_back((float)(s.t * x));
+  s.selfe = std::make_unique<EngBuf>(sizeof(float) * h.size());
+  MB_CUDA(cudaMemcpy(s.selfe->p, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice));
+}
+
 OpView slot_view(const EngineSlot& s) {
   const TableSet& ts = *s.tables;
   OpView v = ts.fused;
@@ -847,7 +1409,20 @@ void rebuild(mb_engine_s* e) {
     d.up_lpos = ts.fused.up_lpos;
     d.dn_sell = ts.fused.dn_sell;
     d.dn_sgrp = ts.fused.dn_sgrp;
-    if (!d.fused) {
+    d.self_up = s.selfe ? (const float*)s.selfe->p : nullptr;
+    d.self_dn = s.selfe ? (const float*)s.selfe->p + s.Du : nullptr;
+    if (e->persistent) {
+      // the persistent step applies a sector's rows block per row when they
+      // are wide (or the sector is large), else warp per row
+      const bool rows = d.fused || s.Dd >= e->p_row_min_cols;
+      auto& list = rows ? items_rows : items_warp;
+      for (int64_t r = 0; r < s.Du; ++r) list.push_back(make_int2((int)e->h_slots.size(), (int)r));
+      if (rows) {
+        e->row_cols = std::max(e->row_cols, (int)s.Dd);
+        max_list = std::max(max_list, ts.fused.max_up_list);
+      }
+      d.fused = 0;
+    } else if (!d.fused) {
       const bool rows = s.Dd >= kEngRowMinCols;
       auto& list = rows ? items_rows : items_warp;
       for (int64_t r = 0; r < s.Du; ++r) list.push_back(make_int2((int)e->h_slots.size(), (int)r));
@@ -891,6 +1466,8 @@ void rebuild(mb_engine_s* e) {
     a.steps = &dsl[i].steps;
     a.beta = d.beta;
     a.ufold = dsl[i].ufold;
+    a.self_up = d.self_up;
+    a.self_dn = d.self_dn;
     for (int q = 0; q < 3; ++q) a.buf[q] = d.buf[q];
     a.t = d.t;
     a.scale = d.scale;
@@ -919,7 +1496,30 @@ void rebuild(mb_engine_s* e) {
   if (!items_warp.empty())
     MB_CUDA(cudaMemcpyAsync(e->d_items_warp->p, items_warp.data(),
                             sizeof(int2) * items_warp.size(), cudaMemcpyHostToDevice, e->st));
-  if (!items_rows.empty()) {
+  if (e->persistent) {
+    if (!items_rows.empty())
+      MB_CUDA(cudaMemcpyAsync(e->d_items_rows->p, items_rows.data(),
+                              sizeof(int2) * items_rows.size(), cudaMemcpyHostToDevice, e->st));
+    // launch shape, set outside any capture: the staged row and its up list,
+    // or the warps' rows, in dynamic shared memory; co-resident blocks
+    const size_t rows_smem = sizeof(float2) * (size_t)(e->row_cols + kSlicedPads) +
+                             sizeof(uint32_t) * (size_t)((max_list + 3) & ~3);
+    const size_t warps_smem = sizeof(float2) * (size_t)kEngPWarps * kEngWarpRowCols;
+    e->p_smem = std::max(rows_smem, warps_smem);
+    MB_CUDA(cudaFuncSetAttribute(k_eng_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)e->p_smem));
+    int bps = 0, sms = 0, dev = 0;
+    MB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_eng_persistent,
+                                                          kEngPWarps * 32, e->p_smem));
+    MB_REQUIRE(bps >= 1, MB_ERR_CAPACITY, "the persistent engine step does not fit on an SM");
+    MB_CUDA(cudaGetDevice(&dev));
+    MB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    e->p_bps = bps;
+    e->p_sms = sms;
+    const int per_sm = e->p_ctas_per_sm > 0 ? std::min(e->p_ctas_per_sm, bps) : bps;
+    e->p_grid = std::max(1, per_sm * sms);
+    if (!e->d_grid) e->d_grid = std::make_unique<EngBuf>(sizeof(EngGrid));
+  } else if (!items_rows.empty()) {
     MB_CUDA(cudaMemcpyAsync(e->d_items_rows->p, items_rows.data(),
                             sizeof(int2) * items_rows.size(), cudaMemcpyHostToDevice, e->st));
     // launch shape, set outside any capture: shared memory and resident blocks
@@ -989,7 +1589,59 @@ void step_kernels(mb_engine_s* e) {
   k_eng_advance<<<(ns + 255) / 256, 256, 0, e->st>>>(dsm, ns);
 }
 
+// The persistent step: the barrier state cleared, then one cooperative
+// launch of `steps` engine steps (graph-capturable).
+void launch_persistent(mb_engine_s* e, int steps, bool apply_only = false) {
+  EngPersistArgs a{};
+  a.slots = (SlotDesc*)e->d_slots->p;
+  a.n_slots = (int)e->h_slots.size();
+  a.items = (const int2*)e->d_items->p;
+  a.n_items = e->n_items;
+  a.items_rows = (const int2*)e->d_items_rows->p;
+  a.n_rows = e->n_rows;
+  a.items_warp = (const int2*)e->d_items_warp->p;
+  a.n_warp = e->n_warp;
+  a.part = (double*)e->d_part->p;
+  a.part2 = a.part + e->n_items;
+  a.row_cols = e->row_cols;
+  a.steps = steps;
+  a.apply_only = apply_only ? 1 : 0;
+  a.grid = (EngGrid*)e->d_grid->p;
+  a.budget = e->wait_budget;
+  MB_CUDA(cudaMemsetAsync(e->d_grid->p, 0, sizeof(EngGrid), e->st));
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)e->p_grid);
+  cfg.blockDim = dim3(kEngPWarps * 32);
+  cfg.dynamicSmemBytes = e->p_smem;
+  cfg.stream = e->st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  MB_CUDA(cudaLaunchKernelEx(&cfg, k_eng_persistent, a));
+}
+
+// MB_ERR_TIMEOUT once a barrier wait of the persistent step ran out (the
+// engine's requests are then lost: a step stopped part-way).
+void check_grid(mb_engine_s* e) {
+  if (!e->persistent || !e->d_grid) return;
+  EngGrid g{};
+  MB_CUDA(cudaMemcpyAsync(&g, e->d_grid->p, sizeof(EngGrid), cudaMemcpyDeviceToHost, e->st));
+  MB_CUDA(cudaStreamSynchronize(e->st));
+  if (g.status != 0) {
+    e->broken = true;
+    throw Error(MB_ERR_TIMEOUT,
+                "a grid barrier of the persistent engine step waited past its budget; "
+                "the engine's requests are lost (destroy the engine)");
+  }
+}
+
 void launch_step(mb_engine_s* e) {
+  if (e->persistent) {
+    launch_persistent(e, 1);
+    return;
+  }
   switch (e->warps) {
     case 2: step_kernels<2>(e); break;
     case 4: step_kernels<4>(e); break;
@@ -1054,6 +1706,17 @@ double rayleigh_fp64(mb_engine_s* e, EngineSlot& s, const SlotDesc& d) {
   EngBuf duf(sizeof(double) * uf.size());
   MB_CUDA(cudaMemcpy(duf.p, uf.data(), sizeof(double) * uf.size(), cudaMemcpyHostToDevice));
   v.u_fold = (const double*)duf.p;
+  std::unique_ptr<EngBuf> dself;
+  v.self_up = v.self_dn = nullptr;
+  if (!ts.self_up1.empty()) {
+    std::vector<double> h(ts.self_up1);
+    h.insert(h.end(), ts.self_dn1.begin(), ts.self_dn1.end());
+    for (double& x : h) x *= s.t;
+    dself = std::make_unique<EngBuf>(sizeof(double) * h.size());
+    MB_CUDA(cudaMemcpy(dself->p, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+    v.self_up = (const double*)dself->p;
+    v.self_dn = (const double*)dself->p + s.Du;
+  }
   EngBuf xd(16 * (size_t)s.dim);
   k_f32_to_f64<<<256, 256, 0, e->st>>>(d.xacc, (double2*)xd.p, s.dim);
   // Rayleigh-Ritz on span{x, Hx, H^2 x} in FP64 (first step: <x,Hx>/<x,x>)
@@ -1127,6 +1790,7 @@ void dos_transition(mb_engine_s* e, EngineSlot& s, SlotDesc& d, bool& changed) {
 
 // Host bookkeeping after a step: convergence, replay, refinement, retirement.
 void after_step(mb_engine_s* e) {
+  check_grid(e);
   fetch_slots(e);
   bool changed = false;
   for (size_t i = 0; i < e->slots.size(); ++i) {
@@ -1252,6 +1916,7 @@ int mb_engine_submit_ground_state(mb_engine_t eng, const mb_sector_desc* desc, u
   return guard([&] {
     auto* e = (mb_engine_s*)eng;
     MB_REQUIRE(e && desc && request_id, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(!e->broken, MB_ERR_TIMEOUT, "the engine stopped after a barrier timeout");
     MB_REQUIRE(kmax >= 1 && kmax <= kEngMaxK, MB_ERR_INVALID_ARG, "kmax must be in [1, 512]");
     MB_REQUIRE(desc->ndim >= 1 && desc->ndim <= 3, MB_ERR_INVALID_ARG, "ndim must be 1..3");
     MB_REQUIRE(!(desc->t * desc->t < kTol * kTol), MB_ERR_INVALID_ARG, "t must be non-zero");
@@ -1274,6 +1939,7 @@ int mb_engine_submit_ground_state(mb_engine_t eng, const mb_sector_desc* desc, u
     s->bytes = need;
     s->vecs = std::make_unique<EngBuf>(4 * 8 * (size_t)s->dim);
     s->scal = std::make_unique<EngBuf>(3 * 8 * (size_t)kEngMaxK);
+    upload_self_energies(*s);
     s->id = e->next_id++;
     s->t_submit = std::chrono::steady_clock::now();
     float2* base = (float2*)s->vecs->p;
@@ -1291,6 +1957,7 @@ int mb_engine_submit_dos(mb_engine_t eng, const mb_sector_desc* desc, int64_t n_
   return guard([&] {
     auto* e = (mb_engine_s*)eng;
     MB_REQUIRE(e && desc && request_id, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(!e->broken, MB_ERR_TIMEOUT, "the engine stopped after a barrier timeout");
     MB_REQUIRE(n_moments >= 2 && n_moments <= 2 * kEngMaxK, MB_ERR_INVALID_ARG,
                "n_moments must be in [2, 1024]");
     MB_REQUIRE(n_probes >= 1, MB_ERR_INVALID_ARG, "n_probes must be >= 1");
@@ -1318,6 +1985,7 @@ int mb_engine_submit_dos(mb_engine_t eng, const mb_sector_desc* desc, int64_t n_
     s->bytes = need;
     s->vecs = std::make_unique<EngBuf>(4 * 8 * (size_t)s->dim);
     s->scal = std::make_unique<EngBuf>(3 * 8 * (size_t)kEngMaxK);
+    upload_self_energies(*s);
     s->id = e->next_id++;
     s->t_submit = std::chrono::steady_clock::now();
     s->phase = 10;
@@ -1354,6 +2022,7 @@ int mb_engine_step(mb_engine_t eng, int n_steps, int* n_active) {
   return guard([&] {
     auto* e = (mb_engine_s*)eng;
     MB_REQUIRE(e && n_steps >= 0, MB_ERR_INVALID_ARG, "bad argument");
+    MB_REQUIRE(!e->broken, MB_ERR_TIMEOUT, "the engine stopped after a barrier timeout");
     for (int i = 0; i < n_steps && !e->slots.empty(); ++i) {
       const auto t0 = std::chrono::steady_clock::now();
       rebuild(e);
@@ -1446,9 +2115,32 @@ int mb_engine_step_fixed(mb_engine_t eng, int n_steps, int use_graph, int* n_act
   return guard([&] {
     auto* e = (mb_engine_s*)eng;
     MB_REQUIRE(e && n_steps >= 0, MB_ERR_INVALID_ARG, "bad argument");
+    MB_REQUIRE(!e->broken, MB_ERR_TIMEOUT, "the engine stopped after a barrier timeout");
     if (!e->slots.empty() && n_steps > 0) {
       rebuild(e);
-      if (use_graph) {
+      if (e->persistent) {
+        // all n steps in one persistent launch, captured as a graph or not
+        if (use_graph) {
+          cudaGraph_t g = nullptr;
+          cudaGraphExec_t ge = nullptr;
+          MB_CUDA(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
+          try {
+            launch_persistent(e, n_steps);
+          } catch (...) {
+            cudaStreamEndCapture(e->st, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+          }
+          MB_CUDA(cudaStreamEndCapture(e->st, &g));
+          MB_CUDA(cudaGraphInstantiate(&ge, g, 0));
+          MB_CUDA(cudaGraphLaunch(ge, e->st));
+          MB_CUDA(cudaStreamSynchronize(e->st));
+          cudaGraphExecDestroy(ge);
+          cudaGraphDestroy(g);
+        } else {
+          launch_persistent(e, n_steps);
+        }
+      } else if (use_graph) {
         cudaGraph_t g = nullptr;
         cudaGraphExec_t ge = nullptr;
         MB_CUDA(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
@@ -1471,12 +2163,112 @@ int mb_engine_step_fixed(mb_engine_t eng, int n_steps, int use_graph, int* n_act
 // Autotuner: times the grouped apply kernel at 2, 4, 8 and 16 warps per
 // block on the current set of requests and keeps the fastest.  The timed
 // launches write only the w buffers, which the next real step overwrites.
+int mb_engine_set_persistent(mb_engine_t eng, int on) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e, MB_ERR_INVALID_ARG, "NULL engine");
+    MB_REQUIRE(!e->broken, MB_ERR_TIMEOUT, "the engine stopped after a barrier timeout");
+    e->persistent = on != 0;
+    e->dirty = true;  // new work lists; every request keeps its progress
+    rebuild(e);
+  });
+}
+
+int mb_engine_set_wait_budget(mb_engine_t eng, int64_t cycles) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e && cycles >= 0, MB_ERR_INVALID_ARG, "NULL engine or negative budget");
+    e->wait_budget = cycles;
+  });
+}
+
+int mb_engine_get_shape(mb_engine_t eng, mb_engine_shape* shape) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e && shape, MB_ERR_INVALID_ARG, "NULL argument");
+    *shape = mb_engine_shape{};
+    shape->persistent = e->persistent ? 1 : 0;
+    shape->row_min_cols = e->p_row_min_cols;
+    shape->ctas_per_sm = e->p_ctas_per_sm;
+    shape->grid = e->p_grid;
+    shape->warps = e->warps;
+  });
+}
+
+int mb_engine_set_shape(mb_engine_t eng, const mb_engine_shape* shape) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e && shape, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(!e->broken, MB_ERR_TIMEOUT, "the engine stopped after a barrier timeout");
+    MB_REQUIRE(shape->row_min_cols >= 32 && shape->row_min_cols <= 1 << 20, MB_ERR_INVALID_ARG,
+               "row_min_cols must be in [32, 2^20]");
+    MB_REQUIRE(shape->ctas_per_sm >= 0 && shape->ctas_per_sm <= 32, MB_ERR_INVALID_ARG,
+               "ctas_per_sm must be in [0, 32]");
+    MB_REQUIRE(shape->warps == 2 || shape->warps == 4 || shape->warps == 8 || shape->warps == 16,
+               MB_ERR_INVALID_ARG, "warps must be 2, 4, 8 or 16");
+    e->persistent = shape->persistent != 0;
+    e->p_row_min_cols = std::min(shape->row_min_cols, kEngWarpRowCols);
+    e->p_ctas_per_sm = shape->ctas_per_sm;
+    e->warps = shape->warps;
+    e->dirty = true;
+    rebuild(e);
+  });
+}
+
 int mb_engine_autotune(mb_engine_t eng, int* chosen, double* ms) {
   return guard([&] {
     auto* e = (mb_engine_s*)eng;
     MB_REQUIRE(e, MB_ERR_INVALID_ARG, "NULL engine");
+    MB_REQUIRE(!e->broken, MB_ERR_TIMEOUT, "the engine stopped after a barrier timeout");
     if (e->slots.empty()) {
       if (chosen) *chosen = e->warps;
+      return;
+    }
+    if (e->persistent) {
+      // the persistent step's shapes, timed on the live requests with
+      // apply-only launches (they write only w and the partials, which the
+      // next step rewrites): rows below row_min_cols columns warp per row,
+      // ctas_per_sm co-resident blocks (0: all that fit)
+      cudaEvent_t a, b;
+      MB_CUDA(cudaEventCreate(&a));
+      MB_CUDA(cudaEventCreate(&b));
+      double best = 1e300;
+      int best_cols = e->p_row_min_cols, best_ctas = e->p_ctas_per_sm;
+      try {
+        for (int cols : {64, 128, 256}) {
+          e->p_row_min_cols = cols;
+          e->dirty = true;
+          rebuild(e);  // new work lists; the block count below needs none
+          for (int ctas : {0, 2, 1}) {
+            e->p_ctas_per_sm = ctas;
+            e->p_grid = std::max(1, (ctas > 0 ? std::min(ctas, e->p_bps) : e->p_bps) * e->p_sms);
+            launch_persistent(e, 1, true);
+            MB_CUDA(cudaEventRecord(a, e->st));
+            for (int rep = 0; rep < 3; ++rep) launch_persistent(e, 1, true);
+            MB_CUDA(cudaEventRecord(b, e->st));
+            MB_CUDA(cudaEventSynchronize(b));
+            float t = 0.f;
+            MB_CUDA(cudaEventElapsedTime(&t, a, b));
+            if (t < best) {
+              best = t;
+              best_cols = cols;
+              best_ctas = ctas;
+            }
+          }
+        }
+      } catch (...) {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        throw;
+      }
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      e->p_row_min_cols = best_cols;
+      e->p_ctas_per_sm = best_ctas;
+      e->dirty = true;
+      rebuild(e);
+      if (chosen) *chosen = e->warps;
+      if (ms) *ms = best / 3.0;
       return;
     }
     rebuild(e);

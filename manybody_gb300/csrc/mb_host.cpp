@@ -280,6 +280,31 @@ SlicedTable sliced_table(const HopTable& t, int64_t D) {
   return s;
 }
 
+SlicedTable16 sliced_table16(const SlicedTable& s, int64_t D) {
+  MB_REQUIRE(D <= kSliced16MaxD, MB_ERR_CAPACITY, "sector too large for 16-bit table entries");
+  SlicedTable16 h;
+  const int64_t ng = (D + 31) / 32;
+  h.grp.resize((size_t)(2 * ng));
+  for (int64_t g = 0; g < ng; ++g) {
+    const size_t base = (size_t)s.grp[(size_t)(2 * g)];
+    const int k = s.grp[(size_t)(2 * g + 1)];
+    const int k8 = (k + 7) & ~7;
+    const size_t b16 = h.ent.size();
+    h.grp[(size_t)(2 * g)] = (int32_t)b16;
+    h.grp[(size_t)(2 * g + 1)] = k;
+    // the slots past k in the last word are never read; they point at a zero
+    h.ent.resize(b16 + (size_t)32 * k8, (uint16_t)D);
+    for (int j = 0; j < k; ++j)
+      for (int l = 0; l < 32; ++l) {
+        const uint32_t w = s.ent[base + 128 * (size_t)(j >> 2) + 4 * (size_t)l + (size_t)(j & 3)];
+        h.ent[b16 + 256 * (size_t)(j >> 3) + 8 * (size_t)l + (size_t)(j & 7)] =
+            (uint16_t)((w & 0x7FFFu) | ((w >> 31) << 15));
+      }
+  }
+  if (h.ent.empty()) h.ent.push_back((uint16_t)D);
+  return h;
+}
+
 // Largest eigenvalue of the symmetric tridiagonal T_m (diagonal a, off-
 // diagonal b) by bisection on the Sturm count (number of eigenvalues below x
 // = number of negative pivots of the LDL^T factorisation of T - x).
@@ -341,6 +366,34 @@ void fill_fused_tables(OpView& v, const HopTable& tu, const HopTable& td, int64_
   v.dn_sell = put(sd.ent);
   v.dn_sgrp = put(sd.grp);
   v.dn_nneg = put(sd.nneg);
+  if (Dd <= kSliced16MaxD) {
+    const SlicedTable16 h = sliced_table16(sd, Dd);
+    v.dn_sell16 = put(h.ent);
+    v.dn_sgrp16 = put(h.grp);
+  }
+  if (Du == Dd && tu.off == td.off && tu.ent == td.ent) {
+    v.up_sell = v.dn_sell;
+    v.up_sgrp = v.dn_sgrp;
+    v.up_nneg = v.dn_nneg;
+    v.up_sell16 = v.dn_sell16;
+    v.up_sgrp16 = v.dn_sgrp16;
+  } else {
+    const SlicedTable su = sliced_table(tu, Du);
+    v.up_sell = put(su.ent);
+    v.up_sgrp = put(su.grp);
+    v.up_nneg = put(su.nneg);
+    if (Du <= kSliced16MaxD) {
+      const SlicedTable16 h = sliced_table16(su, Du);
+      v.up_sell16 = put(h.ent);
+      v.up_sgrp16 = put(h.grp);
+    }
+  }
+  v.row_split = 1;
+  v.table_bits = 32;
+  v.up_prefetch = 0;
+  v.table_stage = 0;
+  v.dn_max_words = 0;
+  for (size_t g = 1; g < sd.grp.size(); g += 2) v.dn_max_words = std::max(v.dn_max_words, (sd.grp[g] + 3) / 4);
 }
 
 std::vector<double> u_fold_table(double u, bool has_u, int L) {

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <condition_variable>
 #include <cstdio>
 #include <functional>
 #include <map>
@@ -272,6 +273,14 @@ struct SlicedTable {
   std::vector<uint8_t> nneg;  // [D] negative entries per state
 };
 SlicedTable sliced_table(const HopTable& t, int64_t D);
+// The same table with 16-bit entries (index | negative << 15; D + kSlicedPads
+// must stay below 2^15), a lane's slots 8i..8i+7 in one 16-byte word.
+struct SlicedTable16 {
+  std::vector<uint16_t> ent;
+  std::vector<int32_t> grp;
+};
+constexpr int64_t kSliced16MaxD = (int64_t(1) << 15) - kSlicedPads;
+SlicedTable16 sliced_table16(const SlicedTable& s, int64_t D);
 
 // Left fold U + U + ... (k terms), the order-independent value the reference
 // accumulates for k doubly occupied sites (matrix_elements.h:85-96).
@@ -304,6 +313,33 @@ struct OpView {
   const uint32_t* dn_sell;
   const int32_t* dn_sgrp;
   const uint8_t* dn_nneg;  // per down state: number of negative hops (doubled twice)
+  // The same sliced table for the up sector (the column pass of the two-pass
+  // applies gathers up hops from a staged column); shares the down table's
+  // memory when the two sectors are the same.
+  const uint32_t* up_sell;
+  const int32_t* up_sgrp;
+  const uint8_t* up_nneg;
+  // 16-bit copies of the two sliced tables (sectors below 32760 states; else
+  // nullptr): entry = index | negative << 15, a lane's slots 8i..8i+7 in one
+  // 16-byte word, group g at sgrp16[2g] with sgrp16[2g+1] slots.
+  const uint16_t* dn_sell16;
+  const int32_t* dn_sgrp16;
+  const uint16_t* up_sell16;
+  const int32_t* up_sgrp16;
+  // Kernel shape of the fused applies (mb_apply_shape): CTAs sharing one row
+  // (each stages the row and takes every split-th column group) and the
+  // sliced-table entry width (32 or 16 bits).
+  int row_split;
+  int table_bits;
+  // 1: before a column group, each warp prefetches the up-hop lines of its
+  // next group into L2 (prefetch.global.L2)
+  int up_prefetch;
+  // 1: each warp copies its next column group's down-table words into a
+  // warp-private shared buffer (cp.async) while it finishes the current one
+  // (MB_PREC_Q64 row-staged applies where it fits); dn_max_words = the most
+  // 16-byte words (four 32-bit slots each) of one group.
+  int table_stage;
+  int dn_max_words;
   int max_up_list;
   // Operators made from a sparse matrix instead of a lattice (mb_op_create_csr):
   // CSR on the device, values complex128 (and complex64 copies for MB_PREC_F32).
@@ -341,6 +377,8 @@ struct EngFusedArgs {
   const int* steps;
   const double* beta;   // beta[k - 1] scales v_prev
   const float* ufold;   // [L + 1] U fold of the slot
+  const float* self_up; // self energies of a size-1 dimension (t-scaled), or nullptr
+  const float* self_dn;
   float2* buf[3];       // v_prev = buf[k % 3], v = buf[(k + 1) % 3], w = buf[(k + 2) % 3]
   const float* cheb_a;  // Chebyshev rescaling (H - b) / a of the current probe
   const float* cheb_b;
@@ -377,7 +415,8 @@ struct mb_op_s {
   int32_t* perm = nullptr;         // tensor -> reference index (lazy)
   int32_t* iperm = nullptr;        // reference -> tensor index (lazy)
   std::mutex mu;
-  std::mutex host_mu;  // host-buffer calls: one at a time (shared staging, stream 0)
+  std::mutex host_mu;  // host-buffer calls: the lane pool and the row groups
+  std::mutex host_link_mu;  // host-buffer calls on page-locked vectors take turns
   // Pipelined host-buffer apply (lattice operators, reference order): the
   // rows in groups by the first reference index among their states, each
   // group in the row schedule's order, so that once groups 0..g are applied
@@ -386,7 +425,23 @@ struct mb_op_s {
   int32_t* host_sched = nullptr;
   std::vector<int64_t> host_row0;
   std::vector<int64_t> host_ready;
-  cudaStream_t host_streams[2] = {nullptr, nullptr};
+  // Host-buffer calls run on lanes: a lane is a pair of non-blocking streams
+  // (compute, copy) whose compute stream keys its own staging and scratch
+  // buffers, so calls from several host threads overlap.  A call takes an
+  // idle lane or makes one (at most kMaxHostLanes; more callers wait).
+  struct HostLane {
+    cudaStream_t comp = nullptr, copy = nullptr;
+    // two page-locked bounce buffers for pageable host vectors (made on first
+    // use): the calling thread copies one chunk while the copy engine moves
+    // the other, so pageable transfers of concurrent calls do not queue
+    // behind each other in the driver's own staging
+    void* bounce[2] = {nullptr, nullptr};
+    cudaEvent_t bev[2] = {nullptr, nullptr};
+  };
+  static constexpr int kMaxHostLanes = 8;
+  std::vector<std::unique_ptr<HostLane>> host_lanes;
+  std::vector<HostLane*> host_idle;
+  std::condition_variable host_cv;
   struct Scratch {
     void* a = nullptr;  // tensor-order copies for reference-order calls
     void* b = nullptr;
@@ -405,6 +460,14 @@ struct mb_op_s {
     void* prm = nullptr;   // QParams
     int* ints = nullptr;   // [max exp, Ex, unused, unused]
   };
+  // per stream: the up-hop sums of the two-pass apply (dim elements)
+  std::map<cudaStream_t, void*> ups_scratch;
+  // Kernel shape of the lattice apply (mb_op_set_apply_shape / the autotuner):
+  // 1 = one pass, 2 = column pass for the up hops, then the row pass.
+  int apply_passes = 1;
+  // (lattice, N_up, N_down, precision) of a lattice operator: the autotuner's
+  // cache key ("" for operators it does not tune)
+  std::string tune_key;
   std::map<cudaStream_t, QScratch> qscratch;
 };
 
@@ -480,7 +543,20 @@ void ensure_host_groups(mb_op_s* op);
 // gather(i0, i1, dst) (reference indices [i0, i1) of the result to dst) on the
 // compute stream; each finished reference range goes from y_stage to y_host on
 // the copy stream while later groups run.  Returns once y_host is written.
-void host_groups_run(mb_op_s* op, size_t elem, void* y_host, void* y_stage,
+// Host <-> device copies of one lane: page-locked host memory by the copy
+// engine directly; pageable memory chunk by chunk through the lane's bounce
+// buffers.  lane_upload calls on_chunk(offset, length, event) once each chunk
+// is queued (event: its transfer done, on the copy stream) and returns once
+// the last chunk is queued; lane_download returns once dst holds the bytes
+// (the copy stream must already wait for their producer).
+bool host_pinned(const void* p);
+void lane_upload(const mb_op_s::HostLane& lane, void* dst_dev, const void* src_host, size_t bytes,
+                 size_t chunk_align,
+                 const std::function<void(size_t, size_t, cudaEvent_t)>& on_chunk);
+void lane_download(const mb_op_s::HostLane& lane, void* dst_host, const void* src_dev,
+                   size_t bytes);
+void host_groups_run(mb_op_s* op, const mb_op_s::HostLane& lane, size_t elem, void* y_host,
+                     void* y_stage,
                      const std::function<void(const OpView&)>& apply_rows,
                      const std::function<void(int64_t, int64_t, void*)>& gather);
 

@@ -125,7 +125,8 @@ static int max_smem_optin() {
 // zero elements past the row), while the up hops read the neighbour rows X[r_up', c] from
 // L2/HBM with coalesced 8/16-byte loads, the row's sign-sorted target list
 // in shared memory (added, then subtracted).  Warp w takes the 32-column
-// groups w, w + 32, ... and prefetches its next group's up-hop lines into L2.
+// groups w, w + 32, ... (with up_prefetch set it first prefetches its next
+// group's up-hop lines into L2).
 // ---------------------------------------------------------------------------
 constexpr int kApplyThreads = 1024;
 // CTAs per SM: complex64 rows are half the size, and two CTAs per SM (32
@@ -181,7 +182,7 @@ __device__ __forceinline__ void apply_rows(
       const int64_t c = (g << 5) + lane;
       const bool live = c < Dd;
       const int64_t cl = live ? c : Dd - 1;
-      if (g + nwarps < ngroups) {
+      if (v.up_prefetch && g + nwarps < ngroups) {
         const int64_t cn = min(((g + nwarps) << 5) + lane, Dd - 1);
         const char* xn = reinterpret_cast<const char*>(x + cn);
         for (int k = 0; k < nu; ++k)
@@ -283,8 +284,8 @@ k_eng_fused(OpView v, EngFusedArgs a) {
     return;  // idle this step: k_eng_fused_place writes zero partials
   }
   apply_rows<float, STAGED, 3>(v, a.buf[(k + 1) % 3], a.buf[(k + 2) % 3], -a.t * sc, sc, shift,
-                               beta, k > 0 ? a.buf[k % 3] : nullptr, a.ufold, nullptr, nullptr,
-                               a.scratch);
+                               beta, k > 0 ? a.buf[k % 3] : nullptr, a.ufold, a.self_up,
+                               a.self_dn, a.scratch);
 }
 
 // The fused slot's block partials into the engine's per-item partial arrays

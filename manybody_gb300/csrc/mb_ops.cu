@@ -13,14 +13,15 @@
 #include <vector>
 
 #include "mb_internal.h"
+#include "mb_q64.h"
 
 namespace mb {
 
 // Q64 hooks (mb_q64_ops.cu)
 void q_op_prepare(mb_op_s* op, const mb_model_s* m, const HopTable& tu, const HopTable& td);
 void q_op_release(mb_op_s* op);
-void q_apply_host_reference(mb_op_s* op, const void* x_host, const void* x_mapped, void* y_host,
-                            void* x_stage, void* y_stage);
+void q_apply_host_reference(mb_op_s* op, const mb_op_s::HostLane& lane, const void* x_host,
+                            const void* x_mapped, void* y_host, void* x_stage, void* y_stage);
 int q_apply_grid(const OpView& v);
 void q_apply_affine(mb_op_s* op, const void* x, void* y, double scale, double shift, double beta,
                     const void* z, int order, cudaStream_t st);
@@ -122,6 +123,10 @@ static void build_op(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m) {
   op->dim = b->dim;
   op->t = m->t;
   op->u = m->u;
+  op->tune_key = "lattice";
+  for (int64_t d : m->dims) op->tune_key += "_" + std::to_string(d);
+  op->tune_key += " n" + std::to_string(b->n_up) + "+" + std::to_string(b->n_down) + " prec" +
+                  std::to_string(op->precision);
   const HopTable tu = build_hop_table(b->up, *m);
   const bool same = b->n_up == b->n_down;
   HopTable td_store;
@@ -198,10 +203,16 @@ static std::vector<int32_t> block_perm(const mb_basis_s& s) {
 }
 
 static void free_op_memory(mb_op_s* op) {
-  for (cudaStream_t& h : op->host_streams) {
-    if (h) cudaStreamDestroy(h);
-    h = nullptr;
+  for (auto& lane : op->host_lanes) {
+    if (lane->comp) cudaStreamDestroy(lane->comp);
+    if (lane->copy) cudaStreamDestroy(lane->copy);
+    for (int b = 0; b < 2; ++b) {
+      if (lane->bounce[b]) cudaFreeHost(lane->bounce[b]);
+      if (lane->bev[b]) cudaEventDestroy(lane->bev[b]);
+    }
   }
+  op->host_lanes.clear();
+  op->host_idle.clear();
   for (auto& kv : op->scratch) {
     for (void* p : {kv.second.a, kv.second.b, kv.second.hx, kv.second.hy})
       if (p) cudaFree(p);
@@ -541,17 +552,77 @@ void ensure_host_groups(mb_op_s* op) {
   MB_CUDA(cudaMalloc(&p, sizeof(int32_t) * (size_t)std::max<int64_t>(Du, 1)));
   op->allocations.push_back(p);
   MB_CUDA(cudaMemcpy(p, order.data(), sizeof(int32_t) * (size_t)Du, cudaMemcpyHostToDevice));
-  for (cudaStream_t& h : op->host_streams)
-    if (!h) MB_CUDA(cudaStreamCreateWithFlags(&h, cudaStreamNonBlocking));
   op->host_row0 = std::move(row0);
   op->host_ready = std::move(ready);
   op->host_sched = (int32_t*)p;
 }
 
-void host_groups_run(mb_op_s* op, size_t elem, void* y_host, void* y_stage,
-                     const std::function<void(const OpView&)>& apply_rows,
+bool host_pinned(const void* p) {
+  cudaPointerAttributes at{};
+  const bool pinned = cudaPointerGetAttributes(&at, p) == cudaSuccess &&
+                      at.type == cudaMemoryTypeHost && at.devicePointer != nullptr;
+  if (!pinned) cudaGetLastError();  // clear a failed query on pageable memory
+  return pinned;
+}
+
+constexpr size_t kBounceBytes = size_t(16) << 20;
+
+static void lane_bounce(const mb_op_s::HostLane& lane_c) {
+  auto& lane = const_cast<mb_op_s::HostLane&>(lane_c);  // the calling thread owns the lane
+  for (int b = 0; b < 2; ++b) {
+    if (!lane.bounce[b]) MB_CUDA(cudaHostAlloc(&lane.bounce[b], kBounceBytes, cudaHostAllocDefault));
+    if (!lane.bev[b]) MB_CUDA(cudaEventCreateWithFlags(&lane.bev[b], cudaEventDisableTiming));
+  }
+}
+
+void lane_upload(const mb_op_s::HostLane& lane, void* dst_dev, const void* src_host, size_t bytes,
+                 size_t chunk_align,
+                 const std::function<void(size_t, size_t, cudaEvent_t)>& on_chunk) {
+  if (bytes == 0) return;
+  lane_bounce(lane);
+  const size_t chunk = kBounceBytes - kBounceBytes % chunk_align;
+  size_t off = 0;
+  for (int c = 0; off < bytes; ++c) {
+    const int b = c & 1;
+    const size_t len = std::min(chunk, bytes - off);
+    // the buffer's previous transfer (two chunks back) is done before refilling it
+    if (c >= 2) MB_CUDA(cudaEventSynchronize(lane.bev[b]));
+    std::memcpy(lane.bounce[b], (const char*)src_host + off, len);
+    MB_CUDA(cudaMemcpyAsync((char*)dst_dev + off, lane.bounce[b], len, cudaMemcpyHostToDevice,
+                            lane.copy));
+    MB_CUDA(cudaEventRecord(lane.bev[b], lane.copy));
+    on_chunk(off, len, lane.bev[b]);
+    off += len;
+  }
+}
+
+void lane_download(const mb_op_s::HostLane& lane, void* dst_host, const void* src_dev,
+                   size_t bytes) {
+  if (bytes == 0) return;
+  lane_bounce(lane);
+  const size_t n = (bytes + kBounceBytes - 1) / kBounceBytes;
+  size_t issued = 0, done = 0;
+  while (done < n) {
+    while (issued < n && issued - done < 2) {
+      const int b = (int)(issued & 1);
+      const size_t off = issued * kBounceBytes, len = std::min(kBounceBytes, bytes - off);
+      MB_CUDA(cudaMemcpyAsync(lane.bounce[b], (const char*)src_dev + off, len,
+                              cudaMemcpyDeviceToHost, lane.copy));
+      MB_CUDA(cudaEventRecord(lane.bev[b], lane.copy));
+      ++issued;
+    }
+    const int b = (int)(done & 1);
+    const size_t off = done * kBounceBytes, len = std::min(kBounceBytes, bytes - off);
+    MB_CUDA(cudaEventSynchronize(lane.bev[b]));
+    std::memcpy((char*)dst_host + off, lane.bounce[b], len);
+    ++done;
+  }
+}
+
+void host_groups_run(mb_op_s* op, const mb_op_s::HostLane& lane, size_t elem, void* y_host,
+                     void* y_stage, const std::function<void(const OpView&)>& apply_rows,
                      const std::function<void(int64_t, int64_t, void*)>& gather) {
-  cudaStream_t comp = op->host_streams[0], copy = op->host_streams[1];
+  cudaStream_t comp = lane.comp, copy = lane.copy;
   const int64_t G = (int64_t)op->host_ready.size();
   Events ev((int)G);
   int64_t done = 0;
@@ -566,15 +637,21 @@ void host_groups_run(mb_op_s* op, size_t elem, void* y_host, void* y_stage,
     done = ready;
   }
   // every compute launch is queued before the first download: a download to
-  // pageable memory returns only when it has finished
+  // pageable memory returns only when it has finished (through the lane's
+  // bounce buffers)
+  const bool pinned = host_pinned(y_host);
   done = 0;
   for (int64_t g = 0; g < G; ++g) {
     const int64_t ready = op->host_ready[(size_t)g];
     if (ready > done) {
       MB_CUDA(cudaStreamWaitEvent(copy, ev[(int)g], 0));
-      MB_CUDA(cudaMemcpyAsync((char*)y_host + elem * (size_t)done,
-                              (const char*)y_stage + elem * (size_t)done,
-                              elem * (size_t)(ready - done), cudaMemcpyDeviceToHost, copy));
+      if (pinned)
+        MB_CUDA(cudaMemcpyAsync((char*)y_host + elem * (size_t)done,
+                                (const char*)y_stage + elem * (size_t)done,
+                                elem * (size_t)(ready - done), cudaMemcpyDeviceToHost, copy));
+      else
+        lane_download(lane, (char*)y_host + elem * (size_t)done,
+                      (const char*)y_stage + elem * (size_t)done, elem * (size_t)(ready - done));
     }
     done = ready;
   }
@@ -1091,6 +1168,228 @@ int mb_op_precision(mb_op_t op, int* precision) {
   });
 }
 
+int mb_op_get_apply_shape(mb_op_t op, mb_apply_shape* shape) {
+  return guard([&] {
+    MB_REQUIRE(op && shape, MB_ERR_INVALID_ARG, "NULL argument");
+    *shape = mb_apply_shape{};
+    shape->passes = op->apply_passes;
+    shape->row_split = std::max(1, op->view.row_split);
+    shape->table_bits = op->view.table_bits == 16 ? 16 : 32;
+    shape->prefetch = op->view.up_prefetch ? 1 : 0;
+    shape->table_stage = op->view.table_stage ? 1 : 0;
+  });
+}
+
+int mb_op_set_apply_shape(mb_op_t op, const mb_apply_shape* shape) {
+  return guard([&] {
+    MB_REQUIRE(op && shape, MB_ERR_INVALID_ARG, "NULL argument");
+    MB_REQUIRE(shape->passes == 1 || shape->passes == 2, MB_ERR_INVALID_ARG,
+               "passes must be 1 or 2");
+    MB_REQUIRE(shape->row_split == 1 || shape->row_split == 2 || shape->row_split == 4,
+               MB_ERR_INVALID_ARG, "row_split must be 1, 2 or 4");
+    MB_REQUIRE(shape->table_bits == 32 || shape->table_bits == 16, MB_ERR_INVALID_ARG,
+               "table_bits must be 32 or 16");
+    MB_REQUIRE(shape->prefetch == 0 || shape->prefetch == 1, MB_ERR_INVALID_ARG,
+               "prefetch must be 0 or 1");
+    MB_REQUIRE(shape->table_stage == 0 || shape->table_stage == 1, MB_ERR_INVALID_ARG,
+               "table_stage must be 0 or 1");
+    const bool lattice = !op->view.csr_row && !op->view.n_blocks && op->view.dn_sell;
+    const bool tuned = shape->passes != 1 || shape->row_split != 1 || shape->table_bits != 32;
+    if (tuned)
+      MB_REQUIRE(op->precision == MB_PREC_Q64 && lattice, MB_ERR_INVALID_ARG,
+                 "passes, row_split and table_bits other than 1, 1, 32 need an MB_PREC_Q64 "
+                 "lattice operator");
+    if (shape->prefetch)
+      MB_REQUIRE(lattice, MB_ERR_INVALID_ARG, "prefetch needs a lattice operator");
+    if (shape->table_stage) {
+      MB_REQUIRE(op->precision == MB_PREC_Q64 && lattice && shape->passes == 1 &&
+                     shape->table_bits == 32,
+                 MB_ERR_INVALID_ARG,
+                 "table_stage needs a one-pass MB_PREC_Q64 lattice apply with 32-bit entries");
+      MB_REQUIRE(q_table_stage_fits(op->view), MB_ERR_CAPACITY,
+                 "the warps' table buffers do not fit beside the staged row");
+    }
+    if (shape->passes == 2)
+      MB_REQUIRE(q_upcol_fits(op->view), MB_ERR_CAPACITY,
+                 "a column of the sector does not fit in shared memory");
+    if (shape->table_bits == 16)
+      MB_REQUIRE(op->view.dn_sell16 && op->view.up_sell16, MB_ERR_CAPACITY,
+                 "16-bit table entries need sectors below 32760 states per spin");
+    std::lock_guard<std::mutex> lk(op->mu);
+    op->apply_passes = shape->passes;
+    op->view.row_split = shape->row_split;
+    op->view.table_bits = shape->table_bits;
+    op->view.up_prefetch = shape->prefetch;
+    op->view.table_stage = shape->table_stage;
+  });
+}
+
+// ---------------------------------------------------------------------------
+// The apply autotuner: every candidate shape of a lattice operator timed on
+// the live GPU (CUDA events, tensor-order device vectors, median of 7 after
+// 2 warm-up applies); the fastest is kept, and cached per (lattice, N_up,
+// N_down, precision) for the process, so later operators of the same sector
+// take it without timing.
+// ---------------------------------------------------------------------------
+static std::mutex g_tune_mu;
+static std::map<std::string, std::pair<mb_apply_shape, double>> g_tune_cache;
+
+static std::vector<mb_apply_shape> tune_candidates(const mb_op_s* op) {
+  std::vector<mb_apply_shape> out;
+  for (int pf = 0; pf <= 1; ++pf) {
+    if (op->precision != MB_PREC_Q64) {
+      mb_apply_shape s{};
+      s.passes = 1;
+      s.row_split = 1;
+      s.table_bits = 32;
+      s.prefetch = pf;
+      out.push_back(s);
+      continue;
+    }
+    for (int passes = 1; passes <= 2; ++passes) {
+      if (passes == 2 && !q_upcol_fits(op->view)) continue;
+      for (int split : {1, 2})
+        for (int tb : {32, 16}) {
+          if (tb == 16 && !(op->view.dn_sell16 && op->view.up_sell16)) continue;
+          if (passes == 2 && pf) continue;  // the row pass of two has no up-hop loads
+          for (int ts = 0; ts <= 1; ++ts) {
+            if (ts && !(passes == 1 && tb == 32 && q_table_stage_fits(op->view))) continue;
+            mb_apply_shape s{};
+            s.passes = passes;
+            s.row_split = split;
+            s.table_bits = tb;
+            s.prefetch = pf;
+            s.table_stage = ts;
+            out.push_back(s);
+          }
+        }
+    }
+  }
+  return out;
+}
+
+}  // extern "C"
+
+namespace mb {
+void q_tune_prepare(mb_op_s* op, void** xq, void** yq, void** prm, cudaStream_t st);
+void q_tune_apply(mb_op_s* op, const void* xq, void* yq, const void* prm, cudaStream_t st);
+}  // namespace mb
+
+extern "C" {
+
+int mb_op_autotune(mb_op_t op, void* stream, mb_apply_shape* chosen, double* best_ms) {
+  return guard([&] {
+    MB_REQUIRE(op, MB_ERR_INVALID_ARG, "NULL operator");
+    cudaStream_t st = (cudaStream_t)stream;
+    mb_apply_shape best{};
+    double best_t = 0.0;
+    bool cached = false;
+    if (!op->tune_key.empty()) {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = g_tune_cache.find(op->tune_key);
+      if (it != g_tune_cache.end()) {
+        best = it->second.first;
+        best_t = it->second.second;
+        cached = true;
+      }
+    }
+    if (!cached && !op->tune_key.empty()) {
+      const auto cands = tune_candidates(op);
+      // device vectors in tensor order: complex128 / complex64, or Q64 mantissas
+      void *x = nullptr, *y = nullptr, *prm = nullptr;
+      std::vector<void*> own;
+      if (op->precision == MB_PREC_Q64) {
+        q_tune_prepare(op, &x, &y, &prm, st);
+        own = {x, y, prm};
+      } else {
+        const size_t vb = elem_bytes(op->precision) * (size_t)op->dim;
+        MB_CUDA(cudaMalloc(&x, vb));
+        own.push_back(x);
+        MB_CUDA(cudaMalloc(&y, vb));
+        own.push_back(y);
+        launch_fill_rng(op->precision, op->Du, op->Dd, 12345, 0, 0, x, st);
+      }
+      struct TimingEvents {  // Events (no timing) will not do for elapsed times
+        cudaEvent_t e[2] = {nullptr, nullptr};
+        TimingEvents() {
+          for (auto& x : e) MB_CUDA(cudaEventCreate(&x));
+        }
+        ~TimingEvents() {
+          for (auto x : e)
+            if (x) cudaEventDestroy(x);
+        }
+        cudaEvent_t operator[](int i) const { return e[i]; }
+      } ev;
+      const mb_apply_shape keep = [&] {
+        mb_apply_shape k{};
+        k.passes = op->apply_passes;
+        k.row_split = std::max(1, op->view.row_split);
+        k.table_bits = op->view.table_bits == 16 ? 16 : 32;
+        k.prefetch = op->view.up_prefetch;
+        k.table_stage = op->view.table_stage;
+        return k;
+      }();
+      try {
+        for (const auto& c : cands) {
+          op->apply_passes = c.passes;
+          op->view.row_split = c.row_split;
+          op->view.table_bits = c.table_bits;
+          op->view.up_prefetch = c.prefetch;
+          op->view.table_stage = c.table_stage;
+          auto run = [&] {
+            if (op->precision == MB_PREC_Q64) q_tune_apply(op, x, y, prm, st);
+            else launch_apply(op->view, op->precision, x, y, 1.0, 0.0, 0.0, nullptr, nullptr, 0, st);
+          };
+          run();
+          run();
+          std::vector<float> ts;
+          for (int i = 0; i < 7; ++i) {
+            MB_CUDA(cudaEventRecord(ev[0], st));
+            run();
+            MB_CUDA(cudaEventRecord(ev[1], st));
+            MB_CUDA(cudaEventSynchronize(ev[1]));
+            float ms = 0.f;
+            MB_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+            ts.push_back(ms);
+          }
+          std::sort(ts.begin(), ts.end());
+          const double t = ts[ts.size() / 2];
+          if (best_t == 0.0 || t < best_t) {
+            best_t = t;
+            best = c;
+          }
+        }
+      } catch (...) {
+        op->apply_passes = keep.passes;
+        op->view.row_split = keep.row_split;
+        op->view.table_bits = keep.table_bits;
+        op->view.up_prefetch = keep.prefetch;
+        op->view.table_stage = keep.table_stage;
+        for (void* p : own) cudaFree(p);
+        throw;
+      }
+      for (void* p : own) cudaFree(p);
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tune_cache[op->tune_key] = {best, best_t};
+    }
+    if (op->tune_key.empty()) {  // operators without shapes keep the default
+      best = mb_apply_shape{};
+      best.passes = 1;
+      best.row_split = 1;
+      best.table_bits = 32;
+    } else {
+      std::lock_guard<std::mutex> lk(op->mu);
+      op->apply_passes = best.passes;
+      op->view.row_split = best.row_split;
+      op->view.table_bits = best.table_bits;
+      op->view.up_prefetch = best.prefetch;
+      op->view.table_stage = best.table_stage;
+    }
+    if (chosen) *chosen = best;
+    if (best_ms) *best_ms = best_t;
+  });
+}
+
 int mb_op_apply(mb_op_t op, const void* x_dev, void* y_dev, int order, void* stream) {
   return guard([&] {
     MB_REQUIRE(op, MB_ERR_INVALID_ARG, "NULL operator");
@@ -1113,9 +1412,9 @@ int mb_op_apply_affine(mb_op_t op, const void* x_dev, void* y_dev, double scale,
 // in flight), then the rows are applied group by group and each finished
 // prefix of the reference order goes back on the copy engine while the later
 // groups run.  Same kernels and arithmetic as mb_op_apply, so the same bits.
-static void host_apply_pipeline(mb_op_s* op, const void* x_host, const void* x_mapped,
-                                void* y_host, mb_op_s::Scratch& s) {
-  cudaStream_t comp = op->host_streams[0], copy = op->host_streams[1];
+static void host_apply_pipeline(mb_op_s* op, const mb_op_s::HostLane& lane, const void* x_host,
+                                const void* x_mapped, void* y_host, mb_op_s::Scratch& s) {
+  cudaStream_t comp = lane.comp, copy = lane.copy;
   int32_t* iperm = op_iperm(op);
   const int prec = op->precision;
   const size_t es = elem_bytes(prec);
@@ -1123,24 +1422,20 @@ static void host_apply_pipeline(mb_op_s* op, const void* x_host, const void* x_m
   char* xt = (char*)s.a;  // tensor order
   char* yt = (char*)s.b;
   char* xs = (char*)s.hx;  // landing, reference order
-  constexpr int kChunks = 8;
   if (x_mapped) {
     launch_scatter(prec, n, iperm, x_mapped, xt, comp);
   } else {
-    Events ev(kChunks);
-    const int64_t step = (n + kChunks - 1) / kChunks;
-    for (int c = 0; c < kChunks; ++c) {
-      const int64_t i0 = std::min<int64_t>(n, c * step), i1 = std::min<int64_t>(n, i0 + step);
-      if (i1 > i0)
-        MB_CUDA(cudaMemcpyAsync(xs + es * (size_t)i0, (const char*)x_host + es * (size_t)i0,
-                                es * (size_t)(i1 - i0), cudaMemcpyHostToDevice, copy));
-      MB_CUDA(cudaEventRecord(ev[c], copy));
-      MB_CUDA(cudaStreamWaitEvent(comp, ev[c], 0));
-      if (i1 > i0) launch_scatter(prec, i1 - i0, iperm + i0, xs + es * (size_t)i0, xt, comp);
-    }
+    // pageable x: through the lane's bounce buffers, each chunk scattered to
+    // tensor order once it has landed
+    (void)copy;
+    lane_upload(lane, xs, x_host, es * (size_t)n, es, [&](size_t off, size_t len, cudaEvent_t e) {
+      MB_CUDA(cudaStreamWaitEvent(comp, e, 0));
+      const int64_t i0 = (int64_t)(off / es);
+      launch_scatter(prec, (int64_t)(len / es), iperm + i0, xs + off, xt, comp);
+    });
   }
   host_groups_run(
-      op, es, y_host, s.hy,
+      op, lane, es, y_host, s.hy,
       [&](const OpView& v) {
         launch_apply(v, prec, xt, yt, 1.0, 0.0, 0.0, nullptr, nullptr, 0, comp);
       },
@@ -1149,15 +1444,62 @@ static void host_apply_pipeline(mb_op_s* op, const void* x_host, const void* x_m
       });
 }
 
+// A lane of the operator's host-buffer pool for the length of one call.
+class LaneLease {
+ public:
+  explicit LaneLease(mb_op_s* op) : op_(op) {
+    std::unique_lock<std::mutex> lk(op->host_mu);
+    op->host_cv.wait(lk, [&] {
+      return !op->host_idle.empty() || (int)op->host_lanes.size() < mb_op_s::kMaxHostLanes;
+    });
+    if (op->host_idle.empty()) {
+      auto lane = std::make_unique<mb_op_s::HostLane>();
+      MB_CUDA(cudaStreamCreateWithFlags(&lane->comp, cudaStreamNonBlocking));
+      MB_CUDA(cudaStreamCreateWithFlags(&lane->copy, cudaStreamNonBlocking));
+      op->host_idle.push_back(lane.get());
+      op->host_lanes.push_back(std::move(lane));
+    }
+    lane_ = op->host_idle.back();
+    op->host_idle.pop_back();
+  }
+  ~LaneLease() {
+    {
+      std::lock_guard<std::mutex> lk(op_->host_mu);
+      op_->host_idle.push_back(lane_);
+    }
+    op_->host_cv.notify_one();
+  }
+  LaneLease(const LaneLease&) = delete;
+  LaneLease& operator=(const LaneLease&) = delete;
+  const mb_op_s::HostLane& lane() const { return *lane_; }
+
+ private:
+  mb_op_s* op_;
+  mb_op_s::HostLane* lane_;
+};
+
 int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
   return guard([&] {
     MB_REQUIRE(op && x_host && y_host, MB_ERR_INVALID_ARG, "NULL argument");
     check_order(order);
     const size_t vb = elem_bytes(op->precision) * (size_t)op->dim;
-    cudaStream_t st = 0;
-    // host threads share the staging buffers and the stream: serialise whole
-    // calls, or one thread's upload could land between another's copy and apply
-    std::lock_guard<std::mutex> lk(op->host_mu);
+    const bool pipelined = order == MB_ORDER_REFERENCE && !op->natural_order &&
+                           !op->view.n_blocks && !op->view.csr_row;
+    if (pipelined) {
+      // the row groups are built once, before any lane uses them
+      std::lock_guard<std::mutex> lk(op->host_mu);
+      ensure_host_groups(op);
+    }
+    // each concurrent call runs on its own lane: its streams key its own
+    // staging and scratch buffers.  A call on page-locked vectors moves them
+    // over the host link at its full rate by itself; such calls take turns
+    // (overlapping them only splits the link and slows each one).
+    const bool link_bound = host_pinned(x_host) || host_pinned(y_host);
+    std::unique_lock<std::mutex> link_lock(op->host_link_mu, std::defer_lock);
+    if (link_bound) link_lock.lock();
+    LaneLease lease(op);
+    const mb_op_s::HostLane& lane = lease.lane();
+    cudaStream_t st = lane.comp;
     auto& s = scratch_for(op, st, 0, true);  // the staging pair; a, b where a path needs them
     // A page-locked y (cudaHostAlloc / cudaHostRegister) is written in place by
     // the last kernel (the order / format change), so the result crosses the
@@ -1168,8 +1510,7 @@ int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
                         at.type == cudaMemoryTypeHost && at.devicePointer != nullptr;
     if (!direct) cudaGetLastError();  // clear a failed query on pageable memory
     if (direct) y_dev = at.devicePointer;
-    if (order == MB_ORDER_REFERENCE && !op->natural_order && !op->view.n_blocks &&
-        !op->view.csr_row) {
+    if (pipelined) {
       // x lands scattered to tensor order as it arrives; each finished prefix
       // of the result (reference order) goes back while later rows run
       cudaPointerAttributes ax{};
@@ -1178,25 +1519,41 @@ int mb_op_apply_host(mb_op_t op, const void* x_host, void* y_host, int order) {
       if (!x_locked) cudaGetLastError();
       const void* x_mapped = x_locked ? ax.devicePointer : nullptr;
       if (op->precision == MB_PREC_Q64) {
-        q_apply_host_reference(op, x_host, x_mapped, y_host, s.hx, s.hy);
+        q_apply_host_reference(op, lane, x_host, x_mapped, y_host, s.hx, s.hy);
         return;
       }
-      ensure_host_groups(op);
       scratch_for(op, st, 2);  // a, b: x and y in tensor order
       try {
-        host_apply_pipeline(op, x_host, x_mapped, y_host, s);
+        host_apply_pipeline(op, lane, x_host, x_mapped, y_host, s);
       } catch (...) {
         // nothing may still read or write the caller's buffers once it sees the error
-        cudaStreamSynchronize(op->host_streams[1]);
-        cudaStreamSynchronize(op->host_streams[0]);
+        cudaStreamSynchronize(lane.copy);
+        cudaStreamSynchronize(lane.comp);
         throw;
       }
       return;
     }
-    MB_CUDA(cudaMemcpyAsync(s.hx, x_host, vb, cudaMemcpyHostToDevice, st));
-    apply_affine(op, s.hx, y_dev, 1.0, 0.0, 0.0, nullptr, order, st);
-    if (!direct) MB_CUDA(cudaMemcpyAsync(y_host, s.hy, vb, cudaMemcpyDeviceToHost, st));
-    MB_CUDA(cudaStreamSynchronize(st));
+    try {
+      if (host_pinned(x_host)) {
+        MB_CUDA(cudaMemcpyAsync(s.hx, x_host, vb, cudaMemcpyHostToDevice, st));
+      } else {
+        lane_upload(lane, s.hx, x_host, vb, 16, [&](size_t, size_t, cudaEvent_t e) {
+          MB_CUDA(cudaStreamWaitEvent(st, e, 0));
+        });
+      }
+      apply_affine(op, s.hx, y_dev, 1.0, 0.0, 0.0, nullptr, order, st);
+      if (!direct) {  // pageable y: through the lane's bounce buffers
+        Events ev(1);
+        MB_CUDA(cudaEventRecord(ev[0], st));
+        MB_CUDA(cudaStreamWaitEvent(lane.copy, ev[0], 0));
+        lane_download(lane, y_host, s.hy, vb);
+      }
+      MB_CUDA(cudaStreamSynchronize(st));
+    } catch (...) {
+      cudaStreamSynchronize(lane.copy);
+      cudaStreamSynchronize(st);
+      throw;
+    }
   });
 }
 

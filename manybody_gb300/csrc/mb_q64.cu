@@ -128,12 +128,104 @@ __device__ void q_block_reduce(double (&v)[NC], unsigned long long magor, double
   }
 }
 
+// Exact block sums of the apply's two dot accumulators (128-bit integers):
+// the block writes {xy_lo, xy_hi, yy_lo, yy_hi} to part128[4 * blockIdx.x]
+// and ORs its max word into *max_or.  Integer sums are exact in any order, so
+// the dot products do not depend on which block applied which rows.
+__device__ __forceinline__ __int128 shfl_down_i128(__int128 v, int o) {
+  const unsigned long long lo = __shfl_down_sync(0xffffffffu, (unsigned long long)v, o);
+  const unsigned long long hi =
+      __shfl_down_sync(0xffffffffu, (unsigned long long)((unsigned __int128)v >> 64), o);
+  return (__int128)(((unsigned __int128)hi << 64) | lo);
+}
+
+__device__ void q_block_reduce_exact(__int128 xy, __int128 yy, unsigned long long magor,
+                                     long long* part128, unsigned long long* max_or) {
+  __shared__ __int128 red[32][2];
+  __shared__ unsigned long long mor[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    xy += shfl_down_i128(xy, o);
+    yy += shfl_down_i128(yy, o);
+    magor |= __shfl_down_sync(0xffffffffu, magor, o);
+  }
+  __syncthreads();
+  if (lane == 0) {
+    red[warp][0] = xy;
+    red[warp][1] = yy;
+    mor[warp] = magor;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    __int128 a = lane < nw ? red[lane][0] : 0, b = lane < nw ? red[lane][1] : 0;
+    unsigned long long m = lane < nw ? mor[lane] : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += shfl_down_i128(a, o);
+      b += shfl_down_i128(b, o);
+      m |= __shfl_down_sync(0xffffffffu, m, o);
+    }
+    if (lane == 0) {
+      if (part128) {
+        long long* p = part128 + 4 * (size_t)blockIdx.x;
+        p[0] = (long long)(unsigned long long)a;
+        p[1] = (long long)(a >> 64);
+        p[2] = (long long)(unsigned long long)b;
+        p[3] = (long long)(b >> 64);
+      }
+      if (max_or && m) atomicOr(max_or, m);
+    }
+  }
+}
+
+// The exact sum of nblocks such partials, converted once to double: out[0]
+// (xy), out[1] (yy).
+__global__ void k_q_reduce128(const long long* __restrict__ part, int nblocks,
+                              double* __restrict__ out) {
+  __int128 a = 0, b = 0;
+  for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
+    const long long* p = part + 4 * (size_t)i;
+    a += (__int128)(((unsigned __int128)(unsigned long long)p[1] << 64) | (unsigned long long)p[0]);
+    b += (__int128)(((unsigned __int128)(unsigned long long)p[3] << 64) | (unsigned long long)p[2]);
+  }
+  __shared__ __int128 red[32][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += shfl_down_i128(a, o);
+    b += shfl_down_i128(b, o);
+  }
+  if (lane == 0) {
+    red[warp][0] = a;
+    red[warp][1] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __int128 sa = 0, sb = 0;
+    for (int w = 0; w < (int)((blockDim.x + 31) >> 5); ++w) {
+      sa += red[w][0];
+      sb += red[w][1];
+    }
+    out[0] = i128_to_f64(sa);
+    out[1] = i128_to_f64(sb);
+  }
+}
+
+void launch_q_reduce128(const void* part, int nblocks, double* out, cudaStream_t st) {
+  k_q_reduce128<<<1, 256, 0, st>>>((const long long*)part, nblocks, out);
+  MB_CUDA(cudaGetLastError());
+}
+
 // ---------------------------------------------------------------------------
 // The Q64 apply: y = scale (H - shift) x + beta z on mantissas.
 //   P = c1 * S + cq[popc(up & down)] * x_q + c3 * z_q      (128-bit)
 //   y_q = round(P / 2^sh)
 // S = sum over hops of +-x_q (doubled bonds listed twice), exact in int64.
-// dots (DOTS bit0): Re<x,y> and <y,y> as exact integer sums >> 32.
+// dots (DOTS bit0): Re<x,y> and <y,y> as exact integer sums >> 32, written
+// per block as 128-bit integers (partials: 4 words a block; k_q_reduce128
+// sums them).
 //
 // One CTA of 1024 threads per SM walks the rows r_up in the row schedule's
 // order (reverse Cuthill-McKee: rows in flight together share neighbour rows
@@ -146,18 +238,188 @@ __device__ void q_block_reduce(double (&v)[NC], unsigned long long magor, double
 //     column's count of negative hops is added back once;
 //   up hops: the row's sign-sorted target list (uniform across the CTA):
 //     coalesced 16-byte loads x[r',c], summed then subtracted, no sign work;
-//     the lines of the warp's next group are prefetched into L2 first.
+//     with up_prefetch set, the lines of the warp's next group are
+//     prefetched into L2 first (the autotuner's choice; off by default).
 // Hops are summed in pairs (three-operand 64-bit adds).
 // ---------------------------------------------------------------------------
 constexpr int kQThreads = 1024;
 
-template <bool STAGED, int DOTS, bool HAS_Z>
+// Sum of +-v over one warp group's sliced-table slots (down hops of a staged
+// row, or up hops of a staged column).  `val` takes the neighbour's byte
+// offset (index * 16).  A negative hop adds v ^ -1 (= -v - 1); the caller adds
+// the state's count of negative hops back once.  The group's slot count k is
+// the same for the whole warp, so the padding slots past k in the last word
+// are skipped without divergence.
+//  32-bit entries: index | negative << 31, four slots per 16-byte load;
+//  16-bit entries: index | negative << 15, eight slots per 16-byte load.
+template <typename Load>
+__device__ __forceinline__ void hop_add(Load& val, uint32_t off, long long m, long long& sr,
+                                        long long& si) {
+  const longlong2 v = val(off);
+  sr += v.x ^ m;
+  si += v.y ^ m;
+}
+
+template <typename Load>
+__device__ __forceinline__ void sliced_sum(const uint32_t* __restrict__ sell, int2 gi, int lane,
+                                           Load&& val, long long& sr, long long& si) {
+  const uint4* ep = reinterpret_cast<const uint4*>(sell + gi.x) + lane;
+  const int k = gi.y;
+  int j = 0;
+  for (; j + 4 <= k; j += 4) {
+    const uint4 e = __ldg(ep + 8 * j);
+    const long long m0 = (int)e.x >> 31, m1 = (int)e.y >> 31;  // 0 or -1
+    const long long m2 = (int)e.z >> 31, m3 = (int)e.w >> 31;
+    const longlong2 v0 = val(e.x << 4), v1 = val(e.y << 4);  // the sign bit shifts out
+    const longlong2 v2 = val(e.z << 4), v3 = val(e.w << 4);
+    sr += (v0.x ^ m0) + (v1.x ^ m1);
+    si += (v0.y ^ m0) + (v1.y ^ m1);
+    sr += (v2.x ^ m2) + (v3.x ^ m3);
+    si += (v2.y ^ m2) + (v3.y ^ m3);
+  }
+  if (j < k) {
+    const uint4 e = __ldg(ep + 8 * j);
+    hop_add(val, e.x << 4, (int)e.x >> 31, sr, si);
+    if (j + 1 < k) hop_add(val, e.y << 4, (int)e.y >> 31, sr, si);
+    if (j + 2 < k) hop_add(val, e.z << 4, (int)e.z >> 31, sr, si);
+  }
+}
+
+// the two 16-bit entries of a word: byte offsets and sign masks
+__device__ __forceinline__ uint32_t off_lo(uint32_t w) { return (w << 4) & 0x7FFF0u; }
+__device__ __forceinline__ uint32_t off_hi(uint32_t w) { return (w >> 12) & 0x7FFF0u; }
+__device__ __forceinline__ long long neg_lo(uint32_t w) { return (int)(w << 16) >> 31; }
+__device__ __forceinline__ long long neg_hi(uint32_t w) { return (int)w >> 31; }
+
+template <typename Load>
+__device__ __forceinline__ void word_add(Load& val, uint32_t w, long long& sr, long long& si) {
+  const longlong2 a = val(off_lo(w)), b = val(off_hi(w));
+  const long long ma = neg_lo(w), mb = neg_hi(w);
+  sr += (a.x ^ ma) + (b.x ^ mb);
+  si += (a.y ^ ma) + (b.y ^ mb);
+}
+
+template <typename Load>
+__device__ __forceinline__ void sliced_sum16(const uint16_t* __restrict__ sell, int2 gi, int lane,
+                                             Load&& val, long long& sr, long long& si) {
+  const uint4* ep = reinterpret_cast<const uint4*>(sell + gi.x) + lane;
+  const int k = gi.y;
+  int j = 0;
+  for (; j + 8 <= k; j += 8) {
+    const uint4 e = __ldg(ep + 4 * j);
+    word_add(val, e.x, sr, si);
+    word_add(val, e.y, sr, si);
+    word_add(val, e.z, sr, si);
+    word_add(val, e.w, sr, si);
+  }
+  if (j < k) {
+    const uint4 e = __ldg(ep + 4 * j);
+    const int rem = k - j;  // 1..7
+    const uint32_t w[4] = {e.x, e.y, e.z, e.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (2 * q + 2 <= rem) word_add(val, w[q], sr, si);
+      else if (2 * q + 1 == rem) hop_add(val, off_lo(w[q]), neg_lo(w[q]), sr, si);
+    }
+  }
+}
+
+// The same sum from a lane's words in a warp-private shared buffer (word w
+// at ep[32 w]).
+template <typename Load>
+__device__ __forceinline__ void sliced_sum_words(const uint4* ep, int k, Load&& val, long long& sr,
+                                                 long long& si) {
+  int j = 0;
+  for (; j + 4 <= k; j += 4) {
+    const uint4 e = ep[8 * j];
+    const long long m0 = (int)e.x >> 31, m1 = (int)e.y >> 31;
+    const long long m2 = (int)e.z >> 31, m3 = (int)e.w >> 31;
+    const longlong2 v0 = val(e.x << 4), v1 = val(e.y << 4);
+    const longlong2 v2 = val(e.z << 4), v3 = val(e.w << 4);
+    sr += (v0.x ^ m0) + (v1.x ^ m1);
+    si += (v0.y ^ m0) + (v1.y ^ m1);
+    sr += (v2.x ^ m2) + (v3.x ^ m3);
+    si += (v2.y ^ m2) + (v3.y ^ m3);
+  }
+  if (j < k) {
+    const uint4 e = ep[8 * j];
+    hop_add(val, e.x << 4, (int)e.x >> 31, sr, si);
+    if (j + 1 < k) hop_add(val, e.y << 4, (int)e.y >> 31, sr, si);
+    if (j + 2 < k) hop_add(val, e.z << 4, (int)e.z >> 31, sr, si);
+  }
+}
+
+template <int TB, typename Load>
+__device__ __forceinline__ void sliced_sum_t(const uint32_t* sell, const uint16_t* sell16,
+                                             int2 gi, int lane, Load&& val, long long& sr,
+                                             long long& si) {
+  if (TB == 16) sliced_sum16(sell16, gi, lane, val, sr, si);
+  else sliced_sum(sell, gi, lane, val, sr, si);
+}
+
+// ---------------------------------------------------------------------------
+// Column pass of the two-pass Q64 apply.  For every column c (down state) the
+// column x[:, c] (Du elements, 16 bytes apart by the row length) and eight zero
+// elements are staged in shared memory; warp w then takes the 32-row groups
+// g = w, w + 32, ... and gathers each row's up hops from the staged column
+// through the up sector's sliced table, exactly as the row pass gathers down
+// hops from a staged row.  The exact int64 hop sum of (r, c) goes to
+// ups[c * Du + r] (column-major: one warp's 32 rows are one 512-byte store).
+// CTAs take consecutive columns, so the strided column loads of the CTAs in
+// flight share their L2 sectors.
+// ---------------------------------------------------------------------------
+constexpr int kQColThreads = 1024;
+
+template <int TB>
+__global__ void __launch_bounds__(kQColThreads, 1)
+k_upcol_q(OpView v, const longlong2* __restrict__ x, longlong2* __restrict__ ups) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  longlong2* col = reinterpret_cast<longlong2*>(smem);
+  const int64_t Dd = v.Dd, Du = v.dim / v.Dd;
+  if (threadIdx.x < kSlicedPads) col[Du + threadIdx.x] = make_longlong2(0, 0);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int64_t ngroups = (Du + 31) >> 5;
+  const int64_t nt = blockDim.x;
+  const int2* sgrp = reinterpret_cast<const int2*>(TB == 16 ? v.up_sgrp16 : v.up_sgrp);
+  auto val = [&](uint32_t off) -> longlong2 {
+    return *reinterpret_cast<const longlong2*>(smem + off);
+  };
+  for (int64_t c = blockIdx.x; c < Dd; c += gridDim.x) {
+    __syncthreads();
+    for (int64_t r0 = threadIdx.x; r0 < Du; r0 += 8 * nt) {
+      longlong2 t[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int64_t r = r0 + k * nt;
+        t[k] = r < Du ? __ldg(x + r * Dd + c) : make_longlong2(0, 0);
+      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int64_t r = r0 + k * nt;
+        if (r < Du) col[r] = t[k];
+      }
+    }
+    __syncthreads();
+    for (int64_t g = warp; g < ngroups; g += nwarps) {
+      const int64_t r = (g << 5) + lane;
+      long long sr = 0, si = 0;
+      sliced_sum_t<TB>(v.up_sell, v.up_sell16, __ldg(sgrp + g), lane, val, sr, si);
+      if (r < Du) {
+        const int nneg = __ldg(&v.up_nneg[r]);
+        ups[c * Du + r] = make_longlong2(sr + nneg, si + nneg);
+      }
+    }
+  }
+}
+
+template <bool STAGED, int DOTS, bool HAS_Z, bool UPS, int TB, bool TS>
 __global__ void __launch_bounds__(kQThreads, 1)
 k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlong2* z,
           const QParams* __restrict__ prm, double* __restrict__ partials,
-          unsigned long long* __restrict__ max_or) {
+          unsigned long long* __restrict__ max_or, const longlong2* __restrict__ ups) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int64_t Dd = v.Dd;
+  const int64_t Du_all = v.dim / v.Dd;
   const uint32_t row_bytes = (uint32_t)(16 * Dd);
   uint32_t* s_up = reinterpret_cast<uint32_t*>(smem + (STAGED ? row_bytes + 16 * kSlicedPads : 0));
   __shared__ long long s_cq[kMaxOrbitals + 1];
@@ -176,20 +438,51 @@ k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlon
   __int128 a_xy = 0, a_yy = 0;
   unsigned long long mor = 0;
   // a down neighbour by table entry: staged row, or the row in global memory
-  auto dn_val = [&](const longlong2* xrow, uint32_t e) -> longlong2 {
-    const uint32_t off = e << 4;  // byte offset; the sign bit shifts out
+  auto dn_val = [&](const longlong2* xrow, uint32_t off) -> longlong2 {
     if (STAGED) return *reinterpret_cast<const longlong2*>(smem + off);
     return off < row_bytes
                ? __ldg(reinterpret_cast<const longlong2*>(reinterpret_cast<const char*>(xrow) + off))
                : make_longlong2(0, 0);
   };
+  const int2* sgrp = reinterpret_cast<const int2*>(TB == 16 ? v.dn_sgrp16 : v.dn_sgrp);
+  // row_split CTAs share a row (the grid is a multiple of it): each stages the
+  // row and takes every split-th column group
+  const int split = v.row_split > 1 ? v.row_split : 1;
+  const int64_t g0 = (int64_t)(blockIdx.x % split) * nwarps, gstep = (int64_t)nwarps * split;
+  const int64_t rstep = gridDim.x / split;
+  // TS: a warp's down-table words of its next column group go to a
+  // warp-private shared buffer (cp.async, one 16-byte word per lane and slot
+  // quadruple) while it finishes the current group, so its down hops read them
+  // from shared memory instead of waiting on L2 once per word.  A warp's groups
+  // are the same in every row: after its last group of a row comes its first.
+  uint4* tbuf = nullptr;
+  int kcur = 0;
+  auto ts_issue = [&](int64_t gg) -> int {
+    const int2 gi = __ldg(sgrp + gg);
+    const uint4* src = reinterpret_cast<const uint4*>(v.dn_sell + gi.x) + lane;
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(tbuf + lane);
+    const int nw = (gi.y + 3) >> 2;
+    for (int w = 0; w < nw; ++w)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 512u * (uint32_t)w),
+                   "l"(src + 32 * w)
+                   : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    return gi.y;
+  };
+  if (TS) {
+    const size_t lists = sizeof(uint32_t) * (size_t)((v.max_up_list + 3) & ~3);
+    tbuf = reinterpret_cast<uint4*>(smem + row_bytes + 16 * kSlicedPads + lists) +
+           (size_t)warp * v.dn_max_words * 32;
+    if (g0 + warp < ngroups && blockIdx.x / split < v.Du) kcur = ts_issue(g0 + warp);
+  }
 
-  for (int64_t ri = blockIdx.x; ri < v.Du; ri += gridDim.x) {
+  for (int64_t ri = blockIdx.x / split; ri < v.Du; ri += rstep) {
     const int64_t r = v.row_sched ? (int64_t)v.row_sched[ri] : ri;
     const longlong2* xrow = x + r * Dd;
     __syncthreads();
-    const int u0 = __ldg(&v.up_loff[r]), nu = __ldg(&v.up_loff[r + 1]) - u0;
-    const int npos = __ldg(&v.up_lpos[r]);
+    const int u0 = UPS ? 0 : __ldg(&v.up_loff[r]);
+    const int nu = UPS ? 0 : __ldg(&v.up_loff[r + 1]) - u0;
+    const int npos = UPS ? 0 : __ldg(&v.up_lpos[r]);
     for (int j = threadIdx.x; j < nu; j += blockDim.x) s_up[j] = __ldg(&v.up_list[u0 + j]);
     if (STAGED)
       for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x)
@@ -198,35 +491,39 @@ k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlon
     const uint32_t um = v.up_mask[r];
     const long long c1 = s_c1, c3 = s_c3;
     const int sh = s_sh;
-    for (int64_t g = warp; g < ngroups; g += nwarps) {
+    for (int64_t g = g0 + warp; g < ngroups; g += gstep) {
       const int64_t c = (g << 5) + lane;
       const bool live = c < Dd;
       const int64_t cl = live ? c : Dd - 1;
-      if (g + nwarps < ngroups) {
+      if (!UPS && v.up_prefetch && g + gstep < ngroups) {
         // the up-hop lines of this warp's next group, into L2 ahead of use
-        const int64_t cn = min(((g + nwarps) << 5) + lane, Dd - 1);
+        const int64_t cn = min(((g + gstep) << 5) + lane, Dd - 1);
         const char* xn = reinterpret_cast<const char*>(x + cn);
         for (int k = 0; k < nu; ++k)
           asm volatile("prefetch.global.L2 [%0];" ::"l"(xn + (uint64_t)s_up[k] * row_bytes));
       }
       long long sr = 0, si = 0;
-      const int2 gi = __ldg(reinterpret_cast<const int2*>(v.dn_sgrp) + g);
-      // four slots per 16-byte load; the last word's unused slots are padding
-      const uint4* ep = reinterpret_cast<const uint4*>(v.dn_sell + gi.x) + lane;
-      for (int j = 0; j < gi.y; j += 4) {
-        const uint4 e = __ldg(ep + 8 * j);
-        const long long m0 = (int)e.x >> 31, m1 = (int)e.y >> 31;  // 0 or -1
-        const long long m2 = (int)e.z >> 31, m3 = (int)e.w >> 31;
-        const longlong2 v0 = dn_val(xrow, e.x), v1 = dn_val(xrow, e.y);
-        const longlong2 v2 = dn_val(xrow, e.z), v3 = dn_val(xrow, e.w);
-        sr += (v0.x ^ m0) + (v1.x ^ m1);
-        si += (v0.y ^ m0) + (v1.y ^ m1);
-        sr += (v2.x ^ m2) + (v3.x ^ m3);
-        si += (v2.y ^ m2) + (v3.y ^ m3);
+      if (TS) {
+        asm volatile("cp.async.wait_all;" ::: "memory");  // this group's words
+        sliced_sum_words(tbuf + lane, kcur, [&](uint32_t off) { return dn_val(xrow, off); }, sr,
+                         si);
+        int64_t gn = g + gstep;
+        if (gn >= ngroups) gn = ri + rstep < v.Du ? g0 + warp : -1;
+        if (gn >= 0) kcur = ts_issue(gn);
+      } else {
+        // four slots per 16-byte load; the last word's unused slots are padding
+        sliced_sum_t<TB>(v.dn_sell, v.dn_sell16, __ldg(sgrp + g), lane,
+                         [&](uint32_t off) { return dn_val(xrow, off); }, sr, si);
       }
       const int nneg = __ldg(&v.dn_nneg[cl]);
       sr += nneg;
       si += nneg;
+      if (UPS) {
+        // up hops: the column pass's exact sum for (r, c)
+        const longlong2 uv = __ldg(ups + cl * Du_all + r);
+        sr += uv.x;
+        si += uv.y;
+      }
       const char* xc = reinterpret_cast<const char*>(x + cl);
       auto up_val = [&](int k) {
         return __ldg(reinterpret_cast<const longlong2*>(xc + (uint64_t)s_up[k] * row_bytes));
@@ -275,10 +572,8 @@ k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlon
       if (DOTS & 4) mor |= mag(out.x) | mag(out.y);
     }
   }
-  if (DOTS) {
-    double vals[2] = {i128_to_f64(a_xy), i128_to_f64(a_yy)};
-    q_block_reduce<2>(vals, mor, partials, max_or);
-  }
+  if (TS) asm volatile("cp.async.wait_all;" ::: "memory");
+  if (DOTS) q_block_reduce_exact(a_xy, a_yy, mor, reinterpret_cast<long long*>(partials), max_or);
 }
 
 static int sm_count() {
@@ -302,42 +597,125 @@ static int smem_optin() {
 }
 
 int q_apply_grid(const OpView& v) {
+  const int split = v.row_split > 1 ? v.row_split : 1;
   int64_t g = sm_count();
-  if (g > v.Du) g = v.Du;
-  return (int)std::max<int64_t>(g, 1);
+  if (g > v.Du * split) g = v.Du * split;
+  g -= g % split;
+  return (int)std::max<int64_t>(g, split);
 }
 
-template <bool STAGED, int DOTS, bool HAS_Z>
+// the table width a launch uses: 16-bit where the view has the copies
+static int q_table_bits(const OpView& v, bool rows) {
+  if (v.table_bits != 16) return 32;
+  return (rows ? v.dn_sell16 : v.up_sell16) ? 16 : 32;
+}
+
+// dynamic shared memory of a launch: the staged row and pads, the up list,
+// and with TS the warps' table buffers
+static size_t q_apply_smem(const OpView& v, bool staged, bool ups, bool ts) {
+  size_t smem = ups ? 0 : sizeof(uint32_t) * (size_t)((v.max_up_list + 3) & ~3);
+  if (staged) smem += sizeof(longlong2) * (size_t)(v.Dd + kSlicedPads);
+  if (ts) smem += (size_t)(kQThreads / 32) * (size_t)v.dn_max_words * 512;
+  return smem;
+}
+
+template <bool STAGED, int DOTS, bool HAS_Z, bool UPS, int TB, bool TS = false>
 static void q_apply_t(const OpView& v, const void* x, void* y, const void* z, const QParams* prm,
-                      double* partials, unsigned long long* max_or, cudaStream_t st) {
-  size_t smem = sizeof(uint32_t) * (size_t)((v.max_up_list + 3) & ~3);
-  if (STAGED) smem += sizeof(longlong2) * (size_t)(v.Dd + kSlicedPads);
-  auto kern = k_apply_q<STAGED, DOTS, HAS_Z>;
+                      double* partials, unsigned long long* max_or, const void* ups,
+                      cudaStream_t st) {
+  const size_t smem = q_apply_smem(v, STAGED, UPS, TS);
+  auto kern = k_apply_q<STAGED, DOTS, HAS_Z, UPS, TB, TS>;
   MB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<q_apply_grid(v), kQThreads, smem, st>>>(v, (const longlong2*)x, (longlong2*)y,
-                                                   (const longlong2*)z, prm, partials, max_or);
+                                                   (const longlong2*)z, prm, partials, max_or,
+                                                   (const longlong2*)ups);
   MB_CUDA(cudaGetLastError());
 }
 
-template <bool STAGED>
+template <bool STAGED, bool UPS, int TB>
 static void q_apply_sel(const OpView& v, const void* x, void* y, const void* z,
                         const QParams* prm, double* partials, unsigned long long* max_or,
-                        int dots, cudaStream_t st) {
+                        int dots, const void* ups, cudaStream_t st) {
   if (z) {
-    if (dots) q_apply_t<STAGED, 7, true>(v, x, y, z, prm, partials, max_or, st);
-    else q_apply_t<STAGED, 0, true>(v, x, y, z, prm, partials, max_or, st);
+    if (dots) q_apply_t<STAGED, 7, true, UPS, TB>(v, x, y, z, prm, partials, max_or, ups, st);
+    else q_apply_t<STAGED, 0, true, UPS, TB>(v, x, y, z, prm, partials, max_or, ups, st);
   } else {
-    if (dots) q_apply_t<STAGED, 7, false>(v, x, y, z, prm, partials, max_or, st);
-    else q_apply_t<STAGED, 0, false>(v, x, y, z, prm, partials, max_or, st);
+    if (dots) q_apply_t<STAGED, 7, false, UPS, TB>(v, x, y, z, prm, partials, max_or, ups, st);
+    else q_apply_t<STAGED, 0, false, UPS, TB>(v, x, y, z, prm, partials, max_or, ups, st);
   }
 }
 
+// the table-staged one-pass apply: where the warps' buffers fit beside the row
+bool q_table_stage_fits(const OpView& v) {
+  return v.dn_max_words > 0 &&
+         q_apply_smem(v, true, false, true) + 2048 <= (size_t)smem_optin();
+}
+
+static void q_apply_ts(const OpView& v, const void* x, void* y, const void* z,
+                       const QParams* prm, double* partials, unsigned long long* max_or,
+                       int dots, cudaStream_t st) {
+  if (z) {
+    if (dots) q_apply_t<true, 7, true, false, 32, true>(v, x, y, z, prm, partials, max_or, nullptr, st);
+    else q_apply_t<true, 0, true, false, 32, true>(v, x, y, z, prm, partials, max_or, nullptr, st);
+  } else {
+    if (dots) q_apply_t<true, 7, false, false, 32, true>(v, x, y, z, prm, partials, max_or, nullptr, st);
+    else q_apply_t<true, 0, false, false, 32, true>(v, x, y, z, prm, partials, max_or, nullptr, st);
+  }
+}
+
+template <bool STAGED, bool UPS>
+static void q_apply_tb(const OpView& v, const void* x, void* y, const void* z,
+                       const QParams* prm, double* partials, unsigned long long* max_or,
+                       int dots, const void* ups, cudaStream_t st) {
+  if (STAGED && !UPS && v.table_stage && q_table_bits(v, true) == 32 && q_table_stage_fits(v)) {
+    q_apply_ts(v, x, y, z, prm, partials, max_or, dots, st);
+    return;
+  }
+  if (q_table_bits(v, true) == 16)
+    q_apply_sel<STAGED, UPS, 16>(v, x, y, z, prm, partials, max_or, dots, ups, st);
+  else q_apply_sel<STAGED, UPS, 32>(v, x, y, z, prm, partials, max_or, dots, ups, st);
+}
+
+bool q_upcol_fits(const OpView& v) {
+  const int64_t Du = v.dim / v.Dd;
+  return sizeof(longlong2) * (size_t)(Du + kSlicedPads) + 1024 <= (size_t)smem_optin() &&
+         v.up_sell != nullptr;
+}
+
+template <int TB>
+static void upcol_t(const OpView& v, const void* x, void* ups, cudaStream_t st) {
+  const int64_t Du = v.dim / v.Dd;
+  const size_t smem = sizeof(longlong2) * (size_t)(Du + kSlicedPads);
+  MB_CUDA(cudaFuncSetAttribute(k_upcol_q<TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem));
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(sm_count(), v.Dd));
+  k_upcol_q<TB><<<grid, kQColThreads, smem, st>>>(v, (const longlong2*)x, (longlong2*)ups);
+  MB_CUDA(cudaGetLastError());
+}
+
+void launch_upcol_q(const OpView& v, const void* x, void* ups, cudaStream_t st) {
+  if (q_table_bits(v, false) == 16) upcol_t<16>(v, x, ups, st);
+  else upcol_t<32>(v, x, ups, st);
+}
+
 void launch_apply_q(const OpView& v, const void* x, void* y, const void* z, const QParams* prm,
-                    double* partials, unsigned long long* max_or, int dots, cudaStream_t st) {
-  const size_t need = sizeof(uint32_t) * (size_t)((v.max_up_list + 3) & ~3) +
-                      sizeof(longlong2) * (size_t)(v.Dd + kSlicedPads) + 2048;
-  if (need <= (size_t)smem_optin()) q_apply_sel<true>(v, x, y, z, prm, partials, max_or, dots, st);
-  else q_apply_sel<false>(v, x, y, z, prm, partials, max_or, dots, st);
+                    double* partials, unsigned long long* max_or, int dots, cudaStream_t st,
+                    const void* ups) {
+  const size_t row = sizeof(longlong2) * (size_t)(v.Dd + kSlicedPads) + 2048;
+  const size_t lists = sizeof(uint32_t) * (size_t)((v.max_up_list + 3) & ~3);
+  if (ups) {
+    // the rows of the whole sector in index order (concurrent rows read
+    // neighbouring elements of the column-major up sums); a row group keeps
+    // its own schedule
+    OpView w = v;
+    if (w.Du == w.dim / w.Dd) w.row_sched = nullptr;
+    if (row <= (size_t)smem_optin()) q_apply_tb<true, true>(w, x, y, z, prm, partials, max_or, dots, ups, st);
+    else q_apply_tb<false, true>(w, x, y, z, prm, partials, max_or, dots, ups, st);
+    return;
+  }
+  if (row + lists <= (size_t)smem_optin())
+    q_apply_tb<true, false>(v, x, y, z, prm, partials, max_or, dots, nullptr, st);
+  else q_apply_tb<false, false>(v, x, y, z, prm, partials, max_or, dots, nullptr, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -38,10 +38,26 @@ struct QPlanInput {
 };
 
 __host__ __device__ void q_plan(QParams* p, const QPlanInput& in);
+// The plan input of y = H x (scale 1, no shift, no z) on an MB_PREC_Q64
+// operator, the exponent of x read on the device.
+QPlanInput q_plain_plan_input(const mb_op_s* op);
 
-// The fused apply (one pass over x; see mb_q64.cu).  y must not alias x or z.
+// The fused apply (see mb_q64.cu).  y must not alias x or z.  With ups (the
+// column pass's up-hop sums of x, launch_upcol_q) the up hops are read from
+// it; without, they are gathered from x in the same pass.
 void launch_apply_q(const OpView& v, const void* x, void* y, const void* z, const QParams* prm_dev,
-                    double* partials, unsigned long long* max_or, int dots, cudaStream_t st);
+                    double* partials, unsigned long long* max_or, int dots, cudaStream_t st,
+                    const void* ups = nullptr);
+// The exact sum of an apply's per-block dot partials (4 words a block:
+// 128-bit Re<x,y> and <y,y>) -> out[0], out[1] as double.
+void launch_q_reduce128(const void* part, int nblocks, double* out, cudaStream_t st);
+// Column pass of the two-pass apply: ups[c * Du + r] = exact sum of the up
+// hops of (r, c) on x's mantissas (dim longlong2 elements of scratch).
+void launch_upcol_q(const OpView& v, const void* x, void* ups, cudaStream_t st);
+// whether a column of the sector fits in shared memory (the column pass)
+bool q_upcol_fits(const OpView& v);
+// whether the warps' table buffers fit beside the staged row (table_stage)
+bool q_table_stage_fits(const OpView& v);
 // blocks that write dot partials for an apply
 int q_apply_grid(const OpView& v);
 int q_blas_grid(int64_t n);

@@ -69,6 +69,9 @@ void q_op_release(mb_op_s* op) {
       if (p) cudaFree(p);
   }
   op->qscratch.clear();
+  for (auto& kv : op->ups_scratch)
+    if (kv.second) cudaFree(kv.second);
+  op->ups_scratch.clear();
 }
 
 static QPlanInput plan_input(const mb_op_s* op, double scale, double shift, double beta, int ex,
@@ -89,6 +92,10 @@ static QPlanInput plan_input(const mb_op_s* op, double scale, double shift, doub
   return in;
 }
 
+QPlanInput q_plain_plan_input(const mb_op_s* op) {
+  return plan_input(op, 1.0, 0.0, 0.0, 0, 0, false);
+}
+
 static mb_op_s::QScratch& qscratch_for(mb_op_s* op, cudaStream_t st) {
   std::lock_guard<std::mutex> lk(op->mu);
   auto& s = op->qscratch[st];
@@ -102,6 +109,53 @@ static mb_op_s::QScratch& qscratch_for(mb_op_s* op, cudaStream_t st) {
   return s;
 }
 
+// The up-hop scratch of `st` when the operator's apply runs in two passes
+// (allocated on first use), else nullptr.
+static void* q_ups_for(mb_op_s* op, cudaStream_t st) {
+  if (op->apply_passes != 2 || !q_upcol_fits(op->view)) return nullptr;
+  std::lock_guard<std::mutex> lk(op->mu);
+  void*& p = op->ups_scratch[st];
+  if (!p) MB_CUDA(cudaMalloc(&p, sizeof(longlong2) * (size_t)op->dim));
+  return p;
+}
+
+// The Q64 apply of the whole sector in the operator's shape.
+static void q_apply_whole(mb_op_s* op, const void* xq, void* yq, const void* zq,
+                          const QParams* prm, double* partials, unsigned long long* max_or,
+                          int dots, cudaStream_t st) {
+  void* ups = q_ups_for(op, st);
+  if (ups) launch_upcol_q(op->view, xq, ups, st);
+  launch_apply_q(op->view, xq, yq, zq, prm, partials, max_or, dots, st, ups);
+}
+
+// The autotuner's Q64 vectors: a seeded vector's mantissas (tensor order), an
+// output and its planned parameters (y = H x).
+void q_tune_prepare(mb_op_s* op, void** xq, void** yq, void** prm, cudaStream_t st) {
+  const size_t vb = sizeof(longlong2) * (size_t)op->dim;
+  QBuf x64(vb), ints(4 * sizeof(int));
+  void *a = nullptr, *b = nullptr, *p = nullptr;
+  try {
+    MB_CUDA(cudaMalloc(&a, vb));
+    MB_CUDA(cudaMalloc(&b, vb));
+    MB_CUDA(cudaMalloc(&p, sizeof(QParams)));
+    launch_fill_rng(MB_PREC_F64, op->Du, op->Dd, 12345, 0, 0, x64.p, st);
+    launch_f64_to_q(op->dim, x64.p, nullptr, op->q_qbits, (int*)ints.p, a, st);
+    launch_q_plan(q_plain_plan_input(op), (const int*)ints.p + 1, (QParams*)p, st);
+    MB_CUDA(cudaStreamSynchronize(st));
+  } catch (...) {
+    for (void* q : {a, b, p})
+      if (q) cudaFree(q);
+    throw;
+  }
+  *xq = a;
+  *yq = b;
+  *prm = p;
+}
+
+void q_tune_apply(mb_op_s* op, const void* xq, void* yq, const void* prm, cudaStream_t st) {
+  q_apply_whole(op, xq, yq, nullptr, (const QParams*)prm, nullptr, nullptr, 0, st);
+}
+
 // y = scale (H - shift) x + beta z on complex128 vectors through Q64.
 // z, when used, is folded in FP64 after the Q64 apply (z keeps its own
 // magnitude): y = Q64[scale (H - shift) x] + beta z.
@@ -112,7 +166,7 @@ void q_apply_affine(mb_op_s* op, const void* x, void* y, double scale, double sh
   int32_t* iperm = order == MB_ORDER_REFERENCE ? op_iperm(op) : nullptr;
   launch_f64_to_q(op->dim, x, perm, op->q_qbits, s.ints, s.xq, st);
   launch_q_plan(plan_input(op, scale, shift, 0.0, 0, 0, false), s.ints + 1, (QParams*)s.prm, st);
-  launch_apply_q(op->view, s.xq, s.yq, nullptr, (const QParams*)s.prm, nullptr, nullptr, 0, st);
+  q_apply_whole(op, s.xq, s.yq, nullptr, (const QParams*)s.prm, nullptr, nullptr, 0, st);
   // the output exponent sits in the planned QParams (field ey)
   const int* ey = (const int*)((const char*)s.prm + offsetof(QParams, ey));
   if (!z) {
@@ -143,56 +197,55 @@ void q_apply_affine(mb_op_s* op, const void* x, void* y, double scale, double sh
 // device-buffer call.
 // ---------------------------------------------------------------------------
 
-static void q_apply_host_pipeline(mb_op_s* op, const void* x_host, const void* x_mapped,
-                                  void* y_host, void* x_stage, void* y_stage);
+static void q_apply_host_pipeline(mb_op_s* op, const mb_op_s::HostLane& lane, const void* x_host,
+                                  const void* x_mapped, void* y_host, void* x_stage,
+                                  void* y_stage);
 
-void q_apply_host_reference(mb_op_s* op, const void* x_host, const void* x_mapped, void* y_host,
-                            void* x_stage, void* y_stage) {
-  ensure_host_groups(op);
+void q_apply_host_reference(mb_op_s* op, const mb_op_s::HostLane& lane, const void* x_host,
+                            const void* x_mapped, void* y_host, void* x_stage, void* y_stage) {
   try {
-    q_apply_host_pipeline(op, x_host, x_mapped, y_host, x_stage, y_stage);
+    q_apply_host_pipeline(op, lane, x_host, x_mapped, y_host, x_stage, y_stage);
   } catch (...) {
     // nothing may still read or write the caller's buffers once it sees the error
-    cudaStreamSynchronize(op->host_streams[1]);
-    cudaStreamSynchronize(op->host_streams[0]);
+    cudaStreamSynchronize(lane.copy);
+    cudaStreamSynchronize(lane.comp);
     throw;
   }
 }
 
-static void q_apply_host_pipeline(mb_op_s* op, const void* x_host, const void* x_mapped,
-                                  void* y_host, void* x_stage, void* y_stage) {
-  cudaStream_t comp = op->host_streams[0], copy = op->host_streams[1];
+static void q_apply_host_pipeline(mb_op_s* op, const mb_op_s::HostLane& lane, const void* x_host,
+                                  const void* x_mapped, void* y_host, void* x_stage,
+                                  void* y_stage) {
+  cudaStream_t comp = lane.comp, copy = lane.copy;
   auto& q = qscratch_for(op, comp);
   int32_t* iperm = op_iperm(op);
   const int64_t n = op->dim;
   constexpr size_t es = sizeof(double2);
-  constexpr int kChunks = 8;  // pageable x: upload chunks
   MB_CUDA(cudaMemsetAsync(q.ints, 0, sizeof(int), comp));
   if (x_mapped) {
     // page-locked x: the scatter kernel reads it over the link directly
     launch_scatter_maxexp(n, x_mapped, iperm, q.xq, q.ints, comp);
   } else {
-    Events ev(kChunks);
-    const int64_t step = (n + kChunks - 1) / kChunks;
-    for (int c = 0; c < kChunks; ++c) {
-      const int64_t i0 = std::min<int64_t>(n, c * step), i1 = std::min<int64_t>(n, i0 + step);
-      if (i1 > i0)
-        MB_CUDA(cudaMemcpyAsync((char*)x_stage + es * (size_t)i0,
-                                (const char*)x_host + es * (size_t)i0, es * (size_t)(i1 - i0),
-                                cudaMemcpyHostToDevice, copy));
-      MB_CUDA(cudaEventRecord(ev[c], copy));
-      MB_CUDA(cudaStreamWaitEvent(comp, ev[c], 0));
-      launch_scatter_maxexp(i1 - i0, (const char*)x_stage + es * (size_t)i0, iperm + i0, q.xq,
+    // pageable x: through the lane's bounce buffers, each chunk scattered once landed
+    (void)copy;
+    lane_upload(lane, x_stage, x_host, es * (size_t)n, es, [&](size_t off, size_t len, cudaEvent_t e) {
+      MB_CUDA(cudaStreamWaitEvent(comp, e, 0));
+      const int64_t i0 = (int64_t)(off / es);
+      launch_scatter_maxexp((int64_t)(len / es), (const char*)x_stage + off, iperm + i0, q.xq,
                             q.ints, comp);
-    }
+    });
   }
   launch_f64_to_q_inplace(n, q.xq, op->q_qbits, q.ints, comp);
   launch_q_plan(plan_input(op, 1.0, 0.0, 0.0, 0, 0, false), q.ints + 1, (QParams*)q.prm, comp);
   const int* ey = (const int*)((const char*)q.prm + offsetof(QParams, ey));
+  // two passes: the column pass covers the whole sector before the first group
+  void* ups = q_ups_for(op, comp);
+  if (ups) launch_upcol_q(op->view, q.xq, ups, comp);
   host_groups_run(
-      op, es, y_host, y_stage,
+      op, lane, es, y_host, y_stage,
       [&](const OpView& v) {
-        launch_apply_q(v, q.xq, q.yq, nullptr, (const QParams*)q.prm, nullptr, nullptr, 0, comp);
+        launch_apply_q(v, q.xq, q.yq, nullptr, (const QParams*)q.prm, nullptr, nullptr, 0, comp,
+                       ups);
       },
       [&](int64_t i0, int64_t i1, void* dst) {
         launch_q_to_f64(i1 - i0, q.yq, iperm + i0, ey, dst, comp);
@@ -236,7 +289,7 @@ struct QKrylov {
   QKrylov(mb_op_s* o, cudaStream_t s)
       : op(o), st(s), n(o->dim), qbits(o->q_qbits),
         partials(sizeof(double) *
-                 (size_t)std::max(q_apply_grid(o->view) * 2,
+                 (size_t)std::max(q_apply_grid(o->view) * 4,
                                   std::max(q_blas_grid(o->dim) * 2,
                                            q_multi_dot_grid(o->dim) * 2 * kQMaxBasis))),
         red_out(sizeof(double) * 2 * kQMaxBasis), maxor(sizeof(unsigned long long)),
@@ -269,6 +322,20 @@ struct QKrylov {
       std::memcpy(&m, host + ncomp, sizeof(m));
       *maxq_out = m ? std::ldexp(1.0, 64 - __builtin_clzll(m)) : 0.0;  // max < 2^bitlen(OR)
     }
+    return host;
+  }
+
+  // The apply's exact dot partials (128-bit, 4 words a block), summed and
+  // converted once, plus the max word; waits on the stream.
+  const double* fetch_apply(double* maxq_out) {
+    launch_q_reduce128(part(), grid_apply, (double*)red_out.p, st);
+    MB_CUDA(cudaMemcpyAsync(host, red_out.p, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
+    MB_CUDA(cudaMemcpyAsync(host + 2, maxor.p, sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, st));
+    MB_CUDA(cudaStreamSynchronize(st));
+    unsigned long long m;
+    std::memcpy(&m, host + 2, sizeof(m));
+    *maxq_out = m ? std::ldexp(1.0, 64 - __builtin_clzll(m)) : 0.0;  // max < 2^bitlen(OR)
     return host;
   }
 
@@ -314,10 +381,9 @@ struct QKrylov {
                             hz ? z->maxq / full : 1.0));
     MB_CUDA(cudaMemcpyAsync(prm.p, hprm, sizeof(QParams), cudaMemcpyHostToDevice, st));
     zero_max();
-    launch_apply_q(op->view, v.p, w.p, hz ? z->p : nullptr, (const QParams*)prm.p, part(),
-                   mor(), 1, st);
+    q_apply_whole(op, v.p, w.p, hz ? z->p : nullptr, (const QParams*)prm.p, part(), mor(), 1, st);
     double mq = 0.0;
-    const double* h = fetch(grid_apply, 2, &mq);
+    const double* h = fetch_apply(&mq);
     w.E = hprm->ey;
     w.maxq = std::max(mq, 1.0);
     return {h[0] * std::ldexp(1.0, v.E + w.E + 32), h[1] * std::ldexp(1.0, 2 * w.E + 32)};
@@ -664,8 +730,7 @@ int mb_op_apply_q64(mb_op_t op, const void* xq_dev, int x_exponent, void* yq_dev
     // a plan per call: the parameter block lives in per-stream scratch, and
     // the copy is ordered before the kernel on the same stream.
     MB_CUDA(cudaMemcpyAsync(s.prm, &p, sizeof(QParams), cudaMemcpyHostToDevice, st));
-    launch_apply_q(op->view, xq_dev, yq_dev, nullptr, (const QParams*)s.prm, nullptr, nullptr, 0,
-                   st);
+    q_apply_whole(op, xq_dev, yq_dev, nullptr, (const QParams*)s.prm, nullptr, nullptr, 0, st);
     *y_exponent = p.ey;
   });
 }

@@ -15,8 +15,10 @@ REF=${MANYBODY_REFERENCE:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src/algebra" ]; then
-  echo "build_ref.sh: reference sources not found under $REF" >&2
-  exit 2
+  # machines without the reference sources use the committed
+  # golden fixtures instead; nothing to build
+  echo "build_ref.sh: no reference sources under $REF (set MANYBODY_REFERENCE); skipped"
+  exit 0
 fi
 rm -rf "$OUT/src"
 mkdir -p "$OUT/src"

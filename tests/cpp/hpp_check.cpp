@@ -33,6 +33,81 @@ double rayleigh(const Op& op, const typename Op::VectorType& v) {
   return (num / den).real();
 }
 
+// The call shape of the reference's find_min_eigenpair (lanczos.h:283-290):
+// the largest eigenvalue of Negated<Op> (linear_operator.h:93-105) by the
+// Lanczos recurrence (lanczos.h:15-40) -- w = A v - beta v_prev, alpha =
+// Re<v, w>, w -= alpha v, beta = ||w||, stop at beta <= 1000 eps -- through
+// nothing but Op::apply and Op::dimension on the operator's own VectorType,
+// then the tridiagonal's largest eigenvalue by Sturm bisection.
+template <typename Op>
+struct Negated {
+  using VectorType = typename Op::VectorType;
+  using ScalarType = typename Op::ScalarType;
+  const Op& op;
+  VectorType apply(const VectorType& v) const {
+    VectorType w = op.apply(v);
+    for (auto& x : w.data) x = -x;
+    return w;
+  }
+  size_t dimension() const { return op.dimension(); }
+};
+
+inline double tridiag_largest(const std::vector<double>& a, const std::vector<double>& b) {
+  const size_t m = a.size();
+  double lo = a[0], hi = a[0];
+  for (size_t i = 0; i < m; ++i) {
+    const double r = (i ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < m ? std::fabs(b[i]) : 0.0);
+    lo = std::fmin(lo, a[i] - r);
+    hi = std::fmax(hi, a[i] + r);
+  }
+  for (int it = 0; it < 200; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    size_t below = 0;
+    double q = 1.0;
+    for (size_t i = 0; i < m; ++i) {
+      q = a[i] - mid - (i ? b[i - 1] * b[i - 1] / q : 0.0);
+      if (q == 0.0) q = -1e-300;
+      if (q < 0.0) ++below;
+    }
+    if (below == m) hi = mid;
+    else lo = mid;
+  }
+  return hi;
+}
+
+template <typename Op>
+double lanczos_largest(const Op& op, const typename Op::VectorType& b, size_t k) {
+  using V = typename Op::VectorType;
+  const size_t n = op.dimension();
+  V v(n), vp(n);
+  double nb = 0.0;
+  for (size_t i = 0; i < n; ++i) nb += std::norm(b.data[i]);
+  nb = std::sqrt(nb);
+  for (size_t i = 0; i < n; ++i) v.data[i] = b.data[i] / nb;
+  std::vector<double> alpha, beta;
+  double bprev = 0.0;
+  for (size_t j = 0; j < k; ++j) {
+    V w = op.apply(v);
+    double al = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+      w.data[i] -= bprev * vp.data[i];
+      al += (std::conj(v.data[i]) * w.data[i]).real();
+    }
+    double nw = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+      w.data[i] -= al * v.data[i];
+      nw += std::norm(w.data[i]);
+    }
+    alpha.push_back(al);
+    bprev = std::sqrt(nw);
+    if (bprev <= 1000.0 * 2.220446049250313e-16) break;
+    beta.push_back(bprev);
+    vp = v;
+    for (size_t i = 0; i < n; ++i) v.data[i] = w.data[i] / bprev;
+  }
+  return tridiag_largest(alpha, beta);
+}
+
 #define CHECK(cond)                                         \
   do {                                                      \
     if (!(cond)) {                                          \
@@ -105,6 +180,12 @@ int main(int argc, char** argv) {
   const double e0 = mbgpu::find_min_eigenpair(op, 200, seed);
   std::printf("E0 = %.12f\n", e0);
   CHECK(std::fabs(e0 - (-4.603526299989141)) < 1e-9);
+  // the same seed driven from the host through GpuHubbardOperator::apply
+  CxVec hseed(4900);
+  mbgpu::check(mb_memcpy(hseed.memptr(), seed, sizeof(std::complex<double>) * 4900, 1));
+  const double e0_host = -lanczos_largest(Negated<mbgpu::GpuHubbardOperator<CxVec>>{op}, hseed, 200);
+  std::printf("E0 (host-driven Lanczos) = %.12f\n", e0_host);
+  CHECK(std::fabs(e0_host - e0) < 1e-9);
   // HubbardMomentumFactorized, constructed as the reference's (basis, sizes,
   // t, U): the real-space ground state, reached in another orbital basis
   mbgpu::HubbardMomentumFactorized<CxVec> fact(basis, {8}, 1.0, 4.0);

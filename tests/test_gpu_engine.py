@@ -102,9 +102,72 @@ def test_autotune_picks_a_valid_shape(mb, cuda):
 def test_engine_rejects_bad_requests(mb, cuda):
     eng = mb.Engine()
     with pytest.raises(mb.MbError):
-        eng.try_submit(mb.sector((1, 4), 1, 1, 1.0, 1.0), 0, 10)   # size-1 dimension
-    with pytest.raises(mb.MbError):
         eng.try_submit(mb.sector((6,), 3, 3, 1.0, 1.0), 0, 10000)  # kmax > 512
+    with pytest.raises(mb.MbError):
+        eng.try_submit(mb.sector((6,), 3, 3, 0.0, 1.0), 0, 10)     # t = 0
+
+
+# Lattices with a size-1 dimension: the reference's HubbardModel2D/3D call
+# hopping(i, i) along it (src/algebra/fermion/model/hubbard_model.h:61-129),
+# a self bond that puts -2t n on the diagonal per spin (term counts pinned by
+# tests/algebra/test_model.cpp:58-62).
+SELF_SECTORS = [
+    ((1,), 1, 1, 4.0),        # the golden single-site sectors: the self bonds
+    ((1,), 1, 1, 3.0),        # cancel U = 4, or leave U - 4 = -1
+    ((1, 4), 2, 2, 4.0),      # 1x4: a self bond on every site, a ring of four
+    ((1, 4), 2, 1, 2.0),
+    ((1, 2, 3), 2, 1, 3.0),   # size-1, size-2 (doubled bonds) and size-3 sides
+]
+
+
+@pytest.mark.parametrize("fused", [1 << 62, 1])
+def test_size1_dimensions_batch(mb, cuda, fused):
+    """Ground states of self-bond lattices through the batch path (grouped and
+    fused applies) against the exact spectrum of the oracle's matrix and the
+    single-operator FP64 solve."""
+    exact = [exact_e0(*x) for x in SELF_SECTORS]
+    d = [mb.sector(dd, nu, nd, 1.0, u) for dd, nu, nd, u in SELF_SECTORS]
+    res = mb.batch_ground_states(d, seeds=list(range(len(d))), kmax=100, autotune=False,
+                                 fused_threshold=fused)
+    for (dd, nu, nd, u), r, e in zip(SELF_SECTORS, res, exact):
+        assert abs(r.e0 - e) <= max(1e-8 * abs(e), 1e-12), (dd, r.e0, e)
+        L = int(np.prod(dd))
+        basis = mb.FermionBasis.with_fixed_particle_number_and_spin(L, nu + nd, nu - nd)
+        op = mb.GpuHubbardOperator(basis, mb._Hubbard(1.0, u, dd), mb.PREC_F64)
+        single = mb.find_min_eigenpair(op, min(100, basis.size()), op.seed_vector(0),
+                                       want_vector=False)
+        assert abs(single.value - r.e0) <= max(1e-8 * abs(e), 1e-12), (dd, single.value, r.e0)
+
+
+def test_size1_dimensions_serve_dos(mb, cuda):
+    """A DOS request and a ground-state request on a 1x4 lattice served
+    together: moments within 1e-4 of the oracle's FP64 moments with the same
+    bounds and probes, the ground state within 1e-8."""
+    eng = mb.Engine()
+    dims, nu, nd, u = (1, 4), 2, 2, 4.0
+    M, R = 64, 2
+    rid = eng.try_submit_dos(mb.sector(dims, nu, nd, 1.0, u), n_moments=M, n_probes=R, seed=5)
+    gid = eng.try_submit(mb.sector((1, 2, 3), 2, 1, 1.0, 3.0), seed=1, kmax=200, rel_tol=1e-12)
+    while eng.step(4):
+        pass
+    mu, lo, hi, _ = eng.poll_dos(rid)
+    H = oracle.hubbard_csc(list(dims), 1.0, u, nu, nd)
+    E = np.linalg.eigvalsh(H.to_dense())
+    assert lo <= E[0] + 1e-9 and hi >= E[-1] - 1e-9
+    a = (hi - lo) / 2 * 1.01
+    b = (hi + lo) / 2
+    basis = mb.FermionBasis.with_fixed_particle_number_and_spin(4, nu + nd, nu - nd)
+    perm = basis.permutation()
+    ref = np.zeros(M)
+    for p in range(R):
+        rt = oracle.philox_phase(5, H.dim, 1 + p)
+        r = np.empty_like(rt)
+        r[perm] = rt
+        ref += H.kpm_dos_moments(r, M, a, b)
+    ref /= R * H.dim
+    assert np.max(np.abs(mu - ref)) <= 1e-4
+    e_exact = exact_e0((1, 2, 3), 2, 1, 3.0)
+    assert abs(eng.poll(gid).e0 - e_exact) <= 1e-8 * abs(e_exact)
 
 
 def test_dos_requests_match_oracle_and_mix_with_ground_states(mb, cuda):
@@ -204,3 +267,67 @@ def test_completed_queue_and_stats(mb, cuda):
         assert eng.poll(rid) is not None
     steps, wall_ms, dev_ms = eng.stats()
     assert steps > 0 and wall_ms > 0 and 0 < dev_ms <= wall_ms
+
+
+def test_persistent_step_matches_grouped_kernels(mb, cuda):
+    """The persistent fused step (one cooperative launch per batch) and the
+    grouped kernels give the same bits for every request applied warp per row
+    or row-staged in both."""
+    d = descs(mb)
+    big = 1 << 62
+    a = mb.batch_ground_states(d, seeds=list(range(len(d))), kmax=120, autotune=False,
+                               fused_threshold=big, persistent=True)
+    b = mb.batch_ground_states(d, seeds=list(range(len(d))), kmax=120, autotune=False,
+                               fused_threshold=big, persistent=False)
+    for x, y in zip(a, b):
+        assert x.e0 == y.e0 and x.e0_raw == y.e0_raw and x.steps == y.steps
+
+
+def test_same_result_alone_and_in_mix_large_request(mb, cuda):
+    """A sector of more than a million states (1D L=13, 6+6: 2,944,656) through
+    the persistent step's block-per-row path gets the same bits alone and in a
+    mix with small requests, with and without graph capture."""
+    big = mb.sector((13,), 6, 6, 1.0, 5.0)
+    small = descs(mb)[:4]
+    for use_graph in (True, False):
+        mixed = mb.batch_ground_states(small + [big], seeds=[7] * 5, kmax=60, autotune=False,
+                                       use_graph=use_graph)
+        alone = mb.batch_ground_states([big], seeds=[7], kmax=60, autotune=False,
+                                       use_graph=use_graph)[0]
+        assert alone.e0 == mixed[4].e0 and alone.e0_raw == mixed[4].e0_raw
+        assert alone.steps == mixed[4].steps
+
+
+def test_persistent_barrier_timeout_returns_status(mb, cuda):
+    """A grid-barrier wait of the persistent step that runs past its budget
+    (a budget of 0 cycles: every block that waits gives up) ends the step with
+    MB_ERR_TIMEOUT instead of hanging; the engine then refuses work, and a new
+    engine on the same GPU solves normally."""
+    eng = mb.Engine()
+    for x in descs(mb)[:4]:
+        assert eng.try_submit(x, seed=1, kmax=50) is not None
+    eng.set_wait_budget(0)
+    with pytest.raises(mb.MbError) as e:
+        eng.step(3)
+    assert e.value.status == mb.MB_ERR_TIMEOUT
+    with pytest.raises(mb.MbError) as e:
+        eng.step(1)
+    assert e.value.status == mb.MB_ERR_TIMEOUT
+    del eng
+    d = descs(mb)[:2]
+    res = mb.batch_ground_states(d, seeds=[0, 1], kmax=150, autotune=False)
+    for r, (dims, nu, nd, u) in zip(res, SECTORS[:2]):
+        ex = exact_e0(dims, nu, nd, u)
+        assert abs(r.e0 - ex) <= 1e-8 * abs(ex)
+
+
+def test_engine_autotune_persistent_shape(mb, cuda):
+    eng = mb.Engine()
+    for x in descs(mb):
+        assert eng.try_submit(x, seed=2, kmax=80) is not None
+    eng.autotune()
+    sh = eng.shape()
+    assert sh["persistent"] == 1 and sh["row_min_cols"] in (64, 128, 256)
+    assert sh["ctas_per_sm"] in (0, 1, 2) and sh["grid"] >= 1
+    while eng.step(10):
+        pass

@@ -216,3 +216,39 @@ def test_q64_host_apply_full_size_bit_identical(mb, cuda):
     assert torch.equal(yh, y)
     del x, y
     torch.cuda.empty_cache()
+
+
+def test_q64_on_a_large_dynamic_range_vector(mb, cuda):
+    """Block floating point keeps one exponent per vector, so an element far
+    below the largest keeps fewer significant bits (~56 - log2(max/|x_i|)).
+    On the converged 3x3, U = 8 ground state (components spread over many
+    decades) the Q64 apply, a Lanczos run started from it and a KPM projector
+    applied to it agree with FP64 to the FP64 bars: the error of every element
+    stays below 2^-50 of the vector's largest, and the norm-wise and energy
+    errors below 1e-13 and 1e-12."""
+    torch = cuda
+    dims, nu, nd, u = (3, 3), 4, 4, 8.0
+    _, _, op64 = make(mb, dims, 1.0, u, nu, nd, prec=0)
+    _, _, opq = make(mb, dims, 1.0, u, nu, nd, prec=2)
+    gs = mb.find_min_eigenpair(op64, 300, op64.seed_vector(0), reorth=True, conv_tol=1e-14)
+    x = gs.vector
+    a = torch.abs(x)
+    nz = a[a > 0]
+    spread = float(nz.max() / nz.min())
+    assert spread > 1e6, spread                       # a large dynamic range
+    y64 = op64.apply(x)
+    yq = opq.apply(x)
+    err = torch.abs(yq - y64)
+    assert float(err.max()) <= 2.0 ** -50 * float(torch.abs(y64).max())
+    assert float(torch.linalg.norm(yq - y64)) <= 1e-13 * float(torch.linalg.norm(y64))
+    # Lanczos from the ground state (a start vector of large dynamic range)
+    e64 = mb.find_min_eigenpair(op64, 20, x, want_vector=False).value
+    eq = mb.find_min_eigenpair(opq, 20, x, want_vector=False).value
+    assert abs(eq - e64) <= 1e-12 * abs(e64)
+    assert abs(e64 - gs.value) <= 1e-10 * abs(gs.value)
+    # the KPM Fermi projector (a 256-term Chebyshev sum) applied to it
+    lo, hi = gs.value, mb.find_max_eigenpair(op64, 200, op64.seed_vector(1), conv_tol=1e-12,
+                                             want_vector=False).value
+    p64 = mb.SparseKPMProjector(op64, 256, lo, hi, 0.5 * (lo + hi)).apply(x)
+    pq = mb.SparseKPMProjector(opq, 256, lo, hi, 0.5 * (lo + hi)).apply(x)
+    assert float(torch.linalg.norm(pq - p64)) <= 1e-12 * float(torch.linalg.norm(p64))
