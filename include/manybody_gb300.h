@@ -488,6 +488,13 @@ int mb_engine_step_fixed(mb_engine_t engine, int n_steps, int use_graph, int* n_
  * in both; a large sector (>= the fused threshold) runs its rows through the
  * block-per-row body here and the fused kernel there. */
 int mb_engine_set_persistent(mb_engine_t engine, int on);
+/* A ground-state request (with refinement) keeps its pass-one Lanczos
+ * vectors (kmax x dim complex64) when they take at most `bytes` (default
+ * 2 GiB; 0: never) and fit the device-memory budget: its Ritz vector is then
+ * summed from them (the replay's order and arithmetic: the same bits) instead
+ * of re-running the recurrence for up to kmax more steps.  Applies to
+ * requests submitted afterwards. */
+int mb_engine_set_basis_limit(mb_engine_t engine, int64_t bytes);
 /* Budget in clock64 cycles of one grid-barrier wait of the persistent step
  * (default 2^32, about two seconds).  A wait that runs past it sets the
  * step's status word; every block then returns at its next barrier and the

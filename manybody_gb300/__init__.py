@@ -169,6 +169,7 @@ SIGNATURES = {
     "mb_engine_autotune": (C.c_int, [_vp, C.POINTER(C.c_int), _dp]),
     "mb_engine_set_persistent": (C.c_int, [_vp, C.c_int]),
     "mb_engine_set_wait_budget": (C.c_int, [_vp, C.c_int64]),
+    "mb_engine_set_basis_limit": (C.c_int, [_vp, C.c_int64]),
     "mb_engine_get_shape": (C.c_int, [_vp, C.POINTER(EngineShape)]),
     "mb_engine_set_shape": (C.c_int, [_vp, C.POINTER(EngineShape)]),
     "mb_op_get_apply_shape": (C.c_int, [_vp, C.POINTER(ApplyShape)]),
@@ -1094,6 +1095,10 @@ class Engine:
         """The persistent fused step (default) or the grouped kernels."""
         _check(lib().mb_engine_set_persistent(self._h, int(bool(on))))
 
+    def set_basis_limit(self, nbytes: int):
+        """Largest pass-one Lanczos basis a ground-state request keeps (0: replay)."""
+        _check(lib().mb_engine_set_basis_limit(self._h, int(nbytes)))
+
     def set_wait_budget(self, cycles: int):
         """clock64 budget of one grid-barrier wait of the persistent step."""
         _check(lib().mb_engine_set_wait_budget(self._h, int(cycles)))
@@ -1125,13 +1130,15 @@ class Engine:
 
 def batch_ground_states(descs, seeds=None, kmax: int = 150, refine: bool = True,
                         use_graph: bool = True, autotune: bool = True, fused_threshold=None,
-                        persistent: bool = True, engine_out=None):
+                        persistent: bool = True, engine_out=None, basis_limit=None):
     """Fixed-length batched Lanczos for many sectors: returns [EngineResult]."""
     eng = Engine()
     if engine_out is not None:
         engine_out.append(eng)
     if not persistent:
         eng.set_persistent(False)
+    if basis_limit is not None:
+        eng.set_basis_limit(basis_limit)
     if fused_threshold is not None:
         eng.set_fused_threshold(fused_threshold)
     seeds = seeds if seeds is not None else [0] * len(descs)

@@ -68,6 +68,10 @@ struct SlotDesc {
   // sector's t = 1 values, per up / down state), else nullptr
   const float* self_up;
   const float* self_dn;
+  // the Lanczos vectors v_0, v_1, ... of pass one (kmax x dim), kept when the
+  // request's basis fits the engine's limit: the Ritz vector is then summed
+  // from them instead of replaying the recurrence; else nullptr
+  float2* basis;
 };
 
 constexpr int kModeIdle = kEngIdle;
@@ -459,13 +463,36 @@ k_eng_normalize(const SlotDesc* __restrict__ slots, const int2* __restrict__ ite
     if (!(b > kTol)) continue;
     const int64_t r = item.y, Dd = s.Dd;
     float2* w = s.buf[(k + 2) % 3] + r * Dd;
+    float2* vb = s.basis && k + 1 < s.kmax ? s.basis + (int64_t)(k + 1) * s.Du * Dd + r * Dd
+                                           : nullptr;
     const float ib = (float)(1.0 / b);
     for (int64_t c = lane; c < Dd; c += 32) {
       float2 o = w[c];
       o.x *= ib;
       o.y *= ib;
       w[c] = o;
+      if (vb) vb[c] = o;
     }
+  }
+}
+
+// x = y_0 v_0 + y_1 v_1 + ... + y_(m-1) v_(m-1) from the kept Lanczos
+// vectors, in the order and arithmetic of the replay (k_eng_replay_init, then
+// one fmaf per replayed step), so the Ritz vector has the replay's bits.
+__global__ void k_eng_combine(const float2* __restrict__ basis, int64_t dim, int m,
+                              const double* __restrict__ yk, float2* __restrict__ x) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < dim;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float y0 = (float)yk[0];
+    const float2 a = basis[i];
+    float2 acc = make_float2(y0 * a.x, y0 * a.y);
+    for (int j = 1; j < m; ++j) {
+      const float y = (float)yk[j];
+      const float2 v = basis[(int64_t)j * dim + i];
+      acc.x = fmaf(y, v.x, acc.x);
+      acc.y = fmaf(y, v.y, acc.y);
+    }
+    x[i] = acc;
   }
 }
 
@@ -1043,6 +1070,8 @@ __device__ void p_normalize_row(const SlotDesc& s, const SlotNow& n, int64_t r) 
   if (!(b > kTol)) return;
   const int64_t Dd = s.Dd;
   float2* w = s.buf[(k + 2) % 3] + r * Dd;
+  float2* vb = s.basis && k + 1 < n.kmax ? s.basis + (int64_t)(k + 1) * s.Du * Dd + r * Dd
+                                         : nullptr;
   const float ib = (float)(1.0 / b);
   int64_t c = lane;
   for (; c + 96 < Dd; c += 128) {
@@ -1050,13 +1079,18 @@ __device__ void p_normalize_row(const SlotDesc& s, const SlotNow& n, int64_t r) 
 #pragma unroll
     for (int q = 0; q < 4; ++q) o[q] = w[c + 32 * q];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) w[c + 32 * q] = make_float2(o[q].x * ib, o[q].y * ib);
+    for (int q = 0; q < 4; ++q) {
+      o[q] = make_float2(o[q].x * ib, o[q].y * ib);
+      w[c + 32 * q] = o[q];
+      if (vb) vb[c + 32 * q] = o[q];
+    }
   }
   for (; c < Dd; c += 32) {
     float2 o = w[c];
     o.x *= ib;
     o.y *= ib;
     w[c] = o;
+    if (vb) vb[c] = o;
   }
 }
 
@@ -1196,6 +1230,7 @@ struct EngineSlot {
   std::unique_ptr<EngBuf> vecs;   // 4 vectors: buf0..2, xacc (complex64)
   std::unique_ptr<EngBuf> scal;   // alpha, beta, yk (double x kEngMaxK each)
   std::unique_ptr<EngBuf> selfe;  // self energies times t, float: [Du] up, [Dd] down (or none)
+  std::unique_ptr<EngBuf> basis;  // pass one's Lanczos vectors (kmax x dim complex64), or none
   int64_t dim = 0, Du = 0, Dd = 0;
   int64_t bytes = 0;
   int phase = 0;                  // 0 pass one, 1 replay, 2 done, 10 DOS bounds, 11 DOS Chebyshev
@@ -1254,6 +1289,9 @@ struct mb_engine_s {
   long long wait_budget = 1LL << 32;  // clock64 cycles one barrier wait may take
   std::unique_ptr<mb::EngBuf> d_grid;  // barrier state and status (mb::EngGrid)
   bool broken = false;                 // a barrier wait ran out: requests are lost
+  // a ground-state request keeps its pass-one Lanczos vectors (kmax x dim
+  // complex64) when they take at most this many bytes (0: never)
+  int64_t basis_limit = int64_t(2) << 30;
   // ids retired since the last mb_engine_completed call
   std::vector<int64_t> newly_done;
   // step statistics: steps run, wall time of the step calls, device time of
@@ -1411,6 +1449,7 @@ void rebuild(mb_engine_s* e) {
     d.dn_sgrp = ts.fused.dn_sgrp;
     d.self_up = s.selfe ? (const float*)s.selfe->p : nullptr;
     d.self_dn = s.selfe ? (const float*)s.selfe->p + s.Du : nullptr;
+    d.basis = s.basis ? (float2*)s.basis->p : nullptr;
     if (e->persistent) {
       // the persistent step applies a sector's rows block per row when they
       // are wide (or the sector is large), else warp per row
@@ -1825,13 +1864,24 @@ void after_step(mb_engine_s* e) {
           ritz_min(a, b, s.m_ritz, &y);
           for (auto& yv : y) yv *= s.b_norm;
           MB_CUDA(cudaMemcpy(d.yk, y.data(), sizeof(double) * s.m_ritz, cudaMemcpyHostToDevice));
-          arm_slot(e, s, d, true);
-          // x = y_0 v_0, v_prev = 0
-          const int2* it = (const int2*)e->d_items->p;
-          push_slots(e);
-          k_eng_replay_init<8><<<eng_grid(d.item1 - d.item0, 8), 256, 0, e->st>>>(
-              (const SlotDesc*)e->d_slots->p, it + d.item0, d.item1 - d.item0);
-          s.phase = 1;
+          if (s.basis) {
+            // the Ritz vector from the kept Lanczos vectors (the replay's bits)
+            // and the FP64 refinement right away
+            const int64_t nb = std::max<int64_t>(1, std::min<int64_t>((s.dim + 255) / 256, 4096));
+            k_eng_combine<<<(unsigned)nb, 256, 0, e->st>>>((const float2*)s.basis->p, s.dim,
+                                                          s.m_ritz, d.yk, d.xacc);
+            MB_CUDA(cudaGetLastError());
+            s.e0 = rayleigh_fp64(e, s, d);
+            s.phase = 2;
+          } else {
+            arm_slot(e, s, d, true);
+            // x = y_0 v_0, v_prev = 0
+            const int2* it = (const int2*)e->d_items->p;
+            push_slots(e);
+            k_eng_replay_init<8><<<eng_grid(d.item1 - d.item0, 8), 256, 0, e->st>>>(
+                (const SlotDesc*)e->d_slots->p, it + d.item0, d.item1 - d.item0);
+            s.phase = 1;
+          }
         } else {
           s.phase = 2;
         }
@@ -1853,6 +1903,8 @@ void after_step(mb_engine_s* e) {
       e->in_use -= sp->bytes;
       sp->vecs.reset();
       sp->scal.reset();
+      sp->basis.reset();
+      sp->selfe.reset();
       sp->tables.reset();
       e->newly_done.push_back(sp->id);
       e->done[sp->id] = std::move(sp);
@@ -1940,10 +1992,19 @@ int mb_engine_submit_ground_state(mb_engine_t eng, const mb_sector_desc* desc, u
     s->vecs = std::make_unique<EngBuf>(4 * 8 * (size_t)s->dim);
     s->scal = std::make_unique<EngBuf>(3 * 8 * (size_t)kEngMaxK);
     upload_self_energies(*s);
+    const int64_t basis_bytes = 8 * s->kmax * s->dim;
+    if (refine && basis_bytes <= e->basis_limit && e->in_use + need + basis_bytes <= e->budget) {
+      s->basis = std::make_unique<EngBuf>((size_t)basis_bytes);
+      need += basis_bytes;
+      s->bytes = need;
+    }
     s->id = e->next_id++;
     s->t_submit = std::chrono::steady_clock::now();
     float2* base = (float2*)s->vecs->p;
     seed_vectors(e, *s, base, base + s->dim);
+    if (s->basis)  // v_0, the normalised start vector
+      MB_CUDA(cudaMemcpyAsync(s->basis->p, base + s->dim, 8 * (size_t)s->dim,
+                              cudaMemcpyDeviceToDevice, e->st));
     e->in_use += need;
     *request_id = s->id;
     // joins at the next step (rebuild keeps the others' progress)
@@ -2171,6 +2232,14 @@ int mb_engine_set_persistent(mb_engine_t eng, int on) {
     e->persistent = on != 0;
     e->dirty = true;  // new work lists; every request keeps its progress
     rebuild(e);
+  });
+}
+
+int mb_engine_set_basis_limit(mb_engine_t eng, int64_t bytes) {
+  return guard([&] {
+    auto* e = (mb_engine_s*)eng;
+    MB_REQUIRE(e && bytes >= 0, MB_ERR_INVALID_ARG, "NULL engine or negative limit");
+    e->basis_limit = bytes;
   });
 }
 

@@ -331,3 +331,17 @@ def test_engine_autotune_persistent_shape(mb, cuda):
     assert sh["ctas_per_sm"] in (0, 1, 2) and sh["grid"] >= 1
     while eng.step(10):
         pass
+
+
+@pytest.mark.parametrize("persistent", [True, False])
+def test_kept_basis_matches_replay(mb, cuda, persistent):
+    """A request that keeps its pass-one Lanczos vectors sums its Ritz vector
+    from them in the replay's order and arithmetic: the same bits as the
+    replayed recurrence, on both step paths."""
+    d = descs(mb)
+    kept = mb.batch_ground_states(d, seeds=list(range(len(d))), kmax=120, autotune=False,
+                                  persistent=persistent)
+    replay = mb.batch_ground_states(d, seeds=list(range(len(d))), kmax=120, autotune=False,
+                                    persistent=persistent, basis_limit=0)
+    for a, b in zip(kept, replay):
+        assert a.e0 == b.e0 and a.e0_raw == b.e0_raw and a.steps == b.steps
