@@ -560,7 +560,7 @@ def run_precision_extra(mb, torch, k=150):
     return {"workload": "1D L=16 N_up=N_down=8 (165,636,900 states), t=1",
             "fp32_reorth": f"full re-orthogonalisation, complex64 basis of at most {k} vectors "
                            "(1.33 GB each), FP64 alpha/beta/projections, stop at Ritz stability "
-                           "1e-10, then FP64 Rayleigh-Ritz on span{x, Hx, H^2 x}",
+                           "1e-10, then FP64 Rayleigh-Ritz on span{x, Hx, ...} (3-8 Krylov directions)",
             "fp64": "plain Lanczos on complex128 with FP64 arithmetic, Ritz stability 1e-12",
             "runs": out}
 
@@ -828,7 +828,7 @@ def run_probe(args):
         prec = {"q64_apply": mb.PREC_Q64, "fp64_apply": mb.PREC_F64,
                 "fp32_apply": mb.PREC_F32}[name]
         op = mb.GpuHubbardOperator(basis, mb._Hubbard(w["t"], w["U"], w["lattice"]), prec)
-        shape, _ = op.autotune()
+        shape = op.apply_shape()  # the default shape: a profiler distorts the tuner's timings
         x = op.seed_vector(0, order=mb.ORDER_TENSOR)
         if prec == mb.PREC_Q64:
             xq, ex = op.q64_from_f64(x, order=mb.ORDER_TENSOR)

@@ -286,7 +286,9 @@ typedef struct {
                            less than conv_tol * |E| between checks (0 = run k steps) */
   int check_every;      /* Ritz check period in steps when conv_tol > 0 (default 10) */
   int refine;           /* MB_PREC_F32 operators: 1 = finish with an FP64 Rayleigh-Ritz
-                           refinement (3 FP64 Lanczos steps from the Ritz vector; a plain
+                           refinement (FP64 Lanczos with full re-orthogonalisation from
+                           the Ritz vector: at least 3 steps, then until the lowest Ritz
+                           value settles to 1e-14, at most 8; a plain
                            run that used all k steps takes the vector from its first
                            settled checkpoint, before ghost copies of E0 form) */
 } mb_lanczos_opts;
@@ -426,8 +428,8 @@ int mb_engine_footprint(const mb_sector_desc* desc, int64_t* bytes);
  * at most kmax <= 512 steps; refine = 1 adds the replay pass that rebuilds
  * the Ritz vector (from T_m; for a run that reached kmax, from its first
  * checkpoint whose Ritz value had settled to 1e-9, before ghost copies of E0
- * form) and an FP64 Rayleigh-Ritz refinement of the energy (3 FP64 Lanczos
- * steps from that vector).  MB_ERR_CAPACITY when the budget is full (retry
+ * form) and an FP64 Rayleigh-Ritz refinement of the energy (3 to 8 FP64
+ * Lanczos steps from that vector, until the lowest Ritz value settles).  MB_ERR_CAPACITY when the budget is full (retry
  * after mb_engine_step retires requests). */
 int mb_engine_submit_ground_state(mb_engine_t engine, const mb_sector_desc* desc, uint64_t seed,
                                   int64_t kmax, double rel_tol, int refine, int64_t* request_id);

@@ -1758,8 +1758,9 @@ double rayleigh_fp64(mb_engine_s* e, EngineSlot& s, const SlotDesc& d) {
   }
   EngBuf xd(16 * (size_t)s.dim);
   k_f32_to_f64<<<256, 256, 0, e->st>>>(d.xacc, (double2*)xd.p, s.dim);
-  // Rayleigh-Ritz on span{x, Hx, H^2 x} in FP64 (first step: <x,Hx>/<x,x>)
-  return fp64_ritz_refine(v, xd.p, 3, e->st);
+  // Rayleigh-Ritz on span{x, Hx, ..., H^(j-1) x} in FP64 (3 to 8 directions,
+  // until the lowest Ritz value settles; the first is <x,Hx>/<x,x>)
+  return fp64_ritz_refine(v, xd.p, kRefineMaxSteps, e->st);
 }
 
 // Seed probe `p` of a DOS request into buf[1] and arm Chebyshev mode.
@@ -1995,6 +1996,7 @@ int mb_engine_submit_ground_state(mb_engine_t eng, const mb_sector_desc* desc, u
     const int64_t basis_bytes = 8 * s->kmax * s->dim;
     if (refine && basis_bytes <= e->basis_limit && e->in_use + need + basis_bytes <= e->budget) {
       s->basis = std::make_unique<EngBuf>((size_t)basis_bytes);
+      MB_CUDA(cudaMemsetAsync(s->basis->p, 0, (size_t)basis_bytes, e->st));
       need += basis_bytes;
       s->bytes = need;
     }

@@ -581,6 +581,10 @@ void launch_invert_perm(int64_t n, const int32_t* perm, int32_t* iperm, cudaStre
 // (Lanczos with full re-orthogonalisation), x complex128 in tensor order.
 // Returns the lowest Ritz value.
 double fp64_ritz_refine(const OpView& v, const void* x64, int steps, cudaStream_t st);
+// the refinement's Krylov steps: at least kRefineMinSteps, then until the
+// lowest Ritz value settles (1e-14 relative), at most kRefineMaxSteps
+constexpr int kRefineMinSteps = 3;
+constexpr int kRefineMaxSteps = 8;
 
 // Host tridiagonal eigensolver (implicit QL, mb_tridiag.cpp).
 bool tridiag_eig(int n, std::vector<double>& d, const std::vector<double>& e,

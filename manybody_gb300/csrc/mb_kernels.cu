@@ -653,10 +653,10 @@ k_multi_dot(int64_t n, const typename C2<TV>::type* __restrict__ V, int64_t ld, 
   using VW = typename C2<TW>::type;
   __shared__ double acc[2 * kMaxBasis];
   __shared__ double2 sw[kMdChunk];
-  // a complex64 basis against a complex128 w: w split into float hi + lo
-  // parts, products on the FP32 pipe (exact products, compensated sums),
-  // FP64 per chunk; the FP64 pipe runs at 1/57 of the FP32 rate here
-  constexpr bool kSplit = sizeof(TV) == 4 && sizeof(TW) == 8;
+  // a complex64 basis: w split into float hi + lo parts (lo = 0 for a
+  // complex64 w), products on the FP32 pipe (exact products, compensated
+  // sums), FP64 per chunk; the FP64 pipe runs at 1/57 of the FP32 rate here
+  constexpr bool kSplit = sizeof(TV) == 4;
   __shared__ float4 swf[kSplit ? kMdChunk : 1];
   for (int j = threadIdx.x; j < 2 * m; j += blockDim.x) acc[j] = 0.0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -769,10 +769,10 @@ k_multi_axpy(int64_t n, const typename C2<TV>::type* __restrict__ V, int64_t ld,
   __shared__ double sc[2 * kMaxBasis];
   for (int j = threadIdx.x; j < 2 * m; j += blockDim.x) sc[j] = c[j];
   __syncthreads();
-  // a complex64 basis under a complex128 w: the correction sum_j c_j V_j on
-  // the FP32 pipe (it is small next to w: the projections measure lost
-  // orthogonality), subtracted in FP64
-  constexpr bool kSplit = sizeof(TV) == 4 && sizeof(TW) == 8;
+  // a complex64 basis: the correction sum_j c_j V_j on the FP32 pipe (it is
+  // small next to w: the projections measure lost orthogonality), subtracted
+  // in FP64
+  constexpr bool kSplit = sizeof(TV) == 4;
   __shared__ float scf[kSplit ? 2 * kMaxBasis : 1];
   if constexpr (kSplit)
     for (int j = threadIdx.x; j < 2 * m; j += blockDim.x) scf[j] = (float)c[j];

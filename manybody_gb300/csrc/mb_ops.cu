@@ -863,7 +863,7 @@ struct Krylov {
 double fp64_ritz_refine(const OpView& v, const void* x64, int steps, cudaStream_t st) {
   const int64_t n = v.dim;
   const size_t vb = 16 * (size_t)n;
-  steps = std::max(1, std::min(steps, 8));
+  steps = std::max(1, std::min(steps, kRefineMaxSteps));
   const int ga = apply_grid(v, MB_PREC_F64), gb = blas_grid(n);
   Reducer red(std::max(std::max(ga, gb), multi_dot_grid(n)), 2 * 8 + 4);
   DevBuf basis(vb * (size_t)steps), w(vb), coef(sizeof(double) * 2 * 8);
@@ -873,7 +873,7 @@ double fp64_ritz_refine(const OpView& v, const void* x64, int steps, cudaStream_
   const double nx = std::sqrt(red.fetch(gb, 3, st)[2]);
   MB_REQUIRE(nx > 0.0, MB_ERR_ZERO_NORM, "refinement start vector has zero norm");
   launch_axpby(MB_PREC_F64, n, 1.0 / nx, 0.0, x64, 0.0, 0.0, col(0), nullptr, 0, st);
-  std::vector<double> alpha, beta;
+  std::vector<double> alpha, beta, theta;
   for (int j = 0; j < steps; ++j) {
     const double bprev = j ? beta.back() : 0.0;
     launch_apply(v, MB_PREC_F64, col(j), w.p, 1.0, 0.0, -bprev, j ? col(j - 1) : nullptr,
@@ -890,15 +890,24 @@ double fp64_ritz_refine(const OpView& v, const void* x64, int steps, cudaStream_
       nn = red.fetch(gb, 3, st)[1];
     }
     const double b = std::sqrt(nn);
+    // the lowest Ritz value so far: past kRefineMinSteps, stop once it has
+    // settled to 1e-14 relative (more steps where the start vector mixes in
+    // states the first few Krylov directions do not separate)
+    {
+      std::vector<double> d(alpha), e(beta);
+      MB_REQUIRE(tridiag_eig((int)d.size(), d, e, nullptr), MB_ERR_EIG_FAILED,
+                 "Eigenvalue decomposition of T_k failed");
+      const double th = d[0];
+      const bool settled = j + 1 >= kRefineMinSteps && !theta.empty() &&
+                           std::fabs(th - theta.back()) <= 1e-14 * std::fabs(th);
+      theta.push_back(th);
+      if (settled) break;
+    }
     if (j + 1 == steps || !(b > kTol)) break;
     beta.push_back(b);
     launch_axpby(MB_PREC_F64, n, 1.0 / b, 0.0, w.p, 0.0, 0.0, col(j + 1), nullptr, 0, st);
   }
-  const int m = (int)alpha.size();
-  std::vector<double> d(alpha), e(beta);
-  e.resize((size_t)std::max(m - 1, 0));
-  MB_REQUIRE(tridiag_eig(m, d, e, nullptr), MB_ERR_EIG_FAILED, "Eigenvalue decomposition of T_k failed");
-  return d[0];
+  return theta.back();
 }
 
 static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
@@ -967,12 +976,13 @@ static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
     }
     if (refine) {
       // FP64 refinement of the FP32 Ritz vector x: Rayleigh-Ritz on
-      // span{x, Hx, H^2 x} with FP64 vectors and arithmetic (its first step is
-      // the Rayleigh quotient <x,Hx>/<x,x>; two more Krylov directions remove
-      // the FP32 error of x to second order).
+      // span{x, Hx, ..., H^(j-1) x} with FP64 vectors and arithmetic (its
+      // first step is the Rayleigh quotient <x,Hx>/<x,x>; further Krylov
+      // directions, 3 to 8 until the lowest Ritz value settles, remove the
+      // FP32 error of x).
       DevBuf x64(16 * (size_t)op->dim);
       launch_convert(MB_PREC_F32, MB_PREC_F64, op->dim, xt.p, x64.p, st);
-      *e_out = fp64_ritz_refine(op->view, x64.p, 3, st);
+      *e_out = fp64_ritz_refine(op->view, x64.p, kRefineMaxSteps, st);
     }
     if (vec) from_tensor(op, xt.p, vec, order, st);
   }
