@@ -560,7 +560,7 @@ def run_precision_extra(mb, torch, k=150):
     return {"workload": "1D L=16 N_up=N_down=8 (165,636,900 states), t=1",
             "fp32_reorth": f"full re-orthogonalisation, complex64 basis of at most {k} vectors "
                            "(1.33 GB each), FP64 alpha/beta/projections, stop at Ritz stability "
-                           "1e-10, then FP64 Rayleigh-Ritz on span{x, Hx, ...} (3-8 Krylov directions)",
+                           "1e-10, then FP64 Rayleigh-Ritz on span{x, Hx, ...} (3-8 Krylov directions, until the lowest Ritz value settles)",
             "fp64": "plain Lanczos on complex128 with FP64 arithmetic, Ritz stability 1e-12",
             "runs": out}
 
@@ -672,11 +672,19 @@ def run_serve_extra(mb, torch, n_requests=400, rate=200.0):
         a, dims, nn, u, kind, _ = by_idx[i]
         e_conv = fp64_solve(mb, dims, nn, nn, u, 500, i, conv_tol=1e-13)
         dE.append(abs(e_served[i] - e_conv) / max(abs(e_conv), 1e-300))
-    dmu = []
+    # a rounding-error model of the FP32 Chebyshev recurrence: mu_n comes from
+    # the k = ceil(n / 2) + 1 steps behind it; each step adds up to ~8 u_32
+    # (u_32 = 2^-24: the apply's sums, the doubling and the subtraction), and
+    # an error made at step j reaches step k through U_(k-j)(H~) (norm <=
+    # k - j + 1 on [-1, 1]), so |d mu_n| <= 8 k^2 u_32
+    dmu, dmu_ratio = [], []
     for i in sorted(dos_served):
         a, dims, nn, u, kind, _ = by_idx[i]
         mu, lo, hi = dos_served[i]
-        dmu.append(float(np.max(np.abs(mu - q64_dos(mb, dims, nn, u, len(mu), i, lo, hi)))))
+        d = np.abs(mu - q64_dos(mb, dims, nn, u, len(mu), i, lo, hi))
+        k = np.ceil(np.arange(len(mu)) / 2.0) + 1.0
+        dmu.append(float(np.max(d)))
+        dmu_ratio.append(float(np.max(d / (8.0 * k * k * 2.0 ** -24))))
     t_chk = time.perf_counter() - t_chk
     return {
         "requests": len(reqs), "arrival_rate_per_s": rate,
@@ -698,6 +706,8 @@ def run_serve_extra(mb, torch, n_requests=400, rate=200.0):
         "max_abs_dmu_vs_fp64class": float(max(dmu)) if dmu else None,
         "dos_requests_checked": len(dmu),
         "dos_within_1e-4": int(sum(x <= 1e-4 for x in dmu)),
+        "max_dmu_over_fp32_rounding_bound": float(max(dmu_ratio)) if dmu_ratio else None,
+        "dos_within_fp32_rounding_bound": int(sum(x <= 1.0 for x in dmu_ratio)),
         "check_seconds": round(t_chk, 2),
     }
 
@@ -809,7 +819,7 @@ def run_reference(args):
 # workload, nothing timed (ncu measures).  Each prints one JSON line.
 # ---------------------------------------------------------------------------
 PROBES = ("q64_apply", "fp64_apply", "fp32_apply", "engine_persistent", "engine_grouped",
-          "momentum_csr")
+          "engine_fused", "momentum_csr")
 
 
 def run_probe(args):
@@ -828,7 +838,9 @@ def run_probe(args):
         prec = {"q64_apply": mb.PREC_Q64, "fp64_apply": mb.PREC_F64,
                 "fp32_apply": mb.PREC_F32}[name]
         op = mb.GpuHubbardOperator(basis, mb._Hubbard(w["t"], w["U"], w["lattice"]), prec)
-        shape = op.apply_shape()  # the default shape: a profiler distorts the tuner's timings
+        if args.apply_shape:  # a given shape; else the default (a profiler distorts the tuner's timings)
+            op.set_apply_shape(**json.loads(args.apply_shape))
+        shape = op.apply_shape()
         x = op.seed_vector(0, order=mb.ORDER_TENSOR)
         if prec == mb.PREC_Q64:
             xq, ex = op.q64_from_f64(x, order=mb.ORDER_TENSOR)
@@ -855,6 +867,18 @@ def run_probe(args):
         states = sum(math.comb(d[0], nu) * math.comb(d[0], nd) for d, nu, nd, _ in secs)
         out = {"probe": name, "requests": len(descs), "steps": args.steps, "states": states,
                "shape": eng.shape()}
+    elif name == "engine_fused":
+        # four 4x4 5+5 requests (19,079,424 states each): large enough for the
+        # grouped engine's fused apply (k_eng_fused)
+        descs = [mb.sector((4, 4), 5, 5, 1.0, u) for u in (2.0, 4.0, 6.0, 8.0)]
+        eng = mb.Engine()
+        eng.set_persistent(False)
+        for i, d in enumerate(descs):
+            eng.try_submit(d, seed=i, kmax=150, rel_tol=0.0)
+        eng.step(args.steps)
+        torch.cuda.synchronize()
+        out = {"probe": name, "requests": len(descs), "steps": args.steps,
+               "states": 4 * 19079424, "shape": eng.shape()}
     else:  # momentum_csr: the K = (0, 0) sector of 4x4, N_up = N_down = 4
         dims = (4, 4)
         basis = mb.FermionBasis.with_fixed_particle_number_spin_momentum(16, 8, 0, dims, (0, 0))
@@ -883,6 +907,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--skip-cfg2-reorth", action="store_true",
                     help="leave out the 300-step fully re-orthogonalised Lanczos at 4x4 6+6")
+    ap.add_argument("--apply-shape", default=None,
+                    help="with --probe q64_apply / fp64_apply / fp32_apply: the apply shape as "
+                         "JSON, e.g. '{\"table_bits\": 16, \"row_split\": 2}'")
     ap.add_argument("--probe", choices=PROBES,
                     help="run a few launches of one kernel's workload for a profiler "
                          "(--steps launches; nothing timed, no bench line)")

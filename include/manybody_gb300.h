@@ -425,12 +425,14 @@ int mb_engine_footprint(const mb_sector_desc* desc, int64_t* bytes);
 /* Ground state of one sector: Lanczos on -H from the Philox start vector of
  * `seed` (tensor order), until the lowest Ritz value changes by less than
  * rel_tol * |E| between checks (every 10 steps; rel_tol 0: run kmax steps),
- * at most kmax <= 512 steps; refine = 1 adds the replay pass that rebuilds
- * the Ritz vector (from T_m; for a run that reached kmax, from its first
+ * at most kmax <= 512 steps; refine = 1 adds the pass that rebuilds the
+ * Ritz vector (from T_m; for a run that reached kmax, from its first
  * checkpoint whose Ritz value had settled to 1e-9, before ghost copies of E0
- * form) and an FP64 Rayleigh-Ritz refinement of the energy (3 to 8 FP64
- * Lanczos steps from that vector, until the lowest Ritz value settles).  MB_ERR_CAPACITY when the budget is full (retry
- * after mb_engine_step retires requests). */
+ * form: summed from the kept Lanczos vectors, or by replaying the
+ * recurrence) and an FP64 Rayleigh-Ritz refinement of the energy (3 to 8
+ * FP64 Lanczos steps from that vector, until the lowest Ritz value settles).
+ * The requests finishing in one step are refined together.  MB_ERR_CAPACITY
+ * when the budget is full (retry after mb_engine_step retires requests). */
 int mb_engine_submit_ground_state(mb_engine_t engine, const mb_sector_desc* desc, uint64_t seed,
                                   int64_t kmax, double rel_tol, int refine, int64_t* request_id);
 /* Density-of-states moments of one sector: spectral bounds from 40 Lanczos

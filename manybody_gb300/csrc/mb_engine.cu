@@ -31,6 +31,10 @@
 namespace mb {
 
 constexpr int kEngMaxK = 512;  // Lanczos steps a slot can record
+// a slot's scalar table: alpha, beta, yk (kEngMaxK doubles each), then the
+// start vector's norm
+constexpr int kEngNormAt = 3 * kEngMaxK;
+constexpr size_t kEngScalBytes = sizeof(double) * (size_t)(kEngNormAt + 1);
 
 // Device descriptor of one slot (POD).
 struct SlotDesc {
@@ -631,6 +635,20 @@ __global__ void k_eng_scale(float2* __restrict__ v, int64_t n, float s) {
   }
 }
 
+// v /= sqrt(*n2), the norm's reciprocal rounded to float as the host would;
+// the norm itself to *norm_out.
+__global__ void k_eng_scale_by_norm(float2* __restrict__ v, int64_t n, const double* __restrict__ n2,
+                                    double* __restrict__ norm_out) {
+  const double nrm = sqrt(*n2);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *norm_out = nrm;
+  const float s = (float)(1.0 / nrm);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 a = v[i];
+    v[i] = make_float2(a.x * s, a.y * s);
+  }
+}
+
 __global__ void k_f32_to_f64(const float2* __restrict__ a, double2* __restrict__ b, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -1176,15 +1194,25 @@ k_eng_persistent(EngPersistArgs a) {
 // ===========================================================================
 namespace mb {
 
+// Device buffer: cudaMalloc, or (with a pool) stream-ordered from the
+// engine's memory pool, so that admitting and retiring requests neither
+// maps nor unmaps device memory nor waits for the device.
 struct EngBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t ps = nullptr;
   EngBuf() = default;
   explicit EngBuf(size_t b) : bytes(b) {
     if (b) MB_CUDA(cudaMalloc(&p, b));
   }
+  EngBuf(size_t b, cudaMemPool_t mp, cudaStream_t st) : bytes(b), pool(mp), ps(st) {
+    if (b) MB_CUDA(cudaMallocFromPoolAsync(&p, b, mp, st));
+  }
   ~EngBuf() {
-    if (p) cudaFree(p);
+    if (!p) return;
+    if (pool) cudaFreeAsync(p, ps);
+    else cudaFree(p);
   }
   EngBuf(const EngBuf&) = delete;
   EngBuf& operator=(const EngBuf&) = delete;
@@ -1228,7 +1256,7 @@ struct EngineSlot {
   int check_every = 10;
   int refine = 1;
   std::unique_ptr<EngBuf> vecs;   // 4 vectors: buf0..2, xacc (complex64)
-  std::unique_ptr<EngBuf> scal;   // alpha, beta, yk (double x kEngMaxK each)
+  std::unique_ptr<EngBuf> scal;   // alpha, beta, yk (double x kEngMaxK each), the start norm
   std::unique_ptr<EngBuf> selfe;  // self energies times t, float: [Du] up, [Dd] down (or none)
   std::unique_ptr<EngBuf> basis;  // pass one's Lanczos vectors (kmax x dim complex64), or none
   int64_t dim = 0, Du = 0, Dd = 0;
@@ -1260,6 +1288,7 @@ struct mb_engine_s {
   int64_t next_id = 1;
   // device work lists
   std::unique_ptr<mb::EngBuf> d_slots, d_items, d_part;
+  std::unique_ptr<mb::EngBuf> d_norm;  // start-vector norm partials (stream-ordered reuse)
   // the apply's work lists: rows of small sectors (warp per row) and rows of
   // medium ones (block per row, staged); large sectors use the fused kernel
   std::unique_ptr<mb::EngBuf> d_items_warp, d_items_rows;
@@ -1299,7 +1328,13 @@ struct mb_engine_s {
   int64_t stat_steps = 0;
   double stat_wall_ms = 0.0, stat_dev_ms = 0.0;
   cudaEvent_t ev[2] = {nullptr, nullptr};
+  // the requests' vectors and scalars: stream-ordered on st, memory kept by
+  // the pool between requests (returned to the device when the engine goes)
+  cudaMemPool_t pool = nullptr;
   ~mb_engine_s() {
+    slots.clear();  // their pool buffers are freed on st
+    if (st) cudaStreamSynchronize(st);
+    if (pool) cudaMemPoolDestroy(pool);
     for (cudaEvent_t x : ev)
       if (x) cudaEventDestroy(x);
     if (st) cudaStreamDestroy(st);
@@ -1361,19 +1396,22 @@ std::shared_ptr<TableSet> get_tables(mb_engine_s* e, const mb_sector_desc& d) {
 }
 
 // Device bytes of one slot: 4 complex64 vectors plus 3 x kEngMaxK doubles.
-int64_t slot_bytes(int64_t dim) { return 4 * 8 * dim + 3 * 8 * kEngMaxK; }
+int64_t slot_bytes(int64_t dim) { return 4 * 8 * dim + (int64_t)kEngScalBytes; }
 
 // The fused-apply view of a slot's sector (tables shared by its TableSet).
 // The slot's self energies (t times the sector's t = 1 values) as float.
-void upload_self_energies(EngineSlot& s) {
+void upload_self_energies(mb_engine_s* e, EngineSlot& s) {
   const TableSet& ts = *s.tables;
   if (ts.self_up1.empty()) return;
   std::vector<float> h;
   h.reserve(ts.self_up1.size() + ts.self_dn1.size());
   for (double x : ts.self_up1) h.push_back((float)(s.t * x));
   for (double x : ts.self_dn1) h.push_back((float)(s.t * x));
-  s.selfe = std::make_unique<EngBuf>(sizeof(float) * h.size());
-  MB_CUDA(cudaMemcpy(s.selfe->p, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice));
+  s.selfe = std::make_unique<EngBuf>(sizeof(float) * h.size(), e->pool, e->st);
+  // on st, after the pool hands the block over (pageable source: staged
+  // before the call returns)
+  MB_CUDA(cudaMemcpyAsync(s.selfe->p, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice,
+                          e->st));
 }
 
 OpView slot_view(const EngineSlot& s) {
@@ -1699,17 +1737,17 @@ void eng_norm2(mb_engine_s* e, const float2* v, int64_t n, double* out) {
   k_eng_sum<<<1, 1, 0, e->st>>>(out + 1, nb, out);
 }
 
-// Seeds v = buf[1] (normalised start vector) and zeroes v_prev = buf[0].
+// Seeds v = buf[1] (normalised start vector) and zeroes v_prev = buf[0],
+// all on the device (no host wait): the norm goes to the slot's scalar table
+// (kEngNormAt), which the host reads with alpha and beta once pass one ends.
+// A Philox uniform(-1, 1) vector is never zero (its entries are never all 0).
 void seed_vectors(mb_engine_s* e, EngineSlot& s, float2* b0, float2* b1) {
+  if (!e->d_norm) e->d_norm = std::make_unique<EngBuf>(sizeof(double) * (kEngNormBlocks + 1));
+  double* nb = (double*)e->d_norm->p;
   k_eng_seed<<<256, 256, 0, e->st>>>(b1, s.dim, s.seed, 1.0);
-  EngBuf nb(sizeof(double) * (kEngNormBlocks + 1));
-  eng_norm2(e, b1, s.dim, (double*)nb.p);
-  double n2 = 0.0;
-  MB_CUDA(cudaMemcpyAsync(&n2, nb.p, sizeof(double), cudaMemcpyDeviceToHost, e->st));
-  MB_CUDA(cudaStreamSynchronize(e->st));
-  s.b_norm = std::sqrt(n2);
-  MB_REQUIRE(s.b_norm > kTol, MB_ERR_ZERO_NORM, "Input vector has zero norm");
-  k_eng_scale<<<256, 256, 0, e->st>>>(b1, s.dim, (float)(1.0 / s.b_norm));
+  eng_norm2(e, b1, s.dim, nb);
+  k_eng_scale_by_norm<<<256, 256, 0, e->st>>>(b1, s.dim, nb, (double*)s.scal->p + kEngNormAt);
+  MB_CUDA(cudaGetLastError());
   MB_CUDA(cudaMemsetAsync(b0, 0, 8 * (size_t)s.dim, e->st));
 }
 
@@ -1737,30 +1775,71 @@ double ritz_min(const std::vector<double>& a, const std::vector<double>& b, int 
   return d[(size_t)m - 1];  // largest of -T: -E0
 }
 
-// FP64 Rayleigh quotient of the slot's Ritz vector on an FP64 operator view.
-double rayleigh_fp64(mb_engine_s* e, EngineSlot& s, const SlotDesc& d) {
-  const TableSet& ts = *s.tables;
-  OpView v = slot_view(s);
-  const std::vector<double> uf = u_fold_table(s.u, !(s.u * s.u < kTol * kTol), ts.basis.L);
-  EngBuf duf(sizeof(double) * uf.size());
-  MB_CUDA(cudaMemcpy(duf.p, uf.data(), sizeof(double) * uf.size(), cudaMemcpyHostToDevice));
-  v.u_fold = (const double*)duf.p;
-  std::unique_ptr<EngBuf> dself;
-  v.self_up = v.self_dn = nullptr;
-  if (!ts.self_up1.empty()) {
-    std::vector<double> h(ts.self_up1);
-    h.insert(h.end(), ts.self_dn1.begin(), ts.self_dn1.end());
-    for (double& x : h) x *= s.t;
-    dself = std::make_unique<EngBuf>(sizeof(double) * h.size());
-    MB_CUDA(cudaMemcpy(dself->p, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
-    v.self_up = (const double*)dself->p;
-    v.self_dn = (const double*)dself->p + s.Du;
+// FP64 refinement of finished ground-state requests, all at once: each
+// slot's FP64 operator view (the engine's tables, its U fold and self
+// energies in FP64) and its Ritz vector in FP64 go to fp64_refine_many,
+// which advances them in lockstep (one host wait per Krylov step for all).
+// The start vectors of a call stay under kEngRefineBytes; more requests run
+// in further calls.
+constexpr size_t kEngRefineBytes = (size_t)4 << 30;
+
+void refine_slots(mb_engine_s* e, const std::vector<size_t>& idx) {
+  size_t i0 = 0;
+  while (i0 < idx.size()) {
+    size_t xbytes = 0, i1 = i0;
+    while (i1 < idx.size()) {
+      const EngineSlot& s = *e->slots[idx[i1]];
+      const size_t b = 16 * (size_t)s.dim;
+      if (i1 > i0 && xbytes + b > kEngRefineBytes) break;
+      xbytes += b;
+      ++i1;
+    }
+    const size_t n = i1 - i0;
+    std::vector<double> tab;
+    std::vector<size_t> uoff(n), soff(n, SIZE_MAX);
+    for (size_t j = 0; j < n; ++j) {
+      const EngineSlot& s = *e->slots[idx[i0 + j]];
+      const TableSet& ts = *s.tables;
+      const std::vector<double> uf = u_fold_table(s.u, !(s.u * s.u < kTol * kTol), ts.basis.L);
+      uoff[j] = tab.size();
+      tab.insert(tab.end(), uf.begin(), uf.end());
+      if (!ts.self_up1.empty()) {
+        soff[j] = tab.size();
+        for (double x : ts.self_up1) tab.push_back(s.t * x);
+        for (double x : ts.self_dn1) tab.push_back(s.t * x);
+      }
+    }
+    EngBuf dtab(sizeof(double) * tab.size(), e->pool, e->st), xs(xbytes, e->pool, e->st);
+    MB_CUDA(cudaMemcpyAsync(dtab.p, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice,
+                            e->st));
+    std::vector<RefineProblem> probs(n);
+    char* xp = (char*)xs.p;
+    for (size_t j = 0; j < n; ++j) {
+      const EngineSlot& s = *e->slots[idx[i0 + j]];
+      const SlotDesc& d = e->h_slots[idx[i0 + j]];
+      RefineProblem& p = probs[j];
+      p.v = slot_view(s);
+      p.v.u_fold = (const double*)dtab.p + uoff[j];
+      p.v.self_up = p.v.self_dn = nullptr;
+      if (soff[j] != SIZE_MAX) {
+        p.v.self_up = (const double*)dtab.p + soff[j];
+        p.v.self_dn = p.v.self_up + s.Du;
+      }
+      k_f32_to_f64<<<256, 256, 0, e->st>>>(d.xacc, (double2*)xp, s.dim);
+      MB_CUDA(cudaGetLastError());
+      p.x = xp;
+      xp += 16 * (size_t)s.dim;
+    }
+    // Rayleigh-Ritz on span{x, Hx, ...} in FP64 (its first step is the
+    // Rayleigh quotient of the Ritz vector)
+    fp64_refine_many(probs.data(), (int)n, e->st);
+    for (size_t j = 0; j < n; ++j) {
+      EngineSlot& s = *e->slots[idx[i0 + j]];
+      s.e0 = probs[j].e0;
+      s.phase = 2;
+    }
+    i0 = i1;
   }
-  EngBuf xd(16 * (size_t)s.dim);
-  k_f32_to_f64<<<256, 256, 0, e->st>>>(d.xacc, (double2*)xd.p, s.dim);
-  // Rayleigh-Ritz on span{x, Hx, ..., H^(j-1) x} in FP64 (3 to 8 directions,
-  // until the lowest Ritz value settles; the first is <x,Hx>/<x,x>)
-  return fp64_ritz_refine(v, xd.p, kRefineMaxSteps, e->st);
 }
 
 // Seed probe `p` of a DOS request into buf[1] and arm Chebyshev mode.
@@ -1833,6 +1912,7 @@ void after_step(mb_engine_s* e) {
   check_grid(e);
   fetch_slots(e);
   bool changed = false;
+  std::vector<size_t> to_refine;  // slots whose Ritz vectors are ready
   for (size_t i = 0; i < e->slots.size(); ++i) {
     EngineSlot& s = *e->slots[i];
     SlotDesc& d = e->h_slots[i];
@@ -1855,6 +1935,8 @@ void after_step(mb_engine_s* e) {
         std::vector<double> a((size_t)m), b((size_t)m), y;
         MB_CUDA(cudaMemcpy(a.data(), d.alpha, sizeof(double) * m, cudaMemcpyDeviceToHost));
         MB_CUDA(cudaMemcpy(b.data(), d.beta, sizeof(double) * m, cudaMemcpyDeviceToHost));
+        MB_CUDA(cudaMemcpy(&s.b_norm, (const double*)s.scal->p + kEngNormAt, sizeof(double),
+                           cudaMemcpyDeviceToHost));
         s.e_raw = -ritz_min(a, b, m, nullptr);
         s.e0 = s.e_raw;
         if (s.refine && m > 0) {
@@ -1866,14 +1948,13 @@ void after_step(mb_engine_s* e) {
           for (auto& yv : y) yv *= s.b_norm;
           MB_CUDA(cudaMemcpy(d.yk, y.data(), sizeof(double) * s.m_ritz, cudaMemcpyHostToDevice));
           if (s.basis) {
-            // the Ritz vector from the kept Lanczos vectors (the replay's bits)
-            // and the FP64 refinement right away
+            // the Ritz vector from the kept Lanczos vectors (the replay's
+            // bits); the FP64 refinement after this pass over the slots
             const int64_t nb = std::max<int64_t>(1, std::min<int64_t>((s.dim + 255) / 256, 4096));
             k_eng_combine<<<(unsigned)nb, 256, 0, e->st>>>((const float2*)s.basis->p, s.dim,
                                                           s.m_ritz, d.yk, d.xacc);
             MB_CUDA(cudaGetLastError());
-            s.e0 = rayleigh_fp64(e, s, d);
-            s.phase = 2;
+            to_refine.push_back(i);
           } else {
             arm_slot(e, s, d, true);
             // x = y_0 v_0, v_prev = 0
@@ -1889,13 +1970,13 @@ void after_step(mb_engine_s* e) {
         changed = true;
       }
     } else if (s.phase == 1 && d.mode == kModeIdle) {
-      s.e0 = rayleigh_fp64(e, s, d);
-      s.phase = 2;
+      to_refine.push_back(i);
       changed = true;
     } else if ((s.phase == 10 || s.phase == 11) && d.mode == kModeIdle) {
       dos_transition(e, s, d, changed);
     }
   }
+  if (!to_refine.empty()) refine_slots(e, to_refine);
   // retire finished slots
   for (size_t i = 0; i < e->slots.size();) {
     if (e->slots[i]->phase == 2) {
@@ -1940,6 +2021,15 @@ int mb_engine_create(int64_t device_bytes_budget, mb_engine_t* out) {
     e->budget = device_bytes_budget > 0 ? device_bytes_budget : (int64_t)(free_b * 0.8);
     MB_CUDA(cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking));
     for (cudaEvent_t& x : e->ev) MB_CUDA(cudaEventCreate(&x));
+    int dev = 0;
+    MB_CUDA(cudaGetDevice(&dev));
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    MB_CUDA(cudaMemPoolCreate(&e->pool, &props));
+    uint64_t keep = UINT64_MAX;  // freed blocks stay in the pool for the next requests
+    MB_CUDA(cudaMemPoolSetAttribute(e->pool, cudaMemPoolAttrReleaseThreshold, &keep));
     *out = (mb_engine_t)e.release();
   });
 }
@@ -1990,13 +2080,13 @@ int mb_engine_submit_ground_state(mb_engine_t eng, const mb_sector_desc* desc, u
     s->Dd = s->tables->basis.down.D;
     s->dim = s->tables->basis.dim;
     s->bytes = need;
-    s->vecs = std::make_unique<EngBuf>(4 * 8 * (size_t)s->dim);
-    s->scal = std::make_unique<EngBuf>(3 * 8 * (size_t)kEngMaxK);
-    upload_self_energies(*s);
+    s->vecs = std::make_unique<EngBuf>(4 * 8 * (size_t)s->dim, e->pool, e->st);
+    s->scal = std::make_unique<EngBuf>(kEngScalBytes, e->pool, e->st);
+    upload_self_energies(e, *s);
     const int64_t basis_bytes = 8 * s->kmax * s->dim;
     if (refine && basis_bytes <= e->basis_limit && e->in_use + need + basis_bytes <= e->budget) {
-      s->basis = std::make_unique<EngBuf>((size_t)basis_bytes);
-      MB_CUDA(cudaMemsetAsync(s->basis->p, 0, (size_t)basis_bytes, e->st));
+      // every vector the Ritz sum reads is written by pass one first
+      s->basis = std::make_unique<EngBuf>((size_t)basis_bytes, e->pool, e->st);
       need += basis_bytes;
       s->bytes = need;
     }
@@ -2046,9 +2136,9 @@ int mb_engine_submit_dos(mb_engine_t eng, const mb_sector_desc* desc, int64_t n_
     s->n_probes = (int)n_probes;
     s->padding = padding;
     s->bytes = need;
-    s->vecs = std::make_unique<EngBuf>(4 * 8 * (size_t)s->dim);
-    s->scal = std::make_unique<EngBuf>(3 * 8 * (size_t)kEngMaxK);
-    upload_self_energies(*s);
+    s->vecs = std::make_unique<EngBuf>(4 * 8 * (size_t)s->dim, e->pool, e->st);
+    s->scal = std::make_unique<EngBuf>(kEngScalBytes, e->pool, e->st);
+    upload_self_energies(e, *s);
     s->id = e->next_id++;
     s->t_submit = std::chrono::steady_clock::now();
     s->phase = 10;

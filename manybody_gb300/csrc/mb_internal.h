@@ -576,15 +576,24 @@ struct Events {
 };
 void launch_invert_perm(int64_t n, const int32_t* perm, int32_t* iperm, cudaStream_t st);
 
-// FP64 refinement of a ground-state estimate: Rayleigh-Ritz on the Krylov
-// space span{x, Hx, ..., H^(steps-1) x} with FP64 vectors and arithmetic
-// (Lanczos with full re-orthogonalisation), x complex128 in tensor order.
-// Returns the lowest Ritz value.
-double fp64_ritz_refine(const OpView& v, const void* x64, int steps, cudaStream_t st);
+// FP64 refinement of ground-state estimates: Rayleigh-Ritz on the Krylov
+// space span{x, Hx, H^2 x, ...} with FP64 vectors and arithmetic (Lanczos with
+// full re-orthogonalisation), x complex128 in tensor order.  fp64_refine_many
+// runs many problems in lockstep (one host wait per step for all) and writes
+// each one's lowest Ritz value to e0.
+struct RefineProblem {
+  OpView v;
+  const void* x;
+  double e0;  // out
+};
+void fp64_refine_many(RefineProblem* probs, int count, cudaStream_t st);
+double fp64_ritz_refine(const OpView& v, const void* x64, cudaStream_t st);
 // the refinement's Krylov steps: at least kRefineMinSteps, then until the
-// lowest Ritz value settles (1e-14 relative), at most kRefineMaxSteps
+// lowest Ritz value moves by at most kRefineSettle relative (above the
+// rounding of FP64 dot products over a sector), at most kRefineMaxSteps
 constexpr int kRefineMinSteps = 3;
 constexpr int kRefineMaxSteps = 8;
+constexpr double kRefineSettle = 1e-13;
 
 // Host tridiagonal eigensolver (implicit QL, mb_tridiag.cpp).
 bool tridiag_eig(int n, std::vector<double>& d, const std::vector<double>& e,

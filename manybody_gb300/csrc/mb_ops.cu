@@ -860,54 +860,158 @@ struct Krylov {
   }
 };
 
-double fp64_ritz_refine(const OpView& v, const void* x64, int steps, cudaStream_t st) {
-  const int64_t n = v.dim;
-  const size_t vb = 16 * (size_t)n;
-  steps = std::max(1, std::min(steps, kRefineMaxSteps));
-  const int ga = apply_grid(v, MB_PREC_F64), gb = blas_grid(n);
-  Reducer red(std::max(std::max(ga, gb), multi_dot_grid(n)), 2 * 8 + 4);
-  DevBuf basis(vb * (size_t)steps), w(vb), coef(sizeof(double) * 2 * 8);
-  auto col = [&](int j) { return (char*)basis.p + vb * (size_t)j; };
-  // v0 = x / ||x||
-  launch_dot(MB_PREC_F64, n, x64, x64, red.p(), st);
-  const double nx = std::sqrt(red.fetch(gb, 3, st)[2]);
-  MB_REQUIRE(nx > 0.0, MB_ERR_ZERO_NORM, "refinement start vector has zero norm");
-  launch_axpby(MB_PREC_F64, n, 1.0 / nx, 0.0, x64, 0.0, 0.0, col(0), nullptr, 0, st);
-  std::vector<double> alpha, beta, theta;
-  for (int j = 0; j < steps; ++j) {
-    const double bprev = j ? beta.back() : 0.0;
-    launch_apply(v, MB_PREC_F64, col(j), w.p, 1.0, 0.0, -bprev, j ? col(j - 1) : nullptr,
-                 red.p(), 1, st);
-    const double a = red.fetch(ga, 3, st)[0];
-    alpha.push_back(a);
-    launch_axpby(MB_PREC_F64, n, -a, 0.0, col(j), 1.0, 0.0, w.p, nullptr, 0, st);
-    double nn = 0.0;
-    for (int pass = 0; pass < 2; ++pass) {  // CGS2 against the j+1 basis vectors
-      launch_multi_dot(MB_PREC_F64, MB_PREC_F64, n, basis.p, n, j + 1, w.p, red.p(), st);
-      launch_reduce(red.p(), multi_dot_grid(n), 2 * (j + 1), (double*)coef.p, st);
-      launch_multi_axpy(MB_PREC_F64, MB_PREC_F64, n, basis.p, n, j + 1, (const double*)coef.p, w.p,
-                        red.p(), st);
-      nn = red.fetch(gb, 3, st)[1];
+// ---------------------------------------------------------------------------
+// FP64 Rayleigh-Ritz refinement of ground-state estimates, many at once.  A
+// problem is an operator view and a start vector x (complex128, tensor
+// order).  Its Krylov space span{x, Hx, H^2 x, ...} is built with FP64
+// vectors and arithmetic: Lanczos with full re-orthogonalisation (w = H q_j
+// orthogonalised against q_0..q_j by classical Gram-Schmidt applied twice;
+// alpha_j is w's total coefficient on q_j, beta_j the norm of what remains).
+// After each step the lowest eigenvalue of T_(j+1) is the estimate; steps
+// continue until it settles to kRefineSettle relative (at least kRefineMinSteps),
+// the space breaks down, or the problem's step budget (kRefineMaxSteps,
+// fewer where the basis would pass kRefineBasisBytes).  The problems advance
+// in lockstep: their kernels queue on one stream and the host waits once per
+// step for all of them.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr size_t kRefineBasisBytes = (size_t)24 << 30;  // one problem's basis at most
+constexpr size_t kRefineChunkBytes = (size_t)4 << 30;   // bases of problems run together
+
+struct RefineRun {
+  RefineProblem* p;
+  int64_t n;
+  size_t vb;
+  int steps, cap;
+  char* q = nullptr;     // cap vectors
+  double* dc = nullptr;  // device: 2 passes x 2 cap coefficients, then 3 reduced norms
+  double* hc = nullptr;  // host mirror
+  std::vector<double> alpha, beta;
+  double theta = 0.0;
+  bool done = false;
+  char* col(int k) const { return q + vb * (size_t)k; }
+};
+}  // namespace
+
+static void refine_chunk(std::vector<RefineRun>& runs, cudaStream_t st) {
+  size_t qbytes = 0, cwords = 0;
+  int pblocks = 1, pcomps = 3;
+  for (auto& r : runs) {
+    qbytes += r.vb * (size_t)r.cap;
+    cwords += 4 * (size_t)r.cap + 4;
+    pblocks = std::max({pblocks, apply_grid(r.p->v, MB_PREC_F64), blas_grid(r.n),
+                        multi_dot_grid(r.n)});
+    pcomps = std::max(pcomps, 2 * r.cap);
+  }
+  DevBuf qbuf(qbytes), cbuf(sizeof(double) * cwords), part(sizeof(double) * (size_t)pblocks * pcomps);
+  double* host = nullptr;
+  MB_CUDA(cudaMallocHost(&host, sizeof(double) * cwords));
+  struct HostFree {
+    double* h;
+    ~HostFree() { cudaFreeHost(h); }
+  } host_free{host};
+  {
+    size_t qo = 0, co = 0;
+    for (auto& r : runs) {
+      r.q = (char*)qbuf.p + qo;
+      r.dc = (double*)cbuf.p + co;
+      r.hc = host + co;
+      qo += r.vb * (size_t)r.cap;
+      co += 4 * (size_t)r.cap + 4;
     }
-    const double b = std::sqrt(nn);
-    // the lowest Ritz value so far: past kRefineMinSteps, stop once it has
-    // settled to 1e-14 relative (more steps where the start vector mixes in
-    // states the first few Krylov directions do not separate)
-    {
-      std::vector<double> d(alpha), e(beta);
+  }
+  double* pp = (double*)part.p;
+  auto sync_all = [&] {
+    MB_CUDA(cudaMemcpyAsync(host, cbuf.p, sizeof(double) * cwords, cudaMemcpyDeviceToHost, st));
+    MB_CUDA(cudaStreamSynchronize(st));
+  };
+  auto nn_off = [](const RefineRun& r) { return 4 * (size_t)r.cap; };
+  // q_0 = x / |x|
+  for (auto& r : runs) {
+    MB_CUDA(cudaMemcpyAsync(r.col(0), r.p->x, r.vb, cudaMemcpyDeviceToDevice, st));
+    launch_dot(MB_PREC_F64, r.n, r.col(0), r.col(0), pp, st);
+    launch_reduce(pp, blas_grid(r.n), 3, r.dc + nn_off(r), st);
+  }
+  sync_all();
+  for (auto& r : runs) {
+    const double nx = std::sqrt(r.hc[nn_off(r) + 2]);
+    MB_REQUIRE(nx > 0.0, MB_ERR_ZERO_NORM, "refinement start vector has zero norm");
+    launch_axpby(MB_PREC_F64, r.n, 1.0 / nx, 0.0, r.col(0), 0.0, 0.0, r.col(0), nullptr, 0, st);
+  }
+  for (int j = 0;; ++j) {
+    bool any = false;
+    for (auto& r : runs) {
+      if (r.done) continue;
+      any = true;
+      // w = H q_j in the next basis slot, then w -= Q Q^H w twice against
+      // q_0..q_j: the passes' coefficients at dc[0..) and dc[2 cap..), the
+      // norm of the rest at dc[4 cap + 1]
+      void* w = r.col(j + 1);
+      launch_apply(r.p->v, MB_PREC_F64, r.col(j), w, 1.0, 0.0, 0.0, nullptr, nullptr, 0, st);
+      for (int pass = 0; pass < 2; ++pass) {
+        double* c = r.dc + 2 * (size_t)r.cap * pass;
+        launch_multi_dot(MB_PREC_F64, MB_PREC_F64, r.n, r.q, r.n, j + 1, w, pp, st);
+        launch_reduce(pp, multi_dot_grid(r.n), 2 * (j + 1), c, st);
+        launch_multi_axpy(MB_PREC_F64, MB_PREC_F64, r.n, r.q, r.n, j + 1, c, w, pp, st);
+      }
+      launch_reduce(pp, blas_grid(r.n), 3, r.dc + nn_off(r), st);
+    }
+    if (!any) break;
+    sync_all();
+    for (auto& r : runs) {
+      if (r.done) continue;
+      r.alpha.push_back(r.hc[2 * j] + r.hc[2 * (size_t)r.cap + 2 * j]);
+      const double b = std::sqrt(r.hc[nn_off(r) + 1]);
+      std::vector<double> d(r.alpha), e(r.beta);
       MB_REQUIRE(tridiag_eig((int)d.size(), d, e, nullptr), MB_ERR_EIG_FAILED,
                  "Eigenvalue decomposition of T_k failed");
-      const double th = d[0];
-      const bool settled = j + 1 >= kRefineMinSteps && !theta.empty() &&
-                           std::fabs(th - theta.back()) <= 1e-14 * std::fabs(th);
-      theta.push_back(th);
-      if (settled) break;
+      const bool settled = j + 1 >= kRefineMinSteps && std::fabs(d[0] - r.theta) <= kRefineSettle * std::fabs(d[0]);
+      r.theta = d[0];
+      if (settled || j + 1 >= r.steps || !(b > kTol)) {
+        r.done = true;
+        r.p->e0 = r.theta;
+        continue;
+      }
+      r.beta.push_back(b);
+      launch_axpby(MB_PREC_F64, r.n, 1.0 / b, 0.0, r.col(j + 1), 0.0, 0.0, r.col(j + 1), nullptr, 0, st);
     }
-    if (j + 1 == steps || !(b > kTol)) break;
-    beta.push_back(b);
-    launch_axpby(MB_PREC_F64, n, 1.0 / b, 0.0, w.p, 0.0, 0.0, col(j + 1), nullptr, 0, st);
   }
-  return theta.back();
+}
+
+void fp64_refine_many(RefineProblem* probs, int count, cudaStream_t st) {
+  std::vector<RefineRun> chunk;
+  size_t chunk_bytes = 0;
+  for (int i = 0; i <= count; ++i) {
+    RefineRun r{};
+    size_t rb = 0;
+    if (i < count) {
+      RefineProblem& p = probs[i];
+      r.p = &p;
+      r.n = p.v.dim;
+      r.vb = 16 * (size_t)r.n;
+      const int64_t fit = (int64_t)(kRefineBasisBytes / std::max<size_t>(r.vb, 1)) - 1;
+      r.steps = (int)std::max<int64_t>(kRefineMinSteps, std::min<int64_t>(kRefineMaxSteps, fit));
+      r.cap = r.steps + 1;
+      rb = r.vb * (size_t)r.cap;
+    }
+    if (i == count || (!chunk.empty() && chunk_bytes + rb > kRefineChunkBytes)) {
+      if (!chunk.empty()) refine_chunk(chunk, st);
+      chunk.clear();
+      chunk_bytes = 0;
+    }
+    if (i < count) {
+      chunk.push_back(std::move(r));
+      chunk_bytes += rb;
+    }
+  }
+}
+
+double fp64_ritz_refine(const OpView& v, const void* x64, cudaStream_t st) {
+  RefineProblem p{};
+  p.v = v;
+  p.x = x64;
+  fp64_refine_many(&p, 1, st);
+  return p.e0;
 }
 
 static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
@@ -982,7 +1086,7 @@ static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
       // FP32 error of x).
       DevBuf x64(16 * (size_t)op->dim);
       launch_convert(MB_PREC_F32, MB_PREC_F64, op->dim, xt.p, x64.p, st);
-      *e_out = fp64_ritz_refine(op->view, x64.p, kRefineMaxSteps, st);
+      *e_out = fp64_ritz_refine(op->view, x64.p, st);
     }
     if (vec) from_tensor(op, xt.p, vec, order, st);
   }
