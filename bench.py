@@ -474,7 +474,9 @@ def run_cfg2_reorth_extra(mb, torch, k=300):
 def run_momentum_extra(mb, torch):
     """4x4, 6+6, U=8 on the total-momentum sector K = (0, 0) (the sector of the
     ground state): the sector basis and its H built on the GPU, the apply in
-    FP64 and FP32, the ground state by plain Lanczos to Ritz stability 1e-12."""
+    FP64, FP32 and block floating point (Q64: exact integer sums of the +-U/N
+    entries), the ground state by plain Lanczos to Ritz stability 1e-12 in
+    FP64 and Q64."""
     dims = (4, 4)
     model = mb.HubbardModelMomentum(1.0, 8.0, dims)
     t0 = time.perf_counter()
@@ -483,7 +485,7 @@ def run_momentum_extra(mb, torch):
     out = {"workload": "2D 4x4, U=8, N_up=N_down=6, total momentum (0,0)", "dim": basis.size(),
            "basis_seconds": round(t_basis, 3)}
     stream = torch.cuda.current_stream()
-    for name, prec in (("f64", mb.PREC_F64), ("f32", mb.PREC_F32)):
+    for name, prec in (("f64", mb.PREC_F64), ("f32", mb.PREC_F32), ("q64", mb.PREC_Q64)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         op = mb.GpuHubbardOperator(basis, model, prec)
@@ -494,12 +496,13 @@ def run_momentum_extra(mb, torch):
         _, per = time_loop(torch, stream, lambda: op.apply(x, out=y, stream=stream.cuda_stream), 10, 3)
         out[f"{name}_build_seconds"] = round(t_build, 3)
         out[f"{name}_apply_ms"] = round(statistics.mean(per), 3)
-        if prec == mb.PREC_F64:
+        if prec != mb.PREC_F32:
             t0 = time.perf_counter()
             r = mb.find_min_eigenpair(op, 300, x, conv_tol=1e-12, check_every=10,
                                       want_vector=False)
-            out.update({"e0": r.value, "lanczos_steps": r.steps,
-                        "e0_seconds": round(time.perf_counter() - t0, 3)})
+            pre = "" if prec == mb.PREC_F64 else "q64_"
+            out.update({pre + "e0": r.value, pre + "lanczos_steps": r.steps,
+                        pre + "e0_seconds": round(time.perf_counter() - t0, 3)})
         del op, x, y
         torch.cuda.empty_cache()
     return out
@@ -819,7 +822,7 @@ def run_reference(args):
 # workload, nothing timed (ncu measures).  Each prints one JSON line.
 # ---------------------------------------------------------------------------
 PROBES = ("q64_apply", "fp64_apply", "fp32_apply", "engine_persistent", "engine_grouped",
-          "engine_fused", "momentum_csr")
+          "engine_fused", "momentum_csr", "momentum_csr_q64")
 
 
 def run_probe(args):
@@ -879,10 +882,11 @@ def run_probe(args):
         torch.cuda.synchronize()
         out = {"probe": name, "requests": len(descs), "steps": args.steps,
                "states": 4 * 19079424, "shape": eng.shape()}
-    else:  # momentum_csr: the K = (0, 0) sector of 4x4, N_up = N_down = 4
+    else:  # momentum_csr(_q64): the K = (0, 0) sector of 4x4, N_up = N_down = 4
         dims = (4, 4)
         basis = mb.FermionBasis.with_fixed_particle_number_spin_momentum(16, 8, 0, dims, (0, 0))
-        op = mb.GpuHubbardOperator(basis, mb.HubbardModelMomentum(1.0, 8.0, dims), mb.PREC_F64)
+        prec = mb.PREC_Q64 if name.endswith("q64") else mb.PREC_F64
+        op = mb.GpuHubbardOperator(basis, mb.HubbardModelMomentum(1.0, 8.0, dims), prec)
         x = op.seed_vector(0)
         y = op.empty()
         for _ in range(args.steps):

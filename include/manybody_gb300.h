@@ -127,8 +127,10 @@ int mb_hubbard_create(const int64_t* dims, int ndim, double t, double u, mb_mode
  * c_{k2,dn} c_{k1,up}, eps(k) = -2t sum_d cos(2 pi k_d / L_d), on momentum
  * orbitals (same lattice indexing).  With a momentum-sector basis it gives
  * the sector's H: mb_compute_matrix_elements_csr (built on the GPU) and
- * mb_op_create (MB_PREC_F64 / MB_PREC_F32: the sector's H kept on the device
- * in signed-column sparse form; reference order).  With a whole (N_up,
+ * mb_op_create (the sector's H kept on the device in signed-column sparse
+ * form; reference order; MB_PREC_F64, MB_PREC_F32, or MB_PREC_Q64 with the
+ * +-U/N entries summed exactly as integers and the diagonal as a per-row
+ * fixed-point coefficient).  With a whole (N_up,
  * N_down) basis (mb_basis_create_fixed_spin) it gives the operator of the
  * reference's HubbardMomentumFactorized (src/numerics/
  * hubbard_momentum_factorized.h:32-249, t sum eps(k) n_k + (U/N) sum_q
@@ -470,8 +472,9 @@ int mb_engine_set_warps(mb_engine_t engine, int warps_per_block);
 int mb_engine_set_fused_threshold(mb_engine_t engine, int64_t min_states);
 /* Times the step's apply at each shape on the current requests and keeps the
  * fastest; *ms = its time per apply.  Persistent step: row_min_cols in
- * {64, 128, 256} x ctas_per_sm in {all that fit, 2, 1}, timed with apply-only
- * launches (they change no request's progress); grouped kernels: warps per
+ * {64, 128, 256} x ctas_per_sm in {all that fit, 2} (set_shape takes any
+ * ctas_per_sm), timed with apply-only launches (they change no request's
+ * progress); grouped kernels: warps per
  * block in {2, 4, 8, 16}.  *chosen = the grouped kernels' warps per block. */
 int mb_engine_autotune(mb_engine_t engine, int* chosen, double* ms);
 /* n_steps steps with no host round trip between them (fixed-length batches).

@@ -2396,16 +2396,18 @@ int mb_engine_autotune(mb_engine_t eng, int* chosen, double* ms) {
       double best = 1e300;
       int best_cols = e->p_row_min_cols, best_ctas = e->p_ctas_per_sm;
       try {
+        // one CTA per SM never won on the measured mixes and costs the most to
+        // time; one warm-up and two timed launches a candidate
         for (int cols : {64, 128, 256}) {
           e->p_row_min_cols = cols;
           e->dirty = true;
           rebuild(e);  // new work lists; the block count below needs none
-          for (int ctas : {0, 2, 1}) {
+          for (int ctas : {0, 2}) {
             e->p_ctas_per_sm = ctas;
             e->p_grid = std::max(1, (ctas > 0 ? std::min(ctas, e->p_bps) : e->p_bps) * e->p_sms);
             launch_persistent(e, 1, true);
             MB_CUDA(cudaEventRecord(a, e->st));
-            for (int rep = 0; rep < 3; ++rep) launch_persistent(e, 1, true);
+            for (int rep = 0; rep < 2; ++rep) launch_persistent(e, 1, true);
             MB_CUDA(cudaEventRecord(b, e->st));
             MB_CUDA(cudaEventSynchronize(b));
             float t = 0.f;
@@ -2429,7 +2431,7 @@ int mb_engine_autotune(mb_engine_t eng, int* chosen, double* ms) {
       e->dirty = true;
       rebuild(e);
       if (chosen) *chosen = e->warps;
-      if (ms) *ms = best / 3.0;
+      if (ms) *ms = best / 2.0;
       return;
     }
     rebuild(e);

@@ -454,6 +454,11 @@ struct mb_op_s {
   int q_qbits = 62;                 // mantissas kept below 2^q_qbits
   bool q_has_double = false;        // any bond of multiplicity 2
   std::vector<double> ufold_host;   // U fold table (host copy)
+  // the plan's hop coefficient -q_t (lattice: t; signed-column CSR: -off) and
+  // diagonal table ufold_host[0..q_L] (lattice: the U fold by double
+  // occupancy; CSR: the diagonal's least and largest entries)
+  double q_t = 0.0;
+  int q_L = 0;
   struct QScratch {
     void* xq = nullptr;
     void* yq = nullptr;

@@ -20,6 +20,8 @@ namespace mb {
 // Q64 hooks (mb_q64_ops.cu)
 void q_op_prepare(mb_op_s* op, const mb_model_s* m, const HopTable& tu, const HopTable& td);
 void q_op_release(mb_op_s* op);
+void q_op_prepare_csr(mb_op_s* op, int64_t max_row_entries, double diag_min, double diag_max,
+                      double off);
 void q_apply_host_reference(mb_op_s* op, const mb_op_s::HostLane& lane, const void* x_host,
                             const void* x_mapped, void* y_host, void* x_stage, void* y_stage);
 int q_apply_grid(const OpView& v);
@@ -334,8 +336,6 @@ static void build_momentum(mb_op_s* op, const mb_basis_s* b, const mb_model_s* m
 // A momentum-sector operator: natural (sector reference) order, signed-column
 // CSR on the device.
 static void build_momentum_op(mb_op_s* op, const mb_basis_s* basis, const mb_model_s* model) {
-  MB_REQUIRE(op->precision != MB_PREC_Q64, MB_ERR_INVALID_ARG,
-             "momentum-sector operators take MB_PREC_F64 or MB_PREC_F32");
   MB_CUDA(cudaGetDevice(&op->device));
   op->L = basis->L;
   op->n_up = basis->n_up;
@@ -352,6 +352,19 @@ static void build_momentum_op(mb_op_s* op, const mb_basis_s* basis, const mb_mod
   op->view.L = basis->L;
   MomBuild mbld;
   build_momentum(op, basis, model, mbld);
+  if (op->precision == MB_PREC_Q64) {
+    // the block-floating-point plan: the longest row bounds the hop sums, the
+    // diagonal's range bounds its coefficients
+    int64_t longest = 0;
+    for (int64_t i = 0; i < mbld.n; ++i)
+      longest = std::max(longest, mbld.row_ptr[(size_t)i + 1] - mbld.row_ptr[(size_t)i]);
+    std::vector<double> d((size_t)mbld.n);
+    if (mbld.n)
+      MB_CUDA(cudaMemcpy(d.data(), mbld.diag, sizeof(double) * (size_t)mbld.n, cudaMemcpyDeviceToHost));
+    const auto mm = std::minmax_element(d.begin(), d.end());
+    q_op_prepare_csr(op, longest, d.empty() ? 0.0 : *mm.first, d.empty() ? 0.0 : *mm.second,
+                     model->u_over_n);
+  }
 }
 
 // The total-momentum sectors of a whole (N_up, N_down) basis on the model's
@@ -454,12 +467,16 @@ static void ensure_perm(mb_op_s* op) {
   op->perm = (int32_t*)p;
 }
 
+// the permutation tensor -> reference order (nullptr: the operator's own index
+// is the reference order)
 int32_t* op_perm(mb_op_s* op) {
+  if (op->natural_order) return nullptr;
   ensure_perm(op);
   return op->perm;
 }
 
 int32_t* op_iperm(mb_op_s* op) {
+  if (op->natural_order) return nullptr;
   ensure_perm(op);
   std::lock_guard<std::mutex> lk(op->mu);
   if (!op->iperm) {

@@ -596,7 +596,117 @@ static int smem_optin() {
   return v;
 }
 
+// ---------------------------------------------------------------------------
+// The Q64 apply of a signed-column CSR operator (a momentum sector: every
+// off-diagonal entry is +-off, the diagonal apart):
+//   P = c1 S + dq x + c3 z   (128-bit),   y = round(P / 2^sh)
+// with S the exact int64 sum of +-x over the row's entries (a negative entry
+// adds x ^ -1 = -x - 1, its count added back once) and dq = round(2^G scale
+// (diag - shift)) the row's fixed-point diagonal, formed here in FP64 once a
+// row.  kQCsrLanes lanes a row, 256 threads a block, the fused exact dots as
+// in k_apply_q.  The integer hop sums run on the integer pipe, where the
+// complex128 kernel's adds wait on this GPU's FP64 pipe.
+// ---------------------------------------------------------------------------
+constexpr int kQCsrThreads = 256;
+constexpr int kQCsrLanes = 8;
+
+template <int DOTS, bool HAS_Z>
+__global__ void __launch_bounds__(kQCsrThreads)
+k_csr_apply_q(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+              const double* __restrict__ diag, const longlong2* __restrict__ x, longlong2* y,
+              const longlong2* __restrict__ z, const QParams* __restrict__ prm,
+              double* __restrict__ partials, unsigned long long* __restrict__ max_or) {
+  constexpr int LPR = kQCsrLanes, RPW = 32 / LPR;
+  const int lane = threadIdx.x & (LPR - 1);
+  const int sub = (threadIdx.x & 31) / LPR;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const long long c1 = prm->c1, c3 = prm->c3;
+  const int sh = prm->sh, G = prm->G;
+  const double scale = prm->scale, shift = prm->shift;
+  __int128 a_xy = 0, a_yy = 0;
+  unsigned long long mor = 0;
+  // the warp steps through its rows together (the shuffles need every lane)
+  for (int64_t rb = w0 * RPW; rb < n; rb += nw * RPW) {
+    const int64_t row = rb + sub;
+    const bool live = row < n;
+    long long sr = 0, si = 0;
+    int neg = 0;
+    if (live) {
+      const int64_t k1 = rp[row + 1];
+#pragma unroll 4
+      for (int64_t k = rp[row] + lane; k < k1; k += LPR) {
+        const uint32_t e = (uint32_t)__ldg(&ci[k]);
+        const long long m = (int)e >> 31;  // 0 or -1
+        const longlong2 v = __ldg(&x[e & 0x7FFFFFFFu]);
+        sr += v.x ^ m;
+        si += v.y ^ m;
+        neg -= (int)m;
+      }
+    }
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) {
+      sr += __shfl_xor_sync(0xffffffffu, sr, o);
+      si += __shfl_xor_sync(0xffffffffu, si, o);
+      neg += __shfl_xor_sync(0xffffffffu, neg, o);
+    }
+    if (live && lane == 0) {
+      sr += neg;
+      si += neg;
+      const longlong2 xv = x[row];
+      const long long dq = llrint(ldexp(scale * (diag[row] - shift), G));
+      __int128 pr = (__int128)c1 * sr + (__int128)dq * xv.x;
+      __int128 pi = (__int128)c1 * si + (__int128)dq * xv.y;
+      if (HAS_Z) {
+        const longlong2 zv = z[row];
+        pr += (__int128)c3 * zv.x;
+        pi += (__int128)c3 * zv.y;
+      }
+      longlong2 out;
+      out.x = round_shift(pr, sh);
+      out.y = round_shift(pi, sh);
+      y[row] = out;
+      if (DOTS & 1) a_xy += prod_hi(xv.x, out.x) + prod_hi(xv.y, out.y);
+      if (DOTS & 2) a_yy += prod_hi(out.x, out.x) + prod_hi(out.y, out.y);
+      if (DOTS & 4) mor |= mag(out.x) | mag(out.y);
+    }
+  }
+  if (DOTS) q_block_reduce_exact(a_xy, a_yy, mor, reinterpret_cast<long long*>(partials), max_or);
+}
+
+static int q_csr_grid(int64_t n) {
+  const int64_t rows_per_block = kQCsrThreads / kQCsrLanes;
+  int64_t g = (n + rows_per_block - 1) / rows_per_block;
+  const int64_t cap = (int64_t)sm_count() * 16;
+  if (g > cap) g = cap;
+  return (int)(g > 0 ? g : 1);
+}
+
+template <int DOTS, bool HAS_Z>
+static void q_csr_t(const OpView& v, const void* x, void* y, const void* z, const QParams* prm,
+                    double* partials, unsigned long long* max_or, cudaStream_t st) {
+  k_csr_apply_q<DOTS, HAS_Z><<<q_csr_grid(v.dim), kQCsrThreads, 0, st>>>(
+      v.dim, v.csr_row, v.csr_col, v.csr_diag, (const longlong2*)x, (longlong2*)y,
+      (const longlong2*)z, prm, partials, max_or);
+  MB_CUDA(cudaGetLastError());
+}
+
+static void launch_csr_apply_q(const OpView& v, const void* x, void* y, const void* z,
+                               const QParams* prm, double* partials, unsigned long long* max_or,
+                               int dots, cudaStream_t st) {
+  MB_REQUIRE(!v.csr_val, MB_ERR_INVALID_ARG,
+             "MB_PREC_Q64 takes only signed-column sparse operators (momentum sectors)");
+  if (z) {
+    if (dots) q_csr_t<7, true>(v, x, y, z, prm, partials, max_or, st);
+    else q_csr_t<0, true>(v, x, y, z, prm, partials, max_or, st);
+  } else {
+    if (dots) q_csr_t<7, false>(v, x, y, z, prm, partials, max_or, st);
+    else q_csr_t<0, false>(v, x, y, z, prm, partials, max_or, st);
+  }
+}
+
 int q_apply_grid(const OpView& v) {
+  if (v.csr_row) return q_csr_grid(v.dim);
   const int split = v.row_split > 1 ? v.row_split : 1;
   int64_t g = sm_count();
   if (g > v.Du * split) g = v.Du * split;
@@ -701,6 +811,10 @@ void launch_upcol_q(const OpView& v, const void* x, void* ups, cudaStream_t st) 
 void launch_apply_q(const OpView& v, const void* x, void* y, const void* z, const QParams* prm,
                     double* partials, unsigned long long* max_or, int dots, cudaStream_t st,
                     const void* ups) {
+  if (v.csr_row) {
+    launch_csr_apply_q(v, x, y, z, prm, partials, max_or, dots, st);
+    return;
+  }
   const size_t row = sizeof(longlong2) * (size_t)(v.Dd + kSlicedPads) + 2048;
   const size_t lists = sizeof(uint32_t) * (size_t)((v.max_up_list + 3) & ~3);
   if (ups) {
@@ -748,6 +862,8 @@ __host__ __device__ void q_plan(QParams* p, const QPlanInput& in) {
   for (int k = in.L + 1; k <= kMaxOrbitals; ++k) p->cq[k] = 0;
   p->c3 = in.has_z ? llrint(ldexp(c3r, G)) : 0;
   p->G = G;
+  p->scale = in.scale;
+  p->shift = in.shift;
   p->ex = in.ex;
   p->ey = ey;
   p->ez = in.ez;

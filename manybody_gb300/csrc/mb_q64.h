@@ -23,6 +23,9 @@ struct QParams {
   int G;
   int ex, ey, ez;
   int pad;
+  // the plan's scale and shift: a sparse-matrix operator's per-row diagonal
+  // coefficient round(2^G scale (diag - shift)) is formed in its kernel
+  double scale, shift;
 };
 
 struct QPlanInput {

@@ -61,6 +61,18 @@ void q_op_prepare(mb_op_s* op, const mb_model_s* m, const HopTable& tu, const Ho
   op->q_has_double = false;
   for (const auto& b : m->bonds) op->q_has_double = op->q_has_double || b.mult == 2;
   op->ufold_host = u_fold_table(m->u, m->has_u, op->L);
+  op->q_t = op->t;
+  op->q_L = op->L;
+}
+
+void q_op_prepare_csr(mb_op_s* op, int64_t max_row_entries, double diag_min, double diag_max,
+                      double off) {
+  op->q_wmax = (double)std::max<int64_t>(max_row_entries, 1);
+  op->q_qbits = 62 - (op->q_wmax > 1.0 ? ceil_log2(op->q_wmax) : 0);
+  op->q_has_double = false;
+  op->ufold_host = {diag_min, diag_max};
+  op->q_t = -off;
+  op->q_L = 1;
 }
 
 void q_op_release(mb_op_s* op) {
@@ -79,13 +91,13 @@ static QPlanInput plan_input(const mb_op_s* op, double scale, double shift, doub
   QPlanInput in{};
   in.x_frac = std::min(x_frac, 1.0);
   in.z_frac = std::min(z_frac, 1.0);
-  in.t = op->t;
+  in.t = op->q_t;
   in.scale = scale;
   in.shift = shift;
   in.beta = beta;
-  for (int k = 0; k <= op->L; ++k) in.ufold[k] = op->ufold_host[(size_t)k];
+  for (int k = 0; k <= op->q_L; ++k) in.ufold[k] = op->ufold_host[(size_t)k];
   in.w_max = op->q_wmax;
-  in.L = op->L;
+  in.L = op->q_L;
   in.ex = ex;
   in.ez = ez;
   in.has_z = has_z ? 1 : 0;

@@ -6,7 +6,9 @@ Krylov drivers.
 
 Tolerances: structure and off-diagonal values (+-U/N) bit-exact; diagonal
 values <= 1e-14 |H|max (the reference sums the same terms in its own order);
-apply <= 1e-13 ||y|| (FP64), <= 2e-6 ||y|| (FP32); E0 <= 1e-10 |E0|.
+apply <= 1e-13 ||y|| (FP64 and the block-floating-point Q64), <= 2e-6 ||y||
+(FP32); E0 <= 1e-10 |E0| (Q64 against FP64: 1e-12); DOS moments Q64 against
+FP64 <= 1e-10.
 """
 import numpy as np
 import pytest
@@ -48,7 +50,7 @@ def test_momentum_matrix_elements_match_reference(mb, cuda, name):
 
 
 @pytest.mark.parametrize("name", momentum_cases())
-@pytest.mark.parametrize("prec,tol", [(0, 1e-13), (1, 2e-6)])
+@pytest.mark.parametrize("prec,tol", [(0, 1e-13), (1, 2e-6), (2, 1e-13)])
 def test_momentum_operator_apply(mb, cuda, name, prec, tol):
     torch = cuda
     g = load_golden(name)
@@ -57,7 +59,7 @@ def test_momentum_operator_apply(mb, cuda, name, prec, tol):
     n = op.dimension()
     rng = np.random.default_rng(3)
     x = rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)
-    dt = torch.complex64 if prec else torch.complex128
+    dt = torch.complex64 if prec == 1 else torch.complex128
     y = op.apply(torch.tensor(x, dtype=dt, device="cuda")).cpu().numpy()
     ref = ref_csr(g) @ x
     assert np.linalg.norm(y - ref) <= tol * max(np.linalg.norm(ref), 1e-300)
@@ -97,10 +99,36 @@ def test_momentum_ground_state_matches_real_space(mb, cuda):
     assert abs(best - e_real) <= 1e-10 * abs(e_real)
 
 
-def test_momentum_operator_rejects_q64_and_mixed_models(mb, cuda):
+def test_q64_momentum_sector_matches_fp64(mb, cuda):
+    """4x4, N_up = N_down = 4, K = (0, 0) (207,184 states): the block-floating-
+    point sector operator (exact integer sums of the +-U/N entries, the
+    diagonal as a per-row fixed-point coefficient) gives the FP64 operator's
+    apply, ground state and DOS moments."""
+    torch = cuda
+    dims = [4, 4]
+    b = mb.FermionBasis.with_fixed_particle_number_spin_momentum(16, 8, 0, dims, (0, 0))
+    model = mb.HubbardModelMomentum(1.0, 8.0, dims)
+    f64 = mb.GpuHubbardOperator(b, model, mb.PREC_F64)
+    q64 = mb.GpuHubbardOperator(b, model, mb.PREC_Q64)
+    x = f64.seed_vector(5)
+    y64, yq = f64.apply(x), q64.apply(x)
+    assert float(torch.linalg.norm(yq - y64)) <= 1e-13 * float(torch.linalg.norm(y64))
+    # affine form: 0.5 (H - 1.5) x + 0.25 z through both
+    z = f64.seed_vector(6)
+    a64 = f64.apply_affine(x, 0.5, 1.5, 0.25, z)
+    aq = q64.apply_affine(x, 0.5, 1.5, 0.25, z)
+    assert float(torch.linalg.norm(aq - a64)) <= 1e-13 * float(torch.linalg.norm(a64))
+    e64 = mb.find_min_eigenpair(f64, 300, x, conv_tol=1e-13, want_vector=False).value
+    eq = mb.find_min_eigenpair(q64, 300, x, conv_tol=1e-13, want_vector=False).value
+    assert abs(eq - e64) <= 1e-12 * abs(e64)
+    lo, hi = e64 - 0.5, 60.0
+    m64 = mb.kpm_dos_moments(f64, 64, 2, 7, lo, hi, 0.01)
+    mq = mb.kpm_dos_moments(q64, 64, 2, 7, lo, hi, 0.01)
+    assert np.max(np.abs(np.asarray(mq) - np.asarray(m64))) <= 1e-10
+
+
+def test_momentum_operator_rejects_mixed_models(mb, cuda):
     b = mb.FermionBasis.with_fixed_particle_number_spin_momentum(4, 2, 0, [4], [0])
-    with pytest.raises(mb.MbError):
-        mb.GpuHubbardOperator(b, mb.HubbardModelMomentum(1.0, 2.0, [4]), mb.PREC_Q64)
     with pytest.raises(mb.MbError):
         mb.GpuHubbardOperator(b, mb.HubbardModel(1.0, 2.0, 4))
     with pytest.raises(mb.MbError):  # a whole basis as well: no Q64 for momentum space
