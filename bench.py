@@ -491,11 +491,13 @@ def run_momentum_extra(mb, torch):
         op = mb.GpuHubbardOperator(basis, model, prec)
         torch.cuda.synchronize()
         t_build = time.perf_counter() - t0
+        shape, _ = op.autotune()  # lanes a CSR row
         x = op.seed_vector(0)
         y = op.empty()
         _, per = time_loop(torch, stream, lambda: op.apply(x, out=y, stream=stream.cuda_stream), 10, 3)
         out[f"{name}_build_seconds"] = round(t_build, 3)
         out[f"{name}_apply_ms"] = round(statistics.mean(per), 3)
+        out[f"{name}_csr_lanes"] = shape["csr_lanes"]
         if prec != mb.PREC_F32:
             t0 = time.perf_counter()
             r = mb.find_min_eigenpair(op, 300, x, conv_tol=1e-12, check_every=10,

@@ -253,7 +253,11 @@ typedef struct {
                       words into its own shared buffer (cp.async) while it
                       finishes the current one (MB_PREC_Q64, one pass, 32-bit
                       entries, where the buffers fit beside the row) */
-  int reserved[3];
+  int csr_lanes;  /* operators held as a sparse matrix (momentum sectors,
+                     mb_op_create_csr): lanes a row, 4, 8, 16 or 32 (0: the
+                     precision's default, 4 complex128 / 8 otherwise); must be
+                     0 for lattice operators */
+  int reserved[2];
 } mb_apply_shape;
 int mb_op_get_apply_shape(mb_op_t op, mb_apply_shape* shape);
 int mb_op_set_apply_shape(mb_op_t op, const mb_apply_shape* shape);

@@ -82,7 +82,8 @@ class EngineShape(C.Structure):
 class ApplyShape(C.Structure):
     """mb_apply_shape: how a lattice operator's H|psi> runs on the GPU."""
     _fields_ = [("passes", C.c_int), ("row_split", C.c_int), ("table_bits", C.c_int),
-                ("prefetch", C.c_int), ("table_stage", C.c_int), ("reserved", C.c_int * 3)]
+                ("prefetch", C.c_int), ("table_stage", C.c_int), ("csr_lanes", C.c_int),
+                ("reserved", C.c_int * 2)]
 
 
 # name -> (restype, argtypes); every exported symbol of include/manybody_gb300.h.
@@ -697,14 +698,14 @@ class GpuHubbardOperator:
         sh = ApplyShape()
         _check(lib().mb_op_get_apply_shape(self._h, C.byref(sh)))
         return {"passes": sh.passes, "row_split": sh.row_split, "table_bits": sh.table_bits,
-                "prefetch": sh.prefetch, "table_stage": sh.table_stage}
+                "prefetch": sh.prefetch, "table_stage": sh.table_stage, "csr_lanes": sh.csr_lanes}
 
     def set_apply_shape(self, passes: int = 1, row_split: int = 1, table_bits: int = 32,
-                        prefetch: int = 0, table_stage: int = 0):
+                        prefetch: int = 0, table_stage: int = 0, csr_lanes: int = 0):
         """Choose the apply's kernel shape (mb_op_set_apply_shape)."""
         sh = ApplyShape()
         sh.passes, sh.row_split, sh.table_bits = passes, row_split, table_bits
-        sh.prefetch, sh.table_stage = prefetch, table_stage
+        sh.prefetch, sh.table_stage, sh.csr_lanes = prefetch, table_stage, csr_lanes
         _check(lib().mb_op_set_apply_shape(self._h, C.byref(sh)))
 
     def autotune(self, stream=None):
@@ -714,7 +715,8 @@ class GpuHubbardOperator:
         ms = C.c_double()
         _check(lib().mb_op_autotune(self._h, self._stream(stream), C.byref(sh), C.byref(ms)))
         return ({"passes": sh.passes, "row_split": sh.row_split, "table_bits": sh.table_bits,
-                 "prefetch": sh.prefetch, "table_stage": sh.table_stage}, ms.value)
+                 "prefetch": sh.prefetch, "table_stage": sh.table_stage,
+                 "csr_lanes": sh.csr_lanes}, ms.value)
 
     def q64_mantissa_bits(self) -> int:
         b = C.c_int()

@@ -351,6 +351,9 @@ struct OpView {
   // of its column, plus a separate diagonal (the momentum-sector operators).
   const double* csr_diag;
   double csr_off;
+  // lanes a CSR row (4, 8, 16 or 32; 0: the precision's default), chosen by
+  // the apply autotuner
+  int csr_lanes;
   // Block-diagonal operators (all spin projections): n_blocks sub-views on
   // consecutive slices of the vector, sub_off[b] their element offsets (host
   // arrays; launch_apply loops over them).

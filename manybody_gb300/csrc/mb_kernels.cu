@@ -312,7 +312,7 @@ static bool apply_staged(const OpView& v, int precision) {
   return apply_smem(v, precision, true) + 1024 <= (size_t)max_smem_optin();
 }
 
-static int csr_grid(int64_t n, int precision);
+static int csr_grid(const OpView& v, int precision);
 
 int apply_grid(const OpView& v, int precision) {
   if (v.n_blocks) {
@@ -320,7 +320,7 @@ int apply_grid(const OpView& v, int precision) {
     for (int b = 0; b < v.n_blocks; ++b) g += apply_grid(v.sub[b], precision);
     return g;
   }
-  if (v.csr_row) return csr_grid(v.dim, precision);
+  if (v.csr_row) return csr_grid(v, precision);
   int64_t g = (int64_t)num_sms() * (precision == MB_PREC_F32 ? kApplyCtasPerSm<float> : 1);
   if (g > v.Du) g = v.Du;
   return (int)(g > 0 ? g : 1);
@@ -464,25 +464,42 @@ k_csr_apply(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict
   }
 }
 
-static int csr_grid(int64_t n, int precision) {
-  const int64_t rows_per_block =
-      kCsrThreads / (precision == MB_PREC_F32 ? csr_lanes<float>() : csr_lanes<double>());
+// the lanes a row of this operator's CSR apply takes
+static int csr_lanes_of(const OpView& v, int precision) {
+  if (v.csr_lanes) return v.csr_lanes;
+  return precision == MB_PREC_F32 ? csr_lanes<float>() : csr_lanes<double>();
+}
+
+static int csr_grid(const OpView& v, int precision) {
+  const int64_t n = v.dim;
+  const int64_t rows_per_block = kCsrThreads / csr_lanes_of(v, precision);
   int64_t g = (n + rows_per_block - 1) / rows_per_block;
   const int64_t cap = (int64_t)num_sms() * 16;
   if (g > cap) g = cap;
   return (int)(g > 0 ? g : 1);
 }
 
-template <typename T, int DOTS>
-static void csr_apply_t(const OpView& v, const void* x, void* y, double scale, double shift,
+template <typename T, int DOTS, int LPR>
+static void csr_apply_l(const OpView& v, const void* x, void* y, double scale, double shift,
                         double beta, const void* z, double* partials, cudaStream_t st) {
   using V2 = typename C2<T>::type;
   const V2* val = sizeof(T) == 8 ? (const V2*)v.csr_val : (const V2*)v.csr_val_f;
-  k_csr_apply<T, DOTS, csr_lanes<T>()><<<csr_grid(v.dim, sizeof(T) == 4 ? MB_PREC_F32 : MB_PREC_F64),
-                                         kCsrThreads, 0, st>>>(
+  k_csr_apply<T, DOTS, LPR><<<csr_grid(v, sizeof(T) == 4 ? MB_PREC_F32 : MB_PREC_F64),
+                              kCsrThreads, 0, st>>>(
       v.dim, v.csr_row, v.csr_col, val, v.csr_diag, (T)v.csr_off, (const V2*)x, (V2*)y,
       (T)scale, (T)shift, (T)beta, (const V2*)z, partials);
   MB_CUDA(cudaGetLastError());
+}
+
+template <typename T, int DOTS>
+static void csr_apply_t(const OpView& v, const void* x, void* y, double scale, double shift,
+                        double beta, const void* z, double* partials, cudaStream_t st) {
+  switch (csr_lanes_of(v, sizeof(T) == 4 ? MB_PREC_F32 : MB_PREC_F64)) {
+    case 4: csr_apply_l<T, DOTS, 4>(v, x, y, scale, shift, beta, z, partials, st); break;
+    case 8: csr_apply_l<T, DOTS, 8>(v, x, y, scale, shift, beta, z, partials, st); break;
+    case 16: csr_apply_l<T, DOTS, 16>(v, x, y, scale, shift, beta, z, partials, st); break;
+    default: csr_apply_l<T, DOTS, 32>(v, x, y, scale, shift, beta, z, partials, st); break;
+  }
 }
 
 template <typename T>

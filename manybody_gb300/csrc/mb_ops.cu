@@ -352,6 +352,12 @@ static void build_momentum_op(mb_op_s* op, const mb_basis_s* basis, const mb_mod
   op->view.L = basis->L;
   MomBuild mbld;
   build_momentum(op, basis, model, mbld);
+  // the apply autotuner's cache key: the sector (lattice, fillings, momentum)
+  op->tune_key = "momentum";
+  for (int64_t d : model->dims) op->tune_key += "_" + std::to_string(d);
+  op->tune_key += " n" + std::to_string(basis->n_up) + "+" + std::to_string(basis->n_down) + " K";
+  for (int64_t k : basis->kvec) op->tune_key += "_" + std::to_string(k);
+  op->tune_key += " prec" + std::to_string(op->precision);
   if (op->precision == MB_PREC_Q64) {
     // the block-floating-point plan: the longest row bounds the hop sums, the
     // diagonal's range bounds its coefficients
@@ -1308,6 +1314,7 @@ int mb_op_get_apply_shape(mb_op_t op, mb_apply_shape* shape) {
     shape->table_bits = op->view.table_bits == 16 ? 16 : 32;
     shape->prefetch = op->view.up_prefetch ? 1 : 0;
     shape->table_stage = op->view.table_stage ? 1 : 0;
+    shape->csr_lanes = op->view.csr_lanes;
   });
 }
 
@@ -1324,6 +1331,11 @@ int mb_op_set_apply_shape(mb_op_t op, const mb_apply_shape* shape) {
                "prefetch must be 0 or 1");
     MB_REQUIRE(shape->table_stage == 0 || shape->table_stage == 1, MB_ERR_INVALID_ARG,
                "table_stage must be 0 or 1");
+    MB_REQUIRE(shape->csr_lanes == 0 || shape->csr_lanes == 4 || shape->csr_lanes == 8 ||
+                   shape->csr_lanes == 16 || shape->csr_lanes == 32,
+               MB_ERR_INVALID_ARG, "csr_lanes must be 0, 4, 8, 16 or 32");
+    MB_REQUIRE(shape->csr_lanes == 0 || (op->view.csr_row && !op->view.n_blocks),
+               MB_ERR_INVALID_ARG, "csr_lanes applies to operators held as one sparse matrix");
     const bool lattice = !op->view.csr_row && !op->view.n_blocks && op->view.dn_sell;
     const bool tuned = shape->passes != 1 || shape->row_split != 1 || shape->table_bits != 32;
     if (tuned)
@@ -1352,6 +1364,7 @@ int mb_op_set_apply_shape(mb_op_t op, const mb_apply_shape* shape) {
     op->view.table_bits = shape->table_bits;
     op->view.up_prefetch = shape->prefetch;
     op->view.table_stage = shape->table_stage;
+    op->view.csr_lanes = shape->csr_lanes;
   });
 }
 
@@ -1367,6 +1380,17 @@ static std::map<std::string, std::pair<mb_apply_shape, double>> g_tune_cache;
 
 static std::vector<mb_apply_shape> tune_candidates(const mb_op_s* op) {
   std::vector<mb_apply_shape> out;
+  if (op->view.csr_row) {  // one sparse matrix: the lanes a row
+    for (int lanes : {4, 8, 16, 32}) {
+      mb_apply_shape s{};
+      s.passes = 1;
+      s.row_split = 1;
+      s.table_bits = 32;
+      s.csr_lanes = lanes;
+      out.push_back(s);
+    }
+    return out;
+  }
   for (int pf = 0; pf <= 1; ++pf) {
     if (op->precision != MB_PREC_Q64) {
       mb_apply_shape s{};
@@ -1458,6 +1482,7 @@ int mb_op_autotune(mb_op_t op, void* stream, mb_apply_shape* chosen, double* bes
         k.table_bits = op->view.table_bits == 16 ? 16 : 32;
         k.prefetch = op->view.up_prefetch;
         k.table_stage = op->view.table_stage;
+        k.csr_lanes = op->view.csr_lanes;
         return k;
       }();
       try {
@@ -1467,6 +1492,7 @@ int mb_op_autotune(mb_op_t op, void* stream, mb_apply_shape* chosen, double* bes
           op->view.table_bits = c.table_bits;
           op->view.up_prefetch = c.prefetch;
           op->view.table_stage = c.table_stage;
+          op->view.csr_lanes = c.csr_lanes;
           auto run = [&] {
             if (op->precision == MB_PREC_Q64) q_tune_apply(op, x, y, prm, st);
             else launch_apply(op->view, op->precision, x, y, 1.0, 0.0, 0.0, nullptr, nullptr, 0, st);
@@ -1496,6 +1522,7 @@ int mb_op_autotune(mb_op_t op, void* stream, mb_apply_shape* chosen, double* bes
         op->view.table_bits = keep.table_bits;
         op->view.up_prefetch = keep.prefetch;
         op->view.table_stage = keep.table_stage;
+        op->view.csr_lanes = keep.csr_lanes;
         for (void* p : own) cudaFree(p);
         throw;
       }
@@ -1515,6 +1542,7 @@ int mb_op_autotune(mb_op_t op, void* stream, mb_apply_shape* chosen, double* bes
       op->view.table_bits = best.table_bits;
       op->view.up_prefetch = best.prefetch;
       op->view.table_stage = best.table_stage;
+      op->view.csr_lanes = best.csr_lanes;
     }
     if (chosen) *chosen = best;
     if (best_ms) *best_ms = best_t;

@@ -608,15 +608,15 @@ static int smem_optin() {
 // complex128 kernel's adds wait on this GPU's FP64 pipe.
 // ---------------------------------------------------------------------------
 constexpr int kQCsrThreads = 256;
-constexpr int kQCsrLanes = 8;
+constexpr int kQCsrLanes = 8;  // lanes a row unless the operator's shape says otherwise
 
-template <int DOTS, bool HAS_Z>
+template <int DOTS, bool HAS_Z, int LPR>
 __global__ void __launch_bounds__(kQCsrThreads)
 k_csr_apply_q(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
               const double* __restrict__ diag, const longlong2* __restrict__ x, longlong2* y,
               const longlong2* __restrict__ z, const QParams* __restrict__ prm,
               double* __restrict__ partials, unsigned long long* __restrict__ max_or) {
-  constexpr int LPR = kQCsrLanes, RPW = 32 / LPR;
+  constexpr int RPW = 32 / LPR;
   const int lane = threadIdx.x & (LPR - 1);
   const int sub = (threadIdx.x & 31) / LPR;
   const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -674,21 +674,35 @@ k_csr_apply_q(int64_t n, const int64_t* __restrict__ rp, const int32_t* __restri
   if (DOTS) q_block_reduce_exact(a_xy, a_yy, mor, reinterpret_cast<long long*>(partials), max_or);
 }
 
-static int q_csr_grid(int64_t n) {
-  const int64_t rows_per_block = kQCsrThreads / kQCsrLanes;
+static int q_csr_lanes(const OpView& v) { return v.csr_lanes ? v.csr_lanes : kQCsrLanes; }
+
+static int q_csr_grid(const OpView& v) {
+  const int64_t n = v.dim;
+  const int64_t rows_per_block = kQCsrThreads / q_csr_lanes(v);
   int64_t g = (n + rows_per_block - 1) / rows_per_block;
   const int64_t cap = (int64_t)sm_count() * 16;
   if (g > cap) g = cap;
   return (int)(g > 0 ? g : 1);
 }
 
-template <int DOTS, bool HAS_Z>
-static void q_csr_t(const OpView& v, const void* x, void* y, const void* z, const QParams* prm,
+template <int DOTS, bool HAS_Z, int LPR>
+static void q_csr_l(const OpView& v, const void* x, void* y, const void* z, const QParams* prm,
                     double* partials, unsigned long long* max_or, cudaStream_t st) {
-  k_csr_apply_q<DOTS, HAS_Z><<<q_csr_grid(v.dim), kQCsrThreads, 0, st>>>(
+  k_csr_apply_q<DOTS, HAS_Z, LPR><<<q_csr_grid(v), kQCsrThreads, 0, st>>>(
       v.dim, v.csr_row, v.csr_col, v.csr_diag, (const longlong2*)x, (longlong2*)y,
       (const longlong2*)z, prm, partials, max_or);
   MB_CUDA(cudaGetLastError());
+}
+
+template <int DOTS, bool HAS_Z>
+static void q_csr_t(const OpView& v, const void* x, void* y, const void* z, const QParams* prm,
+                    double* partials, unsigned long long* max_or, cudaStream_t st) {
+  switch (q_csr_lanes(v)) {
+    case 4: q_csr_l<DOTS, HAS_Z, 4>(v, x, y, z, prm, partials, max_or, st); break;
+    case 8: q_csr_l<DOTS, HAS_Z, 8>(v, x, y, z, prm, partials, max_or, st); break;
+    case 16: q_csr_l<DOTS, HAS_Z, 16>(v, x, y, z, prm, partials, max_or, st); break;
+    default: q_csr_l<DOTS, HAS_Z, 32>(v, x, y, z, prm, partials, max_or, st); break;
+  }
 }
 
 static void launch_csr_apply_q(const OpView& v, const void* x, void* y, const void* z,
@@ -706,7 +720,7 @@ static void launch_csr_apply_q(const OpView& v, const void* x, void* y, const vo
 }
 
 int q_apply_grid(const OpView& v) {
-  if (v.csr_row) return q_csr_grid(v.dim);
+  if (v.csr_row) return q_csr_grid(v);
   const int split = v.row_split > 1 ? v.row_split : 1;
   int64_t g = sm_count();
   if (g > v.Du * split) g = v.Du * split;

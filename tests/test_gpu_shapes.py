@@ -10,9 +10,9 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-Q_SHAPES = [dict(passes=p, row_split=s, table_bits=t, prefetch=f, table_stage=0)
+Q_SHAPES = [dict(passes=p, row_split=s, table_bits=t, prefetch=f, table_stage=0, csr_lanes=0)
             for p, s, t, f in itertools.product((1, 2), (1, 2, 4), (32, 16), (0, 1))]
-Q_SHAPES += [dict(passes=1, row_split=s, table_bits=32, prefetch=f, table_stage=1)
+Q_SHAPES += [dict(passes=1, row_split=s, table_bits=32, prefetch=f, table_stage=1, csr_lanes=0)
              for s, f in itertools.product((1, 2, 4), (0, 1))]
 
 
@@ -69,6 +69,8 @@ def test_prefetch_switch_keeps_fp_bits(mb, cuda, prec):
         op.set_apply_shape(passes=2)          # two passes: Q64 only
     with pytest.raises(mb.MbError):
         op.set_apply_shape(row_split=3)
+    with pytest.raises(mb.MbError):
+        op.set_apply_shape(csr_lanes=8)       # lanes a row: sparse-matrix operators only
 
 
 @pytest.mark.parametrize("prec", [0, 1, 2])
@@ -89,4 +91,41 @@ def test_autotune_picks_a_valid_shape_and_caches_it(mb, cuda, prec):
     # a second operator of the same sector takes the cached choice
     op2 = make(mb, (4, 4), 5, 4, 3.0, prec)
     shape2, ms2 = op2.autotune()
+    assert shape2 == shape and ms2 == ms
+
+
+def momentum_op(mb, prec):
+    dims = [4, 4]
+    b = mb.FermionBasis.with_fixed_particle_number_spin_momentum(16, 6, 0, dims, (1, 0))
+    return mb.GpuHubbardOperator(b, mb.HubbardModelMomentum(1.0, 6.0, dims), prec)
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-14), (1, 1e-6), (2, 0.0)])
+def test_csr_lanes_shapes(mb, cuda, prec, tol):
+    """A momentum sector (4x4, 3+3, K = (1,0)) applied with 4, 8, 16 and 32
+    lanes a row: the Q64 operator's integer row sums give the same bits at
+    every width; the floating-point ones differ only in the order of the
+    lanes' final additions.  The autotuner picks one of them and caches it
+    per sector."""
+    torch = cuda
+    op = momentum_op(mb, prec)
+    x = op.seed_vector(3)
+    ref = None
+    for lanes in (4, 8, 16, 32):
+        op.set_apply_shape(csr_lanes=lanes)
+        assert op.apply_shape()["csr_lanes"] == lanes
+        y = op.apply(x)
+        if ref is None:
+            ref = y.clone()
+        elif tol == 0.0:
+            assert torch.equal(y, ref), lanes
+        else:
+            d = float(torch.linalg.norm((y - ref).to(torch.complex128)))
+            assert d <= tol * float(torch.linalg.norm(ref.to(torch.complex128))), lanes
+    with pytest.raises(mb.MbError):
+        op.set_apply_shape(csr_lanes=12)
+    op.set_apply_shape()
+    shape, ms = op.autotune()
+    assert ms > 0 and shape["csr_lanes"] in (4, 8, 16, 32) and shape == op.apply_shape()
+    shape2, ms2 = momentum_op(mb, prec).autotune()
     assert shape2 == shape and ms2 == ms
