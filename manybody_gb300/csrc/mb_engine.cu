@@ -31,10 +31,11 @@
 namespace mb {
 
 constexpr int kEngMaxK = 512;  // Lanczos steps a slot can record
-// a slot's scalar table: alpha, beta, yk (kEngMaxK doubles each), then the
-// start vector's norm
+// a slot's scalar table: alpha, beta, yk (kEngMaxK doubles each), the start
+// vector's norm, then 1 / beta_k as floats (kEngMaxK)
 constexpr int kEngNormAt = 3 * kEngMaxK;
-constexpr size_t kEngScalBytes = sizeof(double) * (size_t)(kEngNormAt + 1);
+constexpr size_t kEngIbAt = sizeof(double) * (size_t)(kEngNormAt + 1);
+constexpr size_t kEngScalBytes = kEngIbAt + sizeof(float) * (size_t)kEngMaxK;
 
 // Device descriptor of one slot (POD).
 struct SlotDesc {
@@ -50,6 +51,7 @@ struct SlotDesc {
   double* alpha;    // [kEngMaxK]
   double* beta;     // [kEngMaxK]
   double* yk;       // Ritz coefficients for the replay pass [kEngMaxK]
+  float* ib;        // (float)(1 / beta_k) [kEngMaxK]: the persistent step's deferred normalisation
   float ufold[kMaxOrbitals + 1];
   float t;
   float scale;      // Lanczos: -1 Negated H (ground state), +1 H
@@ -780,10 +782,33 @@ __device__ __forceinline__ void eng_acc(float& hi, float& lo, float a, float b) 
   hi = s1;
 }
 
+// Deferred normalisation within one launch of the persistent step.  At the
+// end of step k a Lanczos request's v_k+1 = w_k / beta_k is not written back
+// (except on the launch's last step): the later steps of the launch multiply
+// what is stored by ib = (float)(1 / beta) as they load it, the same float
+// product (no contraction) the normalisation would have stored, so every
+// value, and every bit of the result, is the grouped kernels'.  `step` is the
+// step's index in the launch: v_k is stored unnormalised when step >= 1
+// (w_k-1), v_k-1 when step >= 2.
+struct LazyScale {
+  float v, prev;
+};
+__device__ __forceinline__ LazyScale lazy_scale(const SlotDesc& s, const SlotNow& n, int step) {
+  LazyScale l{1.f, 1.f};
+  if (n.mode == kModeLanczos && n.k < n.kmax) {
+    if (step >= 1) l.v = __ldcg(&s.ib[n.k - 1]);
+    if (step >= 2) l.prev = __ldcg(&s.ib[n.k - 2]);
+  }
+  return l;
+}
+__device__ __forceinline__ float2 lz(float2 a, float f) {
+  return make_float2(__fmul_rn(a.x, f), __fmul_rn(a.y, f));
+}
+
 // Phase A, one staged row (block-level): the arithmetic of k_eng_apply_rows.
 __device__ void p_apply_row(const SlotDesc& s, const SlotNow& n, int64_t r, int64_t pidx,
                             double* part, double* part2, float2* srow, uint32_t* s_up,
-                            double (*red)[2]) {
+                            double (*red)[2], int step) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = n.k;
   const bool lanczos = n.mode == kModeLanczos && k < n.kmax;
@@ -810,8 +835,15 @@ __device__ void p_apply_row(const SlotDesc& s, const SlotNow& n, int64_t r, int6
   const uint32_t um = s.up_mask[r];
   const int u0 = __ldg(&s.up_loff[r]), nu = __ldg(&s.up_loff[r + 1]) - u0;
   const int npos = __ldg(&s.up_lpos[r]);
+  const LazyScale ls = lazy_scale(s, n, step);
+  // v_k in the kept basis: written here when this launch produced it
+  float2* vb = lanczos && s.basis && step >= 1 ? s.basis + (int64_t)k * s.Du * Dd + r * Dd : nullptr;
   __syncthreads();  // the previous item's readers are done with srow / s_up
-  for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) srow[c] = v[c];
+  for (int64_t c = threadIdx.x; c < Dd; c += blockDim.x) {
+    const float2 t = lz(v[c], ls.v);
+    srow[c] = t;
+    if (vb) vb[c] = t;
+  }
   if (threadIdx.x < kSlicedPads) srow[Dd + threadIdx.x] = make_float2(0.f, 0.f);
   for (int j = threadIdx.x; j < nu; j += blockDim.x) s_up[j] = __ldg(&s.up_list[u0 + j]);
   __syncthreads();
@@ -839,7 +871,7 @@ __device__ void p_apply_row(const SlotDesc& s, const SlotNow& n, int64_t r, int6
     }
     const char* xc = reinterpret_cast<const char*>(x + cl);
     auto up = [&](int q) {
-      return *reinterpret_cast<const float2*>(xc + (uint64_t)s_up[q] * row_bytes);
+      return lz(*reinterpret_cast<const float2*>(xc + (uint64_t)s_up[q] * row_bytes), ls.v);
     };
     float pr = 0.f, pi = 0.f, nr = 0.f, ni = 0.f;
     int j = 0;
@@ -865,7 +897,7 @@ __device__ void p_apply_row(const SlotDesc& s, const SlotNow& n, int64_t r, int6
     o.x = fmaf(hop, ar, d * xv.x);
     o.y = fmaf(hop, ai, d * xv.y);
     if (k > 0) {
-      const float2 zv = z[c];
+      const float2 zv = lz(z[c], ls.prev);
       o.x = fmaf(beta, zv.x, o.x);
       o.y = fmaf(beta, zv.y, o.y);
     }
@@ -904,7 +936,7 @@ __device__ void p_apply_row(const SlotDesc& s, const SlotNow& n, int64_t r, int6
 // Phase A, one small row (warp-level, the row staged in the warp's shared
 // memory): the arithmetic of k_eng_apply.
 __device__ void p_apply_warp_row(const SlotDesc& s, const SlotNow& n, int64_t r, int64_t pidx,
-                                 double* part, double* part2, float2* wrow) {
+                                 double* part, double* part2, float2* wrow, int step) {
   const int lane = threadIdx.x & 31;
   const int k = n.k;
   const bool replay = n.mode == kModeReplay;
@@ -917,8 +949,16 @@ __device__ void p_apply_warp_row(const SlotDesc& s, const SlotNow& n, int64_t r,
     const float2* x = s.buf[(k + 1) % 3];
     const float2* z = s.buf[k % 3] + r * Dd;
     float2* w = s.buf[(k + 2) % 3] + r * Dd;
+    const LazyScale ls = lazy_scale(s, n, step);
+    float2* vb = n.mode == kModeLanczos && s.basis && step >= 1
+                     ? s.basis + (int64_t)k * s.Du * Dd + r * Dd
+                     : nullptr;
     __syncwarp();  // the warp's previous row is no longer read
-    for (int64_t c = lane; c < Dd; c += 32) wrow[c] = v[c];
+    for (int64_t c = lane; c < Dd; c += 32) {
+      const float2 t = lz(v[c], ls.v);
+      wrow[c] = t;
+      if (vb) vb[c] = t;
+    }
     __syncwarp();
     const double bprev = cheb ? 1.0 : (k > 0 ? __ldcg(&s.beta[k - 1]) : 0.0);
     const float beta = (float)(-bprev);
@@ -941,7 +981,7 @@ __device__ void p_apply_warp_row(const SlotDesc& s, const SlotNow& n, int64_t r,
       }
       for (int j = u0; j < u1; ++j) {
         const uint32_t e = __ldg(&s.up_ent[j]);
-        const float2 val = x[(int64_t)(e >> 8) * Dd + c];
+        const float2 val = lz(x[(int64_t)(e >> 8) * Dd + c], ls.v);
         float wgt = (e & 2u) ? 2.f : 1.f;
         if (e & 1u) wgt = -wgt;
         ar = fmaf(wgt, val.x, ar);
@@ -954,7 +994,7 @@ __device__ void p_apply_warp_row(const SlotDesc& s, const SlotNow& n, int64_t r,
       o.x = fmaf(hop, ar, d * xv.x);
       o.y = fmaf(hop, ai, d * xv.y);
       if (k > 0) {
-        const float2 zv = z[c];
+        const float2 zv = lz(z[c], ls.prev);
         o.x = fmaf(beta, zv.x, o.x);
         o.y = fmaf(beta, zv.y, o.y);
       }
@@ -1005,8 +1045,13 @@ __device__ void p_seg_reduce(SlotDesc& s, const double* part, const double* part
     __syncthreads();
   }
   if (threadIdx.x == 0 && n.mode == kModeLanczos && k < n.kmax) {
-    if (what == 0) s.alpha[k] = red[0];
-    else s.beta[k] = sqrt(fmax(red[0], 0.0));
+    if (what == 0) {
+      s.alpha[k] = red[0];
+    } else {
+      const double b = sqrt(fmax(red[0], 0.0));
+      s.beta[k] = b;
+      s.ib[k] = (float)(1.0 / b);  // once a request, for the deferred normalisation
+    }
   }
   if (threadIdx.x == 0 && cheb && k < n.kmax) {
     s.alpha[k] = red[0];
@@ -1015,7 +1060,8 @@ __device__ void p_seg_reduce(SlotDesc& s, const double* part, const double* part
 }
 
 // Phase C, one row (warp-level): k_eng_update and k_eng_replay_update.
-__device__ void p_update_row(const SlotDesc& s, const SlotNow& n, int64_t r, int it, double* part) {
+__device__ void p_update_row(const SlotDesc& s, const SlotNow& n, int64_t r, int it, double* part,
+                             int step) {
   const int lane = threadIdx.x & 31;
   const int k = n.k;
   const int64_t Dd = s.Dd;
@@ -1023,6 +1069,7 @@ __device__ void p_update_row(const SlotDesc& s, const SlotNow& n, int64_t r, int
     const float2* v = s.buf[(k + 1) % 3] + r * Dd;
     float2* w = s.buf[(k + 2) % 3] + r * Dd;
     const float a = (float)__ldcg(&s.alpha[k]);
+    const float lv = lazy_scale(s, n, step).v;
     float hi = 0.f, lo = 0.f;
     // four elements a lane in flight (half the threads of the grouped
     // kernels run here), summed in the same order
@@ -1032,7 +1079,7 @@ __device__ void p_update_row(const SlotDesc& s, const SlotNow& n, int64_t r, int
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         o[q] = w[c + 32 * q];
-        xv[q] = v[c + 32 * q];
+        xv[q] = lz(v[c + 32 * q], lv);
       }
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
@@ -1045,7 +1092,7 @@ __device__ void p_update_row(const SlotDesc& s, const SlotNow& n, int64_t r, int
     }
     for (; c < Dd; c += 32) {
       float2 o = w[c];
-      const float2 xv = v[c];
+      const float2 xv = lz(v[c], lv);
       o.x = fmaf(-a, xv.x, o.x);
       o.y = fmaf(-a, xv.y, o.y);
       w[c] = o;
@@ -1079,14 +1126,21 @@ __device__ void p_update_row(const SlotDesc& s, const SlotNow& n, int64_t r, int
   }
 }
 
-// Phase E, one row (warp-level): k_eng_normalize.
-__device__ void p_normalize_row(const SlotDesc& s, const SlotNow& n, int64_t r) {
+// Phase E, one row (warp-level): k_eng_normalize.  Runs on the launch's last
+// step only; v_k, when this launch left it unnormalised, is normalised in
+// place too, so every launch ends with the grouped kernels' vectors.
+__device__ void p_normalize_row(const SlotDesc& s, const SlotNow& n, int64_t r, int step) {
   const int lane = threadIdx.x & 31;
   const int k = n.k;
   if (!(n.mode == kModeLanczos && k < n.kmax)) return;
+  const int64_t Dd = s.Dd;
+  const float lv = lazy_scale(s, n, step).v;
+  if (step >= 1) {
+    float2* v = s.buf[(k + 1) % 3] + r * Dd;
+    for (int64_t c = lane; c < Dd; c += 32) v[c] = lz(v[c], lv);
+  }
   const double b = __ldcg(&s.beta[k]);
   if (!(b > kTol)) return;
-  const int64_t Dd = s.Dd;
   float2* w = s.buf[(k + 2) % 3] + r * Dd;
   float2* vb = s.basis && k + 1 < n.kmax ? s.basis + (int64_t)(k + 1) * s.Du * Dd + r * Dd
                                          : nullptr;
@@ -1132,7 +1186,9 @@ __device__ void p_advance(SlotDesc& s) {
   }
 }
 
-__global__ void __launch_bounds__(kEngPWarps * 32)
+// four co-resident blocks an SM (64 registers a thread): the occupancy the
+// apply phase's gathers need
+__global__ void __launch_bounds__(kEngPWarps * 32, 4)
 k_eng_persistent(EngPersistArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double red[kEngPWarps][2];
@@ -1143,17 +1199,19 @@ k_eng_persistent(EngPersistArgs a) {
   float2* wrow = reinterpret_cast<float2*>(smem) + (size_t)warp * kEngWarpRowCols;
   const int gw = blockIdx.x * kEngPWarps + warp, nw = gridDim.x * kEngPWarps;
   for (int step = 0; step < a.steps; ++step) {
+    const bool last = step + 1 == a.steps;
     // A: apply
     for (int it = blockIdx.x; it < a.n_rows; it += gridDim.x) {
       const int2 item = a.items_rows[it];
       const SlotDesc& s = a.slots[item.x];
-      p_apply_row(s, slot_now(s), item.y, s.item0 + item.y, a.part, a.part2, srow, s_up, red);
+      p_apply_row(s, slot_now(s), item.y, s.item0 + item.y, a.part, a.part2, srow, s_up, red,
+                  step);
     }
     __syncthreads();  // the row items' shared memory becomes the warps' rows
     for (int it = gw; it < a.n_warp; it += nw) {
       const int2 item = a.items_warp[it];
       const SlotDesc& s = a.slots[item.x];
-      p_apply_warp_row(s, slot_now(s), item.y, s.item0 + item.y, a.part, a.part2, wrow);
+      p_apply_warp_row(s, slot_now(s), item.y, s.item0 + item.y, a.part, a.part2, wrow, step);
     }
     if (a.apply_only) return;
     if (!eng_grid_sync(a.grid, a.budget)) return;
@@ -1165,25 +1223,34 @@ k_eng_persistent(EngPersistArgs a) {
     for (int it = gw; it < a.n_items; it += nw) {
       const int2 item = a.items[it];
       const SlotDesc& s = a.slots[item.x];
-      p_update_row(s, slot_now(s), item.y, it, a.part);
+      p_update_row(s, slot_now(s), item.y, it, a.part, step);
     }
     if (!eng_grid_sync(a.grid, a.budget)) return;
-    // D: beta
-    for (int si = blockIdx.x; si < a.n_slots; si += gridDim.x)
+    // D: beta; before the last step, F (advance) right after it by the same
+    // block (no normalisation pass between them: it is deferred)
+    for (int si = blockIdx.x; si < a.n_slots; si += gridDim.x) {
       p_seg_reduce(a.slots[si], a.part, a.part2, 1, sred, sred2);
+      if (!last) {
+        __syncthreads();
+        if (threadIdx.x == 0) p_advance(a.slots[si]);
+      }
+    }
+    if (!last) {
+      if (!eng_grid_sync(a.grid, a.budget)) return;
+      continue;
+    }
     if (!eng_grid_sync(a.grid, a.budget)) return;
-    // E: normalise
+    // E: normalise (the last step)
     for (int it = gw; it < a.n_items; it += nw) {
       const int2 item = a.items[it];
       const SlotDesc& s = a.slots[item.x];
-      p_normalize_row(s, slot_now(s), item.y);
+      p_normalize_row(s, slot_now(s), item.y, step);
     }
     if (!eng_grid_sync(a.grid, a.budget)) return;
     // F: advance
     for (int si = blockIdx.x * blockDim.x + threadIdx.x; si < a.n_slots;
          si += gridDim.x * blockDim.x)
       p_advance(a.slots[si]);
-    if (step + 1 < a.steps && !eng_grid_sync(a.grid, a.budget)) return;
   }
 }
 
@@ -1471,6 +1538,7 @@ void rebuild(mb_engine_s* e) {
     d.alpha = sc;
     d.beta = sc + kEngMaxK;
     d.yk = sc + 2 * kEngMaxK;
+    d.ib = reinterpret_cast<float*>(reinterpret_cast<char*>(sc) + kEngIbAt);
     const std::vector<double> uf = u_fold_table(s.u, !(s.u * s.u < kTol * kTol), ts.basis.L);
     for (int kk = 0; kk <= kMaxOrbitals; ++kk) d.ufold[kk] = kk < (int)uf.size() ? (float)uf[(size_t)kk] : 0.f;
     d.t = (float)s.t;

@@ -916,23 +916,44 @@ struct RefineRun {
 };
 }  // namespace
 
-static void refine_chunk(std::vector<RefineRun>& runs, cudaStream_t st) {
+// The buffers of a group of problems run together, sized for the largest
+// group of a call and reused by each group (one allocation a call).
+struct RefineSizes {
   size_t qbytes = 0, cwords = 0;
   int pblocks = 1, pcomps = 3;
-  for (auto& r : runs) {
+  void add(const RefineRun& r) {
     qbytes += r.vb * (size_t)r.cap;
     cwords += 4 * (size_t)r.cap + 4;
     pblocks = std::max({pblocks, apply_grid(r.p->v, MB_PREC_F64), blas_grid(r.n),
                         multi_dot_grid(r.n)});
     pcomps = std::max(pcomps, 2 * r.cap);
   }
-  DevBuf qbuf(qbytes), cbuf(sizeof(double) * cwords), part(sizeof(double) * (size_t)pblocks * pcomps);
+  void widen(const RefineSizes& o) {
+    qbytes = std::max(qbytes, o.qbytes);
+    cwords = std::max(cwords, o.cwords);
+    pblocks = std::max(pblocks, o.pblocks);
+    pcomps = std::max(pcomps, o.pcomps);
+  }
+};
+struct RefineBufs {
+  DevBuf q, c, part;
   double* host = nullptr;
-  MB_CUDA(cudaMallocHost(&host, sizeof(double) * cwords));
-  struct HostFree {
-    double* h;
-    ~HostFree() { cudaFreeHost(h); }
-  } host_free{host};
+  explicit RefineBufs(const RefineSizes& z)
+      : q(z.qbytes), c(sizeof(double) * z.cwords), part(sizeof(double) * (size_t)z.pblocks * z.pcomps) {
+    MB_CUDA(cudaMallocHost(&host, sizeof(double) * z.cwords));
+  }
+  ~RefineBufs() {
+    if (host) cudaFreeHost(host);
+  }
+};
+
+static void refine_chunk(std::vector<RefineRun>& runs, RefineBufs& bufs, cudaStream_t st) {
+  RefineSizes z;
+  for (auto& r : runs) z.add(r);
+  const size_t cwords = z.cwords;
+  DevBuf& qbuf = bufs.q;
+  DevBuf& cbuf = bufs.c;
+  double* host = bufs.host;
   {
     size_t qo = 0, co = 0;
     for (auto& r : runs) {
@@ -943,7 +964,7 @@ static void refine_chunk(std::vector<RefineRun>& runs, cudaStream_t st) {
       co += 4 * (size_t)r.cap + 4;
     }
   }
-  double* pp = (double*)part.p;
+  double* pp = (double*)bufs.part.p;
   auto sync_all = [&] {
     MB_CUDA(cudaMemcpyAsync(host, cbuf.p, sizeof(double) * cwords, cudaMemcpyDeviceToHost, st));
     MB_CUDA(cudaStreamSynchronize(st));
@@ -1002,31 +1023,34 @@ static void refine_chunk(std::vector<RefineRun>& runs, cudaStream_t st) {
 }
 
 void fp64_refine_many(RefineProblem* probs, int count, cudaStream_t st) {
-  std::vector<RefineRun> chunk;
-  size_t chunk_bytes = 0;
-  for (int i = 0; i <= count; ++i) {
+  if (count <= 0) return;
+  // group the problems (consecutive, bases under kRefineChunkBytes a group)
+  std::vector<std::vector<RefineRun>> groups(1);
+  std::vector<RefineSizes> sizes(1);
+  size_t group_bytes = 0;
+  for (int i = 0; i < count; ++i) {
     RefineRun r{};
-    size_t rb = 0;
-    if (i < count) {
-      RefineProblem& p = probs[i];
-      r.p = &p;
-      r.n = p.v.dim;
-      r.vb = 16 * (size_t)r.n;
-      const int64_t fit = (int64_t)(kRefineBasisBytes / std::max<size_t>(r.vb, 1)) - 1;
-      r.steps = (int)std::max<int64_t>(kRefineMinSteps, std::min<int64_t>(kRefineMaxSteps, fit));
-      r.cap = r.steps + 1;
-      rb = r.vb * (size_t)r.cap;
+    RefineProblem& p = probs[i];
+    r.p = &p;
+    r.n = p.v.dim;
+    r.vb = 16 * (size_t)r.n;
+    const int64_t fit = (int64_t)(kRefineBasisBytes / std::max<size_t>(r.vb, 1)) - 1;
+    r.steps = (int)std::max<int64_t>(kRefineMinSteps, std::min<int64_t>(kRefineMaxSteps, fit));
+    r.cap = r.steps + 1;
+    const size_t rb = r.vb * (size_t)r.cap;
+    if (!groups.back().empty() && group_bytes + rb > kRefineChunkBytes) {
+      groups.emplace_back();
+      sizes.emplace_back();
+      group_bytes = 0;
     }
-    if (i == count || (!chunk.empty() && chunk_bytes + rb > kRefineChunkBytes)) {
-      if (!chunk.empty()) refine_chunk(chunk, st);
-      chunk.clear();
-      chunk_bytes = 0;
-    }
-    if (i < count) {
-      chunk.push_back(std::move(r));
-      chunk_bytes += rb;
-    }
+    sizes.back().add(r);
+    groups.back().push_back(std::move(r));
+    group_bytes += rb;
   }
+  RefineSizes most;
+  for (const auto& z : sizes) most.widen(z);
+  RefineBufs bufs(most);
+  for (auto& g : groups) refine_chunk(g, bufs, st);
 }
 
 double fp64_ritz_refine(const OpView& v, const void* x64, cudaStream_t st) {
@@ -1573,7 +1597,7 @@ int mb_op_apply_affine(mb_op_t op, const void* x_dev, void* y_dev, double scale,
 // groups run.  Same kernels and arithmetic as mb_op_apply, so the same bits.
 static void host_apply_pipeline(mb_op_s* op, const mb_op_s::HostLane& lane, const void* x_host,
                                 const void* x_mapped, void* y_host, mb_op_s::Scratch& s) {
-  cudaStream_t comp = lane.comp, copy = lane.copy;
+  cudaStream_t comp = lane.comp;
   int32_t* iperm = op_iperm(op);
   const int prec = op->precision;
   const size_t es = elem_bytes(prec);
@@ -1586,7 +1610,6 @@ static void host_apply_pipeline(mb_op_s* op, const mb_op_s::HostLane& lane, cons
   } else {
     // pageable x: through the lane's bounce buffers, each chunk scattered to
     // tensor order once it has landed
-    (void)copy;
     lane_upload(lane, xs, x_host, es * (size_t)n, es, [&](size_t off, size_t len, cudaEvent_t e) {
       MB_CUDA(cudaStreamWaitEvent(comp, e, 0));
       const int64_t i0 = (int64_t)(off / es);

@@ -228,7 +228,7 @@ void q_apply_host_reference(mb_op_s* op, const mb_op_s::HostLane& lane, const vo
 static void q_apply_host_pipeline(mb_op_s* op, const mb_op_s::HostLane& lane, const void* x_host,
                                   const void* x_mapped, void* y_host, void* x_stage,
                                   void* y_stage) {
-  cudaStream_t comp = lane.comp, copy = lane.copy;
+  cudaStream_t comp = lane.comp;
   auto& q = qscratch_for(op, comp);
   int32_t* iperm = op_iperm(op);
   const int64_t n = op->dim;
@@ -239,7 +239,6 @@ static void q_apply_host_pipeline(mb_op_s* op, const mb_op_s::HostLane& lane, co
     launch_scatter_maxexp(n, x_mapped, iperm, q.xq, q.ints, comp);
   } else {
     // pageable x: through the lane's bounce buffers, each chunk scattered once landed
-    (void)copy;
     lane_upload(lane, x_stage, x_host, es * (size_t)n, es, [&](size_t off, size_t len, cudaEvent_t e) {
       MB_CUDA(cudaStreamWaitEvent(comp, e, 0));
       const int64_t i0 = (int64_t)(off / es);
