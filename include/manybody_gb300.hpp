@@ -215,6 +215,19 @@ class GpuHubbardOperator {
   }
   size_t dimension() const { return (size_t)dim_; }
   mb_op_t handle() const { return h_; }
+  // Times the apply's kernel shapes on the GPU and keeps the fastest
+  // (mb_op_autotune; cached per sector); returns ms per apply.
+  double autotune() {
+    mb_apply_shape s{};
+    double ms = 0.0;
+    check(mb_op_autotune(h_, nullptr, &s, &ms));
+    return ms;
+  }
+  mb_apply_shape apply_shape() const {
+    mb_apply_shape s{};
+    check(mb_op_get_apply_shape(h_, &s));
+    return s;
+  }
 
  private:
   mb_op_t h_ = nullptr;

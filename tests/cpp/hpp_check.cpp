@@ -174,6 +174,13 @@ int main(int argc, char** argv) {
   CHECK(std::sqrt(err / nrm) < 1e-13);
   const double rq = rayleigh(op, v);
   CHECK(std::isfinite(rq));
+  // the tuned shape applies the same H (FP64: within rounding of the default)
+  CHECK(op.autotune() > 0.0);
+  CHECK(op.apply_shape().passes == 1);
+  CxVec w2 = op.apply(v);
+  double d2 = 0;
+  for (size_t i = 0; i < H.n; ++i) d2 += std::norm(w2.data[i] - w.data[i]);
+  CHECK(std::sqrt(d2 / nrm) < 1e-13);
   void* seed = nullptr;
   mbgpu::check(mb_alloc(&seed, sizeof(std::complex<double>) * 4900));
   mbgpu::check(mb_fill_uniform(op.handle(), 0, 0, seed, MB_ORDER_REFERENCE, nullptr));
