@@ -824,7 +824,7 @@ def run_reference(args):
 # workload, nothing timed (ncu measures).  Each prints one JSON line.
 # ---------------------------------------------------------------------------
 PROBES = ("q64_apply", "fp64_apply", "fp32_apply", "engine_persistent", "engine_grouped",
-          "engine_fused", "momentum_csr", "momentum_csr_q64")
+          "engine_persistent_fixed", "engine_fused", "momentum_csr", "momentum_csr_q64")
 
 
 def run_probe(args):
@@ -859,14 +859,19 @@ def run_probe(args):
         torch.cuda.synchronize()
         out = {"probe": name, "case": args.case, "dim": op.dimension(), "apply_shape": shape,
                "launches": args.steps}
-    elif name in ("engine_persistent", "engine_grouped"):
+    elif name in ("engine_persistent", "engine_grouped", "engine_persistent_fixed"):
+        # engine_persistent_fixed: all --steps steps in one launch (a fixed-length
+        # batch), the others one launch a step
         secs = batch_sectors(n=64)
         descs = [mb.sector(d, nu, nd, 1.0, u) for d, nu, nd, u in secs]
         eng = mb.Engine()
-        eng.set_persistent(name == "engine_persistent")
+        eng.set_persistent(name != "engine_grouped")
         for i, d in enumerate(descs):
             eng.try_submit(d, seed=i, kmax=150, rel_tol=0.0)
-        eng.step(args.steps)
+        if name == "engine_persistent_fixed":
+            eng.step_fixed(args.steps, False)
+        else:
+            eng.step(args.steps)
         torch.cuda.synchronize()
         import math
         states = sum(math.comb(d[0], nu) * math.comb(d[0], nd) for d, nu, nd, _ in secs)
