@@ -283,6 +283,30 @@ def test_persistent_step_matches_grouped_kernels(mb, cuda):
         assert x.e0 == y.e0 and x.e0_raw == y.e0_raw and x.steps == y.steps
 
 
+def test_persistent_launch_boundaries_keep_bits(mb, cuda):
+    """Within a launch the persistent step defers each Lanczos step's
+    normalisation to the next step, and a launch's last step normalises:
+    a batch stepped in launches of 1, 7 and 3 steps, then the rest, gives the
+    bits of the grouped kernels (every step its own launches), with and
+    without kept bases."""
+    d = descs(mb)
+    kmax = 60
+    for limit in (None, 0):
+        ref = mb.batch_ground_states(d, seeds=list(range(len(d))), kmax=kmax, autotune=False,
+                                     persistent=False, basis_limit=limit)
+        eng = mb.Engine()
+        if limit is not None:
+            eng.set_basis_limit(limit)
+        ids = [eng.try_submit(x, i, kmax, 0.0, True) for i, x in enumerate(d)]
+        for n in (1, 7, 3):
+            eng.step_fixed(n, n != 7)
+        while eng.step_fixed(kmax, True):
+            pass
+        for rid, r in zip(ids, ref):
+            got = eng.poll(rid)
+            assert got.e0 == r.e0 and got.e0_raw == r.e0_raw and got.steps == r.steps
+
+
 def test_same_result_alone_and_in_mix_large_request(mb, cuda):
     """A sector of more than a million states (1D L=13, 6+6: 2,944,656) through
     the persistent step's block-per-row path gets the same bits alone and in a
