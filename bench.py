@@ -60,6 +60,23 @@ def measured_peaks():
     return HBM_FALLBACK_GBS, "fallback"
 
 
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64, nominal
+
+
+def mean_hops(lattice, n_up: int, n_down: int) -> float:
+    """Mean number of hops (both spins) of a state of the sector: a bond with
+    exactly one end occupied gives one hop, so per spin the mean is
+    B * 2 n (N - n) / (N (N - 1)) for B bonds (a size-2 side's doubled bond
+    counts twice, a size-1 side's self bond none) on N sites."""
+    N = 1
+    for d in lattice:
+        N *= d
+    B = sum(N for d in lattice if d >= 2)
+    if N < 2:
+        return 0.0
+    return sum(B * 2.0 * n * (N - n) / (N * (N - 1)) for n in (n_up, n_down))
+
+
 def committed_traffic(kernel_key: str):
     """DRAM bytes per launch from the committed ncu summary, if present."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
@@ -270,6 +287,15 @@ def run_gpu(args):
         gbs = 2 * nbytes * dim / (ms * 1e-3) / 1e9
         extras[name] = {"ms_per_apply": round(ms, 4), "GBps": round(gbs, 2),
                         "frac_of_hbm": round(gbs / peak, 4), "apply_shape": shape}
+        if prec == mb.PREC_F64:
+            # the FP64 ALU roofline: ~(2 hops + 6) real FP64 operations an element,
+            # against the nominal 1.25 TFLOP/s of this part (no measured FP64 peak)
+            flops = (2.0 * mean_hops(w["lattice"], w["n_up"], w["n_down"]) + 6.0) * dim
+            tf = flops / (ms * 1e-3) / 1e12
+            extras[name]["fp64_roofline"] = {
+                "flops_per_element": round(flops / dim, 2), "achieved_tflops": round(tf, 4),
+                "nominal_peak_tflops": FP64_NOMINAL_TFLOPS,
+                "frac_of_nominal": round(tf / FP64_NOMINAL_TFLOPS, 4)}
         del op, xv, yv
         torch.cuda.empty_cache()
 
