@@ -466,12 +466,29 @@ def run_cfg2_extra(mb, torch, n_probes=16, n_moments=1024):
     t0 = time.perf_counter()
     mu = mb.kpm_dos_moments(op, n_moments, n_probes, 1, lo.value, hi.value, 0.01)
     t_kpm = time.perf_counter() - t0
+    dim = op.dimension()
+    peak, _ = measured_peaks()
+
+    def step_roofline(seconds, steps, vector_passes):
+        """A step's algorithmic bytes: the matvec (read x, write y) and
+        `vector_passes` more 16-byte vector passes, over its mean wall time."""
+        ms = 1e3 * seconds / max(steps, 1)
+        gbs = (2 + vector_passes) * 16 * dim / (ms * 1e-3) / 1e9
+        return {"ms_per_step": round(ms, 3), "algorithmic_bytes": (2 + vector_passes) * 16 * dim,
+                "GBps": round(gbs, 1), "frac_of_hbm": round(gbs / peak, 4)}
+
+    kpm_steps = n_probes * (n_moments // 2)
     return {
         "workload": "2D 4x4 periodic, t=1, U=8, N_up=N_down=6 (64,128,064 states), Q64 vectors",
         "e0": lo.value, "e0_lanczos_steps": lo.steps, "e0_seconds": round(t_lo, 3),
+        # a Lanczos step: the matvec, then read v, v_prev, w and write w
+        "lanczos_step": step_roofline(t_lo, lo.steps, 4),
         "e_max": hi.value, "e_max_lanczos_steps": hi.steps, "e_max_seconds": round(t_hi, 3),
         "kpm": {"moments": n_moments, "probes": n_probes, "seconds": round(t_kpm, 3),
                 "seconds_per_probe": round(t_kpm / n_probes, 3),
+                # a Chebyshev step (two moments by the doubling identities): the
+                # matvec, then read T_n-1 and write T_n+1
+                "chebyshev_step": step_roofline(t_kpm, kpm_steps, 2),
                 "mu0": float(mu[0]), "mu_1_to_4": [float(v) for v in mu[1:5]]},
     }
 
