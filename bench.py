@@ -290,7 +290,8 @@ def run_gpu(args):
         if prec == mb.PREC_F64:
             # the FP64 ALU roofline: ~(2 hops + 6) real FP64 operations an element,
             # against the nominal 1.25 TFLOP/s of this part (no measured FP64 peak)
-            flops = (2.0 * mean_hops(w["lattice"], w["n_up"], w["n_down"]) + 6.0) * dim
+            cw = CASES[args.case]
+            flops = (2.0 * mean_hops(cw["lattice"], cw["n_up"], cw["n_down"]) + 6.0) * dim
             tf = flops / (ms * 1e-3) / 1e12
             extras[name]["fp64_roofline"] = {
                 "flops_per_element": round(flops / dim, 2), "achieved_tflops": round(tf, 4),
