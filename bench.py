@@ -868,7 +868,8 @@ def run_reference(args):
 # workload, nothing timed (ncu measures).  Each prints one JSON line.
 # ---------------------------------------------------------------------------
 PROBES = ("q64_apply", "fp64_apply", "fp32_apply", "engine_persistent", "engine_grouped",
-          "engine_persistent_fixed", "engine_fused", "momentum_csr", "momentum_csr_q64")
+          "engine_persistent_fixed", "engine_fused", "momentum_csr", "momentum_csr_q64",
+          "q64_lanczos")
 
 
 def run_probe(args):
@@ -903,6 +904,21 @@ def run_probe(args):
         torch.cuda.synchronize()
         out = {"probe": name, "case": args.case, "dim": op.dimension(), "apply_shape": shape,
                "launches": args.steps}
+    elif name == "q64_lanczos":
+        # --steps plain Lanczos steps on the Q64 operator of --case (the
+        # ground-state solve's recurrence: apply with fused dots, w -= alpha v,
+        # v = w / beta)
+        w = CASES[args.case]
+        L = 1
+        for d in w["lattice"]:
+            L *= d
+        basis = mb.FermionBasis.with_fixed_particle_number_and_spin(L, w["n_up"] + w["n_down"],
+                                                                    w["n_up"] - w["n_down"])
+        op = mb.GpuHubbardOperator(basis, mb._Hubbard(w["t"], w["U"], w["lattice"]), mb.PREC_Q64)
+        x = op.seed_vector(0, order=mb.ORDER_TENSOR)
+        r = mb.find_min_eigenpair(op, args.steps, x, order=mb.ORDER_TENSOR, want_vector=False)
+        torch.cuda.synchronize()
+        out = {"probe": name, "case": args.case, "dim": op.dimension(), "steps": r.steps}
     elif name in ("engine_persistent", "engine_grouped", "engine_persistent_fixed"):
         # engine_persistent_fixed: all --steps steps in one launch (a fixed-length
         # batch), the others one launch a step

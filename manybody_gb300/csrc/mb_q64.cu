@@ -761,10 +761,12 @@ static void q_apply_sel(const OpView& v, const void* x, void* y, const void* z,
                         const QParams* prm, double* partials, unsigned long long* max_or,
                         int dots, const void* ups, cudaStream_t st) {
   if (z) {
-    if (dots) q_apply_t<STAGED, 7, true, UPS, TB>(v, x, y, z, prm, partials, max_or, ups, st);
+    if (dots == 5) q_apply_t<STAGED, 5, true, UPS, TB>(v, x, y, z, prm, partials, max_or, ups, st);
+    else if (dots) q_apply_t<STAGED, 7, true, UPS, TB>(v, x, y, z, prm, partials, max_or, ups, st);
     else q_apply_t<STAGED, 0, true, UPS, TB>(v, x, y, z, prm, partials, max_or, ups, st);
   } else {
-    if (dots) q_apply_t<STAGED, 7, false, UPS, TB>(v, x, y, z, prm, partials, max_or, ups, st);
+    if (dots == 5) q_apply_t<STAGED, 5, false, UPS, TB>(v, x, y, z, prm, partials, max_or, ups, st);
+    else if (dots) q_apply_t<STAGED, 7, false, UPS, TB>(v, x, y, z, prm, partials, max_or, ups, st);
     else q_apply_t<STAGED, 0, false, UPS, TB>(v, x, y, z, prm, partials, max_or, ups, st);
   }
 }
@@ -1019,6 +1021,9 @@ void launch_q_plan(const QPlanInput& in, const int* ex_dev, QParams* p_dev, cuda
 //   out = round((A a + B b) / 2^sh), A, B complex fixed-point (re, im), b optional;
 //   partials: <out,out>>>32 ; max_or: OR of |out| components.
 // ---------------------------------------------------------------------------
+// REAL: both coefficients real (ai = bi = 0; the Lanczos recurrence), half
+// the 128-bit products, the same integers
+template <bool REAL>
 __global__ void k_q_lincomb(int64_t n, const longlong2* a, long long ar, long long ai,
                             const longlong2* b, long long br, long long bi, int sh,
                             longlong2* out, double* __restrict__ partials,
@@ -1028,12 +1033,19 @@ __global__ void k_q_lincomb(int64_t n, const longlong2* a, long long ar, long lo
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const longlong2 va = a ? a[i] : make_longlong2(0, 0);
-    __int128 pr = (__int128)ar * va.x - (__int128)ai * va.y;
-    __int128 pi = (__int128)ar * va.y + (__int128)ai * va.x;
+    __int128 pr = (__int128)ar * va.x, pi = (__int128)ar * va.y;
+    if (!REAL) {
+      pr -= (__int128)ai * va.y;
+      pi += (__int128)ai * va.x;
+    }
     if (b) {
       const longlong2 vb = b[i];
-      pr += (__int128)br * vb.x - (__int128)bi * vb.y;
-      pi += (__int128)br * vb.y + (__int128)bi * vb.x;
+      pr += (__int128)br * vb.x;
+      pi += (__int128)br * vb.y;
+      if (!REAL) {
+        pr -= (__int128)bi * vb.y;
+        pi += (__int128)bi * vb.x;
+      }
     }
     longlong2 o;
     o.x = round_shift(pr, sh);
@@ -1051,9 +1063,14 @@ __global__ void k_q_lincomb(int64_t n, const longlong2* a, long long ar, long lo
 void launch_q_lincomb(int64_t n, const void* a, long long ar, long long ai, const void* b,
                       long long br, long long bi, int sh, void* out, double* partials,
                       unsigned long long* max_or, cudaStream_t st) {
-  k_q_lincomb<<<q_blas_grid(n), kQBlas, 0, st>>>(n, (const longlong2*)a, ar, ai,
-                                                 (const longlong2*)b, br, bi, sh,
-                                                 (longlong2*)out, partials, max_or);
+  if (ai == 0 && bi == 0)
+    k_q_lincomb<true><<<q_blas_grid(n), kQBlas, 0, st>>>(n, (const longlong2*)a, ar, ai,
+                                                         (const longlong2*)b, br, bi, sh,
+                                                         (longlong2*)out, partials, max_or);
+  else
+    k_q_lincomb<false><<<q_blas_grid(n), kQBlas, 0, st>>>(n, (const longlong2*)a, ar, ai,
+                                                          (const longlong2*)b, br, bi, sh,
+                                                          (longlong2*)out, partials, max_or);
   MB_CUDA(cudaGetLastError());
 }
 

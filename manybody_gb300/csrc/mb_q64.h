@@ -47,7 +47,8 @@ QPlanInput q_plain_plan_input(const mb_op_s* op);
 
 // The fused apply (see mb_q64.cu).  y must not alias x or z.  With ups (the
 // column pass's up-hop sums of x, launch_upcol_q) the up hops are read from
-// it; without, they are gathered from x in the same pass.
+// it; without, they are gathered from x in the same pass.  dots: 0 none;
+// 5 Re<x,y> and max |y| (<y,y> left 0); any other non-zero value all three.
 void launch_apply_q(const OpView& v, const void* x, void* y, const void* z, const QParams* prm_dev,
                     double* partials, unsigned long long* max_or, int dots, cudaStream_t st,
                     const void* ups = nullptr);

@@ -273,6 +273,10 @@ struct QRef {
   void* p = nullptr;
   int E = 0;
   double maxq = 0.0;
+  // the vector is m times its mantissas' value: a normalisation not yet
+  // applied to them (the plain Lanczos recurrence folds 1 / beta into the
+  // coefficients of the next apply and combination instead of a pass)
+  double m = 1.0;
 };
 
 struct QVec {
@@ -355,6 +359,9 @@ struct QKrylov {
   // Returns ||out||^2.
   double lincomb(QRef& out, const QRef* a, std::complex<double> ca, const QRef* b,
                  std::complex<double> cb) {
+    if (a) ca *= a->m;
+    if (b) cb *= b->m;
+    out.m = 1.0;
     const double ba = a ? std::abs(ca) * std::ldexp(a->maxq, a->E) : 0.0;
     const double bb = b ? std::abs(cb) * std::ldexp(b->maxq, b->E) : 0.0;
     const double bound = (ba + bb) * (1.0 + 1e-12);
@@ -380,24 +387,30 @@ struct QKrylov {
   // w = scale H v - beta_prev v_prev; returns (Re<v,w>, ||w||^2).
   std::pair<double, double> apply(QRef& w, const QRef& v, double scale, double beta_prev,
                                   const QRef* v_prev) {
-    return apply_affine(w, v, scale, 0.0, -beta_prev, v_prev);
+    // the recurrence reads Re<v,w> only: ||w||^2 comes from w -= alpha v
+    return apply_affine(w, v, scale, 0.0, -beta_prev, v_prev, 5);
   }
 
-  // w = scale (H - shift) v + beta z; returns (Re<v,w>, ||w||^2).
+  // w = scale (H - shift) v + beta z; returns (Re<v,w>, ||w||^2) (dots 5: the
+  // second is left 0, saving its 128-bit products).
   std::pair<double, double> apply_affine(QRef& w, const QRef& v, double scale, double shift,
-                                         double beta, const QRef* z) {
+                                         double beta, const QRef* z, int dots = 1) {
+    // scale (H - shift)(m v) = (scale m)(H - shift) v
+    scale *= v.m;
+    if (z) beta *= z->m;
+    w.m = 1.0;
     const bool hz = z && beta != 0.0;
     const double full = std::ldexp(1.0, qbits);
     q_plan(hprm, plan_input(op, scale, shift, beta, v.E, hz ? z->E : v.E, hz, v.maxq / full,
                             hz ? z->maxq / full : 1.0));
     MB_CUDA(cudaMemcpyAsync(prm.p, hprm, sizeof(QParams), cudaMemcpyHostToDevice, st));
     zero_max();
-    q_apply_whole(op, v.p, w.p, hz ? z->p : nullptr, (const QParams*)prm.p, part(), mor(), 1, st);
+    q_apply_whole(op, v.p, w.p, hz ? z->p : nullptr, (const QParams*)prm.p, part(), mor(), dots, st);
     double mq = 0.0;
     const double* h = fetch_apply(&mq);
     w.E = hprm->ey;
     w.maxq = std::max(mq, 1.0);
-    return {h[0] * std::ldexp(1.0, v.E + w.E + 32), h[1] * std::ldexp(1.0, 2 * w.E + 32)};
+    return {v.m * h[0] * std::ldexp(1.0, v.E + w.E + 32), h[1] * std::ldexp(1.0, 2 * w.E + 32)};
   }
 
   void reserve_basis(int64_t k) {
@@ -420,6 +433,7 @@ struct QKrylov {
   }
 
   void store_basis(const QRef& v) {
+    MB_REQUIRE(v.m == 1.0, MB_ERR_INVALID_ARG, "basis vector with a pending normalisation");
     const int64_t j = (int64_t)basis_E.size();
     MB_REQUIRE(j < basis_cap, MB_ERR_CAPACITY, "basis full");
     MB_CUDA(cudaMemcpyAsync((char*)basis.p + sizeof(longlong2) * (size_t)n * (size_t)j, v.p,
@@ -489,8 +503,12 @@ struct QKrylov {
       if (it + 1 < k) betas.push_back(beta);
       std::swap(vp, vc);  // v_prev <- v
       std::swap(vc, ww);  // v <- w / beta
-      QRef cur = *vc;
-      lincomb(*vc, &cur, 1.0 / beta, nullptr, 0.0);
+      if (reorth_on) {  // the basis stores normalised mantissas
+        QRef cur = *vc;
+        lincomb(*vc, &cur, 1.0 / beta, nullptr, 0.0);
+      } else {  // folded into the next apply and combination
+        vc->m = 1.0 / beta;
+      }
       beta_prev = beta;
       if (conv_tol > 0.0 && check_every > 0 && (steps % check_every) == 0 && it + 1 < k) {
         std::vector<double> d(alphas), e(betas);
