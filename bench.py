@@ -869,7 +869,7 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 PROBES = ("q64_apply", "fp64_apply", "fp32_apply", "engine_persistent", "engine_grouped",
           "engine_persistent_fixed", "engine_fused", "momentum_csr", "momentum_csr_q64",
-          "q64_lanczos")
+          "q64_lanczos", "fp32_lanczos_refined")
 
 
 def run_probe(args):
@@ -904,6 +904,23 @@ def run_probe(args):
         torch.cuda.synchronize()
         out = {"probe": name, "case": args.case, "dim": op.dimension(), "apply_shape": shape,
                "launches": args.steps}
+    elif name == "fp32_lanczos_refined":
+        # --steps plain Lanczos steps on complex64 vectors with FP64 alpha/beta,
+        # then the FP64 Rayleigh-Ritz refinement (the precision path), on
+        # --case
+        w = CASES[args.case]
+        L = 1
+        for d in w["lattice"]:
+            L *= d
+        basis = mb.FermionBasis.with_fixed_particle_number_and_spin(L, w["n_up"] + w["n_down"],
+                                                                    w["n_up"] - w["n_down"])
+        op = mb.GpuHubbardOperator(basis, mb._Hubbard(w["t"], w["U"], w["lattice"]), mb.PREC_F32)
+        x = op.seed_vector(0, order=mb.ORDER_TENSOR)
+        r = mb.find_min_eigenpair(op, args.steps, x, order=mb.ORDER_TENSOR, want_vector=False,
+                                  refine=True)
+        torch.cuda.synchronize()
+        out = {"probe": name, "case": args.case, "dim": op.dimension(), "steps": r.steps,
+               "e0": r.value}
     elif name == "q64_lanczos":
         # --steps plain Lanczos steps on the Q64 operator of --case (the
         # ground-state solve's recurrence: apply with fused dots, w -= alpha v,

@@ -888,16 +888,22 @@ struct Krylov {
 // problem is an operator view and a start vector x (complex128, tensor
 // order).  Its Krylov space span{x, Hx, H^2 x, ...} is built with FP64
 // vectors and arithmetic: Lanczos with full re-orthogonalisation (w = H q_j
-// orthogonalised against q_0..q_j by classical Gram-Schmidt applied twice;
-// alpha_j is w's total coefficient on q_j, beta_j the norm of what remains).
-// After each step the lowest eigenvalue of T_(j+1) is the estimate; steps
-// continue until it settles to kRefineSettle relative (at least kRefineMinSteps),
-// the space breaks down, or the problem's step budget (kRefineMaxSteps,
-// fewer where the basis would pass kRefineBasisBytes).  The problems advance
+// orthogonalised against q_0..q_j by classical Gram-Schmidt, kRefinePasses
+// passes; alpha_j is w's total coefficient on q_j, beta_j the norm of what
+// remains).  One pass is the recurrence itself (the coefficients on q_j and
+// q_j-1) plus a first-order correction against the older vectors: over the
+// few steps of a refinement its loss of orthogonality stays at the rounding
+// level (~1e-15 a step), and a second pass (CGS2) doubled the FP64-pipe-bound
+// projections (0.23 s of a 1D L=16 8+8 solve).  After each step the lowest
+// eigenvalue of T_(j+1) is the estimate; steps continue until it settles to
+// kRefineSettle relative (at least kRefineMinSteps), the space breaks down,
+// or the problem's step budget (kRefineMaxSteps, fewer where the basis would
+// pass kRefineBasisBytes).  The problems advance
 // in lockstep: their kernels queue on one stream and the host waits once per
 // step for all of them.
 // ---------------------------------------------------------------------------
 namespace {
+constexpr int kRefinePasses = 1;
 constexpr size_t kRefineBasisBytes = (size_t)24 << 30;  // one problem's basis at most
 constexpr size_t kRefineChunkBytes = (size_t)4 << 30;   // bases of problems run together
 
@@ -992,7 +998,7 @@ static void refine_chunk(std::vector<RefineRun>& runs, RefineBufs& bufs, cudaStr
       // norm of the rest at dc[4 cap + 1]
       void* w = r.col(j + 1);
       launch_apply(r.p->v, MB_PREC_F64, r.col(j), w, 1.0, 0.0, 0.0, nullptr, nullptr, 0, st);
-      for (int pass = 0; pass < 2; ++pass) {
+      for (int pass = 0; pass < kRefinePasses; ++pass) {
         double* c = r.dc + 2 * (size_t)r.cap * pass;
         launch_multi_dot(MB_PREC_F64, MB_PREC_F64, r.n, r.q, r.n, j + 1, w, pp, st);
         launch_reduce(pp, multi_dot_grid(r.n), 2 * (j + 1), c, st);
@@ -1004,7 +1010,9 @@ static void refine_chunk(std::vector<RefineRun>& runs, RefineBufs& bufs, cudaStr
     sync_all();
     for (auto& r : runs) {
       if (r.done) continue;
-      r.alpha.push_back(r.hc[2 * j] + r.hc[2 * (size_t)r.cap + 2 * j]);
+      double a = 0.0;
+      for (int pass = 0; pass < kRefinePasses; ++pass) a += r.hc[2 * (size_t)r.cap * pass + 2 * j];
+      r.alpha.push_back(a);
       const double b = std::sqrt(r.hc[nn_off(r) + 1]);
       std::vector<double> d(r.alpha), e(r.beta);
       MB_REQUIRE(tridiag_eig((int)d.size(), d, e, nullptr), MB_ERR_EIG_FAILED,
