@@ -247,8 +247,9 @@ typedef struct {
   int passes;
   int row_split;
   int table_bits;
-  int prefetch;   /* 1: each warp prefetches its next column group's up-hop
-                     lines into L2 (any lattice operator) */
+  int prefetch;   /* 1: before its down hops, each warp asks L2 for the
+                     up-hop lines of its column group, one 128-byte line a
+                     lane (any lattice operator) */
   int table_stage; /* 1: each warp copies its next column group's down-table
                       words into its own shared buffer (cp.async) while it
                       finishes the current one (MB_PREC_Q64, one pass, 32-bit

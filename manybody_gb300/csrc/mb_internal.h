@@ -267,6 +267,26 @@ SignedLists signed_lists(const HopTable& t, int64_t D);
 // warp's 16-byte gather from the staged row then takes 4 wavefronts, not
 // the ~8 of the hop order.  Padding takes a zero element in a free group.
 constexpr int kSlicedPads = 8;
+
+#ifdef __CUDACC__
+// Apply shape prefetch = 1: before its down hops, a warp asks L2 for the
+// up-hop operands of its column group g, the segments X[s_up[k], 32g .. 32g+31]
+// (ES-byte elements, 32·ES bytes each), so they are on their way while the
+// down hops run from shared memory.  Each lane takes one 128-byte line, so one
+// instruction covers 32·128/(32·ES) segments; lines past the row's end are
+// skipped, so every address stays inside the neighbour's row.
+template <int ES>
+__device__ __forceinline__ void prefetch_up_group(const void* x, const uint32_t* s_up, int nu,
+                                                  int64_t g, int lane, uint32_t row_bytes) {
+  constexpr int kLines = ES / 4;     // lines of one segment
+  constexpr int kPer = 32 / kLines;  // segments one instruction covers
+  const uint32_t lo = (uint32_t)g * (32u * ES) + (uint32_t)(lane % kLines) * 128u;
+  if (lo >= row_bytes) return;
+  const char* xg = static_cast<const char*>(x) + lo;
+  for (int k = lane / kLines; k < nu; k += kPer)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(xg + (uint64_t)s_up[k] * row_bytes));
+}
+#endif
 struct SlicedTable {
   std::vector<uint32_t> ent;
   std::vector<int32_t> grp;
@@ -331,8 +351,8 @@ struct OpView {
   // sliced-table entry width (32 or 16 bits).
   int row_split;
   int table_bits;
-  // 1: before a column group, each warp prefetches the up-hop lines of its
-  // next group into L2 (prefetch.global.L2)
+  // 1: before its down hops, each warp prefetches the up-hop lines of its
+  // column group into L2 (prefetch_up_group)
   int up_prefetch;
   // 1: each warp copies its next column group's down-table words into a
   // warp-private shared buffer (cp.async) while it finishes the current one

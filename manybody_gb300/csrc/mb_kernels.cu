@@ -125,8 +125,8 @@ static int max_smem_optin() {
 // zero elements past the row), while the up hops read the neighbour rows X[r_up', c] from
 // L2/HBM with coalesced 8/16-byte loads, the row's sign-sorted target list
 // in shared memory (added, then subtracted).  Warp w takes the 32-column
-// groups w, w + 32, ... (with up_prefetch set it first prefetches its next
-// group's up-hop lines into L2).
+// groups w, w + 32, ... (with up_prefetch set it asks L2 for the group's
+// up-hop lines before its down hops).
 // ---------------------------------------------------------------------------
 constexpr int kApplyThreads = 1024;
 // CTAs per SM: complex64 rows are half the size, and two CTAs per SM (32
@@ -182,12 +182,7 @@ __device__ __forceinline__ void apply_rows(
       const int64_t c = (g << 5) + lane;
       const bool live = c < Dd;
       const int64_t cl = live ? c : Dd - 1;
-      if (v.up_prefetch && g + nwarps < ngroups) {
-        const int64_t cn = min(((g + nwarps) << 5) + lane, Dd - 1);
-        const char* xn = reinterpret_cast<const char*>(x + cn);
-        for (int k = 0; k < nu; ++k)
-          asm volatile("prefetch.global.L2 [%0];" ::"l"(xn + (uint64_t)s_up[k] * row_bytes));
-      }
+      if (v.up_prefetch) prefetch_up_group<(int)sizeof(V2)>(x, s_up, nu, g, lane, row_bytes);
       T ar = T(0), ai = T(0);
       const int2 gi = __ldg(reinterpret_cast<const int2*>(v.dn_sgrp) + g);
       auto hop = [&](uint32_t e) {

@@ -1344,7 +1344,7 @@ int mb_op_get_apply_shape(mb_op_t op, mb_apply_shape* shape) {
     shape->passes = op->apply_passes;
     shape->row_split = std::max(1, op->view.row_split);
     shape->table_bits = op->view.table_bits == 16 ? 16 : 32;
-    shape->prefetch = op->view.up_prefetch ? 1 : 0;
+    shape->prefetch = op->view.up_prefetch;
     shape->table_stage = op->view.table_stage ? 1 : 0;
     shape->csr_lanes = op->view.csr_lanes;
   });

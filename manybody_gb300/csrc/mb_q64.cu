@@ -238,8 +238,8 @@ void launch_q_reduce128(const void* part, int nblocks, double* out, cudaStream_t
 //     column's count of negative hops is added back once;
 //   up hops: the row's sign-sorted target list (uniform across the CTA):
 //     coalesced 16-byte loads x[r',c], summed then subtracted, no sign work;
-//     with up_prefetch set, the lines of the warp's next group are
-//     prefetched into L2 first (the autotuner's choice; off by default).
+//     with up_prefetch set, the warp asks L2 for its group's up-hop lines
+//     before the down hops (an apply shape the autotuner may pick).
 // Hops are summed in pairs (three-operand 64-bit adds).
 // ---------------------------------------------------------------------------
 constexpr int kQThreads = 1024;
@@ -495,13 +495,7 @@ k_apply_q(OpView v, const longlong2* __restrict__ x, longlong2* y, const longlon
       const int64_t c = (g << 5) + lane;
       const bool live = c < Dd;
       const int64_t cl = live ? c : Dd - 1;
-      if (!UPS && v.up_prefetch && g + gstep < ngroups) {
-        // the up-hop lines of this warp's next group, into L2 ahead of use
-        const int64_t cn = min(((g + gstep) << 5) + lane, Dd - 1);
-        const char* xn = reinterpret_cast<const char*>(x + cn);
-        for (int k = 0; k < nu; ++k)
-          asm volatile("prefetch.global.L2 [%0];" ::"l"(xn + (uint64_t)s_up[k] * row_bytes));
-      }
+      if (!UPS && v.up_prefetch) prefetch_up_group<16>(x, s_up, nu, g, lane, row_bytes);
       long long sr = 0, si = 0;
       if (TS) {
         asm volatile("cp.async.wait_all;" ::: "memory");  // this group's words
