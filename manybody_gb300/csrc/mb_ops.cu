@@ -799,14 +799,21 @@ struct Krylov {
     int64_t steps = 0;
     double last_ritz = 0.0;
     bool have_ritz = false;
+    // FP32 runs without re-orthogonalisation keep their Lanczos vectors
+    // unnormalised, u_j = s_j v_j with s_j = beta_(j-1): the next apply and
+    // the combination take 1/s_j in their coefficients, so a step is two
+    // vector passes (apply, combination) instead of three.  Other runs keep
+    // s_j = 1 and normalise as the reference does.
+    const bool fold = prec == MB_PREC_F32 && !reorth;
+    double s_curr = 1.0, s_prev = 1.0;
     for (int64_t it = 0; it < k; ++it) {
       if (reorth) launch_convert(prec, basis_prec, n, v_curr.p, basis_col(it), st);
       // w = scale*H v - beta_prev v_prev ; alpha = Re<v, w>   (lanczos.h:25-33)
-      launch_apply(op->view, prec, v_curr.p, w.p, scale, 0.0, -beta_prev,
+      launch_apply(op->view, prec, v_curr.p, w.p, scale / s_curr, 0.0, -beta_prev / s_prev,
                    beta_prev != 0.0 ? v_prev.p : nullptr, red.p(), 1, st);
-      const double alpha = red.fetch(grid_apply, 3, st)[0];
+      const double alpha = red.fetch(grid_apply, 3, st)[0] / s_curr;
       // w -= alpha v ; beta = ||w||                             (lanczos.h:34-36)
-      launch_axpby(prec, n, -alpha, 0.0, v_curr.p, 1.0, 0.0, w.p, red.p(), 1, st);
+      launch_axpby(prec, n, -alpha / s_curr, 0.0, v_curr.p, 1.0, 0.0, w.p, red.p(), 1, st);
       double nrm2 = red.fetch(grid_blas, 3, st)[1];
       if (reorth) nrm2 = this->reorth((int)(it + 1), nrm2);
       const double beta = std::sqrt(nrm2);
@@ -817,7 +824,12 @@ struct Krylov {
       // v_prev <- v, v <- w / beta                               (lanczos.h:113-121)
       std::swap(v_prev.p, v_curr.p);
       std::swap(v_curr.p, w.p);
-      launch_axpby(prec, n, 0.0, 0.0, nullptr, 1.0 / beta, 0.0, v_curr.p, nullptr, 0, st);
+      if (fold) {
+        s_prev = s_curr;
+        s_curr = beta;
+      } else {
+        launch_axpby(prec, n, 0.0, 0.0, nullptr, 1.0 / beta, 0.0, v_curr.p, nullptr, 0, st);
+      }
       beta_prev = beta;
       if (conv_tol > 0.0 && check_every > 0 && (steps % check_every) == 0 && it + 1 < k) {
         std::vector<double> d(alphas), e(betas);
@@ -853,16 +865,30 @@ struct Krylov {
     launch_axpby(prec, n, 1.0 / b_norm, 0.0, b, 0.0, 0.0, v_curr.p, nullptr, 0, st);
     MB_CUDA(cudaMemsetAsync(v_prev.p, 0, vb, st));
     launch_axpby(prec, n, y[0].real(), y[0].imag(), v_curr.p, 0.0, 0.0, x, nullptr, 0, st);
+    // FP32: unnormalised vectors u_j = beta_(j-1) v_j as in pass one, and the
+    // whole recurrence in the apply, alpha_j being known here: w =
+    // (scale/s_j)(H - alpha_j/scale) u_j - (beta_(j-1)/s_(j-1)) u_(j-1).
+    const bool fold = prec == MB_PREC_F32;
+    double s_curr = 1.0, s_prev = 1.0;
     for (int64_t j = 0; j + 1 < steps; ++j) {
       const double alpha_j = alphas[(size_t)j], beta_j = betas[(size_t)j];
       const double beta_prev = j == 0 ? 0.0 : betas[(size_t)j - 1];
-      launch_apply(op->view, prec, v_curr.p, w.p, scale, 0.0, -beta_prev,
-                   beta_prev != 0.0 ? v_prev.p : nullptr, nullptr, 0, st);
-      // w = (w - alpha v) / beta
-      launch_axpby(prec, n, -alpha_j / beta_j, 0.0, v_curr.p, 1.0 / beta_j, 0.0, w.p, nullptr, 0,
-                   st);
-      launch_axpby(prec, n, y[(size_t)j + 1].real(), y[(size_t)j + 1].imag(), w.p, 1.0, 0.0, x,
-                   nullptr, 0, st);
+      if (fold) {
+        launch_apply(op->view, prec, v_curr.p, w.p, scale / s_curr, alpha_j / scale,
+                     -beta_prev / s_prev, beta_prev != 0.0 ? v_prev.p : nullptr, nullptr, 0, st);
+        launch_axpby(prec, n, y[(size_t)j + 1].real() / beta_j, y[(size_t)j + 1].imag() / beta_j,
+                     w.p, 1.0, 0.0, x, nullptr, 0, st);
+        s_prev = s_curr;
+        s_curr = beta_j;
+      } else {
+        launch_apply(op->view, prec, v_curr.p, w.p, scale, 0.0, -beta_prev,
+                     beta_prev != 0.0 ? v_prev.p : nullptr, nullptr, 0, st);
+        // w = (w - alpha v) / beta
+        launch_axpby(prec, n, -alpha_j / beta_j, 0.0, v_curr.p, 1.0 / beta_j, 0.0, w.p, nullptr,
+                     0, st);
+        launch_axpby(prec, n, y[(size_t)j + 1].real(), y[(size_t)j + 1].imag(), w.p, 1.0, 0.0, x,
+                     nullptr, 0, st);
+      }
       std::swap(v_prev.p, v_curr.p);
       std::swap(v_curr.p, w.p);
     }
