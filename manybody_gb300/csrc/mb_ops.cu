@@ -916,11 +916,11 @@ struct Krylov {
 // vectors and arithmetic: Lanczos with full re-orthogonalisation (w = H q_j
 // orthogonalised against q_0..q_j by classical Gram-Schmidt, kRefinePasses
 // passes; alpha_j is w's total coefficient on q_j, beta_j the norm of what
-// remains).  One pass is the recurrence itself (the coefficients on q_j and
-// q_j-1) plus a first-order correction against the older vectors: over the
-// few steps of a refinement its loss of orthogonality stays at the rounding
-// level (~1e-15 a step), and a second pass (CGS2) doubled the FP64-pipe-bound
-// projections (0.23 s of a 1D L=16 8+8 solve).  After each step the lowest
+// remains).  Two passes (CGS2): with one, orthogonality decays by about
+// |theta| / beta a step, and a start vector close to an eigenvector of an
+// operator far from zero (beta_0 ~ 1e-5, |E0| ~ 100: 1D L=14 13+13 at U=9.2)
+// lost it within six steps, its lowest Ritz value falling 7 % below E0; the
+// second pass holds it at ~1e-17.  After each step the lowest
 // eigenvalue of T_(j+1) is the estimate; steps continue until it settles to
 // kRefineSettle relative (at least kRefineMinSteps), the space breaks down,
 // or the problem's step budget (kRefineMaxSteps, fewer where the basis would
@@ -929,7 +929,7 @@ struct Krylov {
 // step for all of them.
 // ---------------------------------------------------------------------------
 namespace {
-constexpr int kRefinePasses = 1;
+constexpr int kRefinePasses = 2;
 constexpr size_t kRefineBasisBytes = (size_t)24 << 30;  // one problem's basis at most
 constexpr size_t kRefineChunkBytes = (size_t)4 << 30;   // bases of problems run together
 

@@ -369,3 +369,26 @@ def test_kept_basis_matches_replay(mb, cuda, persistent):
                                     persistent=persistent, basis_limit=0)
     for a, b in zip(kept, replay):
         assert a.e0 == b.e0 and a.e0_raw == b.e0_raw and a.steps == b.steps
+
+
+def test_refinement_far_from_zero_in_engine(mb, cuda):
+    """A served request whose refinement needs the second Gram-Schmidt pass:
+    1D L=14, N_up = N_down = 13, U = 9.24, seed 44 (E0 ~ 107, start vector
+    close to an eigenvector).  Alone and beside the other sectors, every
+    refined energy within 1e-8."""
+    u = 9.240847688353895
+    far = mb.sector((14,), 13, 13, 1.0, u)
+    e_far = exact_e0((14,), 13, 13, u)
+    eng = mb.Engine()  # as served: stop at Ritz stability 1e-10, then refine
+    rid = eng.try_submit(far, seed=44, kmax=400, rel_tol=1e-10, refine=True)
+    for _ in range(1000):
+        eng.step(1)
+        if rid in eng.completed():
+            break
+    served = eng.poll(rid)
+    assert abs(served.e0 - e_far) <= 1e-8 * abs(e_far)
+    alone = mb.batch_ground_states([far], seeds=[44], kmax=150, autotune=False)[0]
+    assert abs(alone.e0 - e_far) <= 1e-8 * abs(e_far)
+    mixed = mb.batch_ground_states([far] + descs(mb), seeds=[44] * 9, kmax=150, autotune=False)
+    for r, e in zip(mixed, [e_far] + [exact_e0(*x) for x in SECTORS]):
+        assert abs(r.e0 - e) <= 1e-8 * abs(e)

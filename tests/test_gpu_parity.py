@@ -428,6 +428,22 @@ def test_fp32_refinement_past_convergence(mb, cuda):
     assert abs(ref.value - e_ref) <= 1e-8 * abs(e_ref)
 
 
+def test_refinement_far_from_zero(mb, cuda):
+    """1D L=14, N_up = N_down = 13 at U = 9.24 (196 states, spectrum 107..121):
+    the FP32 Ritz vector is close to an eigenvector (beta_0 ~ 1e-5) of an
+    operator far from zero, where the refinement's Gram-Schmidt needs its
+    second pass (with one, orthogonality decays by ~|theta|/beta a step and
+    the lowest Ritz value falls below E0).  Refined E0 within 1e-8."""
+    u = 9.240847688353895
+    _, _, op = make(mb, [14], 1.0, u, 13, 13, prec=1)
+    E = np.linalg.eigvalsh(oracle.hubbard_csc([14], 1.0, u, 13, 13).to_dense())
+    for seed in range(4):
+        s = op.seed_vector(seed, order=mb.ORDER_TENSOR)
+        r = mb.find_min_eigenpair(op, 400, s, order=mb.ORDER_TENSOR, conv_tol=1e-10,
+                                  want_vector=False, refine=True)
+        assert abs(r.value - E[0]) <= 1e-8 * abs(E[0])
+
+
 def test_solve_linear_system(mb, cuda):
     """solve(op, b, k, solver) (lanczos.h:220-237) with a tridiagonal solver
     T y = e1: over the full Krylov space x = H^-1 b."""
