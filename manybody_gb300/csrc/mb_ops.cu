@@ -868,7 +868,7 @@ struct Krylov {
     // FP32: unnormalised vectors u_j = beta_(j-1) v_j as in pass one, and the
     // whole recurrence in the apply, alpha_j being known here: w =
     // (scale/s_j)(H - alpha_j/scale) u_j - (beta_(j-1)/s_(j-1)) u_(j-1).
-    const bool fold = prec == MB_PREC_F32;
+    const bool fold = prec == MB_PREC_F32 && scale != 0.0;  // the shift is alpha_j / scale
     double s_curr = 1.0, s_prev = 1.0;
     for (int64_t j = 0; j + 1 < steps; ++j) {
       const double alpha_j = alphas[(size_t)j], beta_j = betas[(size_t)j];
