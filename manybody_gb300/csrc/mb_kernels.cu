@@ -70,26 +70,34 @@ __device__ void block_reduce_store(double (&v)[NC], double* partials) {
   }
 }
 
-// Fixed-order final reduction: out[k] = sum_b partials[b*ncomp + k].
-__global__ void k_reduce(const double* __restrict__ partials, int nblocks, int ncomp,
-                         double* __restrict__ out) {
-  __shared__ double s[256];
-  for (int k = 0; k < ncomp; ++k) {
-    double a = 0.0;
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) a += partials[(size_t)b * ncomp + k];
-    s[threadIdx.x] = a;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-      if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
-      __syncthreads();
+// Fixed-order final reduction: out[k] = sum_b partials[b*ncomp + k].  Warp w
+// takes the components w, w + 32, ...; lane l sums the partials l, l + 32, ...
+// in four chains (partial l + 128 i + 32 q into chain q, then the chains in
+// order), and the lanes meet in a shuffle tree: no block barrier, and the
+// chains keep four loads in flight a lane.
+__global__ void __launch_bounds__(1024)
+k_reduce(const double* __restrict__ partials, int nblocks, int ncomp, double* __restrict__ out) {
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int k = threadIdx.x >> 5; k < ncomp; k += nw) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int b = lane;
+    for (; b + 96 < nblocks; b += 128) {
+      a0 += partials[(size_t)b * ncomp + k];
+      a1 += partials[(size_t)(b + 32) * ncomp + k];
+      a2 += partials[(size_t)(b + 64) * ncomp + k];
+      a3 += partials[(size_t)(b + 96) * ncomp + k];
     }
-    if (threadIdx.x == 0) out[k] = s[0];
-    __syncthreads();
+    for (; b < nblocks; b += 32) a0 += partials[(size_t)b * ncomp + k];
+    double a = (a0 + a1) + (a2 + a3);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) out[k] = a;
   }
 }
 
 void launch_reduce(const double* partials, int nblocks, int ncomp, double* out, cudaStream_t st) {
-  k_reduce<<<1, 256, 0, st>>>(partials, nblocks, ncomp, out);
+  const int warps = ncomp < 1 ? 1 : (ncomp > 32 ? 32 : ncomp);
+  k_reduce<<<1, 32 * warps, 0, st>>>(partials, nblocks, ncomp, out);
   MB_CUDA(cudaGetLastError());
 }
 
