@@ -851,7 +851,13 @@ struct Krylov {
   }
 
   // Pass two (lanczos.h:177-218): x = sum_j y_j v_j by re-running the
-  // recurrence; y complex.  x in tensor order, op precision.
+  // recurrence; y complex.  x in tensor order, op precision.  Each step runs
+  // pass one's kernels with pass one's coefficients (the apply, the update,
+  // the normalisation of an FP64 run), so the replayed vectors are pass one's
+  // bits: after a Ritz pair converges the recurrence amplifies any rounding
+  // difference, and a replay in other arithmetic drifted from the vectors
+  // whose T_m gave y (an FP32 Ritz vector 6 % off the ground state of a
+  // 49-state sector).
   void pass_two(const void* b, int64_t steps, double scale, const std::vector<double>& alphas,
                 const std::vector<double>& betas, double b_norm,
                 const std::vector<std::complex<double>>& y, void* x) {
@@ -865,32 +871,25 @@ struct Krylov {
     launch_axpby(prec, n, 1.0 / b_norm, 0.0, b, 0.0, 0.0, v_curr.p, nullptr, 0, st);
     MB_CUDA(cudaMemsetAsync(v_prev.p, 0, vb, st));
     launch_axpby(prec, n, y[0].real(), y[0].imag(), v_curr.p, 0.0, 0.0, x, nullptr, 0, st);
-    // FP32: unnormalised vectors u_j = beta_(j-1) v_j as in pass one, and the
-    // whole recurrence in the apply, alpha_j being known here: w =
-    // (scale/s_j)(H - alpha_j/scale) u_j - (beta_(j-1)/s_(j-1)) u_(j-1).
-    const bool fold = prec == MB_PREC_F32 && scale != 0.0;  // the shift is alpha_j / scale
+    const bool fold = prec == MB_PREC_F32;  // pass one's unnormalised FP32 vectors
     double s_curr = 1.0, s_prev = 1.0;
     for (int64_t j = 0; j + 1 < steps; ++j) {
       const double alpha_j = alphas[(size_t)j], beta_j = betas[(size_t)j];
       const double beta_prev = j == 0 ? 0.0 : betas[(size_t)j - 1];
+      launch_apply(op->view, prec, v_curr.p, w.p, scale / s_curr, 0.0, -beta_prev / s_prev,
+                   beta_prev != 0.0 ? v_prev.p : nullptr, red.p(), 1, st);
+      launch_axpby(prec, n, -alpha_j / s_curr, 0.0, v_curr.p, 1.0, 0.0, w.p, red.p(), 1, st);
+      std::swap(v_prev.p, v_curr.p);
+      std::swap(v_curr.p, w.p);
       if (fold) {
-        launch_apply(op->view, prec, v_curr.p, w.p, scale / s_curr, alpha_j / scale,
-                     -beta_prev / s_prev, beta_prev != 0.0 ? v_prev.p : nullptr, nullptr, 0, st);
-        launch_axpby(prec, n, y[(size_t)j + 1].real() / beta_j, y[(size_t)j + 1].imag() / beta_j,
-                     w.p, 1.0, 0.0, x, nullptr, 0, st);
         s_prev = s_curr;
         s_curr = beta_j;
       } else {
-        launch_apply(op->view, prec, v_curr.p, w.p, scale, 0.0, -beta_prev,
-                     beta_prev != 0.0 ? v_prev.p : nullptr, nullptr, 0, st);
-        // w = (w - alpha v) / beta
-        launch_axpby(prec, n, -alpha_j / beta_j, 0.0, v_curr.p, 1.0 / beta_j, 0.0, w.p, nullptr,
-                     0, st);
-        launch_axpby(prec, n, y[(size_t)j + 1].real(), y[(size_t)j + 1].imag(), w.p, 1.0, 0.0, x,
-                     nullptr, 0, st);
+        launch_axpby(prec, n, 0.0, 0.0, nullptr, 1.0 / beta_j, 0.0, v_curr.p, nullptr, 0, st);
       }
-      std::swap(v_prev.p, v_curr.p);
-      std::swap(v_curr.p, w.p);
+      // x += y_(j+1) v_(j+1), v_(j+1) = u_(j+1) / s_(j+1)
+      launch_axpby(prec, n, y[(size_t)j + 1].real() / s_curr, y[(size_t)j + 1].imag() / s_curr,
+                   v_curr.p, 1.0, 0.0, x, nullptr, 0, st);
     }
   }
 

@@ -528,7 +528,10 @@ struct QKrylov {
     return steps;
   }
 
-  // x = sum_j y_j v_j by re-running the recurrence (lanczos.h:177-218).
+  // x = sum_j y_j v_j by re-running the recurrence (lanczos.h:177-218) with
+  // pass one's operations and coefficients (the same apply, w -= alpha v, the
+  // 1/beta folded into the next vector), so the replayed vectors are pass
+  // one's mantissas and exponents.
   void pass_two(const QRef& b, double b_norm, int64_t steps, double scale,
                 const std::vector<double>& alphas, const std::vector<double>& betas,
                 const std::vector<std::complex<double>>& y, QRef& x, QRef* vp, QRef* vc,
@@ -539,11 +542,12 @@ struct QKrylov {
       const double beta_prev = j == 0 ? 0.0 : betas[(size_t)j - 1];
       apply(*ww, *vc, scale, beta_prev, beta_prev != 0.0 ? vp : nullptr);
       QRef wv = *ww;
-      lincomb(*ww, vc, -alphas[(size_t)j] / betas[(size_t)j], &wv, 1.0 / betas[(size_t)j]);
-      QRef xv = x;
-      lincomb(x, &xv, 1.0, ww, y[(size_t)j + 1]);
+      lincomb(*ww, vc, -alphas[(size_t)j], &wv, 1.0);
       std::swap(vp, vc);
       std::swap(vc, ww);
+      vc->m = 1.0 / betas[(size_t)j];
+      QRef xv = x;
+      lincomb(x, &xv, 1.0, vc, y[(size_t)j + 1]);
     }
   }
 

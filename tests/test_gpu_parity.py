@@ -444,6 +444,29 @@ def test_refinement_far_from_zero(mb, cuda):
         assert abs(r.value - E[0]) <= 1e-8 * abs(E[0])
 
 
+@pytest.mark.parametrize("prec", [1, 2])
+def test_replayed_ritz_vector_is_the_ground_state(mb, cuda, prec):
+    """1D L=7, N_up = N_down = 6, U = 0.001 (49 states, E1 - E0 = 1.4e-4): plain
+    Lanczos over all 49 steps loses orthogonality once its Ritz pair converges,
+    and pass two has to rebuild pass one's vectors exactly for the Ritz vector
+    to be the ground state (a replay in other arithmetic gave an FP32 vector
+    6 % off it, overlap 1 - 1.9e-3, and a refined energy 1.5e-7 off).  The
+    refined FP32 energy within 1e-8; overlap with the exact ground state
+    >= 1 - 5e-4 in FP32 (the vector of a Ritz value stable to 1e-9 against a
+    gap of 3.5e-5 |H|), >= 1 - 1e-5 in Q64."""
+    u = 0.001
+    _, _, op = make(mb, [7], 1.0, u, 6, 6, prec=prec)
+    E, V = np.linalg.eigh(oracle.hubbard_csc([7], 1.0, u, 6, 6).to_dense())
+    for seed in (158, 0, 1, 2, 3):
+        s = op.seed_vector(seed)
+        r = mb.find_min_eigenpair(op, 49, s, conv_tol=1e-10, refine=prec == 1)
+        v = r.vector.cpu().numpy()
+        ov = abs(np.vdot(V[:, 0], v)) / np.linalg.norm(v)
+        if prec == 1:
+            assert abs(r.value - E[0]) <= 1e-8 * abs(E[0]), (seed, r.value - E[0])
+        assert ov >= 1 - (5e-4 if prec == 1 else 1e-5), (seed, ov)
+
+
 def test_solve_linear_system(mb, cuda):
     """solve(op, b, k, solver) (lanczos.h:220-237) with a tridiagonal solver
     T y = e1: over the full Krylov space x = H^-1 b."""
