@@ -763,6 +763,60 @@ struct Krylov {
     return (char*)basis.p + elem_bytes(basis_prec) * (size_t)n * (size_t)j;
   }
 
+  // Kept Lanczos vectors: a run without re-orthogonalisation that needs its
+  // Ritz vector keeps the vectors pass one applies (u_0, u_1, ..., in chunks
+  // of kKeepChunk) while a tenth of the device memory stays free, and sums
+  // the Ritz vector from them instead of replaying the recurrence; pass two
+  // remains for a run whose Ritz vector needs more vectors than it kept.
+  static constexpr int64_t kKeepChunk = 16;
+  std::vector<DevBuf> keep;
+  DevBuf keep_coef;
+  int64_t kept = 0;  // u_0 .. u_(kept-1) are kept
+
+  void* keep_col(int64_t j) {
+    return (char*)keep[(size_t)(j / kKeepChunk)].p + vb * (size_t)(j % kKeepChunk);
+  }
+
+  bool keep_room(int64_t j) {
+    if ((size_t)(j / kKeepChunk) < keep.size()) return true;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    const size_t need = vb * (size_t)kKeepChunk;
+    if (need + total_b / 10 > free_b) return false;
+    try {
+      keep.emplace_back(need);
+    } catch (const Error&) {
+      cudaGetLastError();
+      return false;
+    }
+    return true;
+  }
+
+  // x = sum_(j < m) y_j v_j from the kept vectors, v_j = u_j / s_j (s_j =
+  // beta_(j-1) for pass one's unnormalised FP32 vectors, 1 otherwise).
+  void combine_kept(int64_t m, const std::vector<double>& betas,
+                    const std::vector<std::complex<double>>& y, void* x) {
+    const bool fold = prec == MB_PREC_F32;
+    std::vector<double> c(2 * (size_t)m);
+    for (int64_t j = 0; j < m; ++j) {
+      const double sj = fold && j > 0 ? betas[(size_t)j - 1] : 1.0;
+      c[2 * (size_t)j] = -y[(size_t)j].real() / sj;  // multi_axpy subtracts
+      c[2 * (size_t)j + 1] = -y[(size_t)j].imag() / sj;
+    }
+    if (keep_coef.bytes < sizeof(double) * c.size()) keep_coef = DevBuf(sizeof(double) * c.size());
+    MB_CUDA(cudaMemcpyAsync(keep_coef.p, c.data(), sizeof(double) * c.size(),
+                            cudaMemcpyHostToDevice, st));
+    MB_CUDA(cudaMemsetAsync(x, 0, vb, st));
+    for (int64_t j0 = 0; j0 < m; j0 += kKeepChunk) {
+      const int cnt = (int)std::min<int64_t>(kKeepChunk, m - j0);
+      launch_multi_axpy(prec, prec, n, keep_col(j0), n, cnt, (const double*)keep_coef.p + 2 * j0,
+                        x, red.p(), st);
+    }
+  }
+
   // Full re-orthogonalisation of w (squared norm nrm2) against the m stored
   // vectors: classical Gram-Schmidt, w -= V (V^H w), with the DGKS test
   // (Daniel, Gragg, Kaufman and Stewart, Math. Comp. 30 (1976); Parlett's
@@ -786,7 +840,8 @@ struct Krylov {
   // Pass one from b (tensor order, op precision).  Returns steps taken.
   int64_t pass_one(const void* b, int64_t k, double scale, std::vector<double>& alphas,
                    std::vector<double>& betas, double& b_norm, bool reorth, double conv_tol,
-                   int check_every, std::vector<double>* ritz_trace = nullptr) {
+                   int check_every, std::vector<double>* ritz_trace = nullptr,
+                   bool keep_vectors = false) {
     b_norm = norm_of(b);
     MB_REQUIRE(b_norm > kTol, MB_ERR_ZERO_NORM, "Input vector has zero norm");
     alphas.clear();
@@ -806,8 +861,13 @@ struct Krylov {
     // s_j = 1 and normalise as the reference does.
     const bool fold = prec == MB_PREC_F32 && !reorth;
     double s_curr = 1.0, s_prev = 1.0;
+    kept = 0;
     for (int64_t it = 0; it < k; ++it) {
       if (reorth) launch_convert(prec, basis_prec, n, v_curr.p, basis_col(it), st);
+      if (keep_vectors && kept == it && keep_room(it)) {
+        MB_CUDA(cudaMemcpyAsync(keep_col(it), v_curr.p, vb, cudaMemcpyDeviceToDevice, st));
+        kept = it + 1;
+      }
       // w = scale*H v - beta_prev v_prev ; alpha = Re<v, w>   (lanczos.h:25-33)
       launch_apply(op->view, prec, v_curr.p, w.p, scale / s_curr, 0.0, -beta_prev / s_prev,
                    beta_prev != 0.0 ? v_prev.p : nullptr, red.p(), 1, st);
@@ -1118,9 +1178,10 @@ static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
   if (reorth) kr.reserve_basis(k, o.basis_precision);
   std::vector<double> alphas, betas;
   double b_norm = 0.0;
+  const bool refine = o.refine && op->precision == MB_PREC_F32;
   // find_min_eigenpair runs find_max_eigenpair on Negated<Op> (lanczos.h:283-290).
   const int64_t m = kr.pass_one(bt.p, k, sign, alphas, betas, b_norm, reorth, o.conv_tol,
-                                o.check_every);
+                                o.check_every, nullptr, !reorth && (vec || refine));
   if (steps_out) *steps_out = m;
   if (m == 0) {
     *e_out = 0.0;
@@ -1134,7 +1195,6 @@ static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
   MB_REQUIRE(tridiag_eig((int)m, d, e, &z), MB_ERR_EIG_FAILED,
              "Eigenvalue decomposition of T_k failed");
   *e_out = sign * d[(size_t)m - 1];
-  const bool refine = o.refine && op->precision == MB_PREC_F32;
   if (vec || refine) {
     // An FP32 run without re-orthogonalisation that ran all k steps takes
     // its Ritz vector from the first converged checkpoint, before a ghost
@@ -1155,6 +1215,8 @@ static void eigenpair(mb_op_s* op, int64_t k, const void* seed, int order,
     DevBuf xt(kr.vb);
     if (reorth) {
       kr.combine_basis(m, y, xt.p);
+    } else if (mv <= kr.kept) {
+      kr.combine_kept(mv, betas, y, xt.p);
     } else {
       kr.pass_two(bt.p, mv, sign, alphas, betas, b_norm, y, xt.p);
     }
@@ -1196,7 +1258,7 @@ static void evolve(mb_op_s* op, const void* psi0, int order, double t, int64_t k
   if (k > op->dim) k = op->dim;
   std::vector<double> alphas, betas;
   double b_norm = 0.0;
-  const int64_t m = kr.pass_one(bt.p, k, 1.0, alphas, betas, b_norm, false, 0.0, 0);
+  const int64_t m = kr.pass_one(bt.p, k, 1.0, alphas, betas, b_norm, false, 0.0, 0, nullptr, true);
   // expm_tridiagonal_first_column_{unitary,imaginary} (evolve_state.h:22-106)
   std::vector<double> d(alphas), z, e(betas);
   e.resize((size_t)std::max<int64_t>(m - 1, 0));
@@ -1215,7 +1277,8 @@ static void evolve(mb_op_s* op, const void* psi0, int order, double t, int64_t k
     y[(size_t)i] = s * b_norm;  // solve() scales y by ||b|| (lanczos.h:231-233)
   }
   DevBuf xt(kr.vb);
-  kr.pass_two(bt.p, m, 1.0, alphas, betas, b_norm, y, xt.p);
+  if (m <= kr.kept) kr.combine_kept(m, betas, y, xt.p);
+  else kr.pass_two(bt.p, m, 1.0, alphas, betas, b_norm, y, xt.p);
   from_tensor(op, xt.p, out, order, st);
   MB_CUDA(cudaStreamSynchronize(st));
 }
