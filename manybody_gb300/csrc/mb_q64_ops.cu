@@ -29,6 +29,7 @@ struct QBuf {
   }
   QBuf(const QBuf&) = delete;
   QBuf& operator=(const QBuf&) = delete;
+  QBuf(QBuf&& o) noexcept : p(o.p) { o.p = nullptr; }
   QBuf& operator=(QBuf&& o) noexcept {
     std::swap(p, o.p);
     return *this;
@@ -300,6 +301,15 @@ struct QKrylov {
   std::vector<double> basis_max;
   QBuf coef;
   long long* hcoef = nullptr;  // pinned
+  // Kept Lanczos vectors (plain runs that need their Ritz vector): the
+  // mantissas of the vectors pass one applies, with their exponents, bounds
+  // and pending normalisations, in chunks of kQKeepChunk columns while a
+  // tenth of the device memory stays free.  The Ritz vector is summed from
+  // them by pass two's combination sequence (the same bits) without
+  // re-running the recurrence.
+  static constexpr int64_t kQKeepChunk = 16;
+  std::vector<QBuf> keep;
+  std::vector<QRef> kept;
 
   QKrylov(mb_op_s* o, cudaStream_t s)
       : op(o), st(s), n(o->dim), qbits(o->q_qbits),
@@ -481,9 +491,11 @@ struct QKrylov {
   // Pass one from b (Q64, tensor order) (lanczos.h:130-175).
   int64_t pass_one(const QRef& b, double b_norm, int64_t k, double scale,
                    std::vector<double>& alphas, std::vector<double>& betas, bool reorth_on,
-                   double conv_tol, int check_every, QRef* vp, QRef* vc, QRef* ww) {
+                   double conv_tol, int check_every, QRef* vp, QRef* vc, QRef* ww,
+                   bool keep_vectors = false) {
     alphas.clear();
     betas.clear();
+    kept.clear();
     if (k == 0) return 0;
     lincomb(*vc, &b, 1.0 / b_norm, nullptr, 0.0);
     double beta_prev = 0.0;
@@ -492,6 +504,7 @@ struct QKrylov {
     bool have_ritz = false;
     for (int64_t it = 0; it < k; ++it) {
       if (reorth_on) store_basis(*vc);
+      if (keep_vectors && (int64_t)kept.size() == it && keep_room(it)) keep_vector(*vc);
       const double alpha = apply(*ww, *vc, scale, beta_prev, beta_prev != 0.0 ? vp : nullptr).first;
       QRef wv = *ww;
       double nrm2 = lincomb(*ww, vc, -alpha, &wv, 1.0);  // w -= alpha v
@@ -548,6 +561,43 @@ struct QKrylov {
       vc->m = 1.0 / betas[(size_t)j];
       QRef xv = x;
       lincomb(x, &xv, 1.0, vc, y[(size_t)j + 1]);
+    }
+  }
+
+  bool keep_room(int64_t j) {
+    if ((size_t)(j / kQKeepChunk) < keep.size()) return true;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    const size_t need = sizeof(longlong2) * (size_t)n * (size_t)kQKeepChunk;
+    if (need + total_b / 10 > free_b) return false;
+    try {
+      keep.emplace_back(need);
+    } catch (const Error&) {
+      cudaGetLastError();
+      return false;
+    }
+    return true;
+  }
+
+  void keep_vector(const QRef& v) {
+    const int64_t j = (int64_t)kept.size();
+    QRef c = v;
+    c.p = (char*)keep[(size_t)(j / kQKeepChunk)].p +
+          sizeof(longlong2) * (size_t)n * (size_t)(j % kQKeepChunk);
+    MB_CUDA(cudaMemcpyAsync(c.p, v.p, sizeof(longlong2) * (size_t)n, cudaMemcpyDeviceToDevice,
+                            st));
+    kept.push_back(c);
+  }
+
+  // x = sum_(j < steps) y_j v_j from the kept vectors, in pass two's order.
+  void combine_kept(int64_t steps, const std::vector<std::complex<double>>& y, QRef& x) {
+    lincomb(x, &kept[0], y[0], nullptr, 0.0);
+    for (int64_t j = 1; j < steps; ++j) {
+      QRef xv = x;
+      lincomb(x, &xv, 1.0, &kept[(size_t)j], y[(size_t)j]);
     }
   }
 
@@ -608,7 +658,7 @@ void q_eigenpair(mb_op_s* op, int64_t k, const void* seed, int order, const mb_l
   if (reorth) kr.reserve_basis(k);
   std::vector<double> alphas, betas;
   const int64_t m = kr.pass_one(b.r, b_norm, k, sign, alphas, betas, reorth, o.conv_tol,
-                                o.check_every, &vp.r, &vc.r, &w.r);
+                                o.check_every, &vp.r, &vc.r, &w.r, vec && !reorth);
   if (steps_out) *steps_out = m;
   if (m == 0) {
     *e_out = 0.0;
@@ -625,6 +675,7 @@ void q_eigenpair(mb_op_s* op, int64_t k, const void* seed, int order, const mb_l
     for (int64_t i = 0; i < m; ++i) y[(size_t)i] = z[(size_t)(m - 1) * m + i] * b_norm;
     QVec x(n);
     if (reorth) kr.combine_basis(m, y, x.r);
+    else if (m <= (int64_t)kr.kept.size()) kr.combine_kept(m, y, x.r);
     else kr.pass_two(b.r, b_norm, m, sign, alphas, betas, y, x.r, &vp.r, &vc.r, &w.r);
     kr.store(x.r, order, vec);
   }
@@ -690,7 +741,7 @@ void q_evolve(mb_op_s* op, const void* psi0, int order, double t, int64_t krylov
   if (k > n) k = n;
   std::vector<double> alphas, betas;
   const int64_t m = kr.pass_one(b.r, psi_norm, k, 1.0, alphas, betas, false, 0.0, 0, &vp.r,
-                                &vc.r, &w.r);
+                                &vc.r, &w.r, true);
   std::vector<double> d(alphas), z, e(betas);
   e.resize((size_t)std::max<int64_t>(m - 1, 0));
   MB_REQUIRE(tridiag_eig((int)m, d, e, &z), MB_ERR_EIG_FAILED,
@@ -707,7 +758,8 @@ void q_evolve(mb_op_s* op, const void* psi0, int order, double t, int64_t krylov
     y[(size_t)i] = s * psi_norm;
   }
   QVec x(n);
-  kr.pass_two(b.r, psi_norm, m, 1.0, alphas, betas, y, x.r, &vp.r, &vc.r, &w.r);
+  if (m <= (int64_t)kr.kept.size()) kr.combine_kept(m, y, x.r);
+  else kr.pass_two(b.r, psi_norm, m, 1.0, alphas, betas, y, x.r, &vp.r, &vc.r, &w.r);
   kr.store(x.r, order, out);
 }
 
