@@ -313,9 +313,9 @@ int mb_lanczos_pass_two(mb_op_t op, const void* b_dev, int order, double scale,
 /* find_min_eigenpair (lanczos.h:283-290): Lanczos on Negated<H> from the given
  * seed vector (the reference draws an unseeded arma::randu seed,
  * linear_operator.h:26-32), eig of T, the Ritz vector.  Without
- * re-orthogonalisation (complex128 / complex64 operators) pass one keeps its
- * vectors while a tenth of the device memory stays free and the Ritz vector
- * is summed from them; pass two replays the recurrence otherwise.  vec_dev
+ * re-orthogonalisation pass one keeps its vectors while a tenth of the
+ * device memory stays free and the Ritz vector is summed from them; pass two
+ * replays the recurrence otherwise.  vec_dev
  * may be NULL.  steps_out (may be NULL) receives the Lanczos steps taken. */
 int mb_find_min_eigenpair(mb_op_t op, int64_t k, const void* seed_dev, int order,
                           const mb_lanczos_opts* opts, double* e0, void* vec_dev,
