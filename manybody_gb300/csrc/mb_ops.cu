@@ -983,9 +983,9 @@ struct Krylov {
 // eigenvalue of T_(j+1) is the estimate; steps continue until it settles to
 // kRefineSettle relative (at least kRefineMinSteps), the space breaks down,
 // or the problem's step budget (kRefineMaxSteps, fewer where the basis would
-// pass kRefineBasisBytes).  The problems advance
-// in lockstep: their kernels queue on one stream and the host waits once per
-// step for all of them.
+// pass kRefineBasisBytes).  The problems advance in lockstep: their kernels
+// queue on kRefineLanes streams and the host waits once per step for all of
+// them.
 // ---------------------------------------------------------------------------
 namespace {
 constexpr int kRefinePasses = 2;
@@ -1026,16 +1026,38 @@ struct RefineSizes {
     pcomps = std::max(pcomps, o.pcomps);
   }
 };
+// The problems of a group spread over kRefineLanes streams (problem i on
+// lane i mod kRefineLanes, each lane with its own partial sums), so the small
+// sectors' latency-bound kernels overlap on the device; every problem's
+// kernels and their order are the same as on one stream, so are its bits.
+constexpr int kRefineLanes = 8;
 struct RefineBufs {
   DevBuf q, c, part;
+  size_t pstride = 0;  // doubles of partial sums a lane
   double* host = nullptr;
+  cudaStream_t lane[kRefineLanes] = {};
+  cudaEvent_t fork = nullptr, done[kRefineLanes] = {};
   explicit RefineBufs(const RefineSizes& z)
-      : q(z.qbytes), c(sizeof(double) * z.cwords), part(sizeof(double) * (size_t)z.pblocks * z.pcomps) {
+      : q(z.qbytes), c(sizeof(double) * z.cwords),
+        part(sizeof(double) * kRefineLanes * (size_t)z.pblocks * z.pcomps),
+        pstride((size_t)z.pblocks * z.pcomps) {
     MB_CUDA(cudaMallocHost(&host, sizeof(double) * z.cwords));
+    MB_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    for (int k = 0; k < kRefineLanes; ++k) {
+      MB_CUDA(cudaStreamCreateWithFlags(&lane[k], cudaStreamNonBlocking));
+      MB_CUDA(cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming));
+    }
   }
   ~RefineBufs() {
+    for (int k = 0; k < kRefineLanes; ++k) {
+      if (lane[k]) cudaStreamDestroy(lane[k]);
+      if (done[k]) cudaEventDestroy(done[k]);
+    }
+    if (fork) cudaEventDestroy(fork);
     if (host) cudaFreeHost(host);
   }
+  RefineBufs(const RefineBufs&) = delete;
+  RefineBufs& operator=(const RefineBufs&) = delete;
 };
 
 static void refine_chunk(std::vector<RefineRun>& runs, RefineBufs& bufs, cudaStream_t st) {
@@ -1055,45 +1077,59 @@ static void refine_chunk(std::vector<RefineRun>& runs, RefineBufs& bufs, cudaStr
       co += 4 * (size_t)r.cap + 4;
     }
   }
-  double* pp = (double*)bufs.part.p;
+  const int nl = std::min<int>(kRefineLanes, (int)runs.size());
+  auto ls = [&](size_t i) { return bufs.lane[i % kRefineLanes]; };
+  auto pp = [&](size_t i) { return (double*)bufs.part.p + bufs.pstride * (i % kRefineLanes); };
+  // the lanes start after the caller's stream (the start vectors), and the
+  // caller's stream waits for every lane before it reads the coefficients
+  MB_CUDA(cudaEventRecord(bufs.fork, st));
+  for (int k = 0; k < nl; ++k) MB_CUDA(cudaStreamWaitEvent(bufs.lane[k], bufs.fork, 0));
   auto sync_all = [&] {
+    for (int k = 0; k < nl; ++k) {
+      MB_CUDA(cudaEventRecord(bufs.done[k], bufs.lane[k]));
+      MB_CUDA(cudaStreamWaitEvent(st, bufs.done[k], 0));
+    }
     MB_CUDA(cudaMemcpyAsync(host, cbuf.p, sizeof(double) * cwords, cudaMemcpyDeviceToHost, st));
     MB_CUDA(cudaStreamSynchronize(st));
   };
   auto nn_off = [](const RefineRun& r) { return 4 * (size_t)r.cap; };
   // q_0 = x / |x|
-  for (auto& r : runs) {
-    MB_CUDA(cudaMemcpyAsync(r.col(0), r.p->x, r.vb, cudaMemcpyDeviceToDevice, st));
-    launch_dot(MB_PREC_F64, r.n, r.col(0), r.col(0), pp, st);
-    launch_reduce(pp, blas_grid(r.n), 3, r.dc + nn_off(r), st);
+  for (size_t i = 0; i < runs.size(); ++i) {
+    RefineRun& r = runs[i];
+    MB_CUDA(cudaMemcpyAsync(r.col(0), r.p->x, r.vb, cudaMemcpyDeviceToDevice, ls(i)));
+    launch_dot(MB_PREC_F64, r.n, r.col(0), r.col(0), pp(i), ls(i));
+    launch_reduce(pp(i), blas_grid(r.n), 3, r.dc + nn_off(r), ls(i));
   }
   sync_all();
-  for (auto& r : runs) {
+  for (size_t i = 0; i < runs.size(); ++i) {
+    RefineRun& r = runs[i];
     const double nx = std::sqrt(r.hc[nn_off(r) + 2]);
     MB_REQUIRE(nx > 0.0, MB_ERR_ZERO_NORM, "refinement start vector has zero norm");
-    launch_axpby(MB_PREC_F64, r.n, 1.0 / nx, 0.0, r.col(0), 0.0, 0.0, r.col(0), nullptr, 0, st);
+    launch_axpby(MB_PREC_F64, r.n, 1.0 / nx, 0.0, r.col(0), 0.0, 0.0, r.col(0), nullptr, 0, ls(i));
   }
   for (int j = 0;; ++j) {
     bool any = false;
-    for (auto& r : runs) {
+    for (size_t i = 0; i < runs.size(); ++i) {
+      RefineRun& r = runs[i];
       if (r.done) continue;
       any = true;
       // w = H q_j in the next basis slot, then w -= Q Q^H w twice against
       // q_0..q_j: the passes' coefficients at dc[0..) and dc[2 cap..), the
       // norm of the rest at dc[4 cap + 1]
       void* w = r.col(j + 1);
-      launch_apply(r.p->v, MB_PREC_F64, r.col(j), w, 1.0, 0.0, 0.0, nullptr, nullptr, 0, st);
+      launch_apply(r.p->v, MB_PREC_F64, r.col(j), w, 1.0, 0.0, 0.0, nullptr, nullptr, 0, ls(i));
       for (int pass = 0; pass < kRefinePasses; ++pass) {
         double* c = r.dc + 2 * (size_t)r.cap * pass;
-        launch_multi_dot(MB_PREC_F64, MB_PREC_F64, r.n, r.q, r.n, j + 1, w, pp, st);
-        launch_reduce(pp, multi_dot_grid(r.n), 2 * (j + 1), c, st);
-        launch_multi_axpy(MB_PREC_F64, MB_PREC_F64, r.n, r.q, r.n, j + 1, c, w, pp, st);
+        launch_multi_dot(MB_PREC_F64, MB_PREC_F64, r.n, r.q, r.n, j + 1, w, pp(i), ls(i));
+        launch_reduce(pp(i), multi_dot_grid(r.n), 2 * (j + 1), c, ls(i));
+        launch_multi_axpy(MB_PREC_F64, MB_PREC_F64, r.n, r.q, r.n, j + 1, c, w, pp(i), ls(i));
       }
-      launch_reduce(pp, blas_grid(r.n), 3, r.dc + nn_off(r), st);
+      launch_reduce(pp(i), blas_grid(r.n), 3, r.dc + nn_off(r), ls(i));
     }
     if (!any) break;
     sync_all();
-    for (auto& r : runs) {
+    for (size_t i = 0; i < runs.size(); ++i) {
+      RefineRun& r = runs[i];
       if (r.done) continue;
       double a = 0.0;
       for (int pass = 0; pass < kRefinePasses; ++pass) a += r.hc[2 * (size_t)r.cap * pass + 2 * j];
@@ -1102,7 +1138,8 @@ static void refine_chunk(std::vector<RefineRun>& runs, RefineBufs& bufs, cudaStr
       std::vector<double> d(r.alpha), e(r.beta);
       MB_REQUIRE(tridiag_eig((int)d.size(), d, e, nullptr), MB_ERR_EIG_FAILED,
                  "Eigenvalue decomposition of T_k failed");
-      const bool settled = j + 1 >= kRefineMinSteps && std::fabs(d[0] - r.theta) <= kRefineSettle * std::fabs(d[0]);
+      const bool settled = j + 1 >= kRefineMinSteps &&
+                           std::fabs(d[0] - r.theta) <= kRefineSettle * std::fabs(d[0]);
       r.theta = d[0];
       if (settled || j + 1 >= r.steps || !(b > kTol)) {
         r.done = true;
@@ -1110,7 +1147,8 @@ static void refine_chunk(std::vector<RefineRun>& runs, RefineBufs& bufs, cudaStr
         continue;
       }
       r.beta.push_back(b);
-      launch_axpby(MB_PREC_F64, r.n, 1.0 / b, 0.0, r.col(j + 1), 0.0, 0.0, r.col(j + 1), nullptr, 0, st);
+      launch_axpby(MB_PREC_F64, r.n, 1.0 / b, 0.0, r.col(j + 1), 0.0, 0.0, r.col(j + 1), nullptr,
+                   0, ls(i));
     }
   }
 }
