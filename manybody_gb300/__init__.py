@@ -1132,9 +1132,12 @@ class Engine:
 
 def batch_ground_states(descs, seeds=None, kmax: int = 150, refine: bool = True,
                         use_graph: bool = True, autotune: bool = True, fused_threshold=None,
-                        persistent: bool = True, engine_out=None, basis_limit=None):
-    """Fixed-length batched Lanczos for many sectors: returns [EngineResult]."""
-    eng = Engine()
+                        persistent: bool = True, engine_out=None, basis_limit=None,
+                        engine=None):
+    """Fixed-length batched Lanczos for many sectors: returns [EngineResult].
+    engine: run on this Engine (its memory pool and sector tables stay warm
+    from earlier batches) instead of a new one."""
+    eng = engine if engine is not None else Engine()
     if engine_out is not None:
         engine_out.append(eng)
     if not persistent:

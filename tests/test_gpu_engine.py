@@ -392,3 +392,14 @@ def test_refinement_far_from_zero_in_engine(mb, cuda):
     mixed = mb.batch_ground_states([far] + descs(mb), seeds=[44] * 9, kmax=150, autotune=False)
     for r, e in zip(mixed, [e_far] + [exact_e0(*x) for x in SECTORS]):
         assert abs(r.e0 - e) <= 1e-8 * abs(e)
+
+
+def test_engine_reused_across_batches(mb, cuda, exact):
+    """A second batch on the same engine (its memory pool and sector tables
+    warm from the first) gives the first batch's bits."""
+    eng = mb.Engine()
+    first = mb.batch_ground_states(descs(mb), seeds=list(range(8)), kmax=80, engine=eng)
+    second = mb.batch_ground_states(descs(mb), seeds=list(range(8)), kmax=80, engine=eng)
+    for a, b, e in zip(first, second, exact):
+        assert a.e0 == b.e0 and a.e0_raw == b.e0_raw and a.steps == b.steps
+        assert abs(a.e0 - e) <= 1e-8 * abs(e)
