@@ -482,8 +482,10 @@ int mb_engine_set_fused_threshold(mb_engine_t engine, int64_t min_states);
  * fastest; *ms = its time per apply.  Persistent step: row_min_cols in
  * {64, 128, 256} x ctas_per_sm in {all that fit, 2} (set_shape takes any
  * ctas_per_sm), timed with apply-only launches (they change no request's
- * progress); grouped kernels: warps per
- * block in {2, 4, 8, 16}.  *chosen = the grouped kernels' warps per block. */
+ * progress); a mix of requests (their sectors' shapes and kinds) that this
+ * engine has tuned for before takes the shape found then, untimed.  Grouped
+ * kernels: warps per block in {2, 4, 8, 16}.  *chosen = the grouped kernels'
+ * warps per block. */
 int mb_engine_autotune(mb_engine_t engine, int* chosen, double* ms);
 /* n_steps steps with no host round trip between them (fixed-length batches).
  * Persistent step (the default): ONE cooperative launch of the fused kernel

@@ -1379,6 +1379,11 @@ struct mb_engine_s {
   bool persistent = true;
   int p_row_min_cols = 256;
   int p_ctas_per_sm = 0;
+  // the persistent shape the autotuner chose for a mix of requests, keyed by
+  // the mix's sorted (Du, Dd, kind) list: the same mix again is not re-timed
+  std::vector<std::tuple<int64_t, int64_t, int>> tuned_mix;
+  int tuned_cols = 256, tuned_ctas = 0;
+  double tuned_ms = 0.0;
   int p_grid = 1;
   int p_bps = 1, p_sms = 1;  // co-resident blocks per SM of the last launch shape, SMs
   size_t p_smem = 0;
@@ -2457,7 +2462,21 @@ int mb_engine_autotune(mb_engine_t eng, int* chosen, double* ms) {
       // the persistent step's shapes, timed on the live requests with
       // apply-only launches (they write only w and the partials, which the
       // next step rewrites): rows below row_min_cols columns warp per row,
-      // ctas_per_sm co-resident blocks (0: all that fit)
+      // ctas_per_sm co-resident blocks (0: all that fit).  A mix of requests
+      // the engine has tuned for before takes that shape without timing.
+      std::vector<std::tuple<int64_t, int64_t, int>> mix;
+      mix.reserve(e->slots.size());
+      for (const auto& sl : e->slots) mix.emplace_back(sl->Du, sl->Dd, sl->kind);
+      std::sort(mix.begin(), mix.end());
+      if (!e->tuned_mix.empty() && mix == e->tuned_mix) {
+        e->p_row_min_cols = e->tuned_cols;
+        e->p_ctas_per_sm = e->tuned_ctas;
+        e->dirty = true;
+        rebuild(e);
+        if (chosen) *chosen = e->warps;
+        if (ms) *ms = e->tuned_ms;
+        return;
+      }
       cudaEvent_t a, b;
       MB_CUDA(cudaEventCreate(&a));
       MB_CUDA(cudaEventCreate(&b));
@@ -2498,6 +2517,10 @@ int mb_engine_autotune(mb_engine_t eng, int* chosen, double* ms) {
       e->p_ctas_per_sm = best_ctas;
       e->dirty = true;
       rebuild(e);
+      e->tuned_mix = std::move(mix);
+      e->tuned_cols = best_cols;
+      e->tuned_ctas = best_ctas;
+      e->tuned_ms = best / 2.0;
       if (chosen) *chosen = e->warps;
       if (ms) *ms = best / 2.0;
       return;
