@@ -1,7 +1,8 @@
 """A seeded sweep over many small sectors: every refined ground-state energy
 (the serving engine's path and the single-operator FP32 path) against an
 independent FP64 eigensolver (ARPACK through scipy on the oracle's matrix, dense
-for the smallest).
+for the smallest), and Krylov time evolution in the three precisions against the
+oracle.
 
 Sectors: 1D L = 4..10 and 2x2, 2x3, 3x3, 2x4 periodic; every filling
 1 <= N_up, N_down <= L-1 (N_up != N_down too); U from -4 to 20, including 0,
@@ -86,3 +87,33 @@ def test_sweep_single_operator_fp32(mb, cuda, cases):
         r = mb.find_min_eigenpair(op, min(400, op.dimension()), s, order=mb.ORDER_TENSOR,
                                   conv_tol=1e-10, want_vector=False, refine=True)
         assert abs(r.value - e) <= 1e-8 * max(abs(e), 1.0), (dims, nu, nd, u, r.value, e)
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-10), (1, 1e-4), (2, 1e-10)])
+@pytest.mark.parametrize("imaginary", [False, True])
+def test_sweep_time_evolution(mb, cuda, prec, tol, imaginary):
+    """Krylov evolution (30 steps, t = 0.1; the result summed from the kept
+    Lanczos vectors) on 16 of the sweep's sectors with at most 5,000 states and
+    |U| <= 10 (|H| t below ~7, where 30 steps converge and the late Lanczos
+    vectors carry no weight), against the oracle's restatement of
+    evolve_state.h on the same start vector: ||dpsi|| <= tol ||psi|| (FP64 and
+    Q64 1e-10, FP32 1e-4)."""
+    n = 0
+    for dims, nu, nd, u, i in sweep_cases():
+        if n == 16:
+            break
+        L = int(np.prod(dims))
+        if abs(u) > 10.0:
+            continue
+        H = oracle.hubbard_csc(list(dims), 1.0, u, nu, nd)
+        if H.dim > 5000:
+            continue
+        n += 1
+        b = mb.FermionBasis.with_fixed_particle_number_and_spin(L, nu + nd, nu - nd)
+        op = mb.GpuHubbardOperator(b, mb._Hubbard(1.0, u, dims), prec)
+        psi = op.seed_vector(i)
+        ph = psi.cpu().numpy().astype(np.complex128)
+        fn = mb.imaginary_time_evolve_state if imaginary else mb.time_evolve_state
+        out = fn(op, psi, 0.1).cpu().numpy().astype(np.complex128)
+        ref = H.time_evolve(ph, 0.1, 30, imaginary)
+        assert np.linalg.norm(out - ref) <= tol * np.linalg.norm(ref), (dims, nu, nd, u)
