@@ -1,8 +1,8 @@
 """A seeded sweep over many small sectors: every refined ground-state energy
 (the serving engine's path and the single-operator FP32 path) against an
 independent FP64 eigensolver (ARPACK through scipy on the oracle's matrix, dense
-for the smallest), and Krylov time evolution in the three precisions against the
-oracle.
+for the smallest); Krylov time evolution and DOS Chebyshev moments in the three
+precisions against the oracle.
 
 Sectors: 1D L = 4..10 and 2x2, 2x3, 3x3, 2x4 periodic; every filling
 1 <= N_up, N_down <= L-1 (N_up != N_down too); U from -4 to 20, including 0,
@@ -117,3 +117,42 @@ def test_sweep_time_evolution(mb, cuda, prec, tol, imaginary):
         out = fn(op, psi, 0.1).cpu().numpy().astype(np.complex128)
         ref = H.time_evolve(ph, 0.1, 30, imaginary)
         assert np.linalg.norm(out - ref) <= tol * np.linalg.norm(ref), (dims, nu, nd, u)
+
+
+# FP32: the Chebyshev recurrence's rounding model, 8 k^2 u32 with k = M/2 + 1
+# steps behind the last moment (each step adds up to ~8 u32, and an error made
+# at step j reaches step k through U_(k-j), norm <= k - j + 1 on [-1, 1])
+@pytest.mark.parametrize("prec,tol", [(0, 1e-10), (1, 8 * 65 ** 2 * 2.0 ** -24), (2, 1e-10)])
+def test_sweep_kpm_moments(mb, cuda, prec, tol):
+    """DOS Chebyshev moments (128 moments, 2 random-phase probes, exact spectral
+    bounds padded by 1 %) on 12 of the sweep's sectors with at most 5,000
+    states, against the oracle's restatement of kpm.h on the same probes:
+    max |dmu_n| <= tol (FP64 and Q64 1e-10, FP32 the rounding model)."""
+    M, R, key = 128, 2, 11
+    n = 0
+    for dims, nu, nd, u, i in sweep_cases():
+        if n == 12:
+            break
+        L = int(np.prod(dims))
+        H = oracle.hubbard_csc(list(dims), 1.0, u, nu, nd)
+        if H.dim > 5000:
+            continue
+        n += 1
+        E = np.linalg.eigvalsh(H.to_dense())
+        emin, emax = float(E[0]), float(E[-1])
+        if emax - emin < 1e-9:
+            continue
+        b = mb.FermionBasis.with_fixed_particle_number_and_spin(L, nu + nd, nu - nd)
+        op = mb.GpuHubbardOperator(b, mb._Hubbard(1.0, u, dims), prec)
+        mu = mb.kpm_dos_moments(op, M, R, key, emin, emax, 0.01)
+        a = (emax - emin) / 2 * 1.01
+        c = (emax + emin) / 2
+        perm = op.basis.permutation()
+        ref = np.zeros(M)
+        for p in range(R):
+            rt = oracle.philox_phase(key, op.dimension(), 1 + p)
+            r = np.empty_like(rt)
+            r[perm] = rt
+            ref += H.kpm_dos_moments(r, M, a, c)
+        ref /= R * op.dimension()
+        assert np.max(np.abs(mu - ref)) <= tol, (dims, nu, nd, u, float(np.max(np.abs(mu - ref))))
