@@ -617,11 +617,12 @@ struct RefineProblem {
 void fp64_refine_many(RefineProblem* probs, int count, cudaStream_t st);
 double fp64_ritz_refine(const OpView& v, const void* x64, cudaStream_t st);
 // the refinement's Krylov steps: at least kRefineMinSteps, then until the
-// lowest Ritz value moves by at most kRefineSettle relative (above the
-// rounding of FP64 dot products over a sector), at most kRefineMaxSteps
+// lowest Ritz value moves by at most kRefineSettle relative (the convergence
+// level of the plain FP64 solver, well above the rounding of FP64 dot products
+// over a sector), at most kRefineMaxSteps
 constexpr int kRefineMinSteps = 3;
 constexpr int kRefineMaxSteps = 8;
-constexpr double kRefineSettle = 1e-13;
+constexpr double kRefineSettle = 1e-12;
 
 // Host tridiagonal eigensolver (implicit QL, mb_tridiag.cpp).
 bool tridiag_eig(int n, std::vector<double>& d, const std::vector<double>& e,
