@@ -32,8 +32,10 @@
 
 #include <complex>
 #include <cstdint>
+#include <memory>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -191,6 +193,10 @@ inline CsrMatrix compute_matrix_elements(const FermionBasis& basis, const Hubbar
 }
 
 // The matrix-free GPU operator, shaped like the reference's LinearOperator.
+// Copies share one device operator (its apply is const and safe from several
+// threads), as the reference's drivers copy the operators they wrap:
+// find_min_eigenpair builds Negated<Op>(op) by value (lanczos.h:283-290,
+// linear_operator.h:93-105).
 template <typename Vector>
 class GpuHubbardOperator {
  public:
@@ -199,38 +205,37 @@ class GpuHubbardOperator {
 
   GpuHubbardOperator(const FermionBasis& basis, const HubbardModelBase& model,
                      int precision = MB_PREC_F64) {
-    check(mb_op_create(basis.handle(), model.handle(), precision, &h_));
-    check(mb_op_dimension(h_, &dim_));
+    mb_op_t h = nullptr;
+    check(mb_op_create(basis.handle(), model.handle(), precision, &h));
+    h_ = std::shared_ptr<std::remove_pointer_t<mb_op_t>>(h, [](mb_op_t p) { mb_op_destroy(p); });
+    check(mb_op_dimension(h, &dim_));
   }
-  GpuHubbardOperator(GpuHubbardOperator&& o) noexcept : h_(std::exchange(o.h_, nullptr)), dim_(o.dim_) {}
-  GpuHubbardOperator(const GpuHubbardOperator&) = delete;
-  ~GpuHubbardOperator() { mb_op_destroy(h_); }
 
   // LinearOperator::apply (linear_operator.h:41): a fresh vector H v.
   VectorType apply(const VectorType& v) const {
     if ((int64_t)v.n_elem != dim_) throw Error(MB_ERR_DIM_MISMATCH, "vector dimension mismatch");
     VectorType out((size_t)dim_);
-    check(mb_op_apply_host(h_, v.memptr(), out.memptr(), MB_ORDER_REFERENCE));
+    check(mb_op_apply_host(h_.get(), v.memptr(), out.memptr(), MB_ORDER_REFERENCE));
     return out;
   }
   size_t dimension() const { return (size_t)dim_; }
-  mb_op_t handle() const { return h_; }
+  mb_op_t handle() const { return h_.get(); }
   // Times the apply's kernel shapes on the GPU and keeps the fastest
   // (mb_op_autotune; cached per sector); returns ms per apply.
   double autotune() {
     mb_apply_shape s{};
     double ms = 0.0;
-    check(mb_op_autotune(h_, nullptr, &s, &ms));
+    check(mb_op_autotune(h_.get(), nullptr, &s, &ms));
     return ms;
   }
   mb_apply_shape apply_shape() const {
     mb_apply_shape s{};
-    check(mb_op_get_apply_shape(h_, &s));
+    check(mb_op_get_apply_shape(h_.get(), &s));
     return s;
   }
 
  private:
-  mb_op_t h_ = nullptr;
+  std::shared_ptr<std::remove_pointer_t<mb_op_t>> h_;
   int64_t dim_ = 0;
 };
 

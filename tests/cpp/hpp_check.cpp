@@ -43,7 +43,7 @@ template <typename Op>
 struct Negated {
   using VectorType = typename Op::VectorType;
   using ScalarType = typename Op::ScalarType;
-  const Op& op;
+  Op op;  // by value, as linear_operator.h:93-105 holds it
   VectorType apply(const VectorType& v) const {
     VectorType w = op.apply(v);
     for (auto& x : w.data) x = -x;
@@ -181,6 +181,14 @@ int main(int argc, char** argv) {
   double d2 = 0;
   for (size_t i = 0; i < H.n; ++i) d2 += std::norm(w2.data[i] - w.data[i]);
   CHECK(std::sqrt(d2 / nrm) < 1e-13);
+  // a copy shares the device operator (the reference's Negated<Op> and
+  // Scaled<Op> hold their operator by value)
+  const mbgpu::GpuHubbardOperator<CxVec> copy = op;
+  CHECK(copy.handle() == op.handle() && copy.dimension() == op.dimension());
+  CxVec w3 = copy.apply(v);
+  bool same = true;
+  for (size_t i = 0; i < H.n; ++i) same = same && w3.data[i] == w2.data[i];
+  CHECK(same);
   void* seed = nullptr;
   mbgpu::check(mb_alloc(&seed, sizeof(std::complex<double>) * 4900));
   mbgpu::check(mb_fill_uniform(op.handle(), 0, 0, seed, MB_ORDER_REFERENCE, nullptr));

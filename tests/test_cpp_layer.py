@@ -44,3 +44,16 @@ def test_sliced_table_order(tmp_path, mb):
                    check=True)
     r = subprocess.run([out], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_reference_drivers_compile_against_the_operator():
+    """The reference's own lanczos.h / evolve_state.h / linear_operator.h,
+    unchanged, instantiate with mbgpu::GpuHubbardOperator<arma::cx_vec>
+    (find_min_eigenpair copies the operator into Negated<Op>), compiled against
+    a minimal Armadillo stand-in; skipped where the reference sources are
+    absent."""
+    script = os.path.join(ROOT, "tests", "cpp", "check_reference_drivers.sh")
+    r = subprocess.run(["sh", script], capture_output=True, text=True)
+    if r.returncode == 77:
+        pytest.skip(r.stdout.strip())
+    assert r.returncode == 0, r.stdout + r.stderr
