@@ -293,11 +293,12 @@ typedef struct {
                            less than conv_tol * |E| between checks (0 = run k steps) */
   int check_every;      /* Ritz check period in steps when conv_tol > 0 (default 10) */
   int refine;           /* MB_PREC_F32 operators: 1 = finish with an FP64 Rayleigh-Ritz
-                           refinement (FP64 Lanczos with full re-orthogonalisation from
-                           the Ritz vector: at least 3 steps, then until the lowest Ritz
-                           value settles to 1e-14, at most 8; a plain
-                           run that used all k steps takes the vector from its first
-                           settled checkpoint, before ghost copies of E0 form) */
+                           refinement (FP64 Lanczos from the Ritz vector, each step
+                           orthogonalised against all earlier ones by two Gram-Schmidt
+                           passes: at least 3 steps, then until the lowest Ritz value
+                           moves by at most 1e-12 relative, at most 8; a plain run that
+                           used all k steps takes the vector from its first settled
+                           checkpoint, before ghost copies of E0 form) */
 } mb_lanczos_opts;
 
 /* lanczos_pass_one (lanczos.h:130-175) on the operator scaled by `scale`
