@@ -9,9 +9,13 @@
  * compared bit-for-bit against outputs of the reference's own code
  * (oracle/build_ref.sh -> oracle/_ref/ref_dump), committed as fixtures under
  * tests/golden/.  The numerics (Lanczos, KPM, Krylov evolution) restate
- * reference headers that need Armadillo, which is absent here; they are
- * pinned against the reference's own test expectations (tests/numerics/)
- * and against numpy dense solves, within stated tolerances.
+ * reference headers that need Armadillo, which is absent here.  Lanczos
+ * (find_min_eigenpair, pass one) and Krylov evolution are pinned against the
+ * reference's own lanczos.h and evolve_state.h, run unchanged on the CPU with
+ * a minimal Armadillo stand-in (tests/cpp/reference_numerics_pin.cpp); KPM,
+ * whose reference projectors take a dense or sparse matrix, against the
+ * reference's own test expectations (tests/numerics/); all of them against
+ * numpy dense solves, within stated tolerances.
  *
  * Every function cites the reference file:line it follows.  Operator packing
  * follows src/algebra/operator.h:15-110: bit 15 = type (0 creation,
