@@ -12,7 +12,7 @@
  * reference headers that need Armadillo, which is absent here.  Lanczos
  * (find_min_eigenpair, pass one) and Krylov evolution are pinned against the
  * reference's own lanczos.h and evolve_state.h, run unchanged on the CPU with
- * a minimal Armadillo stand-in (tests/cpp/reference_numerics_pin.cpp); KPM,
+ * a minimal Armadillo stand-in (oracle/ref_numerics_pin.cpp); KPM,
  * whose reference projectors take a dense or sparse matrix, against the
  * reference's own test expectations (tests/numerics/); all of them against
  * numpy dense solves, within stated tolerances.

@@ -1,8 +1,9 @@
 // Runs the reference's own numerics drivers (numerics/lanczos.h and
 // numerics/evolve_state.h, unchanged, from the reference's source tree) on the
 // CPU, on the reference's own SparseComplexMatrixOperator, with the minimal
-// Armadillo stand-in of tests/cpp/arma_shim; the oracle's restatements are
-// compared with its outputs (tests/test_oracle_numerics_pin.py).
+// Armadillo stand-in of oracle/arma_shim; the oracle's restatements are
+// compared with its outputs (tests/test_oracle_numerics_pin.py).  Test
+// infrastructure, built by oracle/build_ref.sh into oracle/_ref/.
 //
 // Input (binary, native endianness): int64 dim, int64 nnz, int64 k,
 // double t, int64 col_ptr[dim + 1], int64 row_idx[nnz], complex128

@@ -2,8 +2,8 @@
 // numerics/evolve_state.h and numerics/linear_operator.h, unchanged, from the
 // reference's source tree) instantiated with this library's
 // mbgpu::GpuHubbardOperator<arma::cx_vec>.  Built with -fsyntax-only against
-// a minimal Armadillo stand-in (tests/cpp/arma_shim) by
-// tests/cpp/check_reference_drivers.sh; it is not linked or run.
+// a minimal Armadillo stand-in (oracle/arma_shim) by
+// oracle/check_ref_drivers.sh; it is not linked or run.
 #include "manybody_gb300.hpp"
 
 #include "numerics/evolve_state.h"

@@ -52,7 +52,7 @@ def test_reference_drivers_compile_against_the_operator():
     (find_min_eigenpair copies the operator into Negated<Op>), compiled against
     a minimal Armadillo stand-in; skipped where the reference sources are
     absent."""
-    script = os.path.join(ROOT, "tests", "cpp", "check_reference_drivers.sh")
+    script = os.path.join(ROOT, "oracle", "check_ref_drivers.sh")
     r = subprocess.run(["sh", script], capture_output=True, text=True)
     if r.returncode == 77:
         pytest.skip(r.stdout.strip())

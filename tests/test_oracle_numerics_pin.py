@@ -2,8 +2,8 @@
 drivers, pinned against the reference's own code: numerics/lanczos.h and
 numerics/evolve_state.h, unchanged, run on the CPU on the reference's
 SparseComplexMatrixOperator, with a minimal Armadillo stand-in for the library
-the reference links (tests/cpp/reference_numerics_pin.cpp, built by
-tests/cpp/build_reference_numerics_pin.sh).  Same matrix, same start vectors:
+the reference links (oracle/ref_numerics_pin.cpp, built into oracle/_ref/ by
+oracle/build_ref.sh where the reference sources are present).  Same matrix, same start vectors:
 find_min_eigenpair (its seed handed to make_seed_vector), pass one's alpha and
 beta, and exp(-i t H) psi, exp(-t H) psi.  Skipped where the reference sources
 are absent.
@@ -26,7 +26,7 @@ import pytest
 import oracle
 from conftest import ROOT
 
-SCRIPT = os.path.join(ROOT, "tests", "cpp", "build_reference_numerics_pin.sh")
+PIN = os.path.join(ROOT, "oracle", "_ref", "ref_numerics_pin")
 
 # (dims, t, U, N_up, N_down, Lanczos steps, evolution time)
 CASES = [
@@ -39,13 +39,10 @@ CASES = [
 
 
 @pytest.fixture(scope="module")
-def pin_binary(tmp_path_factory):
-    out = str(tmp_path_factory.mktemp("pin") / "reference_numerics_pin")
-    r = subprocess.run(["sh", SCRIPT, out], capture_output=True, text=True)
-    if r.returncode == 77:
-        pytest.skip(r.stdout.strip())
-    assert r.returncode == 0, r.stdout + r.stderr
-    return out
+def pin_binary():
+    if not os.path.exists(PIN):
+        pytest.skip("oracle/_ref/ref_numerics_pin is built only where the reference sources are")
+    return PIN
 
 
 def run_reference(binary, tmp_path, H, k, t, seed, psi):
