@@ -8,9 +8,9 @@
 # (src/algebra/expression_base.h:182-186); 128 gives a 55-operator cap.
 # Also builds oracle/_ref/cereal_pin (oracle/cereal_pin.cpp against the
 # reference's vendored cereal headers) and oracle/_ref/ref_numerics_pin
-# (oracle/ref_numerics_pin.cpp: the reference's numerics/lanczos.h and
-# numerics/evolve_state.h, unchanged and in place, with the Armadillo
-# stand-in oracle/arma_shim).
+# (oracle/ref_numerics_pin.cpp: the reference's numerics/lanczos.h,
+# numerics/evolve_state.h and numerics/kpm.h, unchanged and in place, with the
+# Armadillo stand-in oracle/arma_shim).
 # The copy and the binaries live only under oracle/_ref/ (git-ignored).
 # Test infrastructure: the product never calls anything built here.
 set -e
@@ -43,7 +43,7 @@ echo "built $OUT/ref_dump"
 # The cache-format pin: the vendored cereal library only (no reference code).
 ${CXX:-g++} -std=c++17 -O2 -I"$REF/third-party" "$HERE/cereal_pin.cpp" -o "$OUT/cereal_pin"
 echo "built $OUT/cereal_pin"
-# The numerics pin: the reference's own Lanczos and evolution drivers on the
+# The numerics pin: the reference's own Lanczos, evolution and KPM code on the
 # CPU, with the Armadillo stand-in (the headers are used in place, unpatched).
 ${CXX:-g++} -std=c++20 -O2 -I"$HERE/arma_shim" -I"$REF/src" \
   "$HERE/ref_numerics_pin.cpp" -o "$OUT/ref_numerics_pin"

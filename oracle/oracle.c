@@ -10,10 +10,11 @@
  * (oracle/build_ref.sh -> oracle/_ref/ref_dump), committed as fixtures under
  * tests/golden/.  The numerics (Lanczos, KPM, Krylov evolution) restate
  * reference headers that need Armadillo, which is absent here.  Lanczos
- * (find_min_eigenpair, pass one) and Krylov evolution are pinned against the
- * reference's own lanczos.h and evolve_state.h, run unchanged on the CPU with
- * a minimal Armadillo stand-in (oracle/ref_numerics_pin.cpp); KPM,
- * whose reference projectors take a dense or sparse matrix, against the
+ * (find_min_eigenpair, pass one), Krylov evolution, the KPM kernels, the
+ * projector moments and the sparse KPM projector are pinned against the
+ * reference's own lanczos.h, evolve_state.h and kpm.h, run unchanged on the
+ * CPU with a minimal Armadillo stand-in (oracle/ref_numerics_pin.cpp); the
+ * DOS moments, which the reference does not implement, against the
  * reference's own test expectations (tests/numerics/); all of them against
  * numpy dense solves, within stated tolerances.
  *

@@ -1,12 +1,13 @@
-"""The oracle's restatements of the reference's Lanczos and Krylov-evolution
-drivers, pinned against the reference's own code: numerics/lanczos.h and
-numerics/evolve_state.h, unchanged, run on the CPU on the reference's
-SparseComplexMatrixOperator, with a minimal Armadillo stand-in for the library
+"""The oracle's restatements of the reference's Lanczos, Krylov-evolution and
+KPM code, pinned against the reference's own code: numerics/lanczos.h,
+numerics/evolve_state.h and numerics/kpm.h, unchanged, run on the CPU on the
+reference's SparseComplexMatrixOperator (and SparseKPMProjector), with a minimal Armadillo stand-in for the library
 the reference links (oracle/ref_numerics_pin.cpp, built into oracle/_ref/ by
 oracle/build_ref.sh where the reference sources are present).  Same matrix, same start vectors:
 find_min_eigenpair (its seed handed to make_seed_vector), pass one's alpha and
-beta, and exp(-i t H) psi, exp(-t H) psi.  Skipped where the reference sources
-are absent.
+beta, exp(-i t H) psi, exp(-t H) psi, the Jackson and Lorentz kernels, the
+projector moments and the sparse KPM projector applied to psi.  Skipped where
+the reference sources are absent.
 
 Tolerances: E0 1e-10 relative; the first 20 alpha, beta 1e-12 absolute, up to
 an invariant subspace's end (beta below 1e-8: the rest is rounding noise), since
@@ -14,7 +15,8 @@ later steps amplify rounding differences once Ritz values converge (measured:
 alpha agrees to 1e-12 for the first 33 to 70 steps); the Ritz vectors' overlap
 >= 1 - 1e-3 (after convergence the two recurrences part at the rounding level,
 and a degenerate ground state's vector follows them); the evolved states 1e-10
-relative (measured: 1e-14).
+relative (measured: 1e-14); the kernels and moments 1e-14; the projector
+1e-12 relative.
 """
 import os
 import struct
@@ -45,10 +47,10 @@ def pin_binary():
     return PIN
 
 
-def run_reference(binary, tmp_path, H, k, t, seed, psi):
+def run_reference(binary, tmp_path, H, k, t, seed, psi, M, kb):
     n = H.dim
     vals = (H.re + 1j * H.im).astype(np.complex128)
-    blob = struct.pack("<qqqd", n, H.nnz, k, t)
+    blob = struct.pack("<qqqdq4d", n, H.nnz, k, t, M, *kb)
     blob += np.asarray(H.col_ptr, np.int64).tobytes() + np.asarray(H.row_idx, np.int64).tobytes()
     blob += vals.tobytes() + seed.astype(np.complex128).tobytes() + psi.astype(np.complex128).tobytes()
     fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
@@ -65,7 +67,11 @@ def run_reference(binary, tmp_path, H, k, t, seed, psi):
     be = np.frombuffer(raw, np.float64, max(m - 1, 0), off)
     off += 8 * max(m - 1, 0)
     vec, real_t, imag_t = (np.frombuffer(raw, np.complex128, n, off + 16 * n * i) for i in range(3))
-    return m, e0, al, be, vec, real_t, imag_t
+    off += 48 * n
+    jk, lk, pm = (np.frombuffer(raw, np.float64, M + 1, off + 8 * (M + 1) * i) for i in range(3))
+    off += 24 * (M + 1)
+    proj = np.frombuffer(raw, np.complex128, n, off)
+    return m, e0, al, be, vec, real_t, imag_t, (jk, lk, pm, proj)
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -78,7 +84,12 @@ def test_oracle_matches_reference_drivers(pin_binary, tmp_path, case):
     seed = rng.uniform(0, 1, n) + 1j * rng.uniform(0, 1, n)  # randu, as make_seed_vector draws
     psi = rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)
     psi /= np.linalg.norm(psi)
-    m, e0, al, be, vec, real_t, imag_t = run_reference(pin_binary, tmp_path, H, k, tev, seed, psi)
+    E = np.linalg.eigvalsh(H.to_dense())
+    assert not np.any(H.im)  # the Hubbard H is real: the sparse projector's vectors are real
+    M = 48
+    kb = (float(E[0]), float(E[-1]), float((E[0] + E[-1]) / 2 - 0.1 * (E[-1] - E[0])), 0.01)
+    m, e0, al, be, vec, real_t, imag_t, kpm_out = run_reference(pin_binary, tmp_path, H, k, tev,
+                                                                seed, psi, M, kb)
 
     e_or, vec_or, m_or, al_or, be_or = H.find_min_eigenpair(seed, k)
     assert m == m_or
@@ -94,5 +105,13 @@ def test_oracle_matches_reference_drivers(pin_binary, tmp_path, case):
         ref = H.time_evolve(psi, tev, 30, imaginary)
         assert np.linalg.norm(got - ref) <= 1e-10 * np.linalg.norm(ref), imaginary
     # and both are right: E0 against a dense solve
-    E = np.linalg.eigvalsh(H.to_dense())
     assert abs(e0 - E[0]) <= 1e-8 * max(abs(E[0]), 1.0)
+    # KPM (kpm.h:19-61, 184-229)
+    jk, lk, pm, proj = kpm_out
+    a = (kb[1] - kb[0]) / 2 * (1 + kb[3])
+    eps = (kb[2] - (kb[1] + kb[0]) / 2) / a
+    assert np.allclose(jk, oracle.jackson_kernel(M), rtol=0, atol=1e-14)
+    assert np.allclose(lk, oracle.lorentz_kernel(M, 4.0), rtol=0, atol=1e-14)
+    assert np.allclose(pm, oracle.projector_moments(M, eps), rtol=0, atol=1e-14)
+    ref_p = H.kpm_projector_apply(psi, M, kb[0], kb[1], kb[2], kb[3])
+    assert np.linalg.norm(proj - ref_p) <= 1e-12 * np.linalg.norm(ref_p)
